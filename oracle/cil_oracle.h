@@ -1,0 +1,101 @@
+/* ORACLE — test infrastructure only.
+ *
+ * CPU restatement of the reference's overdamped cell-colony timestep (KokoroSinx/cil_cuda,
+ * Euler integrator: CIL.cu:1013-1020 with calculForcesPressure CIL.cu:999-1007), used as
+ * the checker for the CUDA library and as the timed CPU baseline. Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU legs load it; the product never does.
+ *
+ * Pinning: the random-number layer (dSFMT-19937, Leva normals, onDSphere, uniform
+ * variants) is pinned bit-for-bit against the reference's own mt/dSFMT.c + Random.hpp
+ * (golden vectors in tests/golden/). The reference ships no tests, fixtures or outputs of
+ * this physics, and its step does not compile, so the force laws, binning, division and
+ * apoptosis are "parity unpinned": they are restated from the reference source (cited per
+ * function in cil_oracle.cpp) with the BASELINE force laws slotted into the reference's
+ * PairForceParams / intraCellForce extension points.
+ */
+#ifndef CIL_ORACLE_H
+#define CIL_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORA_FORCE_LJ_WCA = 0, ORA_FORCE_SOFTCORE = 1, ORA_FORCE_HERTZ = 2 };
+
+typedef struct ora_params {
+  int32_t dim;            /* 2 or 3 */
+  int32_t force_law;      /* ORA_FORCE_* */
+  int32_t noise_per_cell; /* 0: one normal per element component, 1: per cell (reference) */
+  int32_t divide;         /* linear growth + division on */
+  double box[3];
+  int32_t periodic[3];
+  int32_t nwalls; /* 0..2 flat one-sided Hertz walls normal to the last axis */
+  int32_t wall_dir[2];
+  double wall_pos[2];
+  double wall_E;
+  double epsilon;    /* LJ epsilon / soft-core epsilon / Hertz modulus E */
+  double rcut_scale; /* cutoff in units of sigma_ij = (sigma_i + sigma_j)/2 */
+  double zeta[2];    /* friction of back/front element; mobility = 1/zeta */
+  double motility[2];/* back element gets -m0*n, front +m1*n (n = back->front unit axis) */
+  double kappa;      /* linear intra-cell spring */
+  double rest0;      /* rest length at birth */
+  double rest1;      /* rest length at division */
+  double noise_D;    /* passive diffusion constant */
+  double dt;
+  double div_tau_mu, div_tau_sigma; /* division time ~ N(mu, sigma), time units */
+  double apop_rate;                 /* per unit time */
+} ora_params;
+
+typedef struct ora_event {
+  int32_t ts;
+  int32_t kind; /* 0 = division (a = mother, b = daughter), 1 = apoptosis (a = slot, b = moved-from) */
+  int32_t a, b;
+} ora_event;
+
+typedef struct ora_obs {
+  int32_t ncells;
+  int32_t pad;
+  double mean_area;
+  double msd;
+  double vacf;
+  int64_t ndiv_total;
+  int64_t napo_total;
+} ora_obs;
+
+void *ora_create(const ora_params *p, int32_t cap_cells, uint32_t seed);
+void ora_destroy(void *h);
+/* 0 = single thread, reference half-stencil order; >0 = OpenMP race-free full stencil */
+void ora_set_threads(void *h, int32_t nthreads);
+int32_t ora_set_state(void *h, int32_t ncells, const double *pos, const double *sigma,
+                      const int32_t *t0, const int32_t *tswitch, int32_t ts);
+int32_t ora_num_cells(const void *h);
+int32_t ora_timestep(const void *h);
+void ora_get_state(const void *h, double *pos, double *sigma, double *vel, double *frc,
+                   int32_t *t0, int32_t *tswitch);
+/* forces at the current state (draws the noise like calculForcesPressure) into frc */
+void ora_compute_forces(void *h);
+/* nsteps full Euler steps; returns 0 or a negative error */
+int32_t ora_step(void *h, int32_t nsteps);
+/* element link list of the current positions (Container.cpp:58-79, Utils.hpp:872-1001);
+ * returns the number of bins, fills ns[3], head[nbins], list[2*ncells] */
+int32_t ora_bin_elements(const void *h, double width, int32_t *ns, int32_t *head, int32_t *list,
+                         int32_t max_bins);
+int32_t ora_num_events(const void *h);
+void ora_get_events(const void *h, ora_event *out);
+void ora_clear_events(void *h);
+void ora_obs_reset(void *h);
+void ora_observables(void *h, ora_obs *out);
+
+/* RNG access for golden-vector checks */
+void ora_rng_seed(void *h, uint32_t seed);
+double ora_rng_close_open(void *h);
+double ora_rng_open_open(void *h);
+double ora_rng_uniform(void *h);
+double ora_rng_normal(void *h);
+void ora_rng_on_dsphere(void *h, int32_t dim, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,242 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper around oracle/_build/liboracle.so, the CPU restatement of the reference's
+cell-colony step (see oracle/cil_oracle.h for what is pinned against the reference and
+what is "parity unpinned"). Only tests/, __graft_entry__.smoke() and bench.py's CPU legs
+import this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ = 0, 1, 2
+
+
+class OraParams(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("force_law", C.c_int32),
+        ("noise_per_cell", C.c_int32),
+        ("divide", C.c_int32),
+        ("box", C.c_double * 3),
+        ("periodic", C.c_int32 * 3),
+        ("nwalls", C.c_int32),
+        ("wall_dir", C.c_int32 * 2),
+        ("wall_pos", C.c_double * 2),
+        ("wall_E", C.c_double),
+        ("epsilon", C.c_double),
+        ("rcut_scale", C.c_double),
+        ("zeta", C.c_double * 2),
+        ("motility", C.c_double * 2),
+        ("kappa", C.c_double),
+        ("rest0", C.c_double),
+        ("rest1", C.c_double),
+        ("noise_D", C.c_double),
+        ("dt", C.c_double),
+        ("div_tau_mu", C.c_double),
+        ("div_tau_sigma", C.c_double),
+        ("apop_rate", C.c_double),
+    ]
+
+
+class OraEvent(C.Structure):
+    _fields_ = [("ts", C.c_int32), ("kind", C.c_int32), ("a", C.c_int32), ("b", C.c_int32)]
+
+
+class OraObs(C.Structure):
+    _fields_ = [
+        ("ncells", C.c_int32),
+        ("pad", C.c_int32),
+        ("mean_area", C.c_double),
+        ("msd", C.c_double),
+        ("vacf", C.c_double),
+        ("ndiv_total", C.c_int64),
+        ("napo_total", C.c_int64),
+    ]
+
+
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["bash", os.path.join(HERE, "build.sh")], check=True, capture_output=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        vp, i32, u32, dp, ip = C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        L.ora_create.restype = vp
+        L.ora_create.argtypes = [C.POINTER(OraParams), i32, u32]
+        L.ora_destroy.argtypes = [vp]
+        L.ora_set_threads.argtypes = [vp, i32]
+        L.ora_set_state.restype = i32
+        L.ora_set_state.argtypes = [vp, i32, dp, dp, ip, ip, i32]
+        L.ora_num_cells.restype = i32
+        L.ora_num_cells.argtypes = [vp]
+        L.ora_timestep.restype = i32
+        L.ora_timestep.argtypes = [vp]
+        L.ora_get_state.argtypes = [vp, dp, dp, dp, dp, ip, ip]
+        L.ora_compute_forces.argtypes = [vp]
+        L.ora_step.restype = i32
+        L.ora_step.argtypes = [vp, i32]
+        L.ora_bin_elements.restype = i32
+        L.ora_bin_elements.argtypes = [vp, C.c_double, ip, ip, ip, i32]
+        L.ora_num_events.restype = i32
+        L.ora_num_events.argtypes = [vp]
+        L.ora_get_events.argtypes = [vp, C.POINTER(OraEvent)]
+        L.ora_clear_events.argtypes = [vp]
+        L.ora_obs_reset.argtypes = [vp]
+        L.ora_observables.argtypes = [vp, C.POINTER(OraObs)]
+        L.ora_rng_seed.argtypes = [vp, u32]
+        for name in ("ora_rng_close_open", "ora_rng_open_open", "ora_rng_uniform", "ora_rng_normal"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [vp]
+        L.ora_rng_on_dsphere.argtypes = [vp, i32, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def make_params(**kw) -> OraParams:
+    p = OraParams()
+    for k, v in kw.items():
+        f = getattr(p, k)
+        if isinstance(f, C.Array):
+            for i, x in enumerate(v):
+                f[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class Oracle:
+    """One colony on the CPU, reference layout pos[cell][elem][dim]."""
+
+    def __init__(self, params: dict, cap_cells: int, seed: int, threads: int = 0):
+        self.L = lib()
+        self.params = make_params(**params)
+        self.dim = params["dim"]
+        self.h = self.L.ora_create(C.byref(self.params), cap_cells, seed)
+        if not self.h:
+            raise ValueError("ora_create failed")
+        self.L.ora_set_threads(self.h, threads)
+
+    def close(self):
+        if self.h:
+            self.L.ora_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, pos, sigma, t0, tswitch, ts=0):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+        t0 = np.ascontiguousarray(t0, dtype=np.int32)
+        tswitch = np.ascontiguousarray(tswitch, dtype=np.int32)
+        n = sigma.shape[0]
+        rc = self.L.ora_set_state(self.h, n, _dp(pos), _dp(sigma), _ip(t0), _ip(tswitch), ts)
+        if rc != 0:
+            raise ValueError(f"ora_set_state rc={rc}")
+
+    @property
+    def ncells(self) -> int:
+        return self.L.ora_num_cells(self.h)
+
+    @property
+    def ts(self) -> int:
+        return self.L.ora_timestep(self.h)
+
+    def state(self) -> dict:
+        n, D = self.ncells, self.dim
+        pos = np.zeros((n, 2, D))
+        vel = np.zeros((n, 2, D))
+        frc = np.zeros((n, 2, D))
+        sig = np.zeros((n, 2))
+        t0 = np.zeros(n, np.int32)
+        tsw = np.zeros(n, np.int32)
+        self.L.ora_get_state(self.h, _dp(pos), _dp(sig), _dp(vel), _dp(frc), _ip(t0), _ip(tsw))
+        return dict(pos=pos, sigma=sig, vel=vel, frc=frc, t0=t0, tswitch=tsw)
+
+    def compute_forces(self) -> np.ndarray:
+        self.L.ora_compute_forces(self.h)
+        return self.state()["frc"]
+
+    def step(self, nsteps: int = 1) -> int:
+        return self.L.ora_step(self.h, nsteps)
+
+    def bin_elements(self, width: float, max_bins: int = 1 << 22):
+        ns = np.zeros(3, np.int32)
+        head = np.zeros(max_bins, np.int32)
+        lst = np.zeros(2 * max(self.ncells, 1), np.int32)
+        nb = self.L.ora_bin_elements(self.h, width, _ip(ns), _ip(head), _ip(lst), max_bins)
+        if nb < 0:
+            raise ValueError(f"too many bins: {-nb}")
+        return ns, head[:nb].copy(), lst
+
+    def events(self) -> np.ndarray:
+        m = self.L.ora_num_events(self.h)
+        out = (OraEvent * max(m, 1))()
+        self.L.ora_get_events(self.h, out)
+        return np.array([(e.ts, e.kind, e.a, e.b) for e in out[:m]], dtype=np.int64).reshape(-1, 4)
+
+    def obs_reset(self):
+        self.L.ora_obs_reset(self.h)
+
+    def observables(self) -> dict:
+        o = OraObs()
+        self.L.ora_observables(self.h, C.byref(o))
+        return dict(ncells=o.ncells, mean_area=o.mean_area, msd=o.msd, vacf=o.vacf,
+                    ndiv_total=o.ndiv_total, napo_total=o.napo_total)
+
+    # RNG passthrough for golden-vector checks
+    def rng_seed(self, s):
+        self.L.ora_rng_seed(self.h, s)
+
+    def rng(self, kind: str, n: int) -> np.ndarray:
+        f = {"close_open": self.L.ora_rng_close_open, "open_open": self.L.ora_rng_open_open,
+             "uniform": self.L.ora_rng_uniform, "normal": self.L.ora_rng_normal}[kind]
+        return np.array([f(self.h) for _ in range(n)])
+
+    def on_dsphere(self, dim: int, n: int) -> np.ndarray:
+        out = np.zeros((n, dim))
+        buf = np.zeros(dim)
+        for i in range(n):
+            self.L.ora_rng_on_dsphere(self.h, dim, _dp(buf))
+            out[i] = buf
+        return out
+
+
+def bins_as_sets(head: np.ndarray, lst: np.ndarray) -> list:
+    """Per-bin sets of element ids from a LIFO head/list pair."""
+    out = []
+    for h in head:
+        s = set()
+        i = int(h)
+        while i >= 0:
+            s.add(i)
+            i = int(lst[i])
+        out.append(s)
+    return out
