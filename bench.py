@@ -1,0 +1,333 @@
+"""Benchmark: particle-steps/s of the 2D colony-growth step at 2M particles on one GB300.
+
+Workload (the reference's headline configuration): 2D soft-core colony growth
+(eps = 5, cutoff at contact, linear growth, division ~ N(1, 0.1), apoptosis 0.01/tau_d,
+D = 0.01, dt = 1e-4, periodic 2048 x 2048 box) at the checkpoint of 1M cells
+(2M particles), division and apoptosis on. The checkpoint is a seeded synthetic grown
+colony (cells uniform in a central disk at packing fraction 0.8, cycle ages uniform).
+
+Arms:
+  default            the library: plain FP64 form and mixed FP32-force/FP64-position form
+                     (value = mixed), device-timed with CUDA events, plus an end-to-end
+                     run through the C ABI with host buffers, plus the CPU baseline (the
+                     oracle on the host cores, bounded sample)
+  --impl reference   the reference's CPU path (the oracle restatement, all host threads,
+                     the reference itself does not build) on the same workload
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Multi-GPU (torchrun): one independent replica per rank (the path does not shard a single
+colony); value = all ranks' particle-steps / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @2M particles 2D: mixed+batched+skin-MLP vs plain FP64, 1 GB300"
+UNIT = "particle-steps/s"
+NCELLS = 1_000_000
+BOX = 2048.0
+CAP = 1_200_000
+GTS = 100  # steps per output frame in the end-to-end arm
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.device)], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(seed: int):
+    from cil_cuda_gb300 import synthetic as S
+    p = S.growth_params(box=BOX)
+    st = S.disk_colony(NCELLS, p, seed=seed)
+    return p, st
+
+
+def dist_init(n_gpus: int):
+    if n_gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch.distributed as dist
+    dist.init_process_group("gloo", init_method="env://")
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def allreduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_form(G, p, st, precision, steps, warmup, device, seed, dist):
+    """Device-timed run of one form; returns particle-steps/s and the timing details."""
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device)
+    eng.upload(0, **st)
+    if warmup:
+        eng.step(warmup)
+    n0 = eng.observables(0)["ncells"]
+    barrier(dist)
+    t0 = time.perf_counter()
+    eng.step(steps)  # synchronises the handle's stream before returning
+    wall = time.perf_counter() - t0
+    tm = eng.timings()
+    n1 = eng.observables(0)["ncells"]
+    eng.close()
+    dev_s = tm["total_ms"] * 1e-3
+    psteps = (n0 + n1) * steps  # 2 elements per cell, trapezoid over the (slow) growth
+    return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm)
+
+
+def run_e2e(G, p, st, precision, steps, device, seed):
+    """The same metric through the reference-facing calls with host buffers: upload the
+    colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
+    call, each returning its status through a device->host read of the counters), and a
+    frame download every GTS steps (outputFrame's input)."""
+    import cil_cuda_gb300 as GG
+    n = len(st["sigma"])
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device)
+    h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
+    d2h = 0
+    t0 = time.perf_counter()
+    eng.upload(0, **st)
+    for k in range(steps):
+        eng.step(1)
+        d2h += 56  # the per-call status read of the colony counters
+        if (k + 1) % GTS == 0 or k == steps - 1:
+            fr = eng.download(0)
+            d2h += fr["pos"].nbytes + fr["sigma"].nbytes + fr["vel"].nbytes + fr["t0"].nbytes + fr["tswitch"].nbytes
+    wall = time.perf_counter() - t0
+    n1 = fr["ncells"]
+    eng.close()
+    del GG
+    return dict(value=(n + n1) * steps / wall, wall_s=wall, h2d=h2d / steps, d2h=d2h / steps)
+
+
+def cpu_baseline(p, st, threads: int, budget_s: float = 20.0):
+    """The oracle (race-free OpenMP variant of the reference's step) on the host cores on
+    the same 2M-particle state, as many whole steps as fit the budget (at least 1)."""
+    from oracle import oracle as O
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    o = O.Oracle(p, CAP, 1, threads=threads)
+    o.set_state(**st)
+    t0 = time.perf_counter()
+    o.step(1)
+    first = time.perf_counter() - t0
+    n = max(0, int(budget_s / max(first, 1e-3)) - 1)
+    n = min(n, 20)
+    if n:
+        o.step(n)
+    wall = time.perf_counter() - t0
+    steps = n + 1
+    value = 2 * (len(st["sigma"]) + o.ncells) / 2 * steps / wall
+    o.close()
+    return dict(value=value, unit=UNIT, cores=threads, kind="port",
+                sample=f"{steps} Euler steps of the 2M-particle checkpoint (full step: forces, "
+                       f"integration, division, apoptosis), {wall:.1f} s")
+
+
+def reference_arm(args):
+    rank, world, dist = dist_init(args.gpus)
+    if rank != 0:
+        return 0
+    p, st = workload(seed=1)
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    o = O.Oracle(p, CAP, 1, threads=threads)
+    o.set_state(**st)
+    # bounded sample: each bench step is one full Euler step of the 2M-particle colony;
+    # the number of timed steps is capped so that the run ends within a few minutes
+    t0 = time.perf_counter()
+    o.step(1)
+    per = time.perf_counter() - t0
+    warm = min(args.warmup, 3)
+    if warm > 1:
+        o.step(warm - 1)
+    k = max(1, min(args.steps, int(90.0 / max(per, 1e-3))))
+    n0 = o.ncells
+    t0 = time.perf_counter()
+    o.step(k)
+    wall = time.perf_counter() - t0
+    n1 = o.ncells
+    value = (n0 + n1) * k / wall
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": k, "warmup": warm, "ms_per_step": wall / k * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
+                               "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
+                   "particles": 2 * n0, "cells": n0, "steps_requested": args.steps},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{k} full Euler steps of the 2M-particle state on {threads} host threads "
+                                   f"(oracle restatement; the reference's step does not compile)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    rank, world, dist = dist_init(args.gpus)
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    import cil_cuda_gb300 as G
+    if not os.path.exists(G.LIB_PATH):
+        from cil_cuda_gb300 import build
+        build.build()
+    p, st = workload(seed=1 + rank)
+    hbm, peak_kind = peaks()
+
+    plain = run_form(G, p, st, G.PREC_FP64, max(1, args.steps // 10), args.warmup, device, 7 + rank, dist)
+    with Clocks(device) as clk:
+        mixed = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist)
+    clocks = clk.summary()
+
+    t_max = allreduce_max(dist, mixed["dev_s"])
+    ps_all = allreduce_sum(dist, mixed["psteps"])
+    value = ps_all / t_max
+    t_plain = allreduce_max(dist, plain["dev_s"])
+    plain_value = allreduce_sum(dist, plain["psteps"]) / t_plain
+
+    # roofline of the dominant kernel (the fused pair-force + integrate kernel)
+    tm = mixed["timings"]
+    force_s = tm["force_ms"] * 1e-3 / args.steps
+    nelem = mixed["n0"] + mixed["n1"]  # mean elements per step (2 * mean cells)
+    bytes_per_elem = 40  # pos in 16 + sigma 4 + id 4 + pos out 16 (2D, FP32-force form)
+    achieved = bytes_per_elem * nelem / force_s / 1e9
+    tp = plain["timings"]
+    plain_force_s = tp["force_ms"] * 1e-3 / max(1, args.steps // 10)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-force/f64-position", "data": "synthetic",
+        "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
+                               "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
+                   "particles": mixed["n0"] * 2, "cells": mixed["n0"], "cells_end": mixed["n1"],
+                   "form": "mixed precision, Philox noise, rebuild every step",
+                   "l2": "working set ~230 MB per step > 126 MB L2, no flush",
+                   "parallelism": f"replicas x{world}"},
+        "forms": {"mixed": value, "plain_fp64": plain_value, "speedup_vs_plain_fp64": value / plain_value},
+        "phases_ms_per_step": {k: tm[k] / args.steps for k in ("rebuild_ms", "force_ms", "events_ms")},
+        "plain_fp64_phases_ms_per_step": {k: tp[k] / max(1, args.steps // 10) for k in ("rebuild_ms", "force_ms", "events_ms")},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_force<2, softcore, mixed>", "algorithmic_bytes_per_element": bytes_per_elem,
+                     "plain_fp64_kernel_GBps": 44 * nelem / plain_force_s / 1e9},
+        "gpu_launches": tm["launches"],
+        "clocks": clocks,
+    }
+    if not args.no_e2e:
+        e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank)
+        line["e2e"] = {"value": allreduce_sum(dist, e2e["value"]), "unit": UNIT,
+                       "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(p, st, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

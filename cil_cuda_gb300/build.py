@@ -1,0 +1,69 @@
+"""Builds libcilgpu.so in-tree for sm_103a (GB300).
+
+Each translation unit under csrc/ is compiled in parallel with
+`nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`, then linked into
+cil_cuda_gb300/_build/libcilgpu.so. No CMake, no torch extension machinery.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libcilgpu.so")
+SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def flags(extra=()):
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                   "-I", os.path.join(ROOT, "include"), "-I", CSRC, *extra]
+
+
+def build(verbose: bool = False, ptxas_info: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    extra = ["-Xptxas", "-v"] if ptxas_info else []
+    procs = []
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        objs.append(obj)
+        src_path = os.path.join(CSRC, src)
+        deps = [src_path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+        deps.append(os.path.join(ROOT, "include", "cil_gpu.h"))
+        if (not ptxas_info and os.path.exists(obj)
+                and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
+            continue
+        cmd = [nvcc(), *flags(extra), "-c", src_path, "-o", obj]
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    failed = []
+    for src, p in procs:
+        out, _ = p.communicate()
+        if verbose or p.returncode != 0 or ptxas_info:
+            sys.stdout.write(out)
+        if p.returncode != 0:
+            failed.append(src)
+    if failed:
+        raise RuntimeError(f"nvcc failed for {failed}")
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stdout.write(r.stdout)
+        raise RuntimeError("link failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, ptxas_info="-v" in sys.argv)
+    print(LIB)

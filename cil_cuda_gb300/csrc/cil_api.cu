@@ -1,0 +1,920 @@
+// Host side of libcilgpu.so: the C ABI declared in include/cil_gpu.h.
+//
+// A handle owns every device array of its colonies (layout in cil_internal.cuh), one CUDA
+// stream, and, in oracle mode (CIL_RNG_DSFMT), a host mirror of the integer cell state
+// (cycle start / end per cell and the cell count) so that the host can draw the
+// reference's random numbers in the reference's order without reading the device back:
+// division is decided by the cycle clock alone and apoptosis tests every slot, so the
+// draw sequence depends only on integers the host already knows.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cil_gpu.h"
+#include "cil_internal.cuh"
+#include "host_rng.h"
+
+using namespace cil;
+
+namespace {
+
+constexpr int kSlotAlign = 1024;
+
+template <typename T>
+T *dalloc(size_t n) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  return static_cast<T *>(p);
+}
+
+struct HostColony {
+  cil_colony_params p{};
+  int cap = 0;
+  bool uploaded = false;
+  double sigma_max = 0.0;
+  // oracle-mode mirror
+  int n = 0;
+  std::vector<int> t0, tsw;
+};
+
+}  // namespace
+
+struct cil_handle {
+  cil_config cfg{};
+  int B = 0, D = 2;
+  std::vector<HostColony> hc;
+  std::vector<ColonyConst> cc;
+  int CC = 0;          // total cell capacity
+  size_t SS = 0;       // total slots
+  int NBpad = 0;       // total padded bins
+  int nscan = 0;       // scan blocks
+  int ctiles = 0;      // max cell tiles
+  int grid_slots = 0;  // persistent grid for slot kernels
+  int grid_cells = 0;
+  int grid_force = 0;
+  int nsm = 0;
+  bool geometry_ready = false;
+  int64_t ts = 0;
+  std::string err;
+  cudaStream_t stream = nullptr;
+
+  // device arrays
+  ColonyConst *d_col = nullptr;
+  ColonyCounters *d_cnt = nullptr;
+  double *d_x[2] = {nullptr, nullptr};
+  double *d_sig[2] = {nullptr, nullptr};
+  int *d_eid[2] = {nullptr, nullptr};
+  int cur = 0, meta = 0;
+  float *d_u = nullptr, *d_sigf = nullptr;
+  double *d_vel = nullptr, *d_frc = nullptr;
+  double *d_vel2 = nullptr;  // second velocity buffer for rebuilds outside a step
+  int *d_key = nullptr;
+  unsigned long long *d_perm = nullptr;
+  int *d_bcount = nullptr;
+  int2 *d_range = nullptr;
+  int *d_scan_sum = nullptr, *d_scan_off = nullptr, *d_scan_col = nullptr;
+  int *d_slot_of = nullptr;
+  int *d_t0 = nullptr, *d_tsw = nullptr;
+  int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
+  int *d_tile_count = nullptr, *d_tile_off = nullptr;
+  int *d_dead = nullptr;
+  double *d_obs = nullptr;  // com_prev, disp, vref: 3 * D * CC
+  bool obs_ready_any = false;
+  std::vector<char> obs_ready;
+  double *d_partials = nullptr;
+  int partials_cap = 0;
+  double *d_stage = nullptr;  // staging for upload/download, sized for the largest colony
+  size_t stage_cap = 0;
+  // oracle mode
+  HostRng rng;
+  double *d_noise = nullptr;
+  double *h_noise = nullptr;  // pinned
+  int *d_oracle_i = nullptr;  // mothers, cycle ends, removal ops
+  double *d_oracle_d = nullptr;
+  size_t oracle_cap = 0;
+  // timings
+  std::vector<cudaEvent_t> evpool;
+  double t_rebuild = 0, t_force = 0, t_events = 0, t_total = 0;
+  int64_t launches = 0;
+};
+
+namespace {
+
+cil_status fail(cil_handle *h, cil_status s, const std::string &m) {
+  if (h) h->err = m;
+  return s;
+}
+
+#define CUDA_TRY(h, call)                                                              \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail((h), CIL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void free_all(cil_handle *h) {
+  void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
+                  h->d_eid[1], h->d_u, h->d_sigf, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
+                  h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
+                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_obs,
+                  h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->h_noise) cudaFreeHost(h->h_noise);
+  for (auto e : h->evpool) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+// bins per axis as LinkListOrtho::get_opt_size + reset (Utils.hpp:872-908)
+void grid_geometry(const cil_colony_params &p, double width, int *ns, bool *single) {
+  const int D = p.dim;
+  double mn = p.box[0];
+  for (int d = 1; d < D; ++d) mn = std::min(mn, p.box[d]);
+  const double ir = 1.0 / (width + mn * 1.0e-8);
+  bool overkill = false;
+  for (int d = 0; d < 3; ++d) ns[d] = 1;
+  for (int d = 0; d < D; ++d) {
+    ns[d] = static_cast<int>(p.box[d] * ir);
+    overkill = overkill || ns[d] < 3;
+  }
+  if (overkill)
+    for (int d = 0; d < D; ++d) ns[d] = 1;
+  *single = overkill;
+}
+
+double bin_width_for(const cil_handle *h, const HostColony &c) {
+  const double need = c.p.rcut_scale * c.sigma_max + h->cfg.skin;
+  return h->cfg.bin_width > need ? h->cfg.bin_width : need;
+}
+
+cil_status setup_geometry(cil_handle *h) {
+  int bin_base = 0;
+  for (int c = 0; c < h->B; ++c) {
+    HostColony &hc = h->hc[c];
+    ColonyConst &C = h->cc[c];
+    if (!hc.uploaded) return fail(h, CIL_ERR_STATE, "colony " + std::to_string(c) + " not uploaded");
+    const double width = bin_width_for(h, hc);
+    bool single;
+    grid_geometry(hc.p, width, C.ns, &single);
+    C.single_bin = single ? 1 : 0;
+    long long nb = 1;
+    for (int d = 0; d < h->D; ++d) nb *= C.ns[d];
+    if (nb > (1ll << 30)) return fail(h, CIL_ERR_CONFIG, "bin grid too large");
+    C.nbins = static_cast<int>(nb);
+    C.nbins_pad = ((C.nbins + kScanItems - 1) / kScanItems) * kScanItems;
+    C.bin_base = bin_base;
+    C.scan_base = bin_base / kScanItems;
+    bin_base += C.nbins_pad;
+    for (int d = 0; d < 3; ++d) {
+      C.bw[d] = d < h->D ? hc.p.box[d] / C.ns[d] : 0.0;
+      C.bwf[d] = static_cast<float>(C.bw[d]);
+    }
+  }
+  if (bin_base != h->NBpad) {
+    cudaFree(h->d_bcount);
+    cudaFree(h->d_range);
+    cudaFree(h->d_scan_sum);
+    cudaFree(h->d_scan_off);
+    cudaFree(h->d_scan_col);
+    h->NBpad = bin_base;
+    h->nscan = bin_base / kScanItems;
+    h->d_bcount = dalloc<int>(h->NBpad);
+    h->d_range = dalloc<int2>(h->NBpad);
+    h->d_scan_sum = dalloc<int>(h->nscan);
+    h->d_scan_off = dalloc<int>(h->nscan);
+    h->d_scan_col = dalloc<int>(h->nscan);
+    if (!h->d_bcount || !h->d_range || !h->d_scan_sum || !h->d_scan_off || !h->d_scan_col)
+      return fail(h, CIL_ERR_CUDA, "out of device memory for bins");
+  }
+  std::vector<int> scol(h->nscan);
+  for (int c = 0; c < h->B; ++c)
+    for (int i = 0; i < h->cc[c].nbins_pad / kScanItems; ++i) scol[h->cc[c].scan_base + i] = c;
+  CUDA_TRY(h, cudaMemsetAsync(h->d_bcount, 0, sizeof(int) * h->NBpad, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(h->d_range, 0, sizeof(int2) * h->NBpad, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_scan_col, scol.data(), sizeof(int) * h->nscan, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_col, h->cc.data(), sizeof(ColonyConst) * h->B, cudaMemcpyHostToDevice, h->stream));
+  h->geometry_ready = true;
+  return CIL_OK;
+}
+
+cil_status ensure_ready(cil_handle *h) {
+  CUDA_TRY(h, cudaSetDevice(h->cfg.device));
+  if (!h->geometry_ready) return setup_geometry(h);
+  return CIL_OK;
+}
+
+RebuildArgs rebuild_args(cil_handle *h) {
+  RebuildArgs a{};
+  a.col = h->d_col;
+  a.cnt = h->d_cnt;
+  a.B = h->B;
+  a.SS = h->SS;
+  a.tiles_used = h->d_tiles_used;
+  a.tiles_live = h->d_tiles_live;
+  a.scan_col = h->d_scan_col;
+  a.nscan = h->nscan;
+  a.x_in = h->d_x[h->cur];
+  a.sig_in = h->d_sig[h->meta];
+  a.eid_in = h->d_eid[h->meta];
+  a.x_out = h->d_x[1 - h->cur];
+  a.sig_out = h->d_sig[1 - h->meta];
+  a.eid_out = h->d_eid[1 - h->meta];
+  a.u_out = h->cfg.precision == CIL_PREC_MIXED ? h->d_u : nullptr;
+  a.sigf_out = h->cfg.precision == CIL_PREC_MIXED ? h->d_sigf : nullptr;
+  a.key = h->d_key;
+  a.bcount = h->d_bcount;
+  a.range = h->d_range;
+  a.perm = h->d_perm;
+  a.scan_sum = h->d_scan_sum;
+  a.scan_off = h->d_scan_off;
+  a.slot_of = h->d_slot_of;
+  a.dim = h->D;
+  return a;
+}
+
+// A rebuild inside a step needs no velocities (the force pass rewrites them); a rebuild
+// outside a step (cil_forces, cil_bins) carries them through the permutation so that a
+// later download still pairs each element with its own velocity.
+cil_status do_rebuild(cil_handle *h, bool carry_vel = false) {
+  RebuildArgs a = rebuild_args(h);
+  if (carry_vel) {
+    if (!h->d_vel2) {
+      h->d_vel2 = dalloc<double>(static_cast<size_t>(h->D) * h->SS);
+      if (!h->d_vel2) return fail(h, CIL_ERR_CUDA, "out of device memory (velocities)");
+    }
+    a.vel_in = h->d_vel;
+    a.vel_out = h->d_vel2;
+  }
+  launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
+  launch_rebuild(a, h->grid_slots, h->stream);
+  h->cur = 1 - h->cur;
+  h->meta = 1 - h->meta;
+  if (carry_vel) std::swap(h->d_vel, h->d_vel2);
+  return CIL_OK;
+}
+
+ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, double *frc) {
+  ForceArgs a{};
+  a.col = h->d_col;
+  a.cnt = h->d_cnt;
+  a.B = h->B;
+  a.SS = h->SS;
+  a.tiles_live = h->d_tiles_live;
+  a.x_in = h->d_x[h->cur];
+  a.x_out = h->d_x[1 - h->cur];
+  a.sig = h->d_sig[h->meta];
+  a.eid = h->d_eid[h->meta];
+  a.u = h->d_u;
+  a.sigf = h->d_sigf;
+  a.range = h->d_range;
+  a.slot_of = h->d_slot_of;
+  a.t0 = h->d_t0;
+  a.tsw = h->d_tsw;
+  a.noise = h->d_noise;
+  a.vel = vel;
+  a.frc = frc;
+  a.ts = static_cast<int>(h->ts);
+  a.seed_lo = static_cast<uint32_t>(h->cfg.seed);
+  a.seed_hi = static_cast<uint32_t>(h->cfg.seed >> 32);
+  a.noise_mode = noise_mode;
+  a.integrate = integrate;
+  return a;
+}
+
+EventArgs event_args(cil_handle *h) {
+  EventArgs a{};
+  a.col = h->d_col;
+  a.cnt = h->d_cnt;
+  a.B = h->B;
+  a.SS = h->SS;
+  a.tiles_cell = h->d_tiles_cell;
+  a.x = h->d_x[h->cur];
+  a.sig = h->d_sig[h->meta];
+  a.eid = h->d_eid[h->meta];
+  a.vel = h->d_vel;
+  a.slot_of = h->d_slot_of;
+  a.t0 = h->d_t0;
+  a.tsw = h->d_tsw;
+  a.tile_count = h->d_tile_count;
+  a.tile_off = h->d_tile_off;
+  a.dead = h->d_dead;
+  if (h->d_obs) {
+    a.obs_com_prev = h->d_obs;
+    a.obs_disp = h->d_obs + static_cast<size_t>(h->D) * h->CC;
+    a.obs_vref = h->d_obs + 2 * static_cast<size_t>(h->D) * h->CC;
+  }
+  a.CC = h->CC;
+  a.ts = static_cast<int>(h->ts);
+  a.seed_lo = static_cast<uint32_t>(h->cfg.seed);
+  a.seed_hi = static_cast<uint32_t>(h->cfg.seed >> 32);
+  return a;
+}
+
+// oracle mode: the passive noise of the coming force evaluation, drawn exactly as
+// updateWienerProcess does (CIL.cu:793-818), in canonical [cell][elem][dim] order
+cil_status draw_oracle_noise(cil_handle *h, bool *any) {
+  *any = false;
+  size_t total = 0;
+  for (int c = 0; c < h->B; ++c) {
+    const HostColony &hc = h->hc[c];
+    if (!(hc.p.noise_D > 0.0)) continue;
+    *any = true;
+    const double amp = std::sqrt(2.0 * hc.p.noise_D) * (1.0 / std::sqrt(hc.p.dt));
+    const int per = hc.p.noise_per_cell ? 1 : 2;
+    const size_t base = static_cast<size_t>(h->cc[c].cell_base) * per * h->D;
+    const size_t m = static_cast<size_t>(hc.n) * per * h->D;
+    for (size_t i = 0; i < m; ++i) h->h_noise[base + i] = amp * h->rng.normal();
+    total = std::max(total, base + m);
+  }
+  if (*any && total > 0)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_noise, h->h_noise, sizeof(double) * total, cudaMemcpyHostToDevice, h->stream));
+  return CIL_OK;
+}
+
+cil_status ensure_oracle_buffers(cil_handle *h, size_t need_i, size_t need_d) {
+  const size_t need = std::max(need_i, need_d);
+  if (need <= h->oracle_cap) return CIL_OK;
+  cudaFree(h->d_oracle_i);
+  cudaFree(h->d_oracle_d);
+  h->oracle_cap = std::max(need, h->oracle_cap * 2);
+  h->d_oracle_i = dalloc<int>(h->oracle_cap);
+  h->d_oracle_d = dalloc<double>(h->oracle_cap);
+  if (!h->d_oracle_i || !h->d_oracle_d) return fail(h, CIL_ERR_CUDA, "out of device memory (oracle lists)");
+  return CIL_OK;
+}
+
+// oracle mode: division and apoptosis draws on the host mirror, replayed on the device
+cil_status oracle_events(cil_handle *h) {
+  const int ts = static_cast<int>(h->ts);
+  for (int c = 0; c < h->B; ++c) {
+    HostColony &hc = h->hc[c];
+    const int D = h->D;
+    std::vector<int> mothers, tsws;
+    std::vector<double> dirs;
+    const int n0 = hc.n;
+    if (hc.p.divide) {
+      for (int i = 0; i < n0; ++i) {
+        if (hc.tsw[i] != ts) continue;
+        if (hc.n >= hc.cap) continue;  // the oracle skips divisions beyond capacity
+        const int k = hc.n++;
+        double dm[3] = {0, 0, 0}, dd[3] = {0, 0, 0};
+        h->rng.on_dsphere(D, dm);
+        h->rng.on_dsphere(D, dd);
+        auto span = [&]() {
+          const int s = nint(h->rng.normal(hc.p.div_tau_mu, hc.p.div_tau_sigma) / hc.p.dt);
+          return s >= 1 ? s : 1;
+        };
+        const int td = ts + span();
+        const int tm = ts + span();
+        hc.t0[k] = ts;
+        hc.tsw[k] = td;
+        hc.t0[i] = ts;
+        hc.tsw[i] = tm;
+        mothers.push_back(i);
+        tsws.push_back(td);
+        tsws.push_back(tm);
+        for (int d = 0; d < D; ++d) dirs.push_back(dm[d]);
+        for (int d = 0; d < D; ++d) dirs.push_back(dd[d]);
+      }
+    }
+    std::vector<int> ops;
+    if (hc.p.apop_rate > 0.0) {
+      const double prob = hc.p.apop_rate * hc.p.dt;
+      int i = 0;
+      while (i < hc.n) {
+        if (h->rng.uniform0x(1.0) <= prob) {
+          const int last = hc.n - 1;
+          hc.t0[i] = hc.t0[last];
+          hc.tsw[i] = hc.tsw[last];
+          hc.n -= 1;
+          ops.push_back(i);
+        } else {
+          ++i;
+        }
+      }
+    }
+    const int ndiv = static_cast<int>(mothers.size());
+    if (ndiv == 0 && ops.empty()) continue;
+    const size_t ni = mothers.size() + tsws.size() + ops.size();
+    cil_status st = ensure_oracle_buffers(h, ni, dirs.size());
+    if (st != CIL_OK) return st;
+    std::vector<int> packed;
+    packed.insert(packed.end(), mothers.begin(), mothers.end());
+    packed.insert(packed.end(), tsws.begin(), tsws.end());
+    packed.insert(packed.end(), ops.begin(), ops.end());
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_oracle_i, packed.data(), sizeof(int) * packed.size(), cudaMemcpyHostToDevice, h->stream));
+    if (!dirs.empty())
+      CUDA_TRY(h, cudaMemcpyAsync(h->d_oracle_d, dirs.data(), sizeof(double) * dirs.size(), cudaMemcpyHostToDevice, h->stream));
+    // the staged host vectors must stay alive until the copies ran
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    EventArgs a = event_args(h);
+    launch_divisions_list(a, c, n0, ndiv, h->d_oracle_i, h->d_oracle_d, h->d_oracle_i + ndiv, D, h->stream);
+    launch_apo_ops_with_div(a, c, ndiv, static_cast<int>(ops.size()), h->d_oracle_i + 3 * ndiv, D, h->stream);
+    h->launches += (ndiv > 0 ? 1 : 0) + 1;
+  }
+  return CIL_OK;
+}
+
+cil_status ensure_stage(cil_handle *h, size_t need) {
+  if (need <= h->stage_cap) return CIL_OK;
+  cudaFree(h->d_stage);
+  h->stage_cap = std::max(need, static_cast<size_t>(1024));
+  h->d_stage = dalloc<double>(h->stage_cap);
+  if (!h->d_stage) {
+    h->stage_cap = 0;
+    return fail(h, CIL_ERR_CUDA, "out of device memory (staging)");
+  }
+  return CIL_OK;
+}
+
+cudaEvent_t pool_event(cil_handle *h, size_t i) {
+  while (h->evpool.size() <= i) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    h->evpool.push_back(e);
+  }
+  return h->evpool[i];
+}
+
+cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = nullptr) {
+  std::vector<ColonyCounters> k(h->B);
+  CUDA_TRY(h, cudaMemcpyAsync(k.data(), h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (out) *out = k;
+  for (int c = 0; c < h->B; ++c) {
+    if (k[c].err & kErrNan) return fail(h, CIL_ERR_NAN, "non-finite force in colony " + std::to_string(c));
+    if (k[c].err & kErrBox) return fail(h, CIL_ERR_OUT_OF_BOX, "element left the box in colony " + std::to_string(c));
+    if (k[c].err & kErrCap) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(c));
+  }
+  return CIL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cil_version(void) { return "cil-gb300 0.1 (sm_103a)"; }
+
+cil_status cil_host_rng_draw(uint32_t seed, int32_t kind, int64_t n, double *out) {
+  if (!out || n < 0 || kind < 0 || kind > 5) return CIL_ERR_CONFIG;
+  HostRng r;
+  r.seed(seed);
+  for (int64_t i = 0; i < n; ++i) {
+    switch (kind) {
+      case 0: out[i] = r.close_open(); break;
+      case 1: out[i] = r.open_open(); break;
+      case 2: out[i] = r.uniform(); break;
+      case 3: out[i] = r.normal(); break;
+      case 4: r.on_dsphere(2, out + 2 * i); break;
+      default: r.on_dsphere(3, out + 3 * i); break;
+    }
+  }
+  return CIL_OK;
+}
+
+void cil_last_error(const cil_handle *h, char *buf, size_t len) {
+  if (!buf || len == 0) return;
+  const std::string &m = h ? h->err : std::string("null handle");
+  std::snprintf(buf, len, "%s", m.c_str());
+}
+
+cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, const int32_t *cap_cells,
+                      cil_handle **out) {
+  if (!out) return CIL_ERR_CONFIG;
+  *out = nullptr;
+  if (!cfg || !params || !cap_cells) return CIL_ERR_CONFIG;
+  if (cfg->dim != 2 && cfg->dim != 3) return CIL_ERR_CONFIG;
+  if (cfg->num_colonies <= 0) return CIL_ERR_CONFIG;
+  if (cfg->force_law < 0 || cfg->force_law > 2) return CIL_ERR_CONFIG;
+  if (cfg->precision != CIL_PREC_FP64 && cfg->precision != CIL_PREC_MIXED) return CIL_ERR_CONFIG;
+  if (cfg->rng_mode != CIL_RNG_PHILOX && cfg->rng_mode != CIL_RNG_DSFMT) return CIL_ERR_CONFIG;
+  if (cfg->skin != 0.0) return CIL_ERR_CONFIG;  // the skin path is not part of this build
+  auto *h = new cil_handle();
+  h->cfg = *cfg;
+  h->B = cfg->num_colonies;
+  h->D = cfg->dim;
+  h->hc.resize(h->B);
+  h->cc.resize(h->B);
+  long long cells = 0, slots = 0;
+  for (int c = 0; c < h->B; ++c) {
+    const cil_colony_params &p = params[c];
+    if (p.dim != cfg->dim || p.force_law != cfg->force_law || cap_cells[c] <= 0 || !(p.dt > 0.0) ||
+        !(p.zeta[0] > 0.0) || !(p.zeta[1] > 0.0) || p.nwalls < 0 || p.nwalls > 2 ||
+        !(p.rcut_scale > 0.0)) {
+      delete h;
+      return CIL_ERR_CONFIG;
+    }
+    for (int d = 0; d < cfg->dim; ++d)
+      if (!(p.box[d] > 0.0)) {
+        delete h;
+        return CIL_ERR_CONFIG;
+      }
+    if (p.apop_rate * p.dt >= 1.0) {  // CIL.cuh:235
+      delete h;
+      return CIL_ERR_CONFIG;
+    }
+    HostColony &hc = h->hc[c];
+    hc.p = p;
+    hc.cap = cap_cells[c];
+    ColonyConst &C = h->cc[c];
+    std::memset(&C, 0, sizeof C);
+    for (int d = 0; d < 3; ++d) {
+      C.box[d] = d < cfg->dim ? p.box[d] : 1.0;
+      C.ih[d] = 1.0 / C.box[d];
+      C.periodic[d] = d < cfg->dim ? (p.periodic[d] != 0) : 0;
+      C.ns[d] = 1;
+    }
+    C.cell_base = static_cast<int>(cells);
+    C.cell_cap = cap_cells[c];
+    C.slot_base = static_cast<int>(slots);
+    C.slot_cap = static_cast<int>(((2ll * cap_cells[c] + kSlotAlign - 1) / kSlotAlign) * kSlotAlign);
+    C.force_law = p.force_law;
+    C.noise_per_cell = p.noise_per_cell;
+    C.divide = p.divide;
+    C.nwalls = p.nwalls;
+    for (int w = 0; w < 2; ++w) {
+      C.wall_dir[w] = p.wall_dir[w];
+      C.wall_pos[w] = p.wall_pos[w];
+    }
+    C.wall_E = p.wall_E;
+    C.epsilon = p.epsilon;
+    C.rcut_scale = p.rcut_scale;
+    for (int j = 0; j < 2; ++j) {
+      C.zeta[j] = p.zeta[j];
+      C.temp[j] = p.dt * (1.0 / p.zeta[j]);
+      C.mu_eff[j] = C.temp[j] / p.dt;
+      C.motility[j] = p.motility[j];
+    }
+    C.kappa = p.kappa;
+    C.rest0 = p.rest0;
+    C.rest1 = p.rest1;
+    C.noise_amp = p.noise_D > 0.0 ? std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt)) : 0.0;
+    C.dt = p.dt;
+    C.div_tau_mu = p.div_tau_mu;
+    C.div_tau_sigma = p.div_tau_sigma;
+    C.apop_p = p.apop_rate * p.dt;
+    cells += cap_cells[c];
+    slots += C.slot_cap;
+    if (cells > (1ll << 29) || slots > (1ll << 30)) {
+      delete h;
+      return CIL_ERR_CONFIG;
+    }
+  }
+  h->CC = static_cast<int>(cells);
+  h->SS = static_cast<size_t>(slots);
+  h->obs_ready.assign(h->B, 0);
+
+  cudaError_t e = cudaSetDevice(cfg->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, cfg->device);
+  if (e != cudaSuccess) {
+    h->err = cudaGetErrorString(e);
+    free_all(h);
+    delete h;
+    return CIL_ERR_CUDA;
+  }
+  const size_t SS = h->SS, D = h->D;
+  h->d_col = dalloc<ColonyConst>(h->B);
+  h->d_cnt = dalloc<ColonyCounters>(h->B);
+  for (int b = 0; b < 2; ++b) {
+    h->d_x[b] = dalloc<double>(D * SS);
+    h->d_sig[b] = dalloc<double>(SS);
+    h->d_eid[b] = dalloc<int>(SS);
+  }
+  if (cfg->precision == CIL_PREC_MIXED) {
+    h->d_u = dalloc<float>(D * SS);
+    h->d_sigf = dalloc<float>(SS);
+  }
+  h->d_vel = dalloc<double>(D * SS);
+  h->d_key = dalloc<int>(SS);
+  h->d_perm = dalloc<unsigned long long>(SS);
+  h->d_slot_of = dalloc<int>(2 * static_cast<size_t>(h->CC));
+  h->d_t0 = dalloc<int>(h->CC);
+  h->d_tsw = dalloc<int>(h->CC);
+  h->d_tiles_used = dalloc<int>(h->B + 1);
+  h->d_tiles_live = dalloc<int>(h->B + 1);
+  h->d_tiles_cell = dalloc<int>(h->B + 1);
+  h->ctiles = 0;
+  for (int c = 0; c < h->B; ++c) h->ctiles += (h->hc[c].cap + kTile - 1) / kTile;
+  h->d_tile_count = dalloc<int>(h->ctiles + 1);
+  h->d_tile_off = dalloc<int>(h->ctiles + 1);
+  h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
+  bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_sig[0] && h->d_sig[1] && h->d_eid[0] &&
+            h->d_eid[1] && h->d_vel && h->d_key && h->d_perm && h->d_slot_of && h->d_t0 && h->d_tsw &&
+            h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell && h->d_tile_count && h->d_tile_off &&
+            h->d_dead && (cfg->precision != CIL_PREC_MIXED || (h->d_u && h->d_sigf));
+  if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {
+    const size_t nn = 2 * static_cast<size_t>(h->CC) * D;
+    h->d_noise = dalloc<double>(nn);
+    ok = h->d_noise && cudaMallocHost(&h->h_noise, sizeof(double) * nn) == cudaSuccess;
+    h->rng.seed(static_cast<uint32_t>(cfg->seed));
+  }
+  if (!ok) {
+    h->err = "out of device memory";
+    free_all(h);
+    delete h;
+    return CIL_ERR_CUDA;
+  }
+  // static parts of the colony table (bases, capacities, physics); the bin geometry is
+  // filled in once every colony has been uploaded
+  cudaMemcpyAsync(h->d_col, h->cc.data(), sizeof(ColonyConst) * h->B, cudaMemcpyHostToDevice, h->stream);
+  cudaMemsetAsync(h->d_cnt, 0, sizeof(ColonyCounters) * h->B, h->stream);
+  cudaMemsetAsync(h->d_vel, 0, sizeof(double) * D * SS, h->stream);
+  cudaMemsetAsync(h->d_eid[0], 0xff, sizeof(int) * SS, h->stream);
+  cudaMemsetAsync(h->d_eid[1], 0xff, sizeof(int) * SS, h->stream);
+  cudaMemsetAsync(h->d_key, 0xff, sizeof(int) * SS, h->stream);
+  h->grid_slots = std::max(1, std::min(h->nsm * 8, static_cast<int>((SS + kTile - 1) / kTile)));
+  h->grid_cells = std::max(1, std::min(h->nsm * 8, h->ctiles));
+  h->grid_force = h->grid_slots;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->err = "initialisation failed";
+    free_all(h);
+    delete h;
+    return CIL_ERR_CUDA;
+  }
+  *out = h;
+  return CIL_OK;
+}
+
+void cil_destroy(cil_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+}
+
+cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !v || !v->pos || !v->sigma || !v->t0 || !v->tswitch)
+    return fail(h, CIL_ERR_CONFIG, "cil_upload: bad arguments");
+  HostColony &hc = h->hc[colony];
+  const int n = v->ncells;
+  if (n < 0 || n > hc.cap) return fail(h, CIL_ERR_CAPACITY, "cil_upload: more cells than the capacity");
+  CUDA_TRY(h, cudaSetDevice(h->cfg.device));
+  const int D = h->D;
+  const ColonyConst &C = h->cc[colony];
+  double smax = 0.0;
+  for (int e = 0; e < 2 * n; ++e) {
+    const double s = v->sigma[e];
+    if (!(s > 0.0) || !std::isfinite(s)) return fail(h, CIL_ERR_CONFIG, "cil_upload: diameters must be positive");
+    smax = std::max(smax, s);
+  }
+  for (long long i = 0; i < 2ll * n * D; ++i) {
+    const int d = static_cast<int>(i % D);
+    const double x = v->pos[i];
+    if (!std::isfinite(x) || x < 0.0 || x >= hc.p.box[d])
+      return fail(h, CIL_ERR_OUT_OF_BOX, "cil_upload: position outside the box (CIL.cuh:54-66)");
+  }
+  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * (D + 1));
+  if (sst != CIL_OK) return sst;
+  // the positions are re-binned by the first rebuild; the fresh slots follow the current
+  // buffers
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, v->pos, sizeof(double) * 2 * n * D, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + 2 * n * D, v->sigma, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_t0 + C.cell_base, v->t0, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_tsw + C.cell_base, v->tswitch, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(h->d_vel + 0, 0, sizeof(double) * D * h->SS, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(h->d_eid[h->meta] + C.slot_base, 0xff, sizeof(int) * C.slot_cap, h->stream));
+  launch_upload_scatter(h->d_col, colony, n, D, h->SS, h->d_stage, h->d_stage + 2 * n * D, h->d_x[h->cur],
+                        h->d_sig[h->meta], h->d_eid[h->meta], h->d_slot_of, h->d_cnt, h->stream);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  hc.uploaded = true;
+  hc.sigma_max = smax;
+  hc.n = n;
+  hc.t0.assign(v->t0, v->t0 + n);
+  hc.tsw.assign(v->tswitch, v->tswitch + n);
+  hc.t0.resize(hc.cap);
+  hc.tsw.resize(hc.cap);
+  h->ts = v->ts;
+  h->obs_ready[colony] = 0;
+  h->geometry_ready = false;
+  return CIL_OK;
+}
+
+cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (nsteps < 0) return fail(h, CIL_ERR_CONFIG, "cil_step: negative step count");
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
+  h->t_rebuild = h->t_force = h->t_events = 0.0;
+  h->launches = 0;
+  for (int k = 0; k < nsteps; ++k) {
+    bool noise = false;
+    if (oracle) {
+      st = draw_oracle_noise(h, &noise);
+      if (st != CIL_OK) return st;
+    } else {
+      for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;
+    }
+    const size_t e0 = 4 * static_cast<size_t>(k);
+    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
+    do_rebuild(h);
+    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 1), h->stream));
+    const bool last = k == nsteps - 1;
+    ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
+    launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+    h->cur = 1 - h->cur;
+    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
+    h->ts += 1;
+    if (oracle) {
+      st = oracle_events(h);
+      if (st != CIL_OK) return st;
+    } else {
+      launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
+      launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
+    }
+    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
+    CUDA_TRY(h, cudaGetLastError());
+  }
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  h->t_total = 0.0;
+  if (nsteps > 0) {
+    float t = 0;
+    cudaEventElapsedTime(&t, h->evpool[0], h->evpool[4 * (nsteps - 1) + 3]);
+    h->t_total = t;
+  }
+  // kernels per step: rebuild 1 + 9, force 1, events 1 + 4 (Philox) or 2 when the host
+  // reports divisions/removals (oracle mode, counted by oracle_events)
+  h->launches += static_cast<int64_t>(nsteps) * (oracle ? 11 : 16);
+  for (int k = 0; k < nsteps; ++k) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, h->evpool[4 * k], h->evpool[4 * k + 1]);
+    cudaEventElapsedTime(&b, h->evpool[4 * k + 1], h->evpool[4 * k + 2]);
+    cudaEventElapsedTime(&c, h->evpool[4 * k + 2], h->evpool[4 * k + 3]);
+    h->t_rebuild += a;
+    h->t_force += b;
+    h->t_events += c;
+  }
+  if (ts_out) *ts_out = h->ts;
+  return check_counters(h);
+}
+
+cil_status cil_forces(cil_handle *h, int32_t colony, double *frc) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !frc) return fail(h, CIL_ERR_CONFIG, "cil_forces: bad arguments");
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
+  bool noise = false;
+  if (oracle) {
+    st = draw_oracle_noise(h, &noise);
+    if (st != CIL_OK) return st;
+  } else {
+    for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;
+  }
+  if (!h->d_frc) {
+    h->d_frc = dalloc<double>(h->D * h->SS);
+    if (!h->d_frc) return fail(h, CIL_ERR_CUDA, "out of device memory (forces)");
+  }
+  st = do_rebuild(h, true);
+  if (st != CIL_OK) return st;
+  ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 0, nullptr, h->d_frc);
+  launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+  std::vector<ColonyCounters> k;
+  st = check_counters(h, &k);
+  if (st != CIL_OK && st != CIL_ERR_NAN) return st;
+  const int n = k[colony].ncell;
+  const ColonyConst &C = h->cc[colony];
+  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * h->D);
+  if (sst != CIL_OK) return sst;
+  launch_gather_canonical(n, h->D, h->SS, C.cell_base, h->d_slot_of, h->d_frc, h->D, h->d_stage, h->stream);
+  CUDA_TRY(h, cudaMemcpyAsync(frc, h->d_stage, sizeof(double) * 2 * n * h->D, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return st;
+}
+
+cil_status cil_bins(cil_handle *h, int32_t colony, int32_t *ns, int32_t *bin_start, int32_t *elems,
+                    int32_t max_bins) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !ns || !bin_start || !elems)
+    return fail(h, CIL_ERR_CONFIG, "cil_bins: bad arguments");
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  const ColonyConst &C = h->cc[colony];
+  for (int d = 0; d < 3; ++d) ns[d] = C.ns[d];
+  if (C.nbins > max_bins) return fail(h, CIL_ERR_CAPACITY, "cil_bins: max_bins too small");
+  st = do_rebuild(h, true);
+  if (st != CIL_OK) return st;
+  std::vector<ColonyCounters> k;
+  st = check_counters(h, &k);
+  if (st != CIL_OK) return st;
+  std::vector<int2> r(C.nbins);
+  const int nlive = k[colony].nlive;
+  std::vector<int> e(std::max(nlive, 1));
+  CUDA_TRY(h, cudaMemcpyAsync(r.data(), h->d_range + C.bin_base, sizeof(int2) * C.nbins, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(e.data(), h->d_eid[h->meta] + C.slot_base, sizeof(int) * nlive, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  for (int b = 0; b < C.nbins; ++b) bin_start[b] = r[b].x - C.slot_base;
+  bin_start[C.nbins] = nlive;
+  for (int i = 0; i < nlive; ++i) elems[i] = e[i] - 2 * C.cell_base;
+  return CIL_OK;
+}
+
+cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *v) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !v) return fail(h, CIL_ERR_CONFIG, "cil_download: bad arguments");
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  std::vector<ColonyCounters> k;
+  st = check_counters(h, &k);
+  const int n = k[colony].ncell;
+  v->ts = static_cast<int32_t>(h->ts);
+  if (n > v->capacity) {
+    v->ncells = n;
+    return fail(h, CIL_ERR_CAPACITY, "cil_download: host arrays too small");
+  }
+  v->ncells = n;
+  const ColonyConst &C = h->cc[colony];
+  const int D = h->D;
+  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * (2 * D + 1));
+  if (sst != CIL_OK) return sst;
+  double *sp = h->d_stage, *ss = h->d_stage + 2 * n * D, *sv = ss + 2 * n;
+  launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_x[h->cur], D, sp, h->stream);
+  launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_sig[h->meta], 1, ss, h->stream);
+  launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_vel, D, sv, h->stream);
+  if (v->pos) CUDA_TRY(h, cudaMemcpyAsync(v->pos, sp, sizeof(double) * 2 * n * D, cudaMemcpyDeviceToHost, h->stream));
+  if (v->sigma) CUDA_TRY(h, cudaMemcpyAsync(v->sigma, ss, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
+  if (v->vel) CUDA_TRY(h, cudaMemcpyAsync(v->vel, sv, sizeof(double) * 2 * n * D, cudaMemcpyDeviceToHost, h->stream));
+  if (v->t0) CUDA_TRY(h, cudaMemcpyAsync(v->t0, h->d_t0 + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  if (v->tswitch) CUDA_TRY(h, cudaMemcpyAsync(v->tswitch, h->d_tsw + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return st;
+}
+
+static cil_status run_obs(cil_handle *h, int32_t colony, int reset, cil_obs *out) {
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  if (!h->d_obs) {
+    h->d_obs = dalloc<double>(3 * static_cast<size_t>(h->D) * h->CC);
+    if (!h->d_obs) return fail(h, CIL_ERR_CUDA, "out of device memory (observables)");
+    CUDA_TRY(h, cudaMemsetAsync(h->d_obs, 0, sizeof(double) * 3 * h->D * h->CC, h->stream));
+  }
+  std::vector<ColonyCounters> k;
+  st = check_counters(h, &k);
+  const int n = k[colony].ncell;
+  const int nblocks = std::max(1, (n + kTile - 1) / kTile);
+  if (nblocks * 4 > h->partials_cap) {
+    cudaFree(h->d_partials);
+    h->partials_cap = nblocks * 4;
+    h->d_partials = dalloc<double>(h->partials_cap);
+    if (!h->d_partials) return fail(h, CIL_ERR_CUDA, "out of device memory (partials)");
+  }
+  if (!reset && !h->obs_ready[colony]) {
+    EventArgs a = event_args(h);
+    launch_observables(a, colony, n, h->D, 1, h->d_partials, nblocks, h->stream);
+  }
+  EventArgs a = event_args(h);
+  launch_observables(a, colony, n, h->D, reset, h->d_partials, nblocks, h->stream);
+  h->obs_ready[colony] = 1;
+  std::vector<double> part(static_cast<size_t>(nblocks) * 4);
+  CUDA_TRY(h, cudaMemcpyAsync(part.data(), h->d_partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (out) {
+    double s[4] = {0, 0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+      for (int q = 0; q < 4; ++q) s[q] += part[static_cast<size_t>(b) * 4 + q];
+    out->ncells = n;
+    out->pad = 0;
+    out->mean_area = n ? s[0] / n : 0.0;
+    out->msd = n ? s[1] / n : 0.0;
+    out->vacf = s[3] > 0.0 ? s[2] / s[3] : 0.0;
+    out->ndiv_total = k[colony].ndiv_total;
+    out->napo_total = k[colony].napo_total;
+  }
+  return st;
+}
+
+cil_status cil_obs_reset(cil_handle *h, int32_t colony) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B) return fail(h, CIL_ERR_CONFIG, "cil_obs_reset: bad colony");
+  return run_obs(h, colony, 1, nullptr);
+}
+
+cil_status cil_observables(cil_handle *h, int32_t colony, cil_obs *out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "cil_observables: bad arguments");
+  return run_obs(h, colony, 0, out);
+}
+
+cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, double *events_ms,
+                       double *total_ms, int64_t *launches) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (rebuild_ms) *rebuild_ms = h->t_rebuild;
+  if (force_ms) *force_ms = h->t_force;
+  if (events_ms) *events_ms = h->t_events;
+  if (total_ms) *total_ms = h->t_total;
+  if (launches) *launches = h->launches;
+  return CIL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,254 @@
+// Rebuild of the binned element storage: a device counting sort that replaces the
+// reference's linked-list cell grid (LinkListOrtho::populate_list, Utils.hpp:982-1001;
+// LinkList/CellLinkList::populate, Container.cpp:58-103).
+//
+//   keys     one thread per used slot: bin id with the reference formula, atomic histogram
+//   scan     per colony exclusive scan of the histogram -> range[b] = (first, end) slot
+//   scatter  one thread per element: claim a slot inside its bin (atomic countdown, which
+//            also returns the histogram to zero for the next rebuild)
+//   sort     one thread per bin: order the bin's entries by element id (deterministic
+//            result independent of the atomic order)
+//   gather   one thread per destination slot: copy position, diameter, id; update slot_of;
+//            write FP32 bin-local coordinates for the mixed-precision pair kernel
+#include "cil_internal.cuh"
+
+namespace cil {
+
+namespace {
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) >= o) v += t;
+  }
+  return v;
+}
+
+// exclusive scan across a block of kTile threads; returns the exclusive prefix of v and
+// the block total in *total
+__device__ __forceinline__ int block_excl_scan(int v, int *total) {
+  __shared__ int warp_sums[kTile / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int inc = warp_incl_scan(v);
+  if (lane == 31) warp_sums[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < kTile / 32 ? warp_sums[lane] : 0;
+    w = warp_incl_scan(w);
+    if (lane < kTile / 32) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  const int base = wid > 0 ? warp_sums[wid - 1] : 0;
+  *total = warp_sums[kTile / 32 - 1];
+  __syncthreads();
+  return base + inc - v;
+}
+
+// tiles[c] = sum over colonies < c of ceil(count_c / kTile); tiles[B] = total.
+// which: 0 = nslot, 1 = nlive, 2 = ncell
+__global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which,
+                        int *__restrict__ tiles) {
+  int carry = 0;
+  for (int base = 0; base < B; base += kTile) {
+    const int c = base + threadIdx.x;
+    int v = 0;
+    if (c < B) {
+      const int n = which == 0 ? cnt[c].nslot : (which == 1 ? cnt[c].nlive : cnt[c].ncell);
+      v = (n + kTile - 1) / kTile;
+    }
+    int total;
+    const int ex = block_excl_scan(v, &total);
+    if (c < B) tiles[c] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) tiles[B] = carry;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_bin_keys(RebuildArgs a) {
+  const int total = a.tiles_used[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_used, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int s = C.slot_base + (t - a.tiles_used[c]) * kTile + threadIdx.x;
+    if (s >= C.slot_base + a.cnt[c].nslot) continue;
+    int k = -1;
+    if (a.eid_in[s] >= 0) {
+      double x[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d] = a.x_in[d * a.SS + s];
+      int b[D];
+      bin_coords<D>(C, x, b);
+      k = C.bin_base + bin_id<D>(C, b);
+      atomicAdd(a.bcount + k, 1);
+    }
+    a.key[s] = k;
+  }
+}
+
+// per scan block: sum of kScanItems bin counts
+__global__ void __launch_bounds__(kTile) k_scan_partial(RebuildArgs a) {
+  const int sb = blockIdx.x;
+  const ColonyConst &C = a.col[a.scan_col[sb]];
+  const int b0 = C.bin_base + (sb - C.scan_base) * kScanItems;
+  const int4 v = reinterpret_cast<const int4 *>(a.bcount + b0)[threadIdx.x];
+  int s = v.x + v.y + v.z + v.w;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ int ws[kTile / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kTile / 32; ++w) t += ws[w];
+    a.scan_sum[sb] = t;
+  }
+}
+
+// one block per colony: exclusive scan of its scan-block sums; nlive = nslot = total
+__global__ void __launch_bounds__(kTile) k_scan_colony(RebuildArgs a) {
+  const int c = blockIdx.x;
+  const ColonyConst &C = a.col[c];
+  const int nsb = C.nbins_pad / kScanItems;
+  int carry = 0;
+  for (int base = 0; base < nsb; base += kTile) {
+    const int i = base + threadIdx.x;
+    const int v = i < nsb ? a.scan_sum[C.scan_base + i] : 0;
+    int total;
+    const int ex = block_excl_scan(v, &total);
+    if (i < nsb) a.scan_off[C.scan_base + i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    a.cnt[c].nlive = carry;
+    a.cnt[c].nslot = carry;
+  }
+}
+
+// per scan block: bin ranges
+__global__ void __launch_bounds__(kTile) k_scan_final(RebuildArgs a) {
+  const int sb = blockIdx.x;
+  const ColonyConst &C = a.col[a.scan_col[sb]];
+  const int b0 = C.bin_base + (sb - C.scan_base) * kScanItems + threadIdx.x * 4;
+  const int4 v = *reinterpret_cast<const int4 *>(a.bcount + b0);
+  const int sum = v.x + v.y + v.z + v.w;
+  int total;
+  const int ex = block_excl_scan(sum, &total);
+  int start = C.slot_base + a.scan_off[sb] + ex;
+  int2 *r = a.range + b0;
+  r[0] = make_int2(start, start + v.x);
+  start += v.x;
+  r[1] = make_int2(start, start + v.y);
+  start += v.y;
+  r[2] = make_int2(start, start + v.z);
+  start += v.z;
+  r[3] = make_int2(start, start + v.w);
+}
+
+__global__ void __launch_bounds__(kTile) k_scatter(RebuildArgs a) {
+  const int total = a.tiles_used[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_used, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int s = C.slot_base + (t - a.tiles_used[c]) * kTile + threadIdx.x;
+    // nslot was overwritten by the scan; the used-slot bound is the tile range itself and
+    // every slot past the old nslot carries key -1 from k_bin_keys' zero-filled tail.
+    if (s >= C.slot_base + C.slot_cap) continue;
+    const int k = a.key[s];
+    if (k < 0) continue;
+    const int pos = a.range[k].x + atomicSub(a.bcount + k, 1) - 1;
+    a.perm[pos] = (static_cast<unsigned long long>(static_cast<uint32_t>(a.eid_in[s])) << 32) |
+                  static_cast<uint32_t>(s);
+  }
+}
+
+__global__ void __launch_bounds__(kTile) k_sort_bins(RebuildArgs a, int nbins_total) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins_total;
+       b += gridDim.x * blockDim.x) {
+    const int2 r = a.range[b];
+    for (int i = r.x + 1; i < r.y; ++i) {
+      const unsigned long long v = a.perm[i];
+      int j = i - 1;
+      while (j >= r.x && a.perm[j] > v) {
+        a.perm[j + 1] = a.perm[j];
+        --j;
+      }
+      a.perm[j + 1] = v;
+    }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_gather(RebuildArgs a) {
+  const int total = a.tiles_live[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_live, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int dst = C.slot_base + (t - a.tiles_live[c]) * kTile + threadIdx.x;
+    if (dst >= C.slot_base + a.cnt[c].nlive) continue;
+    const unsigned long long v = a.perm[dst];
+    const int src = static_cast<int>(v & 0xffffffffu);
+    const int e = static_cast<int>(v >> 32);
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      x[d] = a.x_in[d * a.SS + src];
+      a.x_out[d * a.SS + dst] = x[d];
+    }
+    if (a.vel_out) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) a.vel_out[d * a.SS + dst] = a.vel_in[d * a.SS + src];
+    }
+    const double sg = a.sig_in[src];
+    a.sig_out[dst] = sg;
+    a.eid_out[dst] = e;
+    a.slot_of[e] = dst;
+    if (a.u_out) {
+      int b[D];
+      bin_coords<D>(C, x, b);
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        a.u_out[d * a.SS + dst] = static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]);
+      a.sigf_out[dst] = static_cast<float>(sg);
+    }
+  }
+}
+
+// marks the slots past the used range as empty so that the scatter pass sees key -1
+__global__ void __launch_bounds__(kTile) k_clear_tail_keys(RebuildArgs a) {
+  const int c = blockIdx.y;
+  const ColonyConst &C = a.col[c];
+  const int used = a.cnt[c].nslot;
+  for (int i = used + blockIdx.x * blockDim.x + threadIdx.x; i < ((used + kTile - 1) / kTile) * kTile;
+       i += gridDim.x * blockDim.x)
+    if (i < C.slot_cap) a.key[C.slot_base + i] = -1;
+}
+
+}  // namespace
+
+void launch_tiles(const ColonyConst *, ColonyCounters *cnt, int B, int which, int *tiles,
+                  cudaStream_t s) {
+  k_tiles<<<1, kTile, 0, s>>>(cnt, B, which, tiles);
+}
+
+void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
+  // keys + histogram over the used slots (tiles_used must be current)
+  k_clear_tail_keys<<<dim3(1, a.B), kTile, 0, s>>>(a);
+  if (a.dim == 2)
+    k_bin_keys<2><<<grid_slots, kTile, 0, s>>>(a);
+  else
+    k_bin_keys<3><<<grid_slots, kTile, 0, s>>>(a);
+  k_scan_partial<<<a.nscan, kTile, 0, s>>>(a);
+  k_scan_colony<<<a.B, kTile, 0, s>>>(a);
+  k_scan_final<<<a.nscan, kTile, 0, s>>>(a);
+  k_scatter<<<grid_slots, kTile, 0, s>>>(a);
+  k_sort_bins<<<(a.nscan * kScanItems + kTile - 1) / kTile, kTile, 0, s>>>(a, a.nscan * kScanItems);
+  k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live));
+  if (a.dim == 2)
+    k_gather<2><<<grid_slots, kTile, 0, s>>>(a);
+  else
+    k_gather<3><<<grid_slots, kTile, 0, s>>>(a);
+}
+
+}  // namespace cil

@@ -1,0 +1,533 @@
+// Division, apoptosis, state transfer and observables on the device.
+//
+// Division (calculDivisions, CIL.cu:369-455, with the BASELINE growth model: a cell
+// divides when its cycle ends, ts == tswitch): due cells are ranked by a deterministic
+// per-colony scan in slot order, the daughter takes cell index ncell + rank (addCell
+// appends, Colony.cpp:355-359) and both cells are re-placed as binaryCellDivision does
+// (MD.cu:721-731): mother centred on her old front element, daughter on the old back
+// element, each with half-separation rest0/2 along a random axis.
+//
+// Apoptosis (calculApoptosis, CIL.cu:627-649): Philox mode draws one uniform per cell per
+// step; removals are applied as swap-with-last (removeCell, Colony.cpp:365-399), pairing
+// the holes below the new count with the surviving tail cells in ascending order. Oracle
+// mode replays the host's sequential removal list exactly.
+//
+// Element storage is binned: a removed cell's element slots become tombstones (eid -1)
+// until the next rebuild; a moved cell keeps its slots and only its ids change.
+#include "cil_internal.cuh"
+
+namespace cil {
+
+namespace {
+
+__device__ __forceinline__ int block_excl_scan_ev(int v, int *total) {
+  __shared__ int ws[kTile / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) ws[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < kTile / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < kTile / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  const int base = wid > 0 ? ws[wid - 1] : 0;
+  *total = ws[kTile / 32 - 1];
+  __syncthreads();
+  return base + inc - v;
+}
+
+template <int D>
+__device__ __forceinline__ void place(const ColonyConst &C, const double *master, const double *dir,
+                                      double radius, double *m_out, double *s_out) {
+  // binaryRandomReorientation (MD.cu:650-656): slave = master; master += r dir;
+  // slave -= r dir; both through BoundingBox::updatePos(r, v, dt) (Utils.hpp:561-566)
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double a = __dadd_rn(master[d], __dmul_rn(radius, dir[d]));
+    const double b = __dadd_rn(master[d], __dmul_rn(-radius, dir[d]));
+    m_out[d] = C.periodic[d] ? wrap_like_fmod(a, C.box[d]) : a;
+    s_out[d] = C.periodic[d] ? wrap_like_fmod(b, C.box[d]) : b;
+  }
+}
+
+template <int D>
+__device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int i, int k,
+                            const double *dir_m, const double *dir_d, int tsw_d, int tsw_m,
+                            int nslot0, int rank) {
+  const size_t SS = a.SS;
+  const int g = C.cell_base + i, gk = C.cell_base + k;
+  const int sb = a.slot_of[2 * g], sf = a.slot_of[2 * g + 1];
+  double xb[D], xf[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xb[d] = a.x[d * SS + sb];
+    xf[d] = a.x[d * SS + sf];
+  }
+  const double radius = 0.5 * C.rest0;
+  double m0[D], m1[D], d0[D], d1[D];
+  place<D>(C, xf, dir_m, radius, m1, m0);  // mother: master = front element
+  place<D>(C, xb, dir_d, radius, d0, d1);  // daughter: master = back element
+  const int s0 = C.slot_base + nslot0 + 2 * rank;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    a.x[d * SS + sb] = m0[d];
+    a.x[d * SS + sf] = m1[d];
+    a.x[d * SS + s0] = d0[d];
+    a.x[d * SS + s0 + 1] = d1[d];
+  }
+  a.sig[s0] = a.sig[sb];
+  a.sig[s0 + 1] = a.sig[sf];
+  a.eid[s0] = 2 * gk;
+  a.eid[s0 + 1] = 2 * gk + 1;
+  a.slot_of[2 * gk] = s0;
+  a.slot_of[2 * gk + 1] = s0 + 1;
+  if (a.vel) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      a.vel[d * SS + sb] = 0.0;
+      a.vel[d * SS + sf] = 0.0;
+      a.vel[d * SS + s0] = 0.0;
+      a.vel[d * SS + s0 + 1] = 0.0;
+    }
+  }
+  a.t0[g] = a.ts;
+  a.t0[gk] = a.ts;
+  a.tsw[gk] = tsw_d;
+  a.tsw[g] = tsw_m;
+  if (a.obs_disp) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      a.obs_com_prev[d * a.CC + gk] = a.obs_com_prev[d * a.CC + g];
+      a.obs_disp[d * a.CC + gk] = a.obs_disp[d * a.CC + g];
+      a.obs_vref[d * a.CC + gk] = a.obs_vref[d * a.CC + g];
+    }
+  }
+}
+
+// random axis and cycle length of a division in Philox mode
+template <int D>
+__device__ void division_draws(const EventArgs &a, int g, double *dir_m, double *dir_d,
+                               int &span_d, int &span_m, const ColonyConst &C) {
+  const u32x4 r1 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv, 0u,
+                                 a.seed_lo, a.seed_hi);
+  const u32x4 r2 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv2, 0u,
+                                 a.seed_lo, a.seed_hi);
+  if (D == 2) {
+    double s, c;
+    sincospi(2.0 * uniform53(r1.v[0], r1.v[1]), &s, &c);
+    dir_m[0] = c;
+    dir_m[1] = s;
+    sincospi(2.0 * uniform53(r1.v[2], r1.v[3]), &s, &c);
+    dir_d[0] = c;
+    dir_d[1] = s;
+  } else {
+    const double z1 = 2.0 * uniform53(r1.v[0], r1.v[1]) - 1.0;
+    const double z2 = 2.0 * uniform53(r1.v[2], r1.v[3]) - 1.0;
+    double s, c;
+    const double q1 = sqrt(fmax(0.0, 1.0 - z1 * z1)), q2 = sqrt(fmax(0.0, 1.0 - z2 * z2));
+    sincospi(2.0 * static_cast<double>(r2.v[2]) * 2.3283064365386963e-10, &s, &c);
+    dir_m[0] = q1 * c;
+    dir_m[1] = q1 * s;
+    dir_m[2] = z1;
+    sincospi(2.0 * static_cast<double>(r2.v[3]) * 2.3283064365386963e-10, &s, &c);
+    dir_d[0] = q2 * c;
+    dir_d[1] = q2 * s;
+    dir_d[2] = z2;
+  }
+  float n0, n1;
+  box_muller(r2.v[0], r2.v[1], n0, n1);
+  const int sd = nint((C.div_tau_mu + C.div_tau_sigma * static_cast<double>(n0)) / C.dt);
+  const int sm = nint((C.div_tau_mu + C.div_tau_sigma * static_cast<double>(n1)) / C.dt);
+  span_d = sd >= 1 ? sd : 1;  // randomTimeSpan, MD.cuh:434-436
+  span_m = sm >= 1 ? sm : 1;
+}
+
+__global__ void __launch_bounds__(kTile) k_div_count(EventArgs a) {
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int i = (t - a.tiles_cell[c]) * kTile + threadIdx.x;
+    const bool due = C.divide && i < a.cnt[c].ncell && a.tsw[C.cell_base + i] == a.ts;
+    const int n = __syncthreads_count(due);
+    if (threadIdx.x == 0) a.tile_count[t] = n;
+  }
+}
+
+__global__ void __launch_bounds__(kTile) k_div_scan(EventArgs a) {
+  const int c = blockIdx.x;
+  const ColonyConst &C = a.col[c];
+  const int t0 = a.tiles_cell[c], t1 = a.tiles_cell[c + 1];
+  int carry = 0;
+  for (int base = t0; base < t1; base += kTile) {
+    const int t = base + threadIdx.x;
+    const int v = t < t1 ? a.tile_count[t] : 0;
+    int total;
+    const int ex = block_excl_scan_ev(v, &total);
+    if (t < t1) a.tile_off[t] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    ColonyCounters &K = a.cnt[c];
+    const int room = C.cell_cap - K.ncell;
+    int allowed = carry < room ? carry : room;
+    if (allowed < 0) allowed = 0;
+    if (allowed < carry) K.err |= kErrCap;
+    K.ndiv_step = carry;
+    K.ndiv_allowed = allowed;
+    K.ndead = 0;
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_div_apply(EventArgs a) {
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const ColonyCounters &K = a.cnt[c];
+    const int n = K.ncell;
+    const int i = (t - a.tiles_cell[c]) * kTile + threadIdx.x;
+    const bool live = i < n;
+    const bool due = C.divide && live && a.tsw[C.cell_base + i] == a.ts;
+    int tot;
+    const int rank = a.tile_off[t] + block_excl_scan_ev(due ? 1 : 0, &tot);
+    bool daughter = false;
+    if (due && rank < K.ndiv_allowed) {
+      double dm[D], dd[D];
+      int span_d, span_m;
+      division_draws<D>(a, C.cell_base + i, dm, dd, span_d, span_m, C);
+      divide_cell<D>(a, C, c, i, n + rank, dm, dd, a.ts + span_d, a.ts + span_m, K.nslot, rank);
+      daughter = true;
+    }
+    if (C.apop_p > 0.0) {
+      if (live) {
+        const int g = C.cell_base + i;
+        const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngApo, 0u,
+                                      a.seed_lo, a.seed_hi);
+        if (uniform53(r.v[0], r.v[1]) <= C.apop_p) {
+          const int idx = atomicAdd(&a.cnt[c].ndead, 1);
+          if (idx < kDeadCap) a.dead[c * kDeadCap + idx] = i;
+        }
+      }
+      if (daughter) {
+        const int gk = C.cell_base + n + rank;
+        const u32x4 r = philox4x32_10(static_cast<uint32_t>(gk), static_cast<uint32_t>(a.ts), kRngApo, 0u,
+                                      a.seed_lo, a.seed_hi);
+        if (uniform53(r.v[0], r.v[1]) <= C.apop_p) {
+          const int idx = atomicAdd(&a.cnt[c].ndead, 1);
+          if (idx < kDeadCap) a.dead[c * kDeadCap + idx] = n + rank;
+        }
+      }
+    }
+  }
+}
+
+__device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int src, int D) {
+  const int gd = C.cell_base + dst, gs = C.cell_base + src;
+  a.t0[gd] = a.t0[gs];
+  a.tsw[gd] = a.tsw[gs];
+  for (int j = 0; j < 2; ++j) {
+    const int sl = a.slot_of[2 * gs + j];
+    a.eid[sl] = 2 * gd + j;
+    a.slot_of[2 * gd + j] = sl;
+  }
+  if (a.obs_disp) {
+    for (int d = 0; d < D; ++d) {
+      a.obs_com_prev[d * a.CC + gd] = a.obs_com_prev[d * a.CC + gs];
+      a.obs_disp[d * a.CC + gd] = a.obs_disp[d * a.CC + gs];
+      a.obs_vref[d * a.CC + gd] = a.obs_vref[d * a.CC + gs];
+    }
+  }
+}
+
+// one block per colony: commit the divisions, then swap-with-last removal of the dead
+__global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
+  __shared__ int sd[kDeadCap];
+  __shared__ int s_n1, s_k;
+  const int c = blockIdx.x;
+  const ColonyConst &C = a.col[c];
+  ColonyCounters &K = a.cnt[c];
+  if (threadIdx.x == 0) {
+    const int add = K.ndiv_allowed;
+    K.ncell += add;
+    K.nslot += 2 * add;
+    K.ndiv_total += add;
+    int k = K.ndead;
+    if (k > kDeadCap) {
+      K.err |= kErrCap;
+      k = kDeadCap;
+    }
+    s_n1 = K.ncell;
+    s_k = k;
+  }
+  __syncthreads();
+  const int k = s_k, n1 = s_n1;
+  if (k == 0) return;
+  int P = 1;
+  while (P < k) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sd[i] = i < k ? a.dead[c * kDeadCap + i] : 0x7fffffff;
+  __syncthreads();
+  // bitonic sort (ascending) of the dead list
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int l = i ^ stride;
+        if (l > i) {
+          const bool up = (i & size) == 0;
+          const int x = sd[i], y = sd[l];
+          if ((x > y) == up) {
+            sd[i] = y;
+            sd[l] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  // tombstones
+  for (int r = threadIdx.x; r < k; r += blockDim.x) {
+    const int g = C.cell_base + sd[r];
+    a.eid[a.slot_of[2 * g]] = -1;
+    a.eid[a.slot_of[2 * g + 1]] = -1;
+  }
+  __syncthreads();
+  const int n2 = n1 - k;
+  // movers: live cells of [n2, n1) in ascending order, paired with holes sd[0..h)
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int base = n2; base < n1; base += blockDim.x) {
+    const int q = base + threadIdx.x;
+    bool live = false;
+    if (q < n1) {
+      int lo = 0, hi = k - 1;
+      bool found = false;
+      while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (sd[mid] == q) {
+          found = true;
+          break;
+        }
+        if (sd[mid] < q)
+          lo = mid + 1;
+        else
+          hi = mid - 1;
+      }
+      live = !found;
+    }
+    // rank among live tail cells (block-wide, 1024 threads: serial over warps)
+    const unsigned m = __ballot_sync(0xffffffffu, live);
+    __shared__ int wcount[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) wcount[wid] = __popc(m);
+    __syncthreads();
+    int before = s_carry;
+    for (int w = 0; w < wid; ++w) before += wcount[w];
+    const int rank = before + __popc(m & ((1u << lane) - 1u));
+    if (live) move_cell(a, C, sd[rank], q, D);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += wcount[w];
+      s_carry += tot;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    K.ncell = n2;
+    K.napo_total += k;
+  }
+}
+
+// oracle mode: divisions in the host's order with host-drawn axes and cycle lengths
+template <int D>
+__global__ void k_div_list(EventArgs a, int c, int n0, int ndiv, const int *mothers, const double *dirs,
+                           const int *tsws) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ndiv) return;
+  const ColonyConst &C = a.col[c];
+  divide_cell<D>(a, C, c, mothers[r], n0 + r, dirs + (2 * r) * D, dirs + (2 * r + 1) * D, tsws[2 * r],
+                 tsws[2 * r + 1], a.cnt[c].nslot, r);
+}
+
+// oracle mode: commit divisions, then the sequential removals removeCell(i) in order
+__global__ void k_apo_ops(EventArgs a, int c, int ndiv, int nops, const int *ops, int D) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const ColonyConst &C = a.col[c];
+  ColonyCounters &K = a.cnt[c];
+  K.ncell += ndiv;
+  K.nslot += 2 * ndiv;
+  K.ndiv_total += ndiv;
+  for (int q = 0; q < nops; ++q) {
+    const int i = ops[q];
+    const int last = K.ncell - 1;
+    if (i < 0 || i > last) {
+      K.err |= kErrCap;
+      return;
+    }
+    const int g = C.cell_base + i;
+    a.eid[a.slot_of[2 * g]] = -1;
+    a.eid[a.slot_of[2 * g + 1]] = -1;
+    if (i != last) move_cell(a, C, i, last, D);
+    K.ncell -= 1;
+    K.napo_total += 1;
+  }
+}
+
+template <int D>
+__global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, const double *pos,
+                         const double *sigma, double *x, double *sig, int *eid, int *slot_of,
+                         ColonyCounters *cnt) {
+  const ColonyConst &C = col[c];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < 2 * ncells) {
+    const int slot = C.slot_base + e;
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[d * SS + slot] = pos[static_cast<size_t>(e) * D + d];
+    sig[slot] = sigma[e];
+    eid[slot] = 2 * C.cell_base + e;
+    slot_of[2 * C.cell_base + e] = slot;
+  }
+  if (e == 0) {
+    cnt[c].ncell = ncells;
+    cnt[c].nslot = 2 * ncells;
+    cnt[c].nlive = 0;
+    cnt[c].err = 0;
+    cnt[c].ndead = 0;
+    cnt[c].ndiv_step = 0;
+    cnt[c].ndiv_allowed = 0;
+  }
+}
+
+__global__ void k_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,
+                                   const double *src, int width, double *dst) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 2 * ncells) return;
+  const int slot = slot_of[2 * cell_base + e];
+  for (int d = 0; d < width; ++d) dst[static_cast<size_t>(e) * width + d] = src[d * SS + slot];
+  (void)dim;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, int reset, double *partials) {
+  const ColonyConst &C = a.col[c];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double area = 0.0, msd = 0.0, vv = 0.0, v0 = 0.0;
+  if (i < ncells) {
+    const int g = C.cell_base + i;
+    const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+    double com[D], v[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double r0 = a.x[d * a.SS + s0], r1 = a.x[d * a.SS + s1];
+      double rel = r1 - r0;
+      if (C.periodic[d]) rel -= static_cast<double>(nint(rel / C.box[d])) * C.box[d];
+      const double m = (0.0 + rel) / 2.0;  // calculComs, Colony.cpp:409-432
+      com[d] = C.periodic[d] ? fmod(m + r0 + C.box[d], C.box[d]) : m + r0;
+      v[d] = a.vel ? 0.5 * (a.vel[d * a.SS + s0] + a.vel[d * a.SS + s1]) : 0.0;
+    }
+    const double q0 = a.sig[s0] * 0.5, q1 = a.sig[s1] * 0.5;
+    area = 3.14159265358979323846 * q0 * q0 + 3.14159265358979323846 * q1 * q1;
+    if (reset) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        a.obs_com_prev[d * a.CC + g] = com[d];
+        a.obs_disp[d * a.CC + g] = 0.0;
+        a.obs_vref[d * a.CC + g] = v[d];
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        double dr = com[d] - a.obs_com_prev[d * a.CC + g];
+        if (C.periodic[d]) dr -= static_cast<double>(nint(dr / C.box[d])) * C.box[d];
+        const double acc = a.obs_disp[d * a.CC + g] + dr;
+        a.obs_disp[d * a.CC + g] = acc;
+        a.obs_com_prev[d * a.CC + g] = com[d];
+        msd += acc * acc;
+        const double vr = a.obs_vref[d * a.CC + g];
+        vv += v[d] * vr;
+        v0 += vr * vr;
+      }
+    }
+  }
+  // deterministic block reduction
+  __shared__ double red[4][kTile];
+  red[0][threadIdx.x] = area;
+  red[1][threadIdx.x] = msd;
+  red[2][threadIdx.x] = vv;
+  red[3][threadIdx.x] = v0;
+  __syncthreads();
+  for (int s = kTile / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 4; ++q) partials[blockIdx.x * 4 + q] = red[q][0];
+}
+
+}  // namespace
+
+void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
+  k_div_count<<<grid_cells, kTile, 0, s>>>(a);
+  k_div_scan<<<a.B, kTile, 0, s>>>(a);
+  if (dim == 2)
+    k_div_apply<2><<<grid_cells, kTile, 0, s>>>(a);
+  else
+    k_div_apply<3><<<grid_cells, kTile, 0, s>>>(a);
+  k_apo_apply<<<a.B, 1024, 0, s>>>(a, dim);
+}
+
+void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,
+                           const double *dirs, const int *spans, int dim, cudaStream_t s) {
+  if (ndiv <= 0) return;
+  const int blocks = (ndiv + 127) / 128;
+  if (dim == 2)
+    k_div_list<2><<<blocks, 128, 0, s>>>(a, colony, n0, ndiv, mothers, dirs, spans);
+  else
+    k_div_list<3><<<blocks, 128, 0, s>>>(a, colony, n0, ndiv, mothers, dirs, spans);
+}
+
+void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops, const int *ops, int dim,
+                             cudaStream_t s) {
+  k_apo_ops<<<1, 32, 0, s>>>(a, colony, ndiv, nops, ops, dim);
+}
+
+void launch_upload_scatter(const ColonyConst *col, int colony, int ncells, int dim, size_t SS,
+                           const double *pos, const double *sigma, double *x, double *sig,
+                           int *eid, int *slot_of, ColonyCounters *cnt, cudaStream_t s) {
+  const int n = 2 * ncells > 0 ? 2 * ncells : 1;
+  const int blocks = (n + kTile - 1) / kTile;
+  if (dim == 2)
+    k_upload<2><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, sigma, x, sig, eid, slot_of, cnt);
+  else
+    k_upload<3><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, sigma, x, sig, eid, slot_of, cnt);
+}
+
+void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,
+                             const double *src, int width, double *dst, cudaStream_t s) {
+  if (ncells <= 0) return;
+  const int blocks = (2 * ncells + kTile - 1) / kTile;
+  k_gather_canonical<<<blocks, kTile, 0, s>>>(ncells, dim, SS, cell_base, slot_of, src, width, dst);
+}
+
+void launch_observables(const EventArgs &a, int colony, int ncells, int dim, int reset,
+                        double *partials, int nblocks, cudaStream_t s) {
+  if (dim == 2)
+    k_obs<2><<<nblocks, kTile, 0, s>>>(a, colony, ncells, reset, partials);
+  else
+    k_obs<3><<<nblocks, kTile, 0, s>>>(a, colony, ncells, reset, partials);
+}
+
+}  // namespace cil

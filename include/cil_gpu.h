@@ -1,0 +1,183 @@
+/* cil_gpu.h — C ABI of the GB300 (sm_103a) cell-colony step library, libcilgpu.so.
+ *
+ * Drop-in boundary for the reference's step loop (KokoroSinx/cil_cuda). The reference
+ * plugs its integrator in through `typedef void(*MDIntegrator)(int& ts); extern
+ * MDIntegrator mdStep;` (MD.cuh:450-452), chosen in readMD (Input.cpp:524-546) and called
+ * GTS times per frame (CIL.cu:1106). A host wrapper `gpuEuler(int& ts)` registered there
+ * calls cil_step(); frames cross to the host through cil_download() only. Host arrays keep
+ * the reference CellColony layout (pos/vel/frc[cell][elem][dim], sigmaCore[cell][elem],
+ * cellT0/cellTSwitch[cell]; Colony.hpp:88-123, Colony.cpp:193-313).
+ *
+ * Plain C types only: no exceptions, no C++ or torch types cross this boundary. One host
+ * thread per handle; one CUDA stream per handle; handles are independent.
+ */
+#ifndef CIL_GPU_H
+#define CIL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference reports failures through run_assert -> std::runtime_error
+ * -> exit(1) (Utils.hpp:99-109, CIL.cuh:365-381); a host wrapper maps any non-OK status
+ * to run_assert(false, cil_last_error(...)). */
+typedef enum cil_status {
+  CIL_OK = 0,
+  CIL_ERR_CONFIG = 1,     /* invalid parameters or call order */
+  CIL_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+  CIL_ERR_CAPACITY = 3,   /* more cells than the reserved capacity (division) or host arrays too small */
+  CIL_ERR_NAN = 4,        /* non-finite force or position */
+  CIL_ERR_OUT_OF_BOX = 5, /* an element left the box along a non-periodic axis (checkPositions, CIL.cu:945-966) */
+  CIL_ERR_TIMEOUT = 6,    /* a bounded device wait gave up */
+  CIL_ERR_STATE = 7       /* handle not ready (e.g. step before upload) */
+} cil_status;
+
+/* Pair-force laws (the reference's PairForceParams family, MD.cuh:23-344, with the
+ * BASELINE forms). Force on element i from j is f0(r) * (r_j - r_i). */
+enum {
+  CIL_FORCE_LJ_WCA = 0,   /* LJParams (MD.cuh:47-129): eps_ij = 24 eps, rc^2 = rcut_scale^2 sigma_ij^2 */
+  CIL_FORCE_SOFTCORE = 1, /* F = eps (1 - r/rc)^2, rc = rcut_scale sigma_ij */
+  CIL_FORCE_HERTZ = 2     /* F = E delta^1.5, delta = sigma_ij - r */
+};
+
+/* Arithmetic of the pair forces. */
+enum {
+  CIL_PREC_FP64 = 0, /* everything in FP64 */
+  CIL_PREC_MIXED = 1 /* FP32 pair forces from bin-origin-relative displacements; FP64 positions,
+                        wrap, integration and daughter placement */
+};
+
+/* Random streams. */
+enum {
+  CIL_RNG_PHILOX = 0, /* device Philox4x32-10 keyed by (seed, step, element/cell, purpose) */
+  CIL_RNG_DSFMT = 1   /* oracle mode: host dSFMT-19937 stream in the reference's draw order
+                         (Random.hpp, CIL.cu:369-455, 627-649, 793-818), uploaded each step */
+};
+
+/* Per-colony model parameters (one species of 2-element cells). Times in simulation units. */
+typedef struct cil_colony_params {
+  int32_t dim;            /* 2 or 3; must equal cil_config.dim */
+  int32_t force_law;      /* CIL_FORCE_*; must equal cil_config.force_law */
+  int32_t noise_per_cell; /* 0: independent noise per element component; 1: per cell (reference) */
+  int32_t divide;         /* 1: linear growth of the rest length and division */
+  double box[3];          /* box lengths */
+  int32_t periodic[3];    /* 1 = periodic axis */
+  int32_t nwalls;         /* 0..2 one-sided flat Hertz walls normal to the last axis */
+  int32_t wall_dir[2];    /* +1 keeps elements at larger coordinates, -1 at smaller */
+  double wall_pos[2];
+  double wall_E;
+  double epsilon;         /* LJ eps / soft-core eps / Hertz E */
+  double rcut_scale;      /* cutoff / sigma_ij (WCA: 2^(1/6), soft-core and Hertz: 1) */
+  double zeta[2];         /* friction of back/front element; mobility 1/zeta */
+  double motility[2];     /* back element -m0 n, front +m1 n, n = back->front unit axis */
+  double kappa;           /* linear intra-cell spring constant */
+  double rest0;           /* spring rest length at birth */
+  double rest1;           /* spring rest length at division */
+  double noise_D;         /* passive diffusion constant (noise sqrt(2D/dt) zeta per component) */
+  double dt;
+  double div_tau_mu;      /* division time ~ N(mu, sigma) */
+  double div_tau_sigma;
+  double apop_rate;       /* apoptosis rate per unit time */
+} cil_colony_params;
+
+typedef struct cil_config {
+  int32_t dim;
+  int32_t force_law;
+  int32_t precision;      /* CIL_PREC_* */
+  int32_t rng_mode;       /* CIL_RNG_* */
+  uint64_t seed;          /* dSFMT seed (low 32 bits, Random::init) or Philox key */
+  int32_t num_colonies;
+  int32_t device;         /* CUDA device ordinal */
+  double bin_width;       /* 0: cutoff of the largest element (+ skin); else at least this */
+  double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
+  int32_t block_size;     /* threads per block of the pair kernel (0 = default) */
+  int32_t flags;          /* reserved, 0 */
+} cil_config;
+
+/* Host view of one colony in the reference layout. */
+typedef struct cil_colony_view {
+  int32_t ncells;   /* upload: cells in the arrays; download: cells on the device */
+  int32_t capacity; /* download: cells the host arrays can hold */
+  int32_t ts;       /* time step of the state */
+  int32_t pad;
+  double *pos;      /* [cell][2][dim] */
+  double *sigma;    /* [cell][2] element diameters (sigmaCore) */
+  double *vel;      /* [cell][2][dim], download only, may be NULL */
+  int32_t *t0;      /* [cell] birth step (cellT0) */
+  int32_t *tswitch; /* [cell] division step (cellTSwitch) */
+} cil_colony_view;
+
+/* Observables reduced on the device (per colony). */
+typedef struct cil_obs {
+  int32_t ncells;
+  int32_t pad;
+  double mean_area;   /* mean over cells of sum_j pi (sigma_j/2)^2 */
+  double msd;         /* mean squared unwrapped centre-of-mass displacement since cil_obs_reset */
+  double vacf;        /* <v_c(t).v_c(0)> / <|v_c(0)|^2> of the cell velocity */
+  int64_t ndiv_total; /* divisions since creation */
+  int64_t napo_total; /* apoptoses since creation */
+} cil_obs;
+
+typedef struct cil_handle cil_handle;
+
+/* Creates a handle for num_colonies colonies. params[c] and cap_cells[c] per colony.
+ * Replaces the reference's initialize() step-loop setup (CIL.cuh:332-393) for the GPU. */
+cil_status cil_create(const cil_config *cfg, const cil_colony_params *params,
+                      const int32_t *cap_cells, cil_handle **out);
+void cil_destroy(cil_handle *h);
+
+/* Copies one colony to the device (all colonies must be uploaded before cil_step).
+ * Replaces the host-resident colony state used by Euler (CIL.cu:1013-1020). */
+cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *view);
+
+/* Copies one colony to the host at a frame boundary (outputFrame, OutputWriter.cpp:708).
+ * CIL_ERR_CAPACITY if view->capacity is too small (view->ncells is set to the need). */
+cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *view);
+
+/* Advances every colony by nsteps Euler steps (MDIntegrator mdStep, MD.cuh:450-458;
+ * Euler CIL.cu:1013-1020). *ts (may be NULL) receives the step counter afterwards. */
+cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts);
+
+/* Computes the forces of the current state without integrating (calculForcesPressure,
+ * CIL.cu:999-1007), drawing the noise exactly as a step would, and copies them to frc
+ * [cell][2][dim]. For parity checks and frame output. */
+cil_status cil_forces(cil_handle *h, int32_t colony, double *frc);
+
+/* Bin structure of the current positions (LinkList::populate, Container.cpp:58-79;
+ * Utils.hpp:872-1001) for parity checks: ns[3] bins per axis, bin_start[nbins+1] offsets
+ * into elems[2*ncells] (element ids 2*cell+elem, ascending within a bin). Returns
+ * CIL_ERR_CAPACITY if max_bins is too small. */
+cil_status cil_bins(cil_handle *h, int32_t colony, int32_t *ns, int32_t *bin_start,
+                    int32_t *elems, int32_t max_bins);
+
+/* Observables (offline analysis in the reference: cilJintaoTools.py:97-125,
+ * simulationtools.py:602-607). cil_obs_reset sets the MSD/VACF origin. */
+cil_status cil_obs_reset(cil_handle *h, int32_t colony);
+cil_status cil_observables(cil_handle *h, int32_t colony, cil_obs *out);
+
+/* Device time of the last cil_step, milliseconds, measured with CUDA events on the
+ * handle's stream: per phase summed over its steps (rebuild, forces, events), the whole
+ * call from the first launch to the last (total, including any idle gaps), and the number
+ * of kernels it launched. Any pointer may be NULL. */
+cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, double *events_ms,
+                       double *total_ms, int64_t *launches);
+
+/* The oracle-mode host random stream on its own (no device needed): n draws of `kind`
+ * from a fresh stream seeded with `seed` through the reference's Random:: functions
+ * (Random.hpp:9-118): 0 dsfmt close_open, 1 open_open, 2 uniform, 3 normal (Leva),
+ * 4 onDSphere in 2D (2 values per draw), 5 onDSphere in 3D (3 values per draw). */
+cil_status cil_host_rng_draw(uint32_t seed, int32_t kind, int64_t n, double *out);
+
+/* Last error message of the handle (empty if none). */
+void cil_last_error(const cil_handle *h, char *buf, size_t len);
+
+/* Library version string. */
+const char *cil_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CIL_GPU_H */

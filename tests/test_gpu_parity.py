@@ -1,0 +1,247 @@
+"""CUDA path against the oracle, through the C ABI.
+
+Tolerances (FP64, oracle mode = the reference's dSFMT stream uploaded):
+* bin contents: identical sets per bin (bit-exact integer work)
+* per-step forces: max_i |F_gpu - F_oracle| <= 1e-12 * max_i |F_oracle| (norm-wise; the
+  two sides sum the same pair forces in different orders)
+* 100-step trajectories: max |x_gpu - x_oracle| (minimum image) <= 1e-9
+* division / apoptosis: identical cell counts, birth steps and division steps
+* mixed precision forces: norm-wise relative error <= 2e-5 against the FP64 oracle
+"""
+import numpy as np
+import pytest
+
+from cil_cuda_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-12
+TRAJ_TOL = 1e-9
+MIXED_TOL = 2e-5
+
+
+def minimage(a, b, p):
+    d = np.asarray(a) - np.asarray(b)
+    for k in range(p["dim"]):
+        if p["periodic"][k]:
+            L = p["box"][k]
+            d[..., k] -= np.round(d[..., k] / L) * L
+    return d
+
+
+def engine(G, p, cap, **kw):
+    return G.Engine([p], [cap], **kw)
+
+
+@pytest.fixture(scope="module")
+def lj(gpu_lib):
+    p, st = S.config1(1024, seed=7)
+    st = S.relax(p, st, steps=3000)
+    return p, st
+
+
+@pytest.fixture(scope="module")
+def growth(gpu_lib):
+    p = S.growth_params(box=120.0)
+    st = S.disk_colony(2500, p, seed=11)
+    return p, st
+
+
+@pytest.fixture(scope="module")
+def channel(gpu_lib):
+    p = S.channel_params(lxy=40.0, height=10.0)
+    st = S.channel_colony(1500, p, seed=5)
+    return p, st
+
+
+def bins_gpu(G, p, st, width):
+    eng = engine(G, p, len(st["sigma"]), bin_width=width)
+    eng.upload(0, **st)
+    ns, start, elems = eng.bins(0)
+    eng.close()
+    return ns, start, elems
+
+
+@pytest.mark.parametrize("width", [1.8, 2.6, 5.0])
+def test_bin_contents_match_oracle_2d(gpu_lib, oracle_lib, lj, width):
+    p, st = lj
+    ns, start, elems = bins_gpu(gpu_lib, p, st, width)
+    o = oracle_lib.Oracle(p, len(st["sigma"]), 1)
+    o.set_state(**st)
+    ons, head, lst = o.bin_elements(width)
+    assert list(ns) == list(ons)
+    ref = oracle_lib.bins_as_sets(head, lst)
+    assert len(start) == len(ref) + 1
+    for b, s in enumerate(ref):
+        got = elems[start[b]:start[b + 1]]
+        assert set(got.tolist()) == s
+        assert np.all(np.diff(got) > 0)  # ascending element ids within a bin
+
+
+def test_bin_contents_match_oracle_3d_walls(gpu_lib, oracle_lib, channel):
+    p, st = channel
+    ns, start, elems = bins_gpu(gpu_lib, p, st, 1.3)
+    o = oracle_lib.Oracle(p, len(st["sigma"]), 1)
+    o.set_state(**st)
+    ons, head, lst = o.bin_elements(1.3)
+    assert list(ns) == list(ons)
+    for b, s in enumerate(oracle_lib.bins_as_sets(head, lst)):
+        assert set(elems[start[b]:start[b + 1]].tolist()) == s
+
+
+def test_single_bin_collapse(gpu_lib, oracle_lib):
+    p, st = S.config1(12, seed=1, phi=0.3)
+    ns, start, elems = bins_gpu(gpu_lib, p, st, 4.0)
+    assert list(ns[:2]) == [1, 1] and len(start) == 2
+    assert sorted(elems.tolist()) == list(range(24))
+
+
+def forces_pair(G, O, p, st, seed=42, **kw):
+    n = len(st["sigma"])
+    eng = engine(G, p, n, rng=G.RNG_DSFMT, seed=seed, **kw)
+    eng.upload(0, **st)
+    fg = eng.forces(0)
+    eng.close()
+    o = O.Oracle(p, n, seed)
+    o.set_state(**st)
+    fo = o.compute_forces()
+    return fg, fo
+
+
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "lj_cellnoise"])
+def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, case):
+    p, st = {"lj": lj, "growth": growth, "channel": channel, "lj_cellnoise": lj}[case]
+    if case == "lj_cellnoise":
+        p = dict(p, noise_per_cell=1)
+    fg, fo = forces_pair(gpu_lib, oracle_lib, p, st)
+    assert np.isfinite(fo).all()
+    scale = np.abs(fo).max()
+    err = np.abs(fg - fo).max()
+    assert err <= FORCE_TOL * scale, (err, scale)
+
+
+def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth):
+    for p, st in (lj, growth):
+        p = dict(p, noise_D=0.0)
+        fg, fo = forces_pair(gpu_lib, oracle_lib, p, st, precision=gpu_lib.PREC_MIXED)
+        err = np.abs(fg - fo).max() / np.abs(fo).max()
+        assert err <= MIXED_TOL, err
+
+
+def run_pair(G, O, p, st, nsteps, seed=3, cap=None, **kw):
+    n = len(st["sigma"])
+    cap = cap or n
+    eng = engine(G, p, cap, rng=G.RNG_DSFMT, seed=seed, **kw)
+    eng.upload(0, **st)
+    eng.step(nsteps)
+    g = eng.download(0)
+    eng.close()
+    o = O.Oracle(p, cap, seed)
+    o.set_state(**st)
+    rc = o.step(nsteps)
+    return g, o.state(), rc, o
+
+
+def test_trajectory_100_steps(gpu_lib, oracle_lib, lj):
+    p, st = lj
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100)
+    assert rc == 0
+    assert g["ncells"] == len(s["sigma"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+    verr = np.abs(g["vel"] - s["vel"]).max() / np.abs(s["vel"]).max()
+    assert verr <= 1e-9
+
+
+def test_trajectory_100_steps_3d_channel(gpu_lib, oracle_lib, channel):
+    p, st = channel
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100)
+    assert rc == 0
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
+def test_division_and_apoptosis_events_exact(gpu_lib, oracle_lib):
+    p = S.growth_params(box=80.0, dt=1e-3, div_tau_mu=0.05, div_tau_sigma=0.01, apop_rate=1.0)
+    st = S.disk_colony(400, p, seed=2)
+    g, s, rc, o = run_pair(gpu_lib, oracle_lib, p, st, 120, seed=17, cap=4000)
+    assert rc == 0
+    ev = o.events()
+    assert (ev[:, 1] == 0).sum() > 100 and (ev[:, 1] == 1).sum() > 5  # both kinds happened
+    assert g["ncells"] == len(s["sigma"])
+    np.testing.assert_array_equal(g["t0"], s["t0"])
+    np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    np.testing.assert_array_equal(g["sigma"], s["sigma"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
+def test_philox_mode_deterministic_and_growing(gpu_lib):
+    p = S.growth_params(box=150.0, dt=1e-3, div_tau_mu=0.1, div_tau_sigma=0.01, apop_rate=0.5)
+    st = S.disk_colony(1500, p, seed=4)
+    outs = []
+    for _ in range(2):
+        eng = engine(gpu_lib, p, 20000, seed=123)
+        eng.upload(0, **st)
+        eng.step(150)
+        outs.append(eng.download(0))
+        ob = eng.observables(0)
+        eng.close()
+    a, b = outs
+    assert a["ncells"] == b["ncells"] > 1500
+    np.testing.assert_array_equal(a["pos"], b["pos"])
+    np.testing.assert_array_equal(a["tswitch"], b["tswitch"])
+    assert ob["ndiv_total"] > 0 and ob["ncells"] == a["ncells"]
+
+
+def test_batched_colonies_equal_single(gpu_lib):
+    """Colonies of uneven size stepped in one handle give the same states as separate
+    handles (no noise, no events: a deterministic force field)."""
+    ps, sts = [], []
+    for i, n in enumerate((300, 1200, 700)):
+        p = S.growth_params(box=0.0, noise_D=0.0, divide=0, apop_rate=0.0)
+        p, st = S.square_colony(n, p, seed=i)
+        ps.append(p)
+        sts.append(st)
+    eng = gpu_lib.Engine(ps, [len(s["sigma"]) for s in sts])
+    for c, st in enumerate(sts):
+        eng.upload(c, **st)
+    eng.step(20)
+    batched = [eng.download(c) for c in range(3)]
+    eng.close()
+    for c in range(3):
+        e1 = engine(gpu_lib, ps[c], len(sts[c]["sigma"]))
+        e1.upload(0, **sts[c])
+        e1.step(20)
+        single = e1.download(0)
+        e1.close()
+        np.testing.assert_array_equal(batched[c]["pos"], single["pos"])
+
+
+def test_error_nan(gpu_lib):
+    p = S.base_params(2, gpu_lib.FORCE_LJ_WCA, [10.0, 10.0], noise_D=0.0)
+    pos = np.array([[[5.0, 5.0], [5.5, 5.0]], [[5.0, 5.0], [4.5, 5.0]]])  # coincident back elements
+    eng = engine(gpu_lib, p, 2)
+    eng.upload(0, pos, np.ones((2, 2)), np.zeros(2, np.int32), np.full(2, S.NEVER, np.int32))
+    with pytest.raises(gpu_lib.CilError) as e:
+        eng.step(1)
+    assert e.value.status == 4
+    eng.close()
+
+
+def test_error_capacity_and_box(gpu_lib):
+    p = S.growth_params(box=30.0, dt=1e-3)
+    st = S.disk_colony(50, p, seed=1)
+    st["tswitch"][:] = 1  # everyone divides at the first step
+    eng = engine(gpu_lib, p, 60)
+    eng.upload(0, **st)
+    with pytest.raises(gpu_lib.CilError) as e:
+        eng.step(1)
+    assert e.value.status == 3
+    bad = dict(st)
+    bad["pos"] = st["pos"].copy()
+    bad["pos"][0, 0, 0] = 31.0
+    with pytest.raises(gpu_lib.CilError) as e:
+        eng.upload(0, **bad)
+    assert e.value.status == 5
+    eng.close()
