@@ -261,6 +261,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--only", choices=["mixed", "plain"], default=None,
+                    help="run one form only (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -276,10 +278,19 @@ def main():
     p, st = workload(seed=1 + rank)
     hbm, peak_kind = peaks()
 
-    plain = run_form(G, p, st, G.PREC_FP64, max(1, args.steps // 10), args.warmup, device, 7 + rank, dist)
+    plain_steps = max(1, args.steps // 10)
+    if args.only == "mixed":
+        plain = None
+    else:
+        plain = run_form(G, p, st, G.PREC_FP64, plain_steps, args.warmup, device, 7 + rank, dist)
+    if args.only == "plain":
+        print(json.dumps({"plain_fp64": plain["psteps"] / plain["dev_s"], "timings": plain["timings"]}))
+        return 0
     with Clocks(device) as clk:
         mixed = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist)
     clocks = clk.summary()
+    if plain is None:
+        plain = mixed
 
     t_max = allreduce_max(dist, mixed["dev_s"])
     ps_all = allreduce_sum(dist, mixed["psteps"])
@@ -294,7 +305,7 @@ def main():
     bytes_per_elem = 40  # pos in 16 + sigma 4 + id 4 + pos out 16 (2D, FP32-force form)
     achieved = bytes_per_elem * nelem / force_s / 1e9
     tp = plain["timings"]
-    plain_force_s = tp["force_ms"] * 1e-3 / max(1, args.steps // 10)
+    plain_force_s = tp["force_ms"] * 1e-3 / plain_steps
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -308,7 +319,7 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "forms": {"mixed": value, "plain_fp64": plain_value, "speedup_vs_plain_fp64": value / plain_value},
         "phases_ms_per_step": {k: tm[k] / args.steps for k in ("rebuild_ms", "force_ms", "events_ms")},
-        "plain_fp64_phases_ms_per_step": {k: tp[k] / max(1, args.steps // 10) for k in ("rebuild_ms", "force_ms", "events_ms")},
+        "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
                      "kernel": "k_force<2, softcore, mixed>", "algorithmic_bytes_per_element": bytes_per_elem,

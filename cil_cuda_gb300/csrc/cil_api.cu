@@ -321,6 +321,8 @@ EventArgs event_args(cil_handle *h) {
 // updateWienerProcess does (CIL.cu:793-818), in canonical [cell][elem][dim] order
 cil_status draw_oracle_noise(cil_handle *h, bool *any) {
   *any = false;
+  // the pinned buffer may still be the source of the previous step's copy
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   size_t total = 0;
   for (int c = 0; c < h->B; ++c) {
     const HostColony &hc = h->hc[c];

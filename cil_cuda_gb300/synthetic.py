@@ -171,23 +171,28 @@ def channel_colony(ncells, p, seed=1, phi=0.6, ts=0):
     return dict(pos=pos, sigma=sigma, t0=t0, tswitch=tsw)
 
 
-def relax(p, state, steps=2000, eps=20.0, dt=1e-3, seed=0, device=0):
-    """Removes inter-cell overlaps of a random start with a bounded soft-core repulsion run
-    on the GPU (no noise, no motility, no division), keeping every cell's rest length.
-    Returns a copy of the state with relaxed positions."""
+def relax(p, state, stages=9, steps=300, final=1000, E=1000.0, seed=0, device=0):
+    """Removes inter-cell overlaps of a random start: the diameters are inflated from 60 %
+    to 100 % in `stages` stages while a stiff Hertz repulsion (no noise, no motility, no
+    division) relaxes the packing, then `final` steps at full size. Runs on the GPU through
+    the library. Returns a copy of the state with relaxed positions."""
+    from . import FORCE_HERTZ as HZ
     from . import PREC_FP64, RNG_PHILOX, Engine
 
     q = dict(p)
-    q.update(force_law=FORCE_SOFTCORE, epsilon=eps, rcut_scale=1.0, noise_D=0.0, motility=[0.0, 0.0],
-             divide=0, apop_rate=0.0, dt=dt)
+    q.update(force_law=HZ, epsilon=E, rcut_scale=1.0, noise_D=0.0, motility=[0.0, 0.0], divide=0,
+             apop_rate=0.0, dt=min(1e-3, 0.3 / E), nwalls=0)
     n = len(state["sigma"])
     eng = Engine([q], [n], precision=PREC_FP64, rng=RNG_PHILOX, seed=seed, device=device)
+    pos = np.asarray(state["pos"], np.float64)
     try:
-        eng.upload(0, state["pos"], state["sigma"], np.zeros(n, np.int32), np.full(n, NEVER, np.int32))
-        eng.step(steps)
-        out = eng.download(0)
+        lams = list(np.linspace(0.6, 1.0, stages)) + [1.0]
+        for k, lam in enumerate(lams):
+            eng.upload(0, pos, np.asarray(state["sigma"]) * lam, np.zeros(n, np.int32), np.full(n, NEVER, np.int32))
+            eng.step(final if k == len(lams) - 1 else steps)
+            pos = eng.download(0)["pos"]
     finally:
         eng.close()
     s = dict(state)
-    s["pos"] = out["pos"]
+    s["pos"] = pos
     return s

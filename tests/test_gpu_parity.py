@@ -36,7 +36,7 @@ def engine(G, p, cap, **kw):
 @pytest.fixture(scope="module")
 def lj(gpu_lib):
     p, st = S.config1(1024, seed=7)
-    st = S.relax(p, st, steps=3000)
+    st = S.relax(p, st)
     return p, st
 
 
@@ -155,7 +155,7 @@ def test_trajectory_100_steps(gpu_lib, oracle_lib, lj):
 
 def test_trajectory_100_steps_3d_channel(gpu_lib, oracle_lib, channel):
     p, st = channel
-    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100)
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100, cap=2 * len(st["sigma"]))
     assert rc == 0
     err = np.abs(minimage(g["pos"], s["pos"], p)).max()
     assert err <= TRAJ_TOL, err
