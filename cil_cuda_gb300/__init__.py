@@ -24,7 +24,7 @@ STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPAC
 
 EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces",
             "cil_bins", "cil_obs_reset", "cil_observables", "cil_timings", "cil_last_error",
-            "cil_version", "cil_host_rng_draw"]
+            "cil_version", "cil_host_rng_draw", "cil_bin_elements_noalloc"]
 
 
 class CilError(RuntimeError):
@@ -137,6 +137,8 @@ def lib():
         L.cil_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_version.restype = C.c_char_p
         L.cil_version.argtypes = []
+        L.cil_bin_elements_noalloc.restype = i32
+        L.cil_bin_elements_noalloc.argtypes = [vp, i32, i32, dp, C.c_double, ip, vp, vp, i32, vp]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
