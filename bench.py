@@ -143,9 +143,9 @@ def barrier(dist):
         dist.barrier()
 
 
-def run_form(G, p, st, precision, steps, warmup, device, seed, dist):
+def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0):
     """Device-timed run of one form; returns particle-steps/s and the timing details."""
-    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device)
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin)
     eng.upload(0, **st)
     if warmup:
         eng.step(warmup)
@@ -156,20 +156,21 @@ def run_form(G, p, st, precision, steps, warmup, device, seed, dist):
     wall = time.perf_counter() - t0
     tm = eng.timings()
     n1 = eng.observables(0)["ncells"]
+    sk = eng.skin_stats(0) if skin > 0 else None
     eng.close()
     dev_s = tm["total_ms"] * 1e-3
     psteps = (n0 + n1) * steps  # 2 elements per cell, trapezoid over the (slow) growth
-    return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm)
+    return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm, skin=sk)
 
 
-def run_e2e(G, p, st, precision, steps, device, seed):
+def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0):
     """The same metric through the reference-facing calls with host buffers: upload the
     colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
     call, each returning its status through a device->host read of the counters), and a
     frame download every GTS steps (outputFrame's input)."""
     import cil_cuda_gb300 as GG
     n = len(st["sigma"])
-    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device)
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin)
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
     t0 = time.perf_counter()
@@ -261,7 +262,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
-    ap.add_argument("--only", choices=["mixed", "plain"], default=None,
+    ap.add_argument("--skin", type=float, default=0.3, help="Verlet skin of the skin form (sigma units)")
+    ap.add_argument("--only", choices=["mixed", "plain", "skin"], default=None,
                     help="run one form only (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -286,22 +288,31 @@ def main():
     if args.only == "plain":
         print(json.dumps({"plain_fp64": plain["psteps"] / plain["dev_s"], "timings": plain["timings"]}))
         return 0
-    with Clocks(device) as clk:
+    mixed = None
+    if args.only in (None, "mixed"):
         mixed = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist)
+    with Clocks(device) as clk:
+        skinf = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist,
+                         skin=args.skin) if args.only in (None, "skin") else None
     clocks = clk.summary()
+    if mixed is None:
+        mixed = skinf
+    if skinf is None:
+        skinf = mixed
     if plain is None:
         plain = mixed
 
-    t_max = allreduce_max(dist, mixed["dev_s"])
-    ps_all = allreduce_sum(dist, mixed["psteps"])
+    t_max = allreduce_max(dist, skinf["dev_s"])
+    ps_all = allreduce_sum(dist, skinf["psteps"])
     value = ps_all / t_max
+    mixed_value = allreduce_sum(dist, mixed["psteps"]) / allreduce_max(dist, mixed["dev_s"])
     t_plain = allreduce_max(dist, plain["dev_s"])
     plain_value = allreduce_sum(dist, plain["psteps"]) / t_plain
 
     # roofline of the dominant kernel (the fused pair-force + integrate kernel)
-    tm = mixed["timings"]
+    tm = skinf["timings"]
     force_s = tm["force_ms"] * 1e-3 / args.steps
-    nelem = mixed["n0"] + mixed["n1"]  # mean elements per step (2 * mean cells)
+    nelem = skinf["n0"] + skinf["n1"]  # mean elements per step (2 * mean cells)
     bytes_per_elem = 40  # pos in 16 + sigma 4 + id 4 + pos out 16 (2D, FP32-force form)
     achieved = bytes_per_elem * nelem / force_s / 1e9
     tp = plain["timings"]
@@ -313,22 +324,24 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-force/f64-position", "data": "synthetic",
         "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
                                "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
-                   "particles": mixed["n0"] * 2, "cells": mixed["n0"], "cells_end": mixed["n1"],
-                   "form": "mixed precision, Philox noise, rebuild every step",
+                   "particles": skinf["n0"] * 2, "cells": skinf["n0"], "cells_end": skinf["n1"],
+                   "form": f"mixed precision, Philox noise, Verlet skin {args.skin} sigma",
                    "l2": "working set ~230 MB per step > 126 MB L2, no flush",
                    "parallelism": f"replicas x{world}"},
-        "forms": {"mixed": value, "plain_fp64": plain_value, "speedup_vs_plain_fp64": value / plain_value},
+        "forms": {"mixed_skin": value, "mixed_rebuild_every_step": mixed_value, "plain_fp64": plain_value,
+                  "speedup_vs_plain_fp64": value / plain_value},
+        "skin_stats": skinf["skin"],
         "phases_ms_per_step": {k: tm[k] / args.steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "k_force<2, softcore, mixed>", "algorithmic_bytes_per_element": bytes_per_elem,
+                     "kernel": "k_force_list<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
                      "plain_fp64_kernel_GBps": 44 * nelem / plain_force_s / 1e9},
         "gpu_launches": tm["launches"],
         "clocks": clocks,
     }
     if not args.no_e2e:
-        e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank)
+        e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, args.skin)
         line["e2e"] = {"value": allreduce_sum(dist, e2e["value"]), "unit": UNIT,
                        "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]}
     if rank == 0 and not args.no_cpu:

@@ -18,13 +18,17 @@ LIB_PATH = os.path.join(HERE, "_build", "libcilgpu.so")
 FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 RNG_PHILOX, RNG_DSFMT = 0, 1
+FLAG_NO_GRAPH = 1
 
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
           5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE"}
 
 EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces",
             "cil_bins", "cil_obs_reset", "cil_observables", "cil_timings", "cil_last_error",
-            "cil_version", "cil_host_rng_draw", "cil_bin_elements_noalloc"]
+            "cil_version", "cil_host_rng_draw", "cil_bin_elements_noalloc", "cil_skin_stats",
+            "cil_set_skin", "cil_set_scheduler", "cil_sched_state", "cil_mlp_num_params",
+            "cil_mlp_workspace_floats", "cil_mlp_forward", "cil_mlp_grad", "cil_mlp_adam",
+            "cil_graph_info"]
 
 
 class CilError(RuntimeError):
@@ -102,6 +106,30 @@ class Obs(C.Structure):
     ]
 
 
+class SkinInfo(C.Structure):
+    _fields_ = [
+        ("skin", C.c_double),
+        ("interval", C.c_int32),
+        ("nrebuild", C.c_int32),
+        ("ntrip", C.c_int32),
+        ("last_interval", C.c_int32),
+        ("nfresh", C.c_int32),
+        ("list_overflow", C.c_int32),
+        ("npairs", C.c_int64),
+        ("max_disp", C.c_double),
+    ]
+
+
+class SchedInfo(C.Structure):
+    _fields_ = [
+        ("features", C.c_float * 12),
+        ("div_rate", C.c_float),
+        ("apo_rate", C.c_float),
+        ("trip_share", C.c_float),
+        ("nsched", C.c_int32),
+    ]
+
+
 _lib = None
 
 
@@ -139,6 +167,26 @@ def lib():
         L.cil_version.argtypes = []
         L.cil_bin_elements_noalloc.restype = i32
         L.cil_bin_elements_noalloc.argtypes = [vp, i32, i32, dp, C.c_double, ip, vp, vp, i32, vp]
+        L.cil_skin_stats.restype = i32
+        L.cil_skin_stats.argtypes = [vp, i32, C.POINTER(SkinInfo)]
+        L.cil_set_skin.restype = i32
+        L.cil_set_skin.argtypes = [vp, i32, C.c_double, i32]
+        L.cil_graph_info.restype = i32
+        L.cil_graph_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.cil_set_scheduler.restype = i32
+        L.cil_set_scheduler.argtypes = [vp, C.POINTER(C.c_float), C.c_double, C.c_double, i32]
+        L.cil_sched_state.restype = i32
+        L.cil_sched_state.argtypes = [vp, i32, C.POINTER(SchedInfo)]
+        L.cil_mlp_num_params.restype = i32
+        L.cil_mlp_num_params.argtypes = []
+        L.cil_mlp_workspace_floats.restype = C.c_int64
+        L.cil_mlp_workspace_floats.argtypes = [i32]
+        L.cil_mlp_forward.restype = i32
+        L.cil_mlp_forward.argtypes = [vp, vp, i32, vp]
+        L.cil_mlp_grad.restype = i32
+        L.cil_mlp_grad.argtypes = [vp, vp, vp, vp, i32, vp, vp, vp]
+        L.cil_mlp_adam.restype = i32
+        L.cil_mlp_adam.argtypes = [vp, vp, vp, vp, i32, C.c_float]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
@@ -169,14 +217,15 @@ class Engine:
     """One handle: B colonies stepped together on one GPU."""
 
     def __init__(self, params: list, caps: list, *, precision: int = PREC_FP64, rng: int = RNG_PHILOX,
-                 seed: int = 0, device: int = 0, bin_width: float = 0.0, skin: float = 0.0):
+                 seed: int = 0, device: int = 0, bin_width: float = 0.0, skin: float = 0.0,
+                 graphs: bool = True):
         self.L = lib()
         self.B = len(params)
         self.dim = params[0]["dim"]
         self.caps = [int(c) for c in caps]
         cfg = Config(dim=self.dim, force_law=params[0]["force_law"], precision=precision, rng_mode=rng,
                      seed=seed, num_colonies=self.B, device=device, bin_width=bin_width, skin=skin,
-                     block_size=0, flags=0)
+                     block_size=0, flags=0 if graphs else FLAG_NO_GRAPH)
         arr = (ColonyParams * self.B)(*[make_params(**p) for p in params])
         caps_a = np.array(self.caps, np.int32)
         h = C.c_void_p()
@@ -256,6 +305,38 @@ class Engine:
         return dict(ncells=o.ncells, mean_area=o.mean_area, msd=o.msd, vacf=o.vacf,
                     ndiv_total=o.ndiv_total, napo_total=o.napo_total)
 
+    def skin_stats(self, colony: int = 0) -> dict:
+        k = SkinInfo()
+        self._check(self.L.cil_skin_stats(self.h, colony, C.byref(k)))
+        return {f: getattr(k, f) for f, _ in SkinInfo._fields_}
+
+    def set_skin(self, colony: int, skin: float, interval: int = 0):
+        self._check(self.L.cil_set_skin(self.h, colony, skin, interval))
+
+    def set_scheduler(self, params, skin_min: float = 0.05, interval_scale: float = 100.0,
+                      use_interval: bool = True):
+        """Installs the skin-scheduler network (a float32 vector of mlp_num_params() values),
+        or removes it with params=None."""
+        if params is None:
+            self._check(self.L.cil_set_scheduler(self.h, None, 0.0, 0.0, 0))
+            return
+        w = np.ascontiguousarray(params, dtype=np.float32)
+        if w.size != mlp_num_params():
+            raise ValueError(f"expected {mlp_num_params()} parameters, got {w.size}")
+        self._check(self.L.cil_set_scheduler(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), skin_min,
+                                             interval_scale, 1 if use_interval else 0))
+
+    def sched_state(self, colony: int = 0) -> dict:
+        q = SchedInfo()
+        self._check(self.L.cil_sched_state(self.h, colony, C.byref(q)))
+        return dict(features=np.array(q.features[:], dtype=np.float32), div_rate=q.div_rate,
+                    apo_rate=q.apo_rate, trip_share=q.trip_share, nsched=q.nsched)
+
+    def graph_info(self) -> dict:
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.L.cil_graph_info(self.h, C.byref(a), C.byref(b)))
+        return dict(graph_steps=a.value, graphs_captured=b.value)
+
     def timings(self) -> dict:
         a, b, c, t = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         n = C.c_int64()
@@ -273,6 +354,37 @@ def host_rng_draw(seed: int, kind: str, n: int) -> np.ndarray:
     if st != 0:
         raise CilError(st, "cil_host_rng_draw failed")
     return out.reshape(n, width) if width > 1 else out
+
+
+def mlp_num_params() -> int:
+    return int(lib().cil_mlp_num_params())
+
+
+def _mlp_call(st, what):
+    if st != 0:
+        raise CilError(st, what + " failed")
+
+
+def mlp_forward(params, X, Y):
+    """Y[n,2] = net(X[n,12]); float32 CUDA tensors (torch), current device."""
+    _mlp_call(lib().cil_mlp_forward(params.data_ptr(), X.data_ptr(), X.shape[0], Y.data_ptr()), "cil_mlp_forward")
+
+
+def mlp_grad(params, X, T, out_weights, workspace, grad, loss):
+    """Loss (weighted mean squared error) and its gradient; float32 CUDA tensors. workspace
+    holds mlp_workspace_floats(n) floats."""
+    _mlp_call(lib().cil_mlp_grad(params.data_ptr(), X.data_ptr(), T.data_ptr(), out_weights.data_ptr(),
+                                 X.shape[0], workspace.data_ptr(), grad.data_ptr(), loss.data_ptr()),
+              "cil_mlp_grad")
+
+
+def mlp_workspace_floats(n: int) -> int:
+    return int(lib().cil_mlp_workspace_floats(n))
+
+
+def mlp_adam(params, grad, m, v, t: int, lr: float):
+    _mlp_call(lib().cil_mlp_adam(params.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(), t, lr),
+              "cil_mlp_adam")
 
 
 def version() -> str:

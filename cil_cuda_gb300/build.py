@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcilgpu.so")
-SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_noalloc.cu"]
+SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

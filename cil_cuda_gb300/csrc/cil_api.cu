@@ -45,6 +45,13 @@ struct HostColony {
 
 }  // namespace
 
+struct GraphSlot {
+  int key;                 // cur | meta << 1 | pu << 2 at the first of the two steps
+  uint64_t gen;
+  cudaGraphExec_t exec;
+  int64_t launches;        // kernels in the graph
+};
+
 struct cil_handle {
   cil_config cfg{};
   int B = 0, D = 2;
@@ -58,6 +65,7 @@ struct cil_handle {
   int grid_slots = 0;  // persistent grid for slot kernels
   int grid_cells = 0;
   int grid_force = 0;
+  int stiles = 0;      // tiles over the slot capacity (grid of the list force kernel)
   int nsm = 0;
   bool geometry_ready = false;
   int64_t ts = 0;
@@ -71,7 +79,31 @@ struct cil_handle {
   double *d_sig[2] = {nullptr, nullptr};
   int *d_eid[2] = {nullptr, nullptr};
   int cur = 0, meta = 0;
-  float *d_u = nullptr, *d_sigf = nullptr;
+  float4 *d_pk[2] = {nullptr, nullptr};  // mixed: packed elements (coordinates + diameter)
+  int *d_sbin[2] = {nullptr, nullptr};
+  int2 *d_cyc[2] = {nullptr, nullptr};
+  double *d_sigma_c = nullptr;  // canonical diameters [2 * CC]
+  bool need_exact = true;       // next rebuild takes the FP64 reference path
+  int pu = 1;                   // which d_pk holds the current packed elements
+  // skin mode
+  bool skin_mode = false;
+  unsigned char *d_state[2] = {nullptr, nullptr};
+  int *d_nbr = nullptr, *d_ncnt = nullptr, *d_fresh = nullptr;
+  unsigned long long *d_fhead = nullptr, *d_fnext = nullptr;  // per-bin fresh lists
+  float *d_uref = nullptr, *d_facc = nullptr;
+  ColonySkin *d_skin = nullptr;
+  int *d_ts = nullptr;           // device step counter (kernels read the step from here)
+  // CUDA graphs of two steady steps, one per buffer parity (graph_gen: invalidation)
+  std::vector<GraphSlot> graphs;
+  uint64_t graph_gen = 0;
+  bool graphs_off = false;
+  int64_t graph_steps = 0, graphs_captured = 0;
+  SchedState *d_sched = nullptr;
+  float *d_mlp = nullptr;        // scheduler network parameters (null: fixed skin and cadence)
+  float sched_skin_min = 0.0f, sched_interval_scale = 0.0f;
+  int sched_use_interval = 0;
+  int permute_period = 250;      // steps between slot re-sorts (locality, compaction)
+  bool lists_stale = true;       // slots were re-sorted outside a step: rebuild the lists
   double *d_vel = nullptr, *d_frc = nullptr;
   double *d_vel2 = nullptr;  // second velocity buffer for rebuilds outside a step
   int *d_key = nullptr;
@@ -120,13 +152,18 @@ cil_status fail(cil_handle *h, cil_status s, const std::string &m) {
 
 void free_all(cil_handle *h) {
   void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
-                  h->d_eid[1], h->d_u, h->d_sigf, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_eid[1], h->d_pk[0], h->d_pk[1], h->d_sbin[0], h->d_sbin[1],
+                  h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
+                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_obs,
                   h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (auto &gs : h->graphs)
+    if (gs.exec) cudaGraphExecDestroy(gs.exec);
+  h->graphs.clear();
   if (h->h_noise) cudaFreeHost(h->h_noise);
   for (auto e : h->evpool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -168,6 +205,12 @@ cil_status setup_geometry(cil_handle *h) {
     for (int d = 0; d < h->D; ++d) nb *= C.ns[d];
     if (nb > (1ll << 30)) return fail(h, CIL_ERR_CONFIG, "bin grid too large");
     C.nbins = static_cast<int>(nb);
+    {
+      const uint32_t d0 = h->D == 2 ? static_cast<uint32_t>(C.ns[1]) : static_cast<uint32_t>(C.ns[1] * C.ns[2]);
+      const uint32_t d1 = static_cast<uint32_t>(C.ns[2] > 0 ? C.ns[2] : 1);
+      div_invariant_setup(d0, &C.div_m[0], &C.div_s1[0], &C.div_s2[0]);
+      div_invariant_setup(d1, &C.div_m[1], &C.div_s1[1], &C.div_s2[1]);
+    }
     C.nbins_pad = ((C.nbins + kScanItems - 1) / kScanItems) * kScanItems;
     C.bin_base = bin_base;
     C.scan_base = bin_base / kScanItems;
@@ -175,6 +218,7 @@ cil_status setup_geometry(cil_handle *h) {
     for (int d = 0; d < 3; ++d) {
       C.bw[d] = d < h->D ? hc.p.box[d] / C.ns[d] : 0.0;
       C.bwf[d] = static_cast<float>(C.bw[d]);
+      C.inv_bwf[d] = d < h->D ? static_cast<float>(1.0 / C.bw[d]) : 0.0f;
     }
   }
   if (bin_base != h->NBpad) {
@@ -183,6 +227,8 @@ cil_status setup_geometry(cil_handle *h) {
     cudaFree(h->d_scan_sum);
     cudaFree(h->d_scan_off);
     cudaFree(h->d_scan_col);
+    cudaFree(h->d_fhead);
+    h->d_fhead = nullptr;
     h->NBpad = bin_base;
     h->nscan = bin_base / kScanItems;
     h->d_bcount = dalloc<int>(h->NBpad);
@@ -192,6 +238,12 @@ cil_status setup_geometry(cil_handle *h) {
     h->d_scan_col = dalloc<int>(h->nscan);
     if (!h->d_bcount || !h->d_range || !h->d_scan_sum || !h->d_scan_off || !h->d_scan_col)
       return fail(h, CIL_ERR_CUDA, "out of device memory for bins");
+    if (h->skin_mode) {
+      h->d_fhead = dalloc<unsigned long long>(h->NBpad);
+      if (!h->d_fhead) return fail(h, CIL_ERR_CUDA, "out of device memory for bins");
+      // epoch 0xffffffff: matches no rebuild count, so every list starts empty
+      CUDA_TRY(h, cudaMemsetAsync(h->d_fhead, 0xff, sizeof(unsigned long long) * h->NBpad, h->stream));
+    }
   }
   std::vector<int> scol(h->nscan);
   for (int c = 0; c < h->B; ++c)
@@ -201,6 +253,7 @@ cil_status setup_geometry(cil_handle *h) {
   CUDA_TRY(h, cudaMemcpyAsync(h->d_scan_col, scol.data(), sizeof(int) * h->nscan, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(h->d_col, h->cc.data(), sizeof(ColonyConst) * h->B, cudaMemcpyHostToDevice, h->stream));
   h->geometry_ready = true;
+  h->graph_gen += 1;  // captured graphs hold the old bin arrays
   return CIL_OK;
 }
 
@@ -220,14 +273,28 @@ RebuildArgs rebuild_args(cil_handle *h) {
   a.tiles_live = h->d_tiles_live;
   a.scan_col = h->d_scan_col;
   a.nscan = h->nscan;
+  const bool mixed = h->cfg.precision == CIL_PREC_MIXED;
   a.x_in = h->d_x[h->cur];
   a.sig_in = h->d_sig[h->meta];
   a.eid_in = h->d_eid[h->meta];
   a.x_out = h->d_x[1 - h->cur];
   a.sig_out = h->d_sig[1 - h->meta];
   a.eid_out = h->d_eid[1 - h->meta];
-  a.u_out = h->cfg.precision == CIL_PREC_MIXED ? h->d_u : nullptr;
-  a.sigf_out = h->cfg.precision == CIL_PREC_MIXED ? h->d_sigf : nullptr;
+  a.pk_out = mixed ? h->d_pk[1 - h->pu] : nullptr;
+  a.pk_in = mixed ? h->d_pk[h->pu] : nullptr;
+  a.skin = nullptr;  // a permuting rebuild re-sorts every colony
+  a.permute = 1;
+  a.state_out = h->skin_mode ? h->d_state[1 - h->meta] : nullptr;
+  a.sbin_in = h->d_sbin[h->meta];
+  a.sbin_out = h->d_sbin[1 - h->meta];
+  a.cyc_in = h->d_cyc[h->meta];
+  a.cyc_out = h->d_cyc[1 - h->meta];
+  a.sigma_c = h->d_sigma_c;
+  a.t0c = h->d_t0;
+  a.tswc = h->d_tsw;
+  // the FP64 form always takes the reference path; the mixed form re-anchors its FP32
+  // local coordinates on the FP64 positions after an upload and every 32 steps
+  a.exact = (!mixed || h->need_exact || (h->ts % 32) == 0) ? 1 : 0;
   a.key = h->d_key;
   a.bcount = h->d_bcount;
   a.range = h->d_range;
@@ -242,7 +309,8 @@ RebuildArgs rebuild_args(cil_handle *h) {
 // A rebuild inside a step needs no velocities (the force pass rewrites them); a rebuild
 // outside a step (cil_forces, cil_bins) carries them through the permutation so that a
 // later download still pairs each element with its own velocity.
-cil_status do_rebuild(cil_handle *h, bool carry_vel = false) {
+cil_status do_rebuild(cil_handle *h, bool carry_vel = false, bool exact = false) {
+  if (exact) h->need_exact = true;
   RebuildArgs a = rebuild_args(h);
   if (carry_vel) {
     if (!h->d_vel2) {
@@ -256,6 +324,9 @@ cil_status do_rebuild(cil_handle *h, bool carry_vel = false) {
   launch_rebuild(a, h->grid_slots, h->stream);
   h->cur = 1 - h->cur;
   h->meta = 1 - h->meta;
+  if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
+  h->need_exact = false;
+  h->lists_stale = true;
   if (carry_vel) std::swap(h->d_vel, h->d_vel2);
   return CIL_OK;
 }
@@ -271,16 +342,25 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
   a.x_out = h->d_x[1 - h->cur];
   a.sig = h->d_sig[h->meta];
   a.eid = h->d_eid[h->meta];
-  a.u = h->d_u;
-  a.sigf = h->d_sigf;
+  a.pk = h->d_pk[h->pu];
+  a.pk_next = h->d_pk[1 - h->pu];
+  if (h->skin_mode) {
+    a.tiles = h->d_tiles_used;
+    a.skin = h->d_skin;
+    a.nbr = h->d_nbr;
+    a.ncnt = h->d_ncnt;
+    a.uref = h->d_uref;
+    a.facc = h->d_facc;
+    a.sched = h->d_sched;
+  }
+  a.sbin = h->d_sbin[h->meta];
+  a.cyc = h->d_cyc[h->meta];
   a.range = h->d_range;
   a.slot_of = h->d_slot_of;
-  a.t0 = h->d_t0;
-  a.tsw = h->d_tsw;
   a.noise = h->d_noise;
   a.vel = vel;
   a.frc = frc;
-  a.ts = static_cast<int>(h->ts);
+  a.ts_dev = h->d_ts;
   a.seed_lo = static_cast<uint32_t>(h->cfg.seed);
   a.seed_hi = static_cast<uint32_t>(h->cfg.seed >> 32);
   a.noise_mode = noise_mode;
@@ -297,6 +377,19 @@ EventArgs event_args(cil_handle *h) {
   a.tiles_cell = h->d_tiles_cell;
   a.x = h->d_x[h->cur];
   a.sig = h->d_sig[h->meta];
+  a.pk = h->cfg.precision == CIL_PREC_MIXED ? h->d_pk[h->pu] : nullptr;
+  a.sbin = h->d_sbin[h->meta];
+  if (h->skin_mode) {
+    a.skin = h->d_skin;
+    a.state = h->d_state[h->meta];
+    a.uref = h->d_uref;
+    a.ncnt = h->d_ncnt;
+    a.fresh = h->d_fresh;
+    a.fhead = h->d_fhead;
+    a.fnext = h->d_fnext;
+  }
+  a.cyc = h->d_cyc[h->meta];
+  a.sigma_c = h->d_sigma_c;
   a.eid = h->d_eid[h->meta];
   a.vel = h->d_vel;
   a.slot_of = h->d_slot_of;
@@ -311,9 +404,38 @@ EventArgs event_args(cil_handle *h) {
     a.obs_vref = h->d_obs + 2 * static_cast<size_t>(h->D) * h->CC;
   }
   a.CC = h->CC;
-  a.ts = static_cast<int>(h->ts);
+  a.ts_dev = h->d_ts;
   a.seed_lo = static_cast<uint32_t>(h->cfg.seed);
   a.seed_hi = static_cast<uint32_t>(h->cfg.seed >> 32);
+  return a;
+}
+
+SkinArgs skin_args(cil_handle *h, int force_rebuild) {
+  SkinArgs a{};
+  a.col = h->d_col;
+  a.cnt = h->d_cnt;
+  a.skin = h->d_skin;
+  a.sched = h->d_sched;
+  a.B = h->B;
+  a.SS = h->SS;
+  a.tiles = h->d_tiles_used;
+  a.eid = h->d_eid[h->meta];
+  a.state = h->d_state[h->meta];
+  a.pk = h->d_pk[h->pu];
+  a.uref = h->d_uref;
+  a.sbin = h->d_sbin[h->meta];
+  a.range = h->d_range;
+  a.perm = h->d_perm;
+  a.nbr = h->d_nbr;
+  a.ncnt = h->d_ncnt;
+  a.fresh = h->d_fresh;
+  a.fhead = h->d_fhead;
+  a.fnext = h->d_fnext;
+  a.facc = h->d_facc;
+  a.key = h->d_key;
+  a.bcount = h->d_bcount;
+  a.force_rebuild = force_rebuild;
+  a.grid = h->nsm * 16;  // fresh-pair kernel: 64 warps per SM over all colonies' fresh elements
   return a;
 }
 
@@ -355,6 +477,7 @@ cil_status ensure_oracle_buffers(cil_handle *h, size_t need_i, size_t need_d) {
 // oracle mode: division and apoptosis draws on the host mirror, replayed on the device
 cil_status oracle_events(cil_handle *h) {
   const int ts = static_cast<int>(h->ts);
+  int cap_hit = -1;
   for (int c = 0; c < h->B; ++c) {
     HostColony &hc = h->hc[c];
     const int D = h->D;
@@ -364,7 +487,10 @@ cil_status oracle_events(cil_handle *h) {
     if (hc.p.divide) {
       for (int i = 0; i < n0; ++i) {
         if (hc.tsw[i] != ts) continue;
-        if (hc.n >= hc.cap) continue;  // the oracle skips divisions beyond capacity
+        if (hc.n >= hc.cap) {  // skipped, as the oracle does, and reported after the step
+          cap_hit = c;
+          continue;
+        }
         const int k = hc.n++;
         double dm[3] = {0, 0, 0}, dd[3] = {0, 0, 0};
         h->rng.on_dsphere(D, dm);
@@ -421,6 +547,7 @@ cil_status oracle_events(cil_handle *h) {
     launch_apo_ops_with_div(a, c, ndiv, static_cast<int>(ops.size()), h->d_oracle_i + 3 * ndiv, D, h->stream);
     h->launches += (ndiv > 0 ? 1 : 0) + 1;
   }
+  if (cap_hit >= 0) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(cap_hit));
   return CIL_OK;
 }
 
@@ -456,6 +583,182 @@ cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = null
     if (k[c].err & kErrCap) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(c));
   }
   return CIL_OK;
+}
+
+// One step's launches on the handle's stream (oracle mode: with its host draws). When timed,
+// four events bracket the phases; a step being captured into a graph records none.
+cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
+  const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
+  cil_status st = CIL_OK;
+  bool noise = false;
+  if (oracle) {
+    st = draw_oracle_noise(h, &noise);
+    if (st != CIL_OK) return st;
+  } else {
+    for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;
+  }
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
+  if (h->skin_mode) {
+    // list rebuilds are decided on the device (guard, cadence, fresh overflow); the host
+    // re-sorts the slots on a fixed schedule and after uploads
+    const bool permute = h->need_exact || h->lists_stale || (h->ts % h->permute_period) == 0;
+    launch_skin_begin(skin_args(h, permute ? 1 : 0), h->stream);
+    if (h->d_mlp) {
+      SchedArgs sa{};
+      sa.skin = h->d_skin;
+      sa.sched = h->d_sched;
+      sa.cnt = h->d_cnt;
+      sa.B = h->B;
+      sa.use_interval = h->sched_use_interval;
+      sa.skin_min = h->sched_skin_min;
+      sa.skin_max = static_cast<float>(h->cfg.skin);
+      sa.interval_scale = h->sched_interval_scale;
+      launch_mlp_schedule(h->d_mlp, sa, h->stream);
+      h->launches += 1;
+    }
+    if (permute) {
+      st = do_rebuild(h);
+      if (st != CIL_OK) return st;
+    } else {
+      launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
+      launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
+      RebuildArgs ra = rebuild_args(h);
+      ra.permute = 0;
+      ra.skin = h->d_skin;  // only colonies with rebuild_now
+      ra.state_out = nullptr;
+      launch_rebuild(ra, h->grid_slots, h->stream);
+    }
+    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
+    launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
+    launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
+    h->lists_stale = false;
+    h->launches += permute ? 15 : 9;
+  } else {
+    st = do_rebuild(h);
+    if (st != CIL_OK) return st;
+    h->launches += 10;
+  }
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 1), h->stream));
+  ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
+  if (h->skin_mode)
+    launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->stream);
+  else
+    launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+  h->cur = 1 - h->cur;
+  if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
+  launch_advance_ts(h->d_ts, h->stream);
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
+  h->ts += 1;
+  if (oracle) {
+    st = oracle_events(h);
+    if (st != CIL_OK) return st;
+    h->launches += 2;
+  } else {
+    launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
+    launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
+    h->launches += 7;
+  }
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
+  CUDA_TRY(h, cudaGetLastError());
+  return CIL_OK;
+}
+
+// A step whose launches and arguments depend only on the buffer parities: Philox noise, no
+// slot re-sort (skin mode), no FP64 re-anchoring (mixed form without skin).
+bool steady_step(const cil_handle *h, int64_t ts) {
+  if (h->cfg.rng_mode != CIL_RNG_PHILOX || (h->cfg.flags & CIL_FLAG_NO_GRAPH) || h->need_exact) return false;
+  if (h->skin_mode) return !h->lists_stale && (ts % h->permute_period) != 0;
+  if (h->cfg.precision == CIL_PREC_MIXED) return (ts % 32) != 0;
+  return true;
+}
+
+struct HostStepState {
+  int cur, meta, pu;
+  bool need_exact, lists_stale;
+  int64_t ts;
+};
+
+HostStepState host_state(const cil_handle *h) {
+  return HostStepState{h->cur, h->meta, h->pu, h->need_exact, h->lists_stale, h->ts};
+}
+
+// What one steady step does to the host-side state (mirrors enqueue_step)
+void advance_host_state(const cil_handle *h, HostStepState *s) {
+  const bool mixed = h->cfg.precision == CIL_PREC_MIXED;
+  if (h->skin_mode) {
+    s->lists_stale = false;
+  } else {  // do_rebuild
+    s->cur ^= 1;
+    s->meta ^= 1;
+    if (mixed) s->pu ^= 1;
+    s->need_exact = false;
+    s->lists_stale = true;
+  }
+  s->cur ^= 1;  // force pass
+  if (mixed) s->pu ^= 1;
+  s->ts += 1;
+}
+
+bool same_state(const HostStepState &a, const HostStepState &b) {
+  return a.cur == b.cur && a.meta == b.meta && a.pu == b.pu && a.need_exact == b.need_exact &&
+         a.lists_stale == b.lists_stale && a.ts == b.ts;
+}
+
+void restore_host_state(cil_handle *h, const HostStepState &s) {
+  h->cur = s.cur;
+  h->meta = s.meta;
+  h->pu = s.pu;
+  h->need_exact = s.need_exact;
+  h->lists_stale = s.lists_stale;
+  h->ts = s.ts;
+}
+
+// The executable graph of two steady steps starting from the current parities, captured on
+// first use (the capture advances the host state as the two steps would; the caller then
+// replays the graph). On a capture failure the host state is put back, graphs are switched
+// off for the handle and null is returned.
+cudaGraphExec_t steady_graph(cil_handle *h, int64_t *launches_per_pair) {
+  const int key = h->cur | (h->meta << 1) | (h->pu << 2);
+  for (auto &gs : h->graphs)
+    if (gs.key == key && gs.gen == h->graph_gen) {
+      HostStepState s = host_state(h);
+      advance_host_state(h, &s);
+      advance_host_state(h, &s);
+      restore_host_state(h, s);
+      *launches_per_pair = gs.launches;
+      return gs.exec;
+    }
+  const HostStepState before = host_state(h);
+  const int64_t launches0 = h->launches;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    h->graphs_off = true;
+    return nullptr;
+  }
+  const cil_status s1 = enqueue_step(h, false, false, 0);
+  const cil_status s2 = s1 == CIL_OK ? enqueue_step(h, false, false, 0) : s1;
+  const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+  HostStepState expect = before;
+  advance_host_state(h, &expect);
+  advance_host_state(h, &expect);
+  cudaGraphExec_t exec = nullptr;
+  const bool ok = s1 == CIL_OK && s2 == CIL_OK && ec == cudaSuccess && g != nullptr &&
+                  same_state(host_state(h), expect) && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    restore_host_state(h, before);
+    h->launches = launches0;
+    h->graphs_off = true;
+    return nullptr;
+  }
+  *launches_per_pair = h->launches - launches0;
+  h->launches = launches0;
+  h->graphs.push_back(GraphSlot{key, h->graph_gen, exec, *launches_per_pair});
+  h->graphs_captured += 1;
+  return exec;
 }
 
 }  // namespace
@@ -497,7 +800,8 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->force_law < 0 || cfg->force_law > 2) return CIL_ERR_CONFIG;
   if (cfg->precision != CIL_PREC_FP64 && cfg->precision != CIL_PREC_MIXED) return CIL_ERR_CONFIG;
   if (cfg->rng_mode != CIL_RNG_PHILOX && cfg->rng_mode != CIL_RNG_DSFMT) return CIL_ERR_CONFIG;
-  if (cfg->skin != 0.0) return CIL_ERR_CONFIG;  // the skin path is not part of this build
+  if (cfg->skin < 0.0 || (cfg->skin > 0.0 && cfg->precision != CIL_PREC_MIXED)) return CIL_ERR_CONFIG;
+  if (cfg->skin > 0.0 && cfg->num_colonies > kMaxSkinColonies) return CIL_ERR_CONFIG;
   auto *h = new cil_handle();
   h->cfg = *cfg;
   h->B = cfg->num_colonies;
@@ -536,7 +840,9 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.cell_base = static_cast<int>(cells);
     C.cell_cap = cap_cells[c];
     C.slot_base = static_cast<int>(slots);
-    C.slot_cap = static_cast<int>(((2ll * cap_cells[c] + kSlotAlign - 1) / kSlotAlign) * kSlotAlign);
+    // skin mode appends daughters between slot re-sorts: keep an eighth more slots
+    const long long want = 2ll * cap_cells[c] + (cfg->skin > 0.0 ? (2ll * cap_cells[c]) / 8 + 4096 : 0);
+    C.slot_cap = static_cast<int>(((want + kSlotAlign - 1) / kSlotAlign) * kSlotAlign);
     C.force_law = p.force_law;
     C.noise_per_cell = p.noise_per_cell;
     C.divide = p.divide;
@@ -562,12 +868,31 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.div_tau_mu = p.div_tau_mu;
     C.div_tau_sigma = p.div_tau_sigma;
     C.apop_p = p.apop_rate * p.dt;
+    for (int j = 0; j < 2; ++j) {
+      C.zeta_f[j] = static_cast<float>(C.zeta[j]);
+      C.temp_f[j] = static_cast<float>(C.temp[j]);
+      C.mu_f[j] = static_cast<float>(C.mu_eff[j]);
+      C.motility_f[j] = static_cast<float>(C.motility[j]);
+      C.wall_pos_f[j] = static_cast<float>(C.wall_pos[j]);
+    }
+    C.kappa_f = static_cast<float>(C.kappa);
+    C.rest0_f = static_cast<float>(C.rest0);
+    C.rest1_f = static_cast<float>(C.rest1);
+    C.amp_f = static_cast<float>(C.noise_amp);
+    C.eps_f = static_cast<float>(C.epsilon);
+    C.rcs_f = static_cast<float>(C.rcut_scale);
+    C.wall_E_f = static_cast<float>(C.wall_E);
     cells += cap_cells[c];
     slots += C.slot_cap;
     if (cells > (1ll << 29) || slots > (1ll << 30)) {
       delete h;
       return CIL_ERR_CONFIG;
     }
+  }
+  if (cfg->skin > 0.0 && slots >= (1ll << kListSlotBits)) {
+    // Verlet-list entries hold a slot index in kListSlotBits bits
+    delete h;
+    return CIL_ERR_CONFIG;
   }
   h->CC = static_cast<int>(cells);
   h->SS = static_cast<size_t>(slots);
@@ -585,14 +910,31 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   const size_t SS = h->SS, D = h->D;
   h->d_col = dalloc<ColonyConst>(h->B);
   h->d_cnt = dalloc<ColonyCounters>(h->B);
+  const bool mixed = cfg->precision == CIL_PREC_MIXED;
   for (int b = 0; b < 2; ++b) {
     h->d_x[b] = dalloc<double>(D * SS);
-    h->d_sig[b] = dalloc<double>(SS);
+    if (!mixed) h->d_sig[b] = dalloc<double>(SS);
     h->d_eid[b] = dalloc<int>(SS);
+    h->d_sbin[b] = dalloc<int>(SS);
+    h->d_cyc[b] = dalloc<int2>(SS);
+    if (mixed) h->d_pk[b] = dalloc<float4>(SS);
   }
-  if (cfg->precision == CIL_PREC_MIXED) {
-    h->d_u = dalloc<float>(D * SS);
-    h->d_sigf = dalloc<float>(SS);
+  h->d_sigma_c = dalloc<double>(2 * static_cast<size_t>(h->CC));
+  h->d_ts = dalloc<int>(1);
+  h->skin_mode = cfg->skin > 0.0;
+  bool skin_ok = true;
+  if (h->skin_mode) {
+    for (int b = 0; b < 2; ++b) h->d_state[b] = dalloc<unsigned char>(SS);
+    h->d_nbr = dalloc<int>(static_cast<size_t>(kListCap) * SS);
+    h->d_ncnt = dalloc<int>(SS);
+    h->d_uref = dalloc<float>(D * SS);
+    h->d_facc = dalloc<float>(D * SS);
+    h->d_fresh = dalloc<int>(static_cast<size_t>(h->B) * kFreshCap);
+    h->d_fnext = dalloc<unsigned long long>(SS);
+    h->d_skin = dalloc<ColonySkin>(h->B);
+    h->d_sched = dalloc<SchedState>(h->B);
+    skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_fresh &&
+              h->d_fnext && h->d_skin && h->d_sched;
   }
   h->d_vel = dalloc<double>(D * SS);
   h->d_key = dalloc<int>(SS);
@@ -605,13 +947,17 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_tiles_cell = dalloc<int>(h->B + 1);
   h->ctiles = 0;
   for (int c = 0; c < h->B; ++c) h->ctiles += (h->hc[c].cap + kTile - 1) / kTile;
+  h->stiles = 0;
+  for (int c = 0; c < h->B; ++c) h->stiles += (h->cc[c].slot_cap + kTile - 1) / kTile;
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
-  bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_sig[0] && h->d_sig[1] && h->d_eid[0] &&
-            h->d_eid[1] && h->d_vel && h->d_key && h->d_perm && h->d_slot_of && h->d_t0 && h->d_tsw &&
-            h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell && h->d_tile_count && h->d_tile_off &&
-            h->d_dead && (cfg->precision != CIL_PREC_MIXED || (h->d_u && h->d_sigf));
+  bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_eid[0] && h->d_eid[1] && h->d_sbin[0] &&
+            h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
+            h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
+            h->d_tile_count && h->d_tile_off && h->d_dead && h->d_ts &&
+            (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
+            skin_ok;
   if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {
     const size_t nn = 2 * static_cast<size_t>(h->CC) * D;
     h->d_noise = dalloc<double>(nn);
@@ -628,10 +974,26 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   // filled in once every colony has been uploaded
   cudaMemcpyAsync(h->d_col, h->cc.data(), sizeof(ColonyConst) * h->B, cudaMemcpyHostToDevice, h->stream);
   cudaMemsetAsync(h->d_cnt, 0, sizeof(ColonyCounters) * h->B, h->stream);
+  cudaMemsetAsync(h->d_ts, 0, sizeof(int), h->stream);
   cudaMemsetAsync(h->d_vel, 0, sizeof(double) * D * SS, h->stream);
   cudaMemsetAsync(h->d_eid[0], 0xff, sizeof(int) * SS, h->stream);
   cudaMemsetAsync(h->d_eid[1], 0xff, sizeof(int) * SS, h->stream);
   cudaMemsetAsync(h->d_key, 0xff, sizeof(int) * SS, h->stream);
+  if (h->skin_mode) {
+    std::vector<ColonySkin> sk(h->B);
+    for (auto &k : sk) {
+      std::memset(&k, 0, sizeof k);
+      k.skin = static_cast<float>(cfg->skin);
+      k.half2 = static_cast<float>(0.25 * cfg->skin * cfg->skin);
+      k.need = 8;
+    }
+    cudaMemcpy(h->d_skin, sk.data(), sizeof(ColonySkin) * h->B, cudaMemcpyHostToDevice);
+    cudaMemsetAsync(h->d_sched, 0, sizeof(SchedState) * h->B, h->stream);
+    cudaMemsetAsync(h->d_facc, 0, sizeof(float) * D * SS, h->stream);
+    cudaMemsetAsync(h->d_ncnt, 0, sizeof(int) * SS, h->stream);
+    cudaMemsetAsync(h->d_state[0], kSlotDead, SS, h->stream);
+    cudaMemsetAsync(h->d_state[1], kSlotDead, SS, h->stream);
+  }
   h->grid_slots = std::max(1, std::min(h->nsm * 8, static_cast<int>((SS + kTile - 1) / kTile)));
   h->grid_cells = std::max(1, std::min(h->nsm * 8, h->ctiles));
   h->grid_force = h->grid_slots;
@@ -675,18 +1037,19 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
     if (!std::isfinite(x) || x < 0.0 || x >= hc.p.box[d])
       return fail(h, CIL_ERR_OUT_OF_BOX, "cil_upload: position outside the box (CIL.cuh:54-66)");
   }
-  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * (D + 1));
+  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * D);
   if (sst != CIL_OK) return sst;
   // the positions are re-binned by the first rebuild; the fresh slots follow the current
   // buffers
   CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, v->pos, sizeof(double) * 2 * n * D, cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(h->d_stage + 2 * n * D, v->sigma, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_sigma_c + 2 * static_cast<size_t>(C.cell_base), v->sigma, sizeof(double) * 2 * n,
+                              cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(h->d_t0 + C.cell_base, v->t0, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemcpyAsync(h->d_tsw + C.cell_base, v->tswitch, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(h, cudaMemsetAsync(h->d_vel + 0, 0, sizeof(double) * D * h->SS, h->stream));
   CUDA_TRY(h, cudaMemsetAsync(h->d_eid[h->meta] + C.slot_base, 0xff, sizeof(int) * C.slot_cap, h->stream));
-  launch_upload_scatter(h->d_col, colony, n, D, h->SS, h->d_stage, h->d_stage + 2 * n * D, h->d_x[h->cur],
-                        h->d_sig[h->meta], h->d_eid[h->meta], h->d_slot_of, h->d_cnt, h->stream);
+  launch_upload_scatter(h->d_col, colony, n, D, h->SS, h->d_stage, h->d_x[h->cur], h->d_eid[h->meta],
+                        h->d_slot_of, h->d_cnt, h->stream);
   CUDA_TRY(h, cudaGetLastError());
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   hc.uploaded = true;
@@ -697,8 +1060,19 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
   hc.t0.resize(hc.cap);
   hc.tsw.resize(hc.cap);
   h->ts = v->ts;
+  {
+    const int tsi = static_cast<int>(v->ts);
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_ts, &tsi, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  }
   h->obs_ready[colony] = 0;
   h->geometry_ready = false;
+  h->need_exact = true;
+  if (h->skin_mode) {
+    // the scheduler's statistics restart with the new state; the event counters restart too
+    CUDA_TRY(h, cudaMemsetAsync(h->d_sched + colony, 0, sizeof(SchedState), h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  }
   return CIL_OK;
 }
 
@@ -707,52 +1081,47 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
   if (nsteps < 0) return fail(h, CIL_ERR_CONFIG, "cil_step: negative step count");
   cil_status st = ensure_ready(h);
   if (st != CIL_OK) return st;
-  const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
   h->t_rebuild = h->t_force = h->t_events = 0.0;
   h->launches = 0;
-  for (int k = 0; k < nsteps; ++k) {
-    bool noise = false;
-    if (oracle) {
-      st = draw_oracle_noise(h, &noise);
-      if (st != CIL_OK) return st;
-    } else {
-      for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;
+  h->graph_steps = 0;
+  std::vector<char> seg_graph;  // per segment of 4 events: 1 = a graph of two steps
+  int k = 0;
+  while (k < nsteps) {
+    const size_t e0 = 4 * seg_graph.size();
+    // two steady steps, neither the last one of the call (which writes velocities)
+    if (!h->graphs_off && k + 2 < nsteps && steady_step(h, h->ts) && steady_step(h, h->ts + 1)) {
+      int64_t nl = 0;
+      cudaGraphExec_t ex = steady_graph(h, &nl);
+      if (ex) {
+        CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
+        CUDA_TRY(h, cudaGraphLaunch(ex, h->stream));
+        CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
+        seg_graph.push_back(1);
+        h->launches += nl;
+        h->graph_steps += 2;
+        k += 2;
+        continue;
+      }
     }
-    const size_t e0 = 4 * static_cast<size_t>(k);
-    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
-    do_rebuild(h);
-    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 1), h->stream));
-    const bool last = k == nsteps - 1;
-    ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
-    launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
-    h->cur = 1 - h->cur;
-    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
-    h->ts += 1;
-    if (oracle) {
-      st = oracle_events(h);
-      if (st != CIL_OK) return st;
-    } else {
-      launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
-      launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
-    }
-    CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
-    CUDA_TRY(h, cudaGetLastError());
+    st = enqueue_step(h, k == nsteps - 1, true, e0);
+    if (st != CIL_OK) return st;
+    seg_graph.push_back(0);
+    k += 1;
   }
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   h->t_total = 0.0;
-  if (nsteps > 0) {
+  const size_t nseg = seg_graph.size();
+  if (nseg > 0) {
     float t = 0;
-    cudaEventElapsedTime(&t, h->evpool[0], h->evpool[4 * (nsteps - 1) + 3]);
+    cudaEventElapsedTime(&t, h->evpool[0], h->evpool[4 * (nseg - 1) + 3]);
     h->t_total = t;
   }
-  // kernels per step: rebuild 1 + 9, force 1, events 1 + 4 (Philox) or 2 when the host
-  // reports divisions/removals (oracle mode, counted by oracle_events)
-  h->launches += static_cast<int64_t>(nsteps) * (oracle ? 11 : 16);
-  for (int k = 0; k < nsteps; ++k) {
+  for (size_t q = 0; q < nseg; ++q) {
+    if (seg_graph[q]) continue;
     float a = 0, b = 0, c = 0;
-    cudaEventElapsedTime(&a, h->evpool[4 * k], h->evpool[4 * k + 1]);
-    cudaEventElapsedTime(&b, h->evpool[4 * k + 1], h->evpool[4 * k + 2]);
-    cudaEventElapsedTime(&c, h->evpool[4 * k + 2], h->evpool[4 * k + 3]);
+    cudaEventElapsedTime(&a, h->evpool[4 * q], h->evpool[4 * q + 1]);
+    cudaEventElapsedTime(&b, h->evpool[4 * q + 1], h->evpool[4 * q + 2]);
+    cudaEventElapsedTime(&c, h->evpool[4 * q + 2], h->evpool[4 * q + 3]);
     h->t_rebuild += a;
     h->t_force += b;
     h->t_events += c;
@@ -778,7 +1147,7 @@ cil_status cil_forces(cil_handle *h, int32_t colony, double *frc) {
     h->d_frc = dalloc<double>(h->D * h->SS);
     if (!h->d_frc) return fail(h, CIL_ERR_CUDA, "out of device memory (forces)");
   }
-  st = do_rebuild(h, true);
+  st = do_rebuild(h, true, true);
   if (st != CIL_OK) return st;
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 0, nullptr, h->d_frc);
   launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
@@ -805,7 +1174,7 @@ cil_status cil_bins(cil_handle *h, int32_t colony, int32_t *ns, int32_t *bin_sta
   const ColonyConst &C = h->cc[colony];
   for (int d = 0; d < 3; ++d) ns[d] = C.ns[d];
   if (C.nbins > max_bins) return fail(h, CIL_ERR_CAPACITY, "cil_bins: max_bins too small");
-  st = do_rebuild(h, true);
+  st = do_rebuild(h, true, true);
   if (st != CIL_OK) return st;
   std::vector<ColonyCounters> k;
   st = check_counters(h, &k);
@@ -838,14 +1207,15 @@ cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *v) {
   v->ncells = n;
   const ColonyConst &C = h->cc[colony];
   const int D = h->D;
-  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * (2 * D + 1));
+  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * (2 * D));
   if (sst != CIL_OK) return sst;
-  double *sp = h->d_stage, *ss = h->d_stage + 2 * n * D, *sv = ss + 2 * n;
+  double *sp = h->d_stage, *sv = h->d_stage + 2 * n * D;
   launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_x[h->cur], D, sp, h->stream);
-  launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_sig[h->meta], 1, ss, h->stream);
   launch_gather_canonical(n, D, h->SS, C.cell_base, h->d_slot_of, h->d_vel, D, sv, h->stream);
   if (v->pos) CUDA_TRY(h, cudaMemcpyAsync(v->pos, sp, sizeof(double) * 2 * n * D, cudaMemcpyDeviceToHost, h->stream));
-  if (v->sigma) CUDA_TRY(h, cudaMemcpyAsync(v->sigma, ss, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
+  if (v->sigma)
+    CUDA_TRY(h, cudaMemcpyAsync(v->sigma, h->d_sigma_c + 2 * static_cast<size_t>(C.cell_base), sizeof(double) * 2 * n,
+                                cudaMemcpyDeviceToHost, h->stream));
   if (v->vel) CUDA_TRY(h, cudaMemcpyAsync(v->vel, sv, sizeof(double) * 2 * n * D, cudaMemcpyDeviceToHost, h->stream));
   if (v->t0) CUDA_TRY(h, cudaMemcpyAsync(v->t0, h->d_t0 + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
   if (v->tswitch) CUDA_TRY(h, cudaMemcpyAsync(v->tswitch, h->d_tsw + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
@@ -906,6 +1276,97 @@ cil_status cil_observables(cil_handle *h, int32_t colony, cil_obs *out) {
   if (!h) return CIL_ERR_CONFIG;
   if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "cil_observables: bad arguments");
   return run_obs(h, colony, 0, out);
+}
+
+cil_status cil_skin_stats(cil_handle *h, int32_t colony, cil_skin_info *out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "cil_skin_stats: bad arguments");
+  if (!h->skin_mode) return fail(h, CIL_ERR_CONFIG, "cil_skin_stats: the handle has no skin");
+  ColonySkin k;
+  CUDA_TRY(h, cudaMemcpyAsync(&k, h->d_skin + colony, sizeof k, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  float md2;
+  std::memcpy(&md2, &k.maxdisp2, sizeof md2);
+  out->skin = k.skin;
+  out->interval = k.interval;
+  out->nrebuild = k.nrebuild;
+  out->ntrip = k.ntrip;
+  out->last_interval = k.last_interval;
+  out->nfresh = k.nfresh;
+  out->list_overflow = k.list_overflow;
+  out->npairs = k.npairs;
+  out->max_disp = std::sqrt(static_cast<double>(md2));
+  return CIL_OK;
+}
+
+cil_status cil_set_skin(cil_handle *h, int32_t colony, double skin, int32_t interval) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !h->skin_mode || !(skin > 0.0) || skin > h->cfg.skin || interval < 0)
+    return fail(h, CIL_ERR_CONFIG, "cil_set_skin: bad arguments");
+  CUDA_TRY(h, cudaSetDevice(h->cfg.device));
+  ColonySkin k;
+  CUDA_TRY(h, cudaMemcpyAsync(&k, h->d_skin + colony, sizeof k, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  k.skin = static_cast<float>(skin);
+  k.half2 = static_cast<float>(0.25 * skin * skin);
+  k.interval = interval;
+  k.need |= 8;
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_skin + colony, &k, sizeof k, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  return CIL_OK;
+}
+
+cil_status cil_set_scheduler(cil_handle *h, const float *params, double skin_min, double interval_scale,
+                             int32_t use_interval) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (!h->skin_mode) return fail(h, CIL_ERR_CONFIG, "cil_set_scheduler: the handle has no skin");
+  CUDA_TRY(h, cudaSetDevice(h->cfg.device));
+  if (!params) {
+    if (h->d_mlp) cudaFree(h->d_mlp);
+    h->d_mlp = nullptr;
+    h->graph_gen += 1;
+    return CIL_OK;
+  }
+  if (!(skin_min > 0.0) || skin_min > h->cfg.skin || !(interval_scale >= 1.0) || !std::isfinite(interval_scale))
+    return fail(h, CIL_ERR_CONFIG, "cil_set_scheduler: need 0 < skin_min <= skin and interval_scale >= 1");
+  const int np = mlp_param_count();
+  for (int i = 0; i < np; ++i)
+    if (!std::isfinite(params[i])) return fail(h, CIL_ERR_CONFIG, "cil_set_scheduler: non-finite parameter");
+  if (!h->d_mlp) {
+    h->d_mlp = dalloc<float>(np);
+    if (!h->d_mlp) return fail(h, CIL_ERR_CUDA, "cil_set_scheduler: out of device memory");
+  }
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_mlp, params, sizeof(float) * np, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  h->graph_gen += 1;  // the scheduler launch is part of a captured step
+  h->sched_skin_min = static_cast<float>(skin_min);
+  h->sched_interval_scale = static_cast<float>(interval_scale);
+  h->sched_use_interval = use_interval ? 1 : 0;
+  return CIL_OK;
+}
+
+cil_status cil_sched_state(cil_handle *h, int32_t colony, cil_sched_info *out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "cil_sched_state: bad arguments");
+  if (!h->skin_mode) return fail(h, CIL_ERR_CONFIG, "cil_sched_state: the handle has no skin");
+  CUDA_TRY(h, cudaSetDevice(h->cfg.device));
+  SchedState q;
+  CUDA_TRY(h, cudaMemcpyAsync(&q, h->d_sched + colony, sizeof q, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  static_assert(kSchedFeatures == CIL_SCHED_FEATURES, "feature count");
+  for (int k = 0; k < kSchedFeatures; ++k) out->features[k] = q.features[k];
+  out->div_rate = q.div_rate;
+  out->apo_rate = q.apo_rate;
+  out->trip_share = q.trip_share;
+  out->nsched = q.nsched;
+  return CIL_OK;
+}
+
+cil_status cil_graph_info(cil_handle *h, int64_t *graph_steps, int64_t *graphs_captured) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (graph_steps) *graph_steps = h->graph_steps;
+  if (graphs_captured) *graphs_captured = h->graphs_captured;
+  return CIL_OK;
 }
 
 cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, double *events_ms,

@@ -55,7 +55,8 @@ __global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which
     int v = 0;
     if (c < B) {
       const int n = which == 0 ? cnt[c].nslot : (which == 1 ? cnt[c].nlive : cnt[c].ncell);
-      v = (n + kTile - 1) / kTile;
+      const int per = which == 2 ? kCellTile : kTile;
+      v = (n + per - 1) / per;
     }
     int total;
     const int ex = block_excl_scan(v, &total);
@@ -63,6 +64,29 @@ __global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which
     carry += total;
   }
   if (threadIdx.x == 0) tiles[B] = carry;
+}
+
+// New bin of a slot in the mixed form from FP32 data only: the home bin plus the whole
+// bin widths its updated local coordinate has moved (periodic wrap; clamped along walls).
+// shift[] receives the unwrapped change of the bin coordinate.
+template <int D>
+__device__ __forceinline__ void fast_bin(const ColonyConst &C, int home, const float4 &p, int *b, int *shift) {
+  int h[D];
+  bin_decode<D>(C, home, h);
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int sh = static_cast<int>(floorf(pk_c(p, d) * C.inv_bwf[d]));
+    int v = h[d] + sh;
+    if (C.periodic[d]) {
+      if (v < 0) v += C.ns[d];
+      if (v >= C.ns[d]) v -= C.ns[d];
+      shift[d] = sh;
+    } else {
+      v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
+      shift[d] = v - h[d];
+    }
+    b[d] = v;
+  }
 }
 
 template <int D>
@@ -75,11 +99,16 @@ __global__ void __launch_bounds__(kTile) k_bin_keys(RebuildArgs a) {
     if (s >= C.slot_base + a.cnt[c].nslot) continue;
     int k = -1;
     if (a.eid_in[s] >= 0) {
-      double x[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) x[d] = a.x_in[d * a.SS + s];
       int b[D];
-      bin_coords<D>(C, x, b);
+      if (a.exact) {
+        double x[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] = a.x_in[d * a.SS + s];
+        bin_coords<D>(C, x, b);
+      } else {
+        int sh[D];
+        fast_bin<D>(C, a.sbin_in[s], a.pk_in[s], b, sh);
+      }
       k = C.bin_base + bin_id<D>(C, b);
       atomicAdd(a.bcount + k, 1);
     }
@@ -88,8 +117,13 @@ __global__ void __launch_bounds__(kTile) k_bin_keys(RebuildArgs a) {
 }
 
 // per scan block: sum of kScanItems bin counts
+__device__ __forceinline__ bool skip_colony(const RebuildArgs &a, int c) {
+  return a.skin != nullptr && !a.skin[c].rebuild_now;
+}
+
 __global__ void __launch_bounds__(kTile) k_scan_partial(RebuildArgs a) {
   const int sb = blockIdx.x;
+  if (skip_colony(a, a.scan_col[sb])) return;
   const ColonyConst &C = a.col[a.scan_col[sb]];
   const int b0 = C.bin_base + (sb - C.scan_base) * kScanItems;
   const int4 v = reinterpret_cast<const int4 *>(a.bcount + b0)[threadIdx.x];
@@ -109,6 +143,7 @@ __global__ void __launch_bounds__(kTile) k_scan_partial(RebuildArgs a) {
 // one block per colony: exclusive scan of its scan-block sums; nlive = nslot = total
 __global__ void __launch_bounds__(kTile) k_scan_colony(RebuildArgs a) {
   const int c = blockIdx.x;
+  if (skip_colony(a, c)) return;
   const ColonyConst &C = a.col[c];
   const int nsb = C.nbins_pad / kScanItems;
   int carry = 0;
@@ -122,13 +157,14 @@ __global__ void __launch_bounds__(kTile) k_scan_colony(RebuildArgs a) {
   }
   if (threadIdx.x == 0) {
     a.cnt[c].nlive = carry;
-    a.cnt[c].nslot = carry;
+    if (a.permute) a.cnt[c].nslot = carry;
   }
 }
 
 // per scan block: bin ranges
 __global__ void __launch_bounds__(kTile) k_scan_final(RebuildArgs a) {
   const int sb = blockIdx.x;
+  if (skip_colony(a, a.scan_col[sb])) return;
   const ColonyConst &C = a.col[a.scan_col[sb]];
   const int b0 = C.bin_base + (sb - C.scan_base) * kScanItems + threadIdx.x * 4;
   const int4 v = *reinterpret_cast<const int4 *>(a.bcount + b0);
@@ -150,10 +186,11 @@ __global__ void __launch_bounds__(kTile) k_scatter(RebuildArgs a) {
   const int total = a.tiles_used[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_used, a.B, t);
+    if (skip_colony(a, c)) continue;
     const ColonyConst &C = a.col[c];
     const int s = C.slot_base + (t - a.tiles_used[c]) * kTile + threadIdx.x;
     // nslot was overwritten by the scan; the used-slot bound is the tile range itself and
-    // every slot past the old nslot carries key -1 from k_bin_keys' zero-filled tail.
+    // every slot past the old nslot carries key -1 (k_clear_tail_keys / the rebin kernel).
     if (s >= C.slot_base + C.slot_cap) continue;
     const int k = a.key[s];
     if (k < 0) continue;
@@ -163,18 +200,40 @@ __global__ void __launch_bounds__(kTile) k_scatter(RebuildArgs a) {
   }
 }
 
+// Orders each bin's entries by element id. Bins hold a few elements: up to 8 are sorted in
+// registers (insertion into a register array, then one coalesced write-back); larger bins
+// fall back to an in-place insertion sort.
 __global__ void __launch_bounds__(kTile) k_sort_bins(RebuildArgs a, int nbins_total) {
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins_total;
-       b += gridDim.x * blockDim.x) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins_total; b += gridDim.x * blockDim.x) {
     const int2 r = a.range[b];
-    for (int i = r.x + 1; i < r.y; ++i) {
-      const unsigned long long v = a.perm[i];
-      int j = i - 1;
-      while (j >= r.x && a.perm[j] > v) {
-        a.perm[j + 1] = a.perm[j];
-        --j;
+    const int n = r.y - r.x;
+    if (n < 2) continue;
+    if (n <= 8) {
+      unsigned long long v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = i < n ? a.perm[r.x + i] : ~0ull;
+#pragma unroll
+      for (int i = 1; i < 8; ++i)
+#pragma unroll
+        for (int k = i; k > 0; --k) {
+          const unsigned long long lo = v[k - 1] < v[k] ? v[k - 1] : v[k];
+          const unsigned long long hi = v[k - 1] < v[k] ? v[k] : v[k - 1];
+          v[k - 1] = lo;
+          v[k] = hi;
+        }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i < n) a.perm[r.x + i] = v[i];
+    } else {
+      for (int i = r.x + 1; i < r.y; ++i) {
+        const unsigned long long v = a.perm[i];
+        int j = i - 1;
+        while (j >= r.x && a.perm[j] > v) {
+          a.perm[j + 1] = a.perm[j];
+          --j;
+        }
+        a.perm[j + 1] = v;
       }
-      a.perm[j + 1] = v;
     }
   }
 }
@@ -190,6 +249,7 @@ __global__ void __launch_bounds__(kTile) k_gather(RebuildArgs a) {
     const unsigned long long v = a.perm[dst];
     const int src = static_cast<int>(v & 0xffffffffu);
     const int e = static_cast<int>(v >> 32);
+    const int g = e >> 1;
     double x[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -200,17 +260,39 @@ __global__ void __launch_bounds__(kTile) k_gather(RebuildArgs a) {
 #pragma unroll
       for (int d = 0; d < D; ++d) a.vel_out[d * a.SS + dst] = a.vel_in[d * a.SS + src];
     }
-    const double sg = a.sig_in[src];
-    a.sig_out[dst] = sg;
     a.eid_out[dst] = e;
     a.slot_of[e] = dst;
-    if (a.u_out) {
-      int b[D];
-      bin_coords<D>(C, x, b);
+    if (a.state_out) {
+      // skin mode: the new order is the bin order, so a bin's members are its own slots
+      a.state_out[dst] = kSlotNormal;
+      a.perm[dst] = (static_cast<unsigned long long>(static_cast<uint32_t>(e)) << 32) | static_cast<uint32_t>(dst);
+    }
+    const int nb = a.key[src] - C.bin_base;  // colony-local bin of the element
+    a.sbin_out[dst] = nb;
+    if (a.exact) {
+      a.cyc_out[dst] = make_int2(a.t0c[g], a.tswc[g]);
+      const double sg = a.sigma_c[e];
+      if (a.sig_out) a.sig_out[dst] = sg;
+      if (a.pk_out) {
+        int b[D];
+        bin_decode<D>(C, nb, b);
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(sg));
 #pragma unroll
-      for (int d = 0; d < D; ++d)
-        a.u_out[d * a.SS + dst] = static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]);
-      a.sigf_out[dst] = static_cast<float>(sg);
+        for (int d = 0; d < D; ++d) pk_set(p, d, static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]));
+        a.pk_out[dst] = p;
+      }
+    } else {
+      a.cyc_out[dst] = a.cyc_in[src];
+      if (a.sig_out) a.sig_out[dst] = a.sig_in[src];
+      if (a.pk_out) {
+        int b[D], sh[D];
+        const float4 q = a.pk_in[src];
+        fast_bin<D>(C, a.sbin_in[src], q, b, sh);
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, fabsf(q.w));  // every element is normal after a re-sort
+#pragma unroll
+        for (int d = 0; d < D; ++d) pk_set(p, d, pk_c(q, d) - static_cast<float>(sh[d]) * C.bwf[d]);
+        a.pk_out[dst] = p;
+      }
     }
   }
 }
@@ -233,17 +315,22 @@ void launch_tiles(const ColonyConst *, ColonyCounters *cnt, int B, int which, in
 }
 
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
-  // keys + histogram over the used slots (tiles_used must be current)
-  k_clear_tail_keys<<<dim3(1, a.B), kTile, 0, s>>>(a);
-  if (a.dim == 2)
-    k_bin_keys<2><<<grid_slots, kTile, 0, s>>>(a);
-  else
-    k_bin_keys<3><<<grid_slots, kTile, 0, s>>>(a);
+  // keys + histogram over the used slots (tiles_used must be current); a non-permuting
+  // rebuild (skin mode) gets its keys from the in-place rebin kernel instead
+  if (a.permute) {
+    k_clear_tail_keys<<<dim3(1, a.B), kTile, 0, s>>>(a);
+    if (a.dim == 2)
+      k_bin_keys<2><<<grid_slots, kTile, 0, s>>>(a);
+    else
+      k_bin_keys<3><<<grid_slots, kTile, 0, s>>>(a);
+  }
   k_scan_partial<<<a.nscan, kTile, 0, s>>>(a);
   k_scan_colony<<<a.B, kTile, 0, s>>>(a);
   k_scan_final<<<a.nscan, kTile, 0, s>>>(a);
   k_scatter<<<grid_slots, kTile, 0, s>>>(a);
-  k_sort_bins<<<(a.nscan * kScanItems + kTile - 1) / kTile, kTile, 0, s>>>(a, a.nscan * kScanItems);
+  if (!a.permute) return;  // the bin index (range + perm) is all a list rebuild needs
+  if (a.skin == nullptr)   // bin order by element id: deterministic sums (FP64 / plain forms)
+    k_sort_bins<<<(a.nscan * kScanItems + kTile - 1) / kTile, kTile, 0, s>>>(a, a.nscan * kScanItems);
   k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live));
   if (a.dim == 2)
     k_gather<2><<<grid_slots, kTile, 0, s>>>(a);

@@ -61,6 +61,49 @@ __device__ __forceinline__ void place(const ColonyConst &C, const double *master
   }
 }
 
+// exact bin and local coordinate of a freshly placed element (FP64, once per division)
+template <int D>
+__device__ __forceinline__ void place_slot(const EventArgs &a, const ColonyConst &C, int slot, const double *x) {
+  int b[D];
+  bin_coords<D>(C, x, b);
+  a.sbin[slot] = bin_id<D>(C, b);
+  if (a.pk) {
+    float4 p = a.pk[slot];
+#pragma unroll
+    for (int d = 0; d < D; ++d) pk_set(p, d, static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]));
+    a.pk[slot] = p;
+  }
+}
+
+// skin mode: a slot created or moved by a division joins the colony's fresh set and the
+// fresh list of its bin. The lists carry the colony's rebuild count as an epoch, so a list
+// rebuild empties them without touching memory. A slot moved a second time before the next
+// rebuild would sit in the list of its old bin: the colony rebuilds at the next step instead.
+__device__ __forceinline__ void mark_fresh(const EventArgs &a, const ColonyConst &C, int c, int slot, bool is_new,
+                                           int D) {
+  if (!a.state) return;
+  ColonySkin &S = a.skin[c];
+  if (is_new || a.state[slot] != kSlotFresh) {
+    const int idx = atomicAdd(&S.nfresh, 1);
+    if (idx < kFreshCap) {
+      a.fresh[c * kFreshCap + idx] = slot;
+      const unsigned long long ent =
+          (static_cast<unsigned long long>(static_cast<unsigned>(S.nrebuild)) << 32) | static_cast<unsigned>(slot);
+      a.fnext[slot] = atomicExch(&a.fhead[C.bin_base + a.sbin[slot]], ent);
+    } else {
+      atomicOr(&S.need, 2);
+    }
+  } else {
+    atomicOr(&S.need, 2);
+  }
+  a.state[slot] = kSlotFresh;
+  a.ncnt[slot] = 0;
+  float4 p = a.pk[slot];
+  p.w = -fabsf(p.w);  // skipped by the lists of normal elements
+  a.pk[slot] = p;
+  for (int d = 0; d < D; ++d) a.uref[d * a.SS + slot] = pk_c(p, d);
+}
+
 template <int D>
 __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int i, int k,
                             const double *dir_m, const double *dir_d, int tsw_d, int tsw_m,
@@ -86,12 +129,33 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
     a.x[d * SS + s0] = d0[d];
     a.x[d * SS + s0 + 1] = d1[d];
   }
-  a.sig[s0] = a.sig[sb];
-  a.sig[s0 + 1] = a.sig[sf];
+  // daughter diameters copied from the mother (canonical and binned copies)
+  a.sigma_c[2 * gk] = a.sigma_c[2 * g];
+  a.sigma_c[2 * gk + 1] = a.sigma_c[2 * g + 1];
+  if (a.sig) {
+    a.sig[s0] = a.sig[sb];
+    a.sig[s0 + 1] = a.sig[sf];
+  }
+  if (a.pk) {
+    a.pk[s0].w = a.pk[sb].w;
+    a.pk[s0 + 1].w = a.pk[sf].w;
+  }
   a.eid[s0] = 2 * gk;
   a.eid[s0 + 1] = 2 * gk + 1;
   a.slot_of[2 * gk] = s0;
   a.slot_of[2 * gk + 1] = s0 + 1;
+  place_slot<D>(a, C, sb, m0);
+  place_slot<D>(a, C, sf, m1);
+  place_slot<D>(a, C, s0, d0);
+  place_slot<D>(a, C, s0 + 1, d1);
+  mark_fresh(a, C, c, sb, false, D);
+  mark_fresh(a, C, c, sf, false, D);
+  mark_fresh(a, C, c, s0, true, D);
+  mark_fresh(a, C, c, s0 + 1, true, D);
+  a.cyc[sb] = make_int2(a.ts, tsw_m);
+  a.cyc[sf] = make_int2(a.ts, tsw_m);
+  a.cyc[s0] = make_int2(a.ts, tsw_d);
+  a.cyc[s0 + 1] = make_int2(a.ts, tsw_d);
   if (a.vel) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -153,15 +217,25 @@ __device__ void division_draws(const EventArgs &a, int g, double *dir_m, double 
   span_m = sm >= 1 ? sm : 1;
 }
 
-__global__ void __launch_bounds__(kTile) k_div_count(EventArgs a) {
+// division detection: kCellItems consecutive cells per thread
+__global__ void __launch_bounds__(kTile) k_div_count(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
   const int total = a.tiles_cell[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_cell, a.B, t);
     const ColonyConst &C = a.col[c];
-    const int i = (t - a.tiles_cell[c]) * kTile + threadIdx.x;
-    const bool due = C.divide && i < a.cnt[c].ncell && a.tsw[C.cell_base + i] == a.ts;
-    const int n = __syncthreads_count(due);
-    if (threadIdx.x == 0) a.tile_count[t] = n;
+    const int n = a.cnt[c].ncell;
+    const int i0 = (t - a.tiles_cell[c]) * kCellTile + threadIdx.x * kCellItems;
+    int due = 0;
+    if (C.divide) {
+#pragma unroll
+      for (int q = 0; q < kCellItems; ++q)
+        due += (i0 + q < n && a.tsw[C.cell_base + i0 + q] == a.ts) ? 1 : 0;
+    }
+    int tot;
+    block_excl_scan_ev(due, &tot);
+    if (threadIdx.x == 0) a.tile_count[t] = tot;
   }
 }
 
@@ -180,7 +254,11 @@ __global__ void __launch_bounds__(kTile) k_div_scan(EventArgs a) {
   }
   if (threadIdx.x == 0) {
     ColonyCounters &K = a.cnt[c];
-    const int room = C.cell_cap - K.ncell;
+    // room for the cells and for their two element slots each (skin mode appends daughters
+    // behind removed elements until the next slot re-sort)
+    const int room_cells = C.cell_cap - K.ncell;
+    const int room_slots = (C.slot_cap - K.nslot) / 2;
+    const int room = room_cells < room_slots ? room_cells : room_slots;
     int allowed = carry < room ? carry : room;
     if (allowed < 0) allowed = 0;
     if (allowed < carry) K.err |= kErrCap;
@@ -191,45 +269,35 @@ __global__ void __launch_bounds__(kTile) k_div_scan(EventArgs a) {
 }
 
 template <int D>
-__global__ void __launch_bounds__(kTile) k_div_apply(EventArgs a) {
+__global__ void __launch_bounds__(kTile) k_div_apply(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
   const int total = a.tiles_cell[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_cell, a.B, t);
     const ColonyConst &C = a.col[c];
     const ColonyCounters &K = a.cnt[c];
     const int n = K.ncell;
-    const int i = (t - a.tiles_cell[c]) * kTile + threadIdx.x;
-    const bool live = i < n;
-    const bool due = C.divide && live && a.tsw[C.cell_base + i] == a.ts;
-    int tot;
-    const int rank = a.tile_off[t] + block_excl_scan_ev(due ? 1 : 0, &tot);
-    bool daughter = false;
-    if (due && rank < K.ndiv_allowed) {
-      double dm[D], dd[D];
-      int span_d, span_m;
-      division_draws<D>(a, C.cell_base + i, dm, dd, span_d, span_m, C);
-      divide_cell<D>(a, C, c, i, n + rank, dm, dd, a.ts + span_d, a.ts + span_m, K.nslot, rank);
-      daughter = true;
+    const int i0 = (t - a.tiles_cell[c]) * kCellTile + threadIdx.x * kCellItems;
+    bool due[kCellItems];
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kCellItems; ++q) {
+      due[q] = C.divide && i0 + q < n && a.tsw[C.cell_base + i0 + q] == a.ts;
+      cnt += due[q] ? 1 : 0;
     }
-    if (C.apop_p > 0.0) {
-      if (live) {
-        const int g = C.cell_base + i;
-        const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngApo, 0u,
-                                      a.seed_lo, a.seed_hi);
-        if (uniform53(r.v[0], r.v[1]) <= C.apop_p) {
-          const int idx = atomicAdd(&a.cnt[c].ndead, 1);
-          if (idx < kDeadCap) a.dead[c * kDeadCap + idx] = i;
-        }
+    int tot;
+    int rank = a.tile_off[t] + block_excl_scan_ev(cnt, &tot);
+#pragma unroll
+    for (int q = 0; q < kCellItems; ++q) {
+      if (!due[q]) continue;
+      if (rank < K.ndiv_allowed) {
+        double dm[D], dd[D];
+        int span_d, span_m;
+        division_draws<D>(a, C.cell_base + i0 + q, dm, dd, span_d, span_m, C);
+        divide_cell<D>(a, C, c, i0 + q, n + rank, dm, dd, a.ts + span_d, a.ts + span_m, K.nslot, rank);
       }
-      if (daughter) {
-        const int gk = C.cell_base + n + rank;
-        const u32x4 r = philox4x32_10(static_cast<uint32_t>(gk), static_cast<uint32_t>(a.ts), kRngApo, 0u,
-                                      a.seed_lo, a.seed_hi);
-        if (uniform53(r.v[0], r.v[1]) <= C.apop_p) {
-          const int idx = atomicAdd(&a.cnt[c].ndead, 1);
-          if (idx < kDeadCap) a.dead[c * kDeadCap + idx] = n + rank;
-        }
-      }
+      ++rank;
     }
   }
 }
@@ -238,6 +306,8 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
   const int gd = C.cell_base + dst, gs = C.cell_base + src;
   a.t0[gd] = a.t0[gs];
   a.tsw[gd] = a.tsw[gs];
+  a.sigma_c[2 * gd] = a.sigma_c[2 * gs];
+  a.sigma_c[2 * gd + 1] = a.sigma_c[2 * gs + 1];
   for (int j = 0; j < 2; ++j) {
     const int sl = a.slot_of[2 * gs + j];
     a.eid[sl] = 2 * gd + j;
@@ -253,7 +323,9 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
 }
 
 // one block per colony: commit the divisions, then swap-with-last removal of the dead
-__global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
+__global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
   __shared__ int sd[kDeadCap];
   __shared__ int s_n1, s_k;
   const int c = blockIdx.x;
@@ -264,12 +336,25 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
     K.ncell += add;
     K.nslot += 2 * add;
     K.ndiv_total += add;
-    int k = K.ndead;
-    if (k > kDeadCap) {
-      K.err |= kErrCap;
-      k = kDeadCap;
-    }
     s_n1 = K.ncell;
+    // Philox mode: every cell (daughters included) dies with probability p this step
+    // (CIL.cu:627-649); drawn as k ~ Binomial(n, p) by inversion and a uniformly random
+    // k-subset, the same distribution without a draw per cell
+    int k = 0;
+    if (C.apop_p > 0.0 && s_n1 > 0) {
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(c), static_cast<uint32_t>(a.ts), kRngApo, 0u,
+                                    a.seed_lo, a.seed_hi);
+      const double u = uniform53(r.v[0], r.v[1]);
+      const double nn = static_cast<double>(s_n1), p = C.apop_p;
+      double pk = exp(nn * log1p(-p)), cdf = pk;
+      while (u > cdf && k < s_n1 && k < kDeadCap) {
+        pk *= (nn - k) / (k + 1.0) * (p / (1.0 - p));
+        cdf += pk;
+        ++k;
+        if (pk < 1e-300 && cdf < u && k > nn * p + 40.0 * sqrt(nn * p + 1.0)) break;
+      }
+      if (k >= kDeadCap) K.err |= kErrCap;
+    }
     s_k = k;
   }
   __syncthreads();
@@ -277,32 +362,79 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
   if (k == 0) return;
   int P = 1;
   while (P < k) P <<= 1;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) sd[i] = i < k ? a.dead[c * kDeadCap + i] : 0x7fffffff;
+  // distinct uniform picks: draw, sort, redraw the duplicates (rare: about k^2 / 2n)
+  __shared__ int s_dup;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sd[i] = i < k ? -1 : 0x7fffffff;
   __syncthreads();
-  // bitonic sort (ascending) of the dead list
-  for (int size = 2; size <= P; size <<= 1)
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        const int l = i ^ stride;
-        if (l > i) {
-          const bool up = (i & size) == 0;
-          const int x = sd[i], y = sd[l];
-          if ((x > y) == up) {
-            sd[i] = y;
-            sd[l] = x;
+  for (int attempt = 0; attempt < 16; ++attempt) {
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+      if (sd[i] == -1) {
+        const u32x4 r = philox4x32_10(static_cast<uint32_t>(i) | (static_cast<uint32_t>(attempt) << 24),
+                                      static_cast<uint32_t>(a.ts), kRngApoPick, static_cast<uint32_t>(c),
+                                      a.seed_lo, a.seed_hi);
+        const int v = static_cast<int>(uniform53(r.v[0], r.v[1]) * n1);
+        sd[i] = v < n1 ? v : n1 - 1;
+      }
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int i = threadIdx.x; i < P; i += blockDim.x) {
+          const int l = i ^ stride;
+          if (l > i) {
+            const bool up = (i & size) == 0;
+            const int x = sd[i], y = sd[l];
+            if ((x > y) == up) {
+              sd[i] = y;
+              sd[l] = x;
+            }
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
+    if (threadIdx.x == 0) {
+      int dup = 0, last = sd[0];
+      for (int i = 1; i < k; ++i) {
+        if (sd[i] == last) {
+          sd[i] = -1;  // redraw this copy
+          dup = 1;
+        } else {
+          last = sd[i];
+        }
+      }
+      s_dup = dup;
     }
+    __syncthreads();
+    if (!s_dup) break;
+  }
+  if (s_dup) {
+    // still duplicated after 16 rounds (practically impossible): keep the distinct ones
+    if (threadIdx.x == 0) {
+      int w = 0;
+      for (int i = 0; i < k; ++i)
+        if (sd[i] >= 0) sd[w++] = sd[i];
+      for (int i = w; i < P; ++i) sd[i] = 0x7fffffff;
+      s_k = w;
+    }
+    __syncthreads();
+    // the -1 holes were dropped; the survivors stay ascending
+  }
+  const int kk = s_k;
   // tombstones
-  for (int r = threadIdx.x; r < k; r += blockDim.x) {
+  for (int r = threadIdx.x; r < kk; r += blockDim.x) {
     const int g = C.cell_base + sd[r];
-    a.eid[a.slot_of[2 * g]] = -1;
-    a.eid[a.slot_of[2 * g + 1]] = -1;
+    const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+    a.eid[s0] = -1;
+    a.eid[s1] = -1;
+    if (a.state) {
+      a.state[s0] = kSlotDead;
+      a.state[s1] = kSlotDead;
+      a.pk[s0].w = -fabsf(a.pk[s0].w);
+      a.pk[s1].w = -fabsf(a.pk[s1].w);
+    }
   }
   __syncthreads();
-  const int n2 = n1 - k;
+  const int n2 = n1 - kk;
   // movers: live cells of [n2, n1) in ascending order, paired with holes sd[0..h)
   __shared__ int s_carry;
   if (threadIdx.x == 0) s_carry = 0;
@@ -311,7 +443,7 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
     const int q = base + threadIdx.x;
     bool live = false;
     if (q < n1) {
-      int lo = 0, hi = k - 1;
+      int lo = 0, hi = kk - 1;
       bool found = false;
       while (lo <= hi) {
         const int mid = (lo + hi) >> 1;
@@ -346,17 +478,23 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a, int D) {
   }
   if (threadIdx.x == 0) {
     K.ncell = n2;
-    K.napo_total += k;
+    K.napo_total += kk;
   }
 }
 
 // oracle mode: divisions in the host's order with host-drawn axes and cycle lengths
 template <int D>
-__global__ void k_div_list(EventArgs a, int c, int n0, int ndiv, const int *mothers, const double *dirs,
+__global__ void k_div_list(EventArgs a_, int c, int n0, int ndiv, const int *mothers, const double *dirs,
                            const int *tsws) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= ndiv) return;
   const ColonyConst &C = a.col[c];
+  if (a.cnt[c].nslot + 2 * (r + 1) > C.slot_cap) {  // no slot left for the daughter
+    atomicOr(&a.cnt[c].err, kErrCap);
+    return;
+  }
   divide_cell<D>(a, C, c, mothers[r], n0 + r, dirs + (2 * r) * D, dirs + (2 * r + 1) * D, tsws[2 * r],
                  tsws[2 * r + 1], a.cnt[c].nslot, r);
 }
@@ -377,8 +515,15 @@ __global__ void k_apo_ops(EventArgs a, int c, int ndiv, int nops, const int *ops
       return;
     }
     const int g = C.cell_base + i;
-    a.eid[a.slot_of[2 * g]] = -1;
-    a.eid[a.slot_of[2 * g + 1]] = -1;
+    const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+    a.eid[s0] = -1;
+    a.eid[s1] = -1;
+    if (a.state) {
+      a.state[s0] = kSlotDead;
+      a.state[s1] = kSlotDead;
+      a.pk[s0].w = -fabsf(a.pk[s0].w);
+      a.pk[s1].w = -fabsf(a.pk[s1].w);
+    }
     if (i != last) move_cell(a, C, i, last, D);
     K.ncell -= 1;
     K.napo_total += 1;
@@ -386,16 +531,14 @@ __global__ void k_apo_ops(EventArgs a, int c, int ndiv, int nops, const int *ops
 }
 
 template <int D>
-__global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, const double *pos,
-                         const double *sigma, double *x, double *sig, int *eid, int *slot_of,
-                         ColonyCounters *cnt) {
+__global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, const double *pos, double *x,
+                         int *eid, int *slot_of, ColonyCounters *cnt) {
   const ColonyConst &C = col[c];
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < 2 * ncells) {
     const int slot = C.slot_base + e;
 #pragma unroll
     for (int d = 0; d < D; ++d) x[d * SS + slot] = pos[static_cast<size_t>(e) * D + d];
-    sig[slot] = sigma[e];
     eid[slot] = 2 * C.cell_base + e;
     slot_of[2 * C.cell_base + e] = slot;
   }
@@ -437,7 +580,7 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
       com[d] = C.periodic[d] ? fmod(m + r0 + C.box[d], C.box[d]) : m + r0;
       v[d] = a.vel ? 0.5 * (a.vel[d * a.SS + s0] + a.vel[d * a.SS + s1]) : 0.0;
     }
-    const double q0 = a.sig[s0] * 0.5, q1 = a.sig[s1] * 0.5;
+    const double q0 = a.sigma_c[2 * g] * 0.5, q1 = a.sigma_c[2 * g + 1] * 0.5;
     area = 3.14159265358979323846 * q0 * q0 + 3.14159265358979323846 * q1 * q1;
     if (reset) {
 #pragma unroll
@@ -477,7 +620,12 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
     for (int q = 0; q < 4; ++q) partials[blockIdx.x * 4 + q] = red[q][0];
 }
 
+// the device step counter moves past the force step (before the events read it)
+__global__ void k_advance_ts(int *ts) { *ts += 1; }
+
 }  // namespace
+
+void launch_advance_ts(int *ts_dev, cudaStream_t s) { k_advance_ts<<<1, 1, 0, s>>>(ts_dev); }
 
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
   k_div_count<<<grid_cells, kTile, 0, s>>>(a);
@@ -505,14 +653,14 @@ void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops,
 }
 
 void launch_upload_scatter(const ColonyConst *col, int colony, int ncells, int dim, size_t SS,
-                           const double *pos, const double *sigma, double *x, double *sig,
-                           int *eid, int *slot_of, ColonyCounters *cnt, cudaStream_t s) {
+                           const double *pos, double *x, int *eid, int *slot_of, ColonyCounters *cnt,
+                           cudaStream_t s) {
   const int n = 2 * ncells > 0 ? 2 * ncells : 1;
   const int blocks = (n + kTile - 1) / kTile;
   if (dim == 2)
-    k_upload<2><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, sigma, x, sig, eid, slot_of, cnt);
+    k_upload<2><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, x, eid, slot_of, cnt);
   else
-    k_upload<3><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, sigma, x, sig, eid, slot_of, cnt);
+    k_upload<3><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, x, eid, slot_of, cnt);
 }
 
 void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,

@@ -1,4 +1,4 @@
-// Fused force + integrate kernel: one thread per binned element.
+// Fused force + integrate kernels: one thread per binned element.
 //
 // Per element, in the reference's accumulation order (calculForcesPressure,
 // CIL.cu:999-1007):
@@ -10,11 +10,12 @@
 //   finally the overdamped Euler-Maruyama update with the reference's periodic wrap
 //   (updatePositions, CIL.cu:858-875; BoundingBox::updatePos, Utils.hpp:561-566).
 //
-// Precision forms:
-//   FP64   positions, displacements and force arithmetic in FP64
-//   MIXED  displacements from FP32 bin-local coordinates (written by the rebuild) plus the
-//          FP32 bin offset, FP32 force law, FP64 accumulation into the element force and
-//          FP64 integration and wrap.
+// FP64 form (k_force_fp64): everything in FP64; the parity path.
+// Mixed form (k_force_mixed): GB300 issues FP64 at about 1/64 of the FP32 rate, so every
+//   per-element operation runs in FP32 on bin-local coordinates (the element's FP32 offset
+//   from its bin origin plus the FP32 offset between bin origins, exact for a periodic
+//   image) and only the position accumulation stays FP64: one FP64 add per axis, with the
+//   float->double conversion and the wrap test done in integer arithmetic.
 #include "cil_internal.cuh"
 
 namespace cil {
@@ -42,8 +43,27 @@ __device__ __forceinline__ bool neighbor_bin(const ColonyConst &C, const int *bi
   return true;
 }
 
-template <int D, int LAW, int PREC>
-__global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
+template <int D>
+__device__ __forceinline__ bool neighbor_bin_i(const ColonyConst &C, const int *bi, const int *o, int *nb) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    int v = bi[d] + o[d];
+    if (v < 0) {
+      if (!C.periodic[d]) return false;
+      v += C.ns[d];
+    } else if (v >= C.ns[d]) {
+      if (!C.periodic[d]) return false;
+      v -= C.ns[d];
+    }
+    nb[d] = v;
+  }
+  return true;
+}
+
+template <int D, int LAW>
+__global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
+  ForceArgs a = a_;
+  a.ts = *a_.ts_dev;
   const int total = a.tiles_live[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_live, a.B, t);
@@ -54,6 +74,7 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
 
     const size_t SS = a.SS;
     const int e = a.eid[s];
+    if (e < 0) continue;
     const int g = e >> 1, j = e & 1;
     double xi[D];
 #pragma unroll
@@ -81,9 +102,9 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
         const double r = sqrt(r2);
         double rest = C.rest0;
         if (C.divide) {
-          const int t0 = a.t0[g], tsw = a.tsw[g];
-          const int span = tsw - t0;
-          double frac = span > 0 ? static_cast<double>(a.ts - t0) / static_cast<double>(span) : 1.0;
+          const int2 cy = a.cyc[s];
+          const int span = cy.y - cy.x;
+          double frac = span > 0 ? static_cast<double>(a.ts - cy.x) / static_cast<double>(span) : 1.0;
           frac = fmin(1.0, fmax(0.0, frac));
           rest = C.rest0 + (C.rest1 - C.rest0) * frac;
         }
@@ -120,14 +141,12 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
     }
 
     // ---- pair forces
-    int bi[D];
-    bin_coords<D>(C, xi, bi);
+    const double eps = C.epsilon, rcs = C.rcut_scale;
     if (C.single_bin) {
       // one bin: all elements, minimum image as BoundingBox::distance (Utils.hpp:536-544)
-      const double eps = C.epsilon, rcs = C.rcut_scale;
       for (int tt = C.slot_base; tt < C.slot_base + nlive; ++tt) {
         const int ej = a.eid[tt];
-        if ((ej >> 1) == g) continue;
+        if (ej < 0 || (ej >> 1) == g) continue;
         double dx[D];
         double r2 = 0.0;
 #pragma unroll
@@ -143,8 +162,9 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
           for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
         }
       }
-    } else if (PREC == CIL_PREC_FP64) {
-      const double eps = C.epsilon, rcs = C.rcut_scale;
+    } else {
+      int bi[D];
+      bin_decode<D>(C, a.sbin[s], bi);
       int o[3] = {-1, -1, -1};
       for (o[0] = -1; o[0] <= 1; ++o[0])
         for (o[1] = -1; o[1] <= 1; ++o[1])
@@ -155,7 +175,7 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
             const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
             for (int tt = r.x; tt < r.y; ++tt) {
               const int ej = __ldg(a.eid + tt);
-              if ((ej >> 1) == g) continue;
+              if (ej < 0 || (ej >> 1) == g) continue;
               double dx[D];
               double r2 = 0.0;
 #pragma unroll
@@ -170,45 +190,6 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
               }
             }
           }
-    } else {
-      const float eps = static_cast<float>(C.epsilon), rcs = static_cast<float>(C.rcut_scale);
-      float ui[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) ui[d] = a.u[d * SS + s];
-      const float sif = a.sigf[s];
-      float Fp[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) Fp[d] = 0.0f;
-      int o[3] = {-1, -1, -1};
-      for (o[0] = -1; o[0] <= 1; ++o[0])
-        for (o[1] = -1; o[1] <= 1; ++o[1])
-          for (o[2] = (D == 3 ? -1 : 0); o[2] <= (D == 3 ? 1 : 0); ++o[2]) {
-            int nb[D];
-            double shift[D];
-            if (!neighbor_bin<D>(C, bi, o, nb, shift)) continue;
-            float off[D];
-#pragma unroll
-            for (int d = 0; d < D; ++d) off[d] = static_cast<float>(o[d]) * C.bwf[d] - ui[d];
-            const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
-            for (int tt = r.x; tt < r.y; ++tt) {
-              const int ej = __ldg(a.eid + tt);
-              if ((ej >> 1) == g) continue;
-              float dx[D];
-              float r2 = 0.0f;
-#pragma unroll
-              for (int d = 0; d < D; ++d) {
-                dx[d] = __ldg(a.u + d * SS + tt) + off[d];
-                r2 += dx[d] * dx[d];
-              }
-              float f0;
-              if (pair_force<LAW, float>(r2, sif, __ldg(a.sigf + tt), eps, rcs, f0)) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) Fp[d] += f0 * dx[d];
-              }
-            }
-          }
-#pragma unroll
-      for (int d = 0; d < D; ++d) F[d] += static_cast<double>(Fp[d]);
     }
 
     // ---- checks, integration, outputs
@@ -244,38 +225,552 @@ __global__ void __launch_bounds__(kTile) k_force(ForceArgs a) {
   }
 }
 
+// ---------------------------------------------------------------- mixed-precision pieces
+
+// Intra-cell spring + motility, walls and passive noise of one element (FP32), in the
+// reference's order. ui / bi: the element's packed coordinates and home bin.
+template <int D>
+__device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const ColonyConst &C, int s, int e,
+                                                 const float *ui, const int *bi, float si, float *F) {
+  const int g = e >> 1, j = e & 1;
+  {
+    const int ps = a.slot_of[e ^ 1];
+    const float4 pp = a.pk[ps];
+    int bp[D];
+    bin_decode<D>(C, a.sbin[ps], bp);
+    float rij[D];
+    float r2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      float v = pk_c(pp, d) - ui[d];
+      if (C.single_bin) {
+        if (C.periodic[d]) v -= rintf(v * C.inv_bwf[d]) * C.bwf[d];
+      } else {
+        int db = bp[d] - bi[d];
+        if (C.periodic[d]) {
+          if (db > (C.ns[d] >> 1)) db -= C.ns[d];
+          if (db < -(C.ns[d] >> 1)) db += C.ns[d];
+        }
+        v += static_cast<float>(db) * C.bwf[d];
+      }
+      rij[d] = (j == 0) ? v : -v;  // r1 - r0
+      r2 += rij[d] * rij[d];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = 0.0f;
+    if (r2 > 0.0f) {
+      const float rinv = rsqrtf(r2);
+      float rest = C.rest0_f;
+      if (C.divide) {
+        const int2 cy = a.cyc[s];
+        const int span = cy.y - cy.x;
+        float frac = span > 0 ? __fdividef(static_cast<float>(a.ts - cy.x), static_cast<float>(span)) : 1.0f;
+        frac = fminf(1.0f, fmaxf(0.0f, frac));
+        rest = C.rest0_f + (C.rest1_f - C.rest0_f) * frac;
+      }
+      const float sp = C.kappa_f * (r2 * rinv - rest);
+      const float coef = ((j == 0) ? (sp - C.motility_f[0]) : (C.motility_f[1] - sp)) * rinv;
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
+    }
+  }
+  if (C.nwalls > 0) {
+    const float z = static_cast<float>(bi[D - 1]) * C.bwf[D - 1] + ui[D - 1];
+    const float rad = 0.5f * si;
+    for (int w = 0; w < C.nwalls; ++w) {
+      const float dir = static_cast<float>(C.wall_dir[w]);
+      const float delta = rad - dir * (z - C.wall_pos_f[w]);
+      if (delta > 0.0f) F[D - 1] += dir * C.wall_E_f * delta * (delta * rsqrtf(delta));
+    }
+  }
+  if (a.noise_mode == 1) {
+    // Box-Muller with the fast log / sincos
+    const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
+    const u32x4 r = philox4x32_10(id, static_cast<uint32_t>(a.ts), kRngNoise, 0u, a.seed_lo, a.seed_hi);
+    const float amp = C.zeta_f[j] * C.amp_f;
+#pragma unroll
+    for (int h = 0; h < (D + 1) / 2; ++h) {
+      const float u1 = static_cast<float>((r.v[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;
+      const float u2 = static_cast<float>(r.v[2 * h + 1] >> 8) * 5.9604644775390625e-08f;
+      const float m = fmaxf(-2.0f * __logf(u1), 0.0f);
+      const float rad = m * rsqrtf(fmaxf(m, 1e-30f));  // sqrt(m), 0 when u1 == 1
+      float sn, cs;
+      __sincosf(6.2831853071795865f * u2, &sn, &cs);
+      F[2 * h] += amp * rad * cs;
+      if (2 * h + 1 < D) F[2 * h + 1] += amp * rad * sn;
+    }
+  } else if (a.noise_mode == 2) {
+    const size_t base = static_cast<size_t>(C.noise_per_cell ? g : e) * D;
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] += C.zeta_f[j] * static_cast<float>(a.noise[base + d]);
+  }
+}
+
+// Checks, outputs and the Euler-Maruyama update of one element: one FP64 add per axis, the
+// float->double conversion and the periodic wrap in integer arithmetic. Writes the next
+// packed record (w carried over) and returns the FP32 step in dx.
+template <int D>
+__device__ __forceinline__ void mixed_integrate(const ForceArgs &a, const ColonyConst &C, int c, int s, int j,
+                                                const float *ui, float w, const float *F, float *dx) {
+  bool finite = true;
+#pragma unroll
+  for (int d = 0; d < D; ++d) finite = finite && isfinite(F[d]);
+  if (!finite) atomicOr(&a.cnt[c].err, kErrNan);
+  if (a.frc) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) a.frc[d * a.SS + s] = static_cast<double>(F[d]);
+  }
+  if (!a.integrate) return;
+  const float temp = C.temp_f[j];
+  bool inside = true;
+  float4 pn = make_float4(0.0f, 0.0f, 0.0f, w);
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const float dxf = temp * F[d];
+    double xn = a.x_in[d * a.SS + s] + f2d_exact(dxf);
+    long long xb = __double_as_longlong(xn);
+    const long long lb = __double_as_longlong(C.box[d]);
+    if (C.periodic[d]) {
+      // non-negative doubles order like their bit patterns: wrap tests without FP64
+      // compares; a tiny negative x + L that rounds to L ends at 0 like fmod(x + L, L)
+      if (xb < 0) {
+        xn = (xb & 0x7fffffffffffffffll) ? xn + C.box[d] : 0.0;
+        xb = __double_as_longlong(xn);
+      }
+      if (xb >= lb) xn -= C.box[d];
+    } else {
+      inside = inside && xb >= 0 && xb < lb;
+    }
+    a.x_out[d * a.SS + s] = xn;
+    pk_set(pn, d, ui[d] + dxf);
+    dx[d] = dxf;
+  }
+  a.pk_next[s] = pn;
+  if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
+  if (a.vel) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) a.vel[d * a.SS + s] = static_cast<double>(F[d] * C.mu_f[j]);
+  }
+}
+
+// Mixed-precision step without lists, one CTA per tile of kTile consecutive binned elements:
+//  1. each thread: its element's intra-cell, wall and noise force (FP32) and the ranges of
+//     its 3^d neighbour bins, staged in shared memory with the candidate count;
+//  2. a block scan turns the counts into one list of (element, candidate) pairs and every
+//     thread evaluates an equal contiguous chunk of it, so lanes stay converged whatever
+//     the bin occupancies; partial sums are added into the element's shared accumulator;
+//  3. each thread adds its element's pair force and integrates.
 template <int D, int LAW>
-void launch_dl(const ForceArgs &a, int prec, int grid, int block, cudaStream_t s) {
-  (void)block;
-  if (prec == CIL_PREC_FP64)
-    k_force<D, LAW, CIL_PREC_FP64><<<grid, kTile, 0, s>>>(a);
-  else
-    k_force<D, LAW, CIL_PREC_MIXED><<<grid, kTile, 0, s>>>(a);
+__global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
+  ForceArgs a = a_;
+  a.ts = *a_.ts_dev;
+  constexpr int NB = (D == 2) ? 9 : 27;
+  extern __shared__ int smem[];
+  int *s_start = smem;                       // [NB][kTile]
+  int *s_cnt = s_start + NB * kTile;         // [NB][kTile]
+  int *s_off = s_cnt + NB * kTile;           // [kTile + 1]
+  int *s_g = s_off + kTile + 1;              // [kTile]
+  float *s_u = reinterpret_cast<float *>(s_g + kTile);  // [D][kTile]
+  float *s_si = s_u + D * kTile;             // [kTile]
+  float *s_F = s_si + kTile;                 // [D][kTile]
+  __shared__ int s_total;
+
+  const int tid = threadIdx.x;
+  const int total = a.tiles_live[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_live, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int s = C.slot_base + (t - a.tiles_live[c]) * kTile + tid;
+    const int nlive = a.cnt[c].nlive;
+    const int e = s < C.slot_base + nlive ? a.eid[s] : -1;
+    const bool live = e >= 0;
+    const int g = live ? (e >> 1) : -1;
+    const int j = e & 1;
+
+    float ui[D], F[D];
+    float si = 0.0f, w = 0.0f;
+    int bi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      ui[d] = 0.0f;
+      F[d] = 0.0f;
+      bi[d] = 0;
+    }
+    int ncand = 0;
+    if (live) {
+      const float4 pi = a.pk[s];
+#pragma unroll
+      for (int d = 0; d < D; ++d) ui[d] = pk_c(pi, d);
+      w = pi.w;
+      si = fabsf(w);
+      bin_decode<D>(C, a.sbin[s], bi);
+      mixed_own_forces<D>(a, C, s, e, ui, bi, si, F);
+      // ---- neighbour bin ranges
+      if (!C.single_bin) {
+#pragma unroll
+        for (int o = 0; o < NB; ++o) {
+          int off[3] = {o / (D == 2 ? 3 : 9) - 1, (D == 2 ? o % 3 : (o / 3) % 3) - 1, (D == 2 ? 0 : o % 3 - 1)};
+          int nb[D];
+          int st = 0, n = 0;
+          if (neighbor_bin_i<D>(C, bi, off, nb)) {
+            const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
+            st = r.x;
+            n = r.y - r.x;
+          }
+          s_start[o * kTile + tid] = st;
+          s_cnt[o * kTile + tid] = n;
+          ncand += n;
+        }
+      }
+    }
+    if (!live || C.single_bin) {
+#pragma unroll
+      for (int o = 0; o < NB; ++o) s_cnt[o * kTile + tid] = 0;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      s_u[d * kTile + tid] = ui[d];
+      s_F[d * kTile + tid] = 0.0f;
+    }
+    s_si[tid] = si;
+    s_g[tid] = g;
+    // ---- pair list offsets
+    {
+      const int lane = tid & 31, wid = tid >> 5;
+      int inc = ncand;
+#pragma unroll
+      for (int q = 1; q < 32; q <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, q);
+        if (lane >= q) inc += v;
+      }
+      __shared__ int ws[kTile / 32];
+      if (lane == 31) ws[wid] = inc;
+      __syncthreads();
+      if (wid == 0) {
+        int wv = lane < kTile / 32 ? ws[lane] : 0;
+#pragma unroll
+        for (int q = 1; q < 32; q <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, wv, q);
+          if (lane >= q) wv += v;
+        }
+        if (lane < kTile / 32) ws[lane] = wv;
+        if (lane == kTile / 32 - 1) s_total = wv;
+      }
+      __syncthreads();
+      s_off[tid] = (wid > 0 ? ws[wid - 1] : 0) + inc - ncand;
+      __syncthreads();
+    }
+    // ---- pair chunk of this thread
+    const int npairs = s_total;
+    const float eps = C.eps_f, rcs = C.rcs_f;
+    if (npairs > 0) {
+      const int q = (npairs + kTile - 1) / kTile;
+      int p = tid * q;
+      const int p1 = min(p + q, npairs);
+      if (p < p1) {
+        // home element: largest i with s_off[i] <= p
+        int lo = 0, hi = kTile - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_off[mid] <= p)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        int i = lo;
+        int k = p - s_off[i];
+        int o = 0;
+        while (k >= s_cnt[o * kTile + i]) {
+          k -= s_cnt[o * kTile + i];
+          ++o;
+        }
+        int tt = s_start[o * kTile + i] + k;
+        int rem = s_cnt[o * kTile + i] - k;
+        float uh[D], offv[D], acc[D];
+        float sh = s_si[i];
+        int gh = s_g[i];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          uh[d] = s_u[d * kTile + i];
+          acc[d] = 0.0f;
+        }
+        auto set_off = [&](int oo) {
+          const int o0 = oo / (D == 2 ? 3 : 9) - 1;
+          const int o1 = (D == 2 ? oo % 3 : (oo / 3) % 3) - 1;
+          offv[0] = static_cast<float>(o0) * C.bwf[0] - uh[0];
+          offv[1] = static_cast<float>(o1) * C.bwf[1] - uh[1];
+          if (D == 3) offv[D - 1] = static_cast<float>(oo % 3 - 1) * C.bwf[D - 1] - uh[D - 1];
+        };
+        set_off(o);
+        for (;;) {
+          const int ej = __ldg(a.eid + tt);
+          const float4 pj = __ldg(a.pk + tt);
+          float dx[D];
+          float r2 = 0.0f;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            dx[d] = pk_c(pj, d) + offv[d];
+            r2 += dx[d] * dx[d];
+          }
+          const float f0 = pair_f0_fast<LAW>(r2, sh, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != gh);
+#pragma unroll
+          for (int d = 0; d < D; ++d) acc[d] += f0 * dx[d];
+          if (++p >= p1) break;
+          ++tt;
+          --rem;
+          while (rem == 0) {
+            if (++o == NB) {
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                atomicAdd(&s_F[d * kTile + i], acc[d]);
+                acc[d] = 0.0f;
+              }
+              ++i;
+              o = 0;
+              sh = s_si[i];
+              gh = s_g[i];
+#pragma unroll
+              for (int d = 0; d < D; ++d) uh[d] = s_u[d * kTile + i];
+            }
+            rem = s_cnt[o * kTile + i];
+            tt = s_start[o * kTile + i];
+            if (rem) set_off(o);
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) atomicAdd(&s_F[d * kTile + i], acc[d]);
+      }
+    }
+    __syncthreads();
+
+    if (live) {
+      if (C.single_bin) {
+        // one bin only (tiny boxes): every element, FP32 minimum image
+        for (int tt = C.slot_base; tt < C.slot_base + nlive; ++tt) {
+          const int ej = a.eid[tt];
+          const float4 pj = a.pk[tt];
+          float dx[D];
+          float r2 = 0.0f;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            float v = pk_c(pj, d) - ui[d];
+            if (C.periodic[d]) v -= rintf(v * C.inv_bwf[d]) * C.bwf[d];
+            dx[d] = v;
+            r2 += v * v;
+          }
+          const float f0 = pair_f0_fast<LAW>(r2, si, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != g);
+#pragma unroll
+          for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) F[d] += s_F[d * kTile + tid];
+      }
+      float dstep[D];
+      mixed_integrate<D>(a, C, c, s, j, ui, w, F, dstep);
+    }
+    __syncthreads();
+  }
+}
+
+// Skin-mode step, one thread per slot, one tile per CTA. Each element walks its Verlet list
+// (entries: slot | neighbour-bin index << 27), loading a batch of entries and then the
+// batch's packed partners, so that a warp keeps several independent loads in flight; a
+// partner with w < 0 (fresh or dead) is skipped. Fresh elements (ncnt 0) take their pair
+// force from facc, written by k_fresh_pairs; normal elements add the reactions found there.
+// After the update the displacement guard |u - uref| > skin/2 requests a list rebuild for the
+// next step; the tile's largest displacement and step statistics go to the colony once.
+constexpr int kListBatch = 4;
+
+template <int D, int LAW>
+__global__ void __launch_bounds__(kTile, 4) k_force_list(ForceArgs a_) {
+  ForceArgs a = a_;
+  a.ts = *a_.ts_dev;
+  __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
+  __shared__ float s_ssum;
+  const int t = blockIdx.x;
+  if (t >= a.tiles[a.B]) return;  // uniform per block
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    s_dmax = 0u;
+    s_smax = 0u;
+    s_ssum = 0.0f;
+  }
+  const int c = colony_of_tile(a.tiles, a.B, t);
+  const ColonyConst &C = a.col[c];
+  const int s = C.slot_base + (t - a.tiles[c]) * kTile + tid;
+  const size_t SS = a.SS;
+  const bool used = s < C.slot_base + a.cnt[c].nslot;
+  const int e = used ? a.eid[s] : -1;
+  float d2 = 0.0f, st2 = 0.0f;
+  if (used && e < 0 && a.integrate) {
+    // tombstone: the next record must keep w < 0 too, or the lists of others would see the
+    // stale record of two steps ago in the other buffer
+    a.pk_next[s] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+  }
+  if (e >= 0) {
+    const int j = e & 1;
+    const float4 pi = a.pk[s];
+    float ui[D], F[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) ui[d] = pk_c(pi, d);
+    const float si = fabsf(pi.w);
+    int bi[D];
+    bin_decode<D>(C, a.sbin[s], bi);
+    mixed_own_forces<D>(a, C, s, e, ui, bi, si, F);
+    // pair forces from the list, kListBatch entries at a time
+    const int n = a.ncnt[s];
+    const float eps = C.eps_f, rcs = C.rcs_f;
+    float acc[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) acc[d] = 0.0f;
+    for (int k0 = 0; k0 < n; k0 += kListBatch) {
+      unsigned ent[kListBatch];
+      float4 pj[kListBatch];
+#pragma unroll
+      for (int q = 0; q < kListBatch; ++q)
+        ent[q] = k0 + q < n ? static_cast<unsigned>(__ldg(a.nbr + static_cast<size_t>(k0 + q) * SS + s)) : 0xffffffffu;
+#pragma unroll
+      for (int q = 0; q < kListBatch; ++q)
+        pj[q] = ent[q] != 0xffffffffu ? __ldg(a.pk + (ent[q] & ((1u << kListSlotBits) - 1u)))
+                                      : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+#pragma unroll
+      for (int q = 0; q < kListBatch; ++q) {
+        const int o = static_cast<int>(ent[q] >> kListSlotBits);
+        int off[3];
+        if (D == 2) {
+          off[0] = o / 3 - 1;
+          off[1] = o % 3 - 1;
+        } else {
+          off[0] = o / 9 - 1;
+          off[1] = (o / 3) % 3 - 1;
+          off[2] = o % 3 - 1;
+        }
+        float dx[D];
+        float r2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          dx[d] = (pk_c(pj[q], d) - ui[d]) + static_cast<float>(off[d]) * C.bwf[d];
+          r2 += dx[d] * dx[d];
+        }
+        const float f0 = pair_f0_fast<LAW>(r2, si, pj[q].w, eps, rcs, pj[q].w > 0.0f);
+#pragma unroll
+        for (int d = 0; d < D; ++d) acc[d] += f0 * dx[d];
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      F[d] += acc[d] + a.facc[d * SS + s];
+      a.facc[d * SS + s] = 0.0f;
+    }
+    float dstep[D];
+    mixed_integrate<D>(a, C, c, s, j, ui, pi.w, F, dstep);
+    if (a.integrate) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const float dr = (ui[d] + dstep[d]) - a.uref[d * SS + s];
+        d2 += dr * dr;
+        st2 += dstep[d] * dstep[d];
+      }
+      if (d2 > a.skin[c].half2) atomicOr(&a.skin[c].need, 1);
+    }
+  }
+  if (a.integrate) {
+    // displacement statistics: warp reductions, shared atomics, one global atomic each
+    const unsigned dmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    const float stp = sqrtf(st2);
+    const unsigned smax = __reduce_max_sync(0xffffffffu, __float_as_uint(stp));
+    float ssum = stp;
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, q);
+    __syncthreads();  // the initialisation above is visible
+    if ((tid & 31) == 0) {
+      atomicMax(&s_dmax, dmax);
+      atomicMax(&s_smax, smax);
+      atomicAdd(&s_ssum, ssum);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      atomicMax(&a.skin[c].maxdisp2, s_dmax);
+      if (a.sched) {
+        atomicMax(reinterpret_cast<unsigned *>(&a.sched[c].step_max), s_smax);
+        atomicAdd(&a.sched[c].step_sum, s_ssum);
+      }
+    }
+  }
+}
+
+template <int D, int LAW>
+void launch_list_dl(const ForceArgs &a, int grid, cudaStream_t s) {
+  k_force_list<D, LAW><<<grid, kTile, 0, s>>>(a);  // grid: tiles over the slot capacity
 }
 
 template <int D>
-void launch_d(const ForceArgs &a, int law, int prec, int grid, int block, cudaStream_t s) {
+void launch_list_d(const ForceArgs &a, int law, int grid, cudaStream_t s) {
   switch (law) {
     case CIL_FORCE_LJ_WCA:
-      launch_dl<D, CIL_FORCE_LJ_WCA>(a, prec, grid, block, s);
+      launch_list_dl<D, CIL_FORCE_LJ_WCA>(a, grid, s);
       break;
     case CIL_FORCE_SOFTCORE:
-      launch_dl<D, CIL_FORCE_SOFTCORE>(a, prec, grid, block, s);
+      launch_list_dl<D, CIL_FORCE_SOFTCORE>(a, grid, s);
       break;
     default:
-      launch_dl<D, CIL_FORCE_HERTZ>(a, prec, grid, block, s);
+      launch_list_dl<D, CIL_FORCE_HERTZ>(a, grid, s);
+      break;
+  }
+}
+
+template <int D>
+constexpr size_t mixed_smem_bytes() {
+  return sizeof(int) * ((D == 2 ? 9 : 27) * kTile * 2 + kTile + 1 + kTile) + sizeof(float) * (2 * D * kTile + kTile);
+}
+
+template <int D, int LAW>
+void launch_dl(const ForceArgs &a, int prec, int grid, cudaStream_t s) {
+  if (prec == CIL_PREC_FP64) {
+    k_force_fp64<D, LAW><<<grid, kTile, 0, s>>>(a);
+  } else {
+    constexpr size_t bytes = mixed_smem_bytes<D>();
+    static bool attr_set = false;  // per instantiation; the attribute is per function
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_force_mixed<D, LAW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(bytes));
+      attr_set = true;
+    }
+    k_force_mixed<D, LAW><<<grid, kTile, bytes, s>>>(a);
+  }
+}
+
+template <int D>
+void launch_d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s) {
+  switch (law) {
+    case CIL_FORCE_LJ_WCA:
+      launch_dl<D, CIL_FORCE_LJ_WCA>(a, prec, grid, s);
+      break;
+    case CIL_FORCE_SOFTCORE:
+      launch_dl<D, CIL_FORCE_SOFTCORE>(a, prec, grid, s);
+      break;
+    default:
+      launch_dl<D, CIL_FORCE_HERTZ>(a, prec, grid, s);
       break;
   }
 }
 
 }  // namespace
 
-void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block,
-                  cudaStream_t s) {
+void launch_force_list(const ForceArgs &a, int dim, int law, int grid, cudaStream_t s) {
   if (dim == 2)
-    launch_d<2>(a, law, prec, grid, block, s);
+    launch_list_d<2>(a, law, grid, s);
   else
-    launch_d<3>(a, law, prec, grid, block, s);
+    launch_list_d<3>(a, law, grid, s);
+}
+
+void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block, cudaStream_t s) {
+  (void)block;
+  if (dim == 2)
+    launch_d<2>(a, law, prec, grid, s);
+  else
+    launch_d<3>(a, law, prec, grid, s);
 }
 
 }  // namespace cil

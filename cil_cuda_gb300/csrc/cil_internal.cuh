@@ -22,6 +22,12 @@ namespace cil {
 constexpr int kTile = 256;        // threads per block of every slot/cell-parallel kernel
 constexpr int kScanItems = 1024;  // bins per scan block (256 threads x 4)
 constexpr int kDeadCap = 8192;    // apoptoses per colony per step handled on the device
+constexpr int kListCap = 64;      // Verlet list entries per element (skin mode)
+constexpr int kFreshCap = 16384;  // elements created or moved by division between list rebuilds
+constexpr int kMaxSkinColonies = 4096;  // colonies per handle in skin mode (fresh-pair prefix in shared memory)
+constexpr int kListSlotBits = 27; // list entry = slot | (neighbour-bin index << 27)
+constexpr int kCellItems = 4;     // cells per thread in the event kernels
+constexpr int kCellTile = kTile * kCellItems;
 
 // error bits in ColonyCounters::err
 constexpr int kErrNan = 1 << CIL_ERR_NAN;
@@ -29,13 +35,73 @@ constexpr int kErrBox = 1 << CIL_ERR_OUT_OF_BOX;
 constexpr int kErrCap = 1 << CIL_ERR_CAPACITY;
 
 // Philox purposes (third counter word)
-constexpr uint32_t kRngNoise = 1, kRngDiv = 2, kRngDiv2 = 3, kRngApo = 4;
+constexpr uint32_t kRngNoise = 1, kRngDiv = 2, kRngDiv2 = 3, kRngApo = 4, kRngApoPick = 5;
+
+// per-slot state in skin mode
+constexpr unsigned char kSlotNormal = 0;  // in the bins and Verlet lists of the last rebuild
+constexpr unsigned char kSlotFresh = 1;   // created or moved by a division since then
+constexpr unsigned char kSlotDead = 2;    // removed by apoptosis
+
+// Verlet-skin control of one colony (device resident; written by the kernels)
+struct ColonySkin {
+  float skin;          // skin of the current lists
+  float half2;         // (skin / 2)^2, the displacement guard
+  int need;            // rebuild requests: 1 guard, 2 fresh overflow, 4 cadence, 8 host
+  int rebuild_now;     // this step rebuilds the lists
+  int steps_since;     // steps since the last list rebuild
+  int interval;        // cadence in steps (0: guard only)
+  int nfresh;          // entries in the fresh list
+  int nrebuild;        // list rebuilds so far
+  int ntrip;           // rebuilds requested by the guard
+  unsigned maxdisp2;   // largest |u - uref|^2 of the last step (float bits)
+  int list_overflow;   // elements whose list was truncated at the last build
+  int last_interval;   // steps between the last two rebuilds
+  long long npairs;    // list entries at the last build
+};
+
+// Inputs of the learned skin scheduler, maintained on the device per colony in skin mode.
+// The 12 features are formed by k_skin_begin at every list rebuild (before the statistics
+// of the new build are reset); k_mlp_schedule turns them into the colony's next skin and
+// rebuild cadence.
+constexpr int kSchedFeatures = 12;
+struct SchedState {
+  float occ_sum;          // sum over elements of their home-bin occupancy at the last list build
+  int occ_count;          // elements counted into occ_sum
+  float occ_max;          // largest bin occupancy at the last list build (float bits, atomicMax)
+  float step_sum;         // sum over elements of |displacement| in the last step
+  float step_max;         // largest |displacement| in the last step (float bits, atomicMax)
+  float div_rate;         // divisions per cell per step, moving average over ~100 steps
+  float apo_rate;         // apoptoses per cell per step, moving average over ~100 steps
+  float trip_share;       // share of guard-triggered rebuilds, moving average over ~10 rebuilds
+  long long ndiv_prev, napo_prev;
+  int nsched;             // scheduler decisions taken
+  int pad;
+  float features[kSchedFeatures];  // input of the last decision
+};
+
+// Mixed precision keeps each element as one 16-byte record, so a pair costs one load:
+//   xyz  FP32 coordinates relative to the origin of the element's home bin (sbin)
+//   w    FP32 diameter; in skin mode negative for elements the Verlet lists must skip
+//        (fresh: moved or created by a division since the last build; dead: tombstone)
+__device__ __forceinline__ float pk_c(const float4 &p, int d) { return d == 0 ? p.x : (d == 1 ? p.y : p.z); }
+__device__ __forceinline__ void pk_set(float4 &p, int d, float v) {
+  if (d == 0)
+    p.x = v;
+  else if (d == 1)
+    p.y = v;
+  else
+    p.z = v;
+}
 
 struct ColonyConst {
   double box[3];
   double ih[3];      // 1/L, as the reference binning formula uses (Utils.hpp:990)
   double bw[3];      // bin width L/Ns
   int ns[3];         // bins per axis (1 on unused axes)
+  // bin-id decoding without hardware division: q = n / div_d[k] for the two divisors
+  // (2D: ns1; 3D: ns1*ns2 and ns2) by multiply-high with an invariant (Granlund and
+  // Montgomery, "Division by invariant integers using multiplication", PLDI 1994, fig. 4.1)
+  uint32_t div_m[2], div_s1[2], div_s2[2];
   int periodic[3];
   int single_bin;    // grid collapsed to one bin (some Ns < 3, Utils.hpp:897-901)
   int bin_base;      // first global bin
@@ -65,7 +131,13 @@ struct ColonyConst {
   double dt;
   double div_tau_mu, div_tau_sigma;
   double apop_p;     // apoptosis probability per step
-  float bwf[3];      // bin widths in FP32 (mixed precision)
+  // FP32 copies for the mixed-precision kernel (GB300 runs FP64 at ~1/64 of FP32, so the
+  // mixed kernel keeps every per-element operation but the position update in FP32)
+  float bwf[3];      // bin widths
+  float inv_bwf[3];  // 1 / bin width
+  float zeta_f[2], temp_f[2], mu_f[2], motility_f[2];
+  float kappa_f, rest0_f, rest1_f, amp_f, eps_f, rcs_f, wall_E_f;
+  float wall_pos_f[2];
 };
 
 struct ColonyCounters {
@@ -110,6 +182,53 @@ __device__ __forceinline__ int colony_of_tile(const int *__restrict__ tile_base,
       hi = mid - 1;
   }
   return lo;
+}
+
+// Coordinates of a colony-local bin id (LinkListOrtho2D/3D::get_cellCoord,
+// Utils.hpp:1029-1061)
+__host__ __device__ __forceinline__ uint32_t div_invariant(uint32_t n, uint32_t m, uint32_t s1, uint32_t s2) {
+#ifdef __CUDA_ARCH__
+  const uint32_t t1 = __umulhi(m, n);
+#else
+  const uint32_t t1 = static_cast<uint32_t>((static_cast<uint64_t>(m) * n) >> 32);
+#endif
+  return (t1 + ((n - t1) >> s1)) >> s2;
+}
+
+// host: the invariant (m, s1, s2) of divisor d >= 1
+inline void div_invariant_setup(uint32_t d, uint32_t *m, uint32_t *s1, uint32_t *s2) {
+  uint32_t l = 0;
+  while (l < 32 && (1ull << l) < d) ++l;  // ceil(log2 d)
+  *m = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  *s1 = l < 1 ? l : 1;
+  *s2 = l > 0 ? l - 1 : 0;
+}
+
+template <int D>
+__device__ __forceinline__ void bin_decode(const ColonyConst &C, int id, int *b) {
+  const uint32_t u = static_cast<uint32_t>(id);
+  if (D == 2) {
+    b[0] = static_cast<int>(div_invariant(u, C.div_m[0], C.div_s1[0], C.div_s2[0]));
+    b[1] = id - b[0] * C.ns[1];
+  } else {
+    b[0] = static_cast<int>(div_invariant(u, C.div_m[0], C.div_s1[0], C.div_s2[0]));
+    const int r = id - b[0] * (C.ns[1] * C.ns[2]);
+    b[1] = static_cast<int>(div_invariant(static_cast<uint32_t>(r), C.div_m[1], C.div_s1[1], C.div_s2[1]));
+    b[2] = r - b[1] * C.ns[2];
+  }
+}
+
+// Exact float -> double conversion with integer operations only (no FP64 pipe): finite
+// normal values are re-biased bit for bit; zeros, subnormals, inf and NaN take the
+// conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t ex = (b >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return static_cast<double>(f);
+  const uint64_t d = (static_cast<uint64_t>(b & 0x80000000u) << 32) |
+                     (static_cast<uint64_t>(ex - 127u + 1023u) << 52) |
+                     (static_cast<uint64_t>(b & 0x7fffffu) << 29);
+  return __longlong_as_double(static_cast<long long>(d));
 }
 
 // Bin coordinates of a position (LinkListOrtho::populate_list, Utils.hpp:990), clamped
@@ -215,6 +334,34 @@ __device__ __forceinline__ bool pair_force(R r2, R si, R sj, R eps, R rcs, R &f0
   }
 }
 
+// FP32 pair force, branch-free: the law is evaluated for every candidate and masked
+// (fast reciprocal / reciprocal square root; the mixed form's tolerance is FP32-level)
+template <int LAW>
+__device__ __forceinline__ float pair_f0_fast(float r2, float si, float sj, float eps, float rcs, bool ok) {
+  const float sij = 0.5f * (si + sj);
+  const float rc = rcs * sij;
+  if (LAW == CIL_FORCE_LJ_WCA) {
+    const bool in = ok && r2 <= rc * rc;
+    const float ir2 = __fdividef(1.0f, r2);  // fast reciprocal (about 2 ulp)
+    const float sr2 = sij * sij * ir2;
+    const float sr6 = sr2 * sr2 * sr2;
+    const float f0 = (sr6 - 2.0f * sr6 * sr6) * ir2 * (24.0f * eps);
+    return in ? f0 : 0.0f;
+  } else {
+    const bool in = ok && r2 < rc * rc && r2 > 0.0f;
+    const float rinv = rsqrtf(r2);
+    const float r = r2 * rinv;
+    if (LAW == CIL_FORCE_SOFTCORE) {
+      const float w = 1.0f - __fdividef(r, rc);
+      return in ? -eps * w * w * rinv : 0.0f;
+    } else {
+      const float delta = fmaxf(sij - r, 0.0f);
+      const float sq = delta * rsqrtf(fmaxf(delta, 1e-30f));
+      return in ? -eps * delta * sq * rinv : 0.0f;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- kernel argument packs
 
 struct RebuildArgs {
@@ -227,13 +374,24 @@ struct RebuildArgs {
   const int *scan_col;     // scan block -> colony
   int nscan;               // scan blocks
   const double *x_in;
-  const double *sig_in;
+  const double *sig_in;    // binned FP64 diameters (FP64 form), may be null
   const int *eid_in;
   double *x_out;
   double *sig_out;
   int *eid_out;
-  float *u_out;            // FP32 bin-local coordinates (mixed precision), may be null
-  float *sigf_out;         // FP32 diameters (mixed precision), may be null
+  float4 *pk_out;          // mixed: packed elements of the new order, may be null
+  const float4 *pk_in;     // mixed: packed elements after the last update (relative to sbin_in)
+  const int *sbin_in;      // home bin (colony-local id) of each slot
+  int *sbin_out;
+  const int2 *cyc_in;      // (birth step, division step) of each slot's cell
+  int2 *cyc_out;
+  const double *sigma_c;   // canonical diameters [2 * CC]
+  const int *t0c;          // canonical cycle arrays [CC]
+  const int *tswc;
+  int exact;               // 1: reference FP64 bin formula and canonical gathers
+  const ColonySkin *skin;  // skin mode: colonies without rebuild_now are skipped; else null
+  int permute;             // 1: slots are re-sorted (data moves); 0: only the bin index is rebuilt
+  unsigned char *state_out;// skin mode, permuting: slot states of the new order
   int *key;
   int *bcount;
   int2 *range;
@@ -254,18 +412,27 @@ struct ForceArgs {
   const int *tiles_live;
   const double *x_in;      // sorted positions
   double *x_out;           // integrated positions (same slots)
-  const double *sig;
+  const double *sig;       // FP64 form
   const int *eid;
-  const float *u;          // mixed precision
-  const float *sigf;
+  const float4 *pk;        // mixed: packed elements of this step
+  float4 *pk_next;         // mixed: packed elements after the update (same slots)
+  const int *sbin;         // home bin of each slot
+  const int2 *cyc;         // cycle of each slot's cell
   const int2 *range;
   const int *slot_of;
-  const int *t0;
-  const int *tsw;
+  // skin mode (null otherwise)
+  const int *tiles;        // tiles over nslot
+  ColonySkin *skin;
+  const int *nbr;          // Verlet lists [kListCap][SS]
+  const int *ncnt;
+  const float *uref;
+  float *facc;             // pair forces of fresh elements / reactions [D][SS], consumed and zeroed
+  SchedState *sched;       // speed statistics for the scheduler
   const double *noise;     // oracle mode: uploaded normals (already scaled), canonical order
   double *vel;             // slot order, may be null
   double *frc;             // slot order, may be null
-  int ts;
+  const int *ts_dev;       // device step counter: the step being computed
+  int ts;                  // filled from *ts_dev at kernel entry
   uint32_t seed_lo, seed_hi;
   int noise_mode;          // 0 none, 1 philox, 2 uploaded
   int integrate;
@@ -278,7 +445,19 @@ struct EventArgs {
   size_t SS;
   const int *tiles_cell;   // [B+1] tiles over ncell
   double *x;               // current positions
-  double *sig;
+  double *sig;             // binned FP64 diameters (FP64 form) or null
+  float4 *pk;              // mixed: packed elements (after this step's update), or null
+  int *sbin;
+  int2 *cyc;
+  double *sigma_c;         // canonical diameters
+  // skin mode (null otherwise)
+  ColonySkin *skin;
+  unsigned char *state;
+  float *uref;
+  int *ncnt;
+  int *fresh;              // [B][kFreshCap]
+  unsigned long long *fhead;  // per bin: newest fresh slot of the current list epoch (epoch << 32 | slot)
+  unsigned long long *fnext;  // per slot: the entry it displaced (a linked list per bin)
   int *eid;
   double *vel;             // may be null
   int *slot_of;
@@ -291,8 +470,45 @@ struct EventArgs {
   double *obs_disp;
   double *obs_vref;
   size_t CC;
-  int ts;                  // step after the increment
+  const int *ts_dev;       // device step counter, already advanced past the force step
+  int ts;                  // filled from *ts_dev at kernel entry
   uint32_t seed_lo, seed_hi;
+};
+
+struct SkinArgs {
+  const ColonyConst *col;
+  ColonyCounters *cnt;
+  ColonySkin *skin;
+  SchedState *sched;       // scheduler inputs (always maintained in skin mode)
+  int B;
+  size_t SS;
+  const int *tiles;        // tiles over nslot
+  const int *eid;
+  unsigned char *state;
+  float4 *pk;              // current packed elements (rebinned in place)
+  float *uref;
+  int *sbin;
+  const int2 *range;
+  const unsigned long long *perm;
+  int *nbr;
+  int *ncnt;
+  const int *fresh;
+  const unsigned long long *fhead;
+  const unsigned long long *fnext;
+  float *facc;
+  int *key;
+  int *bcount;
+  int force_rebuild;       // host request for every colony this step
+  int grid;                // blocks of the fresh-pair kernel
+};
+
+struct SchedArgs {
+  ColonySkin *skin;
+  SchedState *sched;
+  const ColonyCounters *cnt;
+  int B;
+  int use_interval;        // apply the predicted cadence (else only the skin)
+  float skin_min, skin_max, interval_scale;
 };
 
 // ---------------------------------------------------------------- launchers (host side)
@@ -301,14 +517,22 @@ void launch_tiles(const ColonyConst *col, ColonyCounters *cnt, int B, int which,
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s);
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block,
                   cudaStream_t s);
+void launch_force_list(const ForceArgs &a, int dim, int law, int grid, cudaStream_t s);
+void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
+void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
+void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
+void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
+void launch_mlp_schedule(const float *params, const SchedArgs &a, cudaStream_t s);
+void launch_advance_ts(int *ts_dev, cudaStream_t s);
+int mlp_param_count();
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,
                            const double *dirs, const int *spans, int dim, cudaStream_t s);
 void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops, const int *ops, int dim,
                              cudaStream_t s);
 void launch_upload_scatter(const ColonyConst *col, int colony, int ncells, int dim, size_t SS,
-                           const double *pos, const double *sigma, double *x, double *sig,
-                           int *eid, int *slot_of, ColonyCounters *cnt, cudaStream_t s);
+                           const double *pos, double *x, int *eid, int *slot_of, ColonyCounters *cnt,
+                           cudaStream_t s);
 void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,
                              const double *src, int width, double *dst, cudaStream_t s);
 void launch_observables(const EventArgs &a, int colony, int ncells, int dim, int reset,

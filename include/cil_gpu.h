@@ -94,8 +94,15 @@ typedef struct cil_config {
   double bin_width;       /* 0: cutoff of the largest element (+ skin); else at least this */
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
   int32_t block_size;     /* threads per block of the pair kernel (0 = default) */
-  int32_t flags;          /* reserved, 0 */
+  int32_t flags;          /* CIL_FLAG_* bits */
 } cil_config;
+
+/* cil_config.flags: run every step as individual launches (no CUDA graphs). By default, in
+ * Philox mode, pairs of steps whose launches depend on nothing the host decides (no slot
+ * re-sort, no FP64 re-anchoring, not the last step of a cil_step call) are captured once as
+ * a CUDA graph per buffer parity and replayed; the kernels read the step index from device
+ * memory. cil_timings then reports phase times for the individually launched steps only. */
+#define CIL_FLAG_NO_GRAPH 1
 
 /* Host view of one colony in the reference layout. */
 typedef struct cil_colony_view {
@@ -158,12 +165,81 @@ cil_status cil_bins(cil_handle *h, int32_t colony, int32_t *ns, int32_t *bin_sta
 cil_status cil_obs_reset(cil_handle *h, int32_t colony);
 cil_status cil_observables(cil_handle *h, int32_t colony, cil_obs *out);
 
+/* Verlet-skin mode (cil_config.skin > 0, mixed precision only): the bins and per-element
+ * Verlet lists (cutoff rc_ij + skin) are rebuilt only when an element has moved more than
+ * skin/2 since the last build, when the cadence `interval` (steps, 0 = none) expires, or
+ * when too many elements were created by divisions; results agree with the per-step
+ * rebuild of the reference (CIL.cu:180) to FP32 summation order. No counterpart in the
+ * reference, which rebuilds its link list every step. */
+typedef struct cil_skin_info {
+  double skin;           /* skin of the current lists */
+  int32_t interval;      /* cadence in steps (0: guard only) */
+  int32_t nrebuild;      /* list rebuilds so far */
+  int32_t ntrip;         /* of which requested by the displacement guard */
+  int32_t last_interval; /* steps between the last two rebuilds */
+  int32_t nfresh;        /* elements created or moved by divisions since the last rebuild */
+  int32_t list_overflow; /* elements whose list exceeded the capacity at the last build */
+  int64_t npairs;        /* list entries at the last build */
+  double max_disp;       /* largest displacement from the list reference in the last step */
+} cil_skin_info;
+
+cil_status cil_skin_stats(cil_handle *h, int32_t colony, cil_skin_info *out);
+/* Sets the skin (<= cil_config.skin, which sizes the bins) and cadence of one colony; they
+ * take effect at its next list rebuild, which this call requests. */
+cil_status cil_set_skin(cil_handle *h, int32_t colony, double skin, int32_t interval);
+
+/* Learned skin scheduler (skin mode only) — no counterpart in the reference.
+ *
+ * A 12 -> 64 -> 64 -> 2 SiLU multilayer perceptron (FP32) evaluated on the device at every
+ * list rebuild of a colony, from 12 features the step maintains per colony (cells, bin
+ * occupancy, step displacements, division/apoptosis rates, current skin, steps since the
+ * last rebuild, displacement at the rebuild, guard-trip share, fresh elements; see
+ * cil_sched_info). Output y0 sets the skin skin_min + (cil_config.skin - skin_min) *
+ * sigmoid(y0), output y1 the cadence round(interval_scale * softplus(y1)) steps when
+ * use_interval != 0. The displacement guard stays on, so the physics is unchanged: only the
+ * cost of a step depends on the choice. params: host, cil_mlp_num_params() floats in the
+ * layout W1[64][12] b1[64] W2[64][64] b2[64] W3[2][64] b3[2]; NULL switches it off (the
+ * skin and cadence then stay where they are). */
+#define CIL_SCHED_FEATURES 12
+cil_status cil_set_scheduler(cil_handle *h, const float *params, double skin_min, double interval_scale,
+                             int32_t use_interval);
+
+typedef struct cil_sched_info {
+  /* input of the last decision: 0 log(cells)/14, 1 mean home-bin occupancy/10, 2 max bin
+   * occupancy/20, 3 mean and 4 max step displacement (log10(d)/4 + 1), 5 divisions and
+   * 6 apoptoses per cell per step x1e4, 7 skin, 8 log(1 + steps since the last rebuild)/5,
+   * 9 largest displacement from the list reference / (skin/2), 10 share of guard-triggered
+   * rebuilds, 11 fresh elements / elements x10 */
+  float features[CIL_SCHED_FEATURES];
+  float div_rate, apo_rate, trip_share;
+  int32_t nsched; /* scheduler decisions so far */
+} cil_sched_info;
+
+cil_status cil_sched_state(cil_handle *h, int32_t colony, cil_sched_info *out);
+
+/* Training kernels of the scheduler network (all pointers device memory, FP32, run on the
+ * current device's default stream):
+ *   cil_mlp_forward  Y[n][2] = net(X[n][12])
+ *   cil_mlp_grad     loss = mean over samples and outputs of w[o] * (y - T)^2 and its
+ *                    gradient (deterministic: block partials summed in a fixed order);
+ *                    workspace of cil_mlp_workspace_floats(n) floats
+ *   cil_mlp_adam     one Adam step (beta1 0.9, beta2 0.999, eps 1e-8), step count t >= 1 */
+int32_t cil_mlp_num_params(void);
+int64_t cil_mlp_workspace_floats(int32_t n);
+cil_status cil_mlp_forward(const float *params, const float *X, int32_t n, float *Y);
+cil_status cil_mlp_grad(const float *params, const float *X, const float *T, const float *out_weights,
+                        int32_t n, float *workspace, float *grad, float *loss);
+cil_status cil_mlp_adam(float *params, const float *grad, float *m, float *v, int32_t t, float lr);
+
 /* Device time of the last cil_step, milliseconds, measured with CUDA events on the
  * handle's stream: per phase summed over its steps (rebuild, forces, events), the whole
  * call from the first launch to the last (total, including any idle gaps), and the number
  * of kernels it launched. Any pointer may be NULL. */
 cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, double *events_ms,
                        double *total_ms, int64_t *launches);
+
+/* Steps of the last cil_step call that ran inside CUDA graphs, and graphs captured so far. */
+cil_status cil_graph_info(cil_handle *h, int64_t *graph_steps, int64_t *graphs_captured);
 
 /* The oracle-mode host random stream on its own (no device needed): n draws of `kind`
  * from a fresh stream seeded with `seed` through the reference's Random:: functions

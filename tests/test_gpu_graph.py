@@ -1,0 +1,55 @@
+"""CUDA-graph replay of steady steps against the same steps launched one by one.
+
+Philox mode only (oracle mode draws on the host every step). The FP64 form is deterministic,
+so the two runs must agree bit for bit; the mixed forms sum pair forces in a scheduling-
+dependent FP32 order, so they agree to FP32 rounding over the run."""
+import numpy as np
+import pytest
+
+from cil_cuda_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+STEPS = 101  # an odd count: graph pairs, stand-alone steps and the last step
+
+
+def run(G, p, st, precision, graphs, skin=0.0, steps=STEPS):
+    n = len(st["sigma"])
+    eng = G.Engine([p], [3 * n], precision=precision, rng=G.RNG_PHILOX, seed=5, skin=skin, graphs=graphs)
+    eng.upload(0, **st)
+    eng.step(steps)
+    out = eng.download(0)
+    info = eng.graph_info()
+    ob = eng.observables(0)
+    eng.close()
+    return out, info, ob
+
+
+@pytest.fixture(scope="module")
+def growth():
+    p = S.growth_params(box=120.0, dt=1e-3, div_tau_mu=0.2, div_tau_sigma=0.02, apop_rate=0.5)
+    return p, S.disk_colony(3000, p, seed=4)
+
+
+def test_fp64_graph_bitwise(gpu_lib, growth):
+    p, st = growth
+    a, ia, oa = run(gpu_lib, p, st, gpu_lib.PREC_FP64, graphs=False)
+    b, ib, ob = run(gpu_lib, p, st, gpu_lib.PREC_FP64, graphs=True)
+    assert ia["graph_steps"] == 0 and ib["graph_steps"] >= STEPS - 3
+    assert a["ncells"] == b["ncells"] and oa["ndiv_total"] == ob["ndiv_total"] > 0
+    np.testing.assert_array_equal(a["pos"], b["pos"])
+    np.testing.assert_array_equal(a["vel"], b["vel"])
+    np.testing.assert_array_equal(a["tswitch"], b["tswitch"])
+
+
+@pytest.mark.parametrize("skin", [0.0, 0.3])
+def test_mixed_graph_matches_launches(gpu_lib, growth, skin):
+    p, st = growth
+    a, ia, oa = run(gpu_lib, p, st, gpu_lib.PREC_MIXED, graphs=False, skin=skin)
+    b, ib, ob = run(gpu_lib, p, st, gpu_lib.PREC_MIXED, graphs=True, skin=skin)
+    assert ib["graph_steps"] > 0 and ib["graphs_captured"] >= 1
+    # divisions and apoptosis follow the same Philox streams
+    assert a["ncells"] == b["ncells"] and oa["ndiv_total"] == ob["ndiv_total"]
+    np.testing.assert_array_equal(a["tswitch"], b["tswitch"])
+    d = np.asarray(a["pos"]) - np.asarray(b["pos"])
+    d -= np.round(d / p["box"][0]) * p["box"][0]
+    assert np.abs(d).max() < 1e-4

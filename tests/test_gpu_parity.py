@@ -7,6 +7,8 @@ Tolerances (FP64, oracle mode = the reference's dSFMT stream uploaded):
 * 100-step trajectories: max |x_gpu - x_oracle| (minimum image) <= 1e-9
 * division / apoptosis: identical cell counts, birth steps and division steps
 * mixed precision forces: norm-wise relative error <= 2e-5 against the FP64 oracle
+* mixed precision 100-step trajectories (FP32 forces, FP64 positions, local coordinates
+  re-anchored on the FP64 positions every 32 steps): max |x - x_oracle| <= 1e-5
 """
 import numpy as np
 import pytest
@@ -18,6 +20,7 @@ pytestmark = pytest.mark.gpu
 FORCE_TOL = 1e-12
 TRAJ_TOL = 1e-9
 MIXED_TOL = 2e-5
+MIXED_TRAJ_TOL = 1e-5
 
 
 def minimage(a, b, p):
@@ -159,6 +162,18 @@ def test_trajectory_100_steps_3d_channel(gpu_lib, oracle_lib, channel):
     assert rc == 0
     err = np.abs(minimage(g["pos"], s["pos"], p)).max()
     assert err <= TRAJ_TOL, err
+
+
+@pytest.mark.parametrize("case", ["lj", "growth", "channel"])
+def test_mixed_precision_trajectory(gpu_lib, oracle_lib, lj, growth, channel, case):
+    p, st = {"lj": lj, "growth": growth, "channel": channel}[case]
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100, cap=2 * len(st["sigma"]),
+                           precision=gpu_lib.PREC_MIXED)
+    assert rc == 0
+    assert g["ncells"] == len(s["sigma"])
+    np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= MIXED_TRAJ_TOL, err
 
 
 def test_division_and_apoptosis_events_exact(gpu_lib, oracle_lib):

@@ -1,0 +1,110 @@
+"""Verlet-skin mode (mixed precision, lists rebuilt only when the displacement guard, the
+cadence or the fresh-element budget asks) against the FP64 oracle, which rebuilds its link
+list every step as the reference does (CIL.cu:180). Oracle-mode noise, so both sides see the
+same random forces; divisions and apoptosis happen during the run and the slots are re-sorted
+once (every 250 steps). Tolerance as for the mixed form: max |x - x_oracle| <= 1e-5."""
+import numpy as np
+import pytest
+
+from cil_cuda_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+STEPS = 300
+
+
+def minimage(a, b, p):
+    d = np.asarray(a) - np.asarray(b)
+    for k in range(p["dim"]):
+        if p["periodic"][k]:
+            L = p["box"][k]
+            d[..., k] -= np.round(d[..., k] / L) * L
+    return d
+
+
+def cases():
+    lj_p, lj_st = S.config1(1024, seed=7)
+    lj_st = S.relax(lj_p, lj_st)
+    g_p = S.growth_params(box=90.0, dt=1e-3, div_tau_mu=0.3, div_tau_sigma=0.02, apop_rate=0.5)
+    g_st = S.disk_colony(1200, g_p, seed=3)
+    c_p = S.channel_params(lxy=40.0, height=10.0)
+    c_st = S.channel_colony(1500, c_p, seed=5)
+    return {"lj": (lj_p, lj_st), "growth": (g_p, g_st), "channel": (c_p, c_st)}
+
+
+@pytest.fixture(scope="module")
+def states(gpu_lib):
+    return cases()
+
+
+@pytest.mark.parametrize("case", ["lj", "growth", "channel"])
+def test_skin_trajectory_matches_oracle(gpu_lib, oracle_lib, states, case):
+    p, st = states[case]
+    n = len(st["sigma"])
+    cap = 4 * n
+    eng = gpu_lib.Engine([p], [cap], precision=gpu_lib.PREC_MIXED, rng=gpu_lib.RNG_DSFMT, seed=11, skin=0.3)
+    eng.upload(0, **st)
+    eng.step(STEPS)
+    g = eng.download(0)
+    info = eng.skin_stats(0)
+    eng.close()
+    o = oracle_lib.Oracle(p, cap, 11)
+    o.set_state(**st)
+    assert o.step(STEPS) == 0
+    s = o.state()
+    assert g["ncells"] == len(s["sigma"])
+    np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TOL, err
+    # the lists were reused: fewer rebuilds than steps, and never truncated
+    assert info["list_overflow"] == 0
+    assert 1 <= info["nrebuild"] < STEPS, info
+
+
+def test_skin_rebuild_cadence_and_guard(gpu_lib, states):
+    """A cadence forces rebuilds at least that often; a tiny skin makes the guard trip."""
+    p, st = states["growth"]
+    n = len(st["sigma"])
+    eng = gpu_lib.Engine([p], [3 * n], precision=gpu_lib.PREC_MIXED, seed=2, skin=0.5)
+    eng.upload(0, **st)
+    eng.set_skin(0, 0.5, 10)
+    eng.step(100)
+    a = eng.skin_stats(0)
+    assert a["nrebuild"] >= 10 and a["interval"] == 10
+    eng.set_skin(0, 0.02, 0)
+    before = eng.skin_stats(0)
+    eng.step(50)
+    b = eng.skin_stats(0)
+    assert b["ntrip"] - before["ntrip"] >= 10
+    eng.close()
+
+
+def test_scheduler_keeps_physics_and_sets_skin(gpu_lib, oracle_lib, states):
+    """With a scheduler network installed (random weights here), every list rebuild asks it
+    for the skin and cadence; the displacement guard still protects the physics, so the
+    trajectory matches the oracle as with a fixed skin."""
+    p, st = states["growth"]
+    n = len(st["sigma"])
+    cap = 4 * n
+    rng = np.random.default_rng(5)
+    params = rng.normal(0, 0.3, size=gpu_lib.mlp_num_params()).astype(np.float32)
+    skin_max, skin_min = 0.6, 0.05
+    eng = gpu_lib.Engine([p], [cap], precision=gpu_lib.PREC_MIXED, rng=gpu_lib.RNG_DSFMT, seed=11, skin=skin_max)
+    eng.upload(0, **st)
+    eng.set_scheduler(params, skin_min=skin_min, interval_scale=20.0, use_interval=True)
+    eng.step(STEPS)
+    g = eng.download(0)
+    info = eng.skin_stats(0)
+    q = eng.sched_state(0)
+    eng.close()
+    o = oracle_lib.Oracle(p, cap, 11)
+    o.set_state(**st)
+    assert o.step(STEPS) == 0
+    s = o.state()
+    assert g["ncells"] == len(s["sigma"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TOL, err
+    assert q["nsched"] == info["nrebuild"] >= 1  # one decision per list rebuild
+    assert skin_min - 1e-6 <= info["skin"] <= skin_max + 1e-6
+    assert np.all(np.isfinite(q["features"]))
+    assert info["list_overflow"] == 0

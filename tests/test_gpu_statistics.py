@@ -2,9 +2,14 @@
 
 Both sides start from the same colony; the oracle runs with dSFMT seeds 1..16 (the
 reference's stream), the library with Philox seeds 1..16, FP64 and mixed precision. Cell
-count, mean cell area, MSD and VACF at the end must agree within 2 standard errors of the
-difference of the ensemble means (SE from the 16-sample spread, as tools/utils.py's block
-errors). The mixed form's deviation from the FP64 oracle is reported per observable.
+count, mean cell area, MSD and VACF at the end are compared through z = |difference of the
+ensemble means| / SE of that difference (SE from the 16-sample spreads, as tools/utils.py's
+block errors). Criterion: every z <= 3, and at most one of the 4 observables above 2
+standard errors (an observable counts once: the FP64 and mixed forms share their division
+and apoptosis streams, so cell count and mean area coincide between them). Under correct
+physics each comparison exceeds 2 SE with probability ~5 %; requiring all four below 2 would
+fail a correct build ~19 % of the time, two or more exceedances happen ~1.4 % of the time.
+The z values are printed per observable (the mixed form's deviation from the FP64 oracle).
 """
 import numpy as np
 import pytest
@@ -51,6 +56,7 @@ def test_observables_within_two_standard_errors(gpu_lib, oracle_lib):
     ora = [run_oracle(oracle_lib, p, st, s) for s in SEEDS]
     m_o, se_o = stats(ora)
     report = {}
+    zmax = np.zeros(len(OBS))
     for name, prec in (("fp64", gpu_lib.PREC_FP64), ("mixed", gpu_lib.PREC_MIXED)):
         gpu = [run_gpu(gpu_lib, p, st, s, prec) for s in SEEDS]
         m_g, se_g = stats(gpu)
@@ -59,6 +65,8 @@ def test_observables_within_two_standard_errors(gpu_lib, oracle_lib):
         report[name] = {k: (float(m_g[i]), float(m_o[i]), float(z[i])) for i, k in enumerate(OBS)}
         print(name, report[name])
         for i, k in enumerate(OBS):
-            assert z[i] <= 2.0, (name, k, m_g[i], m_o[i], se[i])
+            assert z[i] <= 3.0, (name, k, m_g[i], m_o[i], se[i])
+        zmax = np.maximum(zmax, z)
+    assert int((zmax > 2.0).sum()) <= 1, report
     # growth actually happened and the MSD is non-trivial
     assert m_o[0] > 400 and m_o[2] > 0
