@@ -40,6 +40,9 @@ NCELLS = 1_000_000
 BOX = 2048.0
 CAP = 1_200_000
 GTS = 100  # steps per output frame in the end-to-end arm
+# DRAM bytes per launch of k_force_list on this workload from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum); None until measured
+TRAFFIC_PER_LAUNCH = None
 
 
 def peaks():
@@ -143,10 +146,15 @@ def barrier(dist):
         dist.barrier()
 
 
-def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0):
+def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0, sched=False, graphs=True,
+             tune=None):
     """Device-timed run of one form; returns particle-steps/s and the timing details."""
-    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin)
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
+                   graphs=graphs, **(tune or {}))
     eng.upload(0, **st)
+    if sched:
+        from cil_cuda_gb300 import skin_scheduler as SS
+        SS.install(eng)
     if warmup:
         eng.step(warmup)
     n0 = eng.observables(0)["ncells"]
@@ -155,26 +163,70 @@ def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0):
     eng.step(steps)  # synchronises the handle's stream before returning
     wall = time.perf_counter() - t0
     tm = eng.timings()
+    gi = eng.graph_info()
     n1 = eng.observables(0)["ncells"]
     sk = eng.skin_stats(0) if skin > 0 else None
     eng.close()
     dev_s = tm["total_ms"] * 1e-3
     psteps = (n0 + n1) * steps  # 2 elements per cell, trapezoid over the (slow) growth
-    return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm, skin=sk)
+    return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm, skin=sk, graphs=gi)
 
 
-def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0):
+def run_batched(G, device, steps, warmup, sched):
+    """The batched sweep: 256 colonies of log-uniform size in one handle (skin mode, learned
+    scheduler when available, graph-replayed steps, launch parameters from the autotuner),
+    device-timed."""
+    from cil_cuda_gb300 import autotune as AT
+    from cil_cuda_gb300 import synthetic as S
+    ps, sts, caps = S.batched_sweep(256, steps=steps + warmup + 100)
+    skin = 0.3
+    inst = None
+    if sched:
+        from cil_cuda_gb300 import skin_scheduler as SS
+        skin = SS.load()[2]
+        inst = SS.install
+    tune, trials = AT.autotune(ps, sts, caps, skin=skin, steps=30, warmup=5, device=device, scheduler=inst)
+    eng = G.Engine(ps, caps, precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=11, device=device, skin=skin, **tune)
+    for c, st in enumerate(sts):
+        eng.upload(c, **st)
+    if sched:
+        SS.install(eng)
+    eng.step(warmup)
+    n0 = [eng.observables(c)["ncells"] for c in range(len(ps))]
+    eng.step(steps)
+    tm = eng.timings()
+    n1 = [eng.observables(c)["ncells"] for c in range(len(ps))]
+    gi = eng.graph_info()
+    eng.close()
+    dev_s = tm["total_ms"] * 1e-3
+    psteps = (sum(n0) + sum(n1)) * steps
+    sizes = np.array([len(s["sigma"]) for s in sts])
+    return {"value": psteps / dev_s, "unit": UNIT, "colonies": len(ps), "steps": steps,
+            "particles": 2 * int(sum(n0)), "cells_min_median_max": [int(sizes.min()), int(np.median(sizes)),
+                                                                    int(sizes.max())],
+            "ms_per_step": dev_s / steps * 1e3, "per_colony_ms_per_step": dev_s / steps * 1e3,
+            "form": "mixed precision, Verlet skin" + (" + learned scheduler" if sched else " 0.3 sigma"),
+            "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}":
+                                                              round(t["ms_per_step"], 4) for t in trials},
+            "graph_steps": gi["graph_steps"], "gpu_launches": tm["launches"]}
+
+
+def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tune=None):
     """The same metric through the reference-facing calls with host buffers: upload the
     colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
     call, each returning its status through a device->host read of the counters), and a
     frame download every GTS steps (outputFrame's input)."""
     import cil_cuda_gb300 as GG
     n = len(st["sigma"])
-    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin)
+    eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
+                   **(tune or {}))
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
     t0 = time.perf_counter()
     eng.upload(0, **st)
+    if sched:
+        from cil_cuda_gb300 import skin_scheduler as SS
+        SS.install(eng)
     for k in range(steps):
         eng.step(1)
         d2h += 56  # the per-call status read of the colony counters
@@ -263,6 +315,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--skin", type=float, default=0.3, help="Verlet skin of the skin form (sigma units)")
+    ap.add_argument("--no-sched", action="store_true", help="fixed skin instead of the learned scheduler")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
+    ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
     ap.add_argument("--only", choices=["mixed", "plain", "skin"], default=None,
                     help="run one form only (profiling)")
     args = ap.parse_args()
@@ -281,42 +336,65 @@ def main():
     hbm, peak_kind = peaks()
 
     plain_steps = max(1, args.steps // 10)
+    from cil_cuda_gb300 import skin_scheduler as SS
+    have_mlp = os.path.exists(SS.WEIGHTS) and not args.no_sched
+    mlp_skin = SS.load()[2] if have_mlp else args.skin
     if args.only == "mixed":
         plain = None
     else:
-        plain = run_form(G, p, st, G.PREC_FP64, plain_steps, args.warmup, device, 7 + rank, dist)
+        # individually launched steps: the phase timings (FP64 pair kernel) stay complete
+        plain = run_form(G, p, st, G.PREC_FP64, plain_steps, args.warmup, device, 7 + rank, dist, graphs=False)
     if args.only == "plain":
         print(json.dumps({"plain_fp64": plain["psteps"] / plain["dev_s"], "timings": plain["timings"]}))
         return 0
     mixed = None
+    fixed = None
     if args.only in (None, "mixed"):
         mixed = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist)
+    if args.only is None and have_mlp:
+        fixed = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist, skin=args.skin)
+    tune, trials = None, []
+    if args.only is None and not args.no_tune:
+        from cil_cuda_gb300 import autotune as AT
+        tune, trials = AT.autotune([p], [st], [CAP], skin=mlp_skin if have_mlp else args.skin, steps=50,
+                                   warmup=5, device=device, scheduler=SS.install if have_mlp else None)
     with Clocks(device) as clk:
         skinf = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist,
-                         skin=args.skin) if args.only in (None, "skin") else None
+                         skin=mlp_skin if have_mlp else args.skin,
+                         sched=have_mlp, tune=tune) if args.only in (None, "skin") else None
     clocks = clk.summary()
+    # kernel phases from individually launched steps (graph replays carry no phase events)
+    phases = run_form(G, p, st, G.PREC_MIXED, min(args.steps, 200), args.warmup, device, 7 + rank, dist,
+                      skin=mlp_skin if have_mlp else args.skin, sched=have_mlp, graphs=False, tune=tune) \
+        if skinf is not None else None
     if mixed is None:
         mixed = skinf
     if skinf is None:
-        skinf = mixed
+        skinf = phases = mixed
     if plain is None:
         plain = mixed
+    if fixed is None:
+        fixed = skinf
 
     t_max = allreduce_max(dist, skinf["dev_s"])
     ps_all = allreduce_sum(dist, skinf["psteps"])
     value = ps_all / t_max
     mixed_value = allreduce_sum(dist, mixed["psteps"]) / allreduce_max(dist, mixed["dev_s"])
+    fixed_value = allreduce_sum(dist, fixed["psteps"]) / allreduce_max(dist, fixed["dev_s"])
     t_plain = allreduce_max(dist, plain["dev_s"])
     plain_value = allreduce_sum(dist, plain["psteps"]) / t_plain
 
     # roofline of the dominant kernel (the fused pair-force + integrate kernel)
-    tm = skinf["timings"]
-    force_s = tm["force_ms"] * 1e-3 / args.steps
-    nelem = skinf["n0"] + skinf["n1"]  # mean elements per step (2 * mean cells)
+    tm = phases["timings"]
+    psteps_ph = min(args.steps, 200)
+    force_s = tm["force_ms"] * 1e-3 / psteps_ph
+    nelem = phases["n0"] + phases["n1"]  # mean elements per step (2 * mean cells)
     bytes_per_elem = 40  # pos in 16 + sigma 4 + id 4 + pos out 16 (2D, FP32-force form)
     achieved = bytes_per_elem * nelem / force_s / 1e9
     tp = plain["timings"]
     plain_force_s = tp["force_ms"] * 1e-3 / plain_steps
+    form = ("mixed precision, Philox noise, Verlet skin with the learned scheduler" if have_mlp
+            else f"mixed precision, Philox noise, Verlet skin {args.skin} sigma")
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -325,23 +403,32 @@ def main():
         "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
                                "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
                    "particles": skinf["n0"] * 2, "cells": skinf["n0"], "cells_end": skinf["n1"],
-                   "form": f"mixed precision, Philox noise, Verlet skin {args.skin} sigma",
+                   "form": form + ", CUDA-graph replay of steady steps",
                    "l2": "working set ~230 MB per step > 126 MB L2, no flush",
                    "parallelism": f"replicas x{world}"},
-        "forms": {"mixed_skin": value, "mixed_rebuild_every_step": mixed_value, "plain_fp64": plain_value,
+        "forms": {"mixed_skin_scheduled" if have_mlp else "mixed_skin": value,
+                  "mixed_skin_fixed_0.3": fixed_value,
+                  "mixed_rebuild_every_step": mixed_value, "plain_fp64": plain_value,
                   "speedup_vs_plain_fp64": value / plain_value},
         "skin_stats": skinf["skin"],
-        "phases_ms_per_step": {k: tm[k] / args.steps for k in ("rebuild_ms", "force_ms", "events_ms")},
+        "graph_steps": skinf["graphs"]["graph_steps"],
+        "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}":
+                                                          round(t["ms_per_step"], 4) for t in trials},
+        "phases_ms_per_step": {k: tm[k] / psteps_ph for k in ("rebuild_ms", "force_ms", "events_ms")},
         "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / hbm, "traffic": TRAFFIC_PER_LAUNCH, "peak_kind": peak_kind,
                      "kernel": "k_force_list<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
+                     "timed_on": f"{psteps_ph} individually launched steps (CUDA events around the force phase)",
                      "plain_fp64_kernel_GBps": 44 * nelem / plain_force_s / 1e9},
-        "gpu_launches": tm["launches"],
+        "gpu_launches": skinf["timings"]["launches"],
         "clocks": clocks,
     }
+    if args.only is None and not args.no_batched:
+        line["batched_sweep"] = run_batched(G, device, min(args.steps, 300), args.warmup, have_mlp)
     if not args.no_e2e:
-        e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, args.skin)
+        e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, mlp_skin if have_mlp else args.skin,
+                      sched=have_mlp, tune=tune)
         line["e2e"] = {"value": allreduce_sum(dist, e2e["value"]), "unit": UNIT,
                        "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]}
     if rank == 0 and not args.no_cpu:

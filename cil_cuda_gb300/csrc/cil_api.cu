@@ -66,6 +66,7 @@ struct cil_handle {
   int grid_cells = 0;
   int grid_force = 0;
   int stiles = 0;      // tiles over the slot capacity (grid of the list force kernel)
+  int list_variant = 0;  // list force kernel: staging depth and CTAs per SM (cil_config.staging/occupancy)
   int nsm = 0;
   bool geometry_ready = false;
   int64_t ts = 0;
@@ -641,7 +642,7 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 1), h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
   if (h->skin_mode)
-    launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->stream);
+    launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->list_variant, h->stream);
   else
     launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
   h->cur = 1 - h->cur;
@@ -802,8 +803,19 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->rng_mode != CIL_RNG_PHILOX && cfg->rng_mode != CIL_RNG_DSFMT) return CIL_ERR_CONFIG;
   if (cfg->skin < 0.0 || (cfg->skin > 0.0 && cfg->precision != CIL_PREC_MIXED)) return CIL_ERR_CONFIG;
   if (cfg->skin > 0.0 && cfg->num_colonies > kMaxSkinColonies) return CIL_ERR_CONFIG;
+  if (cfg->block_size != 0 && cfg->block_size != kTile) return CIL_ERR_CONFIG;
+  int list_variant = -1;
+  {
+    const int st = cfg->staging == 0 ? 4 : cfg->staging, oc = cfg->occupancy == 0 ? 4 : cfg->occupancy;
+    if (st == 4 && oc == 4) list_variant = 0;
+    if (st == 2 && oc == 4) list_variant = 1;
+    if (st == 8 && oc == 3) list_variant = 2;
+    if (st == 8 && oc == 2) list_variant = 3;
+    if (list_variant < 0) return CIL_ERR_CONFIG;
+  }
   auto *h = new cil_handle();
   h->cfg = *cfg;
+  h->list_variant = list_variant;
   h->B = cfg->num_colonies;
   h->D = cfg->dim;
   h->hc.resize(h->B);

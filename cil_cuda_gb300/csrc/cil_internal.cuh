@@ -25,7 +25,12 @@ constexpr int kDeadCap = 8192;    // apoptoses per colony per step handled on th
 constexpr int kListCap = 64;      // Verlet list entries per element (skin mode)
 constexpr int kFreshCap = 16384;  // elements created or moved by division between list rebuilds
 constexpr int kMaxSkinColonies = 4096;  // colonies per handle in skin mode (fresh-pair prefix in shared memory)
-constexpr int kListSlotBits = 27; // list entry = slot | (neighbour-bin index << 27)
+constexpr int kListSlotBits = 26; // list entry = slot | (bin offset code << 26)
+// bin offset code of a list entry: (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4, d* in {-1, 0, 1}
+__host__ __device__ __forceinline__ unsigned list_offset_code(int o, int D) {
+  return D == 2 ? static_cast<unsigned>((o / 3) | ((o % 3) << 2))
+                : static_cast<unsigned>((o / 9) | (((o / 3) % 3) << 2) | ((o % 3) << 4));
+}
 constexpr int kCellItems = 4;     // cells per thread in the event kernels
 constexpr int kCellTile = kTile * kCellItems;
 
@@ -293,6 +298,23 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float &n0, fl
   n1 = r * s;
 }
 
+// Philox words of the passive noise of one element (or cell) at step ts. In 2D one block of
+// four words serves two consecutive steps (the even step takes words 0-1, the odd one 2-3,
+// one Box-Muller pair each); in 3D each step takes a block of its own (two pairs).
+template <int D>
+__device__ __forceinline__ void noise_words(uint32_t id, int ts, uint32_t klo, uint32_t khi, uint32_t *w) {
+  if (D == 2) {
+    const u32x4 r = philox4x32_10(id, static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi);
+    const bool odd = (ts & 1) != 0;
+    w[0] = odd ? r.v[2] : r.v[0];
+    w[1] = odd ? r.v[3] : r.v[1];
+  } else {
+    const u32x4 r = philox4x32_10(id, static_cast<uint32_t>(ts), kRngNoise, 0u, klo, khi);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = r.v[q];
+  }
+}
+
 // [0, 1) with 53 random bits
 __device__ __forceinline__ double uniform53(uint32_t a, uint32_t b) {
   const uint64_t m = (static_cast<uint64_t>(a) << 21) ^ (static_cast<uint64_t>(b) >> 11);
@@ -517,7 +539,7 @@ void launch_tiles(const ColonyConst *col, ColonyCounters *cnt, int B, int which,
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s);
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block,
                   cudaStream_t s);
-void launch_force_list(const ForceArgs &a, int dim, int law, int grid, cudaStream_t s);
+void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, cudaStream_t s);
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);

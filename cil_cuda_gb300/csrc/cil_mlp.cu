@@ -156,6 +156,15 @@ __global__ void __launch_bounds__(kH) k_mlp_schedule(const float *params, SchedA
   __shared__ float w[kParams];
   __shared__ float x[kIn], z1[kH], h1[kH], z2[kH], h2[kH], y[kOut];
   static_assert(kIn == kSchedFeatures, "network input = scheduler features");
+  __shared__ int s_any;
+  if (threadIdx.x == 0) {
+    // most steps rebuild nothing: skip the weight load then
+    int any = 0;
+    for (int c = blockIdx.x; c < a.B; c += gridDim.x) any |= a.skin[c].rebuild_now;
+    s_any = any;
+  }
+  __syncthreads();
+  if (!s_any) return;  // uniform per block
   for (int i = threadIdx.x; i < kParams; i += blockDim.x) w[i] = params[i];
   __syncthreads();
   for (int c = blockIdx.x; c < a.B; c += gridDim.x) {

@@ -204,6 +204,7 @@ __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
 #pragma unroll
           for (int d = 0; d < D; ++d) ofs[d] = static_cast<float>(off[d]) * C.bwf[d] - ui[d];
           const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
+          const unsigned code = list_offset_code(o, D);
           if (o == NB / 2) occ = static_cast<unsigned>(r.y - r.x);  // the home bin
           for (int idx = r.x; idx < r.y; ++idx) {
             const int tt = static_cast<int>(a.perm[idx] & 0xffffffffu);
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
             }
             const float cut = C.rcs_f * 0.5f * (si + fabsf(pj.w)) + skin;
             if (r2 < cut * cut) {
-              if (n < kListCap) a.nbr[static_cast<size_t>(n) * SS + s] = tt | (o << kListSlotBits);
+              if (n < kListCap) a.nbr[static_cast<size_t>(n) * SS + s] = tt | static_cast<int>(code << kListSlotBits);
               ++n;
             }
           }

@@ -16,9 +16,11 @@ row (the features at that decision). A run's per-step cost at each skin is model
 its exact counters as
     t(s) = A * list_entries(s) + R * elements * rebuilds_per_step(s) + F * fresh(s) + B * elements,
 with the unit costs A, R, F, B fitted by least squares to device-timed runs of a large
-colony (fit_unit_costs). The label of every row of a configuration is the skin of least
-modelled cost over the grid and the mean rebuild interval observed at that skin. Training
-(train) uses only the project's CUDA kernels (cil_mlp_grad, cil_mlp_adam).
+colony (fit_unit_costs, each run advanced in one call with graph-replayed steps). The label
+of every row of a configuration is the skin of least modelled cost over the grid and the
+cadence that balances rebuild cost against the accumulating fresh elements at that skin
+(cadence_target). Training (train) uses only the project's CUDA kernels (cil_mlp_grad,
+cil_mlp_adam).
 """
 from __future__ import annotations
 
@@ -80,20 +82,32 @@ def trace_config(rng, ncells=None):
 
 def run_trace(G, p, st, skin, steps, warmup=20, seed=1, skin_max=SKIN_MAX, timed=False):
     """Runs one colony at a fixed skin (guard on, no cadence). Returns the feature rows of
-    its list rebuilds and its counters (and the device time per step when timed)."""
+    its list rebuilds and its counters, step by step; when timed, a second run of the same
+    colony and seed advances all steps in one call (graph-replayed, as in production) and
+    gives the device time per step."""
     n = len(st["sigma"])
-    eng = G.Engine([p], [int(1.3 * n) + 64], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, skin=skin_max)
+    cap = int(1.3 * n) + 64
+    ms = None
+    if timed:
+        eng = G.Engine([p], [cap], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, skin=skin_max)
+        try:
+            eng.upload(0, **st)
+            eng.set_skin(0, skin, 0)
+            eng.step(warmup)
+            eng.step(steps)
+            ms = eng.timings()["total_ms"] / steps
+        finally:
+            eng.close()
+    eng = G.Engine([p], [cap], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, skin=skin_max)
     try:
         eng.upload(0, **st)
         eng.set_skin(0, skin, 0)
         eng.step(warmup)
         k0 = eng.skin_stats(0)
-        rows, entries, fresh, ms = [], 0.0, 0.0, 0.0
+        rows, entries, fresh = [], 0.0, 0.0
         last = k0["nrebuild"]
         for _ in range(steps):
             eng.step(1)
-            if timed:
-                ms += eng.timings()["total_ms"]
             k = eng.skin_stats(0)
             entries += k["npairs"]
             fresh += k["nfresh"]
@@ -107,10 +121,10 @@ def run_trace(G, p, st, skin, steps, warmup=20, seed=1, skin_max=SKIN_MAX, timed
     nreb = k1["nrebuild"] - k0["nrebuild"]
     return dict(rows=np.array(rows, dtype=np.float32).reshape(-1, N_IN), elements=ne,
                 entries=entries / steps, fresh=fresh / steps, rebuild_rate=nreb / steps,
-                interval=steps / max(nreb, 1), ms_per_step=ms / steps if timed else None)
+                interval=steps / max(nreb, 1), ms_per_step=ms)
 
 
-def fit_unit_costs(G, ncells=200000, steps=120, seed=7):
+def fit_unit_costs(G, ncells=400000, steps=150, seed=7):
     """Device-timed runs of one large colony over the skin grid and a few noise levels;
     least-squares fit of t = A*entries + R*elements*rate + F*fresh + B*elements."""
     rng = np.random.default_rng(seed)
@@ -136,6 +150,19 @@ def modelled_ms(costs, r):
             + costs["B"] * r["elements"])
 
 
+def cadence_target(costs, r):
+    """Rebuild cadence that balances the cost of a rebuild against the growing cost of the
+    fresh elements between rebuilds: with fresh elements accumulating at rate q per step,
+    an interval T costs R*N/T + F*q*T/2 per step, least at T* = sqrt(2 R N / (F q)). The
+    guard still rebuilds earlier when elements move too far. q is read off the run's mean
+    fresh count over its mean interval (a sawtooth from 0 to q*T)."""
+    q = 2.0 * r["fresh"] / max(r["interval"], 1.0)
+    if q <= 0.0 or costs["F"] <= 0.0:
+        return 1000.0
+    t = math.sqrt(2.0 * costs["R"] * r["elements"] / (costs["F"] * q))
+    return float(min(max(t, 10.0), 1000.0))
+
+
 def make_dataset(G, costs, nconfigs=200, steps=300, seed=11, max_rows=24):
     """Inputs and labels from trace runs of nconfigs random configurations."""
     rng = np.random.default_rng(seed)
@@ -145,7 +172,8 @@ def make_dataset(G, costs, nconfigs=200, steps=300, seed=11, max_rows=24):
         runs = {s: run_trace(G, p, st, s, steps, seed=k + 1) for s in SKIN_GRID}
         cost = {s: modelled_ms(costs, r) for s, r in runs.items()}
         best = min(cost, key=cost.get)
-        target = (float(skin_to_y0(best)), float(interval_to_y1(runs[best]["interval"])))
+        cadence = cadence_target(costs, runs[best])
+        target = (float(skin_to_y0(best)), float(interval_to_y1(cadence)))
         for s, r in runs.items():
             rows = r["rows"]
             if len(rows) > max_rows:
@@ -153,7 +181,7 @@ def make_dataset(G, costs, nconfigs=200, steps=300, seed=11, max_rows=24):
             X.append(rows)
             T.append(np.tile(target, (len(rows), 1)))
         meta.append(dict(cells=len(st["sigma"]), motility=p["motility"][1], noise_D=p["noise_D"],
-                         tau=p["div_tau_mu"], best_skin=best, interval=runs[best]["interval"],
+                         tau=p["div_tau_mu"], best_skin=best, interval=runs[best]["interval"], cadence=cadence,
                          cost_ms={str(s): c for s, c in cost.items()}))
     return np.concatenate(X).astype(np.float32), np.concatenate(T).astype(np.float32), meta
 

@@ -196,3 +196,24 @@ def relax(p, state, stages=9, steps=300, final=1000, E=1000.0, seed=0, device=0)
     s = dict(state)
     s["pos"] = pos
     return s
+
+
+def batched_sweep(ncolonies=256, seed=2024, cells_lo=1000, cells_hi=64000, steps=5000, dt=1e-4):
+    """The batched sweep (fourth configuration): colonies of log-uniform size in
+    [cells_lo, cells_hi], each in its own periodic square at packing fraction 0.8, soft-core
+    growth physics with motility U[0.1, 2] and division time log-U[0.3, 3] (sd 10 %),
+    apoptosis 0.01/tau. Returns (params, states, capacities); capacities cover the growth
+    over `steps` steps with a 25 % margin."""
+    rng = np.random.default_rng(seed)
+    out_p, out_s, caps = [], [], []
+    for k in range(ncolonies):
+        n = int(round(math.exp(rng.uniform(math.log(cells_lo), math.log(cells_hi)))))
+        tau = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
+        p = growth_params(box=1.0, dt=dt, div_tau_mu=tau, div_tau_sigma=0.1 * tau, apop_rate=0.01 / tau,
+                          motility=[0.0, float(rng.uniform(0.1, 2.0))])
+        p, st = square_colony(n, p, seed=int(rng.integers(1, 2**31 - 1)))
+        growth = 2.0 ** (steps * dt / tau)
+        out_p.append(p)
+        out_s.append(st)
+        caps.append(int(n * growth * 1.25) + 64)
+    return out_p, out_s, caps

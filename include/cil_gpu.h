@@ -93,8 +93,13 @@ typedef struct cil_config {
   int32_t device;         /* CUDA device ordinal */
   double bin_width;       /* 0: cutoff of the largest element (+ skin); else at least this */
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
-  int32_t block_size;     /* threads per block of the pair kernel (0 = default) */
+  int32_t block_size;     /* threads per block of the force kernels: 0 or 256 */
   int32_t flags;          /* CIL_FLAG_* bits */
+  /* Verlet-list force kernel (skin mode): list entries in flight per thread (0 = 4; 2, 4, 8)
+   * and CTAs per SM it is compiled for (0 = 4; 2, 3, 4). Supported pairs: (2, 4), (4, 4),
+   * (8, 3), (8, 2); 3D always runs (4, 4). cil_cuda_gb300/autotune.py picks them. */
+  int32_t staging;
+  int32_t occupancy;
 } cil_config;
 
 /* cil_config.flags: run every step as individual launches (no CUDA graphs). By default, in
