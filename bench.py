@@ -172,6 +172,32 @@ def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0, s
     return dict(psteps=psteps, dev_s=dev_s, wall_s=wall, n0=n0, n1=n1, timings=tm, skin=sk, graphs=gi)
 
 
+def run_channel(G, device, steps, warmup):
+    """The 3D Hertzian channel (third configuration): 2M cells / 4M particles between flat
+    walls at z = 0 and 20 sigma, periodic 1024^2 in x and y, division on, dt = 5e-5; mixed
+    precision with Verlet lists (0.3 sigma), and the plain FP64 form on a tenth of the steps."""
+    from cil_cuda_gb300 import synthetic as S
+    p = S.channel_params(lxy=1024.0, height=20.0)
+    st = S.channel_colony(2_000_000, p, seed=3)
+    cap = 2_400_000
+    out = {}
+    for name, prec, skin, k in (("mixed_skin", G.PREC_MIXED, 0.3, steps),
+                                ("plain_fp64", G.PREC_FP64, 0.0, max(1, steps // 10))):
+        eng = G.Engine([p], [cap], precision=prec, rng=G.RNG_PHILOX, seed=5, device=device, skin=skin)
+        eng.upload(0, **st)
+        eng.step(warmup)
+        n0 = eng.observables(0)["ncells"]
+        eng.step(k)
+        tm = eng.timings()
+        n1 = eng.observables(0)["ncells"]
+        eng.close()
+        out[name] = (n0 + n1) * k / (tm["total_ms"] * 1e-3)
+        out[name + "_ms_per_step"] = tm["total_ms"] / k
+    return {"value": out["mixed_skin"], "unit": UNIT, "particles": 2 * len(st["sigma"]), "steps": steps,
+            "forms": out, "speedup_vs_plain_fp64": out["mixed_skin"] / out["plain_fp64"],
+            "config": "3D Hertz E=100, walls z=0 and 20, periodic 1024^2, phi=0.6 slab, dt=5e-5, D=0.005, division on"}
+
+
 def run_batched(G, device, steps, warmup, sched):
     """The batched sweep: 256 colonies of log-uniform size in one handle (skin mode, learned
     scheduler when available, graph-replayed steps, launch parameters from the autotuner),
@@ -426,6 +452,10 @@ def main():
     }
     if args.only is None and not args.no_batched:
         line["batched_sweep"] = run_batched(G, device, min(args.steps, 300), args.warmup, have_mlp)
+        try:
+            line["channel_3d"] = run_channel(G, device, min(args.steps, 200), args.warmup)
+        except G.CilError as e:  # reported, not fatal to the headline line
+            line["channel_3d"] = {"error": str(e)}
     if not args.no_e2e:
         e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, mlp_skin if have_mlp else args.skin,
                       sched=have_mlp, tune=tune)

@@ -117,6 +117,7 @@ struct cil_handle {
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
   int *d_tile_count = nullptr, *d_tile_off = nullptr;
   int *d_dead = nullptr;
+  int *d_divq = nullptr;  // division queue [CC]
   double *d_obs = nullptr;  // com_prev, disp, vref: 3 * D * CC
   bool obs_ready_any = false;
   std::vector<char> obs_ready;
@@ -158,7 +159,7 @@ void free_all(cil_handle *h) {
                   h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
-                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_obs,
+                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_divq, h->d_obs,
                   h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -399,6 +400,7 @@ EventArgs event_args(cil_handle *h) {
   a.tile_count = h->d_tile_count;
   a.tile_off = h->d_tile_off;
   a.dead = h->d_dead;
+  a.divq = h->d_divq;
   if (h->d_obs) {
     a.obs_com_prev = h->d_obs;
     a.obs_disp = h->d_obs + static_cast<size_t>(h->D) * h->CC;
@@ -436,6 +438,11 @@ SkinArgs skin_args(cil_handle *h, int force_rebuild) {
   a.key = h->d_key;
   a.bcount = h->d_bcount;
   a.force_rebuild = force_rebuild;
+  a.mlp = h->d_mlp;
+  a.use_interval = h->sched_use_interval;
+  a.skin_min = h->sched_skin_min;
+  a.skin_max = static_cast<float>(h->cfg.skin);
+  a.interval_scale = h->sched_interval_scale;
   a.grid = h->nsm * 16;  // fresh-pair kernel: 64 warps per SM over all colonies' fresh elements
   return a;
 }
@@ -604,19 +611,6 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     // re-sorts the slots on a fixed schedule and after uploads
     const bool permute = h->need_exact || h->lists_stale || (h->ts % h->permute_period) == 0;
     launch_skin_begin(skin_args(h, permute ? 1 : 0), h->stream);
-    if (h->d_mlp) {
-      SchedArgs sa{};
-      sa.skin = h->d_skin;
-      sa.sched = h->d_sched;
-      sa.cnt = h->d_cnt;
-      sa.B = h->B;
-      sa.use_interval = h->sched_use_interval;
-      sa.skin_min = h->sched_skin_min;
-      sa.skin_max = static_cast<float>(h->cfg.skin);
-      sa.interval_scale = h->sched_interval_scale;
-      launch_mlp_schedule(h->d_mlp, sa, h->stream);
-      h->launches += 1;
-    }
     if (permute) {
       st = do_rebuild(h);
       if (st != CIL_OK) return st;
@@ -657,7 +651,7 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
   } else {
     launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
     launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
-    h->launches += 7;
+    h->launches += 8;
   }
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
   CUDA_TRY(h, cudaGetLastError());
@@ -880,6 +874,9 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.div_tau_mu = p.div_tau_mu;
     C.div_tau_sigma = p.div_tau_sigma;
     C.apop_p = p.apop_rate * p.dt;
+    C.apop_log1m_p = static_cast<float>(std::log1p(-C.apop_p));
+    C.tau_mu_steps_f = static_cast<float>(p.div_tau_mu / p.dt);
+    C.tau_sd_steps_f = static_cast<float>(p.div_tau_sigma / p.dt);
     for (int j = 0; j < 2; ++j) {
       C.zeta_f[j] = static_cast<float>(C.zeta[j]);
       C.temp_f[j] = static_cast<float>(C.temp[j]);
@@ -964,10 +961,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
+  h->d_divq = dalloc<int>(static_cast<size_t>(h->CC));
   bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_eid[0] && h->d_eid[1] && h->d_sbin[0] &&
             h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
             h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
-            h->d_tile_count && h->d_tile_off && h->d_dead && h->d_ts &&
+            h->d_tile_count && h->d_tile_off && h->d_dead && h->d_divq && h->d_ts &&
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
             skin_ok;
   if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {

@@ -183,36 +183,39 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
 template <int D>
 __device__ void division_draws(const EventArgs &a, int g, double *dir_m, double *dir_d,
                                int &span_d, int &span_m, const ColonyConst &C) {
+  // fast mode: FP32 draws (the FP64 placement arithmetic stays in place / place_slot); the
+  // axes are FP32 unit vectors widened exactly to FP64
   const u32x4 r1 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv, 0u,
                                  a.seed_lo, a.seed_hi);
   const u32x4 r2 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv2, 0u,
                                  a.seed_lo, a.seed_hi);
+  const float k24 = 5.9604644775390625e-08f;  // 2^-24
   if (D == 2) {
-    double s, c;
-    sincospi(2.0 * uniform53(r1.v[0], r1.v[1]), &s, &c);
+    float s, c;
+    sincospif(2.0f * static_cast<float>(r1.v[0] >> 8) * k24, &s, &c);
     dir_m[0] = c;
     dir_m[1] = s;
-    sincospi(2.0 * uniform53(r1.v[2], r1.v[3]), &s, &c);
+    sincospif(2.0f * static_cast<float>(r1.v[1] >> 8) * k24, &s, &c);
     dir_d[0] = c;
     dir_d[1] = s;
   } else {
-    const double z1 = 2.0 * uniform53(r1.v[0], r1.v[1]) - 1.0;
-    const double z2 = 2.0 * uniform53(r1.v[2], r1.v[3]) - 1.0;
-    double s, c;
-    const double q1 = sqrt(fmax(0.0, 1.0 - z1 * z1)), q2 = sqrt(fmax(0.0, 1.0 - z2 * z2));
-    sincospi(2.0 * static_cast<double>(r2.v[2]) * 2.3283064365386963e-10, &s, &c);
+    const float z1 = 2.0f * static_cast<float>(r1.v[0] >> 8) * k24 - 1.0f;
+    const float z2 = 2.0f * static_cast<float>(r1.v[1] >> 8) * k24 - 1.0f;
+    const float q1 = sqrtf(fmaxf(0.0f, 1.0f - z1 * z1)), q2 = sqrtf(fmaxf(0.0f, 1.0f - z2 * z2));
+    float s, c;
+    sincospif(2.0f * static_cast<float>(r1.v[2] >> 8) * k24, &s, &c);
     dir_m[0] = q1 * c;
     dir_m[1] = q1 * s;
     dir_m[2] = z1;
-    sincospi(2.0 * static_cast<double>(r2.v[3]) * 2.3283064365386963e-10, &s, &c);
+    sincospif(2.0f * static_cast<float>(r1.v[3] >> 8) * k24, &s, &c);
     dir_d[0] = q2 * c;
     dir_d[1] = q2 * s;
     dir_d[2] = z2;
   }
   float n0, n1;
   box_muller(r2.v[0], r2.v[1], n0, n1);
-  const int sd = nint((C.div_tau_mu + C.div_tau_sigma * static_cast<double>(n0)) / C.dt);
-  const int sm = nint((C.div_tau_mu + C.div_tau_sigma * static_cast<double>(n1)) / C.dt);
+  const int sd = __float2int_rn(C.tau_mu_steps_f + C.tau_sd_steps_f * n0);
+  const int sm = __float2int_rn(C.tau_mu_steps_f + C.tau_sd_steps_f * n1);
   span_d = sd >= 1 ? sd : 1;  // randomTimeSpan, MD.cuh:434-436
   span_m = sm >= 1 ? sm : 1;
 }
@@ -268,10 +271,11 @@ __global__ void __launch_bounds__(kTile) k_div_scan(EventArgs a) {
   }
 }
 
-template <int D>
-__global__ void __launch_bounds__(kTile) k_div_apply(EventArgs a_) {
-  EventArgs a = a_;
-  a.ts = *a_.ts_dev;
+// due cells of the step, ranked in cell order: the first ndiv_allowed go to the colony's
+// division queue (the placement work runs in k_div_exec, so this scan stays light)
+__global__ void __launch_bounds__(kTile) k_div_rank(EventArgs a_) {
+  const EventArgs &a = a_;
+  const int ts = *a.ts_dev;
   const int total = a.tiles_cell[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_cell, a.B, t);
@@ -283,22 +287,37 @@ __global__ void __launch_bounds__(kTile) k_div_apply(EventArgs a_) {
     int cnt = 0;
 #pragma unroll
     for (int q = 0; q < kCellItems; ++q) {
-      due[q] = C.divide && i0 + q < n && a.tsw[C.cell_base + i0 + q] == a.ts;
+      due[q] = C.divide && i0 + q < n && a.tsw[C.cell_base + i0 + q] == ts;
       cnt += due[q] ? 1 : 0;
     }
     int tot;
     int rank = a.tile_off[t] + block_excl_scan_ev(cnt, &tot);
+    const int allowed = K.ndiv_allowed;
 #pragma unroll
     for (int q = 0; q < kCellItems; ++q) {
       if (!due[q]) continue;
-      if (rank < K.ndiv_allowed) {
-        double dm[D], dd[D];
-        int span_d, span_m;
-        division_draws<D>(a, C.cell_base + i0 + q, dm, dd, span_d, span_m, C);
-        divide_cell<D>(a, C, c, i0 + q, n + rank, dm, dd, a.ts + span_d, a.ts + span_m, K.nslot, rank);
-      }
+      if (rank < allowed) a.divq[C.cell_base + rank] = i0 + q;
       ++rank;
     }
+  }
+}
+
+// one thread per division of the queue: draws, FP64 placement of the four elements, new
+// cycles; daughters take cells n + rank and slots nslot + 2 rank
+template <int D>
+__global__ void __launch_bounds__(128) k_div_exec(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
+  const int c = blockIdx.y;
+  const ColonyConst &C = a.col[c];
+  const ColonyCounters &K = a.cnt[c];
+  const int nd = K.ndiv_allowed, n = K.ncell, nslot = K.nslot;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nd; r += gridDim.x * blockDim.x) {
+    const int i = a.divq[C.cell_base + r];
+    double dm[D], dd[D];
+    int span_d, span_m;
+    division_draws<D>(a, C.cell_base + i, dm, dd, span_d, span_m, C);
+    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
   }
 }
 
@@ -323,6 +342,80 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
 }
 
 // one block per colony: commit the divisions, then swap-with-last removal of the dead
+// warp-level path of k_apo_apply for k <= 32 deaths among n1 cells: distinct uniform picks
+// (redrawn while duplicated, at most 16 rounds), tombstones, then the live cells of the tail
+// [n1 - k, n1) move into the holes below it in ascending order (removeCell's swap-with-last,
+// Colony.cpp:365-399, for a sorted set of victims)
+__device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, ColonyCounters &K, int k, int n1,
+                          int D) {
+  const int lane = threadIdx.x & 31;
+  int v = 0x7fffffff;
+  bool need = lane < k;
+  for (int attempt = 0; attempt < 16; ++attempt) {
+    if (need) {
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(lane) | (static_cast<uint32_t>(attempt) << 24),
+                                    static_cast<uint32_t>(a.ts), kRngApoPick, static_cast<uint32_t>(c),
+                                    a.seed_lo, a.seed_hi);
+      const int x = static_cast<int>(uniform53(r.v[0], r.v[1]) * n1);
+      v = x < n1 ? x : n1 - 1;
+    }
+    // bitonic sort of the 32 lanes, ascending
+    for (int size = 2; size <= 32; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        const int o = __shfl_xor_sync(0xffffffffu, v, stride);
+        const bool up = (lane & size) == 0 || size == 32;
+        const bool low = (lane & stride) == 0;
+        v = (low == up) ? min(v, o) : max(v, o);
+      }
+    const int prev = __shfl_up_sync(0xffffffffu, v, 1);
+    need = lane > 0 && lane < k && v == prev;  // a duplicate: redraw it
+    if (!__any_sync(0xffffffffu, need)) break;
+    if (need) v = 0x7fffffff;  // sorts to the end, redrawn in the next round
+  }
+  // duplicates left after 16 rounds (practically impossible) are dropped
+  const int prev_v = __shfl_up_sync(0xffffffffu, v, 1);  // every lane takes part in a shuffle
+  const bool dup = lane > 0 && lane < k && v == prev_v;
+  const bool keep = lane < k && v < n1 && !dup;
+  const unsigned km = __ballot_sync(0xffffffffu, keep);
+  const int kk = __popc(km);
+  // the kept victims, ascending, to lanes 0..kk-1
+  int sdv = 0x7fffffff;
+  for (int src = 0; src < 32; ++src) {
+    const int val = __shfl_sync(0xffffffffu, v, src);
+    if (((km >> src) & 1u) && __popc(km & ((1u << src) - 1u)) == lane) sdv = val;
+  }
+  if (lane < kk) {
+    const int g = C.cell_base + sdv;
+    const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+    a.eid[s0] = -1;
+    a.eid[s1] = -1;
+    if (a.state) {
+      a.state[s0] = kSlotDead;
+      a.state[s1] = kSlotDead;
+      a.pk[s0].w = -fabsf(a.pk[s0].w);
+      a.pk[s1].w = -fabsf(a.pk[s1].w);
+    }
+  }
+  __syncwarp();
+  const int n2 = n1 - kk;
+  const int q = n2 + lane;
+  bool victim = false;
+  for (int src = 0; src < kk; ++src) {
+    const int vs = __shfl_sync(0xffffffffu, sdv, src);  // unconditional: every lane shuffles
+    victim = victim || vs == q;
+  }
+  const bool live = lane < kk && !victim;
+  const unsigned lm = __ballot_sync(0xffffffffu, live);
+  const int rank = __popc(lm & ((1u << lane) - 1u));
+  const int hole = __shfl_sync(0xffffffffu, sdv, rank & 31);
+  if (live) move_cell(a, C, hole, q, D);
+  __syncwarp();
+  if (lane == 0) {
+    K.ncell = n2;
+    K.napo_total += kk;
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
   EventArgs a = a_;
   a.ts = *a_.ts_dev;
@@ -344,22 +437,43 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
     if (C.apop_p > 0.0 && s_n1 > 0) {
       const u32x4 r = philox4x32_10(static_cast<uint32_t>(c), static_cast<uint32_t>(a.ts), kRngApo, 0u,
                                     a.seed_lo, a.seed_hi);
-      const double u = uniform53(r.v[0], r.v[1]);
-      const double nn = static_cast<double>(s_n1), p = C.apop_p;
-      double pk = exp(nn * log1p(-p)), cdf = pk;
-      while (u > cdf && k < s_n1 && k < kDeadCap) {
-        pk *= (nn - k) / (k + 1.0) * (p / (1.0 - p));
-        cdf += pk;
-        ++k;
-        if (pk < 1e-300 && cdf < u && k > nn * p + 40.0 * sqrt(nn * p + 1.0)) break;
+      const float nn = static_cast<float>(s_n1), p = static_cast<float>(C.apop_p);
+      const float mean = nn * p;
+      if (mean < 30.0f) {
+        // inversion of the binomial CDF from k = 0 (FP32: P(0) = exp(n log(1 - p)) >= e^-30);
+        // at most 200 terms (P(k > 200) is below FP32 resolution for a mean under 30)
+        const float u = static_cast<float>(r.v[0] >> 8) * 5.9604644775390625e-08f;
+        const float ratio = p / (1.0f - p);
+        float pk = __expf(nn * C.apop_log1m_p), cdf = pk;
+        while (u > cdf && k < s_n1 && k < kDeadCap && k < 200) {
+          pk *= (nn - static_cast<float>(k)) / static_cast<float>(k + 1) * ratio;
+          cdf += pk;
+          ++k;
+        }
+      } else {
+        // large means: normal approximation with continuity rounding
+        float z0, z1;
+        box_muller(r.v[0], r.v[1], z0, z1);
+        const float kf = rintf(mean + sqrtf(mean * (1.0f - p)) * z0);
+        k = kf < 0.0f ? 0 : static_cast<int>(fminf(kf, nn));
       }
-      if (k >= kDeadCap) K.err |= kErrCap;
+      if (k >= kDeadCap) {
+        K.err |= kErrCap;
+        k = kDeadCap - 1;
+      }
     }
     s_k = k;
+
   }
   __syncthreads();
   const int k = s_k, n1 = s_n1;
   if (k == 0) return;
+  if (k <= 32) {
+    // few deaths (the usual case): one warp, no block barriers
+    if (threadIdx.x >= 32) return;
+    apo_small(a, C, c, K, k, n1, D);
+    return;
+  }
   int P = 1;
   while (P < k) P <<= 1;
   // distinct uniform picks: draw, sort, redraw the duplicates (rare: about k^2 / 2n)
@@ -630,10 +744,12 @@ void launch_advance_ts(int *ts_dev, cudaStream_t s) { k_advance_ts<<<1, 1, 0, s>
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
   k_div_count<<<grid_cells, kTile, 0, s>>>(a);
   k_div_scan<<<a.B, kTile, 0, s>>>(a);
+  k_div_rank<<<grid_cells, kTile, 0, s>>>(a);
+  const dim3 g(8, a.B);
   if (dim == 2)
-    k_div_apply<2><<<grid_cells, kTile, 0, s>>>(a);
+    k_div_exec<2><<<g, 128, 0, s>>>(a);
   else
-    k_div_apply<3><<<grid_cells, kTile, 0, s>>>(a);
+    k_div_exec<3><<<g, 128, 0, s>>>(a);
   k_apo_apply<<<a.B, 1024, 0, s>>>(a, dim);
 }
 

@@ -66,7 +66,7 @@ struct ColonySkin {
 
 // Inputs of the learned skin scheduler, maintained on the device per colony in skin mode.
 // The 12 features are formed by k_skin_begin at every list rebuild (before the statistics
-// of the new build are reset); k_mlp_schedule turns them into the colony's next skin and
+// of the new build are reset); the scheduler network (k_skin_begin) turns them into the colony's next skin and
 // rebuild cadence.
 constexpr int kSchedFeatures = 12;
 struct SchedState {
@@ -136,6 +136,8 @@ struct ColonyConst {
   double dt;
   double div_tau_mu, div_tau_sigma;
   double apop_p;     // apoptosis probability per step
+  float apop_log1m_p;  // log(1 - apop_p) (FP32 binomial draw of the fast mode)
+  float tau_mu_steps_f, tau_sd_steps_f;  // division time mean and sd in steps (FP32 draws)
   // FP32 copies for the mixed-precision kernel (GB300 runs FP64 at ~1/64 of FP32, so the
   // mixed kernel keeps every per-element operation but the position update in FP32)
   float bwf[3];      // bin widths
@@ -488,6 +490,7 @@ struct EventArgs {
   int *tile_count;
   int *tile_off;
   int *dead;               // [B * kDeadCap]
+  int *divq;               // [CC] per colony: the cells dividing this step, in rank order
   double *obs_com_prev;    // [D * CC] or null
   double *obs_disp;
   double *obs_vref;
@@ -522,16 +525,54 @@ struct SkinArgs {
   int *bcount;
   int force_rebuild;       // host request for every colony this step
   int grid;                // blocks of the fresh-pair kernel
-};
-
-struct SchedArgs {
-  ColonySkin *skin;
-  SchedState *sched;
-  const ColonyCounters *cnt;
-  int B;
-  int use_interval;        // apply the predicted cadence (else only the skin)
+  // learned scheduler (null: skin and cadence stay as set)
+  const float *mlp;
+  int use_interval;
   float skin_min, skin_max, interval_scale;
 };
+
+// ---------------------------------------------------------------- scheduler network
+// 12 -> 64 -> 64 -> 2 multilayer perceptron, SiLU, FP32; one flat parameter vector
+//   W1[64][12] b1[64] W2[64][64] b2[64] W3[2][64] b3[2]
+constexpr int kMlpIn = 12, kMlpH = 64, kMlpOut = 2;
+constexpr int kMlpW1 = 0, kMlpB1 = kMlpW1 + kMlpH * kMlpIn, kMlpW2 = kMlpB1 + kMlpH,
+              kMlpB2 = kMlpW2 + kMlpH * kMlpH, kMlpW3 = kMlpB2 + kMlpH, kMlpB3 = kMlpW3 + kMlpOut * kMlpH,
+              kMlpParams = kMlpB3 + kMlpOut;
+
+__device__ __forceinline__ float mlp_silu(float z) { return z / (1.0f + expf(-z)); }
+
+// The network on one input, evaluated by one whole warp (every lane calls it): lane l owns
+// hidden units l and l + 32; every lane holds x; both outputs are returned to all lanes.
+// Weights are read from global memory (they stay in L2).
+__device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ w, const float *x, float *y) {
+  const int lane = threadIdx.x & 31;
+  float h1[2], h2[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int u = lane + 32 * q;
+    float z = __ldg(w + kMlpB1 + u);
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) z += __ldg(w + kMlpW1 + u * kMlpIn + k) * x[k];
+    h1[q] = mlp_silu(z);
+  }
+  float z2[2] = {__ldg(w + kMlpB2 + lane), __ldg(w + kMlpB2 + lane + 32)};
+  for (int v = 0; v < kMlpH; ++v) {
+    const float hv = __shfl_sync(0xffffffffu, v < 32 ? h1[0] : h1[1], v & 31);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) z2[q] += __ldg(w + kMlpW2 + (lane + 32 * q) * kMlpH + v) * hv;
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) h2[q] = mlp_silu(z2[q]);
+#pragma unroll
+  for (int o = 0; o < kMlpOut; ++o) {
+    float part = __ldg(w + kMlpW3 + o * kMlpH + lane) * h2[0] + __ldg(w + kMlpW3 + o * kMlpH + lane + 32) * h2[1];
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) part += __shfl_xor_sync(0xffffffffu, part, q);
+    y[o] = part + __ldg(w + kMlpB3 + o);
+  }
+}
+
+
 
 // ---------------------------------------------------------------- launchers (host side)
 void launch_tiles(const ColonyConst *col, ColonyCounters *cnt, int B, int which, int *tiles,
@@ -544,7 +585,6 @@ void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
 void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
-void launch_mlp_schedule(const float *params, const SchedArgs &a, cudaStream_t s);
 void launch_advance_ts(int *ts_dev, cudaStream_t s);
 int mlp_param_count();
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);

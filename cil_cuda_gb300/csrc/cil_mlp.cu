@@ -7,10 +7,9 @@
 // Gradients are formed per block in shared memory and summed over blocks in a fixed order,
 // so a training step is deterministic.
 //
-// Inference (k_mlp_schedule) runs on the device at every list rebuild of a colony: the
-// colony's features go through the network, output 0 becomes the skin
-// skin_min + (skin_max - skin_min) * sigmoid(y0) and output 1 the cadence
-// round(interval_scale * softplus(y1)).
+// Inference runs inside the skin-mode rebuild decision (k_skin_begin, one warp per colony,
+// mlp_forward_warp): output 0 becomes the skin skin_min + (skin_max - skin_min) * sigmoid(y0)
+// and output 1 the cadence round(interval_scale * softplus(y1)).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -22,9 +21,9 @@
 namespace cil {
 namespace {
 
-constexpr int kIn = 12, kH = 64, kOut = 2;
-constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kIn, kOffW2 = kOffB1 + kH, kOffB2 = kOffW2 + kH * kH,
-              kOffW3 = kOffB2 + kH, kOffB3 = kOffW3 + kOut * kH, kParams = kOffB3 + kOut;
+constexpr int kIn = kMlpIn, kH = kMlpH, kOut = kMlpOut;
+constexpr int kOffW1 = kMlpW1, kOffB1 = kMlpB1, kOffW2 = kMlpW2, kOffB2 = kMlpB2, kOffW3 = kMlpW3, kOffB3 = kMlpB3,
+              kParams = kMlpParams;
 constexpr int kSamplesPerBlock = 32;
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
@@ -148,50 +147,6 @@ __global__ void k_adam(float *params, const float *grad, float *m, float *v, int
 }
 
 }  // namespace
-
-// ---------------------------------------------------------------- scheduler inference
-// One block per rebuilding colony: the features formed by k_skin_begin go through the
-// network; output 0 sets the skin, output 1 the cadence (when enabled).
-__global__ void __launch_bounds__(kH) k_mlp_schedule(const float *params, SchedArgs a) {
-  __shared__ float w[kParams];
-  __shared__ float x[kIn], z1[kH], h1[kH], z2[kH], h2[kH], y[kOut];
-  static_assert(kIn == kSchedFeatures, "network input = scheduler features");
-  __shared__ int s_any;
-  if (threadIdx.x == 0) {
-    // most steps rebuild nothing: skip the weight load then
-    int any = 0;
-    for (int c = blockIdx.x; c < a.B; c += gridDim.x) any |= a.skin[c].rebuild_now;
-    s_any = any;
-  }
-  __syncthreads();
-  if (!s_any) return;  // uniform per block
-  for (int i = threadIdx.x; i < kParams; i += blockDim.x) w[i] = params[i];
-  __syncthreads();
-  for (int c = blockIdx.x; c < a.B; c += gridDim.x) {
-    ColonySkin &S = a.skin[c];
-    if (!S.rebuild_now) continue;  // uniform per block
-    if (threadIdx.x < kIn) x[threadIdx.x] = a.sched[c].features[threadIdx.x];
-    __syncthreads();
-    forward_one(w, x, z1, h1, z2, h2, y);
-    if (threadIdx.x == 0) {
-      const float sg = 1.0f / (1.0f + expf(-y[0]));
-      const float skin = a.skin_min + (a.skin_max - a.skin_min) * sg;
-      const float sp = y[1] > 20.0f ? y[1] : log1pf(expf(y[1]));
-      int interval = static_cast<int>(fminf(rintf(a.interval_scale * sp), 1e6f));
-      interval = interval < 1 ? 1 : interval;
-      S.skin = skin;
-      S.half2 = 0.25f * skin * skin;
-      S.interval = a.use_interval ? interval : 0;
-      a.sched[c].nsched += 1;
-    }
-    __syncthreads();
-  }
-}
-
-void launch_mlp_schedule(const float *params, const SchedArgs &a, cudaStream_t s) {
-  const int grid = a.B < 1024 ? a.B : 1024;
-  k_mlp_schedule<<<grid, kH, 0, s>>>(params, a);
-}
 
 int mlp_param_count() { return kParams; }
 

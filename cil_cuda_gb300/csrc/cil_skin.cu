@@ -53,9 +53,9 @@ __device__ __forceinline__ bool nb_bin(const ColonyConst &C, const int *bi, cons
 
 __device__ __forceinline__ float log_disp(float d) { return 0.25f * log10f(fmaxf(d, 1e-8f)) + 1.0f; }
 
-__global__ void k_skin_begin(SkinArgs a) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= a.B) return;
+// per colony (lane 0 of the colony's warp): the rebuild decision and, at a rebuild, the
+// scheduler's features; returns whether the colony rebuilds this step
+__device__ __forceinline__ int skin_begin_colony(const SkinArgs &a, int c) {
   ColonySkin &S = a.skin[c];
   int need = S.need;
   if (a.force_rebuild) need |= 8;
@@ -115,6 +115,38 @@ __global__ void k_skin_begin(SkinArgs a) {
   Q.step_max = 0.0f;
   S.steps_since += 1;
   S.maxdisp2 = 0u;
+  return now;
+}
+
+// one warp per colony: the decision, then (rebuilding colony, scheduler installed) the
+// network on the colony's features sets the skin of the new lists and the cadence
+__global__ void k_skin_begin(SkinArgs a) {
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= a.B) return;  // uniform per warp
+  const int lane = threadIdx.x & 31;
+  int now = 0;
+  if (lane == 0) now = skin_begin_colony(a, c);
+  now = __shfl_sync(0xffffffffu, now, 0);
+  if (!now || !a.mlp) return;  // uniform per warp
+  __syncwarp();
+  SchedState &Q = a.sched[c];
+  float x[kMlpIn];
+#pragma unroll
+  for (int k = 0; k < kMlpIn; ++k) x[k] = Q.features[k];
+  float y[kMlpOut];
+  mlp_forward_warp(a.mlp, x, y);
+  if (lane == 0) {
+    ColonySkin &S = a.skin[c];
+    const float sg = 1.0f / (1.0f + expf(-y[0]));
+    const float skin = a.skin_min + (a.skin_max - a.skin_min) * sg;
+    const float sp = y[1] > 20.0f ? y[1] : log1pf(expf(y[1]));
+    int interval = static_cast<int>(fminf(rintf(a.interval_scale * sp), 1e6f));
+    interval = interval < 1 ? 1 : interval;
+    S.skin = skin;
+    S.half2 = 0.25f * skin * skin;
+    S.interval = a.use_interval ? interval : 0;
+    Q.nsched += 1;
+  }
 }
 
 template <int D>
@@ -452,7 +484,7 @@ void fresh_d(const SkinArgs &a, int law, cudaStream_t s) {
 }  // namespace
 
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s) {
-  k_skin_begin<<<(a.B + 127) / 128, 128, 0, s>>>(a);
+  k_skin_begin<<<(32 * a.B + 127) / 128, 128, 0, s>>>(a);
 }
 
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s) {

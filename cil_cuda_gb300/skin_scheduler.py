@@ -36,9 +36,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "skin_mlp.npz")
 
 N_IN, N_H, N_OUT = 12, 64, 2
-SKIN_MIN, SKIN_MAX = 0.1, 0.5            # output range; SKIN_MAX also sizes the bins
+SKIN_MIN, SKIN_MAX = 0.1, 0.3            # output range; SKIN_MAX also sizes the bins
 INTERVAL_SCALE = 100.0                    # cadence = INTERVAL_SCALE * softplus(y1)
-SKIN_GRID = (0.1, 0.15, 0.2, 0.3, 0.4, 0.5)
+SKIN_GRID = (0.1, 0.15, 0.2, 0.25, 0.3)
 FEATURES = ("log_cells", "mean_occupancy", "max_occupancy", "mean_step", "max_step", "div_rate",
             "apo_rate", "skin", "log_interval", "disp_ratio", "trip_share", "fresh_share")
 
