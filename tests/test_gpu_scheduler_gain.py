@@ -24,10 +24,10 @@ STEPS, WARMUP = 400, 40
 def held_out():
     rng = np.random.default_rng(987654)
     out = []
-    for ncells, mot in ((150000, 0.3), (150000, 1.5), (60000, 1.0)):
+    for ncells, mot in ((1000000, 1.0), (150000, 0.3), (150000, 1.5), (60000, 1.0)):
         tau = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
-        p = S.growth_params(box=1024.0, div_tau_mu=tau, div_tau_sigma=0.1 * tau, apop_rate=0.01 / tau,
-                            motility=[0.0, mot])
+        p = S.growth_params(box=2048.0 if ncells > 500000 else 1024.0, div_tau_mu=tau, div_tau_sigma=0.1 * tau,
+                            apop_rate=0.01 / tau, motility=[0.0, mot])
         out.append((p, S.disk_colony(ncells, p, seed=int(rng.integers(1, 2**31 - 1)))))
     return out
 
