@@ -614,6 +614,8 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     if (permute) {
       st = do_rebuild(h);
       if (st != CIL_OK) return st;
+      // the re-sort compacted the slots: tile tables for the list build
+      launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
     } else {
       launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
       launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
@@ -621,13 +623,12 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
       ra.permute = 0;
       ra.skin = h->d_skin;  // only colonies with rebuild_now
       ra.state_out = nullptr;
-      launch_rebuild(ra, h->grid_slots, h->stream);
+      launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
     }
-    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
     launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
-    h->launches += permute ? 15 : 9;
+    h->launches += permute ? 15 : 8;
   } else {
     st = do_rebuild(h);
     if (st != CIL_OK) return st;

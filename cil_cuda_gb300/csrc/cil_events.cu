@@ -61,49 +61,15 @@ __device__ __forceinline__ void place(const ColonyConst &C, const double *master
   }
 }
 
-// exact bin and local coordinate of a freshly placed element (FP64, once per division)
-template <int D>
-__device__ __forceinline__ void place_slot(const EventArgs &a, const ColonyConst &C, int slot, const double *x) {
-  int b[D];
-  bin_coords<D>(C, x, b);
-  a.sbin[slot] = bin_id<D>(C, b);
-  if (a.pk) {
-    float4 p = a.pk[slot];
-#pragma unroll
-    for (int d = 0; d < D; ++d) pk_set(p, d, static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]));
-    a.pk[slot] = p;
-  }
-}
-
-// skin mode: a slot created or moved by a division joins the colony's fresh set and the
-// fresh list of its bin. The lists carry the colony's rebuild count as an epoch, so a list
-// rebuild empties them without touching memory. A slot moved a second time before the next
-// rebuild would sit in the list of its old bin: the colony rebuilds at the next step instead.
-__device__ __forceinline__ void mark_fresh(const EventArgs &a, const ColonyConst &C, int c, int slot, bool is_new,
-                                           int D) {
-  if (!a.state) return;
-  ColonySkin &S = a.skin[c];
-  if (is_new || a.state[slot] != kSlotFresh) {
-    const int idx = atomicAdd(&S.nfresh, 1);
-    if (idx < kFreshCap) {
-      a.fresh[c * kFreshCap + idx] = slot;
-      const unsigned long long ent =
-          (static_cast<unsigned long long>(static_cast<unsigned>(S.nrebuild)) << 32) | static_cast<unsigned>(slot);
-      a.fnext[slot] = atomicExch(&a.fhead[C.bin_base + a.sbin[slot]], ent);
-    } else {
-      atomicOr(&S.need, 2);
-    }
-  } else {
-    atomicOr(&S.need, 2);
-  }
-  a.state[slot] = kSlotFresh;
-  a.ncnt[slot] = 0;
-  float4 p = a.pk[slot];
-  p.w = -fabsf(p.w);  // skipped by the lists of normal elements
-  a.pk[slot] = p;
-  for (int d = 0; d < D; ++d) a.uref[d * a.SS + slot] = pk_c(p, d);
-}
-
+// Division of cell i into i (mother, its slots sb, sf) and k (daughter, new slots s0, s0+1):
+// binaryCellDivision (MD.cu:721-731) placement in FP64, then every output of the four
+// elements written once. All loads are issued before the first store, and each record is
+// formed in registers (no store-then-reload), so the per-division chain of memory round trips
+// stays short. In skin mode the four slots become fresh: one atomic reserves their entries
+// in the colony's fresh set, and each joins the fresh list of its bin. The lists carry the
+// colony's rebuild count as an epoch, so a list rebuild empties them without touching
+// memory; a slot that was already fresh (moved twice before a rebuild) would sit in the list
+// of its old bin, so the colony rebuilds at the next step instead.
 template <int D>
 __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int i, int k,
                             const double *dir_m, const double *dir_d, int tsw_d, int tsw_m,
@@ -111,60 +77,116 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
   const size_t SS = a.SS;
   const int g = C.cell_base + i, gk = C.cell_base + k;
   const int sb = a.slot_of[2 * g], sf = a.slot_of[2 * g + 1];
+  const int s0 = C.slot_base + nslot0 + 2 * rank;
+  const int slots[4] = {sb, sf, s0, s0 + 1};
+  // ---- loads
   double xb[D], xf[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     xb[d] = a.x[d * SS + sb];
     xf[d] = a.x[d * SS + sf];
   }
-  const double radius = 0.5 * C.rest0;
-  double m0[D], m1[D], d0[D], d1[D];
-  place<D>(C, xf, dir_m, radius, m1, m0);  // mother: master = front element
-  place<D>(C, xb, dir_d, radius, d0, d1);  // daughter: master = back element
-  const int s0 = C.slot_base + nslot0 + 2 * rank;
+  const double sgb = a.sigma_c[2 * g], sgf = a.sigma_c[2 * g + 1];
+  double sigb = 0.0, sigf = 0.0;
+  if (a.sig) {
+    sigb = a.sig[sb];
+    sigf = a.sig[sf];
+  }
+  float wb = 0.0f, wf = 0.0f;
+  if (a.pk) {
+    wb = fabsf(a.pk[sb].w);
+    wf = fabsf(a.pk[sf].w);
+  }
+  const bool skin = a.state != nullptr;
+  bool was_fresh_b = false, was_fresh_f = false;
+  if (skin) {
+    was_fresh_b = a.state[sb] == kSlotFresh;
+    was_fresh_f = a.state[sf] == kSlotFresh;
+  }
+  double ocp[D], odi[D], ovr[D];
+  if (a.obs_disp) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    a.x[d * SS + sb] = m0[d];
-    a.x[d * SS + sf] = m1[d];
-    a.x[d * SS + s0] = d0[d];
-    a.x[d * SS + s0 + 1] = d1[d];
+    for (int d = 0; d < D; ++d) {
+      ocp[d] = a.obs_com_prev[d * a.CC + g];
+      odi[d] = a.obs_disp[d * a.CC + g];
+      ovr[d] = a.obs_vref[d * a.CC + g];
+    }
+  }
+  // ---- placement (FP64), bins and records
+  const double radius = 0.5 * C.rest0;
+  double xs[4][D];
+  place<D>(C, xf, dir_m, radius, xs[1], xs[0]);  // mother: master = front element
+  place<D>(C, xb, dir_d, radius, xs[2], xs[3]);  // daughter: master = back element
+  int bins[4];
+  float4 rec[4];
+  const float wsign = skin ? -1.0f : 1.0f;  // fresh elements are skipped by the lists
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int b[D];
+    bin_coords<D>(C, xs[q], b);
+    bins[q] = bin_id<D>(C, b);
+    rec[q] = make_float4(0.0f, 0.0f, 0.0f, wsign * ((q & 1) ? wf : wb));
+#pragma unroll
+    for (int d = 0; d < D; ++d) pk_set(rec[q], d, static_cast<float>(xs[q][d] - static_cast<double>(b[d]) * C.bw[d]));
+  }
+  // ---- fresh-set entries and per-bin fresh lists (skin mode)
+  if (skin) {
+    ColonySkin &S = a.skin[c];
+    const bool push[4] = {!was_fresh_b, !was_fresh_f, true, true};
+    const int npush = 2 + (was_fresh_b ? 0 : 1) + (was_fresh_f ? 0 : 1);
+    if (was_fresh_b || was_fresh_f) atomicOr(&S.need, 2);
+    const int idx0 = atomicAdd(&S.nfresh, npush);
+    const unsigned epoch = static_cast<unsigned>(S.nrebuild);
+    unsigned long long prev[4];
+    bool listed[4];
+    int idx = idx0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      listed[q] = push[q] && idx < kFreshCap;
+      if (push[q]) {
+        if (listed[q]) {
+          a.fresh[c * kFreshCap + idx] = slots[q];
+          const unsigned long long ent =
+              (static_cast<unsigned long long>(epoch) << 32) | static_cast<unsigned>(slots[q]);
+          prev[q] = atomicExch(&a.fhead[C.bin_base + bins[q]], ent);
+        }
+        ++idx;
+      }
+    }
+    if (idx > kFreshCap) atomicOr(&S.need, 2);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (listed[q]) a.fnext[slots[q]] = prev[q];
+      a.state[slots[q]] = kSlotFresh;
+      a.ncnt[slots[q]] = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) a.uref[d * SS + slots[q]] = pk_c(rec[q], d);
+    }
+  }
+  // ---- stores
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) a.x[d * SS + slots[q]] = xs[q][d];
+    a.sbin[slots[q]] = bins[q];
+    if (a.pk) a.pk[slots[q]] = rec[q];
+    a.cyc[slots[q]] = make_int2(a.ts, q < 2 ? tsw_m : tsw_d);
+    if (a.vel) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) a.vel[d * SS + slots[q]] = 0.0;
+    }
   }
   // daughter diameters copied from the mother (canonical and binned copies)
-  a.sigma_c[2 * gk] = a.sigma_c[2 * g];
-  a.sigma_c[2 * gk + 1] = a.sigma_c[2 * g + 1];
+  a.sigma_c[2 * gk] = sgb;
+  a.sigma_c[2 * gk + 1] = sgf;
   if (a.sig) {
-    a.sig[s0] = a.sig[sb];
-    a.sig[s0 + 1] = a.sig[sf];
-  }
-  if (a.pk) {
-    a.pk[s0].w = a.pk[sb].w;
-    a.pk[s0 + 1].w = a.pk[sf].w;
+    a.sig[s0] = sigb;
+    a.sig[s0 + 1] = sigf;
   }
   a.eid[s0] = 2 * gk;
   a.eid[s0 + 1] = 2 * gk + 1;
   a.slot_of[2 * gk] = s0;
   a.slot_of[2 * gk + 1] = s0 + 1;
-  place_slot<D>(a, C, sb, m0);
-  place_slot<D>(a, C, sf, m1);
-  place_slot<D>(a, C, s0, d0);
-  place_slot<D>(a, C, s0 + 1, d1);
-  mark_fresh(a, C, c, sb, false, D);
-  mark_fresh(a, C, c, sf, false, D);
-  mark_fresh(a, C, c, s0, true, D);
-  mark_fresh(a, C, c, s0 + 1, true, D);
-  a.cyc[sb] = make_int2(a.ts, tsw_m);
-  a.cyc[sf] = make_int2(a.ts, tsw_m);
-  a.cyc[s0] = make_int2(a.ts, tsw_d);
-  a.cyc[s0 + 1] = make_int2(a.ts, tsw_d);
-  if (a.vel) {
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      a.vel[d * SS + sb] = 0.0;
-      a.vel[d * SS + sf] = 0.0;
-      a.vel[d * SS + s0] = 0.0;
-      a.vel[d * SS + s0 + 1] = 0.0;
-    }
-  }
   a.t0[g] = a.ts;
   a.t0[gk] = a.ts;
   a.tsw[gk] = tsw_d;
@@ -172,9 +194,9 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
   if (a.obs_disp) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      a.obs_com_prev[d * a.CC + gk] = a.obs_com_prev[d * a.CC + g];
-      a.obs_disp[d * a.CC + gk] = a.obs_disp[d * a.CC + g];
-      a.obs_vref[d * a.CC + gk] = a.obs_vref[d * a.CC + g];
+      a.obs_com_prev[d * a.CC + gk] = ocp[d];
+      a.obs_disp[d * a.CC + gk] = odi[d];
+      a.obs_vref[d * a.CC + gk] = ovr[d];
     }
   }
 }
@@ -183,7 +205,7 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
 template <int D>
 __device__ void division_draws(const EventArgs &a, int g, double *dir_m, double *dir_d,
                                int &span_d, int &span_m, const ColonyConst &C) {
-  // fast mode: FP32 draws (the FP64 placement arithmetic stays in place / place_slot); the
+  // fast mode: FP32 draws (the FP64 placement arithmetic stays in place / divide_cell); the
   // axes are FP32 unit vectors widened exactly to FP64
   const u32x4 r1 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv, 0u,
                                  a.seed_lo, a.seed_hi);

@@ -227,32 +227,62 @@ __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
         const float skin = S.skin;
         int bi[D];
         bin_decode<D>(C, a.sbin[s], bi);
+        // the 3^d bin ranges, loaded together; candidates are then taken as one flattened
+        // range in batches of kLB, so each batch costs two round trips (slots, then records)
+        constexpr int kLB = 8;
+        int start[NB], pre[NB + 1];
+        pre[0] = 0;
+#pragma unroll
         for (int o = 0; o < NB; ++o) {
           int off[3];
           nb_offsets<D>(o, off);
           int nb[D];
-          if (!nb_bin<D>(C, bi, off, nb)) continue;
-          float ofs[D];
-#pragma unroll
-          for (int d = 0; d < D; ++d) ofs[d] = static_cast<float>(off[d]) * C.bwf[d] - ui[d];
-          const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
-          const unsigned code = list_offset_code(o, D);
+          int2 r = make_int2(0, 0);
+          if (nb_bin<D>(C, bi, off, nb)) r = a.range[C.bin_base + bin_id<D>(C, nb)];
+          start[o] = r.x;
+          pre[o + 1] = pre[o] + (r.y - r.x);
           if (o == NB / 2) occ = static_cast<unsigned>(r.y - r.x);  // the home bin
-          for (int idx = r.x; idx < r.y; ++idx) {
-            const int tt = static_cast<int>(a.perm[idx] & 0xffffffffu);
-            if (tt == s) continue;
-            const int ej = a.eid[tt];
-            if ((ej >> 1) == g) continue;
-            const float4 pj = a.pk[tt];
+        }
+        const int ncand = pre[NB];
+        for (int k0 = 0; k0 < ncand; k0 += kLB) {
+          int tt[kLB], oo[kLB];
+#pragma unroll
+          for (int q = 0; q < kLB; ++q) {
+            const int kq = k0 + q;
+            int o = 0, base = start[0];  // select chain: constant indices keep the arrays in registers
+#pragma unroll
+            for (int b = 1; b < NB; ++b) {
+              if (kq >= pre[b]) {
+                o = b;
+                base = start[b] - pre[b];
+              }
+            }
+            oo[q] = o;
+            tt[q] = kq < ncand ? static_cast<int>(a.perm[base + kq] & 0xffffffffu) : -1;
+          }
+          int ej[kLB];
+          float4 pj[kLB];
+#pragma unroll
+          for (int q = 0; q < kLB; ++q) {
+            ej[q] = tt[q] >= 0 ? a.eid[tt[q]] : -2;
+            pj[q] = tt[q] >= 0 ? a.pk[tt[q]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          }
+#pragma unroll
+          for (int q = 0; q < kLB; ++q) {
+            if (tt[q] < 0 || tt[q] == s || (ej[q] >> 1) == g) continue;
+            int off[3];
+            nb_offsets<D>(oo[q], off);
             float r2 = 0.0f;
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-              const float dx = pk_c(pj, d) + ofs[d];
+              const float dx = pk_c(pj[q], d) + (static_cast<float>(off[d]) * C.bwf[d] - ui[d]);
               r2 += dx * dx;
             }
-            const float cut = C.rcs_f * 0.5f * (si + fabsf(pj.w)) + skin;
+            const float cut = C.rcs_f * 0.5f * (si + fabsf(pj[q].w)) + skin;
             if (r2 < cut * cut) {
-              if (n < kListCap) a.nbr[static_cast<size_t>(n) * SS + s] = tt | static_cast<int>(code << kListSlotBits);
+              if (n < kListCap)
+                a.nbr[static_cast<size_t>(n) * SS + s] =
+                    tt[q] | static_cast<int>(list_offset_code(oo[q], D) << kListSlotBits);
               ++n;
             }
           }
