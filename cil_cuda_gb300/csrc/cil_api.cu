@@ -94,6 +94,7 @@ struct cil_handle {
   float *d_uref = nullptr, *d_facc = nullptr;
   ColonySkin *d_skin = nullptr;
   int *d_ts = nullptr;           // device step counter (kernels read the step from here)
+  int *d_anyreb = nullptr;       // skin mode: [2] some colony rebuilds at step ts (ts & 1)
   // CUDA graphs of two steady steps, one per buffer parity (graph_gen: invalidation)
   std::vector<GraphSlot> graphs;
   uint64_t graph_gen = 0;
@@ -156,7 +157,7 @@ void free_all(cil_handle *h) {
   void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
                   h->d_eid[1], h->d_pk[0], h->d_pk[1], h->d_sbin[0], h->d_sbin[1],
                   h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
-                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_divq, h->d_obs,
@@ -438,6 +439,8 @@ SkinArgs skin_args(cil_handle *h, int force_rebuild) {
   a.key = h->d_key;
   a.bcount = h->d_bcount;
   a.force_rebuild = force_rebuild;
+  a.ts_dev = h->d_ts;
+  a.any_rebuild = h->d_anyreb;
   a.mlp = h->d_mlp;
   a.use_interval = h->sched_use_interval;
   a.skin_min = h->sched_skin_min;
@@ -622,6 +625,8 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
       RebuildArgs ra = rebuild_args(h);
       ra.permute = 0;
       ra.skin = h->d_skin;  // only colonies with rebuild_now
+      ra.any_rebuild = h->d_anyreb;
+      ra.ts_dev = h->d_ts;
       ra.state_out = nullptr;
       launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
     }
@@ -642,7 +647,7 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
-  launch_advance_ts(h->d_ts, h->stream);
+  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream);
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
   h->ts += 1;
   if (oracle) {
@@ -941,10 +946,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_facc = dalloc<float>(D * SS);
     h->d_fresh = dalloc<int>(static_cast<size_t>(h->B) * kFreshCap);
     h->d_fnext = dalloc<unsigned long long>(SS);
+    h->d_anyreb = dalloc<int>(2);
     h->d_skin = dalloc<ColonySkin>(h->B);
     h->d_sched = dalloc<SchedState>(h->B);
     skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_fresh &&
-              h->d_fnext && h->d_skin && h->d_sched;
+              h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
   h->d_vel = dalloc<double>(D * SS);
   h->d_key = dalloc<int>(SS);
@@ -1000,6 +1006,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     }
     cudaMemcpy(h->d_skin, sk.data(), sizeof(ColonySkin) * h->B, cudaMemcpyHostToDevice);
     cudaMemsetAsync(h->d_sched, 0, sizeof(SchedState) * h->B, h->stream);
+    cudaMemsetAsync(h->d_anyreb, 0, 2 * sizeof(int), h->stream);
     cudaMemsetAsync(h->d_facc, 0, sizeof(float) * D * SS, h->stream);
     cudaMemsetAsync(h->d_ncnt, 0, sizeof(int) * SS, h->stream);
     cudaMemsetAsync(h->d_state[0], kSlotDead, SS, h->stream);

@@ -121,7 +121,13 @@ __device__ __forceinline__ bool skip_colony(const RebuildArgs &a, int c) {
   return a.skin != nullptr && !a.skin[c].rebuild_now;
 }
 
+// skin mode: no colony rebuilds this step (uniform over the grid; checked before any barrier)
+__device__ __forceinline__ bool no_rebuild(const RebuildArgs &a) {
+  return a.any_rebuild != nullptr && a.any_rebuild[*a.ts_dev & 1] == 0;
+}
+
 __global__ void __launch_bounds__(kTile) k_scan_partial(RebuildArgs a) {
+  if (no_rebuild(a)) return;
   const int sb = blockIdx.x;
   if (skip_colony(a, a.scan_col[sb])) return;
   const ColonyConst &C = a.col[a.scan_col[sb]];
@@ -142,6 +148,7 @@ __global__ void __launch_bounds__(kTile) k_scan_partial(RebuildArgs a) {
 
 // one block per colony: exclusive scan of its scan-block sums; nlive = nslot = total
 __global__ void __launch_bounds__(kTile) k_scan_colony(RebuildArgs a) {
+  if (no_rebuild(a)) return;
   const int c = blockIdx.x;
   if (skip_colony(a, c)) return;
   const ColonyConst &C = a.col[c];
@@ -163,6 +170,7 @@ __global__ void __launch_bounds__(kTile) k_scan_colony(RebuildArgs a) {
 
 // per scan block: bin ranges
 __global__ void __launch_bounds__(kTile) k_scan_final(RebuildArgs a) {
+  if (no_rebuild(a)) return;
   const int sb = blockIdx.x;
   if (skip_colony(a, a.scan_col[sb])) return;
   const ColonyConst &C = a.col[a.scan_col[sb]];
@@ -183,6 +191,7 @@ __global__ void __launch_bounds__(kTile) k_scan_final(RebuildArgs a) {
 }
 
 __global__ void __launch_bounds__(kTile) k_scatter(RebuildArgs a) {
+  if (no_rebuild(a)) return;
   const int total = a.tiles_used[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_used, a.B, t);

@@ -757,11 +757,17 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
 }
 
 // the device step counter moves past the force step (before the events read it)
-__global__ void k_advance_ts(int *ts) { *ts += 1; }
+// (skin mode: also clears the next step's any-rebuild flag)
+__global__ void k_advance_ts(int *ts, int *any_rebuild) {
+  if (any_rebuild) any_rebuild[(*ts + 1) & 1] = 0;
+  *ts += 1;
+}
 
 }  // namespace
 
-void launch_advance_ts(int *ts_dev, cudaStream_t s) { k_advance_ts<<<1, 1, 0, s>>>(ts_dev); }
+void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s) {
+  k_advance_ts<<<1, 1, 0, s>>>(ts_dev, any_rebuild);
+}
 
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
   k_div_count<<<grid_cells, kTile, 0, s>>>(a);

@@ -414,6 +414,8 @@ struct RebuildArgs {
   const int *tswc;
   int exact;               // 1: reference FP64 bin formula and canonical gathers
   const ColonySkin *skin;  // skin mode: colonies without rebuild_now are skipped; else null
+  const int *any_rebuild;  // skin mode: [2] per step parity, 0 = no colony rebuilds (kernels return); else null
+  const int *ts_dev;
   int permute;             // 1: slots are re-sorted (data moves); 0: only the bin index is rebuilt
   unsigned char *state_out;// skin mode, permuting: slot states of the new order
   int *key;
@@ -525,6 +527,8 @@ struct SkinArgs {
   int *bcount;
   int force_rebuild;       // host request for every colony this step
   int grid;                // blocks of the fresh-pair kernel
+  const int *ts_dev;       // device step counter
+  int *any_rebuild;        // [2]: some colony rebuilds at step ts (index ts & 1), or null
   // learned scheduler (null: skin and cadence stay as set)
   const float *mlp;
   int use_interval;
@@ -585,7 +589,7 @@ void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
 void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
-void launch_advance_ts(int *ts_dev, cudaStream_t s);
+void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s);
 int mlp_param_count();
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,

@@ -125,7 +125,10 @@ __global__ void k_skin_begin(SkinArgs a) {
   if (c >= a.B) return;  // uniform per warp
   const int lane = threadIdx.x & 31;
   int now = 0;
-  if (lane == 0) now = skin_begin_colony(a, c);
+  if (lane == 0) {
+    now = skin_begin_colony(a, c);
+    if (now && a.any_rebuild) atomicOr(&a.any_rebuild[*a.ts_dev & 1], 1);
+  }
   now = __shfl_sync(0xffffffffu, now, 0);
   if (!now || !a.mlp) return;  // uniform per warp
   __syncwarp();
@@ -151,6 +154,7 @@ __global__ void k_skin_begin(SkinArgs a) {
 
 template <int D>
 __global__ void __launch_bounds__(kTile) k_skin_rebin(SkinArgs a) {
+  if (a.any_rebuild && a.any_rebuild[*a.ts_dev & 1] == 0) return;  // uniform
   const int total = a.tiles[a.B];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles, a.B, t);
@@ -192,6 +196,7 @@ __global__ void __launch_bounds__(kTile) k_skin_rebin(SkinArgs a) {
 template <int D, int LAW>
 __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
   constexpr int NB = (D == 2) ? 9 : 27;
+  if (a.any_rebuild && a.any_rebuild[*a.ts_dev & 1] == 0) return;  // uniform, before any barrier
   __shared__ unsigned s_occ_sum, s_occ_max, s_cnt;
   __shared__ unsigned long long s_pairs;
   __shared__ int s_over;
