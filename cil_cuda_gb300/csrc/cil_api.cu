@@ -330,7 +330,10 @@ cil_status do_rebuild(cil_handle *h, bool carry_vel = false, bool exact = false)
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
   h->need_exact = false;
   h->lists_stale = true;
-  if (carry_vel) std::swap(h->d_vel, h->d_vel2);
+  if (carry_vel) {
+    std::swap(h->d_vel, h->d_vel2);
+    h->graph_gen += 1;  // captured steps hold the old velocity buffer
+  }
   return CIL_OK;
 }
 
@@ -1248,6 +1251,7 @@ static cil_status run_obs(cil_handle *h, int32_t colony, int reset, cil_obs *out
     h->d_obs = dalloc<double>(3 * static_cast<size_t>(h->D) * h->CC);
     if (!h->d_obs) return fail(h, CIL_ERR_CUDA, "out of device memory (observables)");
     CUDA_TRY(h, cudaMemsetAsync(h->d_obs, 0, sizeof(double) * 3 * h->D * h->CC, h->stream));
+    h->graph_gen += 1;  // captured steps hold the event arguments without the observable arrays
   }
   std::vector<ColonyCounters> k;
   st = check_counters(h, &k);

@@ -53,3 +53,24 @@ def test_mixed_graph_matches_launches(gpu_lib, growth, skin):
     d = np.asarray(a["pos"]) - np.asarray(b["pos"])
     d -= np.round(d / p["box"][0]) * p["box"][0]
     assert np.abs(d).max() < 1e-4
+
+
+def test_graphs_follow_buffers_allocated_between_calls(gpu_lib, growth):
+    """Observables are allocated at the first obs_reset; steps captured before it must not be
+    replayed after it (they would hold no observable arrays and divisions would not carry the
+    tracks to the daughters)."""
+    p, st = growth
+    res = []
+    for graphs in (False, True):
+        n = len(st["sigma"])
+        eng = gpu_lib.Engine([p], [3 * n], precision=gpu_lib.PREC_FP64, rng=gpu_lib.RNG_PHILOX, seed=5,
+                             graphs=graphs)
+        eng.upload(0, **st)
+        eng.step(21)
+        eng.obs_reset(0)
+        eng.step(61)
+        res.append(eng.observables(0))
+        eng.close()
+    assert res[0]["ndiv_total"] > 0
+    for k in ("ncells", "mean_area", "msd", "vacf"):
+        assert res[0][k] == res[1][k], (k, res[0][k], res[1][k])
