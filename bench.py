@@ -40,9 +40,10 @@ NCELLS = 1_000_000
 BOX = 2048.0
 CAP = 1_200_000
 GTS = 100  # steps per output frame in the end-to-end arm
-# DRAM bytes per launch of k_force_list on this workload from an ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum); None until measured
-TRAFFIC_PER_LAUNCH = None
+# DRAM bytes per launch of k_force_list on this workload (learned scheduler, 2M particles) from one
+# ncu capture: dram__bytes_read.sum + dram__bytes_write.sum = 220.26 MB + 58.50 MB
+# (profiles/k_force_list_2d_softcore_2M.md)
+TRAFFIC_PER_LAUNCH = 278_759_168
 
 
 def peaks():
@@ -443,7 +444,8 @@ def main():
         "phases_ms_per_step": {k: tm[k] / psteps_ph for k in ("rebuild_ms", "force_ms", "events_ms")},
         "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": TRAFFIC_PER_LAUNCH, "peak_kind": peak_kind,
+                     "frac": achieved / hbm, "traffic": TRAFFIC_PER_LAUNCH, "traffic_unit": "bytes per launch (ncu)",
+                     "peak_kind": peak_kind,
                      "kernel": "k_force_list<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
                      "timed_on": f"{psteps_ph} individually launched steps (CUDA events around the force phase)",
                      "plain_fp64_kernel_GBps": 44 * nelem / plain_force_s / 1e9},
