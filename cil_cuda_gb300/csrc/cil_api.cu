@@ -92,6 +92,7 @@ struct cil_handle {
   int *d_nbr = nullptr, *d_ncnt = nullptr, *d_fresh = nullptr;
   unsigned long long *d_fhead = nullptr, *d_fnext = nullptr;  // per-bin fresh lists
   float *d_uref = nullptr, *d_facc = nullptr;
+  unsigned *d_ftouch = nullptr;  // one bit per slot: facc holds a fresh-pair contribution
   ColonySkin *d_skin = nullptr;
   int *d_ts = nullptr;           // device step counter (kernels read the step from here)
   int *d_anyreb = nullptr;       // skin mode: [2] some colony rebuilds at step ts (ts & 1)
@@ -157,7 +158,7 @@ void free_all(cil_handle *h) {
   void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
                   h->d_eid[1], h->d_pk[0], h->d_pk[1], h->d_sbin[0], h->d_sbin[1],
                   h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
-                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_divq, h->d_obs,
@@ -222,6 +223,10 @@ cil_status setup_geometry(cil_handle *h) {
       C.bw[d] = d < h->D ? hc.p.box[d] / C.ns[d] : 0.0;
       C.bwf[d] = static_cast<float>(C.bw[d]);
       C.inv_bwf[d] = d < h->D ? static_cast<float>(1.0 / C.bw[d]) : 0.0f;
+      if (d < 2) {
+        C.uq_scale[d] = static_cast<float>(65535.0 / C.bw[d]);
+        C.uq_inv[d] = static_cast<float>(C.bw[d] / 65535.0);
+      }
     }
   }
   if (bin_base != h->NBpad) {
@@ -357,6 +362,7 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
     a.ncnt = h->d_ncnt;
     a.uref = h->d_uref;
     a.facc = h->d_facc;
+    a.ftouch = h->d_ftouch;
     a.sched = h->d_sched;
   }
   a.sbin = h->d_sbin[h->meta];
@@ -439,6 +445,7 @@ SkinArgs skin_args(cil_handle *h, int force_rebuild) {
   a.fhead = h->d_fhead;
   a.fnext = h->d_fnext;
   a.facc = h->d_facc;
+  a.ftouch = h->d_ftouch;
   a.key = h->d_key;
   a.bcount = h->d_bcount;
   a.force_rebuild = force_rebuild;
@@ -947,12 +954,14 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_ncnt = dalloc<int>(SS);
     h->d_uref = dalloc<float>(D * SS);
     h->d_facc = dalloc<float>(D * SS);
+    h->d_ftouch = dalloc<unsigned>((SS + 31) / 32);
     h->d_fresh = dalloc<int>(static_cast<size_t>(h->B) * kFreshCap);
     h->d_fnext = dalloc<unsigned long long>(SS);
     h->d_anyreb = dalloc<int>(2);
     h->d_skin = dalloc<ColonySkin>(h->B);
     h->d_sched = dalloc<SchedState>(h->B);
-    skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_fresh &&
+    skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_ftouch &&
+              h->d_fresh &&
               h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
   h->d_vel = dalloc<double>(D * SS);
@@ -1011,6 +1020,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     cudaMemsetAsync(h->d_sched, 0, sizeof(SchedState) * h->B, h->stream);
     cudaMemsetAsync(h->d_anyreb, 0, 2 * sizeof(int), h->stream);
     cudaMemsetAsync(h->d_facc, 0, sizeof(float) * D * SS, h->stream);
+    cudaMemsetAsync(h->d_ftouch, 0, sizeof(unsigned) * ((SS + 31) / 32), h->stream);
     cudaMemsetAsync(h->d_ncnt, 0, sizeof(int) * SS, h->stream);
     cudaMemsetAsync(h->d_state[0], kSlotDead, SS, h->stream);
     cudaMemsetAsync(h->d_state[1], kSlotDead, SS, h->stream);

@@ -159,8 +159,12 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
       if (listed[q]) a.fnext[slots[q]] = prev[q];
       a.state[slots[q]] = kSlotFresh;
       a.ncnt[slots[q]] = 0;
+      if (D == 2) {
+        rec[q].z = uref_pack2(C.uq_scale, rec[q].x, rec[q].y);  // list reference in the record
+      } else {
 #pragma unroll
-      for (int d = 0; d < D; ++d) a.uref[d * SS + slots[q]] = pk_c(rec[q], d);
+        for (int d = 0; d < D; ++d) a.uref[d * SS + slots[q]] = pk_c(rec[q], d);
+      }
     }
   }
   // ---- stores

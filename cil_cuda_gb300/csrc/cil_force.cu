@@ -617,6 +617,9 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
   const int s = C.slot_base + (t - a.tiles[c]) * kTile + tid;
   const bool used = s < C.slot_base + a.cnt[c].nslot;
   const int e = used ? __ldg(a.eid + s) : -1;
+  // fresh-pair contributions: one bit per slot, one word per warp (slot bases are 32-aligned)
+  const unsigned tword = a.ftouch[s >> 5];
+  const bool touched = (tword >> (s & 31)) & 1u;
   float d2 = 0.0f, st2 = 0.0f;
   if (e >= 0) {
     // ---- loads
@@ -633,8 +636,13 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       xin[d] = __ldg(a.x_in + d * SS + s);
-      uref[d] = __ldg(a.uref + d * SS + s);
-      fa[d] = a.facc[d * SS + s];
+      fa[d] = touched ? a.facc[d * SS + s] : 0.0f;
+    }
+    if (D == 2) {
+      uref_unpack2(C.uq_inv, pi.z, uref);
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) uref[d] = __ldg(a.uref + d * SS + s);
     }
     const float4 pp = __ldg(a.pk + ps);
     const int sbp = __ldg(a.sbin + ps);
@@ -763,12 +771,15 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
 #pragma unroll
       for (int d = 0; d < D; ++d) a.frc[d * SS + s] = static_cast<double>(F[d]);
     }
+    if (touched) {
 #pragma unroll
-    for (int d = 0; d < D; ++d) a.facc[d * SS + s] = 0.0f;
+      for (int d = 0; d < D; ++d) a.facc[d * SS + s] = 0.0f;
+    }
     if (a.integrate) {
       const float temp = C.temp_f[j];
       bool inside = true;
-      float4 pn = make_float4(0.0f, 0.0f, 0.0f, pi.w);
+      // 2D: z carries the packed list reference to the next record
+      float4 pn = make_float4(0.0f, 0.0f, D == 2 ? pi.z : 0.0f, pi.w);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const float dxf = temp * F[d];
@@ -793,7 +804,13 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
       }
       a.pk_next[s] = pn;
       if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
-      if (d2 > s_half2) atomicOr(&a.skin[c].need, 1);
+      if (D == 2) {
+        // guard with the fixed-point rounding allowed for: trips no later than |u - uref| > skin/2
+        const float h = fmaxf(sqrtf(s_half2) - (C.uq_inv[0] + C.uq_inv[1]), 0.0f);
+        if (d2 > h * h) atomicOr(&a.skin[c].need, 1);
+      } else if (d2 > s_half2) {
+        atomicOr(&a.skin[c].need, 1);
+      }
       if (a.vel) {
 #pragma unroll
         for (int d = 0; d < D; ++d) a.vel[d * SS + s] = static_cast<double>(F[d] * C.mu_f[j]);
@@ -804,6 +821,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
     // stale record of two steps ago in the other buffer
     a.pk_next[s] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
   }
+  __syncwarp();  // every lane has read the touch word
+  if (tword != 0u && (tid & 31) == 0) a.ftouch[s >> 5] = 0u;
   if (a.integrate) {
     // displacement statistics: warp reductions, shared atomics, one global atomic each
     const unsigned dmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));

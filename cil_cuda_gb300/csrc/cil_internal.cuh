@@ -84,6 +84,21 @@ struct SchedState {
   float features[kSchedFeatures];  // input of the last decision
 };
 
+// 2D skin mode: an element's list reference rides in the record's unused z word as two 16-bit
+// fixed-point fractions of the bin width (resolution bw / 65535; list references lie in the
+// home bin, [0, bw)). The displacement guard allows for the rounding (uref_margin).
+struct ColonyConst;
+__device__ __forceinline__ float uref_pack2(const float *scale, float u0, float u1) {
+  const float a = fminf(fmaxf(rintf(u0 * scale[0]), 0.0f), 65535.0f);
+  const float b = fminf(fmaxf(rintf(u1 * scale[1]), 0.0f), 65535.0f);
+  return __uint_as_float(static_cast<unsigned>(a) | (static_cast<unsigned>(b) << 16));
+}
+__device__ __forceinline__ void uref_unpack2(const float *inv, float z, float *r) {
+  const unsigned v = __float_as_uint(z);
+  r[0] = static_cast<float>(v & 0xffffu) * inv[0];
+  r[1] = static_cast<float>(v >> 16) * inv[1];
+}
+
 // Mixed precision keeps each element as one 16-byte record, so a pair costs one load:
 //   xyz  FP32 coordinates relative to the origin of the element's home bin (sbin)
 //   w    FP32 diameter; in skin mode negative for elements the Verlet lists must skip
@@ -107,6 +122,8 @@ struct ColonyConst {
   // (2D: ns1; 3D: ns1*ns2 and ns2) by multiply-high with an invariant (Granlund and
   // Montgomery, "Division by invariant integers using multiplication", PLDI 1994, fig. 4.1)
   uint32_t div_m[2], div_s1[2], div_s2[2];
+  // 2D skin mode: 16-bit fixed-point list reference (fraction of the bin width per axis)
+  float uq_scale[2], uq_inv[2];
   int periodic[3];
   int single_bin;    // grid collapsed to one bin (some Ns < 3, Utils.hpp:897-901)
   int bin_base;      // first global bin
@@ -451,8 +468,9 @@ struct ForceArgs {
   ColonySkin *skin;
   const int *nbr;          // Verlet lists [kListCap][SS]
   const int *ncnt;
-  const float *uref;
+  const float *uref;       // 3D only (2D: packed in the record's z word)
   float *facc;             // pair forces of fresh elements / reactions [D][SS], consumed and zeroed
+  unsigned *ftouch;        // one bit per slot: facc holds a contribution
   SchedState *sched;       // speed statistics for the scheduler
   const double *noise;     // oracle mode: uploaded normals (already scaled), canonical order
   double *vel;             // slot order, may be null
@@ -523,6 +541,7 @@ struct SkinArgs {
   const unsigned long long *fhead;
   const unsigned long long *fnext;
   float *facc;
+  unsigned *ftouch;        // one bit per slot: facc holds a contribution
   int *key;
   int *bcount;
   int force_rebuild;       // host request for every colony this step

@@ -293,8 +293,12 @@ __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
           }
         }
         a.ncnt[s] = n < kListCap ? n : kListCap;
+        if (D == 2) {
+          a.pk[s].z = uref_pack2(C.uq_scale, ui[0], ui[1]);  // list reference in the record
+        } else {
 #pragma unroll
-        for (int d = 0; d < D; ++d) a.uref[d * SS + s] = ui[d];
+          for (int d = 0; d < D; ++d) a.uref[d * SS + s] = ui[d];
+        }
         a.state[s] = kSlotNormal;
         counted = 1u;
         a.pk[s].w = si;  // normal: visible to the lists of others
@@ -451,6 +455,7 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
           acc[d] += f0 * dx[d];
           atomicAdd(&a.facc[d * SS + tt], -f0 * dx[d]);
         }
+        atomicOr(&a.ftouch[tt >> 5], 1u << (tt & 31));
       }
     }
     // fresh partners: lane o walks the fresh list of bin o (current epoch only)
@@ -482,6 +487,7 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
       for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(0xffffffffu, v, q);
       if (lane == 0) atomicAdd(&a.facc[d * SS + f], v);
     }
+    if (lane == 0) atomicOr(&a.ftouch[f >> 5], 1u << (f & 31));
   }
 }
 
