@@ -41,9 +41,9 @@ BOX = 2048.0
 CAP = 1_200_000
 GTS = 100  # steps per output frame in the end-to-end arm
 # DRAM bytes per launch of k_force_list on this workload (learned scheduler, 2M particles) from one
-# ncu capture: dram__bytes_read.sum + dram__bytes_write.sum = 220.26 MB + 58.50 MB
+# ncu capture: dram__bytes_read.sum + dram__bytes_write.sum = 187.23 MB + 45.94 MB
 # (profiles/k_force_list_2d_softcore_2M.md)
-TRAFFIC_PER_LAUNCH = 278_759_168
+TRAFFIC_PER_LAUNCH = 233_163_008
 
 
 def peaks():
