@@ -241,30 +241,109 @@ def run_batched(G, device, steps, warmup, sched):
 def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tune=None):
     """The same metric through the reference-facing calls with host buffers: upload the
     colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
-    call, each returning its status through a device->host read of the counters), and a
-    frame download every GTS steps (outputFrame's input)."""
-    import cil_cuda_gb300 as GG
+    call, each returning its status through a device->host read of the counters), and a GSD
+    frame every GTS steps written by the device-fed frame writer (outputFrame,
+    OutputWriter.cpp:640-644; its copy to the host and its file writes overlap the next
+    steps). The file is flushed and closed inside the timed region."""
+    import tempfile
     n = len(st["sigma"])
     eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
                    **(tune or {}))
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
-    t0 = time.perf_counter()
-    eng.upload(0, **st)
-    if sched:
-        from cil_cuda_gb300 import skin_scheduler as SS
-        SS.install(eng)
-    for k in range(steps):
-        eng.step(1)
-        d2h += 56  # the per-call status read of the colony counters
-        if (k + 1) % GTS == 0 or k == steps - 1:
-            fr = eng.download(0)
-            d2h += fr["pos"].nbytes + fr["sigma"].nbytes + fr["vel"].nbytes + fr["t0"].nbytes + fr["tswitch"].nbytes
-    wall = time.perf_counter() - t0
-    n1 = fr["ncells"]
+    with tempfile.TemporaryDirectory() as tmp:
+        t0 = time.perf_counter()
+        eng.upload(0, **st)
+        if sched:
+            from cil_cuda_gb300 import skin_scheduler as SS
+            SS.install(eng)
+        w = eng.frame_writer(0, os.path.join(tmp, "e2e.gsd"))
+        for k in range(steps):
+            eng.step(1)
+            d2h += 56  # the per-call status read of the colony counters
+            if (k + 1) % GTS == 0 or k == steps - 1:
+                w.write()
+        w.close()
+        wall = time.perf_counter() - t0
+        fs = w.last_stats
+    n1 = eng.observables(0)["ncells"]
     eng.close()
-    del GG
-    return dict(value=(n + n1) * steps / wall, wall_s=wall, h2d=h2d / steps, d2h=d2h / steps)
+    d2h += fs["d2h_bytes"]
+    return dict(value=(n + n1) * steps / wall, wall_s=wall, h2d=h2d / steps, d2h=d2h / steps,
+                frames=fs["frames_written"], file_bytes=fs["file_bytes"])
+
+
+def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
+    """Cost of frame output at the headline workload: steps in cil_step(GTS) calls (graph
+    replay) with a GSD frame after every call, written (a) by the device-fed frame writer, whose
+    copy and file writes overlap the following steps, and (b) synchronously, the way the
+    reference's outputFrame runs: download the frame, then write the chunks on the host (the
+    library's GSD file layer) before stepping on; (c) no frames. Wall-clock times."""
+    import tempfile
+    out = {}
+    nframes = max(1, steps // GTS)
+    with tempfile.TemporaryDirectory() as tmp:
+        for mode in ("none", "async", "sync"):
+            eng = G.Engine([p], [CAP], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, device=device,
+                           skin=skin, **(tune or {}))
+            eng.upload(0, **st)
+            if sched:
+                from cil_cuda_gb300 import skin_scheduler as SS
+                SS.install(eng)
+            eng.step(GTS)
+            path = os.path.join(tmp, mode + ".gsd")
+            w = eng.frame_writer(0, path) if mode == "async" else None
+            gw = G.GSDWriter(path) if mode == "sync" else None
+            L = np.asarray(p["box"], np.float64)
+            t0 = time.perf_counter()
+            for _ in range(nframes):
+                eng.step(GTS)
+                if w is not None:
+                    w.write()
+                elif gw is not None:
+                    fr = eng.download(0, want=("pos", "sigma", "vel"))
+                    E = 2 * fr["ncells"]
+                    pos = np.zeros((E, 3), np.float32)
+                    x = fr["pos"].reshape(E, 2)
+                    pos[:, 0] = x[:, 0] - 0.5 * L[0]
+                    pos[:, 1] = x[:, 1] - 0.5 * L[1]
+                    pos[0::2, 2] = np.float32(-0.0)
+                    pos[1::2, 2] = np.float32(-0.01)
+                    vel = np.zeros((E, 3), np.float32)
+                    vel[:, :2] = fr["vel"].reshape(E, 2)
+                    dia = fr["sigma"].reshape(E).astype(np.float32)
+                    gw.write_chunk("configuration/step", np.array([0], np.uint64))
+                    gw.write_chunk("configuration/dimensions", np.array([3], np.uint8))
+                    gw.write_chunk("configuration/box", np.array([L[0], L[1], 1.0, 0, 0, 0], np.float32))
+                    gw.write_chunk("particles/N", np.array([E], np.uint32))
+                    gw.write_chunk("particles/Z", dia)
+                    gw.write_chunk("particles/diameter", dia)
+                    gw.write_chunk("particles/typeid", np.tile(np.array([0, 1], np.uint32), E // 2))
+                    gw.write_chunk("particles/charge", np.full(E, -1.0, np.float32))
+                    gw.write_chunk("particles/position", pos)
+                    gw.write_chunk("particles/velocity", vel)
+                    gw.write_chunk("particles/mass", np.zeros(E, np.float32))
+                    gw.end_frame()
+            if w is not None:
+                w.close()
+                st_w = w.last_stats
+            if gw is not None:
+                gw.close()
+            eng.step(1)  # drains the stream
+            wall = time.perf_counter() - t0
+            out[mode] = wall
+            if mode == "async":
+                out["async_stats"] = st_w
+            eng.close()
+    base = out["none"]
+    return {"frames": nframes, "steps_per_frame": GTS, "particles": 2 * len(st["sigma"]),
+            "bytes_per_frame_d2h": out["async_stats"]["d2h_bytes"] / nframes,
+            "file_bytes_per_frame": out["async_stats"]["file_bytes"] / nframes,
+            "wall_s": {k: out[k] for k in ("none", "async", "sync")},
+            "overhead_ms_per_frame": {"async_writer": (out["async"] - base) / nframes * 1e3,
+                                      "sync_download_and_write": (out["sync"] - base) / nframes * 1e3},
+            "writer_thread_ms_per_frame": out["async_stats"]["write_ms"] / nframes,
+            "enqueue_ms_per_frame": out["async_stats"]["enqueue_ms"] / nframes}
 
 
 def cpu_baseline(p, st, threads: int, budget_s: float = 20.0):
@@ -344,6 +423,7 @@ def main():
     ap.add_argument("--skin", type=float, default=0.3, help="Verlet skin of the skin form (sigma units)")
     ap.add_argument("--no-sched", action="store_true", help="fixed skin instead of the learned scheduler")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
+    ap.add_argument("--no-frames", action="store_true", help="skip the frame-output leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
     ap.add_argument("--only", choices=["mixed", "plain", "skin"], default=None,
                     help="run one form only (profiling)")
@@ -462,7 +542,11 @@ def main():
         e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, mlp_skin if have_mlp else args.skin,
                       sched=have_mlp, tune=tune)
         line["e2e"] = {"value": allreduce_sum(dist, e2e["value"]), "unit": UNIT,
-                       "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"]}
+                       "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
+                       "frames": e2e["frames"], "frame_every": GTS, "gsd_file_bytes": e2e["file_bytes"]}
+    if args.only is None and not args.no_frames:
+        line["frame_output"] = run_frames(G, p, st, min(args.steps, 1000), device, 7 + rank,
+                                          mlp_skin if have_mlp else args.skin, have_mlp, tune)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p, st, os.cpu_count() or 1)
     if rank == 0:

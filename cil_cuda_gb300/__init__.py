@@ -21,14 +21,16 @@ RNG_PHILOX, RNG_DSFMT = 0, 1
 FLAG_NO_GRAPH = 1
 
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
-          5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE"}
+          5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE", 8: "CIL_ERR_IO"}
 
 EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces",
             "cil_bins", "cil_obs_reset", "cil_observables", "cil_timings", "cil_last_error",
             "cil_version", "cil_host_rng_draw", "cil_bin_elements_noalloc", "cil_skin_stats",
             "cil_set_skin", "cil_set_scheduler", "cil_sched_state", "cil_mlp_num_params",
             "cil_mlp_workspace_floats", "cil_mlp_forward", "cil_mlp_grad", "cil_mlp_adam",
-            "cil_graph_info"]
+            "cil_graph_info", "cil_gsd_create", "cil_gsd_write_chunk", "cil_gsd_end_frame", "cil_gsd_nframes",
+            "cil_gsd_close", "cil_gsd_last_error", "cil_frame_open", "cil_frame_write", "cil_frame_flush",
+            "cil_frame_close", "cil_frame_get_stats", "cil_frame_last_error"]
 
 
 class CilError(RuntimeError):
@@ -132,6 +134,31 @@ class SchedInfo(C.Structure):
     ]
 
 
+class FrameOptions(C.Structure):
+    _fields_ = [
+        ("cell_name", C.c_char_p),
+        ("elem_names", C.c_char_p * 2),
+        ("length_unit", C.c_double),
+        ("lz", C.c_double),
+        ("flags", C.c_int32),
+        ("pad", C.c_int32),
+    ]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [
+        ("frames_queued", C.c_int64),
+        ("frames_written", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+        ("file_bytes", C.c_int64),
+        ("enqueue_ms", C.c_double),
+        ("slot_wait_ms", C.c_double),
+        ("write_ms", C.c_double),
+    ]
+
+
+FRAME_TYPES_IN_FIRST = 1
+
 _lib = None
 
 
@@ -189,6 +216,30 @@ def lib():
         L.cil_mlp_grad.argtypes = [vp, vp, vp, vp, i32, vp, vp, vp]
         L.cil_mlp_adam.restype = i32
         L.cil_mlp_adam.argtypes = [vp, vp, vp, vp, i32, C.c_float]
+        L.cil_gsd_create.restype = i32
+        L.cil_gsd_create.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(vp)]
+        L.cil_gsd_write_chunk.restype = i32
+        L.cil_gsd_write_chunk.argtypes = [vp, C.c_char_p, i32, C.c_uint64, C.c_uint32, vp]
+        L.cil_gsd_end_frame.restype = i32
+        L.cil_gsd_end_frame.argtypes = [vp]
+        L.cil_gsd_nframes.restype = C.c_uint64
+        L.cil_gsd_nframes.argtypes = [vp]
+        L.cil_gsd_close.restype = i32
+        L.cil_gsd_close.argtypes = [vp]
+        L.cil_gsd_last_error.restype = None
+        L.cil_gsd_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.cil_frame_open.restype = i32
+        L.cil_frame_open.argtypes = [vp, i32, C.c_char_p, C.POINTER(FrameOptions), C.POINTER(vp)]
+        L.cil_frame_write.restype = i32
+        L.cil_frame_write.argtypes = [vp, C.c_int64, C.POINTER(C.c_int64)]
+        L.cil_frame_flush.restype = i32
+        L.cil_frame_flush.argtypes = [vp]
+        L.cil_frame_close.restype = i32
+        L.cil_frame_close.argtypes = [vp]
+        L.cil_frame_get_stats.restype = i32
+        L.cil_frame_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
+        L.cil_frame_last_error.restype = None
+        L.cil_frame_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
@@ -236,6 +287,7 @@ class Engine:
         if st != 0:
             raise CilError(st, "cil_create failed")
         self.h = h
+        self._writers = []
 
     def _check(self, st: int):
         if st != 0:
@@ -244,9 +296,19 @@ class Engine:
             raise CilError(st, buf.value.decode())
 
     def close(self):
+        for w in list(getattr(self, "_writers", ())):
+            w.close()
         if getattr(self, "h", None):
             self.L.cil_destroy(self.h)
             self.h = None
+
+    def frame_writer(self, colony: int, path: str, *, cell_name: str = "A", elem_names=("BACK", "FRONT"),
+                     length_unit: float = 1.0, lz: float = 0.0, types_in_first: bool = False) -> "FrameWriter":
+        """GSD frame output of one colony (cil_frame_open, include/cil_gsd.h)."""
+        w = FrameWriter(self, colony, path, cell_name=cell_name, elem_names=elem_names, length_unit=length_unit,
+                        lz=lz, types_in_first=types_in_first)
+        self._writers.append(w)
+        return w
 
     def __del__(self):
         try:
@@ -392,3 +454,121 @@ def mlp_adam(params, grad, m, v, t: int, lr: float):
 
 def version() -> str:
     return lib().cil_version().decode()
+
+
+class FrameWriter:
+    """Device-fed GSD frame writer of one colony (include/cil_gsd.h, cil_frame_*): write()
+    enqueues a pack kernel and an asynchronous copy and returns; a host thread writes the
+    file. Close it (or the engine) to flush."""
+
+    def __init__(self, engine: Engine, colony: int, path: str, *, cell_name="A", elem_names=("BACK", "FRONT"),
+                 length_unit=1.0, lz=0.0, types_in_first=False):
+        self.engine = engine
+        self.L = engine.L
+        o = FrameOptions(cell_name=cell_name.encode(), length_unit=length_unit, lz=lz,
+                         flags=FRAME_TYPES_IN_FIRST if types_in_first else 0)
+        o.elem_names[0] = elem_names[0].encode()
+        o.elem_names[1] = elem_names[1].encode()
+        w = C.c_void_p()
+        engine._check(self.L.cil_frame_open(engine.h, colony, os.fsencode(path), C.byref(o), C.byref(w)))
+        self.w = w
+        self.path = path
+
+    def _check(self, st: int):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.L.cil_frame_last_error(self.w, buf, 512)
+            msg = buf.value.decode()
+            if not msg and self.engine.h:
+                self.L.cil_last_error(self.engine.h, buf, 512)
+                msg = buf.value.decode()
+            raise CilError(st, msg)
+
+    def write(self, step: int = -1) -> int:
+        """Queues a frame of the current state; step < 0 labels it with the engine's step."""
+        idx = C.c_int64()
+        self._check(self.L.cil_frame_write(self.w, step, C.byref(idx)))
+        return idx.value
+
+    def flush(self):
+        self._check(self.L.cil_frame_flush(self.w))
+
+    def stats(self) -> dict:
+        s = FrameStats()
+        self._check(self.L.cil_frame_get_stats(self.w, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in FrameStats._fields_}
+
+    def close(self):
+        """Flushes and closes; the final counters stay in last_stats."""
+        if getattr(self, "w", None):
+            fst = self.L.cil_frame_flush(self.w)
+            s = FrameStats()
+            self.L.cil_frame_get_stats(self.w, C.byref(s))
+            self.last_stats = {k: getattr(s, k) for k, _ in FrameStats._fields_}
+            buf = C.create_string_buffer(512)
+            self.L.cil_frame_last_error(self.w, buf, 512)
+            w, self.w = self.w, None
+            if self in self.engine._writers:
+                self.engine._writers.remove(self)
+            st = self.L.cil_frame_close(w)
+            if fst != 0 or st != 0:
+                raise CilError(fst or st, "cil_frame_close: " + buf.value.decode())
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class GSDWriter:
+    """The library's GSD 1.0 file writer (cil_gsd_*): chunks of the open frame, end_frame()
+    closes it. Needs no GPU."""
+
+    def __init__(self, path: str, application: str = "CIL", schema: str = "hoomd", schema_version=(1, 1)):
+        self.L = lib()
+        f = C.c_void_p()
+        ver = (schema_version[0] << 16) | schema_version[1]
+        st = self.L.cil_gsd_create(os.fsencode(path), application.encode(), schema.encode(), ver, C.byref(f))
+        if st != 0:
+            raise CilError(st, f"cil_gsd_create({path}) failed")
+        self.f = f
+
+    def _check(self, st: int):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.L.cil_gsd_last_error(self.f, buf, 512)
+            raise CilError(st, buf.value.decode())
+
+    def write_chunk(self, name: str, data, gsd_type: int | None = None):
+        """data: numpy array of 1 or 2 dimensions (N rows x M columns)."""
+        a = np.ascontiguousarray(data)
+        if gsd_type is None:
+            gsd_type = GSD_TYPE_OF[a.dtype.str.lstrip("<=|")]
+        n = a.shape[0] if a.ndim else 1
+        m = a.shape[1] if a.ndim > 1 else 1
+        ptr = a.ctypes.data_as(C.c_void_p) if a.size else None
+        self._check(self.L.cil_gsd_write_chunk(self.f, name.encode(), gsd_type, n, m, ptr))
+
+    def end_frame(self):
+        self._check(self.L.cil_gsd_end_frame(self.f))
+
+    @property
+    def nframes(self) -> int:
+        return int(self.L.cil_gsd_nframes(self.f))
+
+    def close(self):
+        if getattr(self, "f", None):
+            f, self.f = self.f, None
+            st = self.L.cil_gsd_close(f)
+            if st != 0:
+                raise CilError(st, "cil_gsd_close failed")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+GSD_TYPE_OF = {"u1": 1, "u2": 2, "u4": 3, "u8": 4, "i1": 5, "i2": 6, "i4": 7, "i8": 8, "f4": 9, "f8": 10}

@@ -15,7 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcilgpu.so")
-SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu"]
+SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu",
+           "cil_frame.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,7 +42,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs.append(obj)
         src_path = os.path.join(CSRC, src)
         deps = [src_path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
-        deps.append(os.path.join(ROOT, "include", "cil_gpu.h"))
+        deps += [os.path.join(ROOT, "include", h) for h in ("cil_gpu.h", "cil_gsd.h")]
         if (not ptxas_info and os.path.exists(obj)
                 and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
             continue
@@ -56,7 +57,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             failed.append(src)
     if failed:
         raise RuntimeError(f"nvcc failed for {failed}")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lpthread"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         sys.stdout.write(r.stdout)

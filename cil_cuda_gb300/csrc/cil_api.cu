@@ -1254,6 +1254,40 @@ cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *v) {
   return st;
 }
 
+}  // extern "C"
+
+cil_status cil::frame_source(cil_handle *h, int colony, FrameSource *out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "frame_source: bad arguments");
+  cil_status st = ensure_ready(h);
+  if (st != CIL_OK) return st;
+  std::vector<ColonyCounters> k;
+  st = check_counters(h, &k);
+  if (st != CIL_OK) return st;
+  const ColonyConst &C = h->cc[colony];
+  const HostColony &hc = h->hc[colony];
+  FrameSource s{};
+  s.x = h->d_x[h->cur];
+  s.vel = h->d_vel;
+  s.slot_of = h->d_slot_of;
+  s.sigma_c = h->d_sigma_c;
+  s.SS = h->SS;
+  s.cell_base = C.cell_base;
+  s.ncells = k[colony].ncell;
+  s.dim = h->D;
+  s.divide = hc.p.divide;
+  s.dying = hc.p.apop_rate > 0.0;
+  for (int d = 0; d < 3; ++d) s.box[d] = hc.p.box[d];
+  s.sigma_max = hc.sigma_max;
+  s.ts = h->ts;
+  s.device = h->cfg.device;
+  s.stream = h->stream;
+  *out = s;
+  return CIL_OK;
+}
+
+extern "C" {
+
 static cil_status run_obs(cil_handle *h, int32_t colony, int reset, cil_obs *out) {
   cil_status st = ensure_ready(h);
   if (st != CIL_OK) return st;

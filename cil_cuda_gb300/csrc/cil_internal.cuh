@@ -623,4 +623,32 @@ void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, cons
 void launch_observables(const EventArgs &a, int colony, int ncells, int dim, int reset,
                         double *partials, int nblocks, cudaStream_t s);
 
+// ---------------------------------------------------------------- frame output
+// The device state of one colony as the frame writer reads it: SoA FP64 positions and
+// velocities by slot (x[d * SS + slot]), the canonical element -> slot map and the canonical
+// diameters [cell][2]; valid on `stream` until the caller's next cil_step.
+struct FrameSource {
+  const double *x;
+  const double *vel;
+  const int *slot_of;
+  const double *sigma_c;
+  size_t SS;
+  int cell_base;
+  int ncells;
+  int dim;
+  int divide;
+  int dying;
+  double box[3];
+  double sigma_max;
+  int64_t ts;
+  int device;
+  cudaStream_t stream;
+};
+// Waits for the handle's queued work and fills *out (cil_api.cu).
+cil_status frame_source(cil_handle *h, int colony, FrameSource *out);
+// Packs a colony's elements in canonical order into FP32 frame arrays: position [E][3]
+// (shifted by -half, 2D z from zj[j]), velocity [E][3], diameter [E] (cil_frame.cu).
+void launch_frame_pack(const FrameSource &s, const double half[3], const float zj[2], float *out,
+                       cudaStream_t st);
+
 }  // namespace cil

@@ -32,7 +32,8 @@ typedef enum cil_status {
   CIL_ERR_NAN = 4,        /* non-finite force or position */
   CIL_ERR_OUT_OF_BOX = 5, /* an element left the box along a non-periodic axis (checkPositions, CIL.cu:945-966) */
   CIL_ERR_TIMEOUT = 6,    /* a bounded device wait gave up */
-  CIL_ERR_STATE = 7       /* handle not ready (e.g. step before upload) */
+  CIL_ERR_STATE = 7,      /* handle not ready (e.g. step before upload) */
+  CIL_ERR_IO = 8          /* a file could not be written (frame output, cil_gsd.h) */
 } cil_status;
 
 /* Pair-force laws (the reference's PairForceParams family, MD.cuh:23-344, with the

@@ -1,8 +1,12 @@
 #!/usr/bin/env bash
-# Compiles the parts of the reference that build standalone (its vendored dSFMT and the
-# header-only Random.hpp) from the reference tree into oracle/_ref/ for cross-checking
-# the oracle's restated RNG. Outputs go to oracle/_ref/ only (git-ignored). The rest of
-# the reference does not build (missing Cell.hpp/MD.hpp/CIL.hpp/Units.hpp, Boost, HDF5).
+# Compiles the parts of the reference that build standalone from the reference tree into
+# oracle/_ref/ (git-ignored):
+#   libref_random.so - its vendored dSFMT and Random.cpp, to cross-check the oracle's
+#                      restated RNG;
+#   libref_gsd.so    - its vendored GSD 1.0 library gsd.c, to read the files the frame writer
+#                      writes and to write the golden files it must reproduce byte for byte.
+# The rest of the reference does not build (missing Cell.hpp/MD.hpp/CIL.hpp/Units.hpp,
+# Boost, HDF5).
 set -euo pipefail
 REF=${CIL_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -17,3 +21,7 @@ g++ -O2 -fPIC -std=c++11 -DDSFMT_MEXP=19937 -I"$REF" -c "$REF/Random.cpp" -o "$O
 g++ -O2 -fPIC -std=c++11 -DDSFMT_MEXP=19937 -I"$REF" -c "$HERE/ref_random_shim.cpp" -o "$OUT/shim.o"
 g++ -shared -o "$OUT/libref_random.so" "$OUT/shim.o" "$OUT/Random.o" "$OUT/dSFMT.o"
 echo "built $OUT/libref_random.so"
+if [ -f "$REF/gsd.c" ]; then
+  gcc -O2 -fPIC -shared -I"$REF" "$REF/gsd.c" -o "$OUT/libref_gsd.so"
+  echo "built $OUT/libref_gsd.so"
+fi

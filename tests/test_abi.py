@@ -1,5 +1,6 @@
-"""The C-ABI library loads without a GPU and exports every entry point the public header
-declares; argument validation and the oracle-mode host stream work without a device."""
+"""The C-ABI library loads without a GPU and exports every entry point the public headers
+declare; argument validation and the oracle-mode host stream work without a device."""
+import glob
 import json
 import os
 import re
@@ -9,7 +10,7 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "cil_gpu.h")
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 @pytest.fixture(scope="module")
@@ -22,7 +23,7 @@ def G():
 
 
 def declared_functions():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(cil_[a-z_0-9]+)\s*\(", text)))
 
@@ -30,7 +31,8 @@ def declared_functions():
 def test_header_declares_expected_entry_points():
     names = declared_functions()
     for n in ("cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces",
-              "cil_bins", "cil_observables", "cil_obs_reset", "cil_last_error"):
+              "cil_bins", "cil_observables", "cil_obs_reset", "cil_last_error", "cil_gsd_create",
+              "cil_gsd_write_chunk", "cil_gsd_end_frame", "cil_frame_open", "cil_frame_write", "cil_frame_close"):
         assert n in names
 
 
