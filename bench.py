@@ -325,12 +325,14 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
                     gw.write_chunk("particles/mass", np.zeros(E, np.float32))
                     gw.end_frame()
             if w is not None:
+                w.flush()  # every frame in the file
+            eng.step(1)  # drains the stream
+            wall = time.perf_counter() - t0
+            if w is not None:
                 w.close()
                 st_w = w.last_stats
             if gw is not None:
                 gw.close()
-            eng.step(1)  # drains the stream
-            wall = time.perf_counter() - t0
             out[mode] = wall
             if mode == "async":
                 out["async_stats"] = st_w

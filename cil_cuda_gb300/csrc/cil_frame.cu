@@ -561,7 +561,17 @@ cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const
   for (int k = 0; ok && k < kSlots; ++k)
     ok = cudaEventCreateWithFlags(&w->packed[k], cudaEventDisableTiming) == cudaSuccess &&
          cudaEventCreateWithFlags(&w->copied[k], cudaEventDisableTiming) == cudaSuccess;
+  // staging for the colony's current size and a quarter more, so that frames of a growing
+  // colony rarely reallocate inside the run
+  const size_t need = 7 * static_cast<size_t>(2 * s.ncells);
+  const size_t cap = need + need / 4 + 1024;
+  for (int k = 0; ok && k < kSlots; ++k) {
+    ok = cudaMalloc(&w->d_buf[k], cap * sizeof(float)) == cudaSuccess &&
+         cudaHostAlloc(&w->h_buf[k], cap * sizeof(float), cudaHostAllocDefault) == cudaSuccess;
+    if (ok) w->cap[k] = cap;
+  }
   if (!ok) {
+    cudaGetLastError();
     w->release();
     cil_gsd_close(w->file);
     delete w;

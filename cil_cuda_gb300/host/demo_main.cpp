@@ -1,13 +1,16 @@
 // A reference-style main loop driving the GPU step through the MDIntegrator plug-in
 // (CIL.cu:1072-1127 shape: frames of GTS mdStep calls, host arrays read at frames).
 // Reads a colony from a binary file, runs `frames` x `gts` steps in oracle mode, writes
-// the final colony. Used by tests/test_cpp_host.py; not part of the library.
+// the final colony; with a sixth argument, also a GSD frame at step 0 and after every frame
+// of steps through the device-fed frame writer (outputFrame's GSD branch,
+// OutputWriter.cpp:708-712). Used by tests/test_cpp_host.py; not part of the library.
 //
 // input:  int32 ncells, int32 dim, int32 capacity, double[17] params (see below),
 //         pos[n*2*dim], sigma[n*2], int32 t0[n], int32 tswitch[n]
 // output: int32 ncells, int32 ts, pos, sigma, vel, t0, tswitch
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <vector>
 
 #include "gpu_euler.hpp"
@@ -16,7 +19,7 @@ typedef void (*MDIntegrator)(int &ts);
 
 int main(int argc, char **argv) {
   if (argc < 6) {
-    std::fprintf(stderr, "usage: %s in.bin out.bin frames gts seed\n", argv[0]);
+    std::fprintf(stderr, "usage: %s in.bin out.bin frames gts seed [frames.gsd]\n", argv[0]);
     return 2;
   }
   FILE *f = std::fopen(argv[1], "rb");
@@ -79,8 +82,16 @@ int main(int argc, char **argv) {
     cilgpu::GpuEuler plugin(cfg, p, cap, host, gts);
     cilgpu::bindGpuEuler(&plugin);
     MDIntegrator mdStep = cilgpu::gpuEuler;  // readMD's selection (Input.cpp:524-546)
-    for (int frame = 1; frame <= frames; ++frame)
+    std::unique_ptr<cilgpu::GpuGsdOutput> gsd;
+    if (argc > 6) {
+      gsd.reset(new cilgpu::GpuGsdOutput(plugin, argv[6]));  // initializeOutput (OutputWriter.cpp:714-721)
+      gsd->frame(ts);
+    }
+    for (int frame = 1; frame <= frames; ++frame) {
       for (int its = 0; its < gts; ++its) mdStep(ts);  // CIL.cu:1106
+      if (gsd) gsd->frame(ts);
+    }
+    gsd.reset();  // finalizeOutput: flush and close
     n = plugin.host().ncells;
   } catch (const std::exception &e) {
     std::fprintf(stderr, "%s\n", e.what());

@@ -9,6 +9,11 @@
 // where it reads them. `gpuEuler` is a free function with the MDIntegrator signature that
 // dispatches to the bound plug-in.
 //
+// GpuGsdOutput replaces the reference's GSD output of that colony (initGSDOutput,
+// outputGSDFrame and gsd_close, OutputWriter.cpp:619-644 and 726-735) with the device-fed
+// frame writer of cil_gsd.h: a frame is packed on the GPU and written by a host thread while
+// the next mdStep calls run.
+//
 // Errors follow the reference's run_assert (Utils.hpp:99-109): any status other than
 // CIL_OK throws std::runtime_error carrying cil_last_error().
 #pragma once
@@ -18,6 +23,7 @@
 #include <string>
 
 #include "cil_gpu.h"
+#include "cil_gsd.h"
 
 namespace cilgpu {
 
@@ -75,6 +81,10 @@ class GpuEuler {
 
   const SpeciesArrays &host() const { return host_; }
   cil_handle *handle() { return h_; }
+  // Uploads the host colony if no step has run yet (frame output before the first step).
+  void ensure_uploaded(int ts = 0) {
+    if (!uploaded_) upload(ts);
+  }
 
  private:
   cil_colony_view view() const {
@@ -108,6 +118,44 @@ class GpuEuler {
   std::function<SpeciesArrays(int)> grow_;
   bool uploaded_ = false;
   long long calls_ = 0;
+};
+
+// GSD frames of the plug-in's colony. frame(ts) is outputGSDFrame(fp, id, ts): the caller
+// passes the step label (the final-state file passes 0). Destruction flushes and closes.
+class GpuGsdOutput {
+ public:
+  GpuGsdOutput(GpuEuler &g, const std::string &path, const cil_frame_options *opt = nullptr) : g_(g) {
+    g_.ensure_uploaded();
+    const cil_status s = cil_frame_open(g_.handle(), 0, path.c_str(), opt, &w_);
+    if (s != CIL_OK) {
+      char buf[512];
+      cil_last_error(g_.handle(), buf, sizeof buf);
+      throw std::runtime_error("cil_frame_open(" + path + ") failed (" + std::to_string(static_cast<int>(s)) +
+                               "): " + buf);
+    }
+  }
+  ~GpuGsdOutput() { cil_frame_close(w_); }
+  GpuGsdOutput(const GpuGsdOutput &) = delete;
+  GpuGsdOutput &operator=(const GpuGsdOutput &) = delete;
+
+  void frame(int ts) { check(cil_frame_write(w_, ts, nullptr), "cil_frame_write"); }
+  void flush() { check(cil_frame_flush(w_), "cil_frame_flush"); }
+  cil_frame_stats stats() const {
+    cil_frame_stats s{};
+    cil_frame_get_stats(w_, &s);
+    return s;
+  }
+
+ private:
+  void check(cil_status s, const char *what) {
+    if (s == CIL_OK) return;
+    char buf[512];
+    cil_frame_last_error(w_, buf, sizeof buf);
+    if (!buf[0]) cil_last_error(g_.handle(), buf, sizeof buf);
+    throw std::runtime_error(std::string(what) + " failed (" + std::to_string(static_cast<int>(s)) + "): " + buf);
+  }
+  GpuEuler &g_;
+  cil_frame_writer *w_ = nullptr;
 };
 
 // The MDIntegrator-compatible entry point (assign `mdStep = cilgpu::gpuEuler;`).

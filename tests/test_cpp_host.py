@@ -38,7 +38,8 @@ def test_cpp_plugin_matches_oracle(gpu_lib, oracle_lib, tmp_path):
         f.write(st["tswitch"].astype(np.int32).tobytes())
     fout = tmp_path / "out.bin"
     frames, gts, seed = 4, 25, 31
-    r = subprocess.run([str(exe), str(fin), str(fout), str(frames), str(gts), str(seed)],
+    fgsd = tmp_path / "frames.gsd"
+    r = subprocess.run([str(exe), str(fin), str(fout), str(frames), str(gts), str(seed), str(fgsd)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     raw = open(fout, "rb").read()
@@ -63,3 +64,12 @@ def test_cpp_plugin_matches_oracle(gpu_lib, oracle_lib, tmp_path):
     d = pos - s["pos"]
     d -= np.round(d / 60.0) * 60.0
     assert np.abs(d).max() <= 1e-9
+    # the GSD frames written along the way: the last one is the final state
+    from cil_cuda_gb300.gsd import GSDFile
+    g = GSDFile(str(fgsd))
+    assert g.nframes == frames + 1
+    assert [int(g.read(k, "configuration/step")[0]) for k in range(g.nframes)] == [k * gts for k in range(frames + 1)]
+    assert int(g.read(0, "particles/N")[0]) == 2 * n and int(g.read(frames, "particles/N")[0]) == 2 * ng
+    exp = (pos.reshape(-1, 2) - 30.0).astype(np.float32)
+    np.testing.assert_array_equal(g.read(frames, "particles/position")[:, :2], exp)
+    np.testing.assert_array_equal(g.read(frames, "particles/diameter"), sig.reshape(-1).astype(np.float32))
