@@ -40,6 +40,7 @@ NCELLS = 1_000_000
 BOX = 2048.0
 CAP = 1_200_000
 GTS = 100  # steps per output frame in the end-to-end arm
+FRAME_CAP = 1_600_000  # cells: the frame-output leg grows the colony for 3000 steps
 # DRAM bytes per launch of k_force_list on this workload (learned scheduler, 2M particles) from one
 # ncu capture: dram__bytes_read.sum + dram__bytes_write.sum = 187.23 MB + 45.94 MB
 # (profiles/k_force_list_2d_softcore_2M.md)
@@ -284,7 +285,7 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
     nframes = max(1, steps // GTS)
     with tempfile.TemporaryDirectory() as tmp:
         for mode in ("none", "async", "sync"):
-            eng = G.Engine([p], [CAP], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, device=device,
+            eng = G.Engine([p], [FRAME_CAP], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=seed, device=device,
                            skin=skin, **(tune or {}))
             eng.upload(0, **st)
             if sched:
@@ -345,6 +346,8 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
             "overhead_ms_per_frame": {"async_writer": (out["async"] - base) / nframes * 1e3,
                                       "sync_download_and_write": (out["sync"] - base) / nframes * 1e3},
             "writer_thread_ms_per_frame": out["async_stats"]["write_ms"] / nframes,
+            "pack_kernel_ms_per_frame": out["async_stats"]["pack_ms"] / nframes,
+            "d2h_copy_ms_per_frame": out["async_stats"]["copy_ms"] / nframes,
             "enqueue_ms_per_frame": out["async_stats"]["enqueue_ms"] / nframes}
 
 
@@ -547,7 +550,7 @@ def main():
                        "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
                        "frames": e2e["frames"], "frame_every": GTS, "gsd_file_bytes": e2e["file_bytes"]}
     if args.only is None and not args.no_frames:
-        line["frame_output"] = run_frames(G, p, st, min(args.steps, 1000), device, 7 + rank,
+        line["frame_output"] = run_frames(G, p, st, 3000, device, 7 + rank,
                                           mlp_skin if have_mlp else args.skin, have_mlp, tune)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p, st, os.cpu_count() or 1)

@@ -154,6 +154,8 @@ class FrameStats(C.Structure):
         ("enqueue_ms", C.c_double),
         ("slot_wait_ms", C.c_double),
         ("write_ms", C.c_double),
+        ("pack_ms", C.c_double),
+        ("copy_ms", C.c_double),
     ]
 
 

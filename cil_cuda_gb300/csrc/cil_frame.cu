@@ -363,6 +363,7 @@ struct cil_frame_writer {
   int flags = 0;
   std::vector<char> types;  // [2][63]
   cudaStream_t copy = nullptr;
+  cudaEvent_t begin[kSlots] = {nullptr, nullptr};  // before the pack kernel
   cudaEvent_t packed[kSlots] = {nullptr, nullptr};
   cudaEvent_t copied[kSlots] = {nullptr, nullptr};
   float *d_buf[kSlots] = {nullptr, nullptr};
@@ -383,7 +384,7 @@ struct cil_frame_writer {
   std::vector<float> fill_buf;
   // counters
   int64_t queued = 0, done = 0, d2h_bytes = 0, file_bytes = 0;
-  double enqueue_ms = 0, slot_wait_ms = 0, write_ms = 0;
+  double enqueue_ms = 0, slot_wait_ms = 0, write_ms = 0, pack_ms = 0, copy_ms = 0;
 
   void set_error(cil_status s, const std::string &m) {  // caller holds mu
     if (err_st == CIL_OK) {
@@ -450,6 +451,11 @@ struct cil_frame_writer {
       cil_status st = CIL_OK;
       std::string m;
       const cudaError_t ce = cudaEventSynchronize(copied[j.slot]);
+      float pk = 0.0f, cp = 0.0f;
+      if (ce == cudaSuccess) {
+        cudaEventElapsedTime(&pk, begin[j.slot], packed[j.slot]);
+        cudaEventElapsedTime(&cp, packed[j.slot], copied[j.slot]);
+      }
       if (ce != cudaSuccess) {
         st = CIL_ERR_CUDA;
         m = std::string("frame copy: ") + cudaGetErrorString(ce);
@@ -472,6 +478,8 @@ struct cil_frame_writer {
         done += 1;
         file_bytes = file->file_size;
         write_ms += ms;
+        pack_ms += pk;
+        copy_ms += cp;
       }
       cv.notify_all();
     }
@@ -499,6 +507,7 @@ struct cil_frame_writer {
     }
     if (copy) cudaStreamSynchronize(copy);
     for (int s = 0; s < kSlots; ++s) {
+      if (begin[s]) cudaEventDestroy(begin[s]);
       if (packed[s]) cudaEventDestroy(packed[s]);
       if (copied[s]) cudaEventDestroy(copied[s]);
       if (d_buf[s]) cudaFree(d_buf[s]);
@@ -559,8 +568,8 @@ cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const
   }
   bool ok = cudaStreamCreateWithFlags(&w->copy, cudaStreamNonBlocking) == cudaSuccess;
   for (int k = 0; ok && k < kSlots; ++k)
-    ok = cudaEventCreateWithFlags(&w->packed[k], cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&w->copied[k], cudaEventDisableTiming) == cudaSuccess;
+    ok = cudaEventCreate(&w->begin[k]) == cudaSuccess && cudaEventCreate(&w->packed[k]) == cudaSuccess &&
+         cudaEventCreate(&w->copied[k]) == cudaSuccess;
   // staging for the colony's current size and a quarter more, so that frames of a growing
   // colony rarely reallocate inside the run
   const size_t need = 7 * static_cast<size_t>(2 * s.ncells);
@@ -614,8 +623,8 @@ cil_status cil_frame_write(cil_frame_writer *w, int64_t step, int64_t *frame) {
     }
     w->cap[slot] = cap;
   }
-  cudaError_t ce = cudaSuccess;
-  if (E > 0) {
+  cudaError_t ce = cudaEventRecord(w->begin[slot], s.stream);
+  if (ce == cudaSuccess && E > 0) {
     cil::launch_frame_pack(s, w->half, w->zj, w->d_buf[slot], s.stream);
     ce = cudaGetLastError();
   }
@@ -673,6 +682,8 @@ cil_status cil_frame_get_stats(const cil_frame_writer *w, cil_frame_stats *out) 
   out->enqueue_ms = w->enqueue_ms;
   out->slot_wait_ms = w->slot_wait_ms;
   out->write_ms = w->write_ms;
+  out->pack_ms = w->pack_ms;
+  out->copy_ms = w->copy_ms;
   return CIL_OK;
 }
 

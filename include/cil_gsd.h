@@ -120,9 +120,10 @@ cil_status cil_frame_flush(cil_frame_writer *w);
 /* Flushes, closes the file and frees the writer. NULL is a no-op. */
 cil_status cil_frame_close(cil_frame_writer *w);
 
-/* Counters of the writer: frames queued and written, bytes copied from the device, and the
+/* Counters of the writer: frames queued and written, bytes copied from the device, the
  * host time spent inside cil_frame_write (enqueue, waits for a free slot included) and in
- * the writer thread (copy wait and file writes). */
+ * the writer thread (copy wait and file writes), and the device time of the pack kernels and
+ * of the device-to-host copies (CUDA events, summed over the frames written). */
 typedef struct cil_frame_stats {
   int64_t frames_queued;
   int64_t frames_written;
@@ -131,6 +132,8 @@ typedef struct cil_frame_stats {
   double enqueue_ms;
   double slot_wait_ms;
   double write_ms;
+  double pack_ms;
+  double copy_ms;
 } cil_frame_stats;
 
 cil_status cil_frame_get_stats(const cil_frame_writer *w, cil_frame_stats *out);
