@@ -30,7 +30,8 @@ EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step
             "cil_mlp_workspace_floats", "cil_mlp_forward", "cil_mlp_grad", "cil_mlp_adam",
             "cil_graph_info", "cil_gsd_create", "cil_gsd_write_chunk", "cil_gsd_end_frame", "cil_gsd_nframes",
             "cil_gsd_close", "cil_gsd_last_error", "cil_frame_open", "cil_frame_write", "cil_frame_flush",
-            "cil_frame_close", "cil_frame_get_stats", "cil_frame_last_error"]
+            "cil_frame_close", "cil_frame_get_stats", "cil_frame_last_error", "cil_input_load", "cil_input_config",
+            "cil_input_initial_state", "cil_input_last_error", "cil_input_free"]
 
 
 class CilError(RuntimeError):
@@ -159,6 +160,23 @@ class FrameStats(C.Structure):
     ]
 
 
+class RunInfo(C.Structure):
+    _fields_ = [
+        ("gts", C.c_int32),
+        ("frames", C.c_int32),
+        ("output_gsd", C.c_int32),
+        ("output_h5", C.c_int32),
+        ("ncells", C.c_int32),
+        ("capacity", C.c_int32),
+        ("use_scheduler", C.c_int32),
+        ("seed", C.c_int32),
+        ("output_dir", C.c_char * 256),
+        ("output_name", C.c_char * 256),
+        ("cell_name", C.c_char * 64),
+        ("elem_names", (C.c_char * 64) * 2),
+    ]
+
+
 FRAME_TYPES_IN_FIRST = 1
 
 _lib = None
@@ -242,6 +260,16 @@ def lib():
         L.cil_frame_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
         L.cil_frame_last_error.restype = None
         L.cil_frame_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.cil_input_load.restype = i32
+        L.cil_input_load.argtypes = [C.c_char_p, i32, C.POINTER(vp)]
+        L.cil_input_config.restype = i32
+        L.cil_input_config.argtypes = [vp, C.POINTER(Config), C.POINTER(ColonyParams), C.POINTER(RunInfo)]
+        L.cil_input_initial_state.restype = i32
+        L.cil_input_initial_state.argtypes = [vp, C.POINTER(ColonyView)]
+        L.cil_input_last_error.restype = None
+        L.cil_input_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.cil_input_free.restype = None
+        L.cil_input_free.argtypes = [vp]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
@@ -574,3 +602,73 @@ class GSDWriter:
 
 
 GSD_TYPE_OF = {"u1": 1, "u2": 2, "u4": 3, "u8": 4, "i1": 5, "i2": 6, "i4": 7, "i8": 8, "f4": 9, "f8": 10}
+
+
+def _struct_dict(st) -> dict:
+    out = {}
+    for k, _ in st._fields_:
+        v = getattr(st, k)
+        if isinstance(v, C.Array):
+            v = [x.value.decode() if isinstance(x, C.Array) else x for x in v]
+        elif isinstance(v, bytes):
+            v = v.decode()
+        out[k] = v
+    return out
+
+
+class RunInput:
+    """The reference's JSON run description read by the library (include/cil_input.h):
+    .config (cil_config fields), .params (cil_colony_params fields, the dict Engine takes),
+    .run (GTS, FRAMES, output names ...), .initial_state() (INIT, reference layout)."""
+
+    def __init__(self, source: str, is_path: bool = True):
+        self.L = lib()
+        h = C.c_void_p()
+        data = os.fsencode(source) if is_path else source.encode()
+        st = self.L.cil_input_load(data, 1 if is_path else 0, C.byref(h))
+        self.h = h
+        if st != 0:
+            buf = C.create_string_buffer(1024)
+            self.L.cil_input_last_error(h, buf, 1024)
+            self.close()
+            raise CilError(st, buf.value.decode())
+        cfg, prm, run = Config(), ColonyParams(), RunInfo()
+        self._check(self.L.cil_input_config(h, C.byref(cfg), C.byref(prm), C.byref(run)))
+        self.config = _struct_dict(cfg)
+        self.params = _struct_dict(prm)
+        self.run = _struct_dict(run)
+
+    def _check(self, st: int):
+        if st != 0:
+            buf = C.create_string_buffer(1024)
+            self.L.cil_input_last_error(self.h, buf, 1024)
+            raise CilError(st, buf.value.decode())
+
+    def initial_state(self) -> dict:
+        n, D = self.run["ncells"], self.config["dim"]
+        pos = np.zeros((n, 2, D))
+        sig = np.zeros((n, 2))
+        t0 = np.zeros(n, np.int32)
+        tsw = np.zeros(n, np.int32)
+        v = ColonyView(ncells=0, capacity=n, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig), vel=None, t0=_ip(t0),
+                       tswitch=_ip(tsw))
+        self._check(self.L.cil_input_initial_state(self.h, C.byref(v)))
+        return dict(pos=pos, sigma=sig, t0=t0, tswitch=tsw)
+
+    def engine(self, device: int = 0, **over) -> Engine:
+        """An Engine configured from the run description (keyword arguments override)."""
+        c = self.config
+        kw = dict(precision=c["precision"], rng=c["rng_mode"], seed=c["seed"], device=device, skin=c["skin"])
+        kw.update(over)
+        return Engine([self.params], [self.run["capacity"]], **kw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cil_input_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -15,8 +15,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcilgpu.so")
+RUNNER = os.path.join(OUT, "cil_gpu_run")
 SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu",
-           "cil_frame.cu"]
+           "cil_frame.cu", "cil_input.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -28,7 +29,10 @@ def nvcc() -> str:
 
 
 def flags(extra=()):
+    # host code: no FMA contraction, so that the oracle-mode host draws and the INIT draws give
+    # the same bits on x86-64 and aarch64 hosts
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                   "-Xcompiler", "-ffp-contract=off",
                    "-I", os.path.join(ROOT, "include"), "-I", CSRC, *extra]
 
 
@@ -38,11 +42,11 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     procs = []
     objs = []
     for src in SOURCES:
-        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         src_path = os.path.join(CSRC, src)
         deps = [src_path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
-        deps += [os.path.join(ROOT, "include", h) for h in ("cil_gpu.h", "cil_gsd.h")]
+        deps += [os.path.join(ROOT, "include", h) for h in os.listdir(os.path.join(ROOT, "include"))]
         if (not ptxas_info and os.path.exists(obj)
                 and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
             continue
@@ -62,6 +66,13 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     if r.returncode != 0:
         sys.stdout.write(r.stdout)
         raise RuntimeError("link failed")
+    # the reference-shaped runner: JSON run description -> GPU step -> GSD frames
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), os.path.join(HERE, "host", "run_json.cpp"),
+           "-L", OUT, "-lcilgpu", "-Wl,-rpath,$ORIGIN", "-o", RUNNER]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stdout.write(r.stdout)
+        raise RuntimeError("cil_gpu_run build failed")
     return LIB
 
 

@@ -1,0 +1,90 @@
+/*
+ * cil_input.h - the reference's JSON run description (Input.cpp, CIL.cuh:332-393) read into
+ * the step library's configuration, and its initial configuration (INIT, Input.cpp:591-761;
+ * initializeCellStatus, CIL.cuh:253-330) built on the host for cil_upload.
+ *
+ * What is read, and what it becomes:
+ *   UNITS       LENGTH, MOTILITY, FRICTION must be 1: the derived units need the reference's
+ *               Units class, which is not part of its tree.
+ *   MD          DIM, BOX, PBC, GTS, FRAMES; DT (MANUAL); INTEGRATOR EULER (no noise) or
+ *               STOCHASTIC_EULER (passive noise). AUTOSCALE, STOCHASTIC_HEUN and DPD are
+ *               refused with a message.
+ *   RUNTIME     RNG.SEED (<= 0: the current time, as Random::init(time(NULL))).
+ *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 needs libhdf5, which this
+ *               build does not have, and is reported back as not served).
+ *   SPECIES     one species of two-element cells: NELEM, NAMES, MOTILITY, FRICTION,
+ *               NOISE.PASSIVE, the element diameters of the selected pair force, FENE RMAX /
+ *               KAPPA_PULL (for the steady-state length rss that INIT RANDOM uses),
+ *               DIVISION (ENABLED, CONST_FORCE, TAU_DIVISION, TAU_MIGRATION), APOPTOSIS
+ *               (ENABLED, APOP_RATE).
+ *   INTERACTIONS PAIRFORCES.SELECT "LJ" with ATTRACTION OFF is the reference's own law
+ *               (WCA, cil_gpu.h CIL_FORCE_LJ_WCA, epsilon from the species' LJ EPSILON).
+ *   GPU         (optional block, this library's own): PRECISION "FP64" | "MIXED", RNG
+ *               "PHILOX" | "DSFMT", SKIN, SCHEDULER, CAPACITY, NOISE_PER_CELL, and the model
+ *               parameters the reference's JSON has no key for: FORCE_LAW ("LJ_WCA",
+ *               "SOFTCORE", "HERTZ") with EPSILON and RCUT_SCALE (required for SC/HZ runs,
+ *               whose reference laws differ from this library's), SPRING {KAPPA, REST0, REST1}
+ *               (the linear intra-cell spring; required: the reference's FENE law differs),
+ *               WALLS {E, POS[], DIR[]}.
+ *   INIT        per species: RANDOM (NUMBER) with the reference's draw sequence, so that the
+ *               positions equal the reference's bit for bit for the same seed; JSON (element
+ *               positions). H5 restart needs libhdf5 and is refused.
+ *
+ * Errors carry the JSON key that failed, as json_parser's std::domain_error messages do
+ * (JsonParser.hpp:13-135).
+ */
+#ifndef CIL_INPUT_H
+#define CIL_INPUT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cil_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cil_input cil_input;
+
+/* Run-level settings that are not part of cil_config / cil_colony_params. */
+typedef struct cil_run_info {
+  int32_t gts;                 /* MD.GTS: steps per frame */
+  int32_t frames;              /* MD.FRAMES */
+  int32_t output_gsd;          /* OUTPUT.FORMAT lists "GSD" */
+  int32_t output_h5;           /* OUTPUT.FORMAT lists "H5" (not served by this library) */
+  int32_t ncells;              /* cells of the initial configuration */
+  int32_t capacity;            /* GPU.CAPACITY, else 4 x ncells + 64 */
+  int32_t use_scheduler;       /* GPU.SCHEDULER */
+  int32_t seed;                /* RUNTIME.RNG.SEED as used (time-based when <= 0 in the file) */
+  char output_dir[256];        /* OUTPUT.DIR */
+  char output_name[256];       /* OUTPUT.NAME */
+  char cell_name[64];          /* SPECIES.DEFINE[0] */
+  char elem_names[2][64];      /* SPECIES.<cell>.NAMES */
+} cil_run_info;
+
+/* Parses a JSON document (is_path != 0: `text` is a file name) and reads the run
+ * description. On failure *out is still set (unless it is NULL) so that the message can be
+ * read with cil_input_last_error; free it with cil_input_free. */
+cil_status cil_input_load(const char *text, int32_t is_path, cil_input **out);
+
+/* The configuration for cil_create (num_colonies = 1) and the colony's parameters. */
+cil_status cil_input_config(const cil_input *in, cil_config *cfg, cil_colony_params *params, cil_run_info *run);
+
+/* Builds the initial configuration on the host in the reference layout: pos [cell][2][dim],
+ * sigma [cell][2] (the species' element diameters), t0 = 0 and tswitch from the reference's
+ * cell-status draws (initializeCellStatus), ts = 0. The view's arrays must hold
+ * run.ncells cells (view->capacity); view->ncells receives the count. INIT RANDOM consumes
+ * the reference's Random stream in the reference's order: positions, cell status, then
+ * positions again (initialize() reads INIT twice, CIL.cuh:374-378, and the second read wins). */
+cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *view);
+
+/* Message of the last failure (empty if none). */
+void cil_input_last_error(const cil_input *in, char *buf, size_t len);
+
+void cil_input_free(cil_input *in);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CIL_INPUT_H */

@@ -1,0 +1,70 @@
+"""A run started from the reference's JSON run description (include/cil_input.h): the Engine
+built from it steps like the oracle with the same parameters and INIT (oracle mode: the
+reference's host draws, FP64), and the reference-shaped runner cil_gpu_run (JSON -> GPU step
+-> GSD frames) writes the frames and the final-state file of that same run."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from cil_cuda_gb300.gsd import GSDFile
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+FIXTURE = os.path.join(ROOT, "tests", "golden", "input_two_element_2d.json")
+
+
+def test_run_from_json_matches_oracle(gpu_lib, oracle_lib):
+    G = gpu_lib
+    r = G.RunInput(FIXTURE)
+    st = r.initial_state()
+    eng = r.engine()
+    eng.upload(0, **st)
+    steps = r.run["gts"] * r.run["frames"]
+    eng.step(steps)
+    g = eng.download(0)
+    eng.close()
+    o = oracle_lib.Oracle(r.params, r.run["capacity"], r.config["seed"])
+    o.set_state(**st)
+    assert o.step(steps) == 0
+    s = o.state()
+    assert g["ncells"] == len(s["sigma"]) and g["ncells"] != r.run["ncells"]
+    np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    d = g["pos"] - s["pos"]
+    d -= np.round(d / 60.0) * 60.0
+    assert np.abs(d).max() <= 1e-9
+
+
+def test_runner_writes_the_run(gpu_lib, tmp_path):
+    G = gpu_lib
+    from cil_cuda_gb300 import build
+    assert os.path.exists(build.RUNNER)
+    doc = json.load(open(FIXTURE))
+    doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
+    cfg = tmp_path / "run.json"
+    cfg.write_text(json.dumps(doc))
+    res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    lines = [ln for ln in res.stderr.splitlines() if ln.startswith("# ts =")]
+    assert len(lines) == doc["MD"]["FRAMES"]
+    f = GSDFile(str(tmp_path / "out" / "colony.gsd"))
+    assert f.nframes == doc["MD"]["FRAMES"] + 1
+    gts = doc["MD"]["GTS"]
+    assert [int(f.read(k, "configuration/step")[0]) for k in range(f.nframes)] == [k * gts for k in range(f.nframes)]
+    assert f.types(0) == ["A_BACK", "A_FRONT"]
+    # the same run through the Python binding gives the same final frame
+    r = G.RunInput(str(cfg))
+    eng = r.engine()
+    eng.upload(0, **r.initial_state())
+    eng.step(gts * doc["MD"]["FRAMES"])
+    g = eng.download(0)
+    eng.close()
+    E = 2 * g["ncells"]
+    assert int(f.read(f.nframes - 1, "particles/N")[0]) == E
+    exp = (g["pos"].reshape(E, 2) - 30.0).astype(np.float32)
+    np.testing.assert_array_equal(f.read(f.nframes - 1, "particles/position")[:, :2], exp)
+    last = GSDFile(str(tmp_path / "out" / "Last" / "colony.Last.gsd"))
+    assert last.nframes == 1 and int(last.read(0, "configuration/step")[0]) == 0
+    np.testing.assert_array_equal(last.read(0, "particles/position"), f.read(f.nframes - 1, "particles/position"))

@@ -1,0 +1,175 @@
+"""The reference's JSON run description read by the library (include/cil_input.h): settings
+mapped into cil_config / cil_colony_params, INIT RANDOM equal bit for bit to the reference's
+own draws (golden file written from the reference's Random:: by
+tests/golden/make_input_golden.py, and live where the reference's RNG is built), INIT JSON,
+and the refusals, with the key that caused them, for what the GPU step does not model. No GPU."""
+import copy
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, GOLDEN)
+
+import reference_init as R  # noqa: E402
+
+FIXTURE = os.path.join(GOLDEN, "input_two_element_2d.json")
+REF_DIR = os.environ.get("CIL_REFERENCE_DIR", "/root/reference")
+
+
+@pytest.fixture(scope="module")
+def G():
+    import cil_cuda_gb300 as G
+    if not os.path.exists(G.LIB_PATH):
+        from cil_cuda_gb300 import build
+        build.build()
+    G.lib()
+    return G
+
+
+def doc():
+    return json.load(open(FIXTURE))
+
+
+def load(G, d):
+    return G.RunInput(json.dumps(d), is_path=False)
+
+
+def test_settings_are_mapped(G):
+    r = G.RunInput(FIXTURE)
+    c, p, run = r.config, r.params, r.run
+    assert (c["dim"], c["precision"], c["rng_mode"], c["seed"], c["num_colonies"]) == (2, G.PREC_FP64, G.RNG_DSFMT,
+                                                                                        4357, 1)
+    assert c["force_law"] == p["force_law"] == G.FORCE_SOFTCORE
+    assert p["box"][:2] == [60.0, 60.0] and p["periodic"][:2] == [1, 1]
+    assert p["motility"] == [0.0, 1.0] and p["zeta"] == [1.0, 1.0]
+    assert (p["epsilon"], p["rcut_scale"], p["kappa"], p["rest0"], p["rest1"]) == (5.0, 1.0, 1.0, 0.5, 1.0)
+    assert (p["noise_D"], p["dt"], p["divide"], p["div_tau_mu"], p["div_tau_sigma"], p["apop_rate"]) == \
+        (0.001, 0.001, 1, 0.05, 0.005, 0.5)
+    assert (run["gts"], run["frames"], run["output_gsd"], run["output_h5"], run["ncells"], run["capacity"]) == \
+        (25, 4, 1, 0, 300, 4000)
+    assert (run["output_dir"], run["output_name"], run["cell_name"], run["elem_names"]) == \
+        ("output", "colony", "A", ["BACK", "FRONT"])
+
+
+def test_random_init_matches_reference_golden(G):
+    st = G.RunInput(FIXTURE).initial_state()
+    gold = json.load(open(os.path.join(GOLDEN, "input_random_init_golden.json")))
+    pos = np.array([float.fromhex(x) for x in gold["pos"]]).reshape(st["pos"].shape)
+    np.testing.assert_array_equal(st["pos"], pos)
+    np.testing.assert_array_equal(st["tswitch"], np.array(gold["tswitch"], np.int32))
+    assert np.all(st["t0"] == 0)
+    np.testing.assert_array_equal(st["sigma"], np.tile([1.0, 0.9], (300, 1)))
+
+
+@pytest.mark.parametrize("variant", ["euler_no_division", "const_force", "open_y"])
+def test_random_init_matches_reference_live(G, variant):
+    if not os.path.exists(R.LIB):
+        pytest.skip("reference RNG not built (reference tree absent)")
+    d = doc()
+    loc = d["SPECIES"]["A"]
+    if variant == "euler_no_division":
+        d["MD"]["INTEGRATOR"]["SELECT"] = "EULER"
+        loc["DIVISION"]["ENABLED"] = False
+        d["RUNTIME"]["RNG"]["SEED"] = 99
+    elif variant == "const_force":
+        loc["DIVISION"]["CONST_FORCE"] = True
+        d["INIT"]["A"]["RANDOM"]["NUMBER"] = 57
+    else:  # 2D with an open axis: no wrap along y
+        d["MD"]["PBC"] = [True, False]
+        d["RUNTIME"]["RNG"]["SEED"] = 7
+    r = load(G, d)
+    st = r.initial_state()
+    args = R.from_fixture(d)
+    pos, tsw = R.reference_init(**args)
+    np.testing.assert_array_equal(st["pos"], pos)
+    if loc["DIVISION"]["ENABLED"]:
+        np.testing.assert_array_equal(st["tswitch"], tsw)
+    else:
+        assert np.all(st["tswitch"] == -1)
+
+
+def test_json_init(G):
+    d = doc()
+    rows = [[1.0 + k, 2.0 + 0.5 * k] for k in range(8)]
+    d["INIT"]["A"] = {"SELECT": "JSON", "JSON": rows}
+    st = load(G, d).initial_state()
+    np.testing.assert_array_equal(st["pos"].reshape(-1, 2), np.array(rows))
+    assert len(st["sigma"]) == 4
+
+
+def test_random_init_3d_out_of_bounds_is_refused(G):
+    """In 3D the reference draws sin(phi) as uniform() * pi (Input.cpp:747), so most cells get
+    sqrt(1 - sin^2) of a negative number: the reference stops with "Input Positions Out of
+    Bounds!" when z is periodic; the library refuses the start in every case."""
+    d = doc()
+    d["MD"].update(DIM=3, BOX=[20, 20, 20], PBC=[True, True, True])
+    r = load(G, d)
+    with pytest.raises(G.CilError) as e:
+        r.initial_state()
+    assert "Out of Bounds" in str(e.value)
+
+
+@pytest.mark.parametrize("edit,needle", [
+    (lambda d: d["UNITS"].update(LENGTH=2), "UNITS.LENGTH"),
+    (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="DPD"), "MD.INTEGRATOR.SELECT"),
+    (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="VERLET"), "not one of"),
+    (lambda d: d["MD"]["DT"].update(SELECT="AUTOSCALE"), "MD.DT.SELECT"),
+    (lambda d: d["MD"].update(BOX=[60]), "vector should be of size 2. Got 1"),
+    (lambda d: d["SPECIES"].update(DEFINE=["A", "B"]), "SPECIES.DEFINE"),
+    (lambda d: d["SPECIES"]["A"].update(NELEM=1), "SPECIES.A.NELEM"),
+    (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
+    (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
+    (lambda d: d["GPU"].pop("FORCE_LAW"), "GPU.FORCE_LAW"),
+    (lambda d: d["INIT"]["A"].update(SELECT="H5"), "libhdf5"),
+    (lambda d: d["SPECIES"]["A"]["APOPTOSIS"].update(APOP_RATE=5000.0), "Apoptosis rate per time step >= 1"),
+])
+def test_refusals_name_the_key(G, edit, needle):
+    d = copy.deepcopy(doc())
+    edit(d)
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert needle in str(e.value)
+
+
+def test_lj_is_the_reference_law(G):
+    d = doc()
+    d["INTERACTIONS"]["PAIRFORCES"] = {"SELECT": "LJ", "LJ": {"ATTRACTION": {"SELECT": "OFF"}}}
+    del d["GPU"]["FORCE_LAW"]
+    r = load(G, d)
+    assert r.params["force_law"] == G.FORCE_LJ_WCA and r.params["epsilon"] == 1.0
+    assert abs(r.params["rcut_scale"] - 2 ** (1 / 6)) < 1e-15
+    d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["SELECT"] = "ON"
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "ATTRACTION" in str(e.value)
+
+
+def test_parse_errors(G):
+    for text, needle in (("{\"A\": 1,}", "expected a string key"), ("[1, 2", "expected ',' or ']'"),
+                         ("{\"A\": tru}", "unexpected character"), ("{} x", "trailing characters"),
+                         ("{\"A\": \"\\q\"}", "bad escape")):
+        with pytest.raises(G.CilError) as e:
+            G.RunInput(text, is_path=False)
+        assert needle in str(e.value), (text, str(e.value))
+    with pytest.raises(G.CilError) as e:
+        G.RunInput(os.path.join(GOLDEN, "no_such_file.json"))
+    assert e.value.status == 8
+
+
+@pytest.mark.parametrize("name,needle", [
+    ("input/cil.json", "JSON parse error at line"),  # holds an unresolved merge conflict
+    ("input/test.2d.json", "SPECIES.C.NELEM"),  # single-element cells
+    ("PRX_MDCK_2D.json", "NELEM"),  # single-element cells
+])
+def test_reference_configs_are_read_or_refused_with_reason(G, name, needle):
+    p = os.path.join(REF_DIR, name)
+    if not os.path.exists(p):
+        pytest.skip("reference configs absent")
+    with pytest.raises(G.CilError) as e:
+        G.RunInput(p)
+    assert needle in str(e.value), str(e.value)
