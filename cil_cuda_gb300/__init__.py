@@ -19,6 +19,7 @@ FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 RNG_PHILOX, RNG_DSFMT = 0, 1
 FLAG_NO_GRAPH = 1
+INTEGRATOR_EULER, INTEGRATOR_HEUN = 0, 1
 
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
           5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE", 8: "CIL_ERR_IO"}
@@ -82,6 +83,7 @@ class Config(C.Structure):
         ("flags", C.c_int32),
         ("staging", C.c_int32),
         ("occupancy", C.c_int32),
+        ("integrator", C.c_int32),
     ]
 
 
@@ -301,7 +303,7 @@ class Engine:
 
     def __init__(self, params: list, caps: list, *, precision: int = PREC_FP64, rng: int = RNG_PHILOX,
                  seed: int = 0, device: int = 0, bin_width: float = 0.0, skin: float = 0.0,
-                 graphs: bool = True, staging: int = 0, occupancy: int = 0):
+                 graphs: bool = True, staging: int = 0, occupancy: int = 0, integrator: int = INTEGRATOR_EULER):
         self.L = lib()
         self.B = len(params)
         self.dim = params[0]["dim"]
@@ -309,7 +311,7 @@ class Engine:
         cfg = Config(dim=self.dim, force_law=params[0]["force_law"], precision=precision, rng_mode=rng,
                      seed=seed, num_colonies=self.B, device=device, bin_width=bin_width, skin=skin,
                      block_size=0, flags=0 if graphs else FLAG_NO_GRAPH, staging=staging,
-                     occupancy=occupancy)
+                     occupancy=occupancy, integrator=integrator)
         arr = (ColonyParams * self.B)(*[make_params(**p) for p in params])
         caps_a = np.array(self.caps, np.int32)
         h = C.c_void_p()
@@ -658,7 +660,8 @@ class RunInput:
     def engine(self, device: int = 0, **over) -> Engine:
         """An Engine configured from the run description (keyword arguments override)."""
         c = self.config
-        kw = dict(precision=c["precision"], rng=c["rng_mode"], seed=c["seed"], device=device, skin=c["skin"])
+        kw = dict(precision=c["precision"], rng=c["rng_mode"], seed=c["seed"], device=device, skin=c["skin"],
+                  integrator=c["integrator"])
         kw.update(over)
         return Engine([self.params], [self.run["capacity"]], **kw)
 

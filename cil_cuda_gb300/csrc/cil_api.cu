@@ -608,7 +608,41 @@ cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = null
 
 // One step's launches on the handle's stream (oracle mode: with its host draws). When timed,
 // four events bracket the phases; a step being captured into a graph records none.
+cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cudaEvent_t before_force);
+
+// One Euler step, or the two half steps of a Heun step (each: noise draw, bins or lists,
+// force pass with its position update), then the step counter and the events. Timed phases:
+// rebuild = the first pass's bins / lists; force = the rest up to the last force pass.
 cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
+  const bool heun = h->cfg.integrator == CIL_INTEGRATOR_HEUN;
+  const int passes = heun ? 2 : 1;
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
+  for (int pass = 0; pass < passes; ++pass) {
+    const cil_status st = enqueue_force_pass(h, last, heun ? pass + 1 : 0, pass == 0,
+                                             timed && pass == 0 ? pool_event(h, e0 + 1) : nullptr);
+    if (st != CIL_OK) return st;
+  }
+  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream);
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
+  h->ts += 1;
+  if (h->cfg.rng_mode == CIL_RNG_DSFMT) {
+    const cil_status st = oracle_events(h);
+    if (st != CIL_OK) return st;
+    h->launches += 2;
+  } else {
+    launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
+    launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
+    h->launches += 8;
+  }
+  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
+  CUDA_TRY(h, cudaGetLastError());
+  return CIL_OK;
+}
+
+// Noise draw (oracle mode), bins or Verlet lists, and one force pass with its position
+// update. heun: 0 for an Euler step, 1 / 2 for the half steps of a Heun step. first: the
+// first pass of the step (the slot re-sort of skin mode happens there only).
+cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cudaEvent_t before_force) {
   const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
   cil_status st = CIL_OK;
   bool noise = false;
@@ -618,11 +652,11 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
   } else {
     for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;
   }
-  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
   if (h->skin_mode) {
     // list rebuilds are decided on the device (guard, cadence, fresh overflow); the host
     // re-sorts the slots on a fixed schedule and after uploads
-    const bool permute = h->need_exact || h->lists_stale || (h->ts % h->permute_period) == 0;
+    const bool permute =
+        h->need_exact || h->lists_stale || (first && (h->ts % h->permute_period) == 0);
     launch_skin_begin(skin_args(h, permute ? 1 : 0), h->stream);
     if (permute) {
       st = do_rebuild(h);
@@ -649,28 +683,15 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     if (st != CIL_OK) return st;
     h->launches += 10;
   }
-  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 1), h->stream));
+  if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
+  fa.heun = heun;
   if (h->skin_mode)
     launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->list_variant, h->stream);
   else
     launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
-  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream);
-  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
-  h->ts += 1;
-  if (oracle) {
-    st = oracle_events(h);
-    if (st != CIL_OK) return st;
-    h->launches += 2;
-  } else {
-    launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
-    launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
-    h->launches += 8;
-  }
-  if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
-  CUDA_TRY(h, cudaGetLastError());
   return CIL_OK;
 }
 
@@ -696,17 +717,20 @@ HostStepState host_state(const cil_handle *h) {
 // What one steady step does to the host-side state (mirrors enqueue_step)
 void advance_host_state(const cil_handle *h, HostStepState *s) {
   const bool mixed = h->cfg.precision == CIL_PREC_MIXED;
-  if (h->skin_mode) {
-    s->lists_stale = false;
-  } else {  // do_rebuild
-    s->cur ^= 1;
-    s->meta ^= 1;
+  const int passes = h->cfg.integrator == CIL_INTEGRATOR_HEUN ? 2 : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    if (h->skin_mode) {
+      s->lists_stale = false;
+    } else {  // do_rebuild
+      s->cur ^= 1;
+      s->meta ^= 1;
+      if (mixed) s->pu ^= 1;
+      s->need_exact = false;
+      s->lists_stale = true;
+    }
+    s->cur ^= 1;  // force pass
     if (mixed) s->pu ^= 1;
-    s->need_exact = false;
-    s->lists_stale = true;
   }
-  s->cur ^= 1;  // force pass
-  if (mixed) s->pu ^= 1;
   s->ts += 1;
 }
 
@@ -814,6 +838,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->skin < 0.0 || (cfg->skin > 0.0 && cfg->precision != CIL_PREC_MIXED)) return CIL_ERR_CONFIG;
   if (cfg->skin > 0.0 && cfg->num_colonies > kMaxSkinColonies) return CIL_ERR_CONFIG;
   if (cfg->block_size != 0 && cfg->block_size != kTile) return CIL_ERR_CONFIG;
+  if (cfg->integrator != CIL_INTEGRATOR_EULER && cfg->integrator != CIL_INTEGRATOR_HEUN) return CIL_ERR_CONFIG;
   int list_variant = -1;
   {
     const int st = cfg->staging == 0 ? 4 : cfg->staging, oc = cfg->occupancy == 0 ? 4 : cfg->occupancy;

@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
     } else if (a.noise_mode == 1) {
       const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
       uint32_t w[4];
-      noise_words<D>(id, a.ts, a.seed_lo, a.seed_hi, w);
+      noise_words<D>(id, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
       float n[4];
       box_muller(w[0], w[1], n[0], n[1]);
       if (D == 3) box_muller(w[2], w[3], n[2], n[3]);
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       for (int d = 0; d < D; ++d) a.frc[d * SS + s] = F[d];
     }
     if (a.integrate) {
-      const double temp = C.temp[j];
+      const double temp = a.heun ? 0.5 * C.temp[j] : C.temp[j];  // (dt/2) / zeta is exact
       bool inside = true;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
@@ -220,7 +220,10 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
       if (a.vel) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) a.vel[d * SS + s] = F[d] * C.mu_eff[j];
+        for (int d = 0; d < D; ++d) {
+          const double v = F[d] * C.mu_eff[j];
+          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * SS + s] + v) : v;
+        }
       }
     }
   }
@@ -288,7 +291,7 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
     // Box-Muller with the fast log / sincos
     const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
     uint32_t w[4];
-    noise_words<D>(id, a.ts, a.seed_lo, a.seed_hi, w);
+    noise_words<D>(id, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
     const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
     for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -323,7 +326,7 @@ __device__ __forceinline__ void mixed_integrate(const ForceArgs &a, const Colony
     for (int d = 0; d < D; ++d) a.frc[d * a.SS + s] = static_cast<double>(F[d]);
   }
   if (!a.integrate) return;
-  const float temp = C.temp_f[j];
+  const float temp = a.heun ? 0.5f * C.temp_f[j] : C.temp_f[j];
   bool inside = true;
   float4 pn = make_float4(0.0f, 0.0f, 0.0f, w);
 #pragma unroll
@@ -351,7 +354,10 @@ __device__ __forceinline__ void mixed_integrate(const ForceArgs &a, const Colony
   if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
   if (a.vel) {
 #pragma unroll
-    for (int d = 0; d < D; ++d) a.vel[d * a.SS + s] = static_cast<double>(F[d] * C.mu_f[j]);
+    for (int d = 0; d < D; ++d) {
+      const double v = static_cast<double>(F[d] * C.mu_f[j]);
+      a.vel[d * a.SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * a.SS + s] + v) : v;
+    }
   }
 }
 
@@ -704,7 +710,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
     if (a.noise_mode == 1) {
       const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
       uint32_t w[4];
-      noise_words<D>(id, ts, a.seed_lo, a.seed_hi, w);
+      noise_words<D>(id, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w);
       const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
       for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -776,7 +782,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
       for (int d = 0; d < D; ++d) a.facc[d * SS + s] = 0.0f;
     }
     if (a.integrate) {
-      const float temp = C.temp_f[j];
+      const float temp = a.heun ? 0.5f * C.temp_f[j] : C.temp_f[j];
       bool inside = true;
       // 2D: z carries the packed list reference to the next record
       float4 pn = make_float4(0.0f, 0.0f, D == 2 ? pi.z : 0.0f, pi.w);
@@ -813,7 +819,10 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
       }
       if (a.vel) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) a.vel[d * SS + s] = static_cast<double>(F[d] * C.mu_f[j]);
+        for (int d = 0; d < D; ++d) {
+          const double v = static_cast<double>(F[d] * C.mu_f[j]);
+          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * SS + s] + v) : v;
+        }
       }
     }
   } else if (used && a.integrate) {

@@ -410,8 +410,8 @@ void read_all(cil_input *in) {
       if (!(L[d] > 0.0)) key_error("MD.BOX", "box lengths must be positive");
     }
     integrator = md.child("INTEGRATOR").pick("SELECT", {"EULER", "STOCHASTIC_EULER", "STOCHASTIC_HEUN", "DPD"});
-    if (integrator == "STOCHASTIC_HEUN" || integrator == "DPD")
-      key_error("MD.INTEGRATOR.SELECT", integrator + " is not implemented by the GPU step (EULER, STOCHASTIC_EULER)");
+    if (integrator == "DPD")
+      key_error("MD.INTEGRATOR.SELECT", "DPD is not implemented by the GPU step (EULER, STOCHASTIC_EULER, STOCHASTIC_HEUN)");
     Node dtn = md.child("DT");  // initializeTimeStep (CIL.cuh:167-250)
     if (dtn.pick("SELECT", {"AUTOSCALE", "MANUAL"}) == "AUTOSCALE")
       key_error("MD.DT.SELECT", "AUTOSCALE needs the reference's force-law time scales; use MANUAL");
@@ -470,7 +470,13 @@ void read_all(cil_input *in) {
     key_error("INTERACTIONS.PAIRFORCES.SELECT", "GHOSTS is not modelled by the GPU step");
   }
   double noise_D = 0.0;
-  if (integrator == "STOCHASTIC_EULER") noise_D = loc.child("NOISE").num("PASSIVE");
+  if (integrator != "EULER") {  // NOISE_ON (Input.cpp:527-535, 99-111)
+    Node nz = loc.child("NOISE");
+    noise_D = nz.num("PASSIVE");
+    if (integrator == "STOCHASTIC_HEUN")  // NOISE_ACTIVE: radial and angular noise of the cell axis
+      for (const char *k : {"RADIAL", "ANGULAR"})
+        if (nz.num(k) != 0.0) key_error(nz.path + "." + k, "active cell noise is not modelled by the GPU step");
+  }
   {  // steady-state length (Input.cpp:139-144) for INIT RANDOM
     Node fene = loc.child("FENE");
     const double kappa = fene.nums("KAPPA_PULL", 1)[0];
@@ -504,6 +510,7 @@ void read_all(cil_input *in) {
     return has_gpu && gpu.has(k) ? gpu.pick(k, ok) : std::string(dflt);
   };
   cfg.dim = in->dim;
+  cfg.integrator = integrator == "STOCHASTIC_HEUN" ? CIL_INTEGRATOR_HEUN : CIL_INTEGRATOR_EULER;
   cfg.precision = gpick("PRECISION", {"FP64", "MIXED"}, "MIXED") == "FP64" ? CIL_PREC_FP64 : CIL_PREC_MIXED;
   cfg.rng_mode = gpick("RNG", {"PHILOX", "DSFMT"}, "PHILOX") == "DSFMT" ? CIL_RNG_DSFMT : CIL_RNG_PHILOX;
   cfg.seed = static_cast<uint64_t>(static_cast<uint32_t>(run.seed));

@@ -480,7 +480,13 @@ struct ForceArgs {
   uint32_t seed_lo, seed_hi;
   int noise_mode;          // 0 none, 1 philox, 2 uploaded
   int integrate;
+  int heun;                // 0 Euler step; 1, 2: first, second half step of a Heun step
 };
+
+// Half-step helpers of the Heun integrator (CIL_INTEGRATOR_HEUN): the Philox noise index of
+// a force pass (the two passes of step ts take 2 ts and 2 ts + 1, one Philox block per step
+// in 2D), and the step fraction of its position update.
+__device__ __forceinline__ int noise_index(int ts, int heun) { return heun ? 2 * ts + (heun - 1) : ts; }
 
 struct EventArgs {
   const ColonyConst *col;

@@ -101,7 +101,17 @@ typedef struct cil_config {
    * (8, 3), (8, 2); 3D always runs (4, 4). cil_cuda_gb300/autotune.py picks them. */
   int32_t staging;
   int32_t occupancy;
+  int32_t integrator;     /* CIL_INTEGRATOR_*: 0 = Euler */
 } cil_config;
+
+/* cil_config.integrator. EULER is the reference's Euler (CIL.cu:1013-1020). HEUN is its
+ * StochasticHeun (CIL.cu:1028-1050): per step, two half steps dt/2, each with a force
+ * evaluation and its own noise draw (forces -> x += (dt/2) F / zeta, twice), then the step
+ * counter, division and apoptosis. The reference's predictor copy (pos0) is never read and
+ * its Heun never updates the velocities; here the velocity of a Heun step is the mean of the
+ * two half steps' F / zeta, i.e. the step's displacement over dt. */
+#define CIL_INTEGRATOR_EULER 0
+#define CIL_INTEGRATOR_HEUN 1
 
 /* cil_config.flags: run every step as individual launches (no CUDA graphs). By default, in
  * Philox mode, pairs of steps whose launches depend on nothing the host decides (no slot

@@ -6,9 +6,10 @@
  * What is read, and what it becomes:
  *   UNITS       LENGTH, MOTILITY, FRICTION must be 1: the derived units need the reference's
  *               Units class, which is not part of its tree.
- *   MD          DIM, BOX, PBC, GTS, FRAMES; DT (MANUAL); INTEGRATOR EULER (no noise) or
- *               STOCHASTIC_EULER (passive noise). AUTOSCALE, STOCHASTIC_HEUN and DPD are
- *               refused with a message.
+ *   MD          DIM, BOX, PBC, GTS, FRAMES; DT (MANUAL); INTEGRATOR EULER (no noise),
+ *               STOCHASTIC_EULER (passive noise) or STOCHASTIC_HEUN (CIL_INTEGRATOR_HEUN;
+ *               its active RADIAL/ANGULAR noise must be 0). AUTOSCALE and DPD are refused
+ *               with a message.
  *   RUNTIME     RNG.SEED (<= 0: the current time, as Random::init(time(NULL))).
  *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 needs libhdf5, which this
  *               build does not have, and is reported back as not served).

@@ -7,6 +7,10 @@
 //   forces (noise draw CIL.cu:793-818, intra CIL.cu:30-100, inter CIL.cu:177-231)
 //   -> integrate (CIL.cu:858-875 / Utils.hpp:561-566) -> ++ts -> division (CIL.cu:369-455)
 //   -> apoptosis (CIL.cu:627-649).
+// With ora_set_integrator(h, 1) a step is the reference's StochasticHeun (CIL.cu:1028-1050):
+// two half steps, each a force evaluation with its own noise draw and x += (dt/2) F / zeta,
+// then ++ts, division, apoptosis. The reference leaves the velocities of a Heun step stale;
+// here they are the mean of the two half steps' F / zeta (the library's definition).
 // Build: oracle/build.sh (gcc -O2 -ffp-contract=off -fno-fast-math, optional OpenMP).
 #include "cil_oracle.h"
 
@@ -163,6 +167,7 @@ struct Oracle {
   int D = 2;
   int cap = 0, n = 0, ts = 0;
   int nthreads = 0;
+  int integrator = 0;  // 0 Euler, 1 Heun
   std::vector<double> pos, vel, frc, sig, wiener;
   std::vector<int> t0, tsw;
   Rng rng;
@@ -419,13 +424,18 @@ struct Oracle {
 
   // updatePositions (CIL.cu:858-875) with mobility 1/zeta; velocity v = F * (temp/dt) as
   // updateVelocityPositions does (CIL.cu:923-935).
-  void integrate() {
+  // heun: 0 a full Euler step; 1, 2 the first and second half step of a Heun step
+  // (temp = (dt/2) / zeta, CIL.cu:1037-1042; velocity: F/zeta, then the mean of both halves).
+  void integrate(int heun = 0) {
     for (int c = 0; c < n; ++c)
       for (int j = 0; j < 2; ++j) {
         const double temp = p.dt * (1.0 / p.zeta[j]);
-        update_pos(P(c, j), F(c, j), temp);
+        update_pos(P(c, j), F(c, j), heun ? 0.5 * temp : temp);
         const double mu = temp / p.dt;
-        for (int d = 0; d < D; ++d) V(c, j)[d] = F(c, j)[d] * mu;
+        for (int d = 0; d < D; ++d) {
+          const double v = F(c, j)[d] * mu;
+          V(c, j)[d] = heun == 2 ? 0.5 * (V(c, j)[d] + v) : v;
+        }
       }
   }
 
@@ -512,8 +522,15 @@ struct Oracle {
   }
 
   int step() {
-    compute_forces();
-    integrate();
+    if (integrator == 1) {
+      compute_forces();
+      integrate(1);
+      compute_forces();
+      integrate(2);
+    } else {
+      compute_forces();
+      integrate();
+    }
     ++ts;
     const int err = divisions();
     apoptosis();
@@ -562,6 +579,8 @@ void *ora_create(const ora_params *p, int32_t cap_cells, uint32_t seed) {
 void ora_destroy(void *h) { delete H(h); }
 
 void ora_set_threads(void *h, int32_t nthreads) { H(h)->nthreads = nthreads < 0 ? 0 : nthreads; }
+
+void ora_set_integrator(void *h, int32_t integrator) { H(h)->integrator = integrator == 1 ? 1 : 0; }
 
 int32_t ora_set_state(void *h, int32_t ncells, const double *pos, const double *sigma,
                       const int32_t *t0, const int32_t *tswitch, int32_t ts) {

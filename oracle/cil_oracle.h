@@ -67,6 +67,8 @@ void *ora_create(const ora_params *p, int32_t cap_cells, uint32_t seed);
 void ora_destroy(void *h);
 /* 0 = single thread, reference half-stencil order; >0 = OpenMP race-free full stencil */
 void ora_set_threads(void *h, int32_t nthreads);
+/* 0: Euler (CIL.cu:1013-1020); 1: StochasticHeun (CIL.cu:1028-1050), two half steps. */
+void ora_set_integrator(void *h, int32_t integrator);
 int32_t ora_set_state(void *h, int32_t ncells, const double *pos, const double *sigma,
                       const int32_t *t0, const int32_t *tswitch, int32_t ts);
 int32_t ora_num_cells(const void *h);

@@ -81,6 +81,8 @@ def lib():
         L.ora_create.argtypes = [C.POINTER(OraParams), i32, u32]
         L.ora_destroy.argtypes = [vp]
         L.ora_set_threads.argtypes = [vp, i32]
+        L.ora_set_integrator.restype = None
+        L.ora_set_integrator.argtypes = [vp, i32]
         L.ora_set_state.restype = i32
         L.ora_set_state.argtypes = [vp, i32, dp, dp, ip, ip, i32]
         L.ora_num_cells.restype = i32
@@ -131,7 +133,7 @@ def make_params(**kw) -> OraParams:
 class Oracle:
     """One colony on the CPU, reference layout pos[cell][elem][dim]."""
 
-    def __init__(self, params: dict, cap_cells: int, seed: int, threads: int = 0):
+    def __init__(self, params: dict, cap_cells: int, seed: int, threads: int = 0, integrator: int = 0):
         self.L = lib()
         self.params = make_params(**params)
         self.dim = params["dim"]
@@ -139,6 +141,7 @@ class Oracle:
         if not self.h:
             raise ValueError("ora_create failed")
         self.L.ora_set_threads(self.h, threads)
+        self.L.ora_set_integrator(self.h, integrator)
 
     def close(self):
         if self.h:

@@ -117,6 +117,8 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
 @pytest.mark.parametrize("edit,needle", [
     (lambda d: d["UNITS"].update(LENGTH=2), "UNITS.LENGTH"),
     (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="DPD"), "MD.INTEGRATOR.SELECT"),
+    (lambda d: (d["MD"]["INTEGRATOR"].update(SELECT="STOCHASTIC_HEUN"),
+                d["SPECIES"]["A"]["NOISE"].update(RADIAL=0.1, ANGULAR=0.0)), "SPECIES.A.NOISE.RADIAL"),
     (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="VERLET"), "not one of"),
     (lambda d: d["MD"]["DT"].update(SELECT="AUTOSCALE"), "MD.DT.SELECT"),
     (lambda d: d["MD"].update(BOX=[60]), "vector should be of size 2. Got 1"),
@@ -173,3 +175,11 @@ def test_reference_configs_are_read_or_refused_with_reason(G, name, needle):
     with pytest.raises(G.CilError) as e:
         G.RunInput(p)
     assert needle in str(e.value), str(e.value)
+
+
+def test_heun_is_read(G):
+    d = doc()
+    d["MD"]["INTEGRATOR"]["SELECT"] = "STOCHASTIC_HEUN"
+    d["SPECIES"]["A"]["NOISE"].update(RADIAL=0.0, ANGULAR=0.0)
+    r = load(G, d)
+    assert r.config["integrator"] == G.INTEGRATOR_HEUN and r.params["noise_D"] == 0.001

@@ -195,3 +195,20 @@ def test_division_replay(oracle_lib):
     assert [tuple(e) for e in ev] == expect
     st = o.state()
     assert list(st["tswitch"]) == t
+
+
+def test_heun_is_two_half_euler_steps(oracle_lib):
+    """Without noise and events, a StochasticHeun step of dt (CIL.cu:1028-1050) is two Euler
+    steps of dt/2: bit for bit."""
+    from cil_cuda_gb300 import synthetic as S
+    p = S.growth_params(box=40.0, dt=1e-3, divide=0, apop_rate=0.0, noise_D=0.0)
+    st = S.disk_colony(200, p, seed=3)
+    a = oracle_lib.Oracle(p, 800, 5, integrator=1)
+    a.set_state(**st)
+    a.step(50)
+    q = dict(p)
+    q["dt"] = 0.5e-3
+    b = oracle_lib.Oracle(q, 800, 5)
+    b.set_state(**st)
+    b.step(100)
+    np.testing.assert_array_equal(a.state()["pos"], b.state()["pos"])
