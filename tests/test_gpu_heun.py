@@ -22,9 +22,9 @@ def wrapdiff(a, b, L):
 
 def test_heun_oracle_mode_matches_oracle(gpu_lib, oracle_lib):
     G = gpu_lib
-    p = S.growth_params(box=60.0, dt=1e-3, div_tau_mu=0.03, div_tau_sigma=0.005, apop_rate=2.0, noise_D=0.002)
+    p = S.growth_params(box=60.0, dt=1e-3, div_tau_mu=0.06, div_tau_sigma=0.01, apop_rate=2.0, noise_D=0.002)
     st = S.disk_colony(400, p, seed=21)
-    cap = 4000
+    cap = 8000
     eng = G.Engine([p], [cap], precision=G.PREC_FP64, rng=G.RNG_DSFMT, seed=17, integrator=G.INTEGRATOR_HEUN)
     eng.upload(0, **st)
     eng.step(120)
