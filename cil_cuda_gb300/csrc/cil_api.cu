@@ -317,10 +317,15 @@ RebuildArgs rebuild_args(cil_handle *h) {
 // A rebuild inside a step needs no velocities (the force pass rewrites them); a rebuild
 // outside a step (cil_forces, cil_bins) carries them through the permutation so that a
 // later download still pairs each element with its own velocity.
-cil_status do_rebuild(cil_handle *h, bool carry_vel = false, bool exact = false) {
+// vel_to: carry the velocities through the permutation into this buffer instead (the first
+// half step's velocities of a Heun step, read by the second half step; no buffer swap).
+cil_status do_rebuild(cil_handle *h, bool carry_vel = false, bool exact = false, double *vel_to = nullptr) {
   if (exact) h->need_exact = true;
   RebuildArgs a = rebuild_args(h);
-  if (carry_vel) {
+  if (vel_to) {
+    a.vel_in = h->d_vel;
+    a.vel_out = vel_to;
+  } else if (carry_vel) {
     if (!h->d_vel2) {
       h->d_vel2 = dalloc<double>(static_cast<size_t>(h->D) * h->SS);
       if (!h->d_vel2) return fail(h, CIL_ERR_CUDA, "out of device memory (velocities)");
@@ -679,17 +684,32 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     h->lists_stale = false;
     h->launches += permute ? 15 : 8;
   } else {
-    st = do_rebuild(h);
+    // the second half step of a Heun step reads the first half's velocities: carried through
+    // the re-sort (only when velocities are written, i.e. the last step of a cil_step call)
+    double *vel_prev = nullptr;
+    if (heun == 2 && last) {
+      if (!h->d_vel2) {
+        h->d_vel2 = dalloc<double>(static_cast<size_t>(h->D) * h->SS);
+        if (!h->d_vel2) return fail(h, CIL_ERR_CUDA, "out of device memory (velocities)");
+      }
+      vel_prev = h->d_vel2;
+    }
+    st = do_rebuild(h, false, false, vel_prev);
     if (st != CIL_OK) return st;
     h->launches += 10;
+    if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
+    ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
+    fa.heun = heun;
+    fa.vel_prev = vel_prev;
+    launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+    h->cur = 1 - h->cur;
+    if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
+    return CIL_OK;
   }
   if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
   fa.heun = heun;
-  if (h->skin_mode)
-    launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->list_variant, h->stream);
-  else
-    launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+  launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->list_variant, h->stream);  // skin mode
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
   return CIL_OK;

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           const double v = F[d] * C.mu_eff[j];
-          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * SS + s] + v) : v;
+          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * ((a.vel_prev ? a.vel_prev : a.vel)[d * SS + s] + v) : v;
         }
       }
     }
@@ -356,7 +356,7 @@ __device__ __forceinline__ void mixed_integrate(const ForceArgs &a, const Colony
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       const double v = static_cast<double>(F[d] * C.mu_f[j]);
-      a.vel[d * a.SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * a.SS + s] + v) : v;
+      a.vel[d * a.SS + s] = a.heun == 2 ? 0.5 * ((a.vel_prev ? a.vel_prev : a.vel)[d * a.SS + s] + v) : v;
     }
   }
 }
@@ -821,7 +821,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           const double v = static_cast<double>(F[d] * C.mu_f[j]);
-          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * (a.vel[d * SS + s] + v) : v;
+          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * ((a.vel_prev ? a.vel_prev : a.vel)[d * SS + s] + v) : v;
         }
       }
     }

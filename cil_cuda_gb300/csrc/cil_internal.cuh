@@ -474,6 +474,7 @@ struct ForceArgs {
   SchedState *sched;       // speed statistics for the scheduler
   const double *noise;     // oracle mode: uploaded normals (already scaled), canonical order
   double *vel;             // slot order, may be null
+  const double *vel_prev;  // Heun second half step: the first half's velocities (null: vel itself)
   double *frc;             // slot order, may be null
   const int *ts_dev;       // device step counter: the step being computed
   int ts;                  // filled from *ts_dev at kernel entry

@@ -43,12 +43,12 @@ def test_heun_oracle_mode_matches_oracle(gpu_lib, oracle_lib):
 def test_heun_is_two_half_euler_steps(gpu_lib):
     G = gpu_lib
     p = S.growth_params(box=60.0, dt=1e-3, divide=0, apop_rate=0.0, noise_D=0.0)
-    st = S.disk_colony(2000, p, seed=22)
+    st = S.disk_colony(1000, p, seed=22)
     q = dict(p)
     q["dt"] = 0.5e-3
     out = []
     for params, integ, n in ((p, G.INTEGRATOR_HEUN, 60), (q, G.INTEGRATOR_EULER, 120)):
-        eng = G.Engine([params], [2100], precision=G.PREC_FP64, rng=G.RNG_PHILOX, seed=3, integrator=integ)
+        eng = G.Engine([params], [1100], precision=G.PREC_FP64, rng=G.RNG_PHILOX, seed=3, integrator=integ)
         eng.upload(0, **st)
         eng.step(n)
         out.append(eng.download(0)["pos"])
