@@ -149,10 +149,10 @@ def barrier(dist):
 
 
 def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0, sched=False, graphs=True,
-             tune=None):
+             tune=None, integrator=0):
     """Device-timed run of one form; returns particle-steps/s and the timing details."""
     eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
-                   graphs=graphs, **(tune or {}))
+                   graphs=graphs, integrator=integrator, **(tune or {}))
     eng.upload(0, **st)
     if sched:
         from cil_cuda_gb300 import skin_scheduler as SS
@@ -537,6 +537,13 @@ def main():
         "gpu_launches": skinf["timings"]["launches"],
         "clocks": clocks,
     }
+    if args.only is None:
+        # the reference's StochasticHeun (two force passes per step) in the headline form
+        heun = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist,
+                        skin=mlp_skin if have_mlp else args.skin, sched=have_mlp, tune=tune,
+                        integrator=G.INTEGRATOR_HEUN)
+        line["forms"]["mixed_skin_heun"] = allreduce_sum(dist, heun["psteps"]) / allreduce_max(dist, heun["dev_s"])
+        line["forms"]["mixed_skin_heun_ms_per_step"] = heun["dev_s"] / args.steps * 1e3
     if args.only is None and not args.no_batched:
         line["batched_sweep"] = run_batched(G, device, min(args.steps, 300), args.warmup, have_mlp)
         try:
