@@ -46,7 +46,7 @@ struct HostColony {
 }  // namespace
 
 struct GraphSlot {
-  int key;                 // cur | meta << 1 | pu << 2 at the first of the two steps
+  int key;                 // cur | meta << 1 | pu << 2 at the first step, | two steps << 3, | last << 4
   uint64_t gen;
   cudaGraphExec_t exec;
   int64_t launches;        // kernels in the graph
@@ -768,19 +768,19 @@ void restore_host_state(cil_handle *h, const HostStepState &s) {
   h->ts = s.ts;
 }
 
-// The executable graph of two steady steps starting from the current parities, captured on
-// first use (the capture advances the host state as the two steps would; the caller then
-// replays the graph). On a capture failure the host state is put back, graphs are switched
-// off for the handle and null is returned.
-cudaGraphExec_t steady_graph(cil_handle *h, int64_t *launches_per_pair) {
-  const int key = h->cur | (h->meta << 1) | (h->pu << 2);
+// The executable graph of `nsteps` (1 or 2) steady steps starting from the current
+// parities, the last of them writing the velocities when `last` (the final step of a cil_step
+// call), captured on first use (the capture advances the host state as the steps would; the
+// caller then replays the graph). On a capture failure the host state is put back, graphs are
+// switched off for the handle and null is returned.
+cudaGraphExec_t steady_graph(cil_handle *h, int nsteps, bool last, int64_t *launches_per_graph) {
+  const int key = h->cur | (h->meta << 1) | (h->pu << 2) | ((nsteps == 2 ? 1 : 0) << 3) | ((last ? 1 : 0) << 4);
   for (auto &gs : h->graphs)
     if (gs.key == key && gs.gen == h->graph_gen) {
       HostStepState s = host_state(h);
-      advance_host_state(h, &s);
-      advance_host_state(h, &s);
+      for (int i = 0; i < nsteps; ++i) advance_host_state(h, &s);
       restore_host_state(h, s);
-      *launches_per_pair = gs.launches;
+      *launches_per_graph = gs.launches;
       return gs.exec;
     }
   const HostStepState before = host_state(h);
@@ -791,15 +791,14 @@ cudaGraphExec_t steady_graph(cil_handle *h, int64_t *launches_per_pair) {
     h->graphs_off = true;
     return nullptr;
   }
-  const cil_status s1 = enqueue_step(h, false, false, 0);
-  const cil_status s2 = s1 == CIL_OK ? enqueue_step(h, false, false, 0) : s1;
+  cil_status sc = CIL_OK;
+  for (int i = 0; i < nsteps && sc == CIL_OK; ++i) sc = enqueue_step(h, last && i == nsteps - 1, false, 0);
   const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
   HostStepState expect = before;
-  advance_host_state(h, &expect);
-  advance_host_state(h, &expect);
+  for (int i = 0; i < nsteps; ++i) advance_host_state(h, &expect);
   cudaGraphExec_t exec = nullptr;
-  const bool ok = s1 == CIL_OK && s2 == CIL_OK && ec == cudaSuccess && g != nullptr &&
-                  same_state(host_state(h), expect) && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+  const bool ok = sc == CIL_OK && ec == cudaSuccess && g != nullptr && same_state(host_state(h), expect) &&
+                  cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
   if (g) cudaGraphDestroy(g);
   if (!ok) {
     cudaGetLastError();
@@ -809,9 +808,9 @@ cudaGraphExec_t steady_graph(cil_handle *h, int64_t *launches_per_pair) {
     h->graphs_off = true;
     return nullptr;
   }
-  *launches_per_pair = h->launches - launches0;
+  *launches_per_graph = h->launches - launches0;
   h->launches = launches0;
-  h->graphs.push_back(GraphSlot{key, h->graph_gen, exec, *launches_per_pair});
+  h->graphs.push_back(GraphSlot{key, h->graph_gen, exec, *launches_per_graph});
   h->graphs_captured += 1;
   return exec;
 }
@@ -1010,6 +1009,9 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
               h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
   h->d_vel = dalloc<double>(D * SS);
+  // Heun without lists carries the first half step's velocities through the second re-sort;
+  // allocated here so that a captured step never allocates
+  if (h->cfg.integrator == CIL_INTEGRATOR_HEUN && !h->skin_mode && !h->d_vel2) h->d_vel2 = dalloc<double>(D * SS);
   h->d_key = dalloc<int>(SS);
   h->d_perm = dalloc<unsigned long long>(SS);
   h->d_slot_of = dalloc<int>(2 * static_cast<size_t>(h->CC));
@@ -1164,18 +1166,20 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
   int k = 0;
   while (k < nsteps) {
     const size_t e0 = 4 * seg_graph.size();
-    // two steady steps, neither the last one of the call (which writes velocities)
-    if (!h->graphs_off && k + 2 < nsteps && steady_step(h, h->ts) && steady_step(h, h->ts + 1)) {
+    // steady steps replay a captured graph: two at a time, or one (the call's last step,
+    // which writes the velocities, or a step followed by a re-sort)
+    if (!h->graphs_off && steady_step(h, h->ts)) {
+      const int n = (k + 2 <= nsteps && steady_step(h, h->ts + 1)) ? 2 : 1;
       int64_t nl = 0;
-      cudaGraphExec_t ex = steady_graph(h, &nl);
+      cudaGraphExec_t ex = steady_graph(h, n, k + n == nsteps, &nl);
       if (ex) {
         CUDA_TRY(h, cudaEventRecord(pool_event(h, e0), h->stream));
         CUDA_TRY(h, cudaGraphLaunch(ex, h->stream));
         CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
         seg_graph.push_back(1);
         h->launches += nl;
-        h->graph_steps += 2;
-        k += 2;
+        h->graph_steps += n;
+        k += n;
         continue;
       }
     }

@@ -114,10 +114,12 @@ typedef struct cil_config {
 #define CIL_INTEGRATOR_HEUN 1
 
 /* cil_config.flags: run every step as individual launches (no CUDA graphs). By default, in
- * Philox mode, pairs of steps whose launches depend on nothing the host decides (no slot
- * re-sort, no FP64 re-anchoring, not the last step of a cil_step call) are captured once as
- * a CUDA graph per buffer parity and replayed; the kernels read the step index from device
- * memory. cil_timings then reports phase times for the individually launched steps only. */
+ * Philox mode, steps whose launches depend on nothing the host decides (no slot re-sort, no
+ * FP64 re-anchoring) are captured once as CUDA graphs of two steps or of one step (per buffer
+ * parity, and with or without the velocity output of a call's last step) and replayed, so a
+ * one-step cil_step call (the reference's mdStep) launches one graph; the kernels read the
+ * step index from device memory. cil_timings then reports phase times for the individually
+ * launched steps only. */
 #define CIL_FLAG_NO_GRAPH 1
 
 /* Host view of one colony in the reference layout. */
