@@ -54,6 +54,7 @@ struct GraphSlot {
 
 struct cil_handle {
   cil_config cfg{};
+  ColonyCounters *h_cnt = nullptr;  // pinned host copy of d_cnt (cil_step's status read)
   int B = 0, D = 2;
   std::vector<HostColony> hc;
   std::vector<ColonyConst> cc;
@@ -169,6 +170,7 @@ void free_all(cil_handle *h) {
     if (gs.exec) cudaGraphExecDestroy(gs.exec);
   h->graphs.clear();
   if (h->h_noise) cudaFreeHost(h->h_noise);
+  if (h->h_cnt) cudaFreeHost(h->h_cnt);
   for (auto e : h->evpool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
@@ -598,17 +600,22 @@ cudaEvent_t pool_event(cil_handle *h, size_t i) {
   return h->evpool[i];
 }
 
-cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = nullptr) {
-  std::vector<ColonyCounters> k(h->B);
-  CUDA_TRY(h, cudaMemcpyAsync(k.data(), h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-  if (out) *out = k;
+// Error bits of the colonies' counters as a status (and the handle's message).
+cil_status counter_status(cil_handle *h, const ColonyCounters *k) {
   for (int c = 0; c < h->B; ++c) {
     if (k[c].err & kErrNan) return fail(h, CIL_ERR_NAN, "non-finite force in colony " + std::to_string(c));
     if (k[c].err & kErrBox) return fail(h, CIL_ERR_OUT_OF_BOX, "element left the box in colony " + std::to_string(c));
     if (k[c].err & kErrCap) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(c));
   }
   return CIL_OK;
+}
+
+cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = nullptr) {
+  std::vector<ColonyCounters> k(h->B);
+  CUDA_TRY(h, cudaMemcpyAsync(k.data(), h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (out) *out = k;
+  return counter_status(h, k.data());
 }
 
 // One step's launches on the handle's stream (oracle mode: with its host draws). When timed,
@@ -979,6 +986,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   const size_t SS = h->SS, D = h->D;
   h->d_col = dalloc<ColonyConst>(h->B);
   h->d_cnt = dalloc<ColonyCounters>(h->B);
+  // pinned copy of the counters: the status read that ends every cil_step call
+  if (!h->h_cnt && cudaHostAlloc(&h->h_cnt, sizeof(ColonyCounters) * h->B, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    h->h_cnt = nullptr;
+  }
   const bool mixed = cfg->precision == CIL_PREC_MIXED;
   for (int b = 0; b < 2; ++b) {
     h->d_x[b] = dalloc<double>(D * SS);
@@ -1188,6 +1200,9 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
     seg_graph.push_back(0);
     k += 1;
   }
+  if (h->h_cnt)
+    CUDA_TRY(h, cudaMemcpyAsync(h->h_cnt, h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost,
+                                h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   h->t_total = 0.0;
   const size_t nseg = seg_graph.size();
@@ -1207,7 +1222,7 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
     h->t_events += c;
   }
   if (ts_out) *ts_out = h->ts;
-  return check_counters(h);
+  return h->h_cnt ? counter_status(h, h->h_cnt) : check_counters(h);
 }
 
 cil_status cil_forces(cil_handle *h, int32_t colony, double *frc) {
