@@ -32,7 +32,9 @@ EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step
             "cil_graph_info", "cil_gsd_create", "cil_gsd_write_chunk", "cil_gsd_end_frame", "cil_gsd_nframes",
             "cil_gsd_close", "cil_gsd_last_error", "cil_frame_open", "cil_frame_write", "cil_frame_flush",
             "cil_frame_close", "cil_frame_get_stats", "cil_frame_last_error", "cil_input_load", "cil_input_config",
-            "cil_input_initial_state", "cil_input_last_error", "cil_input_free"]
+            "cil_input_initial_state", "cil_input_last_error", "cil_input_free", "cil_cycle_create",
+            "cil_cycle_destroy", "cil_cycle_upload", "cil_cycle_step", "cil_cycle_check_positions",
+            "cil_cycle_download", "cil_cycle_timings", "cil_cycle_last_error"]
 
 
 class CilError(RuntimeError):
@@ -180,6 +182,52 @@ class RunInfo(C.Structure):
 
 
 FRAME_TYPES_IN_FIRST = 1
+APOP_NONE, APOP_CYCLE_PRESSURE, APOP_PRESSURE_TIME = 0, 1, 2
+
+CYCLE_FIELDS = [
+    ("dim", C.c_int32), ("periodic", C.c_int32 * 3), ("box", C.c_double * 3), ("dt", C.c_double),
+    ("sigma_core", C.c_double), ("E", C.c_double), ("nu", C.c_double), ("adhesion", C.c_double),
+    ("motility", C.c_double), ("zeta", C.c_double), ("zeta_p", C.c_double), ("zeta_p_beta", C.c_double),
+    ("noise_D", C.c_double), ("divide", C.c_int32), ("apoptosis", C.c_int32),
+    ("tau_div_mu", C.c_double), ("tau_div_sigma", C.c_double), ("tau_mig_mu", C.c_double),
+    ("tau_mig_sigma", C.c_double), ("v1", C.c_double), ("cycle_tau_r", C.c_double), ("cycle_tau_v", C.c_double),
+    ("cycle_tau_p", C.c_double), ("cycle_sigma_min", C.c_double), ("cycle_p0", C.c_double),
+    ("cycle_beta_vs", C.c_double), ("cycle_rho_ratio", C.c_double), ("cycle_r_maxed", C.c_double),
+    ("cycle_p_shift", C.c_double), ("cycle_p_shift_tau", C.c_double), ("osmotic_pressure", C.c_double),
+    ("apop_pressure", C.c_double), ("apop_duration", C.c_double), ("apop_rate", C.c_double),
+    ("extr_gamma", C.c_double), ("drain", C.c_int32), ("pad", C.c_int32),
+]
+
+
+class CycleParams(C.Structure):
+    _fields_ = CYCLE_FIELDS
+
+
+class CycleView(C.Structure):
+    _fields_ = [("ncells", C.c_int32), ("capacity", C.c_int32), ("ts", C.c_int32), ("pad", C.c_int32)] + [
+        (k, C.POINTER(C.c_double)) for k in ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "pressure")
+    ] + [("tpressure", C.POINTER(C.c_int32))]
+
+
+def cycle_params(**kw) -> CycleParams:
+    """cil_cycle_params with the reference's defaults (Cell.cuh:236-260) for what is not given."""
+    base = dict(dim=2, periodic=[1, 1, 0], box=[100.0, 100.0, 0.0], dt=1e-5, sigma_core=1.1283791670955126, E=100.0,
+                nu=0.5, adhesion=0.2, motility=0.0, zeta=0.01, zeta_p=0.0, zeta_p_beta=0.0, noise_D=0.0, divide=1,
+                apoptosis=APOP_NONE, tau_div_mu=1.0, tau_div_sigma=0.1, tau_mig_mu=0.0, tau_mig_sigma=0.0, v1=15.0,
+                cycle_tau_r=1.0, cycle_tau_v=1.0, cycle_tau_p=0.0, cycle_sigma_min=1.1283791670955126, cycle_p0=5.0,
+                cycle_beta_vs=0.0, cycle_rho_ratio=1.0, cycle_r_maxed=1.0, cycle_p_shift=0.0, cycle_p_shift_tau=0.0,
+                osmotic_pressure=0.0, apop_pressure=1.0, apop_duration=8.0, apop_rate=0.0, extr_gamma=0.0, drain=0,
+                pad=0)
+    base.update(kw)
+    q = CycleParams()
+    for k, v in base.items():
+        f = getattr(q, k)
+        if isinstance(f, C.Array):
+            for i, x in enumerate(v):
+                f[i] = x
+        else:
+            setattr(q, k, v)
+    return q
 
 _lib = None
 
@@ -272,6 +320,22 @@ def lib():
         L.cil_input_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_input_free.restype = None
         L.cil_input_free.argtypes = [vp]
+        L.cil_cycle_create.restype = i32
+        L.cil_cycle_create.argtypes = [C.POINTER(CycleParams), i32, C.c_uint64, i32, C.POINTER(vp)]
+        L.cil_cycle_destroy.restype = None
+        L.cil_cycle_destroy.argtypes = [vp]
+        L.cil_cycle_upload.restype = i32
+        L.cil_cycle_upload.argtypes = [vp, C.POINTER(CycleView)]
+        L.cil_cycle_step.restype = i32
+        L.cil_cycle_step.argtypes = [vp, i32, C.POINTER(C.c_int64)]
+        L.cil_cycle_check_positions.restype = i32
+        L.cil_cycle_check_positions.argtypes = [vp]
+        L.cil_cycle_download.restype = i32
+        L.cil_cycle_download.argtypes = [vp, C.POINTER(CycleView)]
+        L.cil_cycle_timings.restype = i32
+        L.cil_cycle_timings.argtypes = [vp, dp, C.POINTER(C.c_int64)]
+        L.cil_cycle_last_error.restype = None
+        L.cil_cycle_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
@@ -668,6 +732,86 @@ class RunInput:
     def close(self):
         if getattr(self, "h", None):
             self.L.cil_input_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CycleEngine:
+    """The single-element cell-cycle model (include/cil_cycle.h) of one colony on one GPU."""
+
+    def __init__(self, params: dict, capacity: int, *, seed: int = 0, device: int = 0):
+        self.L = lib()
+        self.params = dict(params)
+        self.p = cycle_params(**params)
+        self.dim = self.p.dim
+        self.cap = int(capacity)
+        h = C.c_void_p()
+        st = self.L.cil_cycle_create(C.byref(self.p), self.cap, seed, device, C.byref(h))
+        if st != 0:
+            raise CilError(st, "cil_cycle_create failed")
+        self.h = h
+
+    def _check(self, st):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self.L.cil_cycle_last_error(self.h, buf, 512)
+            raise CilError(st, buf.value.decode())
+
+    def upload(self, pos, sigma=None, sigma_t=None, theta=None, rho=None, angvel=None, pressure=None,
+               tpressure=None, ts: int = 0):
+        pos = np.ascontiguousarray(pos, np.float64)
+        n = pos.shape[0]
+        keep = []
+
+        def ptr(a, dt=np.float64):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(C.c_double if dt == np.float64 else C.c_int32))
+
+        v = CycleView(ncells=n, capacity=n, ts=ts, pad=0, pos=_dp(pos), vel=None, sigma=ptr(sigma),
+                      sigma_t=ptr(sigma_t), theta=ptr(theta), rho=ptr(rho), angvel=ptr(angvel),
+                      pressure=ptr(pressure), tpressure=ptr(tpressure, np.int32))
+        self._check(self.L.cil_cycle_upload(self.h, C.byref(v)))
+
+    def step(self, n: int = 1) -> int:
+        ts = C.c_int64()
+        self._check(self.L.cil_cycle_step(self.h, n, C.byref(ts)))
+        return ts.value
+
+    def check_positions(self):
+        self._check(self.L.cil_cycle_check_positions(self.h))
+
+    def download(self) -> dict:
+        cap, D = self.cap, self.dim
+        a = {k: np.zeros(cap) for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure")}
+        a["pos"] = np.zeros((cap, D))
+        a["vel"] = np.zeros((cap, D))
+        a["tpressure"] = np.zeros(cap, np.int32)
+        v = CycleView(ncells=0, capacity=cap, ts=0, pad=0, tpressure=_ip(a["tpressure"]),
+                      **{k: _dp(a[k]) for k in ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "pressure")})
+        self._check(self.L.cil_cycle_download(self.h, C.byref(v)))
+        n = v.ncells
+        out = {k: x[:n] for k, x in a.items()}
+        out["ncells"] = n
+        out["ts"] = v.ts
+        return out
+
+    def timings(self) -> dict:
+        t = C.c_double()
+        nl = C.c_int64()
+        self._check(self.L.cil_cycle_timings(self.h, C.byref(t), C.byref(nl)))
+        return dict(total_ms=t.value, launches=nl.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cil_cycle_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -17,7 +17,10 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcilgpu.so")
 RUNNER = os.path.join(OUT, "cil_gpu_run")
 SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu",
-           "cil_frame.cu", "cil_input.cpp"]
+           "cil_frame.cu", "cil_input.cpp", "cil_cycle.cu"]
+# per-file flags: the single-element cycle model keeps FP64 products and sums separate (no FMA
+# contraction) so that it computes exactly what its host restatement computes
+EXTRA = {"cil_cycle.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -50,7 +53,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         if (not ptxas_info and os.path.exists(obj)
                 and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
             continue
-        cmd = [nvcc(), *flags(extra), "-c", src_path, "-o", obj]
+        cmd = [nvcc(), *flags(extra), *EXTRA.get(src, []), "-c", src_path, "-o", obj]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     failed = []
     for src, p in procs:

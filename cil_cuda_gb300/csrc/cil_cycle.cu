@@ -1,0 +1,1072 @@
+// The single-element cell-cycle model on the GPU (include/cil_cycle.h).
+//
+// Layout: structure of arrays in index order (cell i at i), FP64. Two complete state sets;
+// a removal (apoptosis, drain) compacts the survivors stably into the other set and the host
+// flips the set index. Positions are double-buffered within a step (the force pass reads one
+// buffer and writes the other).
+//
+// A step (no host synchronisation; the cell count lives on the device):
+//   bins       k_cy_keys / scan / k_cy_scatter / k_cy_sort: a counting sort of the cells into
+//              bins of fixed width (the largest diameter at upload), ascending cell index
+//              inside a bin; the pair search walks +-k bins with k from the colony's largest
+//              diameter of the previous step, so growing cells never outgrow the search;
+//   forces     k_cy_force: motility along the velocity, passive noise, Hertz contacts with
+//              adhesion and the pressure sum, then the position update with the pressure-
+//              dependent friction, in one thread per cell;
+//   cycle      k_cy_cycle (ODEs, division flag, per-block count) / k_cy_scan_blocks /
+//              k_cy_divide (daughters appended in mother order);
+//   apoptosis  k_cy_apo_mark / scan / k_cy_compact (only with apoptosis on).
+// The file is compiled without FMA contraction, so that the arithmetic is that of the host
+// restatement the tests compare with.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "cil_cycle.h"
+#include "cil_internal.cuh"
+
+namespace {
+
+using cil::kTile;
+using cil::philox4x32_10;
+using cil::u32x4;
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kLn2 = 0.69314718055994530942;
+constexpr int kScanTile = 1024;  // elements per block of the scans
+
+// Philox purposes (third counter word)
+constexpr uint32_t kCyNoise = 11, kCyDir = 12, kCyDiv = 13, kCyApo = 14, kCyInit = 15;
+
+struct CyConst {
+  int D;
+  int periodic[3];
+  double box[3];
+  double dt;
+  int ns[3];
+  double bw[3];       // bin width per axis
+  double inv_bw[3];
+  double sigma_core;
+  double hz_c;        // (1 - nu^2) / E
+  double adhesion;
+  double motility, zeta, zeta_p, zeta_p_beta;
+  double noise_amp;   // sqrt(2 D) / sqrt(dt)
+  int divide;
+  int apoptosis;
+  double tau_div_mu, tau_div_sigma, tau_mig_mu, tau_mig_sigma;
+  double v1, tau_r, tau_v, tau_p;   // tau_* in steps
+  double v_s;
+  double p0, beta_vs, rho_ratio, r_maxed_inv, p_shift, p_shift_tau_inv, osm;
+  double apop_pressure, apop_duration, apop_rate_step, extr_gamma;
+  double apop_steps;  // apop_duration / dt
+  uint32_t seed_lo, seed_hi;
+  int capacity;
+};
+
+struct CySet {
+  double *x;      // [D][cap]
+  double *v;      // [D][cap]
+  double *sig, *sigt, *theta, *rho, *om, *p;
+  int *tp, *t0, *tsw;
+};
+
+struct CyCounters {
+  int n;
+  int err;
+  long long ndiv_total;
+  long long napo_total;
+  unsigned long long sigma_max_bits;  // largest diameter (non-negative doubles order like their bits)
+  int ndiv_step;
+  int nrem_step;
+};
+
+constexpr int kErrCapacity = 1;
+constexpr int kErrNonFinite = 2;
+constexpr int kErrOutOfBox = 4;
+constexpr int kErrCrowded = 8;     // a bin holds more than kBinSortMax cells
+constexpr int kBinSortMax = 256;   // cells a bin may hold (about 1 at the bin width used)
+
+// ---------------------------------------------------------------- draws
+__host__ __device__ inline double u53(uint32_t a, uint32_t b) {
+  const uint64_t m = (static_cast<uint64_t>(a) << 21) ^ (static_cast<uint64_t>(b) >> 11);
+  return static_cast<double>(m & ((1ull << 53) - 1)) * 1.1102230246251565e-16;
+}
+
+// Two standard normals (Box-Muller, FP64) from the four words of one Philox block.
+__device__ inline void normal2(const u32x4 &r, double *n0, double *n1) {
+  const double a = 1.0 - u53(r.v[0], r.v[1]);  // (0, 1]
+  const double b = u53(r.v[2], r.v[3]);
+  const double rad = sqrt(-2.0 * log(a));
+  const double ang = 6.283185307179586 * b;
+  *n0 = rad * cos(ang);
+  *n1 = rad * sin(ang);
+}
+
+__device__ inline u32x4 draw(const CyConst &C, uint32_t cell, int ts, uint32_t purpose, uint32_t sub) {
+  return philox4x32_10(cell, static_cast<uint32_t>(ts), purpose, sub, C.seed_lo, C.seed_hi);
+}
+
+__device__ inline int nint(double a) { return a >= 0.0 ? static_cast<int>(a + 0.5) : static_cast<int>(a - 0.5); }
+
+// max(Nint(x / dt), 1) (randomTimeSpan, MD.cuh:434-436)
+__device__ inline int span_steps(double x, double dt) {
+  const int s = nint(x / dt);
+  return s > 1 ? s : 1;
+}
+
+// exp(mu2 + s2 Z), mu2 = log(mu^2 / sqrt(mu^2 + s^2)), s2 = sqrt(log(1 + s^2/mu^2)) (Random.hpp:55-60)
+__device__ inline double lognormal(double mu, double s, double z) {
+  const double mu2 = log((mu * mu) / (sqrt(mu * mu + s * s)));
+  const double s2 = sqrt(log(1 + (s * s) / (mu * mu)));
+  return exp(mu2 + s2 * z);
+}
+
+// ---------------------------------------------------------------- geometry (Utils.hpp:223-256)
+__device__ inline double area_of(double s) { return kPi * ((s / 2) * (s / 2)); }
+__device__ inline double volume_of(double s) { return 4 * kPi * ((s / 2) * (s / 2) * (s / 2)) / 3; }
+__device__ inline double sigma_of_area(double a) { return 2 * sqrt(a / kPi); }
+__device__ inline double sigma_of_volume(double v) { return 2 * cbrt(3 * v / (4 * kPi)); }
+
+__device__ inline double contact_length(double a, double b, double h) {
+  const double ra = a / 2, rb = b / 2;
+  const double q = ra - (2 * rb * h - h * h) / (2 * (ra + rb - h));
+  double t = 2 * sqrt(ra * ra - q * q);
+  const double small_r = (a <= b) ? a : b;
+  return isnan(t) ? small_r : t;
+}
+
+__device__ inline double contact_area(double r, double a, double b) {
+  const double ra = a / 2, rb = b / 2;
+  const double u = r * r - rb * rb + ra * ra;
+  const double t = sqrt(4 * (r * r) * (ra * ra) - u * u) / (2 * r);
+  return t > 0 ? kPi * (t * t) : 0.0;
+}
+
+__device__ inline double wrap(double t, double L) {  // fmod(t + L, L)
+  return fmod(t + L, L);
+}
+
+__device__ inline int bin_of(const CyConst &C, const double *xd) {
+  int b = 0;
+  for (int d = 0; d < C.D; ++d) {
+    int v = static_cast<int>(xd[d] * C.inv_bw[d]);
+    v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
+    b = b * C.ns[d] + v;
+  }
+  return b;
+}
+
+// ---------------------------------------------------------------- block scan
+__device__ inline int block_excl_scan(int v, int *total) {
+  __shared__ int ws[kTile / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) ws[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < kTile / 32 ? ws[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < kTile / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  const int base = wid > 0 ? ws[wid - 1] : 0;
+  *total = ws[kTile / 32 - 1];
+  __syncthreads();
+  return base + inc - v;
+}
+
+// Exclusive scan of `count[0..m)` in place by one block; count[m] receives the total.
+__global__ void k_cy_scan_small(int *count, int m) {
+  int carry = 0;
+  for (int base = 0; base < m; base += kTile) {
+    const int i = base + threadIdx.x;
+    const int v = i < m ? count[i] : 0;
+    int tot;
+    const int ex = block_excl_scan(v, &tot);
+    if (i < m) count[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) count[m] = carry;
+}
+
+// Block sums of kScanTile-sized chunks (4 per thread)
+__global__ void k_cy_chunk_sums(const int *count, int m, int *part) {
+  const int b0 = blockIdx.x * kScanTile + threadIdx.x * 4;
+  int s = 0;
+  for (int q = 0; q < 4; ++q) s += (b0 + q < m) ? count[b0 + q] : 0;
+  int tot;
+  block_excl_scan(s, &tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// Exclusive scan of count[0..m) using the scanned chunk sums, into start[0..m] (start[m] =
+// total; the chunks cover index m, count[m] reads as 0)
+__global__ void k_cy_chunk_apply(const int *count, int m, const int *part, int *start) {
+  const int b0 = blockIdx.x * kScanTile + threadIdx.x * 4;
+  int c[4], s = 0;
+  for (int q = 0; q < 4; ++q) {
+    c[q] = (b0 + q < m) ? count[b0 + q] : 0;
+    s += c[q];
+  }
+  int tot;
+  int e = part[blockIdx.x] + block_excl_scan(s, &tot);
+  for (int q = 0; q < 4; ++q) {
+    if (b0 + q <= m) start[b0 + q] = e;
+    e += c[q];
+  }
+}
+
+// ---------------------------------------------------------------- bins
+__global__ void k_cy_clear(int *a, int m) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) a[i] = 0;
+}
+
+__global__ void k_cy_keys(CyConst C, CySet S, const CyCounters *cnt, int *key, int *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt->n) return;
+  double xd[3];
+  for (int d = 0; d < C.D; ++d) xd[d] = S.x[static_cast<size_t>(d) * C.capacity + i];
+  const int b = bin_of(C, xd);
+  key[i] = b;
+  atomicAdd(count + b, 1);
+}
+
+__global__ void k_cy_scatter(const CyCounters *cnt, const int *key, const int *start, int *cursor, int *list) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt->n) return;
+  const int b = key[i];
+  const int pos = start[b] + atomicAdd(cursor + b, 1);
+  list[pos] = i;
+}
+
+// ascending cell index inside every bin (insertion sort: bins hold a few cells; a bin with
+// more than kBinSortMax cells means overlapping cells and is reported instead of sorted)
+__global__ void k_cy_sort(const int *start, int nbins, int *list, CyCounters *cnt) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  const int lo = start[b], hi = start[b + 1];
+  if (hi - lo > kBinSortMax) {
+    atomicOr(&cnt->err, kErrCrowded);
+    return;
+  }
+  for (int i = lo + 1; i < hi; ++i) {
+    const int v = list[i];
+    int j = i - 1;
+    while (j >= lo && list[j] > v) {
+      list[j + 1] = list[j];
+      --j;
+    }
+    list[j + 1] = v;
+  }
+}
+
+// ---------------------------------------------------------------- forces + update
+__global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
+                                                    CyCounters *cnt, const int *start, const int *list,
+                                                    const int *ts_dev) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  if (i >= n) return;
+  const int ts = *ts_dev;
+  const size_t cap = C.capacity;
+  const int D = C.D;
+  double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, F[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) {
+    xi[d] = S.x[d * cap + i];
+    vi[d] = S.v[d * cap + i];
+  }
+  const double si = S.sig[i];
+  // ---- motility along the velocity (singleCellForce, MD.cu:600-646)
+  {
+    double v2 = 0.0;
+    for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+    double vl = sqrt(v2);
+    if (vl == 0.0) {  // a direction at random, length 1e-11 (BIG_TOL_MP)
+      const u32x4 r = draw(C, i, ts, kCyDir, 0);
+      if (D == 2) {
+        const double ang = 6.283185307179586 * u53(r.v[0], r.v[1]);
+        vi[0] = 1e-11 * cos(ang);
+        vi[1] = 1e-11 * sin(ang);
+      } else {
+        const double z = 2.0 * u53(r.v[0], r.v[1]) - 1.0;
+        const double ang = 6.283185307179586 * u53(r.v[2], r.v[3]);
+        const double s = sqrt(1.0 - z * z);
+        vi[0] = 1e-11 * (s * cos(ang));
+        vi[1] = 1e-11 * (s * sin(ang));
+        vi[2] = 1e-11 * z;
+      }
+      v2 = 0.0;
+      for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+      vl = sqrt(v2);
+    }
+    for (int d = 0; d < D; ++d) F[d] = C.motility * (vi[d] / vl);
+  }
+  // ---- passive noise (CIL.cu:84-97)
+  if (C.noise_amp > 0.0) {
+    double nz[4];
+    normal2(draw(C, i, ts, kCyNoise, 0), &nz[0], &nz[1]);
+    if (D == 3) normal2(draw(C, i, ts, kCyNoise, 1), &nz[2], &nz[3]);
+    for (int d = 0; d < D; ++d) F[d] += C.zeta * (C.noise_amp * nz[d]);
+  }
+  // ---- Hertz contacts with adhesion and the pressure (device draft, MD.cu:302-366)
+  double pres = 0.0;
+  {
+    int bi[3] = {0, 0, 0};
+    {
+      int b = 0;
+      for (int d = 0; d < D; ++d) {
+        int v = static_cast<int>(xi[d] * C.inv_bw[d]);
+        v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
+        bi[d] = v;
+        b = b * C.ns[d] + v;
+      }
+      (void)b;
+    }
+    // bins to search on each side: the largest diameter of the colony over the bin width
+    const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      const double kk = ceil(smax * C.inv_bw[d]);
+      const int k = (kk >= 0.0 && kk < C.ns[d]) ? static_cast<int>(kk) : C.ns[d];
+      if (2 * k + 1 >= C.ns[d]) {  // the whole axis, each bin once
+        lo[d] = -bi[d];
+        hi[d] = C.ns[d] - 1 - bi[d];
+      } else if (C.periodic[d]) {
+        lo[d] = -k;
+        hi[d] = k;
+      } else {
+        lo[d] = bi[d] - k < 0 ? -bi[d] : -k;
+        hi[d] = bi[d] + k >= C.ns[d] ? C.ns[d] - 1 - bi[d] : k;
+      }
+    }
+    const double c2 = C.hz_c + C.hz_c;
+    for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
+      for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
+        for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
+          const int oo[3] = {o0, o1, o2};
+          int b = 0;
+          for (int d = 0; d < D; ++d) {
+            int v = bi[d] + oo[d];
+            if (v < 0) v += C.ns[d];
+            if (v >= C.ns[d]) v -= C.ns[d];
+            b = b * C.ns[d] + v;
+          }
+          const int e0 = start[b], e1 = start[b + 1];
+          for (int q = e0; q < e1; ++q) {
+            const int j = list[q];
+            if (j == i) continue;
+            double rij[3] = {0, 0, 0};
+            double r2 = 0.0;
+            for (int d = 0; d < D; ++d) {
+              double dd = S.x[d * cap + j] - xi[d];
+              if (C.periodic[d]) dd -= static_cast<double>(nint(dd / C.box[d])) * C.box[d];
+              rij[d] = dd;
+              r2 += dd * dd;
+            }
+            const double sj = S.sig[j];
+            const double r = sqrt(r2);
+            if (!(r <= (si + sj) / 2) || r == 0.0) continue;
+            // the pair's first cell is the one of lower index (the contact length is not
+            // symmetric in the two diameters)
+            const double sa = i < j ? si : sj, sb = i < j ? sj : si;
+            const double h = fmax((si + sj) / 2 - r, 0.0);
+            const double fel = pow(h, 1.5) / (0.75 * c2 * sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
+            double A, vol;
+            if (D == 3) {
+              A = contact_area(r, sa, sb);
+              vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+            } else {
+              A = contact_length(sa, sb, h);
+              vol = A;
+            }
+            const double f0 = -fel + C.adhesion * A;
+            if (vol != 0.0) pres -= f0 / vol;
+            for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
+          }
+        }
+  }
+  // ---- position update with the pressure-dependent friction (CIL.cu:902-939)
+  const double pnd = pres / C.p0;
+  const double temp = C.dt * 1 / ((C.zeta + C.zeta_p * pow(pnd, C.zeta_p_beta)) * area_of(si));
+  bool finite = true;
+  for (int d = 0; d < D; ++d) {
+    finite = finite && isfinite(F[d]);
+    const double t = xi[d] + temp * F[d];
+    x_out[d * cap + i] = C.periodic[d] ? wrap(t, C.box[d]) : t;
+    S.v[d * cap + i] = F[d] * (temp / C.dt);
+    if (frc) frc[d * cap + i] = F[d];
+  }
+  S.p[i] = pres;
+  if (!finite) atomicOr(&cnt->err, kErrNonFinite);
+}
+
+// ---------------------------------------------------------------- cell cycle and divisions
+__global__ void __launch_bounds__(kTile) k_cy_cycle(CyConst C, CySet S, CyCounters *cnt, const int *ts_dev,
+                                                    int *flag, int *block_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  const int ts = *ts_dev;
+  int div = 0;
+  if (i < n) {
+    // cellTPressure (CIL.cu:493-494): every cell is in the dividing state when the species divides
+    if (!C.divide || S.p[i] < C.apop_pressure)
+      S.tp[i] = 0;
+    else
+      S.tp[i] += 1;
+    if (C.divide) {
+      const double shift = C.p_shift * exp(-ts * C.p_shift_tau_inv);
+      const double pnd = fmax(0., S.p[i] + shift) / C.p0;
+      const double om = S.om[i];
+      double rho = S.rho[i];
+      S.theta[i] += om * fmin(C.r_maxed_inv * rho, 1.0);
+      const bool d3 = C.D == 3;
+      double vt = d3 ? volume_of(S.sigt[i]) : area_of(S.sigt[i]);
+      double v = d3 ? volume_of(S.sig[i]) : area_of(S.sig[i]);
+      const double c0 = om * kLn2 + (C.v1 - 1) / C.tau_v;
+      const double vt_prime = c0 * rho - (((vt - C.v_s) / C.v_s) / C.tau_v);
+      vt += vt_prime * vt;
+      const double v_prime = -(v - (vt / (1 + C.beta_vs * (C.osm + pnd)))) / C.tau_p;
+      v += v_prime;
+      v = C.tau_p == 0 ? vt : v;
+      S.sigt[i] = d3 ? sigma_of_volume(vt) : sigma_of_area(vt);
+      S.sig[i] = d3 ? sigma_of_volume(v) : sigma_of_area(v);
+      const double r_np = (1 - rho - pnd);
+      const double tau_r_pre = r_np > 0 ? 1 : C.rho_ratio;
+      const double r_prime = r_np / (C.tau_r * tau_r_pre);
+      rho += r_prime * rho;
+      S.rho[i] = rho;
+      div = S.theta[i] >= 1 ? 1 : 0;
+    }
+    flag[i] = div;
+  }
+  int tot;
+  block_excl_scan(div, &tot);
+  if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
+}
+
+__device__ inline void put_sigma_max(CyCounters *cnt, double s) {
+  atomicMax(&cnt->sigma_max_bits, static_cast<unsigned long long>(__double_as_longlong(s)));
+}
+
+// Divisions in mother order: daughter of the k-th dividing cell at n + k (calculDivisionsSingle,
+// CIL.cu:527-600; singleCellDivision, MD.cu:664-718).
+__global__ void __launch_bounds__(kTile) k_cy_divide(CyConst C, CySet S, CyCounters *cnt, const int *ts_dev,
+                                                     const int *flag, const int *block_start, int n_blocks) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  const int ts = *ts_dev;
+  const int f = (i < n) ? flag[i] : 0;
+  int tot;
+  const int rank = block_start[blockIdx.x] + block_excl_scan(f, &tot);
+  const size_t cap = C.capacity;
+  if (i < n) put_sigma_max(cnt, S.sig[i]);
+  if (f) {
+    const int inew = n + rank;
+    if (inew >= C.capacity) {
+      atomicOr(&cnt->err, kErrCapacity);
+    } else {
+      const int D = C.D;
+      const double lmom = S.sig[i];
+      double ldau, newsig;
+      double dr[3] = {0, 0, 0};
+      const u32x4 r0 = draw(C, i, ts, kCyDiv, 0);
+      if (D == 2) {
+        ldau = lmom / sqrt(2.0);
+        newsig = ldau;
+        const double rr = (lmom - ldau) / 2;
+        const double alpha = u53(r0.v[0], r0.v[1]) * 6.283185307179586;
+        dr[0] = rr * sin(alpha);
+        dr[1] = rr * cos(alpha);
+      } else {
+        const double rmom = lmom / 2;
+        const double vmom = 4 * kPi * rmom * rmom * rmom / 3;
+        const double a = 9 * lmom / 4;
+        const double b = -(3 * (lmom * lmom) / 2);
+        const double c = lmom * lmom * lmom / 4 - 3 * vmom / (kPi);
+        ldau = (-b + sqrt(b * b - 4 * a * c)) / (2 * a);
+        newsig = ldau;
+        const double rr = (lmom - ldau) / 2;
+        const double alpha = u53(r0.v[0], r0.v[1]) * 6.283185307179586;
+        const double beta = u53(r0.v[2], r0.v[3]) * 6.283185307179586;
+        dr[0] = rr * sin(alpha) * cos(beta);
+        dr[1] = rr * sin(alpha) * sin(beta);
+        dr[2] = rr * cos(alpha);
+      }
+      for (int d = 0; d < D; ++d) {
+        const double m = S.x[d * cap + i];
+        double xd = m + dr[d], xm = m + (-dr[d]);
+        if (C.periodic[d]) {
+          xd = wrap(xd, C.box[d]);
+          xm = wrap(xm, C.box[d]);
+        }
+        S.x[d * cap + inew] = xd;
+        S.x[d * cap + i] = xm;
+        S.v[d * cap + inew] = 0.0;
+        S.v[d * cap + i] = 0.0;
+      }
+      // cycle times: migration spans (daughter, then mother), log-normal cycle speeds (mother,
+      // then daughter), as the reference draws them
+      double z0, z1, z2, z3;
+      normal2(draw(C, i, ts, kCyDiv, 1), &z0, &z1);
+      normal2(draw(C, i, ts, kCyDiv, 2), &z2, &z3);
+      S.tsw[inew] = ts + span_steps(C.tau_mig_mu + C.tau_mig_sigma * z0, C.dt);
+      S.tsw[i] = ts + span_steps(C.tau_mig_mu + C.tau_mig_sigma * z1, C.dt);
+      S.om[i] = 1.0 / span_steps(lognormal(C.tau_div_mu, C.tau_div_sigma, z2), C.dt);
+      S.om[inew] = 1.0 / span_steps(lognormal(C.tau_div_mu, C.tau_div_sigma, z3), C.dt);
+      S.sig[inew] = newsig;
+      S.sig[i] = newsig;
+      S.sigt[inew] = newsig;
+      S.sigt[i] = newsig;
+      S.t0[inew] = ts;
+      S.t0[i] = ts;
+      S.theta[i] = 0;
+      S.theta[inew] = 0;
+      S.p[inew] = S.p[i];
+      S.rho[inew] = S.rho[i];
+      S.tp[inew] = -1;  // an unused slot of the reference's arrays (Colony.cpp:253)
+    }
+  }
+}
+
+__global__ void k_cy_commit_divisions(CyCounters *cnt, const int *block_start, int n_blocks, int capacity) {
+  const int nd = block_start[n_blocks];
+  const int room = capacity - cnt->n;
+  const int add = nd < room ? nd : (room > 0 ? room : 0);
+  cnt->n += add;
+  cnt->ndiv_total += add;
+  cnt->ndiv_step = add;
+}
+
+__global__ void k_cy_reset_smax(CyCounters *cnt) { cnt->sigma_max_bits = 0ull; }
+
+__global__ void k_cy_advance(int *ts) { *ts += 1; }
+
+// ---------------------------------------------------------------- removals
+// mode 1: apoptosis (CyclePressure or PressureTime law); mode 2: outside the box (drain)
+__global__ void __launch_bounds__(kTile) k_cy_mark(CyConst C, CySet S, CyCounters *cnt, const int *ts_dev,
+                                                   int mode, int *keep, int *block_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  int k = 0;
+  if (i < n) {
+    k = 1;
+    if (mode == 1) {
+      const int ts = *ts_dev;
+      const u32x4 r = draw(C, i, ts, kCyApo, 0);
+      const double u = u53(r.v[0], r.v[1]);
+      if (C.apoptosis == CIL_APOP_CYCLE_PRESSURE) {
+        const double p = S.p[i];
+        const double rate = C.apop_rate_step * pow((1 - (S.rho[i] / C.apop_pressure)), C.apop_duration) *
+                            pow(p / (p + C.p0), C.extr_gamma);
+        if (u <= rate) k = 0;
+      } else {
+        if (((C.apop_duration > 0) && (S.tp[i] >= C.apop_steps)) || ((C.apop_rate_step > 0) && (u <= C.apop_rate_step)))
+          k = 0;
+      }
+    } else {
+      for (int d = 0; d < C.D; ++d) {
+        const double x = S.x[static_cast<size_t>(d) * C.capacity + i];
+        if (!(x >= 0.0 && x < C.box[d])) k = 0;
+      }
+    }
+    keep[i] = k;
+  }
+  int tot;
+  block_excl_scan(k, &tot);
+  if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kTile) k_cy_compact(CyConst C, CySet A, CySet B, const CyCounters *cnt,
+                                                      const int *keep, const int *block_start) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  const int k = (i < n) ? keep[i] : 0;
+  int tot;
+  const int dst = block_start[blockIdx.x] + block_excl_scan(k, &tot);
+  if (!k) return;
+  const size_t cap = C.capacity;
+  for (int d = 0; d < C.D; ++d) {
+    B.x[d * cap + dst] = A.x[d * cap + i];
+    B.v[d * cap + dst] = A.v[d * cap + i];
+  }
+  B.sig[dst] = A.sig[i];
+  B.sigt[dst] = A.sigt[i];
+  B.theta[dst] = A.theta[i];
+  B.rho[dst] = A.rho[i];
+  B.om[dst] = A.om[i];
+  B.p[dst] = A.p[i];
+  B.tp[dst] = A.tp[i];
+  B.t0[dst] = A.t0[i];
+  B.tsw[dst] = A.tsw[i];
+}
+
+__global__ void k_cy_commit_removals(CyCounters *cnt, const int *block_start, int n_blocks, int mode) {
+  const int kept = block_start[n_blocks];
+  const int removed = cnt->n - kept;
+  cnt->n = kept;
+  cnt->nrem_step = removed;
+  if (mode == 1) cnt->napo_total += removed;
+}
+
+// ---------------------------------------------------------------- initial cell status
+// initializeCellStatus (CIL.cuh:253-330) for single-element cells, counter-based draws
+__global__ void k_cy_init_status(CyConst C, CySet S, const CyCounters *cnt, int ts, int fill_sigma, int fill_cycle) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt->n) return;
+  if (fill_sigma) {
+    S.sig[i] = C.sigma_core;
+    S.sigt[i] = C.sigma_core;
+  }
+  S.tp[i] = 0;
+  S.t0[i] = 0;
+  if (!fill_cycle) return;
+  S.tsw[i] = -1;
+  S.rho[i] = 1;
+  if (!C.divide) {
+    S.theta[i] = 0;
+    S.om[i] = 0;
+    return;
+  }
+  // every cell starts in the dividing state (the migration probability is 0): a cycle length
+  // max(Nint(N(tau_div) / dt), 1), the phase U[0, 1), and the elapsed part of the span
+  const u32x4 r0 = draw(C, i, ts, kCyInit, 0);
+  double z0, z1;
+  normal2(draw(C, i, ts, kCyInit, 1), &z0, &z1);
+  int span = span_steps(C.tau_div_mu + C.tau_div_sigma * z0, C.dt);
+  S.om[i] = 1.0 / span;
+  S.theta[i] = u53(r0.v[2], r0.v[3]);
+  const u32x4 r2 = draw(C, i, ts, kCyInit, 2);
+  span -= nint(u53(r2.v[0], r2.v[1]) * static_cast<double>(span)) - 1;
+  S.tsw[i] = S.t0[i] + span;
+}
+
+__global__ void k_cy_sigma_max(CyConst C, CySet S, CyCounters *cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cnt->n) put_sigma_max(cnt, S.sig[i]);
+}
+
+}  // namespace
+
+// ================================================================ host side
+struct cil_cycle {
+  cil_cycle_params p{};
+  CyConst C{};
+  int device = 0;
+  int cap = 0;
+  cudaStream_t stream = nullptr;
+  CySet set[2] = {};
+  int cur = 0;
+  double *xs = nullptr;   // position output buffer of the force pass
+  double *frc = nullptr;  // last forces (output only)
+  CyCounters *cnt = nullptr;
+  CyCounters *h_cnt = nullptr;  // pinned
+  int *ts_dev = nullptr;
+  int *key = nullptr, *bcount = nullptr, *bstart = nullptr, *cursor = nullptr, *list = nullptr, *part = nullptr;
+  int *flag = nullptr, *blk = nullptr;
+  int nbins = 0, nparts = 0, nblocks = 0;
+  int64_t ts = 0;
+  bool uploaded = false;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  double t_total = 0.0;
+  int64_t launches = 0;
+  std::string err;
+  std::vector<void *> allocs;
+
+  template <typename T>
+  T *alloc(size_t n) {
+    void *q = nullptr;
+    if (cudaMalloc(&q, n * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    allocs.push_back(q);
+    return static_cast<T *>(q);
+  }
+  cil_status fail(cil_status s, const std::string &m) {
+    err = m;
+    return s;
+  }
+};
+
+#define CY_TRY(h, call)                                                                      \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return (h)->fail(CIL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+namespace {
+
+cil_status check_params(const cil_cycle_params *p) {
+  if (p->dim != 2 && p->dim != 3) return CIL_ERR_CONFIG;
+  if (!(p->dt > 0.0) || !(p->sigma_core > 0.0) || !(p->E > 0.0) || !(p->zeta > 0.0)) return CIL_ERR_CONFIG;
+  for (int d = 0; d < p->dim; ++d)
+    if (!(p->box[d] > 0.0)) return CIL_ERR_CONFIG;
+  if (p->apoptosis < CIL_APOP_NONE || p->apoptosis > CIL_APOP_PRESSURE_TIME) return CIL_ERR_CONFIG;
+  if (p->divide && (!(p->tau_div_mu > 0.0) || !(p->cycle_p0 != 0.0) || !(p->cycle_sigma_min > 0.0) ||
+                    !(p->cycle_tau_r > 0.0) || !(p->cycle_tau_v > 0.0)))
+    return CIL_ERR_CONFIG;
+  // a migration time (crawling state) takes cells out of the single-element cycle for good in
+  // the reference (initializeCellStatus with calculDivisionsSingle); the shipped runs use 0
+  if (p->divide && p->tau_mig_mu != 0.0) return CIL_ERR_CONFIG;
+  return CIL_OK;
+}
+
+int blocks_for(int n) { return n > 0 ? (n + kTile - 1) / kTile : 1; }
+
+// scan of count[0..m) into start[0..m] (start[m] = total)
+void scan_into(cil_cycle *h, const int *count, int m, int *start) {
+  const int nchunks = m / kScanTile + 1;  // covers index m
+  k_cy_chunk_sums<<<nchunks, kTile, 0, h->stream>>>(count, m, h->part);
+  k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->part, nchunks);
+  k_cy_chunk_apply<<<nchunks, kTile, 0, h->stream>>>(count, m, h->part, start);
+  h->launches += 3;
+}
+
+cil_status bin_cells(cil_cycle *h) {
+  const CySet &S = h->set[h->cur];
+  const int g = blocks_for(h->cap);
+  k_cy_clear<<<256, kTile, 0, h->stream>>>(h->bcount, h->nbins);
+  k_cy_keys<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->key, h->bcount);
+  scan_into(h, h->bcount, h->nbins, h->bstart);
+  k_cy_clear<<<256, kTile, 0, h->stream>>>(h->cursor, h->nbins);
+  k_cy_scatter<<<g, kTile, 0, h->stream>>>(h->cnt, h->key, h->bstart, h->cursor, h->list);
+  k_cy_sort<<<blocks_for(h->nbins), kTile, 0, h->stream>>>(h->bstart, h->nbins, h->list, h->cnt);
+  h->launches += 5;
+  return CIL_OK;
+}
+
+cil_status removals(cil_cycle *h, int mode) {
+  const int g = blocks_for(h->cap);
+  CySet &A = h->set[h->cur];
+  CySet &B = h->set[1 - h->cur];
+  k_cy_mark<<<g, kTile, 0, h->stream>>>(h->C, A, h->cnt, h->ts_dev, mode, h->flag, h->blk);
+  k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
+  k_cy_compact<<<g, kTile, 0, h->stream>>>(h->C, A, B, h->cnt, h->flag, h->blk);
+  k_cy_commit_removals<<<1, 1, 0, h->stream>>>(h->cnt, h->blk, g, mode);
+  h->launches += 4;
+  h->cur = 1 - h->cur;
+  return CIL_OK;
+}
+
+cil_status enqueue_step(cil_cycle *h) {
+  bin_cells(h);
+  const int g = blocks_for(h->cap);
+  CySet &S = h->set[h->cur];
+  k_cy_force<<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
+  std::swap(S.x, h->xs);
+  k_cy_advance<<<1, 1, 0, h->stream>>>(h->ts_dev);
+  h->ts += 1;
+  h->launches += 2;
+  if (h->C.divide) {
+    k_cy_cycle<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk);
+    k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
+    k_cy_reset_smax<<<1, 1, 0, h->stream>>>(h->cnt);
+    k_cy_divide<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk, g);
+    k_cy_commit_divisions<<<1, 1, 0, h->stream>>>(h->cnt, h->blk, g, h->cap);
+    h->launches += 5;
+  }
+  if (h->C.apoptosis != CIL_APOP_NONE) removals(h, 1);
+  CY_TRY(h, cudaGetLastError());
+  return CIL_OK;
+}
+
+cil_status read_counters(cil_cycle *h) {
+  CY_TRY(h, cudaMemcpyAsync(h->h_cnt, h->cnt, sizeof(CyCounters), cudaMemcpyDeviceToHost, h->stream));
+  CY_TRY(h, cudaStreamSynchronize(h->stream));
+  if (h->h_cnt->err & kErrNonFinite) return h->fail(CIL_ERR_NAN, "non-finite force");
+  if (h->h_cnt->err & kErrCapacity) return h->fail(CIL_ERR_CAPACITY, "cell capacity exceeded");
+  if (h->h_cnt->err & kErrOutOfBox) return h->fail(CIL_ERR_OUT_OF_BOX, "Particle outside domain!");
+  if (h->h_cnt->err & kErrCrowded) return h->fail(CIL_ERR_CAPACITY, "more than 256 cells in one bin (overlapping cells)");
+  return CIL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_t seed, int32_t device,
+                            cil_cycle **out) {
+  if (!p || !out || capacity <= 0) return CIL_ERR_CONFIG;
+  *out = nullptr;
+  if (check_params(p) != CIL_OK) return CIL_ERR_CONFIG;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return CIL_ERR_CUDA;
+  }
+  cil_cycle *h = new cil_cycle();
+  h->p = *p;
+  h->device = device;
+  h->cap = capacity;
+  CyConst &C = h->C;
+  C.D = p->dim;
+  C.capacity = capacity;
+  C.dt = p->dt;
+  for (int d = 0; d < 3; ++d) {
+    C.periodic[d] = d < p->dim ? p->periodic[d] : 0;
+    C.box[d] = d < p->dim ? p->box[d] : 1.0;
+  }
+  // bins: width at least the diameter of a new cell (the search widens as cells grow)
+  h->nbins = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < p->dim) {
+      int ns = static_cast<int>(C.box[d] / p->sigma_core);
+      ns = ns < 1 ? 1 : (ns > 4096 ? 4096 : ns);
+      C.ns[d] = ns;
+      C.bw[d] = C.box[d] / ns;
+      C.inv_bw[d] = ns / C.box[d];
+    } else {
+      C.ns[d] = 1;
+      C.bw[d] = 1.0;
+      C.inv_bw[d] = 1.0;
+    }
+    h->nbins *= C.ns[d];
+  }
+  C.sigma_core = p->sigma_core;
+  C.hz_c = (1 - p->nu * p->nu) / p->E;
+  C.adhesion = p->adhesion;
+  C.motility = p->motility;
+  C.zeta = p->zeta;
+  C.zeta_p = p->zeta_p;
+  C.zeta_p_beta = p->zeta_p_beta;
+  C.noise_amp = p->noise_D > 0.0 ? std::sqrt(2.0 * p->noise_D) * (1.0 / std::sqrt(p->dt)) : 0.0;
+  C.divide = p->divide;
+  C.apoptosis = p->apoptosis;
+  C.tau_div_mu = p->tau_div_mu;
+  C.tau_div_sigma = p->tau_div_sigma;
+  C.tau_mig_mu = p->tau_mig_mu;
+  C.tau_mig_sigma = p->tau_mig_sigma;
+  // cycle times in steps (Input.cpp:176-178, CIL.cuh:225-233)
+  C.v1 = p->v1;
+  C.tau_r = p->cycle_tau_r * p->tau_div_mu / p->dt;
+  C.tau_v = p->cycle_tau_v * p->tau_div_mu / p->dt;
+  C.tau_p = p->cycle_tau_p * p->tau_div_mu / p->dt;
+  {
+    const double r = p->cycle_sigma_min / 2;
+    C.v_s = p->dim == 3 ? 4 * kPi * (r * r * r) / 3 : kPi * (r * r);  // Sigma2Volume / Sigma2Area
+  }
+  C.p0 = p->cycle_p0;
+  C.beta_vs = p->cycle_beta_vs;
+  C.rho_ratio = p->cycle_rho_ratio;
+  C.r_maxed_inv = p->cycle_r_maxed > 0.0 ? 1.0 / p->cycle_r_maxed : 1.0;
+  C.p_shift = p->cycle_p_shift * p->cycle_p0;
+  C.p_shift_tau_inv = p->cycle_p_shift_tau > 0.0 ? 1.0 / (p->cycle_p_shift_tau * p->tau_div_mu) * p->dt : 0.0;
+  C.osm = p->osmotic_pressure;
+  C.apop_pressure = p->apop_pressure;
+  C.apop_duration = p->apop_duration;
+  C.apop_rate_step = p->apop_rate * p->dt;
+  C.extr_gamma = p->extr_gamma;
+  C.apop_steps = p->apop_duration / p->dt;
+  C.seed_lo = static_cast<uint32_t>(seed);
+  C.seed_hi = static_cast<uint32_t>(seed >> 32);
+
+  const size_t cap = capacity, D = p->dim;
+  bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreate(&h->ev[0]) == cudaSuccess && cudaEventCreate(&h->ev[1]) == cudaSuccess;
+  for (int s = 0; ok && s < 2; ++s) {
+    CySet &S = h->set[s];
+    S.x = h->alloc<double>(D * cap);
+    S.v = h->alloc<double>(D * cap);
+    S.sig = h->alloc<double>(cap);
+    S.sigt = h->alloc<double>(cap);
+    S.theta = h->alloc<double>(cap);
+    S.rho = h->alloc<double>(cap);
+    S.om = h->alloc<double>(cap);
+    S.p = h->alloc<double>(cap);
+    S.tp = h->alloc<int>(cap);
+    S.t0 = h->alloc<int>(cap);
+    S.tsw = h->alloc<int>(cap);
+    ok = S.x && S.v && S.sig && S.sigt && S.theta && S.rho && S.om && S.p && S.tp && S.t0 && S.tsw;
+  }
+  h->nblocks = blocks_for(capacity);
+  h->nparts = (h->nbins + kScanTile - 1) / kScanTile + 1;
+  if (ok) {
+    h->xs = h->alloc<double>(D * cap);
+    h->frc = h->alloc<double>(D * cap);
+    h->cnt = h->alloc<CyCounters>(1);
+    h->ts_dev = h->alloc<int>(1);
+    h->key = h->alloc<int>(cap);
+    h->bcount = h->alloc<int>(h->nbins + 1);
+    h->bstart = h->alloc<int>(h->nbins + 1);
+    h->cursor = h->alloc<int>(h->nbins + 1);
+    h->list = h->alloc<int>(cap);
+    h->part = h->alloc<int>(h->nparts + 1);
+    h->flag = h->alloc<int>(cap);
+    h->blk = h->alloc<int>(h->nblocks + 1);
+    ok = h->xs && h->frc && h->cnt && h->ts_dev && h->key && h->bcount && h->bstart && h->cursor && h->list &&
+         h->part && h->flag && h->blk &&
+         cudaHostAlloc(&h->h_cnt, sizeof(CyCounters), cudaHostAllocDefault) == cudaSuccess;
+  }
+  if (ok) ok = cudaMemsetAsync(h->cnt, 0, sizeof(CyCounters), h->stream) == cudaSuccess &&
+               cudaMemsetAsync(h->ts_dev, 0, sizeof(int), h->stream) == cudaSuccess &&
+               cudaStreamSynchronize(h->stream) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    cil_cycle_destroy(h);
+    return CIL_ERR_CUDA;
+  }
+  *out = h;
+  return CIL_OK;
+}
+
+void cil_cycle_destroy(cil_cycle *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void *q : h->allocs) cudaFree(q);
+  if (h->h_cnt) cudaFreeHost(h->h_cnt);
+  for (auto e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+cil_status cil_cycle_upload(cil_cycle *h, const cil_cycle_view *v) {
+  if (!h || !v || !v->pos) return CIL_ERR_CONFIG;
+  if (v->ncells < 0 || v->ncells > h->cap) return h->fail(CIL_ERR_CAPACITY, "cil_cycle_upload: more cells than the capacity");
+  CY_TRY(h, cudaSetDevice(h->device));
+  const int n = v->ncells, D = h->C.D;
+  const size_t cap = h->cap;
+  h->cur = 0;
+  CySet &S = h->set[0];
+  std::vector<double> t(static_cast<size_t>(n));
+  for (int d = 0; d < D; ++d) {
+    for (int i = 0; i < n; ++i) {
+      const double x = v->pos[static_cast<size_t>(i) * D + d];
+      if (!(x >= 0.0 && x < h->C.box[d])) return h->fail(CIL_ERR_OUT_OF_BOX, "Input Positions Out of Bounds!");
+      t[i] = x;
+    }
+    CY_TRY(h, cudaMemcpy(S.x + d * cap, t.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    CY_TRY(h, cudaMemset(S.v + d * cap, 0, sizeof(double) * cap));
+  }
+  auto up = [&](double *dst, const double *src) -> cudaError_t {
+    return src ? cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
+  CY_TRY(h, up(S.sig, v->sigma));
+  CY_TRY(h, up(S.sigt, v->sigma_t ? v->sigma_t : v->sigma));
+  CY_TRY(h, up(S.theta, v->theta));
+  CY_TRY(h, up(S.rho, v->rho));
+  CY_TRY(h, up(S.om, v->angvel));
+  CY_TRY(h, cudaMemset(S.p, 0, sizeof(double) * cap));
+  if (v->pressure) CY_TRY(h, up(S.p, v->pressure));
+  CyCounters c{};
+  c.n = n;
+  CY_TRY(h, cudaMemcpy(h->cnt, &c, sizeof(c), cudaMemcpyHostToDevice));
+  const int ts = v->ts;
+  CY_TRY(h, cudaMemcpy(h->ts_dev, &ts, sizeof(int), cudaMemcpyHostToDevice));
+  h->ts = ts;
+  const int fill_sigma = v->sigma ? 0 : 1;
+  const int fill_cycle = (v->theta && v->rho && v->angvel) ? 0 : 1;
+  k_cy_init_status<<<blocks_for(h->cap), kTile, 0, h->stream>>>(h->C, S, h->cnt, ts, fill_sigma, fill_cycle);
+  if (v->tpressure) {
+    CY_TRY(h, cudaStreamSynchronize(h->stream));
+    CY_TRY(h, cudaMemcpy(S.tp, v->tpressure, sizeof(int) * n, cudaMemcpyHostToDevice));
+  }
+  k_cy_sigma_max<<<blocks_for(h->cap), kTile, 0, h->stream>>>(h->C, S, h->cnt);
+  CY_TRY(h, cudaGetLastError());
+  CY_TRY(h, cudaStreamSynchronize(h->stream));
+  h->uploaded = true;
+  return CIL_OK;
+}
+
+cil_status cil_cycle_step(cil_cycle *h, int32_t nsteps, int64_t *ts) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (!h->uploaded) return h->fail(CIL_ERR_STATE, "cil_cycle_step before cil_cycle_upload");
+  if (nsteps < 0) return h->fail(CIL_ERR_CONFIG, "negative step count");
+  CY_TRY(h, cudaSetDevice(h->device));
+  h->launches = 0;
+  CY_TRY(h, cudaEventRecord(h->ev[0], h->stream));
+  for (int k = 0; k < nsteps; ++k) {
+    const cil_status st = enqueue_step(h);
+    if (st != CIL_OK) return st;
+  }
+  CY_TRY(h, cudaEventRecord(h->ev[1], h->stream));
+  const cil_status st = read_counters(h);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+  h->t_total = ms;
+  if (ts) *ts = h->ts;
+  return st;
+}
+
+cil_status cil_cycle_check_positions(cil_cycle *h) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (!h->uploaded) return h->fail(CIL_ERR_STATE, "not uploaded");
+  CY_TRY(h, cudaSetDevice(h->device));
+  if (h->p.drain) {
+    removals(h, 2);
+    CY_TRY(h, cudaGetLastError());
+    return read_counters(h);
+  }
+  // without drain any cell off the box is an error (run_assert, CIL.cu:956)
+  const int g = blocks_for(h->cap);
+  k_cy_mark<<<g, kTile, 0, h->stream>>>(h->C, h->set[h->cur], h->cnt, h->ts_dev, 2, h->flag, h->blk);
+  k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
+  CY_TRY(h, cudaGetLastError());
+  cil_status st = read_counters(h);
+  if (st != CIL_OK) return st;
+  int kept = 0;
+  CY_TRY(h, cudaMemcpy(&kept, h->blk + g, sizeof(int), cudaMemcpyDeviceToHost));
+  if (kept != h->h_cnt->n) return h->fail(CIL_ERR_OUT_OF_BOX, "Particle outside domain!");
+  return CIL_OK;
+}
+
+cil_status cil_cycle_download(cil_cycle *h, cil_cycle_view *v) {
+  if (!h || !v) return CIL_ERR_CONFIG;
+  CY_TRY(h, cudaSetDevice(h->device));
+  const cil_status st = read_counters(h);
+  const int n = h->h_cnt->n, D = h->C.D;
+  v->ncells = n;
+  v->ts = static_cast<int32_t>(h->ts);
+  if (n > v->capacity) return h->fail(CIL_ERR_CAPACITY, "cil_cycle_download: host arrays too small");
+  const CySet &S = h->set[h->cur];
+  const size_t cap = h->cap;
+  std::vector<double> t(static_cast<size_t>(n) * D);
+  auto vec = [&](double *dst, const double *src) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    for (int d = 0; d < D; ++d) {
+      const cudaError_t e = cudaMemcpy(t.data() + static_cast<size_t>(d) * n, src + d * cap, sizeof(double) * n,
+                                       cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return e;
+    }
+    for (int i = 0; i < n; ++i)
+      for (int d = 0; d < D; ++d) dst[static_cast<size_t>(i) * D + d] = t[static_cast<size_t>(d) * n + i];
+    return cudaSuccess;
+  };
+  auto sca = [&](void *dst, const void *src, size_t es) -> cudaError_t {
+    return dst ? cudaMemcpy(dst, src, es * n, cudaMemcpyDeviceToHost) : cudaSuccess;
+  };
+  CY_TRY(h, vec(v->pos, S.x));
+  CY_TRY(h, vec(v->vel, S.v));
+  CY_TRY(h, sca(v->sigma, S.sig, sizeof(double)));
+  CY_TRY(h, sca(v->sigma_t, S.sigt, sizeof(double)));
+  CY_TRY(h, sca(v->theta, S.theta, sizeof(double)));
+  CY_TRY(h, sca(v->rho, S.rho, sizeof(double)));
+  CY_TRY(h, sca(v->angvel, S.om, sizeof(double)));
+  CY_TRY(h, sca(v->pressure, S.p, sizeof(double)));
+  CY_TRY(h, sca(v->tpressure, S.tp, sizeof(int)));
+  return st;
+}
+
+cil_status cil_cycle_timings(cil_cycle *h, double *total_ms, int64_t *launches) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (total_ms) *total_ms = h->t_total;
+  if (launches) *launches = h->launches;
+  return CIL_OK;
+}
+
+void cil_cycle_last_error(const cil_cycle *h, char *buf, size_t len) {
+  if (!buf || len == 0) return;
+  snprintf(buf, len, "%s", h ? h->err.c_str() : "");
+}
+
+}  // extern "C"

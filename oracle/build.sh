@@ -6,5 +6,5 @@ set -euo pipefail
 HERE=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$HERE/_build"
 g++ -std=c++17 -O2 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared \
-    -o "$HERE/_build/liboracle.so" "$HERE/cil_oracle.cpp"
+    -o "$HERE/_build/liboracle.so" "$HERE/cil_oracle.cpp" "$HERE/cil_cycle_oracle.cpp"
 echo "built $HERE/_build/liboracle.so"

@@ -243,3 +243,71 @@ def bins_as_sets(head: np.ndarray, lst: np.ndarray) -> list:
             i = int(lst[i])
         out.append(s)
     return out
+
+
+class CycleOracle:
+    """The single-element cell-cycle model on the CPU (oracle/cil_cycle_oracle.cpp), with the
+    GPU model's counter-based draws. Test infrastructure."""
+
+    def __init__(self, params, capacity: int, seed: int):
+        from cil_cuda_gb300 import cycle_params
+        self.L = lib()
+        L = self.L
+        vp, i32, dp, ip = C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        L.cyo_create.restype = vp
+        L.cyo_create.argtypes = [vp, i32, C.c_uint64]
+        L.cyo_destroy.argtypes = [vp]
+        L.cyo_set_state.argtypes = [vp, i32, i32] + [dp] * 8 + [ip]
+        L.cyo_step.restype = i32
+        L.cyo_step.argtypes = [vp, i32]
+        L.cyo_check_positions.restype = i32
+        L.cyo_check_positions.argtypes = [vp]
+        L.cyo_num_cells.restype = i32
+        L.cyo_num_cells.argtypes = [vp]
+        L.cyo_get_state.argtypes = [vp] + [dp] * 8 + [ip, C.POINTER(C.c_int64)]
+        self.p = cycle_params(**params)
+        self.dim = self.p.dim
+        self.h = L.cyo_create(C.byref(self.p), capacity, seed)
+
+    def set_state(self, pos, sigma, theta, rho, angvel, sigma_t=None, vel=None, pressure=None, tpressure=None, ts=0):
+        def d(a):
+            return None if a is None else np.ascontiguousarray(a, np.float64)
+        arrs = [d(pos), d(vel), d(sigma), d(sigma_t), d(theta), d(rho), d(angvel), d(pressure)]
+        tp = None if tpressure is None else np.ascontiguousarray(tpressure, np.int32)
+        self._keep = (arrs, tp)
+        ptrs = [None if a is None else a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]
+        self.L.cyo_set_state(self.h, len(arrs[0]), ts, *ptrs,
+                             None if tp is None else tp.ctypes.data_as(C.POINTER(C.c_int32)))
+
+    def step(self, n: int) -> int:
+        return self.L.cyo_step(self.h, n)
+
+    def check_positions(self) -> int:
+        return self.L.cyo_check_positions(self.h)
+
+    def state(self) -> dict:
+        n = self.L.cyo_num_cells(self.h)
+        D = self.dim
+        a = {k: np.zeros(n) for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure")}
+        a["pos"] = np.zeros((n, D))
+        a["vel"] = np.zeros((n, D))
+        a["tpressure"] = np.zeros(n, np.int32)
+        counts = np.zeros(3, np.int64)
+        P = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+        self.L.cyo_get_state(self.h, P(a["pos"]), P(a["vel"]), P(a["sigma"]), P(a["sigma_t"]), P(a["theta"]),
+                             P(a["rho"]), P(a["angvel"]), P(a["pressure"]),
+                             a["tpressure"].ctypes.data_as(C.POINTER(C.c_int32)),
+                             counts.ctypes.data_as(C.POINTER(C.c_int64)))
+        a.update(ncells=n, ts=int(counts[0]), ndiv=int(counts[1]), napo=int(counts[2]))
+        return a
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cyo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

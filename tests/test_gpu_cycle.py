@@ -1,0 +1,150 @@
+"""The single-element cell-cycle model on the GPU (include/cil_cycle.h) against its CPU
+restatement (oracle/cil_cycle_oracle.cpp), which draws the same counter-based random numbers
+and sums the pair forces in the same order: cell counts, division and apoptosis events and
+the per-cell states must agree; the remaining differences are the last bits of libm (log,
+exp, pow, sin, cos) between the host and the device, so positions and cycle variables are
+compared at 1e-9 relative.
+
+The parameters are the shipped configurations' (Hertz contacts E = 100, nu = 0.5, adhesion
+0.2, CYCLE_P0 5, V1 15, TAU_DIVISION 1 +- 0.1) with a time step raised so that cells divide
+within a short test."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIG0 = 1.1283791670955126
+
+
+def colony(rng, n, box, dim=2, spread=0.0):
+    pos = rng.uniform(0, 1, size=(n, dim)) * np.asarray(box[:dim])
+    return dict(pos=pos, sigma=SIG0 * (1 + spread * rng.uniform(-1, 1, n)), theta=rng.uniform(0, 1, n),
+                rho=rng.uniform(0.5, 1.0, n), angvel=np.full(n, 2e-3) * rng.uniform(0.5, 1.5, n))
+
+
+def run_both(G, O, prm, st, steps, cap=20000, seed=11):
+    eng = G.CycleEngine(prm, cap, seed=seed)
+    eng.upload(**st)
+    eng.step(steps)
+    g = eng.download()
+    eng.close()
+    o = O.CycleOracle(prm, cap, seed)
+    o.set_state(**st)
+    assert o.step(steps) == 0
+    return g, o.state()
+
+
+def close(a, b, L=None, rel=1e-9):
+    d = np.asarray(a, float) - np.asarray(b, float)
+    if L is not None:
+        d = d - np.round(d / L) * L
+    scale = max(1.0, float(np.abs(b).max()) if np.size(b) else 1.0)
+    return float(np.abs(d).max()) <= rel * scale if np.size(d) else True
+
+
+def compare(g, s, box):
+    assert g["ncells"] == s["ncells"]
+    assert g["ts"] == s["ts"]
+    np.testing.assert_array_equal(g["tpressure"], s["tpressure"])
+    L = np.asarray(box[:g["pos"].shape[1]])
+    assert close(g["pos"], s["pos"], L)
+    for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure", "vel"):
+        assert close(g[k], s[k]), k
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cycle_model_matches_oracle(gpu_lib, oracle_lib, dim):
+    rng = np.random.default_rng(40 + dim)
+    box = [30.0, 30.0, 30.0] if dim == 2 else [12.0, 12.0, 12.0]
+    n = 500 if dim == 2 else 800
+    prm = dict(dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, zeta=0.01, noise_D=0.002, v1=15.0)
+    st = colony(rng, n, box, dim)
+    g, s = run_both(gpu_lib, oracle_lib, prm, st, 300)
+    assert s["ndiv"] > 20 and g["ncells"] == n + s["ndiv"]
+    compare(g, s, box)
+    assert np.all(np.isfinite(g["pressure"])) and np.abs(g["pressure"]).max() > 0
+
+
+@pytest.mark.parametrize("law", [1, 2])
+def test_apoptosis_laws_match_oracle(gpu_lib, oracle_lib, law):
+    rng = np.random.default_rng(50 + law)
+    box = [30.0, 30.0, 0.0]
+    prm = dict(box=box, dt=2e-4, motility=0.5, zeta=0.01, apoptosis=law, apop_rate=40.0, apop_pressure=1.5,
+               apop_duration=1.0, extr_gamma=0.5, cycle_p0=5.0)
+    if law == 2:
+        prm.update(apop_pressure=0.0, apop_duration=0.01)  # removal after 50 steps at non-negative pressure
+    st = colony(rng, 600, box)
+    g, s = run_both(gpu_lib, oracle_lib, prm, st, 120)
+    assert s["napo"] > 0
+    compare(g, s, box)
+
+
+def test_drain_removes_cells_off_the_open_axis(gpu_lib, oracle_lib):
+    """Ecoli_channel_2D.json's geometry: periodic x, open y, DRAIN on (checkPositions, CIL.cu:945-966)."""
+    G, O = gpu_lib, oracle_lib
+    rng = np.random.default_rng(61)
+    box = [5.0, 40.0, 0.0]
+    prm = dict(box=box, periodic=[1, 0, 0], dt=2e-4, motility=4.0, zeta=0.01, drain=1, zeta_p=0.01, zeta_p_beta=3.0)
+    st = colony(rng, 120, box)
+    st["pos"][:, 1] = rng.uniform(0.2, 1.0, 120)  # near the open lower edge, motility pushes some out
+    eng = G.CycleEngine(prm, 4000, seed=5)
+    eng.upload(**st)
+    o = O.CycleOracle(prm, 4000, 5)
+    o.set_state(**st)
+    removed = 0
+    for _ in range(4):
+        eng.step(50)
+        assert o.step(50) == 0
+        eng.check_positions()
+        removed += o.check_positions()
+        g = eng.download()
+        assert g["ncells"] == o.state()["ncells"]
+    s = o.state()
+    assert removed > 0
+    compare(g, s, box)
+    g2 = eng.download()
+    assert np.all(g2["pos"][:, 1] >= 0.0) and np.all(g2["pos"][:, 1] < 40.0)
+    eng.close()
+    # without drain a cell off the box is an error
+    prm["drain"] = 0
+    eng = G.CycleEngine(prm, 4000, seed=5)
+    eng.upload(**st)
+    eng.step(200)
+    with pytest.raises(G.CilError) as e:
+        eng.check_positions()
+    assert e.value.status == 5
+    eng.close()
+
+
+def test_initial_cell_status(gpu_lib):
+    """initializeCellStatus (CIL.cuh:253-330): sigma = SIGMA_CORE, rho = 1, theta uniform on
+    [0, 1), cycle speed 1 / max(Nint(N(1, 0.1) / dt), 1)."""
+    G = gpu_lib
+    rng = np.random.default_rng(7)
+    n = 20000
+    box = [400.0, 400.0, 0.0]
+    prm = dict(box=box, dt=1e-3)
+    eng = G.CycleEngine(prm, n, seed=3)
+    eng.upload(pos=rng.uniform(0, 400.0, size=(n, 2)))
+    s = eng.download()
+    eng.close()
+    assert np.all(s["sigma"] == SIG0) and np.all(s["sigma_t"] == SIG0) and np.all(s["rho"] == 1.0)
+    assert 0.0 <= s["theta"].min() and s["theta"].max() < 1.0 and abs(s["theta"].mean() - 0.5) < 0.01
+    span = 1.0 / s["angvel"]
+    assert np.allclose(span, np.round(span))
+    assert abs(span.mean() * 1e-3 - 1.0) < 0.005 and abs(span.std() * 1e-3 - 0.1) < 0.005
+
+
+def test_shipped_configuration_grows_from_one_cell(gpu_lib):
+    """PRX_MDCK_2D.json's model (HZ, adhesion 0.2, motility 1, V1 15, P0 5) from a single cell,
+    with dt raised to 2e-4: the colony doubles about once per cycle time and stays finite."""
+    G = gpu_lib
+    prm = dict(box=[100.0, 100.0, 0.0], dt=2e-4, motility=1.0, zeta=0.01, v1=15.0)
+    eng = G.CycleEngine(prm, 4096, seed=9)
+    eng.upload(pos=np.array([[50.0, 50.0]]), theta=np.array([0.0]), rho=np.array([1.0]),
+               angvel=np.array([2e-4]), sigma=np.array([SIG0]))
+    eng.step(25000)  # 5 cycle times
+    s = eng.download()
+    eng.close()
+    assert 16 <= s["ncells"] <= 64, s["ncells"]
+    assert np.all(np.isfinite(s["pos"])) and np.all(np.isfinite(s["sigma"]))
