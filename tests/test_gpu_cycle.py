@@ -6,8 +6,10 @@ exp, pow, sin, cos) between the host and the device, so positions and cycle vari
 compared at 1e-9 relative.
 
 The parameters are the shipped configurations' (Hertz contacts E = 100, nu = 0.5, adhesion
-0.2, CYCLE_P0 5, V1 15, TAU_DIVISION 1 +- 0.1) with a time step raised so that cells divide
-within a short test."""
+0.2, CYCLE_P0 5, V1 15, TAU_DIVISION 1 +- 0.1) with the time step raised 20x so that cells
+divide within a short test, and the friction raised with it (dt / zeta = 1e-3 as in
+PRX_MDCK_2D.json): with the shipped friction at this time step the random overlaps of the
+start are resolved so violently that the last-bit differences grow 14 % per step."""
 import numpy as np
 import pytest
 
@@ -56,8 +58,8 @@ def compare(g, s, box):
 def test_cycle_model_matches_oracle(gpu_lib, oracle_lib, dim):
     rng = np.random.default_rng(40 + dim)
     box = [30.0, 30.0, 30.0] if dim == 2 else [12.0, 12.0, 12.0]
-    n = 500 if dim == 2 else 800
-    prm = dict(dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, zeta=0.01, noise_D=0.002, v1=15.0)
+    n = 400 if dim == 2 else 700
+    prm = dict(dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, zeta=0.2, noise_D=0.002, v1=15.0)
     st = colony(rng, n, box, dim)
     g, s = run_both(gpu_lib, oracle_lib, prm, st, 300)
     assert s["ndiv"] > 20 and g["ncells"] == n + s["ndiv"]
@@ -69,7 +71,7 @@ def test_cycle_model_matches_oracle(gpu_lib, oracle_lib, dim):
 def test_apoptosis_laws_match_oracle(gpu_lib, oracle_lib, law):
     rng = np.random.default_rng(50 + law)
     box = [30.0, 30.0, 0.0]
-    prm = dict(box=box, dt=2e-4, motility=0.5, zeta=0.01, apoptosis=law, apop_rate=40.0, apop_pressure=1.5,
+    prm = dict(box=box, dt=2e-4, motility=0.5, zeta=0.2, apoptosis=law, apop_rate=40.0, apop_pressure=1.5,
                apop_duration=1.0, extr_gamma=0.5, cycle_p0=5.0)
     if law == 2:
         prm.update(apop_pressure=0.0, apop_duration=0.01)  # removal after 50 steps at non-negative pressure
@@ -84,9 +86,9 @@ def test_drain_removes_cells_off_the_open_axis(gpu_lib, oracle_lib):
     G, O = gpu_lib, oracle_lib
     rng = np.random.default_rng(61)
     box = [5.0, 40.0, 0.0]
-    prm = dict(box=box, periodic=[1, 0, 0], dt=2e-4, motility=4.0, zeta=0.01, drain=1, zeta_p=0.01, zeta_p_beta=3.0)
-    st = colony(rng, 120, box)
-    st["pos"][:, 1] = rng.uniform(0.2, 1.0, 120)  # near the open lower edge, motility pushes some out
+    prm = dict(box=box, periodic=[1, 0, 0], dt=2e-4, motility=20.0, zeta=0.2, drain=1, zeta_p=0.01, zeta_p_beta=3.0)
+    st = colony(rng, 40, box)
+    st["pos"][:, 1] = rng.uniform(0.3, 8.0, 40)  # near the open lower edge: the cells moving down leave
     eng = G.CycleEngine(prm, 4000, seed=5)
     eng.upload(**st)
     o = O.CycleOracle(prm, 4000, 5)
@@ -139,7 +141,7 @@ def test_shipped_configuration_grows_from_one_cell(gpu_lib):
     """PRX_MDCK_2D.json's model (HZ, adhesion 0.2, motility 1, V1 15, P0 5) from a single cell,
     with dt raised to 2e-4: the colony doubles about once per cycle time and stays finite."""
     G = gpu_lib
-    prm = dict(box=[100.0, 100.0, 0.0], dt=2e-4, motility=1.0, zeta=0.01, v1=15.0)
+    prm = dict(box=[100.0, 100.0, 0.0], dt=2e-4, motility=1.0, zeta=0.2, v1=15.0)
     eng = G.CycleEngine(prm, 4096, seed=9)
     eng.upload(pos=np.array([[50.0, 50.0]]), theta=np.array([0.0]), rho=np.array([1.0]),
                angvel=np.array([2e-4]), sigma=np.array([SIG0]))
