@@ -34,7 +34,8 @@ EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step
             "cil_frame_close", "cil_frame_get_stats", "cil_frame_last_error", "cil_input_load", "cil_input_config",
             "cil_input_initial_state", "cil_input_last_error", "cil_input_free", "cil_cycle_create",
             "cil_cycle_destroy", "cil_cycle_upload", "cil_cycle_step", "cil_cycle_check_positions",
-            "cil_cycle_download", "cil_cycle_timings", "cil_cycle_last_error"]
+            "cil_cycle_download", "cil_cycle_timings", "cil_cycle_last_error", "cil_input_elements",
+            "cil_input_cycle_config", "cil_input_cycle_initial_state"]
 
 
 class CilError(RuntimeError):
@@ -320,6 +321,12 @@ def lib():
         L.cil_input_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_input_free.restype = None
         L.cil_input_free.argtypes = [vp]
+        L.cil_input_elements.restype = i32
+        L.cil_input_elements.argtypes = [vp]
+        L.cil_input_cycle_config.restype = i32
+        L.cil_input_cycle_config.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.cil_input_cycle_initial_state.restype = i32
+        L.cil_input_cycle_initial_state.argtypes = [vp, C.c_void_p]
         L.cil_cycle_create.restype = i32
         L.cil_cycle_create.argtypes = [C.POINTER(CycleParams), i32, C.c_uint64, i32, C.POINTER(vp)]
         L.cil_cycle_destroy.restype = None
@@ -698,10 +705,18 @@ class RunInput:
             self.L.cil_input_last_error(h, buf, 1024)
             self.close()
             raise CilError(st, buf.value.decode())
-        cfg, prm, run = Config(), ColonyParams(), RunInfo()
-        self._check(self.L.cil_input_config(h, C.byref(cfg), C.byref(prm), C.byref(run)))
-        self.config = _struct_dict(cfg)
-        self.params = _struct_dict(prm)
+        self.elements = int(self.L.cil_input_elements(h))
+        run = RunInfo()
+        if self.elements == 1:  # single-element cells: the cell-cycle model (cil_cycle.h)
+            q = CycleParams()
+            self._check(self.L.cil_input_cycle_config(h, C.byref(q), C.byref(run)))
+            self.config = None
+            self.params = _struct_dict(q)
+        else:
+            cfg, prm = Config(), ColonyParams()
+            self._check(self.L.cil_input_config(h, C.byref(cfg), C.byref(prm), C.byref(run)))
+            self.config = _struct_dict(cfg)
+            self.params = _struct_dict(prm)
         self.run = _struct_dict(run)
 
     def _check(self, st: int):
@@ -720,6 +735,19 @@ class RunInput:
                        tswitch=_ip(tsw))
         self._check(self.L.cil_input_initial_state(self.h, C.byref(v)))
         return dict(pos=pos, sigma=sig, t0=t0, tswitch=tsw)
+
+    def cycle_initial_state(self) -> dict:
+        """INIT and the cell status of a single-element run (cil_input_cycle_initial_state)."""
+        n, D = self.run["ncells"], self.params["dim"]
+        a = {k: np.zeros(n) for k in ("sigma", "sigma_t", "theta", "rho", "angvel")}
+        a["pos"] = np.zeros((n, D))
+        v = CycleView(ncells=0, capacity=n, ts=0, pad=0, vel=None, pressure=None, tpressure=None,
+                      **{k: _dp(x) for k, x in a.items()})
+        self._check(self.L.cil_input_cycle_initial_state(self.h, C.byref(v)))
+        return a
+
+    def cycle_engine(self, device: int = 0) -> "CycleEngine":
+        return CycleEngine(self.params, self.run["capacity"], seed=self.run["seed"], device=device)
 
     def engine(self, device: int = 0, **over) -> Engine:
         """An Engine configured from the run description (keyword arguments override)."""

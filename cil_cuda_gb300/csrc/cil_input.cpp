@@ -31,6 +31,7 @@
 #include <utility>
 #include <vector>
 
+#include "cil_cycle.h"
 #include "cil_input.h"
 #include "host_rng.h"
 
@@ -378,10 +379,119 @@ struct cil_input {
   double tau_div[2] = {0, 0}, tau_mig[2] = {0, 0};
   std::string init_kind;
   int ncells = 0;
-  std::vector<double> json_pos;  // INIT JSON: [cell][2][dim]
+  std::vector<double> json_pos;  // INIT JSON: [cell][elements][dim]
+  // MD keys of either model
+  bool drain = false;
+  double osm = 0.0;
+  // single-element species: the cell-cycle model (cil_cycle.h)
+  int nelem = 2;
+  cil_cycle_params cyc{};
 };
 
 namespace {
+
+// INIT block of either model: RANDOM cell count, or JSON element positions (rows of DIM)
+void read_init(cil_input *in, const Node &root, const std::string &cell, int nelem) {
+  Node init = root.child("INIT").child(cell);
+  in->init_kind = init.pick("SELECT", {"JSON", "H5", "RANDOM"});
+  if (in->init_kind == "H5") key_error(init.path + ".SELECT", "H5 restart needs libhdf5, which this build does not have");
+  if (in->init_kind == "RANDOM") {
+    const int n = init.child("RANDOM").integer("NUMBER");
+    if (n < 0) key_error(init.path + ".RANDOM.NUMBER", "negative cell count");
+    in->ncells = n;
+    return;
+  }
+  Node jn{nullptr, ""};
+  const auto &rows = init.array("JSON", &jn);
+  if (rows.size() % nelem) key_error(jn.path, "element count is not a multiple of NELEM");
+  in->ncells = static_cast<int>(rows.size() / nelem);
+  in->json_pos.reserve(rows.size() * in->dim);
+  for (const auto &r : rows) {
+    if (r.kind != JVal::kArr || r.arr.size() != static_cast<size_t>(in->dim))
+      key_error(jn.path, "rows should be of size " + std::to_string(in->dim));
+    for (const auto &x : r.arr) {
+      if (x.kind != JVal::kNum) key_error(jn.path, "expected numbers");
+      in->json_pos.push_back(x.num);
+    }
+  }
+}
+
+// A single-element species: the cell-cycle model (readSpecs, Input.cpp:6-262, for NELEM 1)
+void read_single(cil_input *in, const Node &root, const Node &loc, const std::string &cell,
+                 const std::string &integrator, const std::string &pair) {
+  in->nelem = 1;
+  cil_cycle_params &q = in->cyc;
+  cil_run_info &run = in->run;
+  const auto enames = loc.strs("NAMES");
+  if (enames.size() != 1) key_error(loc.path + ".NAMES", "vector should be of size 1. Got " + std::to_string(enames.size()));
+  copy_str(run.elem_names[0], sizeof run.elem_names[0], enames[0]);
+  run.elem_names[1][0] = 0;
+  if (integrator == "STOCHASTIC_HEUN")
+    key_error("MD.INTEGRATOR.SELECT", "the single-element model runs EULER or STOCHASTIC_EULER");
+  if (pair != "HZ") key_error("INTERACTIONS.PAIRFORCES.SELECT", "the single-element model's contacts are the Hertz law (HZ)");
+  q.dim = in->dim;
+  for (int d = 0; d < 3; ++d) {
+    q.box[d] = in->box[d];
+    q.periodic[d] = in->pbc[d] ? 1 : 0;
+  }
+  q.dt = in->dt;
+  Node hz = loc.child("PAIRFORCES").child("HZ");
+  q.E = hz.nums("ELASTIC_MODULUS", 1)[0];
+  q.nu = hz.nums("POISSON_RATIO", 1)[0];
+  q.sigma_core = hz.nums("SIGMA_CORE", 1)[0];
+  q.adhesion = hz.nums("ADHESION_CONSTANT", 1)[0];
+  q.motility = loc.nums("MOTILITY", 1)[0];
+  q.zeta = loc.nums("FRICTION", 1)[0];
+  if (!(q.zeta > 0.0)) key_error(loc.path + ".FRICTION", "In Euler, zeta should > 0!!!");
+  q.zeta_p = loc.nums("P_FRICTION", 1)[0];
+  q.zeta_p_beta = loc.nums("P_FRICTION_BETA", 1)[0];
+  q.noise_D = integrator == "EULER" ? 0.0 : loc.child("NOISE").num("PASSIVE");
+  q.osmotic_pressure = in->osm;
+  q.drain = in->drain ? 1 : 0;
+  q.cycle_rho_ratio = 1.0;  // Cell.cuh:242-254 defaults
+  q.cycle_r_maxed = 1.0;
+  q.v1 = 1.0;
+  Node dv = loc.child("DIVISION");
+  q.divide = dv.boolean("ENABLED") ? 1 : 0;
+  if (q.divide) {
+    if (dv.boolean("CONST_FORCE"))
+      key_error(dv.path + ".CONST_FORCE", "constant-force cells do not enter the single-element cycle");
+    q.tau_div_mu = dv.child("TAU_DIVISION").num("AVG");
+    q.tau_div_sigma = dv.child("TAU_DIVISION").num("SIGMA");
+    q.tau_mig_mu = dv.child("TAU_MIGRATION").num("AVG");
+    q.tau_mig_sigma = dv.child("TAU_MIGRATION").num("SIGMA");
+    if (q.tau_mig_mu != 0.0)
+      key_error(dv.path + ".TAU_MIGRATION.AVG", "crawling cells never re-enter the single-element cycle (must be 0)");
+    q.v1 = dv.num("V1");
+    q.cycle_tau_r = dv.num("CYCLE_TAU_R");
+    q.cycle_tau_v = dv.num("CYCLE_TAU_V");
+    q.cycle_tau_p = dv.num("CYCLE_TAU_P");
+    q.cycle_sigma_min = dv.num("CYCLE_SIGMA_MIN");
+    q.cycle_p0 = dv.num("CYCLE_P0");
+    q.cycle_beta_vs = dv.num("CYCLE_BETA_VS");
+    q.cycle_rho_ratio = dv.num("CYCLE_RHO_RATIO");
+    if (dv.has("CYCLE_R_MAXED")) q.cycle_r_maxed = dv.num("CYCLE_R_MAXED");
+    if (dv.has("CYCLE_P_SHIFT")) q.cycle_p_shift = dv.num("CYCLE_P_SHIFT");
+    if (dv.has("CYCLE_P_SHIFT_TAU")) q.cycle_p_shift_tau = dv.num("CYCLE_P_SHIFT_TAU");
+  }
+  if (loc.has("APOPTOSIS") && loc.child("APOPTOSIS").boolean("ENABLED")) {  // Input.cpp:247-262
+    Node a = loc.child("APOPTOSIS");
+    q.apoptosis = CIL_APOP_CYCLE_PRESSURE;  // the law the Euler step applies (CIL.cu:1017)
+    q.apop_pressure = a.num("APOP_PRESSURE");
+    q.apop_duration = a.num("APOP_DURATION");
+    q.apop_rate = a.num("APOP_RATE");
+    q.extr_gamma = a.num("EXTR_GAMMA");
+    (void)a.num("APOP_ACTIVITY_ALPHA");
+    (void)a.num("APOP_GAMMA");
+    (void)a.num("EXTR_RATE");
+    if (!(q.apop_rate * q.dt < 1.0)) key_error(a.path + ".APOP_RATE", "Apoptosis rate per time step >= 1");
+  }
+  const bool has_gpu = root.has("GPU");
+  read_init(in, root, cell, 1);
+  run.ncells = in->ncells;
+  run.capacity = has_gpu && root.child("GPU").has("CAPACITY") ? root.child("GPU").integer("CAPACITY")
+                                                                : 4 * in->ncells + 64;
+}
 
 void read_all(cil_input *in) {
   Node root{&in->root, ""};
@@ -417,6 +527,8 @@ void read_all(cil_input *in) {
       key_error("MD.DT.SELECT", "AUTOSCALE needs the reference's force-law time scales; use MANUAL");
     in->dt = dtn.num("MANUAL");
     if (!(in->dt > 0.0)) key_error("MD.DT.MANUAL", "dt <= 0");
+    in->drain = md.boolean("DRAIN");
+    in->osm = md.num("OSMOTIC_PRESSURE");
   }
   std::string pair = root.child("INTERACTIONS").child("PAIRFORCES").pick("SELECT", {"LJ", "SC", "HZ", "EA", "GHOSTS"});
   {  // readRunTime (Input.cpp:560-588)
@@ -440,7 +552,12 @@ void read_all(cil_input *in) {
   const std::string cell = names[0];
   copy_str(run.cell_name, sizeof run.cell_name, cell);
   Node loc = sp.child(cell);
-  if (loc.integer("NELEM") != 2) key_error(loc.path + ".NELEM", "the GPU step models two-element cells");
+  const int nelem = loc.integer("NELEM");
+  if (nelem == 1) {
+    read_single(in, root, loc, cell, integrator, pair);
+    return;
+  }
+  if (nelem != 2) key_error(loc.path + ".NELEM", "the GPU step models cells of one or two elements");
   const auto enames = loc.strs("NAMES");
   if (enames.size() != 2) key_error(loc.path + ".NAMES", "vector should be of size 2. Got " + std::to_string(enames.size()));
   if (enames[0] == enames[1]) key_error(loc.path + ".NAMES", "element names must be unique!");
@@ -573,29 +690,7 @@ void read_all(cil_input *in) {
   p.div_tau_sigma = in->tau_div[1];
   p.apop_rate = apop;
 
-  // readInit (Input.cpp:591-761)
-  Node init = root.child("INIT").child(cell);
-  in->init_kind = init.pick("SELECT", {"JSON", "H5", "RANDOM"});
-  if (in->init_kind == "H5") key_error(init.path + ".SELECT", "H5 restart needs libhdf5, which this build does not have");
-  if (in->init_kind == "RANDOM") {
-    const int n = init.child("RANDOM").integer("NUMBER");
-    if (n < 0) key_error(init.path + ".RANDOM.NUMBER", "negative cell count");
-    in->ncells = n;
-  } else {
-    Node jn{nullptr, ""};
-    const auto &rows = init.array("JSON", &jn);
-    if (rows.size() % 2) key_error(jn.path, "element count is not a multiple of NELEM");
-    in->ncells = static_cast<int>(rows.size() / 2);
-    in->json_pos.reserve(rows.size() * in->dim);
-    for (const auto &r : rows) {
-      if (r.kind != JVal::kArr || r.arr.size() != static_cast<size_t>(in->dim))
-        key_error(jn.path, "rows should be of size " + std::to_string(in->dim));
-      for (const auto &x : r.arr) {
-        if (x.kind != JVal::kNum) key_error(jn.path, "expected numbers");
-        in->json_pos.push_back(x.num);
-      }
-    }
-  }
+  read_init(in, root, cell, 2);  // readInit (Input.cpp:591-761)
   run.ncells = in->ncells;
   run.capacity = has_gpu && gpu.has("CAPACITY") ? gpu.integer("CAPACITY") : 4 * in->ncells + 64;
 }
@@ -660,6 +755,10 @@ cil_status cil_input_load(const char *text, int32_t is_path, cil_input **out) {
 
 cil_status cil_input_config(const cil_input *in, cil_config *cfg, cil_colony_params *params, cil_run_info *run) {
   if (!in || !in->ok) return CIL_ERR_STATE;
+  if (in->nelem != 2) {
+    const_cast<cil_input *>(in)->err = "the run describes single-element cells: use cil_input_cycle_config";
+    return CIL_ERR_STATE;
+  }
   if (cfg) *cfg = in->cfg;
   if (params) *params = in->p;
   if (run) *run = in->run;
@@ -667,7 +766,7 @@ cil_status cil_input_config(const cil_input *in, cil_config *cfg, cil_colony_par
 }
 
 cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *v) {
-  if (!in || !in->ok) return CIL_ERR_STATE;
+  if (!in || !in->ok || in->nelem != 2) return CIL_ERR_STATE;
   cil_input *m = const_cast<cil_input *>(in);
   if (!v || !v->pos || !v->sigma || !v->t0 || !v->tswitch) {
     m->err = "cil_input_initial_state: NULL arrays";
@@ -711,6 +810,74 @@ cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *v) {
       if (std::isnan(r) || (in->pbc[d] && !(r >= 0.0 && r < in->box[d]))) {
         m->err = "Input Positions Out of Bounds! (cell " + std::to_string(i / 2) + ", element " +
                  std::to_string(i % 2) + ", axis " + std::to_string(d) + ")";
+        return CIL_ERR_CONFIG;
+      }
+    }
+  return CIL_OK;
+}
+
+int32_t cil_input_elements(const cil_input *in) { return in && in->ok ? in->nelem : 0; }
+
+cil_status cil_input_cycle_config(const cil_input *in, cil_cycle_params *params, cil_run_info *run) {
+  if (!in || !in->ok) return CIL_ERR_STATE;
+  if (in->nelem != 1) {
+    const_cast<cil_input *>(in)->err = "the run describes two-element cells: use cil_input_config";
+    return CIL_ERR_STATE;
+  }
+  if (params) *params = in->cyc;
+  if (run) *run = in->run;
+  return CIL_OK;
+}
+
+cil_status cil_input_cycle_initial_state(const cil_input *in, cil_cycle_view *v) {
+  if (!in || !in->ok) return CIL_ERR_STATE;
+  cil_input *m = const_cast<cil_input *>(in);
+  if (in->nelem != 1) {
+    m->err = "the run describes two-element cells: use cil_input_initial_state";
+    return CIL_ERR_STATE;
+  }
+  if (!v || !v->pos || !v->sigma || !v->sigma_t || !v->theta || !v->rho || !v->angvel) {
+    m->err = "cil_input_cycle_initial_state: NULL arrays";
+    return CIL_ERR_CONFIG;
+  }
+  const int n = in->ncells, D = in->dim;
+  v->ncells = n;
+  v->ts = 0;
+  if (v->capacity < n) {
+    m->err = "cil_input_cycle_initial_state: the view holds fewer cells than the initial configuration";
+    return CIL_ERR_CAPACITY;
+  }
+  const cil_cycle_params &q = in->cyc;
+  cil::HostRng rng;
+  rng.seed(static_cast<uint32_t>(in->run.seed));
+  auto positions = [&]() {  // Input.cpp:736-757 with one element: a uniform position per cell
+    for (int i = 0; i < n; ++i)
+      for (int d = 0; d < D; ++d) v->pos[static_cast<size_t>(i) * D + d] = rng.uniform0x(in->box[d]);
+  };
+  if (in->init_kind == "RANDOM") positions();
+  else std::memcpy(v->pos, in->json_pos.data(), sizeof(double) * in->json_pos.size());
+  // initializeCellStatus (CIL.cuh:253-330): every cell dividing, its cycle speed from the span
+  const double tau[2] = {q.tau_div_mu, q.tau_div_sigma};
+  for (int i = 0; i < n; ++i) {
+    v->sigma[i] = q.sigma_core;
+    v->sigma_t[i] = q.sigma_core;
+    v->rho[i] = 1.0;
+    v->theta[i] = -1.0;
+    v->angvel[i] = -1.0;
+    if (q.divide) {
+      (void)rng.uniform0x(1.0);  // the migration test, probability 0 here
+      int span = time_span(rng, tau, in->dt);
+      v->angvel[i] = 1.0 / span;
+      v->theta[i] = rng.uniform0x(1);
+      span -= nint(rng.uniform0x(static_cast<double>(span))) - 1;
+    }
+  }
+  if (in->init_kind == "RANDOM") positions();  // the second readInit
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < D; ++d) {
+      const double r = v->pos[static_cast<size_t>(i) * D + d];
+      if (std::isnan(r) || (in->pbc[d] && !(r >= 0.0 && r < in->box[d]))) {
+        m->err = "Input Positions Out of Bounds! (cell " + std::to_string(i) + ", axis " + std::to_string(d) + ")";
         return CIL_ERR_CONFIG;
       }
     }

@@ -13,11 +13,15 @@
  *   RUNTIME     RNG.SEED (<= 0: the current time, as Random::init(time(NULL))).
  *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 needs libhdf5, which this
  *               build does not have, and is reported back as not served).
- *   SPECIES     one species of two-element cells: NELEM, NAMES, MOTILITY, FRICTION,
+ *   SPECIES     one species. Two-element cells (cil_gpu.h): NELEM, NAMES, MOTILITY, FRICTION,
  *               NOISE.PASSIVE, the element diameters of the selected pair force, FENE RMAX /
  *               KAPPA_PULL (for the steady-state length rss that INIT RANDOM uses),
  *               DIVISION (ENABLED, CONST_FORCE, TAU_DIVISION, TAU_MIGRATION), APOPTOSIS
- *               (ENABLED, APOP_RATE).
+ *               (ENABLED, APOP_RATE). Single-element cells, the shipped runs (the cell-cycle
+ *               model, cil_cycle.h): PAIRFORCES.HZ (ELASTIC_MODULUS, POISSON_RATIO, SIGMA_CORE,
+ *               ADHESION_CONSTANT), MOTILITY, FRICTION, P_FRICTION, P_FRICTION_BETA, NOISE,
+ *               DIVISION (TAU_DIVISION, V1, CYCLE_*), APOPTOSIS (the Euler step's cycle-pressure
+ *               law); MD.OSMOTIC_PRESSURE and MD.DRAIN.
  *   INTERACTIONS PAIRFORCES.SELECT "LJ" with ATTRACTION OFF is the reference's own law
  *               (WCA, cil_gpu.h CIL_FORCE_LJ_WCA, epsilon from the species' LJ EPSILON).
  *   GPU         (optional block, this library's own): PRECISION "FP64" | "MIXED", RNG
@@ -40,6 +44,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "cil_cycle.h"
 #include "cil_gpu.h"
 
 #ifdef __cplusplus
@@ -79,6 +84,21 @@ cil_status cil_input_config(const cil_input *in, cil_config *cfg, cil_colony_par
  * the reference's Random stream in the reference's order: positions, cell status, then
  * positions again (initialize() reads INIT twice, CIL.cuh:374-378, and the second read wins). */
 cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *view);
+
+/* Elements per cell of the described species: 2 (cil_input_config / cil_input_initial_state,
+ * the two-element step) or 1 (cil_input_cycle_config / cil_input_cycle_initial_state, the
+ * cell-cycle model); 0 if the description did not load. */
+int32_t cil_input_elements(const cil_input *in);
+
+/* The cell-cycle model's parameters of a single-element run. */
+cil_status cil_input_cycle_config(const cil_input *in, cil_cycle_params *params, cil_run_info *run);
+
+/* Initial state of a single-element run for cil_cycle_upload: positions (INIT RANDOM with the
+ * reference's draws, or JSON), sigma = sigma_t = SIGMA_CORE, rho = 1, and theta and the cycle
+ * speed from the reference's cell-status draws (theta = U[0, 1), angvel = 1 / max(Nint(N(tau_div)
+ * / dt), 1)), all on the reference's Random stream in its order. pos, sigma, sigma_t, theta,
+ * rho and angvel must be given. */
+cil_status cil_input_cycle_initial_state(const cil_input *in, cil_cycle_view *view);
 
 /* Message of the last failure (empty if none). */
 void cil_input_last_error(const cil_input *in, char *buf, size_t len);

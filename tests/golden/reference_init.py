@@ -87,3 +87,30 @@ def from_fixture(doc):
                 box=md["BOX"], pbc=md["PBC"], rss=rss, divide=dv["ENABLED"], const_force=dv.get("CONST_FORCE", False),
                 tau_div=(dv["TAU_DIVISION"]["AVG"], dv["TAU_DIVISION"]["SIGMA"]),
                 tau_mig=(dv["TAU_MIGRATION"]["AVG"], dv["TAU_MIGRATION"]["SIGMA"]), dt=md["DT"]["MANUAL"])
+
+
+def reference_cycle_init(seed, n, dim, box, tau_div, dt, random=True):
+    """INIT RANDOM and the cell status of a single-element species (Input.cpp:736-757 with
+    one element; CIL.cuh:253-330), on the reference's Random:: functions."""
+    L = load()
+    L.ref_init(seed)
+
+    def positions():
+        pos = np.zeros((n, dim))
+        for i in range(n):
+            for d in range(dim):
+                pos[i, d] = L.ref_uniform0x(box[d])
+        return pos
+
+    if random:
+        positions()
+    theta = np.zeros(n)
+    angvel = np.zeros(n)
+    for i in range(n):
+        L.ref_uniform0x(1.0)  # the migration test
+        span = max(nint(L.ref_normal_ms(tau_div[0], tau_div[1]) / dt), 1)
+        angvel[i] = 1.0 / span
+        theta[i] = L.ref_uniform0x(1.0)
+        L.ref_uniform0x(float(span))
+    pos = positions() if random else None
+    return pos, theta, angvel

@@ -68,3 +68,44 @@ def test_runner_writes_the_run(gpu_lib, tmp_path):
     last = GSDFile(str(tmp_path / "out" / "Last" / "colony.Last.gsd"))
     assert last.nframes == 1 and int(last.read(0, "configuration/step")[0]) == 0
     np.testing.assert_array_equal(last.read(0, "particles/position"), f.read(f.nframes - 1, "particles/position"))
+
+
+SINGLE = os.path.join(ROOT, "tests", "golden", "input_single_element_2d.json")
+REFERENCE_FRAME_CHUNKS = ["configuration/step", "configuration/dimensions", "configuration/box", "particles/N",
+                          "particles/types", "particles/Z", "particles/diameter", "particles/typeid",
+                          "particles/charge", "particles/position", "particles/velocity", "particles/mass"]
+
+
+def test_runner_single_element_run(gpu_lib, tmp_path):
+    """A single-element run (the shipped configurations' model) through cil_gpu_run: frames of
+    the cell-cycle model with the chunks of the reference's own final-state files, equal to the
+    same run through the Python binding."""
+    G = gpu_lib
+    from cil_cuda_gb300 import build
+    doc = json.load(open(SINGLE))
+    doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
+    cfg = tmp_path / "single.json"
+    cfg.write_text(json.dumps(doc))
+    res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    f = GSDFile(str(tmp_path / "out" / "single.gsd"))
+    frames, gts = doc["MD"]["FRAMES"], doc["MD"]["GTS"]
+    assert f.nframes == frames + 1
+    assert f.chunk_names(0) == REFERENCE_FRAME_CHUNKS and f.types(0) == ["C1"]
+    last = GSDFile(str(tmp_path / "out" / "Last" / "single.Last.gsd"))
+    assert last.chunk_names(0) == REFERENCE_FRAME_CHUNKS
+    r = G.RunInput(str(cfg))
+    eng = r.cycle_engine()
+    eng.upload(**r.cycle_initial_state())
+    for _ in range(frames):
+        eng.step(gts)
+        eng.check_positions()
+    s = eng.download()
+    eng.close()
+    n = s["ncells"]
+    assert n > 200 and int(f.read(frames, "particles/N")[0]) == n
+    exp = (s["pos"] - 20.0).astype(np.float32)
+    np.testing.assert_array_equal(f.read(frames, "particles/position")[:, :2], exp)
+    np.testing.assert_array_equal(f.read(frames, "particles/charge"), s["rho"].astype(np.float32))
+    np.testing.assert_array_equal(f.read(frames, "particles/mass"), s["pressure"].astype(np.float32))
+    np.testing.assert_array_equal(last.read(0, "particles/diameter"), s["sigma"].astype(np.float32))

@@ -123,7 +123,8 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
     (lambda d: d["MD"]["DT"].update(SELECT="AUTOSCALE"), "MD.DT.SELECT"),
     (lambda d: d["MD"].update(BOX=[60]), "vector should be of size 2. Got 1"),
     (lambda d: d["SPECIES"].update(DEFINE=["A", "B"]), "SPECIES.DEFINE"),
-    (lambda d: d["SPECIES"]["A"].update(NELEM=1), "SPECIES.A.NELEM"),
+    (lambda d: d["SPECIES"]["A"].update(NELEM=3), "SPECIES.A.NELEM"),
+    (lambda d: d["SPECIES"]["A"].update(NELEM=1), "SPECIES.A.NAMES : vector should be of size 1"),
     (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
     (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
     (lambda d: d["GPU"].pop("FORCE_LAW"), "GPU.FORCE_LAW"),
@@ -165,16 +166,63 @@ def test_parse_errors(G):
 
 @pytest.mark.parametrize("name,needle", [
     ("input/cil.json", "JSON parse error at line"),  # holds an unresolved merge conflict
-    ("input/test.2d.json", "SPECIES.C.NELEM"),  # single-element cells
-    ("PRX_MDCK_2D.json", "NELEM"),  # single-element cells
+    ("input/test.2d.json", "SPECIES.C.P_FRICTION : key not found"),  # the reference's readSpecs needs it too
 ])
-def test_reference_configs_are_read_or_refused_with_reason(G, name, needle):
+def test_reference_configs_refused_with_reason(G, name, needle):
     p = os.path.join(REF_DIR, name)
     if not os.path.exists(p):
         pytest.skip("reference configs absent")
     with pytest.raises(G.CilError) as e:
         G.RunInput(p)
     assert needle in str(e.value), str(e.value)
+
+
+@pytest.mark.parametrize("name,ncells,drain,v1", [("PRX_MDCK_2D.json", 1, 1, 15.0),
+                                                  ("Match_Puliafito_2D.json", 1, 1, 35.0),
+                                                  ("Ecoli_channel_2D.json", 2, 1, 3.0)])
+def test_shipped_configs_load_as_the_cycle_model(G, name, ncells, drain, v1):
+    """The three shipped configurations are single-element runs of the cell-cycle model."""
+    p = os.path.join(REF_DIR, name)
+    if not os.path.exists(p):
+        pytest.skip("reference configs absent")
+    r = G.RunInput(p)
+    assert r.elements == 1 and r.config is None
+    q = r.params
+    assert (q["E"], q["nu"], q["adhesion"], q["divide"], q["drain"], q["v1"]) == (100.0, 0.5, 0.2, 1, drain, v1)
+    assert r.run["ncells"] == ncells and r.run["output_gsd"] == 1
+    st = r.cycle_initial_state()
+    assert st["pos"].shape == (ncells, 2) and np.all(st["rho"] == 1.0) and np.all(st["angvel"] > 0)
+
+
+SINGLE = os.path.join(GOLDEN, "input_single_element_2d.json")
+
+
+def test_single_element_init_matches_reference_golden(G):
+    r = G.RunInput(SINGLE)
+    st = r.cycle_initial_state()
+    gold = json.load(open(os.path.join(GOLDEN, "input_single_element_golden.json")))
+    h = lambda k: np.array([float.fromhex(x) for x in gold[k]])  # noqa: E731
+    np.testing.assert_array_equal(st["pos"].ravel(), h("pos"))
+    np.testing.assert_array_equal(st["theta"], h("theta"))
+    np.testing.assert_array_equal(st["angvel"], h("angvel"))
+    assert np.all(st["sigma"] == 1.1283791670955126) and np.all(st["rho"] == 1.0)
+    q = r.params
+    assert (q["dim"], q["motility"], q["zeta"], q["tau_div_mu"], q["cycle_p0"], q["apoptosis"]) == \
+        (2, 1.0, 0.2, 0.2, 5.0, G.APOP_NONE)
+
+
+def test_single_element_init_matches_reference_live(G):
+    if not os.path.exists(R.LIB):
+        pytest.skip("reference RNG not built (reference tree absent)")
+    d = json.load(open(SINGLE))
+    d["RUNTIME"]["RNG"]["SEED"] = 77
+    d["INIT"]["C1"]["RANDOM"]["NUMBER"] = 64
+    r = load(G, d)
+    st = r.cycle_initial_state()
+    pos, theta, angvel = R.reference_cycle_init(77, 64, 2, [40.0, 40.0], (0.2, 0.02), 0.0002)
+    np.testing.assert_array_equal(st["pos"], pos)
+    np.testing.assert_array_equal(st["theta"], theta)
+    np.testing.assert_array_equal(st["angvel"], angvel)
 
 
 def test_heun_is_read(G):
