@@ -351,6 +351,53 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
             "enqueue_ms_per_frame": out["async_stats"]["enqueue_ms"] / nframes}
 
 
+def run_cycle(G, device, steps, warmup):
+    """The single-element cell-cycle model that the shipped configurations run
+    (PRX_MDCK_2D.json: Hertz contacts E = 100 with adhesion 0.2, motility 1, friction 0.01,
+    dt = 1e-5, V1 15, P0 5), 1M cells on a jittered square lattice of spacing 1.1 in a periodic
+    1100^2 box, cycle phases uniform; device-timed, and the restatement on one host thread over
+    a 20k-cell sample of the same packing for scale."""
+    side = 1000
+    rng = np.random.default_rng(17)
+    n = side * side
+    g = (np.arange(n) % side, np.arange(n) // side)
+    pos = np.stack([(g[0] + 0.5) * 1.1, (g[1] + 0.5) * 1.1], axis=1) + rng.uniform(-0.05, 0.05, size=(n, 2))
+    prm = dict(box=[1100.0, 1100.0, 0.0], dt=1e-5, motility=1.0, zeta=0.01, v1=15.0)
+    st = dict(pos=pos, sigma=np.full(n, 1.1283791670955126), theta=rng.uniform(0, 1, n), rho=np.ones(n),
+              angvel=np.full(n, 1e-5))
+    eng = G.CycleEngine(prm, int(1.2 * n), seed=3, device=device)
+    eng.upload(**st)
+    eng.step(warmup)
+    n0 = eng.download()["ncells"]
+    eng.step(steps)
+    tm = eng.timings()
+    n1 = eng.download()["ncells"]
+    eng.close()
+    dev_s = tm["total_ms"] * 1e-3
+    out = {"value": (n0 + n1) / 2 * steps / dev_s, "unit": "cell-steps/s", "cells": n0, "cells_end": n1,
+           "steps": steps, "ms_per_step": tm["total_ms"] / steps, "gpu_launches": tm["launches"],
+           "config": "single-element cell-cycle model (PRX_MDCK_2D.json parameters), FP64, 1M cells"}
+    try:
+        from oracle import oracle as O
+        O.build()
+        m = 140  # a 140 x 140 corner of the lattice in its own periodic box
+        sel = (g[0] < m) & (g[1] < m)
+        k = int(sel.sum())
+        so = dict(pos=pos[sel], sigma=np.full(k, 1.1283791670955126), theta=st["theta"][sel], rho=np.ones(k),
+                  angvel=np.full(k, 1e-5))
+        q = dict(prm)
+        q["box"] = [m * 1.1, m * 1.1, 0.0]
+        o = O.CycleOracle(q, 2 * k, 3)
+        o.set_state(**so)
+        t0 = time.perf_counter()
+        o.step(10)
+        cpu_s = time.perf_counter() - t0
+        out["cpu_restatement_1_thread"] = {"value": k * 10 / cpu_s, "unit": "cell-steps/s", "cells": k, "steps": 10}
+    except Exception as e:  # reported, not fatal
+        out["cpu_restatement_1_thread"] = {"error": str(e)}
+    return out
+
+
 def cpu_baseline(p, st, threads: int, budget_s: float = 20.0):
     """The oracle (race-free OpenMP variant of the reference's step) on the host cores on
     the same 2M-particle state, as many whole steps as fit the budget (at least 1)."""
@@ -550,6 +597,10 @@ def main():
             line["channel_3d"] = run_channel(G, device, min(args.steps, 200), args.warmup)
         except G.CilError as e:  # reported, not fatal to the headline line
             line["channel_3d"] = {"error": str(e)}
+        try:
+            line["cycle_model"] = run_cycle(G, device, min(args.steps, 200), args.warmup)
+        except G.CilError as e:
+            line["cycle_model"] = {"error": str(e)}
     if not args.no_e2e:
         e2e = run_e2e(G, p, st, G.PREC_MIXED, args.steps, device, 7 + rank, mlp_skin if have_mlp else args.skin,
                       sched=have_mlp, tune=tune)
