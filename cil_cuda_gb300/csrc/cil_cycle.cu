@@ -48,6 +48,7 @@ struct CyConst {
   double dt;
   int ns[3];
   double bw[3];       // bin width per axis
+  double half[3];     // box / 2
   double inv_bw[3];
   double sigma_core;
   double hz_c;        // (1 - nu^2) / E
@@ -368,19 +369,28 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             double rij[3] = {0, 0, 0};
             double r2 = 0.0;
             for (int d = 0; d < D; ++d) {
+              // nearest image: |dd| < L, so Nint(dd / L) is -1, 0 or 1; the two forms differ
+              // only at |dd| = L/2, far beyond any contact
               double dd = S.x[d * cap + j] - xi[d];
-              if (C.periodic[d]) dd -= static_cast<double>(nint(dd / C.box[d])) * C.box[d];
+              if (C.periodic[d]) {
+                if (dd > C.half[d])
+                  dd -= C.box[d];
+                else if (dd < -C.half[d])
+                  dd += C.box[d];
+              }
               rij[d] = dd;
               r2 += dd * dd;
             }
             const double sj = S.sig[j];
+            const double cut = (si + sj) / 2;
+            if (r2 > 1.0000001 * (cut * cut)) continue;  // outside the contact distance (exact test below)
             const double r = sqrt(r2);
-            if (!(r <= (si + sj) / 2) || r == 0.0) continue;
+            if (!(r <= cut) || r == 0.0) continue;
             // the pair's first cell is the one of lower index (the contact length is not
             // symmetric in the two diameters)
             const double sa = i < j ? si : sj, sb = i < j ? sj : si;
             const double h = fmax((si + sj) / 2 - r, 0.0);
-            const double fel = pow(h, 1.5) / (0.75 * c2 * sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
+            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));  // h^1.5
             double A, vol;
             if (D == 3) {
               A = contact_area(r, sa, sb);
@@ -424,7 +434,7 @@ __global__ void __launch_bounds__(kTile) k_cy_cycle(CyConst C, CySet S, CyCounte
     else
       S.tp[i] += 1;
     if (C.divide) {
-      const double shift = C.p_shift * exp(-ts * C.p_shift_tau_inv);
+      const double shift = C.p_shift != 0.0 ? C.p_shift * exp(-ts * C.p_shift_tau_inv) : 0.0;
       const double pnd = fmax(0., S.p[i] + shift) / C.p0;
       const double om = S.om[i];
       double rho = S.rho[i];
@@ -469,7 +479,14 @@ __global__ void __launch_bounds__(kTile) k_cy_divide(CyConst C, CySet S, CyCount
   int tot;
   const int rank = block_start[blockIdx.x] + block_excl_scan(f, &tot);
   const size_t cap = C.capacity;
-  if (i < n) put_sigma_max(cnt, S.sig[i]);
+  {  // the block's largest diameter, one atomic per block
+    __shared__ unsigned long long smax;
+    if (threadIdx.x == 0) smax = 0ull;
+    __syncthreads();
+    if (i < n) atomicMax(&smax, static_cast<unsigned long long>(__double_as_longlong(S.sig[i])));
+    __syncthreads();
+    if (threadIdx.x == 0 && smax) atomicMax(&cnt->sigma_max_bits, smax);
+  }
   if (f) {
     const int inew = n + rank;
     if (inew >= C.capacity) {
@@ -814,6 +831,7 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
   for (int d = 0; d < 3; ++d) {
     C.periodic[d] = d < p->dim ? p->periodic[d] : 0;
     C.box[d] = d < p->dim ? p->box[d] : 1.0;
+    C.half[d] = 0.5 * C.box[d];
   }
   // bins: width at least the diameter of a new cell (the search widens as cells grow)
   h->nbins = 1;

@@ -244,7 +244,12 @@ struct Model {
               double rij[3] = {0, 0, 0}, r2 = 0;
               for (int d = 0; d < D; ++d) {
                 double dd = c[j].x[d] - ci.x[d];
-                if (p.periodic[d]) dd -= static_cast<double>(nint(dd / p.box[d])) * p.box[d];
+                if (p.periodic[d]) {  // nearest image (Box::distance's Nint, |dd| < L)
+                  if (dd > 0.5 * p.box[d])
+                    dd -= p.box[d];
+                  else if (dd < -(0.5 * p.box[d]))
+                    dd += p.box[d];
+                }
                 rij[d] = dd;
                 r2 += dd * dd;
               }
@@ -253,7 +258,7 @@ struct Model {
               if (!(r <= (si + sj) / 2) || r == 0.0) continue;
               const double sa = i < j ? si : sj, sb = i < j ? sj : si;
               const double h = std::fmax((si + sj) / 2 - r, 0.0);
-              const double fel = std::pow(h, 1.5) / (0.75 * c2 * std::sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
+              const double fel = (h * std::sqrt(h)) / (0.75 * c2 * std::sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
               double A, vol;
               if (D == 3) {
                 A = contact_area(r, sa, sb);
@@ -296,7 +301,7 @@ struct Model {
       else
         ci.tp += 1;
       if (!p.divide) continue;
-      const double shift = p_shift * std::exp(-ts * p_shift_tau_inv);
+      const double shift = p_shift != 0.0 ? p_shift * std::exp(-ts * p_shift_tau_inv) : 0.0;
       const double pnd = std::fmax(0., ci.p + shift) / p.cycle_p0;
       const double om = ci.om;
       double rho = ci.rho;
