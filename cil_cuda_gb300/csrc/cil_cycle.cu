@@ -351,6 +351,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
       }
     }
     const double c2 = C.hz_c + C.hz_c;
+    const double inv_ri = 1.0 / (si / 2);
     for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
       for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
         for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             // symmetric in the two diameters)
             const double sa = i < j ? si : sj, sb = i < j ? sj : si;
             const double h = fmax((si + sj) / 2 - r, 0.0);
-            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));  // h^1.5
+            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(inv_ri + 1.0 / (sj / 2)));  // h^1.5
             double A, vol;
             if (D == 3) {
               A = contact_area(r, sa, sb);
@@ -407,7 +408,9 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   }
   // ---- position update with the pressure-dependent friction (CIL.cu:902-939)
   const double pnd = pres / C.p0;
-  const double temp = C.dt * 1 / ((C.zeta + C.zeta_p * pow(pnd, C.zeta_p_beta)) * area_of(si));
+  // pow(x, 0) is 1 for every x
+  const double pw = C.zeta_p_beta == 0.0 ? 1.0 : pow(pnd, C.zeta_p_beta);
+  const double temp = C.dt * 1 / ((C.zeta + C.zeta_p * pw) * area_of(si));
   bool finite = true;
   for (int d = 0; d < D; ++d) {
     finite = finite && isfinite(F[d]);
