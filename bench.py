@@ -351,7 +351,7 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
             "enqueue_ms_per_frame": out["async_stats"]["enqueue_ms"] / nframes}
 
 
-def run_cycle(G, device, steps, warmup):
+def run_cycle(G, device, steps, warmup, precision=0):
     """The single-element cell-cycle model that the shipped configurations run
     (PRX_MDCK_2D.json: Hertz contacts E = 100 with adhesion 0.2, motility 1, friction 0.01,
     dt = 1e-5, V1 15, P0 5), 1M cells on a jittered square lattice of spacing 1.1 in a periodic
@@ -362,7 +362,7 @@ def run_cycle(G, device, steps, warmup):
     n = side * side
     g = (np.arange(n) % side, np.arange(n) // side)
     pos = np.stack([(g[0] + 0.5) * 1.1, (g[1] + 0.5) * 1.1], axis=1) + rng.uniform(-0.05, 0.05, size=(n, 2))
-    prm = dict(box=[1100.0, 1100.0, 0.0], dt=1e-5, motility=1.0, zeta=0.01, v1=15.0)
+    prm = dict(box=[1100.0, 1100.0, 0.0], dt=1e-5, motility=1.0, zeta=0.01, v1=15.0, precision=precision)
     st = dict(pos=pos, sigma=np.full(n, 1.1283791670955126), theta=rng.uniform(0, 1, n), rho=np.ones(n),
               angvel=np.full(n, 1e-5))
     eng = G.CycleEngine(prm, int(1.2 * n), seed=3, device=device)
@@ -376,7 +376,10 @@ def run_cycle(G, device, steps, warmup):
     dev_s = tm["total_ms"] * 1e-3
     out = {"value": (n0 + n1) / 2 * steps / dev_s, "unit": "cell-steps/s", "cells": n0, "cells_end": n1,
            "steps": steps, "ms_per_step": tm["total_ms"] / steps, "gpu_launches": tm["launches"],
-           "config": "single-element cell-cycle model (PRX_MDCK_2D.json parameters), FP64, 1M cells"}
+           "config": "single-element cell-cycle model (PRX_MDCK_2D.json parameters), "
+                     + ("FP32 contacts / FP64 state" if precision else "FP64") + ", 1M cells"}
+    if precision:
+        return out
     try:
         from oracle import oracle as O
         O.build()
@@ -493,6 +496,7 @@ def main():
         build.build()
     if args.only == "cycle":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
+        print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1)))
         return 0
     p, st = workload(seed=1 + rank)
     hbm, peak_kind = peaks()
@@ -602,6 +606,7 @@ def main():
             line["channel_3d"] = {"error": str(e)}
         try:
             line["cycle_model"] = run_cycle(G, device, min(args.steps, 200), args.warmup)
+            line["cycle_model"]["fp32_contacts"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1)
         except G.CilError as e:
             line["cycle_model"] = {"error": str(e)}
     if not args.no_e2e:

@@ -196,7 +196,7 @@ CYCLE_FIELDS = [
     ("cycle_beta_vs", C.c_double), ("cycle_rho_ratio", C.c_double), ("cycle_r_maxed", C.c_double),
     ("cycle_p_shift", C.c_double), ("cycle_p_shift_tau", C.c_double), ("osmotic_pressure", C.c_double),
     ("apop_pressure", C.c_double), ("apop_duration", C.c_double), ("apop_rate", C.c_double),
-    ("extr_gamma", C.c_double), ("drain", C.c_int32), ("pad", C.c_int32),
+    ("extr_gamma", C.c_double), ("drain", C.c_int32), ("precision", C.c_int32),
 ]
 
 
@@ -218,7 +218,7 @@ def cycle_params(**kw) -> CycleParams:
                 cycle_tau_r=1.0, cycle_tau_v=1.0, cycle_tau_p=0.0, cycle_sigma_min=1.1283791670955126, cycle_p0=5.0,
                 cycle_beta_vs=0.0, cycle_rho_ratio=1.0, cycle_r_maxed=1.0, cycle_p_shift=0.0, cycle_p_shift_tau=0.0,
                 osmotic_pressure=0.0, apop_pressure=1.0, apop_duration=8.0, apop_rate=0.0, extr_gamma=0.0, drain=0,
-                pad=0)
+                precision=0)
     base.update(kw)
     q = CycleParams()
     for k, v in base.items():

@@ -272,6 +272,11 @@ __global__ void k_cy_sort(const int *start, int nbins, int *list, CyCounters *cn
 }
 
 // ---------------------------------------------------------------- forces + update
+// MIXED: the candidate test and the contact arithmetic in FP32 on the FP64 separation (GB300
+// runs FP64 at a small fraction of its FP32 rate); the forces and the pressure are summed in
+// FP32 over the contacts and added to the FP64 motility and noise; the position update and
+// the cell state stay FP64.
+template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
                                                     CyCounters *cnt, const int *start, const int *list,
                                                     const int *ts_dev) {
@@ -352,6 +357,9 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
     }
     const double c2 = C.hz_c + C.hz_c;
     const double inv_ri = 1.0 / (si / 2);
+    const float sif = static_cast<float>(si), c2f = static_cast<float>(c2), adhf = static_cast<float>(C.adhesion);
+    const float inv_rif = 2.0f / sif;
+    float Ff[3] = {0.0f, 0.0f, 0.0f}, presf = 0.0f;
     for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
       for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
         for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
@@ -367,6 +375,46 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
           for (int q = e0; q < e1; ++q) {
             const int j = list[q];
             if (j == i) continue;
+            if (MIXED) {
+              float df[3] = {0.0f, 0.0f, 0.0f};
+              float r2f = 0.0f;
+              for (int d = 0; d < D; ++d) {
+                double dd = S.x[d * cap + j] - xi[d];
+                if (C.periodic[d]) {
+                  if (dd > C.half[d])
+                    dd -= C.box[d];
+                  else if (dd < -C.half[d])
+                    dd += C.box[d];
+                }
+                df[d] = static_cast<float>(dd);
+                r2f += df[d] * df[d];
+              }
+              const float sjf = static_cast<float>(S.sig[j]);
+              const float cut = 0.5f * (sif + sjf);
+              if (!(r2f <= cut * cut) || r2f == 0.0f) continue;
+              const float r = sqrtf(r2f);
+              const float sa = i < j ? sif : sjf, sb = i < j ? sjf : sif;
+              const float h = fmaxf(cut - r, 0.0f);
+              const float fel = (h * sqrtf(h)) / (0.75f * c2f * sqrtf(inv_rif + 2.0f / sjf));
+              float A, vol;
+              if (D == 3) {
+                const float ra = 0.5f * sa, rb = 0.5f * sb;
+                const float u = r2f - rb * rb + ra * ra;
+                const float t = sqrtf(4.0f * r2f * (ra * ra) - u * u) / (2.0f * r);
+                A = t > 0.0f ? static_cast<float>(kPi) * (t * t) : 0.0f;
+                vol = A == 0.0f ? 0.0f : (4.0f * static_cast<float>(kPi) * (ra * ra) / 3.0f);
+              } else {
+                const float ra = 0.5f * sa, rb = 0.5f * sb;
+                const float qq = ra - (2.0f * rb * h - h * h) / (2.0f * (ra + rb - h));
+                const float t = 2.0f * sqrtf(ra * ra - qq * qq);
+                A = isnan(t) ? fminf(sa, sb) : t;
+                vol = A;
+              }
+              const float f0 = -fel + adhf * A;
+              if (vol != 0.0f) presf -= f0 / vol;
+              for (int d = 0; d < D; ++d) Ff[d] += f0 * df[d];
+              continue;
+            }
             double rij[3] = {0, 0, 0};
             double r2 = 0.0;
             for (int d = 0; d < D; ++d) {
@@ -405,6 +453,10 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
           }
         }
+    if (MIXED) {
+      pres += static_cast<double>(presf);
+      for (int d = 0; d < D; ++d) F[d] += static_cast<double>(Ff[d]);
+    }
   }
   // ---- position update with the pressure-dependent friction (CIL.cu:902-939)
   const double pnd = pres / C.p0;
@@ -672,7 +724,12 @@ __global__ void k_cy_init_status(CyConst C, CySet S, const CyCounters *cnt, int 
 
 __global__ void k_cy_sigma_max(CyConst C, CySet S, CyCounters *cnt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < cnt->n) put_sigma_max(cnt, S.sig[i]);
+  __shared__ unsigned long long smax;
+  if (threadIdx.x == 0) smax = 0ull;
+  __syncthreads();
+  if (i < cnt->n) atomicMax(&smax, static_cast<unsigned long long>(__double_as_longlong(S.sig[i])));
+  __syncthreads();
+  if (threadIdx.x == 0 && smax) put_sigma_max(cnt, __longlong_as_double(static_cast<long long>(smax)));
 }
 
 }  // namespace
@@ -732,6 +789,7 @@ cil_status check_params(const cil_cycle_params *p) {
   for (int d = 0; d < p->dim; ++d)
     if (!(p->box[d] > 0.0)) return CIL_ERR_CONFIG;
   if (p->apoptosis < CIL_APOP_NONE || p->apoptosis > CIL_APOP_PRESSURE_TIME) return CIL_ERR_CONFIG;
+  if (p->precision != 0 && p->precision != 1) return CIL_ERR_CONFIG;
   if (p->divide && (!(p->tau_div_mu > 0.0) || !(p->cycle_p0 != 0.0) || !(p->cycle_sigma_min > 0.0) ||
                     !(p->cycle_tau_r > 0.0) || !(p->cycle_tau_v > 0.0)))
     return CIL_ERR_CONFIG;
@@ -782,7 +840,10 @@ cil_status enqueue_step(cil_cycle *h) {
   bin_cells(h);
   const int g = blocks_for(h->cap);
   CySet &S = h->set[h->cur];
-  k_cy_force<<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
+  if (h->p.precision == 1)
+    k_cy_force<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
+  else
+    k_cy_force<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
   std::swap(S.x, h->xs);
   k_cy_advance<<<1, 1, 0, h->stream>>>(h->ts_dev);
   h->ts += 1;

@@ -26,7 +26,8 @@
  * Random draws are counter-based (Philox4x32-10 keyed by seed, step, cell index and purpose),
  * so runs are reproducible and independent of the launch configuration; the reference draws
  * from one dSFMT stream inside OpenMP loops, whose order is not reproducible with threads.
- * FP64 throughout. Cells are kept in index order; removals compact stably.
+ * FP64 (or FP32 contacts, cil_cycle_params.precision). Cells are kept in index order; removals
+ * compact stably.
  */
 #ifndef CIL_CYCLE_H
 #define CIL_CYCLE_H
@@ -79,7 +80,9 @@ typedef struct cil_cycle_params {
   /* apoptosis (APOPTOSIS block) */
   double apop_pressure, apop_duration, apop_rate, extr_gamma;
   int32_t drain;           /* MD.DRAIN: cil_cycle_check_positions removes cells off the box */
-  int32_t pad;
+  int32_t precision;       /* 0: FP64 throughout (computes what the CPU restatement computes);
+                            * 1: FP32 contact arithmetic on the FP64 separations, FP64 positions,
+                            * forces of motility and noise, and cell state */
 } cil_cycle_params;
 
 /* Per-cell state in index order. Arrays may be NULL where not wanted. */

@@ -37,7 +37,7 @@ typedef struct cyo_params {  // the layout of cil_cycle_params (include/cil_cycl
       cycle_r_maxed, cycle_p_shift, cycle_p_shift_tau, osmotic_pressure;
   double apop_pressure, apop_duration, apop_rate, extr_gamma;
   int32_t drain;
-  int32_t pad;
+  int32_t precision;  // read by the GPU model only: the restatement is FP64
 } cyo_params;
 
 }  // extern "C"

@@ -150,3 +150,27 @@ def test_shipped_configuration_grows_from_one_cell(gpu_lib):
     eng.close()
     assert 16 <= s["ncells"] <= 64, s["ncells"]
     assert np.all(np.isfinite(s["pos"])) and np.all(np.isfinite(s["sigma"]))
+
+
+def test_fp32_contacts_follow_fp64(gpu_lib):
+    """precision = 1: FP32 contact arithmetic on the FP64 separations. Over 100 steps it keeps
+    the FP64 run's cells and events, and its positions and pressures to FP32 rounding."""
+    G = gpu_lib
+    rng = np.random.default_rng(71)
+    box = [30.0, 30.0, 0.0]
+    prm = dict(box=box, dt=2e-4, motility=1.0, zeta=0.2, noise_D=0.002, v1=15.0)
+    st = colony(rng, 400, box)
+    out = []
+    for prec in (0, 1):
+        eng = G.CycleEngine(dict(prm, precision=prec), 20000, seed=11)
+        eng.upload(**st)
+        eng.step(100)
+        out.append(eng.download())
+        eng.close()
+    a, b = out
+    assert a["ncells"] == b["ncells"] > 400
+    d = a["pos"] - b["pos"]
+    d -= np.round(d / 30.0) * 30.0
+    assert np.abs(d).max() < 1e-4
+    assert np.abs(a["pressure"] - b["pressure"]).max() < 1e-3 * max(1.0, np.abs(a["pressure"]).max())
+    np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
