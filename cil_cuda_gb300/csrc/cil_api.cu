@@ -1345,6 +1345,23 @@ cil_status cil::frame_source(cil_handle *h, int colony, FrameSource *out) {
   s.sigma_max = hc.sigma_max;
   s.ts = h->ts;
   s.device = h->cfg.device;
+  s.capacity = hc.cap;
+  s.stream = h->stream;
+  *out = s;
+  return CIL_OK;
+}
+
+cil_status cil::frame_layout(cil_handle *h, int colony, FrameSource *out) {
+  if (!h) return CIL_ERR_CONFIG;
+  if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "frame_layout: bad arguments");
+  const HostColony &hc = h->hc[colony];
+  FrameSource s{};
+  s.dim = h->D;
+  s.divide = hc.p.divide;
+  s.dying = hc.p.apop_rate > 0.0;
+  for (int d = 0; d < 3; ++d) s.box[d] = hc.p.box[d];
+  s.device = h->cfg.device;
+  s.capacity = hc.cap;
   s.stream = h->stream;
   *out = s;
   return CIL_OK;

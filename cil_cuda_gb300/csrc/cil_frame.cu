@@ -358,6 +358,8 @@ struct cil_frame_writer {
   int dim = 2;
   int divide = 0, dying = 0;
   float box[6] = {0, 0, 0, 0, 0, 0};
+  double lz_opt = 0.0;
+  bool box_ready = false;
   double half[3] = {0, 0, 0};
   float zj[2] = {0, 0};
   int flags = 0;
@@ -534,8 +536,12 @@ cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const
   if (!h || !path || !out) return CIL_ERR_CONFIG;
   *out = nullptr;
   cil::FrameSource s{};
-  cil_status st = cil::frame_source(h, colony, &s);
+  cil_status st = cil::frame_layout(h, colony, &s);
   if (st != CIL_OK) return st;
+  if (cudaSetDevice(s.device) != cudaSuccess) {
+    cudaGetLastError();
+    return CIL_ERR_CUDA;
+  }
   cil_frame_options o{};
   if (opt) o = *opt;
   cil_frame_writer *w = new cil_frame_writer();
@@ -546,10 +552,11 @@ cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const
   w->divide = s.divide;
   w->dying = s.dying;
   w->flags = o.flags;
-  const double lz = s.dim == 3 ? s.box[2] : (o.lz > 0.0 ? o.lz : s.sigma_max);
+  // 2D box z: the option, else the largest uploaded diameter, read at the first frame
+  w->lz_opt = o.lz;
   w->box[0] = static_cast<float>(s.box[0]);
   w->box[1] = static_cast<float>(s.box[1]);
-  w->box[2] = static_cast<float>(lz);
+  w->box[2] = static_cast<float>(s.dim == 3 ? s.box[2] : o.lz);
   for (int d = 0; d < 3; ++d) w->half[d] = 0.5 * s.box[d];
   // zhack[j] = j * (-0.01 * units.Length) in FP64, then FP32 (OutputWriter.cpp:607-610);
   // element 0 lands on -0.0.
@@ -570,10 +577,8 @@ cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const
   for (int k = 0; ok && k < kSlots; ++k)
     ok = cudaEventCreate(&w->begin[k]) == cudaSuccess && cudaEventCreate(&w->packed[k]) == cudaSuccess &&
          cudaEventCreate(&w->copied[k]) == cudaSuccess;
-  // staging for the colony's current size and a quarter more, so that frames of a growing
-  // colony rarely reallocate inside the run
-  const size_t need = 7 * static_cast<size_t>(2 * s.ncells);
-  const size_t cap = need + need / 4 + 1024;
+  // staging for the colony's capacity, allocated here so that frames never allocate
+  const size_t cap = 7 * static_cast<size_t>(2 * s.capacity) + 1024;
   for (int k = 0; ok && k < kSlots; ++k) {
     ok = cudaMalloc(&w->d_buf[k], cap * sizeof(float)) == cudaSuccess &&
          cudaHostAlloc(&w->h_buf[k], cap * sizeof(float), cudaHostAllocDefault) == cudaSuccess;
@@ -599,6 +604,10 @@ cil_status cil_frame_write(cil_frame_writer *w, int64_t step, int64_t *frame) {
   cil::FrameSource s{};
   st = cil::frame_source(w->h, w->colony, &s);
   if (st != CIL_OK) return st;  // the handle holds the message
+  if (!w->box_ready) {  // before any frame is queued, so the writer thread never sees it change
+    if (w->dim == 2 && !(w->lz_opt > 0.0)) w->box[2] = static_cast<float>(s.sigma_max);  // lz2d
+    w->box_ready = true;
+  }
   const int slot = w->next_slot;
   {
     const auto tw = Clock::now();

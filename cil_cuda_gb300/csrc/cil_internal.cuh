@@ -649,10 +649,14 @@ struct FrameSource {
   double sigma_max;
   int64_t ts;
   int device;
+  int capacity;  // cells the colony can hold
   cudaStream_t stream;
 };
 // Waits for the handle's queued work and fills *out (cil_api.cu).
 cil_status frame_source(cil_handle *h, int colony, FrameSource *out);
+// The colony's static layout only (dim, box, flags, capacity, device), without waiting and
+// before any upload; the device pointers, cell count, sigma_max and ts are left empty.
+cil_status frame_layout(cil_handle *h, int colony, FrameSource *out);
 // Packs a colony's elements in canonical order into FP32 frame arrays: position [E][3]
 // (shifted by -half, 2D z from zj[j]), velocity [E][3], diameter [E] (cil_frame.cu).
 void launch_frame_pack(const FrameSource &s, const double half[3], const float zj[2], float *out,

@@ -94,8 +94,10 @@ typedef struct cil_frame_options {
 #define CIL_FRAME_TYPES_IN_FIRST 1
 
 /* Creates the GSD file (application "CIL", schema "hoomd" 1.1, OutputWriter.cpp:619) and the
- * device and pinned staging of the writer for one colony of h. The writer must be closed
- * before h is destroyed. */
+ * device and pinned staging of the writer for one colony of h, sized for the colony's
+ * capacity (28 bytes per element, twice on the device and twice in pinned memory). It may be
+ * called before the colony is uploaded, as the reference opens its output before the run
+ * (initializeOutput). The writer must be closed before h is destroyed. */
 cil_status cil_frame_open(cil_handle *h, int32_t colony, const char *path, const cil_frame_options *opt,
                           cil_frame_writer **out);
 
