@@ -166,3 +166,25 @@ def test_final_state_file_and_options(gpu_lib, tmp_path):
     assert np.all(z[1::2] == np.float32(1.0 * (-0.01 * 2.5)))
     assert int(f.read(1, "configuration/step")[0]) == 60
     eng.close()
+
+
+def test_writer_opened_before_upload(gpu_lib, tmp_path):
+    """The output opens before the colony is uploaded (initializeOutput precedes the run); the
+    2D box z is the largest uploaded diameter, read at the first frame."""
+    G = gpu_lib
+    p = S.growth_params(box=120.0, dt=1e-3, div_tau_mu=0.3, div_tau_sigma=0.03, apop_rate=0.0)
+    st = S.disk_colony(800, p, seed=14)
+    eng = G.Engine([p], [4 * len(st["sigma"])], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=2, skin=0.3)
+    path = str(tmp_path / "early.gsd")
+    w = eng.frame_writer(0, path)
+    eng.upload(0, **st)
+    exp0 = expected_frame(eng.download(0), p, 2, float(st["sigma"].max()))
+    w.write()
+    eng.step(20)
+    exp1 = expected_frame(eng.download(0), p, 2, float(st["sigma"].max()))
+    w.write()
+    w.close()
+    f = GSDFile(path)
+    check_frame(f, 0, exp0, 0, types=True, per_elem=True, charge=True)
+    check_frame(f, 1, exp1, 20, types=False, per_elem=True, charge=True)
+    eng.close()
