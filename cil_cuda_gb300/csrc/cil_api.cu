@@ -73,8 +73,6 @@ struct cil_handle {
   int64_t ts = 0;
   std::string err;
   cudaStream_t stream = nullptr;
-  cudaStream_t body_stream = nullptr;  // captures the conditional list-rebuild body of a graph
-  bool capturing = false;              // enqueue_step is being captured into a graph
 
   // device arrays
   ColonyConst *d_col = nullptr;
@@ -175,7 +173,6 @@ void free_all(cil_handle *h) {
   if (h->h_cnt) cudaFreeHost(h->h_cnt);
   for (auto e : h->evpool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
-  if (h->body_stream) cudaStreamDestroy(h->body_stream);
 }
 
 // bins per axis as LinkListOrtho::get_opt_size + reset (Utils.hpp:872-908)
@@ -625,39 +622,6 @@ cil_status check_counters(cil_handle *h, std::vector<ColonyCounters> *out = null
 // four events bracket the phases; a step being captured into a graph records none.
 cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cudaEvent_t before_force);
 
-// Appends to the graph being captured on h->stream: a one-thread kernel that sets the
-// condition (any colony rebuilds its lists this step) and an IF node whose body (captured on
-// h->body_stream) holds the rebin, bin-index and list kernels of a non-permuting rebuild.
-cil_status capture_rebuild_body(cil_handle *h, const RebuildArgs &ra) {
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t g = nullptr;
-  const cudaGraphNode_t *deps = nullptr;
-  size_t nd = 0;
-  CUDA_TRY(h, cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &g, &deps, nullptr, &nd));
-  if (cs != cudaStreamCaptureStatusActive) return fail(h, CIL_ERR_CUDA, "capture_rebuild_body: stream not capturing");
-  cudaGraphConditionalHandle cond;
-  CUDA_TRY(h, cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault));
-  launch_set_rebuild_cond(cond, h->d_anyreb, h->d_ts, h->stream);
-  CUDA_TRY(h, cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &g, &deps, nullptr, &nd));
-  cudaGraphNodeParams np{};
-  np.type = cudaGraphNodeTypeConditional;
-  np.conditional.handle = cond;
-  np.conditional.type = cudaGraphCondTypeIf;
-  np.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  CUDA_TRY(h, cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  CUDA_TRY(h, cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-  CUDA_TRY(h, cudaStreamBeginCaptureToGraph(h->body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->body_stream);
-  launch_rebuild(ra, h->grid_slots, h->body_stream);
-  launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->body_stream);
-  cudaGraph_t captured = nullptr;
-  CUDA_TRY(h, cudaStreamEndCapture(h->body_stream, &captured));
-  h->launches += 1;
-  return CIL_OK;
-}
-
 // One Euler step, or the two half steps of a Heun step (each: noise draw, bins or lists,
 // force pass with its position update), then the step counter and the events. Timed phases:
 // rebuild = the first pass's bins / lists; force = the rest up to the last force pass.
@@ -713,25 +677,16 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
       launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
     } else {
       launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
+      launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
       RebuildArgs ra = rebuild_args(h);
       ra.permute = 0;
       ra.skin = h->d_skin;  // only colonies with rebuild_now
       ra.any_rebuild = h->d_anyreb;
       ra.ts_dev = h->d_ts;
       ra.state_out = nullptr;
-      if (h->capturing) {
-        // in a captured step the rebin / bin index / list build run as the body of a
-        // conditional node, launched only when some colony rebuilds (each kernel would
-        // otherwise start and return at once on the other steps)
-        st = capture_rebuild_body(h, ra);
-        if (st != CIL_OK) return st;
-      } else {
-        launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
-        launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
-        launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
-      }
+      launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
     }
-    if (permute) launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
+    launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
     h->launches += permute ? 15 : 8;
@@ -844,9 +799,7 @@ cudaGraphExec_t steady_graph(cil_handle *h, int nsteps, bool last, int64_t *laun
     return nullptr;
   }
   cil_status sc = CIL_OK;
-  h->capturing = h->body_stream != nullptr;
   for (int i = 0; i < nsteps && sc == CIL_OK; ++i) sc = enqueue_step(h, last && i == nsteps - 1, false, 0);
-  h->capturing = false;
   const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
   HostStepState expect = before;
   for (int i = 0; i < nsteps; ++i) advance_host_state(h, &expect);
@@ -1023,10 +976,6 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
 
   cudaError_t e = cudaSetDevice(cfg->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess && cudaStreamCreateWithFlags(&h->body_stream, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaGetLastError();  // no conditional rebuild bodies: captured steps launch the kernels as before
-    h->body_stream = nullptr;
-  }
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, cfg->device);
   if (e != cudaSuccess) {
     h->err = cudaGetErrorString(e);

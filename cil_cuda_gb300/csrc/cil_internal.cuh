@@ -612,7 +612,6 @@ void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int 
                   cudaStream_t s);
 void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, cudaStream_t s);
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
-void launch_set_rebuild_cond(cudaGraphConditionalHandle cond, const int *any_rebuild, const int *ts, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
 void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);

@@ -524,17 +524,6 @@ void fresh_d(const SkinArgs &a, int law, cudaStream_t s) {
 
 }  // namespace
 
-namespace {
-// The condition of the list-rebuild body of a captured step: any colony rebuilds this step.
-__global__ void k_set_rebuild_cond(cudaGraphConditionalHandle cond, const int *any_rebuild, const int *ts) {
-  cudaGraphSetConditional(cond, any_rebuild[*ts & 1] != 0 ? 1u : 0u);
-}
-}  // namespace
-
-void launch_set_rebuild_cond(cudaGraphConditionalHandle cond, const int *any_rebuild, const int *ts, cudaStream_t s) {
-  k_set_rebuild_cond<<<1, 1, 0, s>>>(cond, any_rebuild, ts);
-}
-
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s) {
   k_skin_begin<<<(32 * a.B + 127) / 128, 128, 0, s>>>(a);
 }
