@@ -242,14 +242,16 @@ def run_batched(G, device, steps, warmup, sched):
 def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tune=None):
     """The same metric through the reference-facing calls with host buffers: upload the
     colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
-    call, each returning its status through a device->host read of the counters), and a GSD
+    call; every step's counters are read back to the host, and with CIL_FLAG_DEFERRED_STATUS
+    each call returns the previous call's status, so the host queues the next step while the
+    GPU runs this one), and a GSD
     frame every GTS steps written by the device-fed frame writer (outputFrame,
     OutputWriter.cpp:640-644; its copy to the host and its file writes overlap the next
     steps). The file is flushed and closed inside the timed region."""
     import tempfile
     n = len(st["sigma"])
     eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
-                   **(tune or {}))
+                   deferred_status=True, **(tune or {}))
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
     with tempfile.TemporaryDirectory() as tmp:

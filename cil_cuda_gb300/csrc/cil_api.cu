@@ -54,7 +54,10 @@ struct GraphSlot {
 
 struct cil_handle {
   cil_config cfg{};
-  ColonyCounters *h_cnt = nullptr;  // pinned host copy of d_cnt (cil_step's status read)
+  ColonyCounters *h_cnt = nullptr;  // pinned host copies of d_cnt (cil_step's status read), 2 x B
+  cudaEvent_t cnt_ev[2] = {nullptr, nullptr};  // deferred status: copy of each half done
+  int cnt_slot = 0;                  // deferred status: half the next copy goes to
+  int cnt_pending = -1;              // deferred status: half holding the previous call's copy
   int B = 0, D = 2;
   std::vector<HostColony> hc;
   std::vector<ColonyConst> cc;
@@ -171,6 +174,8 @@ void free_all(cil_handle *h) {
   h->graphs.clear();
   if (h->h_noise) cudaFreeHost(h->h_noise);
   if (h->h_cnt) cudaFreeHost(h->h_cnt);
+  for (auto e : h->cnt_ev)
+    if (e) cudaEventDestroy(e);
   for (auto e : h->evpool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
@@ -987,7 +992,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_col = dalloc<ColonyConst>(h->B);
   h->d_cnt = dalloc<ColonyCounters>(h->B);
   // pinned copy of the counters: the status read that ends every cil_step call
-  if (!h->h_cnt && cudaHostAlloc(&h->h_cnt, sizeof(ColonyCounters) * h->B, cudaHostAllocDefault) != cudaSuccess) {
+  if (!h->h_cnt && cudaHostAlloc(&h->h_cnt, 2 * sizeof(ColonyCounters) * h->B, cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
     h->h_cnt = nullptr;
   }
@@ -1199,6 +1204,24 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
     if (st != CIL_OK) return st;
     seg_graph.push_back(0);
     k += 1;
+  }
+  if ((h->cfg.flags & CIL_FLAG_DEFERRED_STATUS) && h->h_cnt) {
+    // the previous call's status; this call's counters are copied behind its launches
+    for (auto &e : h->cnt_ev)
+      if (!e) CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    const int slot = h->cnt_slot;
+    ColonyCounters *dst = h->h_cnt + static_cast<size_t>(slot) * h->B;
+    CUDA_TRY(h, cudaMemcpyAsync(dst, h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaEventRecord(h->cnt_ev[slot], h->stream));
+    cil_status prev = CIL_OK;
+    if (h->cnt_pending >= 0) {
+      CUDA_TRY(h, cudaEventSynchronize(h->cnt_ev[h->cnt_pending]));
+      prev = counter_status(h, h->h_cnt + static_cast<size_t>(h->cnt_pending) * h->B);
+    }
+    h->cnt_pending = slot;
+    h->cnt_slot = 1 - slot;
+    if (ts_out) *ts_out = h->ts;
+    return prev;
   }
   if (h->h_cnt)
     CUDA_TRY(h, cudaMemcpyAsync(h->h_cnt, h->d_cnt, sizeof(ColonyCounters) * h->B, cudaMemcpyDeviceToHost,

@@ -122,6 +122,14 @@ typedef struct cil_config {
  * launched steps only. */
 #define CIL_FLAG_NO_GRAPH 1
 
+/* cil_config.flags: cil_step returns once its launches and an asynchronous copy of the colony
+ * counters are enqueued, and reports the status of the previous call (whose copy it waits
+ * for), so that the host queues the next step while the GPU runs this one. The reference's
+ * mdStep returns nothing; its run_assert stops the run. Errors surface one call late; calls
+ * that read state (cil_download, cil_observables, ...) synchronise as always. cil_timings is
+ * not updated by such calls. */
+#define CIL_FLAG_DEFERRED_STATUS 2
+
 /* Host view of one colony in the reference layout. */
 typedef struct cil_colony_view {
   int32_t ncells;   /* upload: cells in the arrays; download: cells on the device */

@@ -74,3 +74,40 @@ def test_graphs_follow_buffers_allocated_between_calls(gpu_lib, growth):
     assert res[0]["ndiv_total"] > 0
     for k in ("ncells", "mean_area", "msd", "vacf"):
         assert res[0][k] == res[1][k], (k, res[0][k], res[1][k])
+
+
+def test_deferred_status(gpu_lib):
+    """CIL_FLAG_DEFERRED_STATUS: the same run, and a capacity overflow reported by the call
+    after the step that overflowed."""
+    G = gpu_lib
+    p = S.growth_params(box=80.0, dt=1e-3, div_tau_mu=0.02, div_tau_sigma=0.002, apop_rate=0.0)
+    st = S.disk_colony(600, p, seed=9)
+    res = []
+    for deferred in (False, True):
+        eng = G.Engine([p], [700], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=5, skin=0.3,
+                       deferred_status=deferred)
+        eng.upload(0, **st)
+        fail_at = None
+        for k in range(60):
+            try:
+                eng.step(1)
+            except G.CilError as e:
+                assert e.status == 3  # CIL_ERR_CAPACITY
+                fail_at = k
+                break
+        res.append(fail_at)
+        eng.close()
+    assert res[0] is not None and res[1] == res[0] + 1
+    out = []
+    for deferred in (False, True):
+        eng = G.Engine([p], [4000], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=5, skin=0.3,
+                       deferred_status=deferred)
+        eng.upload(0, **st)
+        for _ in range(40):
+            eng.step(1)
+        out.append(eng.download(0))
+        eng.close()
+    assert out[0]["ncells"] == out[1]["ncells"]
+    d = out[0]["pos"] - out[1]["pos"]
+    d -= np.round(d / 80.0) * 80.0
+    assert np.abs(d).max() < 1e-4
