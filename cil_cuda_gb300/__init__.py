@@ -452,7 +452,9 @@ class Engine:
         start = start[: nb + 1].copy()
         return ns, start, elems[: start[-1]].copy()
 
-    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch")) -> dict:
+    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch"), strict: bool = True) -> dict:
+        """The colony's state. strict=False keeps the state that a failed step left (its status
+        under "status") instead of raising."""
         cap = self.caps[colony]
         D = self.dim
         pos = np.zeros((cap, 2, D))
@@ -462,10 +464,15 @@ class Engine:
         tsw = np.zeros(cap, np.int32)
         v = ColonyView(ncells=0, capacity=cap, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig), vel=_dp(vel),
                        t0=_ip(t0), tswitch=_ip(tsw))
-        self._check(self.L.cil_download(self.h, colony, C.byref(v)))
+        st = self.L.cil_download(self.h, colony, C.byref(v))
+        if strict or st not in (3, 4, 5) or v.ncells > cap:
+            self._check(st)
         n = v.ncells
         out = dict(ncells=n, ts=v.ts, pos=pos[:n], sigma=sig[:n], vel=vel[:n], t0=t0[:n], tswitch=tsw[:n])
-        return {k: out[k] for k in out if k in want or k in ("ncells", "ts")}
+        out = {k: out[k] for k in out if k in want or k in ("ncells", "ts")}
+        if st != 0:
+            out["status"] = st
+        return out
 
     def obs_reset(self, colony: int = 0):
         self._check(self.L.cil_obs_reset(self.h, colony))

@@ -198,6 +198,8 @@ void grid_geometry(const cil_colony_params &p, double width, int *ns, bool *sing
 }
 
 double bin_width_for(const cil_handle *h, const HostColony &c) {
+  // a colony without cells stays without (nothing divides): one bin
+  if (!(c.sigma_max > 0.0)) return std::max(c.p.box[0], std::max(c.p.box[1], c.p.box[2]));
   const double need = c.p.rcut_scale * c.sigma_max + h->cfg.skin;
   return h->cfg.bin_width > need ? h->cfg.bin_width : need;
 }

@@ -167,7 +167,10 @@ void cil_destroy(cil_handle *h);
 cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *view);
 
 /* Copies one colony to the host at a frame boundary (outputFrame, OutputWriter.cpp:708).
- * CIL_ERR_CAPACITY if view->capacity is too small (view->ncells is set to the need). */
+ * CIL_ERR_CAPACITY if view->capacity is too small (view->ncells is set to the need). After a step
+ * that failed on a colony's counters (CIL_ERR_NAN, CIL_ERR_OUT_OF_BOX, CIL_ERR_CAPACITY) the view
+ * is still filled with the state that step left, which never holds more cells than the colony's
+ * capacity, and the call returns that status again. */
 cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *view);
 
 /* Advances every colony by nsteps Euler steps (MDIntegrator mdStep, MD.cuh:450-458;
