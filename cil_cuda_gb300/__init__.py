@@ -184,7 +184,8 @@ class RunInfo(C.Structure):
 
 
 FRAME_TYPES_IN_FIRST = 1
-APOP_NONE, APOP_CYCLE_PRESSURE, APOP_PRESSURE_TIME = 0, 1, 2
+APOP_NONE, APOP_CYCLE_PRESSURE, APOP_PRESSURE_TIME, APOP_RATE, APOP_CYCLE, APOP_CYCLE_EXTRUDE = 0, 1, 2, 3, 4, 5
+CYCLE_EULER, CYCLE_DPD = 0, 1
 
 CYCLE_FIELDS = [
     ("dim", C.c_int32), ("periodic", C.c_int32 * 3), ("box", C.c_double * 3), ("dt", C.c_double),
@@ -198,6 +199,8 @@ CYCLE_FIELDS = [
     ("cycle_p_shift", C.c_double), ("cycle_p_shift_tau", C.c_double), ("osmotic_pressure", C.c_double),
     ("apop_pressure", C.c_double), ("apop_duration", C.c_double), ("apop_rate", C.c_double),
     ("extr_gamma", C.c_double), ("drain", C.c_int32), ("precision", C.c_int32),
+    ("integrator", C.c_int32), ("pad", C.c_int32), ("mass", C.c_double), ("kbt", C.c_double),
+    ("dis_same", C.c_double), ("dis_diff", C.c_double), ("dis_bg", C.c_double), ("extr_rate", C.c_double),
 ]
 
 
@@ -219,7 +222,8 @@ def cycle_params(**kw) -> CycleParams:
                 cycle_tau_r=1.0, cycle_tau_v=1.0, cycle_tau_p=0.0, cycle_sigma_min=1.1283791670955126, cycle_p0=5.0,
                 cycle_beta_vs=0.0, cycle_rho_ratio=1.0, cycle_r_maxed=1.0, cycle_p_shift=0.0, cycle_p_shift_tau=0.0,
                 osmotic_pressure=0.0, apop_pressure=1.0, apop_duration=8.0, apop_rate=0.0, extr_gamma=0.0, drain=0,
-                precision=0)
+                precision=0, integrator=CYCLE_EULER, pad=0, mass=1.0, kbt=0.0, dis_same=0.0, dis_diff=0.0,
+                dis_bg=0.0, extr_rate=0.0)
     base.update(kw)
     q = CycleParams()
     for k, v in base.items():
@@ -801,7 +805,7 @@ class CycleEngine:
             raise CilError(st, buf.value.decode())
 
     def upload(self, pos, sigma=None, sigma_t=None, theta=None, rho=None, angvel=None, pressure=None,
-               tpressure=None, ts: int = 0):
+               tpressure=None, ts: int = 0, vel=None):
         pos = np.ascontiguousarray(pos, np.float64)
         n = pos.shape[0]
         keep = []
@@ -813,7 +817,7 @@ class CycleEngine:
             keep.append(a)
             return a.ctypes.data_as(C.POINTER(C.c_double if dt == np.float64 else C.c_int32))
 
-        v = CycleView(ncells=n, capacity=n, ts=ts, pad=0, pos=_dp(pos), vel=None, sigma=ptr(sigma),
+        v = CycleView(ncells=n, capacity=n, ts=ts, pad=0, pos=_dp(pos), vel=ptr(vel), sigma=ptr(sigma),
                       sigma_t=ptr(sigma_t), theta=ptr(theta), rho=ptr(rho), angvel=ptr(angvel),
                       pressure=ptr(pressure), tpressure=ptr(tpressure, np.int32))
         self._check(self.L.cil_cycle_upload(self.h, C.byref(v)))

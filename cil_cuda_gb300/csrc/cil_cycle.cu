@@ -16,6 +16,10 @@
 //   cycle      k_cy_cycle (ODEs, division flag, per-block count) / k_cy_scan_blocks /
 //              k_cy_divide (daughters appended in mother order);
 //   apoptosis  k_cy_apo_mark / scan / k_cy_compact (only with apoptosis on).
+// The DPD integrator: k_dpd_kick_drift (first half kick and the drift), the bins, k_cy_force in
+// its forces-only mode (Fc and the pressure), k_dpd_pair (the pair dissipative and random
+// forces and the second half kick, into the spare velocity buffer), k_dpd_dis (background and
+// pair dissipation at the new velocities), then the same cycle and apoptosis kernels.
 // The file is compiled without FMA contraction, so that the arithmetic is that of the host
 // restatement the tests compare with.
 #include <cuda_runtime.h>
@@ -40,6 +44,8 @@ constexpr int kScanTile = 1024;  // elements per block of the scans
 
 // Philox purposes (third counter word)
 constexpr uint32_t kCyNoise = 11, kCyDir = 12, kCyDiv = 13, kCyApo = 14, kCyInit = 15;
+// DPD pair normals: counter (lower cell index, step, purpose, higher cell index)
+constexpr uint32_t kCyDpd0 = 16, kCyDpd1 = 17;
 
 struct CyConst {
   int D;
@@ -63,6 +69,12 @@ struct CyConst {
   double p0, beta_vs, rho_ratio, r_maxed_inv, p_shift, p_shift_tau_inv, osm;
   double apop_pressure, apop_duration, apop_rate_step, extr_gamma;
   double apop_steps;  // apop_duration / dt
+  double extr_rate;
+  // DPD
+  int dpd;
+  double kick_div;    // 2 (2 m): updateVel's divisor with the mass argument 2 m
+  double sqrt_dt;
+  double gamma_d, gamma_b, sigma_r;  // DISDIFCEL, DISBG, sqrt(2 DISDIFCEL kT)
   uint32_t seed_lo, seed_hi;
   int capacity;
 };
@@ -72,6 +84,7 @@ struct CySet {
   double *v;      // [D][cap]
   double *sig, *sigt, *theta, *rho, *om, *p;
   int *tp, *t0, *tsw;
+  double *fc, *fd, *fr;  // [D][cap], DPD only (conservative, dissipative, random forces)
 };
 
 struct CyCounters {
@@ -158,6 +171,65 @@ __device__ inline int bin_of(const CyConst &C, const double *xd) {
     b = b * C.ns[d] + v;
   }
   return b;
+}
+
+// The bins around a cell that hold every cell within `radius` of it: k = ceil(radius / bin
+// width) bins on each side, the whole axis (each bin once) when 2k + 1 covers it, clipped at
+// non-periodic walls.
+struct Stencil {
+  int bi[3], lo[3], hi[3];
+};
+
+__device__ inline void stencil_of(const CyConst &C, const double *xi, double radius, Stencil &s) {
+  for (int d = 0; d < 3; ++d) s.bi[d] = s.lo[d] = s.hi[d] = 0;
+  for (int d = 0; d < C.D; ++d) {
+    int v = static_cast<int>(xi[d] * C.inv_bw[d]);
+    v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
+    s.bi[d] = v;
+    const double kk = ceil(radius * C.inv_bw[d]);
+    const int k = (kk >= 0.0 && kk < C.ns[d]) ? static_cast<int>(kk) : C.ns[d];
+    if (2 * k + 1 >= C.ns[d]) {
+      s.lo[d] = -s.bi[d];
+      s.hi[d] = C.ns[d] - 1 - s.bi[d];
+    } else if (C.periodic[d]) {
+      s.lo[d] = -k;
+      s.hi[d] = k;
+    } else {
+      s.lo[d] = s.bi[d] - k < 0 ? -s.bi[d] : -k;
+      s.hi[d] = s.bi[d] + k >= C.ns[d] ? C.ns[d] - 1 - s.bi[d] : k;
+    }
+  }
+}
+
+__device__ inline int stencil_bin(const CyConst &C, const Stencil &s, int o0, int o1, int o2) {
+  const int oo[3] = {o0, o1, o2};
+  int b = 0;
+  for (int d = 0; d < C.D; ++d) {
+    int v = s.bi[d] + oo[d];
+    if (v < 0) v += C.ns[d];
+    if (v >= C.ns[d]) v -= C.ns[d];
+    b = b * C.ns[d] + v;
+  }
+  return b;
+}
+
+// r_j - r_i at the nearest image (|dd| < L, so Nint(dd / L) is -1, 0 or 1; the two forms differ
+// only at |dd| = L/2, far beyond any contact); returns |r_j - r_i|^2
+__device__ inline double separation(const CyConst &C, const CySet &S, const double *xi, int j, double *rij) {
+  const size_t cap = C.capacity;
+  double r2 = 0.0;
+  for (int d = 0; d < C.D; ++d) {
+    double dd = S.x[d * cap + j] - xi[d];
+    if (C.periodic[d]) {
+      if (dd > C.half[d])
+        dd -= C.box[d];
+      else if (dd < -C.half[d])
+        dd += C.box[d];
+    }
+    rij[d] = dd;
+    r2 += dd * dd;
+  }
+  return r2;
 }
 
 // ---------------------------------------------------------------- block scan
@@ -276,14 +348,17 @@ __global__ void k_cy_sort(const int *start, int nbins, int *list, CyCounters *cn
 // runs FP64 at a small fraction of its FP32 rate); the forces and the pressure are summed in
 // FP32 over the contacts and added to the FP64 motility and noise; the position update and
 // the cell state stay FP64.
+// mode 0 (Euler): the position update with the pressure-dependent friction follows, into x_out,
+// and the velocity; mode 1 (DPD): the force goes to frc and nothing moves. Draws are keyed by
+// the device step counter + key_off.
 template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
                                                     CyCounters *cnt, const int *start, const int *list,
-                                                    const int *ts_dev) {
+                                                    const int *ts_dev, int mode, int key_off) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = cnt->n;
   if (i >= n) return;
-  const int ts = *ts_dev;
+  const int ts = *ts_dev + key_off;
   const size_t cap = C.capacity;
   const int D = C.D;
   double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, F[3] = {0, 0, 0};
@@ -327,66 +402,29 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   // ---- Hertz contacts with adhesion and the pressure (device draft, MD.cu:302-366)
   double pres = 0.0;
   {
-    int bi[3] = {0, 0, 0};
-    {
-      int b = 0;
-      for (int d = 0; d < D; ++d) {
-        int v = static_cast<int>(xi[d] * C.inv_bw[d]);
-        v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
-        bi[d] = v;
-        b = b * C.ns[d] + v;
-      }
-      (void)b;
-    }
     // bins to search on each side: the largest diameter of the colony over the bin width
-    const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int d = 0; d < D; ++d) {
-      const double kk = ceil(smax * C.inv_bw[d]);
-      const int k = (kk >= 0.0 && kk < C.ns[d]) ? static_cast<int>(kk) : C.ns[d];
-      if (2 * k + 1 >= C.ns[d]) {  // the whole axis, each bin once
-        lo[d] = -bi[d];
-        hi[d] = C.ns[d] - 1 - bi[d];
-      } else if (C.periodic[d]) {
-        lo[d] = -k;
-        hi[d] = k;
-      } else {
-        lo[d] = bi[d] - k < 0 ? -bi[d] : -k;
-        hi[d] = bi[d] + k >= C.ns[d] ? C.ns[d] - 1 - bi[d] : k;
-      }
-    }
+    Stencil st;
+    stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
     const double c2 = C.hz_c + C.hz_c;
     const double inv_ri = 1.0 / (si / 2);
     const float sif = static_cast<float>(si), c2f = static_cast<float>(c2), adhf = static_cast<float>(C.adhesion);
     const float inv_rif = 2.0f / sif;
     float Ff[3] = {0.0f, 0.0f, 0.0f}, presf = 0.0f;
-    for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
-      for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
-        for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
-          const int oo[3] = {o0, o1, o2};
-          int b = 0;
-          for (int d = 0; d < D; ++d) {
-            int v = bi[d] + oo[d];
-            if (v < 0) v += C.ns[d];
-            if (v >= C.ns[d]) v -= C.ns[d];
-            b = b * C.ns[d] + v;
-          }
+    for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
+      for (int o1 = (D > 1 ? st.lo[1] : 0); o1 <= (D > 1 ? st.hi[1] : 0); ++o1)
+        for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
+          const int b = stencil_bin(C, st, o0, o1, o2);
           const int e0 = start[b], e1 = start[b + 1];
           for (int q = e0; q < e1; ++q) {
             const int j = list[q];
             if (j == i) continue;
+            double rij[3] = {0, 0, 0};
+            const double r2 = separation(C, S, xi, j, rij);
             if (MIXED) {
               float df[3] = {0.0f, 0.0f, 0.0f};
               float r2f = 0.0f;
               for (int d = 0; d < D; ++d) {
-                double dd = S.x[d * cap + j] - xi[d];
-                if (C.periodic[d]) {
-                  if (dd > C.half[d])
-                    dd -= C.box[d];
-                  else if (dd < -C.half[d])
-                    dd += C.box[d];
-                }
-                df[d] = static_cast<float>(dd);
+                df[d] = static_cast<float>(rij[d]);
                 r2f += df[d] * df[d];
               }
               const float sjf = static_cast<float>(S.sig[j]);
@@ -414,21 +452,6 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
               if (vol != 0.0f) presf -= f0 / vol;
               for (int d = 0; d < D; ++d) Ff[d] += f0 * df[d];
               continue;
-            }
-            double rij[3] = {0, 0, 0};
-            double r2 = 0.0;
-            for (int d = 0; d < D; ++d) {
-              // nearest image: |dd| < L, so Nint(dd / L) is -1, 0 or 1; the two forms differ
-              // only at |dd| = L/2, far beyond any contact
-              double dd = S.x[d * cap + j] - xi[d];
-              if (C.periodic[d]) {
-                if (dd > C.half[d])
-                  dd -= C.box[d];
-                else if (dd < -C.half[d])
-                  dd += C.box[d];
-              }
-              rij[d] = dd;
-              r2 += dd * dd;
             }
             const double sj = S.sig[j];
             const double cut = (si + sj) / 2;
@@ -458,21 +481,143 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
       for (int d = 0; d < D; ++d) F[d] += static_cast<double>(Ff[d]);
     }
   }
+  bool finite = true;
+  for (int d = 0; d < D; ++d) finite = finite && isfinite(F[d]);
+  S.p[i] = pres;
+  if (!finite) atomicOr(&cnt->err, kErrNonFinite);
+  if (mode == 1) {
+    for (int d = 0; d < D; ++d) frc[d * cap + i] = F[d];
+    return;
+  }
   // ---- position update with the pressure-dependent friction (CIL.cu:902-939)
   const double pnd = pres / C.p0;
   // pow(x, 0) is 1 for every x
   const double pw = C.zeta_p_beta == 0.0 ? 1.0 : pow(pnd, C.zeta_p_beta);
   const double temp = C.dt * 1 / ((C.zeta + C.zeta_p * pw) * area_of(si));
-  bool finite = true;
   for (int d = 0; d < D; ++d) {
-    finite = finite && isfinite(F[d]);
     const double t = xi[d] + temp * F[d];
     x_out[d * cap + i] = C.periodic[d] ? wrap(t, C.box[d]) : t;
     S.v[d * cap + i] = F[d] * (temp / C.dt);
     if (frc) frc[d * cap + i] = F[d];
   }
-  S.p[i] = pres;
+}
+
+// ---------------------------------------------------------------- DPD
+__device__ inline double kick(const CyConst &C, double v, double fc, double fd, double fr) {
+  return v + (fc * C.dt + fd * C.dt + fr * C.sqrt_dt) / C.kick_div;  // updateVel (Utils.hpp:568-571)
+}
+
+// updateVelocities then updatePositions (CIL.cu:871-897, 849-866; DPD step, CIL.cu:1055-1056)
+__global__ void __launch_bounds__(kTile) k_dpd_kick_drift(CyConst C, CySet S, const CyCounters *cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt->n) return;
+  const size_t cap = C.capacity;
+  for (int d = 0; d < C.D; ++d) {
+    const size_t k = d * cap + i;
+    const double v = kick(C, S.v[k], S.fc[k], S.fd[k], S.fr[k]);
+    S.v[k] = v;
+    const double x = S.x[k];
+    S.x[k] = C.periodic[d] ? wrap(x + C.dt * v, C.box[d]) : x + v * C.dt;  // BoundingBox::updatePos
+  }
+}
+
+// Pair dissipative and random forces (cellCellDisRanForce, MD.cu:861-905) over the pairs closer
+// than the lower-index cell's diameter; then, with `kick`, the second half kick into v_out.
+__global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *v_out, CyCounters *cnt,
+                                                    const int *start, const int *list, const int *ts_dev,
+                                                    int key_off, int kick_on) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  if (i >= n) return;
+  const uint32_t ts = static_cast<uint32_t>(*ts_dev + key_off);
+  const size_t cap = C.capacity;
+  const int D = C.D;
+  double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, Fd[3] = {0, 0, 0}, Fr[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) {
+    xi[d] = S.x[d * cap + i];
+    vi[d] = S.v[d * cap + i];
+  }
+  const double si = S.sig[i];
+  Stencil st;
+  stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
+  for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
+    for (int o1 = (D > 1 ? st.lo[1] : 0); o1 <= (D > 1 ? st.hi[1] : 0); ++o1)
+      for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
+        const int b = stencil_bin(C, st, o0, o1, o2);
+        for (int q = start[b]; q < start[b + 1]; ++q) {
+          const int j = list[q];
+          if (j == i) continue;
+          double rij[3] = {0, 0, 0};
+          const double r = sqrt(separation(C, S, xi, j, rij));
+          const double rc = i < j ? si : S.sig[j];
+          if (!(r < rc) || r == 0.0) continue;
+          const double w = 1 - (r / rc);
+          const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
+          double xi_n[4];
+          normal2(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xi_n[0], &xi_n[1]);
+          if (D == 3) normal2(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xi_n[2], &xi_n[3]);
+          const double sw = sqrt(w);
+          for (int d = 0; d < D; ++d) {
+            const double nd = rij[d] / r;
+            const double vj = S.v[d * cap + j];
+            Fd[d] -= C.gamma_d * w * ((vi[d] - vj) * nd) * nd;
+            Fr[d] += C.sigma_r * sw * nd * xi_n[d];
+          }
+        }
+      }
+  bool finite = true;
+  for (int d = 0; d < D; ++d) {
+    const size_t k = d * cap + i;
+    S.fd[k] = Fd[d];
+    S.fr[k] = Fr[d];
+    if (kick_on) {
+      const double v = kick(C, vi[d], S.fc[k], Fd[d], Fr[d]);
+      v_out[k] = v;
+      finite = finite && isfinite(v);
+    }
+  }
   if (!finite) atomicOr(&cnt->err, kErrNonFinite);
+}
+
+// Background and pair dissipation at the new velocities (calculDisForces, CIL.cu:294-364:
+// sameCellDisForce zeroes a single-element cell's Fd, cellBackDisForce subtracts gamma_bg v,
+// cellCellDisForce, MD.cu:951-985, with w = 1 - r^2 / sigma_core for r < sigma_core)
+__global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyCounters *cnt, const int *start,
+                                                   const int *list) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = cnt->n;
+  if (i >= n) return;
+  const size_t cap = C.capacity;
+  const int D = C.D;
+  double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, Fd[3] = {0, 0, 0};
+  for (int d = 0; d < D; ++d) {
+    xi[d] = S.x[d * cap + i];
+    vi[d] = S.v[d * cap + i];
+    Fd[d] = 0;
+    Fd[d] -= C.gamma_b * vi[d];
+  }
+  const double rc = C.sigma_core;
+  const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
+  Stencil st;
+  stencil_of(C, xi, smax > rc ? smax : rc, st);
+  for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
+    for (int o1 = (D > 1 ? st.lo[1] : 0); o1 <= (D > 1 ? st.hi[1] : 0); ++o1)
+      for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
+        const int b = stencil_bin(C, st, o0, o1, o2);
+        for (int q = start[b]; q < start[b + 1]; ++q) {
+          const int j = list[q];
+          if (j == i) continue;
+          double rij[3] = {0, 0, 0};
+          const double r = sqrt(separation(C, S, xi, j, rij));
+          if (!(r < rc) || r == 0.0) continue;
+          const double w = 1 - ((r * r) / rc);
+          for (int d = 0; d < D; ++d) {
+            const double nd = -rij[d] / r;
+            Fd[d] -= C.gamma_d * w * ((vi[d] - S.v[d * cap + j]) * nd) * nd;
+          }
+        }
+      }
+  for (int d = 0; d < D; ++d) S.fd[d * cap + i] = Fd[d];
 }
 
 // ---------------------------------------------------------------- cell cycle and divisions
@@ -585,6 +730,10 @@ __global__ void __launch_bounds__(kTile) k_cy_divide(CyConst C, CySet S, CyCount
         S.x[d * cap + i] = xm;
         S.v[d * cap + inew] = 0.0;
         S.v[d * cap + i] = 0.0;
+        if (S.fc) {  // resetFrc (CIL.cu:597-598)
+          S.fc[d * cap + inew] = S.fd[d * cap + inew] = S.fr[d * cap + inew] = 0.0;
+          S.fc[d * cap + i] = S.fd[d * cap + i] = S.fr[d * cap + i] = 0.0;
+        }
       }
       // cycle times: migration spans (daughter, then mother), log-normal cycle speeds (mother,
       // then daughter), as the reference draws them
@@ -624,7 +773,8 @@ __global__ void k_cy_reset_smax(CyCounters *cnt) { cnt->sigma_max_bits = 0ull; }
 __global__ void k_cy_advance(int *ts) { *ts += 1; }
 
 // ---------------------------------------------------------------- removals
-// mode 1: apoptosis (CyclePressure or PressureTime law); mode 2: outside the box (drain)
+// mode 1: apoptosis (the law of C.apoptosis, one Philox block per cell and step); mode 2:
+// outside the box (drain)
 __global__ void __launch_bounds__(kTile) k_cy_mark(CyConst C, CySet S, CyCounters *cnt, const int *ts_dev,
                                                    int mode, int *keep, int *block_count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -636,13 +786,24 @@ __global__ void __launch_bounds__(kTile) k_cy_mark(CyConst C, CySet S, CyCounter
       const int ts = *ts_dev;
       const u32x4 r = draw(C, i, ts, kCyApo, 0);
       const double u = u53(r.v[0], r.v[1]);
+      const double rho = S.rho[i];
       if (C.apoptosis == CIL_APOP_CYCLE_PRESSURE) {
         const double p = S.p[i];
-        const double rate = C.apop_rate_step * pow((1 - (S.rho[i] / C.apop_pressure)), C.apop_duration) *
+        const double rate = C.apop_rate_step * pow((1 - (rho / C.apop_pressure)), C.apop_duration) *
                             pow(p / (p + C.p0), C.extr_gamma);
         if (u <= rate) k = 0;
-      } else {
+      } else if (C.apoptosis == CIL_APOP_PRESSURE_TIME) {
         if (((C.apop_duration > 0) && (S.tp[i] >= C.apop_steps)) || ((C.apop_rate_step > 0) && (u <= C.apop_rate_step)))
+          k = 0;
+      } else if (C.apoptosis == CIL_APOP_RATE) {
+        if (u <= C.apop_rate_step) k = 0;
+      } else if (C.apoptosis == CIL_APOP_CYCLE) {
+        if (rho < 1 && u <= C.apop_rate_step * pow((1 - (rho / C.apop_pressure)), C.apop_duration)) k = 0;
+      } else {  // CIL_APOP_CYCLE_EXTRUDE
+        if (rho < 1 && u <= C.apop_rate_step) k = 0;
+        const double u2 = u53(r.v[2], r.v[3]);
+        if (rho <= 0.1 &&
+            u2 <= C.extr_rate * pow(((S.p[i] - C.apop_pressure) / C.apop_pressure), C.extr_gamma))
           k = 0;
       }
     } else {
@@ -670,6 +831,11 @@ __global__ void __launch_bounds__(kTile) k_cy_compact(CyConst C, CySet A, CySet 
   for (int d = 0; d < C.D; ++d) {
     B.x[d * cap + dst] = A.x[d * cap + i];
     B.v[d * cap + dst] = A.v[d * cap + i];
+    if (A.fc) {
+      B.fc[d * cap + dst] = A.fc[d * cap + i];
+      B.fd[d * cap + dst] = A.fd[d * cap + i];
+      B.fr[d * cap + dst] = A.fr[d * cap + i];
+    }
   }
   B.sig[dst] = A.sig[i];
   B.sigt[dst] = A.sigt[i];
@@ -744,6 +910,7 @@ struct cil_cycle {
   CySet set[2] = {};
   int cur = 0;
   double *xs = nullptr;   // position output buffer of the force pass
+  double *vs = nullptr;   // velocity output buffer of the DPD pair pass
   double *frc = nullptr;  // last forces (output only)
   CyCounters *cnt = nullptr;
   CyCounters *h_cnt = nullptr;  // pinned
@@ -785,10 +952,20 @@ namespace {
 
 cil_status check_params(const cil_cycle_params *p) {
   if (p->dim != 2 && p->dim != 3) return CIL_ERR_CONFIG;
-  if (!(p->dt > 0.0) || !(p->sigma_core > 0.0) || !(p->E > 0.0) || !(p->zeta > 0.0)) return CIL_ERR_CONFIG;
+  if (!(p->dt > 0.0) || !(p->sigma_core > 0.0) || !(p->E > 0.0)) return CIL_ERR_CONFIG;
   for (int d = 0; d < p->dim; ++d)
     if (!(p->box[d] > 0.0)) return CIL_ERR_CONFIG;
-  if (p->apoptosis < CIL_APOP_NONE || p->apoptosis > CIL_APOP_PRESSURE_TIME) return CIL_ERR_CONFIG;
+  if (p->integrator == CIL_CYCLE_EULER) {
+    if (!(p->zeta > 0.0)) return CIL_ERR_CONFIG;  // "In Euler, zeta should > 0!!!" (CIL.cu:924)
+  } else if (p->integrator == CIL_CYCLE_DPD) {
+    // the reference's DPD step draws no passive noise (NOISE_ON is set by the stochastic
+    // integrators only, Input.cpp:527-535)
+    if (!(p->mass > 0.0) || !(p->kbt >= 0.0) || !(p->dis_diff >= 0.0) || !(p->dis_bg >= 0.0) || p->noise_D != 0.0)
+      return CIL_ERR_CONFIG;
+  } else {
+    return CIL_ERR_CONFIG;
+  }
+  if (p->apoptosis < CIL_APOP_NONE || p->apoptosis > CIL_APOP_CYCLE_EXTRUDE) return CIL_ERR_CONFIG;
   if (p->precision != 0 && p->precision != 1) return CIL_ERR_CONFIG;
   if (p->divide && (!(p->tau_div_mu > 0.0) || !(p->cycle_p0 != 0.0) || !(p->cycle_sigma_min > 0.0) ||
                     !(p->cycle_tau_r > 0.0) || !(p->cycle_tau_v > 0.0)))
@@ -836,18 +1013,47 @@ cil_status removals(cil_cycle *h, int mode) {
   return CIL_OK;
 }
 
-cil_status enqueue_step(cil_cycle *h) {
+void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, int key_off) {
+  const int g = blocks_for(h->cap);
+  if (h->p.precision == 1)
+    k_cy_force<true><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
+                                                 key_off);
+  else
+    k_cy_force<false><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
+                                                  key_off);
+  h->launches += 1;
+}
+
+// Fc, pressure, Fd and Fr at the current positions and velocities (the forces the reference
+// evaluates before its first step, CIL.cu:1096), draws keyed by the current step counter
+void dpd_initial_forces(cil_cycle *h) {
+  CySet &S = h->set[h->cur];
+  const int g = blocks_for(h->cap);
   bin_cells(h);
+  launch_force(h, S, nullptr, S.fc, 1, 0);
+  k_dpd_pair<<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, 0, 0);
+  h->launches += 1;
+}
+
+cil_status enqueue_step(cil_cycle *h) {
   const int g = blocks_for(h->cap);
   CySet &S = h->set[h->cur];
-  if (h->p.precision == 1)
-    k_cy_force<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
-  else
-    k_cy_force<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->xs, h->frc, h->cnt, h->bstart, h->list, h->ts_dev);
-  std::swap(S.x, h->xs);
+  if (h->C.dpd) {  // DPD (CIL.cu:1054-1066); this step's draws are keyed by ts + 1
+    k_dpd_kick_drift<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt);
+    bin_cells(h);
+    launch_force(h, S, nullptr, S.fc, 1, 1);
+    k_dpd_pair<<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, 1, 1);
+    std::swap(S.v, h->vs);
+    k_dpd_dis<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
+    h->launches += 3;
+  } else {
+    bin_cells(h);
+    launch_force(h, S, h->xs, h->frc, 0, 0);
+    std::swap(S.x, h->xs);
+  }
   k_cy_advance<<<1, 1, 0, h->stream>>>(h->ts_dev);
   h->ts += 1;
-  h->launches += 2;
+  h->launches += 1;
   if (h->C.divide) {
     k_cy_cycle<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk);
     k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
@@ -948,6 +1154,13 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
   C.apop_rate_step = p->apop_rate * p->dt;
   C.extr_gamma = p->extr_gamma;
   C.apop_steps = p->apop_duration / p->dt;
+  C.extr_rate = p->extr_rate;
+  C.dpd = p->integrator == CIL_CYCLE_DPD ? 1 : 0;
+  C.kick_div = 2 * (2 * p->mass);
+  C.sqrt_dt = std::sqrt(p->dt);
+  C.gamma_d = p->dis_diff;
+  C.gamma_b = p->dis_bg;
+  C.sigma_r = std::sqrt(2 * p->dis_diff * p->kbt);  // Sigma (MD.cu:872)
   C.seed_lo = static_cast<uint32_t>(seed);
   C.seed_hi = static_cast<uint32_t>(seed >> 32);
 
@@ -968,6 +1181,16 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     S.t0 = h->alloc<int>(cap);
     S.tsw = h->alloc<int>(cap);
     ok = S.x && S.v && S.sig && S.sigt && S.theta && S.rho && S.om && S.p && S.tp && S.t0 && S.tsw;
+    if (ok && C.dpd) {
+      S.fc = h->alloc<double>(D * cap);
+      S.fd = h->alloc<double>(D * cap);
+      S.fr = h->alloc<double>(D * cap);
+      ok = S.fc && S.fd && S.fr;
+    }
+  }
+  if (ok && C.dpd) {
+    h->vs = h->alloc<double>(D * cap);
+    ok = h->vs != nullptr;
   }
   h->nblocks = blocks_for(capacity);
   h->nparts = (h->nbins + kScanTile - 1) / kScanTile + 1;
@@ -1029,6 +1252,10 @@ cil_status cil_cycle_upload(cil_cycle *h, const cil_cycle_view *v) {
     }
     CY_TRY(h, cudaMemcpy(S.x + d * cap, t.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     CY_TRY(h, cudaMemset(S.v + d * cap, 0, sizeof(double) * cap));
+    if (v->vel) {
+      for (int i = 0; i < n; ++i) t[i] = v->vel[static_cast<size_t>(i) * D + d];
+      CY_TRY(h, cudaMemcpy(S.v + d * cap, t.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
   }
   auto up = [&](double *dst, const double *src) -> cudaError_t {
     return src ? cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice) : cudaSuccess;
@@ -1054,10 +1281,11 @@ cil_status cil_cycle_upload(cil_cycle *h, const cil_cycle_view *v) {
     CY_TRY(h, cudaMemcpy(S.tp, v->tpressure, sizeof(int) * n, cudaMemcpyHostToDevice));
   }
   k_cy_sigma_max<<<blocks_for(h->cap), kTile, 0, h->stream>>>(h->C, S, h->cnt);
+  if (h->C.dpd) dpd_initial_forces(h);
   CY_TRY(h, cudaGetLastError());
   CY_TRY(h, cudaStreamSynchronize(h->stream));
   h->uploaded = true;
-  return CIL_OK;
+  return h->C.dpd ? read_counters(h) : CIL_OK;
 }
 
 cil_status cil_cycle_step(cil_cycle *h, int32_t nsteps, int64_t *ts) {

@@ -20,8 +20,32 @@
  *     two of volume v/2 placed +-dr around it (singleCellDivision, MD.cu:664-700), both with
  *     theta = 0 and new cycle speeds 1 / lognormal(tau_div) (randomTimeSpanLogNormal,
  *     MD.cuh:438-440);
- *   apoptosis (calculApoptosisCyclePressure, CIL.cu:711-738; the PressureTime law of the DPD
- *     integrator, CIL.cu:653-676, is selectable).
+ *   apoptosis (calculApoptosisCyclePressure, CIL.cu:711-738; the reference's other laws are
+ *     selectable: PressureTime, CIL.cu:653-676, which its DPD step applies; the constant rate,
+ *     CIL.cu:627-649; Cycle, CIL.cu:681-709; CycleExtrude, CIL.cu:749-788).
+ *
+ * The reference's DPD step (CIL.cu:1054-1066) is the other integrator (CIL_CYCLE_DPD): cells
+ * carry a velocity, a mass and three forces (conservative Fc, dissipative Fd, random Fr), and a
+ * step is
+ *   v += (Fc dt + Fd dt + Fr sqrt(dt)) / (4m); x += v dt           (updateVelocities passes
+ *     2m as the mass to updateVel, which divides by twice the mass: CIL.cu:894, Utils.hpp:568-571;
+ *     updatePositions, CIL.cu:849-866)
+ *   Fc, pressure: motility along v and the Hertz contacts as above; Fd, Fr over the pairs with
+ *     r < sigma_a (sigma_a: the diameter of the pair's lower-index cell), w = 1 - r / sigma_a:
+ *     Fd_i,d -= gamma w (v_i,d - v_j,d) n_d n_d, Fr_i,d += sqrt(2 gamma kT) sqrt(w) n_d xi_d,
+ *     n the unit vector from i to j, one standard normal xi_d per pair and axis shared by the
+ *     two cells (cellCellDisRanForce, MD.cu:861-905)
+ *   v += (Fc dt + Fd dt + Fr sqrt(dt)) / (4m)
+ *   Fd = -gamma_bg v_i - sum over r < sigma_core of gamma (1 - r^2 / sigma_core)(v_i,d - v_j,d)
+ *     n_d n_d (calculDisForces, CIL.cu:294-364; cellBackDisForce, MD.cu:846-859;
+ *     cellCellDisForce, MD.cu:951-985)
+ *   ++ts, cell cycle and divisions (both cells of a division restart at rest with zero forces,
+ *     CIL.cu:593-598), apoptosis.
+ * cil_cycle_upload evaluates Fc, Fd and Fr once at the uploaded positions and velocities, as
+ * the reference does before its first step (CIL.cu:1096). Where the reference's DPD loops are
+ * not well defined, this is what they compute with every pair visited once: they never reset
+ * the random force (it sums over all steps), apply the background term once per neighbour
+ * bin, and let OpenMP threads reset and add to one cell's forces at the same time.
  *
  * Random draws are counter-based (Philox4x32-10 keyed by seed, step, cell index and purpose),
  * so runs are reproducible and independent of the launch configuration; the reference draws
@@ -44,8 +68,19 @@ extern "C" {
 enum {
   CIL_APOP_NONE = 0,
   CIL_APOP_CYCLE_PRESSURE = 1, /* calculApoptosisCyclePressure (Euler, CIL.cu:711-738) */
-  CIL_APOP_PRESSURE_TIME = 2   /* calculApoptosisPressureTime (DPD, CIL.cu:653-676) */
+  CIL_APOP_PRESSURE_TIME = 2,  /* calculApoptosisPressureTime (DPD, CIL.cu:653-676) */
+  CIL_APOP_RATE = 3,           /* calculApoptosis (Heun, CIL.cu:627-649): u <= apop_rate dt */
+  CIL_APOP_CYCLE = 4,          /* calculApoptosisCycle (CIL.cu:681-709): cells with rho < 1,
+                                * u <= apop_rate dt (1 - rho / apop_pressure)^apop_duration
+                                * (the reference's loop never advances past a cell with
+                                * rho >= 1; such a cell is kept) */
+  CIL_APOP_CYCLE_EXTRUDE = 5   /* calculApoptosisCycleExtrude (CIL.cu:749-788): rho < 1 and
+                                * u1 <= apop_rate dt, or rho <= 0.1 and
+                                * u2 <= extr_rate ((p - apop_pressure) / apop_pressure)^extr_gamma
+                                * (extr_rate per step, as the reference uses it) */
 };
+
+enum { CIL_CYCLE_EULER = 0, CIL_CYCLE_DPD = 1 };
 
 /* Model parameters with the reference's JSON meaning (Input.cpp:6-262; Cell.cuh:236-260
  * defaults). Times in time units; cycle times in units of tau_div_mu as in the JSON. */
@@ -83,6 +118,14 @@ typedef struct cil_cycle_params {
   int32_t precision;       /* 0: FP64 throughout (computes what the CPU restatement computes);
                             * 1: FP32 contact arithmetic on the FP64 separations, FP64 positions,
                             * forces of motility and noise, and cell state */
+  int32_t integrator;      /* CIL_CYCLE_EULER or CIL_CYCLE_DPD (MD.INTEGRATOR.SELECT) */
+  int32_t pad;
+  double mass;             /* MASS (DPD) */
+  double kbt;              /* MD.KBT (DPD) */
+  double dis_same;         /* DISSAMCEL: acts between the elements of one cell, none here */
+  double dis_diff;         /* DISDIFCEL (DPD) */
+  double dis_bg;           /* DISBG (DPD) */
+  double extr_rate;        /* EXTR_RATE (CIL_APOP_CYCLE_EXTRUDE) */
 } cil_cycle_params;
 
 /* Per-cell state in index order. Arrays may be NULL where not wanted. */
@@ -92,7 +135,7 @@ typedef struct cil_cycle_view {
   int32_t ts;
   int32_t pad;
   double *pos;       /* [cell][dim] */
-  double *vel;       /* [cell][dim], download only */
+  double *vel;       /* [cell][dim]; upload: NULL for cells at rest */
   double *sigma;     /* sigmaCore */
   double *sigma_t;   /* sigmaCoreT, the target diameter */
   double *theta;     /* cellTTheta, cycle phase */

@@ -11,8 +11,15 @@
 //   length / area, Utils.hpp:236-250), the position update with pressure-dependent friction
 //   (updateVelocityPositions, CIL.cu:902-939), ++ts, the cycle ODEs and divisions
 //   (calculDivisionsSingle, CIL.cu:469-619; singleCellDivision, MD.cu:664-718), apoptosis
-//   (calculApoptosisCyclePressure, CIL.cu:711-738; calculApoptosisPressureTime, CIL.cu:653-676),
-//   and checkPositions with DRAIN (CIL.cu:945-966).
+//   (calculApoptosisCyclePressure, CIL.cu:711-738; calculApoptosisPressureTime, CIL.cu:653-676;
+//   calculApoptosis, CIL.cu:627-649; calculApoptosisCycle, CIL.cu:681-709;
+//   calculApoptosisCycleExtrude, CIL.cu:749-788), and checkPositions with DRAIN (CIL.cu:945-966).
+// The DPD step (CIL.cu:1054-1066): half kick and drift (updateVelocities / updatePositions,
+//   CIL.cu:871-897, 849-866), the forces with the pair dissipative and random forces
+//   (cellCellDisRanForce, MD.cu:861-905), the second half kick, the background and pair
+//   dissipation (calculDisForces, CIL.cu:294-364), ++ts, divisions and apoptosis; every pair is
+//   visited once and the forces are reset at every evaluation, which the reference's OpenMP
+//   loops do not do (include/cil_cycle.h lists the differences).
 // Random numbers: Philox4x32-10 (Salmon et al., SC'11) keyed by (cell, step, purpose, sub)
 // exactly as the GPU model keys them, so that both draw the same numbers; the pair search
 // visits bins and cells in the GPU model's order, so that the force sums agree to the last
@@ -38,6 +45,9 @@ typedef struct cyo_params {  // the layout of cil_cycle_params (include/cil_cycl
   double apop_pressure, apop_duration, apop_rate, extr_gamma;
   int32_t drain;
   int32_t precision;  // read by the GPU model only: the restatement is FP64
+  int32_t integrator;  // 0 Euler, 1 DPD
+  int32_t pad;
+  double mass, kbt, dis_same, dis_diff, dis_bg, extr_rate;
 } cyo_params;
 
 }  // extern "C"
@@ -45,7 +55,7 @@ typedef struct cyo_params {  // the layout of cil_cycle_params (include/cil_cycl
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
-constexpr uint32_t kNoise = 11, kDir = 12, kDiv = 13, kApo = 14, kInit = 15;
+constexpr uint32_t kNoise = 11, kDir = 12, kDiv = 13, kApo = 14, kInit = 15, kDpd0 = 16, kDpd1 = 17;
 
 struct Block {
   uint32_t v[4];
@@ -114,6 +124,7 @@ struct Cell {
   double x[3], v[3];
   double sig, sigt, theta, rho, om, p;
   int tp, t0, tsw;
+  double fc[3], fd[3], fr[3];  // DPD forces
 };
 
 struct Model {
@@ -160,6 +171,9 @@ struct Model {
     noise_amp = q.noise_D > 0.0 ? std::sqrt(2.0 * q.noise_D) * (1.0 / std::sqrt(q.dt)) : 0.0;
     apop_rate_step = q.apop_rate * q.dt;
     apop_steps = q.apop_duration / q.dt;
+    kick_div = 2 * (2 * q.mass);
+    sqrt_dt = std::sqrt(q.dt);
+    sigma_r = std::sqrt(2 * q.dis_diff * q.kbt);
   }
 
   int bin_coord(double x, int d) const {
@@ -167,115 +181,147 @@ struct Model {
     return v < 0 ? 0 : (v >= ns[d] ? ns[d] - 1 : v);
   }
 
-  void forces(std::vector<double> &xn) {
-    const int n = static_cast<int>(c.size());
-    const int nb = ns[0] * ns[1] * ns[2];
-    std::vector<std::vector<int>> bins(nb);
-    for (int i = 0; i < n; ++i) {
+  using Bins = std::vector<std::vector<int>>;
+
+  // cells per bin in ascending index (the GPU model's counting sort order)
+  Bins bin_cells() const {
+    Bins bins(static_cast<size_t>(ns[0]) * ns[1] * ns[2]);
+    for (int i = 0; i < static_cast<int>(c.size()); ++i) {
       int b = 0;
       for (int d = 0; d < D; ++d) b = b * ns[d] + bin_coord(c[i].x[d], d);
       bins[b].push_back(i);
     }
+    return bins;
+  }
+
+  // every other cell in the bins within `radius` of cell i, in the GPU model's visiting order
+  template <class Fn>
+  void each_neighbour(int i, double radius, const Bins &bins, Fn fn) const {
+    int bi[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      bi[d] = bin_coord(c[i].x[d], d);
+      const double kk = std::ceil(radius * inv_bw[d]);
+      const int k = (kk >= 0.0 && kk < ns[d]) ? static_cast<int>(kk) : ns[d];
+      if (2 * k + 1 >= ns[d]) {
+        lo[d] = -bi[d];
+        hi[d] = ns[d] - 1 - bi[d];
+      } else if (p.periodic[d]) {
+        lo[d] = -k;
+        hi[d] = k;
+      } else {
+        lo[d] = bi[d] - k < 0 ? -bi[d] : -k;
+        hi[d] = bi[d] + k >= ns[d] ? ns[d] - 1 - bi[d] : k;
+      }
+    }
+    for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
+      for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
+        for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
+          const int oo[3] = {o0, o1, o2};
+          int b = 0;
+          for (int d = 0; d < D; ++d) {
+            int v = bi[d] + oo[d];
+            if (v < 0) v += ns[d];
+            if (v >= ns[d]) v -= ns[d];
+            b = b * ns[d] + v;
+          }
+          for (int j : bins[b])
+            if (j != i) fn(j);
+        }
+  }
+
+  // r_j - r_i at the nearest image (Box::distance's Nint, |dd| < L); returns its square length
+  double separation(int i, int j, double *rij) const {
+    double r2 = 0;
+    for (int d = 0; d < D; ++d) {
+      double dd = c[j].x[d] - c[i].x[d];
+      if (p.periodic[d]) {
+        if (dd > 0.5 * p.box[d])
+          dd -= p.box[d];
+        else if (dd < -(0.5 * p.box[d]))
+          dd += p.box[d];
+      }
+      rij[d] = dd;
+      r2 += dd * dd;
+    }
+    return r2;
+  }
+
+  // motility, passive noise, Hertz contacts with adhesion, and the pressure of cell i; draws
+  // keyed by step `key`
+  void conservative(int i, const Bins &bins, int key, double *F, double *pres_out) {
+    const Cell &ci = c[i];
     const double c2 = (1 - p.nu * p.nu) / p.E + (1 - p.nu * p.nu) / p.E;
+    double vi[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) F[d] = 0;
+    for (int d = 0; d < D; ++d) vi[d] = ci.v[d];
+    double v2 = 0;
+    for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+    double vl = std::sqrt(v2);
+    if (vl == 0.0) {
+      const Block r = draw(i, key, kDir, 0);
+      if (D == 2) {
+        const double ang = 6.283185307179586 * u53(r.v[0], r.v[1]);
+        vi[0] = 1e-11 * std::cos(ang);
+        vi[1] = 1e-11 * std::sin(ang);
+      } else {
+        const double z = 2.0 * u53(r.v[0], r.v[1]) - 1.0;
+        const double ang = 6.283185307179586 * u53(r.v[2], r.v[3]);
+        const double s = std::sqrt(1.0 - z * z);
+        vi[0] = 1e-11 * (s * std::cos(ang));
+        vi[1] = 1e-11 * (s * std::sin(ang));
+        vi[2] = 1e-11 * z;
+      }
+      v2 = 0;
+      for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+      vl = std::sqrt(v2);
+    }
+    for (int d = 0; d < D; ++d) F[d] = p.motility * (vi[d] / vl);
+    if (noise_amp > 0.0) {
+      double nz[4];
+      normal2(draw(i, key, kNoise, 0), &nz[0], &nz[1]);
+      if (D == 3) normal2(draw(i, key, kNoise, 1), &nz[2], &nz[3]);
+      for (int d = 0; d < D; ++d) F[d] += p.zeta * (noise_amp * nz[d]);
+    }
+    double pres = 0;
+    each_neighbour(i, smax, bins, [&](int j) {
+      double rij[3] = {0, 0, 0};
+      const double r2 = separation(i, j, rij);
+      const double si = ci.sig, sj = c[j].sig;
+      const double r = std::sqrt(r2);
+      if (!(r <= (si + sj) / 2) || r == 0.0) return;
+      const double sa = i < j ? si : sj, sb = i < j ? sj : si;
+      const double h = std::fmax((si + sj) / 2 - r, 0.0);
+      const double fel = (h * std::sqrt(h)) / (0.75 * c2 * std::sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
+      double A, vol;
+      if (D == 3) {
+        A = contact_area(r, sa, sb);
+        vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+      } else {
+        A = contact_length(sa, sb, h);
+        vol = A;
+      }
+      const double f0 = -fel + p.adhesion * A;
+      if (vol != 0.0) pres -= f0 / vol;
+      for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
+    });
+    for (int d = 0; d < D; ++d)
+      if (!std::isfinite(F[d])) err |= 2;
+    *pres_out = pres;
+  }
+
+  // Euler: forces, then the position update with pressure-dependent friction (CIL.cu:902-939)
+  void forces(std::vector<double> &xn) {
+    const int n = static_cast<int>(c.size());
+    const Bins bins = bin_cells();
     xn.assign(static_cast<size_t>(n) * D, 0.0);
     std::vector<double> vn(static_cast<size_t>(n) * D), pn(n);
     for (int i = 0; i < n; ++i) {
-      Cell &ci = c[i];
-      double F[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
-      for (int d = 0; d < D; ++d) vi[d] = ci.v[d];
-      double v2 = 0;
-      for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
-      double vl = std::sqrt(v2);
-      if (vl == 0.0) {
-        const Block r = draw(i, ts, kDir, 0);
-        if (D == 2) {
-          const double ang = 6.283185307179586 * u53(r.v[0], r.v[1]);
-          vi[0] = 1e-11 * std::cos(ang);
-          vi[1] = 1e-11 * std::sin(ang);
-        } else {
-          const double z = 2.0 * u53(r.v[0], r.v[1]) - 1.0;
-          const double ang = 6.283185307179586 * u53(r.v[2], r.v[3]);
-          const double s = std::sqrt(1.0 - z * z);
-          vi[0] = 1e-11 * (s * std::cos(ang));
-          vi[1] = 1e-11 * (s * std::sin(ang));
-          vi[2] = 1e-11 * z;
-        }
-        v2 = 0;
-        for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
-        vl = std::sqrt(v2);
-      }
-      for (int d = 0; d < D; ++d) F[d] = p.motility * (vi[d] / vl);
-      if (noise_amp > 0.0) {
-        double nz[4];
-        normal2(draw(i, ts, kNoise, 0), &nz[0], &nz[1]);
-        if (D == 3) normal2(draw(i, ts, kNoise, 1), &nz[2], &nz[3]);
-        for (int d = 0; d < D; ++d) F[d] += p.zeta * (noise_amp * nz[d]);
-      }
-      double pres = 0;
-      int bi[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-      for (int d = 0; d < D; ++d) {
-        bi[d] = bin_coord(ci.x[d], d);
-        const double kk = std::ceil(smax * inv_bw[d]);
-        const int k = (kk >= 0.0 && kk < ns[d]) ? static_cast<int>(kk) : ns[d];
-        if (2 * k + 1 >= ns[d]) {
-          lo[d] = -bi[d];
-          hi[d] = ns[d] - 1 - bi[d];
-        } else if (p.periodic[d]) {
-          lo[d] = -k;
-          hi[d] = k;
-        } else {
-          lo[d] = bi[d] - k < 0 ? -bi[d] : -k;
-          hi[d] = bi[d] + k >= ns[d] ? ns[d] - 1 - bi[d] : k;
-        }
-      }
-      for (int o0 = lo[0]; o0 <= hi[0]; ++o0)
-        for (int o1 = (D > 1 ? lo[1] : 0); o1 <= (D > 1 ? hi[1] : 0); ++o1)
-          for (int o2 = (D > 2 ? lo[2] : 0); o2 <= (D > 2 ? hi[2] : 0); ++o2) {
-            const int oo[3] = {o0, o1, o2};
-            int b = 0;
-            for (int d = 0; d < D; ++d) {
-              int v = bi[d] + oo[d];
-              if (v < 0) v += ns[d];
-              if (v >= ns[d]) v -= ns[d];
-              b = b * ns[d] + v;
-            }
-            for (int j : bins[b]) {
-              if (j == i) continue;
-              double rij[3] = {0, 0, 0}, r2 = 0;
-              for (int d = 0; d < D; ++d) {
-                double dd = c[j].x[d] - ci.x[d];
-                if (p.periodic[d]) {  // nearest image (Box::distance's Nint, |dd| < L)
-                  if (dd > 0.5 * p.box[d])
-                    dd -= p.box[d];
-                  else if (dd < -(0.5 * p.box[d]))
-                    dd += p.box[d];
-                }
-                rij[d] = dd;
-                r2 += dd * dd;
-              }
-              const double si = ci.sig, sj = c[j].sig;
-              const double r = std::sqrt(r2);
-              if (!(r <= (si + sj) / 2) || r == 0.0) continue;
-              const double sa = i < j ? si : sj, sb = i < j ? sj : si;
-              const double h = std::fmax((si + sj) / 2 - r, 0.0);
-              const double fel = (h * std::sqrt(h)) / (0.75 * c2 * std::sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
-              double A, vol;
-              if (D == 3) {
-                A = contact_area(r, sa, sb);
-                vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
-              } else {
-                A = contact_length(sa, sb, h);
-                vol = A;
-              }
-              const double f0 = -fel + p.adhesion * A;
-              if (vol != 0.0) pres -= f0 / vol;
-              for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
-            }
-          }
+      const Cell &ci = c[i];
+      double F[3], pres;
+      conservative(i, bins, ts, F, &pres);
       const double pnd = pres / p.cycle_p0;
       const double temp = p.dt * 1 / ((p.zeta + p.zeta_p * std::pow(pnd, p.zeta_p_beta)) * area_of(ci.sig));
       for (int d = 0; d < D; ++d) {
-        if (!std::isfinite(F[d])) err |= 2;
         const double t = ci.x[d] + temp * F[d];
         xn[static_cast<size_t>(i) * D + d] = p.periodic[d] ? std::fmod(t + p.box[d], p.box[d]) : t;
         vn[static_cast<size_t>(i) * D + d] = F[d] * (temp / p.dt);
@@ -289,6 +335,101 @@ struct Model {
       }
       c[i].p = pn[i];
     }
+  }
+
+  // ---- DPD (CIL.cu:1054-1066)
+  double kick_div = 1, sqrt_dt = 1, sigma_r = 0;
+
+  double kick(double v, double fc, double fd, double fr) const {  // updateVel, Utils.hpp:568-571
+    return v + (fc * p.dt + fd * p.dt + fr * sqrt_dt) / kick_div;
+  }
+
+  // Fc and the pressure, then the pair dissipative and random forces (cellCellDisRanForce,
+  // MD.cu:861-905) over the pairs closer than the lower-index cell's diameter, one normal per
+  // pair and axis keyed (lower index, key, purpose, higher index); with `kick_on`, the second
+  // half kick
+  void dpd_forces(int key, bool kick_on) {
+    const int n = static_cast<int>(c.size());
+    const Bins bins = bin_cells();
+    std::vector<double> fc(static_cast<size_t>(n) * 3), pn(n);
+    for (int i = 0; i < n; ++i) conservative(i, bins, key, &fc[static_cast<size_t>(i) * 3], &pn[i]);
+    std::vector<double> fd(static_cast<size_t>(n) * 3, 0.0), fr(static_cast<size_t>(n) * 3, 0.0),
+        vn(static_cast<size_t>(n) * 3, 0.0);
+    for (int i = 0; i < n; ++i) {
+      double *Fd = &fd[static_cast<size_t>(i) * 3], *Fr = &fr[static_cast<size_t>(i) * 3];
+      const double si = c[i].sig;
+      each_neighbour(i, smax, bins, [&](int j) {
+        double rij[3] = {0, 0, 0};
+        const double r = std::sqrt(separation(i, j, rij));
+        const double rc = i < j ? si : c[j].sig;
+        if (!(r < rc) || r == 0.0) return;
+        const double w = 1 - (r / rc);
+        const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
+        double xi[4];
+        normal2(philox(a, static_cast<uint32_t>(key), kDpd0, z, k0, k1), &xi[0], &xi[1]);
+        if (D == 3) normal2(philox(a, static_cast<uint32_t>(key), kDpd1, z, k0, k1), &xi[2], &xi[3]);
+        const double sw = std::sqrt(w);
+        for (int d = 0; d < D; ++d) {
+          const double nd = rij[d] / r;
+          Fd[d] -= p.dis_diff * w * ((c[i].v[d] - c[j].v[d]) * nd) * nd;
+          Fr[d] += sigma_r * sw * nd * xi[d];
+        }
+      });
+      for (int d = 0; d < D; ++d) {
+        const size_t k = static_cast<size_t>(i) * 3 + d;
+        vn[k] = kick(c[i].v[d], fc[k], fd[k], fr[k]);
+        if (kick_on && !std::isfinite(vn[k])) err |= 2;
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      c[i].p = pn[i];
+      for (int d = 0; d < D; ++d) {
+        const size_t k = static_cast<size_t>(i) * 3 + d;
+        c[i].fc[d] = fc[k];
+        c[i].fd[d] = fd[k];
+        c[i].fr[d] = fr[k];
+        if (kick_on) c[i].v[d] = vn[k];
+      }
+    }
+  }
+
+  // background and pair dissipation at the current velocities (calculDisForces,
+  // CIL.cu:294-364; cellBackDisForce, MD.cu:846-859; cellCellDisForce, MD.cu:951-985)
+  void dpd_dis() {
+    const int n = static_cast<int>(c.size());
+    const Bins bins = bin_cells();
+    const double rc = p.sigma_core;
+    std::vector<double> fd(static_cast<size_t>(n) * 3, 0.0);
+    for (int i = 0; i < n; ++i) {
+      double *Fd = &fd[static_cast<size_t>(i) * 3];
+      for (int d = 0; d < D; ++d) {
+        Fd[d] = 0;
+        Fd[d] -= p.dis_bg * c[i].v[d];
+      }
+      each_neighbour(i, smax > rc ? smax : rc, bins, [&](int j) {
+        double rij[3] = {0, 0, 0};
+        const double r = std::sqrt(separation(i, j, rij));
+        if (!(r < rc) || r == 0.0) return;
+        const double w = 1 - ((r * r) / rc);
+        for (int d = 0; d < D; ++d) {
+          const double nd = -rij[d] / r;
+          Fd[d] -= p.dis_diff * w * ((c[i].v[d] - c[j].v[d]) * nd) * nd;
+        }
+      });
+    }
+    for (int i = 0; i < n; ++i)
+      for (int d = 0; d < D; ++d) c[i].fd[d] = fd[static_cast<size_t>(i) * 3 + d];
+  }
+
+  void dpd_step() {
+    for (Cell &ci : c)  // updateVelocities, updatePositions (CIL.cu:1055-1056)
+      for (int d = 0; d < D; ++d) {
+        ci.v[d] = kick(ci.v[d], ci.fc[d], ci.fd[d], ci.fr[d]);
+        const double x = ci.x[d];
+        ci.x[d] = p.periodic[d] ? std::fmod(x + p.dt * ci.v[d] + p.box[d], p.box[d]) : x + ci.v[d] * p.dt;
+      }
+    dpd_forces(ts + 1, true);
+    dpd_dis();
   }
 
   void cycle() {
@@ -366,6 +507,8 @@ struct Model {
         m.x[d] = xm;
         dau.v[d] = 0;
         m.v[d] = 0;
+        dau.fc[d] = dau.fd[d] = dau.fr[d] = 0;  // resetFrc (CIL.cu:597-598)
+        m.fc[d] = m.fd[d] = m.fr[d] = 0;
       }
       double z0, z1, z2, z3;
       normal2(draw(i, ts, kDiv, 1), &z0, &z1);
@@ -401,13 +544,24 @@ struct Model {
     for (int i = 0; i < n; ++i) {
       const Block r = draw(i, ts, kApo, 0);
       const double u = u53(r.v[0], r.v[1]);
-      if (p.apoptosis == 1) {
+      const double rho = c[i].rho;
+      if (p.apoptosis == 1) {  // CyclePressure (CIL.cu:711-738)
         const double pr = c[i].p;
-        const double rate = apop_rate_step * std::pow((1 - (c[i].rho / p.apop_pressure)), p.apop_duration) *
+        const double rate = apop_rate_step * std::pow((1 - (rho / p.apop_pressure)), p.apop_duration) *
                             std::pow(pr / (pr + p.cycle_p0), p.extr_gamma);
         if (u <= rate) keep[i] = 0;
-      } else if (((p.apop_duration > 0) && (c[i].tp >= apop_steps)) || ((apop_rate_step > 0) && (u <= apop_rate_step))) {
-        keep[i] = 0;
+      } else if (p.apoptosis == 2) {  // PressureTime (CIL.cu:653-676)
+        if (((p.apop_duration > 0) && (c[i].tp >= apop_steps)) || ((apop_rate_step > 0) && (u <= apop_rate_step)))
+          keep[i] = 0;
+      } else if (p.apoptosis == 3) {  // constant rate (CIL.cu:627-649)
+        if (u <= apop_rate_step) keep[i] = 0;
+      } else if (p.apoptosis == 4) {  // Cycle (CIL.cu:681-709); cells with rho >= 1 stay
+        if (rho < 1 && u <= apop_rate_step * std::pow((1 - (rho / p.apop_pressure)), p.apop_duration)) keep[i] = 0;
+      } else {  // CycleExtrude (CIL.cu:749-788)
+        if (rho < 1 && u <= apop_rate_step) keep[i] = 0;
+        const double u2 = u53(r.v[2], r.v[3]);
+        if (rho <= 0.1 && u2 <= p.extr_rate * std::pow(((c[i].p - p.apop_pressure) / p.apop_pressure), p.extr_gamma))
+          keep[i] = 0;
       }
     }
     const size_t before = c.size();
@@ -416,8 +570,12 @@ struct Model {
   }
 
   void step() {
-    std::vector<double> xn;
-    forces(xn);
+    if (p.integrator == 1) {
+      dpd_step();
+    } else {
+      std::vector<double> xn;
+      forces(xn);
+    }
     ++ts;
     cycle();
     apoptosis();
@@ -476,6 +634,7 @@ void cyo_set_state(void *h, int32_t n, int32_t ts, const double *pos, const doub
     c.tsw = -1;
     m->smax = std::fmax(m->smax, c.sig);
   }
+  if (m->p.integrator == 1) m->dpd_forces(ts, false);  // the forces before the first step (CIL.cu:1096)
 }
 
 int32_t cyo_step(void *h, int32_t nsteps) {

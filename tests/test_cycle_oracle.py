@@ -55,3 +55,44 @@ def test_check_positions(oracle_lib, drain):
         assert r == 2 and o.state()["ncells"] == 1
     else:
         assert r == -1 and o.state()["ncells"] == 3
+
+
+DPD = dict(integrator=1, mass=1.0, kbt=0.01, dis_diff=2.0, dis_bg=0.0, motility=0.0, divide=0)
+
+
+def test_dpd_pair_forces_conserve_momentum(oracle_lib):
+    """With no motility and no background term every DPD force is a pair force, equal and
+    opposite on the two cells (the Hertz contact, w (v_i,d - v_j,d) n_d^2, and the random force
+    with one normal per pair and axis): the total momentum stays at its start."""
+    rng = np.random.default_rng(81)
+    n, box = 300, [20.0, 20.0, 0.0]
+    prm = dict(DPD, box=box, dt=1e-3)
+    o = oracle_lib.CycleOracle(prm, 1000, 4)
+    vel = rng.normal(0, 0.3, size=(n, 2))
+    o.set_state(rng.uniform(0, 20.0, size=(n, 2)), sigma=np.full(n, SIG0), theta=np.zeros(n), rho=np.ones(n),
+                angvel=np.zeros(n), vel=vel)
+    p0 = vel.sum(axis=0)
+    assert o.step(200) == 0
+    s = o.state()
+    assert s["ncells"] == n
+    assert np.abs(s["vel"].sum(axis=0) - p0).max() < 1e-10
+    assert np.abs(s["vel"] - vel).max() > 0.05  # the pair forces did act
+
+
+def test_dpd_background_damping_of_isolated_cells(oracle_lib):
+    """Cells far apart feel only DISBG: Fd = -gamma_bg v after each step, and each half kick
+    divides by twice the mass argument 2m (updateVelocities, CIL.cu:894; updateVel,
+    Utils.hpp:568-571), so v_k = v_0 (1 - gamma_bg dt / (4m))^(k-1) (the first step kicks with
+    the forces of the start, whose Fd is the pair part only)."""
+    prm = dict(DPD, box=[40.0, 40.0, 0.0], dt=1e-3, dis_bg=3.0, mass=0.7)
+    o = oracle_lib.CycleOracle(prm, 16, 5)
+    pos = np.array([[5.0, 5.0], [25.0, 5.0], [5.0, 25.0], [25.0, 25.0]])
+    vel = np.array([[1.0, 0.5], [-0.2, 0.3], [0.0, -1.0], [0.4, 0.4]])
+    o.set_state(pos, sigma=np.full(4, SIG0), theta=np.zeros(4), rho=np.ones(4), angvel=np.zeros(4), vel=vel)
+    k = 50
+    assert o.step(k) == 0
+    s = o.state()
+    f = 1 - 3.0 * 1e-3 / (4 * 0.7)
+    np.testing.assert_allclose(s["vel"], vel * f ** (k - 1), rtol=1e-12)
+    disp = vel * 1e-3 * sum(f ** max(j - 1, 0) for j in range(1, k + 1))
+    np.testing.assert_allclose(s["pos"], pos + disp, rtol=0, atol=1e-12)

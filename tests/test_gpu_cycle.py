@@ -67,8 +67,9 @@ def test_cycle_model_matches_oracle(gpu_lib, oracle_lib, dim):
     assert np.all(np.isfinite(g["pressure"])) and np.abs(g["pressure"]).max() > 0
 
 
-@pytest.mark.parametrize("law", [1, 2])
+@pytest.mark.parametrize("law", [1, 2, 3, 4, 5])
 def test_apoptosis_laws_match_oracle(gpu_lib, oracle_lib, law):
+    """CyclePressure (1), PressureTime (2), the constant rate (3), Cycle (4) and CycleExtrude (5)."""
     rng = np.random.default_rng(50 + law)
     box = [30.0, 30.0, 0.0]
     prm = dict(box=box, dt=2e-4, motility=0.5, zeta=0.2, apoptosis=law, apop_rate=40.0, apop_pressure=1.5,
@@ -76,9 +77,68 @@ def test_apoptosis_laws_match_oracle(gpu_lib, oracle_lib, law):
     if law == 2:
         prm.update(apop_pressure=0.0, apop_duration=0.01)  # removal after 50 steps at non-negative pressure
     st = colony(rng, 600, box)
+    if law == 5:  # quiescent cells (rho <= 0.1) under a pressure above APOP_PRESSURE are extruded
+        prm.update(apop_rate=5.0, apop_pressure=0.05, extr_rate=2e-3, extr_gamma=1.0)
+        st["rho"] = rng.uniform(0.0, 0.3, 600)
     g, s = run_both(gpu_lib, oracle_lib, prm, st, 120)
     assert s["napo"] > 0
     compare(g, s, box)
+
+
+DPD = dict(integrator=1, mass=1.0, kbt=0.01, dis_diff=2.0, dis_bg=0.5)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_dpd_matches_oracle(gpu_lib, oracle_lib, dim):
+    """The DPD integrator (CIL.cu:1054-1066) with divisions and the PressureTime apoptosis law
+    its step applies: the half kicks, the pair dissipative and random forces (one normal per
+    pair and axis, shared by the two cells), the background dissipation and the resets at
+    division agree with the restatement."""
+    rng = np.random.default_rng(90 + dim)
+    box = [30.0, 30.0, 30.0] if dim == 2 else [12.0, 12.0, 12.0]
+    n = 400 if dim == 2 else 700
+    prm = dict(DPD, dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, v1=15.0, apoptosis=2,
+               apop_pressure=40.0, apop_duration=0.01)  # the random start's deepest overlaps are removed
+    st = colony(rng, n, box, dim)
+    st["vel"] = rng.normal(0, 0.2, size=(n, dim))
+    g, s = run_both(gpu_lib, oracle_lib, prm, st, 150)
+    assert s["ndiv"] > 20 and s["napo"] > 0
+    compare(g, s, box)
+    assert np.abs(g["vel"]).max() > 0
+
+
+def test_dpd_restart_and_drain(gpu_lib, oracle_lib):
+    """A DPD run in frames (cil_cycle_check_positions with DRAIN between them, Ecoli_channel_2D's
+    open y axis) against the restatement; then a download and upload of the state (velocities
+    included) restarts the run: the forces are evaluated again at the uploaded state, as the
+    reference does at its start."""
+    G, O = gpu_lib, oracle_lib
+    rng = np.random.default_rng(97)
+    box = [5.0, 40.0, 0.0]
+    prm = dict(DPD, box=box, periodic=[1, 0, 0], dt=2e-4, motility=20.0, drain=1, divide=0)
+    st = colony(rng, 60, box)
+    st["pos"][:, 1] = rng.uniform(0.02, 1.0, 60)  # near the open lower edge, moving down
+    st["vel"] = np.tile([0.0, -10.0], (60, 1)) + rng.normal(0, 1.0, size=(60, 2))
+    eng = G.CycleEngine(prm, 4000, seed=5)
+    eng.upload(**st)
+    o = O.CycleOracle(prm, 4000, 5)
+    o.set_state(**st)
+    removed = 0
+    for _ in range(4):
+        eng.step(50)
+        assert o.step(50) == 0
+        eng.check_positions()
+        removed += o.check_positions()
+    g, s = eng.download(), o.state()
+    assert 0 < removed < 60
+    compare(g, s, box)
+    keys = ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "tpressure")
+    eng.upload(ts=g["ts"], **{k: g[k] for k in keys})
+    o.set_state(ts=s["ts"], **{k: s[k] for k in keys})
+    eng.step(30)
+    assert o.step(30) == 0
+    compare(eng.download(), o.state(), box)
+    eng.close()
 
 
 def test_drain_removes_cells_off_the_open_axis(gpu_lib, oracle_lib):
