@@ -355,18 +355,21 @@ def run_frames(G, p, st, steps, device, seed, skin, sched, tune):
             "enqueue_ms_per_frame": out["async_stats"]["enqueue_ms"] / nframes}
 
 
-def run_cycle(G, device, steps, warmup, precision=0):
+def run_cycle(G, device, steps, warmup, precision=0, dpd=False):
     """The single-element cell-cycle model that the shipped configurations run
     (PRX_MDCK_2D.json: Hertz contacts E = 100 with adhesion 0.2, motility 1, friction 0.01,
     dt = 1e-5, V1 15, P0 5), 1M cells on a jittered square lattice of spacing 1.1 in a periodic
     1100^2 box, cycle phases uniform; device-timed, and the restatement on one host thread over
-    a 20k-cell sample of the same packing for scale."""
+    a 20k-cell sample of the same packing for scale. dpd: the DPD integrator instead of Euler
+    (mass 1, KBT 0.003 as in the shipped files, DISDIFCEL 1, DISBG 0.01)."""
     side = 1000
     rng = np.random.default_rng(17)
     n = side * side
     g = (np.arange(n) % side, np.arange(n) // side)
     pos = np.stack([(g[0] + 0.5) * 1.1, (g[1] + 0.5) * 1.1], axis=1) + rng.uniform(-0.05, 0.05, size=(n, 2))
     prm = dict(box=[1100.0, 1100.0, 0.0], dt=1e-5, motility=1.0, zeta=0.01, v1=15.0, precision=precision)
+    if dpd:
+        prm.update(integrator=G.CYCLE_DPD, mass=1.0, kbt=0.003, dis_diff=1.0, dis_bg=0.01)
     st = dict(pos=pos, sigma=np.full(n, 1.1283791670955126), theta=rng.uniform(0, 1, n), rho=np.ones(n),
               angvel=np.full(n, 1e-5))
     eng = G.CycleEngine(prm, int(1.2 * n), seed=3, device=device)
@@ -381,8 +384,9 @@ def run_cycle(G, device, steps, warmup, precision=0):
     out = {"value": (n0 + n1) / 2 * steps / dev_s, "unit": "cell-steps/s", "cells": n0, "cells_end": n1,
            "steps": steps, "ms_per_step": tm["total_ms"] / steps, "gpu_launches": tm["launches"],
            "config": "single-element cell-cycle model (PRX_MDCK_2D.json parameters), "
-                     + ("FP32 contacts / FP64 state" if precision else "FP64") + ", 1M cells"}
-    if precision:
+                     + ("DPD, " if dpd else "") + ("FP32 contacts / FP64 state" if precision else "FP64")
+                     + ", 1M cells"}
+    if precision or dpd:
         return out
     try:
         from oracle import oracle as O
@@ -501,6 +505,7 @@ def main():
     if args.only == "cycle":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1)))
+        print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
         return 0
     p, st = workload(seed=1 + rank)
     hbm, peak_kind = peaks()
@@ -611,6 +616,7 @@ def main():
         try:
             line["cycle_model"] = run_cycle(G, device, min(args.steps, 200), args.warmup)
             line["cycle_model"]["fp32_contacts"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1)
+            line["cycle_model"]["dpd"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 0, dpd=True)
         except G.CilError as e:
             line["cycle_model"] = {"error": str(e)}
     if not args.no_e2e:

@@ -383,6 +383,7 @@ struct cil_input {
   // MD keys of either model
   bool drain = false;
   double osm = 0.0;
+  double dpd_same = 0.0, dpd_diff = 0.0, dpd_bg = 0.0, kbt = 0.0;  // MD.INTEGRATOR.DPD, MD.KBT
   // single-element species: the cell-cycle model (cil_cycle.h)
   int nelem = 2;
   cil_cycle_params cyc{};
@@ -442,10 +443,21 @@ void read_single(cil_input *in, const Node &root, const Node &loc, const std::st
   q.adhesion = hz.nums("ADHESION_CONSTANT", 1)[0];
   q.motility = loc.nums("MOTILITY", 1)[0];
   q.zeta = loc.nums("FRICTION", 1)[0];
-  if (!(q.zeta > 0.0)) key_error(loc.path + ".FRICTION", "In Euler, zeta should > 0!!!");
+  const bool dpd = integrator == "DPD";
+  if (!dpd && !(q.zeta > 0.0)) key_error(loc.path + ".FRICTION", "In Euler, zeta should > 0!!!");
   q.zeta_p = loc.nums("P_FRICTION", 1)[0];
   q.zeta_p_beta = loc.nums("P_FRICTION_BETA", 1)[0];
-  q.noise_D = integrator == "EULER" ? 0.0 : loc.child("NOISE").num("PASSIVE");
+  // NOISE_ON only with the stochastic integrators (Input.cpp:527-535)
+  q.noise_D = (integrator == "EULER" || dpd) ? 0.0 : loc.child("NOISE").num("PASSIVE");
+  q.integrator = dpd ? CIL_CYCLE_DPD : CIL_CYCLE_EULER;
+  if (dpd) {
+    q.mass = loc.nums("MASS", 1)[0];
+    if (!(q.mass > 0.0)) key_error(loc.path + ".MASS", "DPD needs a positive mass");
+    q.kbt = in->kbt;
+    q.dis_same = in->dpd_same;
+    q.dis_diff = in->dpd_diff;
+    q.dis_bg = in->dpd_bg;
+  }
   q.osmotic_pressure = in->osm;
   q.drain = in->drain ? 1 : 0;
   q.cycle_rho_ratio = 1.0;  // Cell.cuh:242-254 defaults
@@ -476,14 +488,16 @@ void read_single(cil_input *in, const Node &root, const Node &loc, const std::st
   }
   if (loc.has("APOPTOSIS") && loc.child("APOPTOSIS").boolean("ENABLED")) {  // Input.cpp:247-262
     Node a = loc.child("APOPTOSIS");
-    q.apoptosis = CIL_APOP_CYCLE_PRESSURE;  // the law the Euler step applies (CIL.cu:1017)
+    // the law each step applies: Euler calculApoptosisCyclePressure (CIL.cu:1017), DPD
+    // calculApoptosisPressureTime (CIL.cu:1064)
+    q.apoptosis = dpd ? CIL_APOP_PRESSURE_TIME : CIL_APOP_CYCLE_PRESSURE;
     q.apop_pressure = a.num("APOP_PRESSURE");
     q.apop_duration = a.num("APOP_DURATION");
     q.apop_rate = a.num("APOP_RATE");
     q.extr_gamma = a.num("EXTR_GAMMA");
     (void)a.num("APOP_ACTIVITY_ALPHA");
     (void)a.num("APOP_GAMMA");
-    (void)a.num("EXTR_RATE");
+    q.extr_rate = a.num("EXTR_RATE");
     if (!(q.apop_rate * q.dt < 1.0)) key_error(a.path + ".APOP_RATE", "Apoptosis rate per time step >= 1");
   }
   const bool has_gpu = root.has("GPU");
@@ -520,8 +534,13 @@ void read_all(cil_input *in) {
       if (!(L[d] > 0.0)) key_error("MD.BOX", "box lengths must be positive");
     }
     integrator = md.child("INTEGRATOR").pick("SELECT", {"EULER", "STOCHASTIC_EULER", "STOCHASTIC_HEUN", "DPD"});
-    if (integrator == "DPD")
-      key_error("MD.INTEGRATOR.SELECT", "DPD is not implemented by the GPU step (EULER, STOCHASTIC_EULER, STOCHASTIC_HEUN)");
+    if (integrator == "DPD") {  // Input.cpp:538-544, 555-556 (units all 1)
+      Node dpd = md.child("INTEGRATOR").child("DPD");
+      in->dpd_same = dpd.num("DISSAMCEL");
+      in->dpd_diff = dpd.num("DISDIFCEL");
+      in->dpd_bg = dpd.num("DISBG");
+      in->kbt = md.num("KBT");
+    }
     Node dtn = md.child("DT");  // initializeTimeStep (CIL.cuh:167-250)
     if (dtn.pick("SELECT", {"AUTOSCALE", "MANUAL"}) == "AUTOSCALE")
       key_error("MD.DT.SELECT", "AUTOSCALE needs the reference's force-law time scales; use MANUAL");
@@ -558,6 +577,8 @@ void read_all(cil_input *in) {
     return;
   }
   if (nelem != 2) key_error(loc.path + ".NELEM", "the GPU step models cells of one or two elements");
+  if (integrator == "DPD")  // its step divides with calculDivisionsSingle (CIL.cu:1063)
+    key_error("MD.INTEGRATOR.SELECT", "the GPU step runs DPD for single-element cells (NELEM 1)");
   const auto enames = loc.strs("NAMES");
   if (enames.size() != 2) key_error(loc.path + ".NAMES", "vector should be of size 2. Got " + std::to_string(enames.size()));
   if (enames[0] == enames[1]) key_error(loc.path + ".NAMES", "element names must be unique!");

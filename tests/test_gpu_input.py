@@ -76,14 +76,18 @@ REFERENCE_FRAME_CHUNKS = ["configuration/step", "configuration/dimensions", "con
                           "particles/charge", "particles/position", "particles/velocity", "particles/mass"]
 
 
-def test_runner_single_element_run(gpu_lib, tmp_path):
+@pytest.mark.parametrize("integrator", ["EULER", "DPD"])
+def test_runner_single_element_run(gpu_lib, tmp_path, integrator):
     """A single-element run (the shipped configurations' model) through cil_gpu_run: frames of
     the cell-cycle model with the chunks of the reference's own final-state files, equal to the
-    same run through the Python binding."""
+    same run through the Python binding; with the Euler step and with DPD."""
     G = gpu_lib
     from cil_cuda_gb300 import build
     doc = json.load(open(SINGLE))
     doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
+    if integrator == "DPD":
+        doc["MD"]["INTEGRATOR"] = {"SELECT": "DPD", "DPD": {"DISSAMCEL": 0.0, "DISDIFCEL": 2.0, "DISBG": 0.5}}
+        doc["MD"]["KBT"] = 0.01
     cfg = tmp_path / "single.json"
     cfg.write_text(json.dumps(doc))
     res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
@@ -103,7 +107,8 @@ def test_runner_single_element_run(gpu_lib, tmp_path):
     s = eng.download()
     eng.close()
     n = s["ncells"]
-    assert n > 200 and int(f.read(frames, "particles/N")[0]) == n
+    assert n > (200 if integrator == "EULER" else 20) and int(f.read(frames, "particles/N")[0]) == n
+    np.testing.assert_array_equal(f.read(frames, "particles/velocity")[:, :2], s["vel"].astype(np.float32))
     exp = (s["pos"] - 20.0).astype(np.float32)
     np.testing.assert_array_equal(f.read(frames, "particles/position")[:, :2], exp)
     np.testing.assert_array_equal(f.read(frames, "particles/charge"), s["rho"].astype(np.float32))

@@ -116,7 +116,9 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
 
 @pytest.mark.parametrize("edit,needle", [
     (lambda d: d["UNITS"].update(LENGTH=2), "UNITS.LENGTH"),
-    (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="DPD"), "MD.INTEGRATOR.SELECT"),
+    (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="DPD"), "MD.INTEGRATOR.DPD : key not found"),
+    (lambda d: (d["MD"]["INTEGRATOR"].update(SELECT="DPD", DPD=dict(DISSAMCEL=1, DISDIFCEL=1, DISBG=0)),
+                d["MD"].update(KBT=0.01)), "runs DPD for single-element cells"),
     (lambda d: (d["MD"]["INTEGRATOR"].update(SELECT="STOCHASTIC_HEUN"),
                 d["SPECIES"]["A"]["NOISE"].update(RADIAL=0.1, ANGULAR=0.0)), "SPECIES.A.NOISE.RADIAL"),
     (lambda d: d["MD"]["INTEGRATOR"].update(SELECT="VERLET"), "not one of"),
@@ -231,3 +233,25 @@ def test_heun_is_read(G):
     d["SPECIES"]["A"]["NOISE"].update(RADIAL=0.0, ANGULAR=0.0)
     r = load(G, d)
     assert r.config["integrator"] == G.INTEGRATOR_HEUN and r.params["noise_D"] == 0.001
+
+
+def test_single_element_dpd_is_read(G):
+    """MD.INTEGRATOR.SELECT = DPD (Input.cpp:538-544): DISSAMCEL / DISDIFCEL / DISBG from
+    MD.INTEGRATOR.DPD, KBT from MD, MASS from the species; no passive noise (NOISE_ON belongs to
+    the stochastic integrators) and the PressureTime apoptosis law that the DPD step applies."""
+    d = json.load(open(SINGLE))
+    d["MD"]["INTEGRATOR"] = {"SELECT": "DPD", "DPD": {"DISSAMCEL": 4.5, "DISDIFCEL": 3.0, "DISBG": 0.0045}}
+    d["MD"]["KBT"] = 0.002
+    c = d["SPECIES"]["DEFINE"][0]
+    d["SPECIES"][c]["MASS"] = [2.5]
+    d["SPECIES"][c]["NOISE"]["PASSIVE"] = 0.3
+    d["SPECIES"][c]["FRICTION"] = [0.0]  # only the Euler step needs a friction
+    d["SPECIES"][c]["APOPTOSIS"]["ENABLED"] = True
+    q = load(G, d).params
+    assert (q["integrator"], q["mass"], q["kbt"], q["dis_same"], q["dis_diff"], q["dis_bg"]) == \
+        (G.CYCLE_DPD, 2.5, 0.002, 4.5, 3.0, 0.0045)
+    assert q["noise_D"] == 0.0 and q["apoptosis"] == G.APOP_PRESSURE_TIME and q["extr_rate"] == 0.1
+    d["SPECIES"][c]["MASS"] = [0.0]
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "MASS" in str(e.value)
