@@ -36,7 +36,8 @@ EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step
             "cil_input_initial_state", "cil_input_last_error", "cil_input_free", "cil_cycle_create",
             "cil_cycle_destroy", "cil_cycle_upload", "cil_cycle_step", "cil_cycle_check_positions",
             "cil_cycle_download", "cil_cycle_timings", "cil_cycle_last_error", "cil_input_elements",
-            "cil_input_cycle_config", "cil_input_cycle_initial_state"]
+            "cil_input_cycle_config", "cil_input_cycle_initial_state", "cil_h5_shape", "cil_h5_read",
+            "cil_h5_last_error", "cil_h5_write_state"]
 
 
 class CilError(RuntimeError):
@@ -211,7 +212,66 @@ class CycleParams(C.Structure):
 class CycleView(C.Structure):
     _fields_ = [("ncells", C.c_int32), ("capacity", C.c_int32), ("ts", C.c_int32), ("pad", C.c_int32)] + [
         (k, C.POINTER(C.c_double)) for k in ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "pressure")
-    ] + [("tpressure", C.POINTER(C.c_int32))]
+    ] + [("tpressure", C.POINTER(C.c_int32))] + [
+        (k, C.POINTER(C.c_double)) for k in ("force", "force_dis", "force_ran")
+    ] + [("t0", C.POINTER(C.c_int32)), ("pad2", C.c_int32)]
+
+
+class H5State(C.Structure):
+    _fields_ = [("ncells", C.c_int32), ("nelem", C.c_int32), ("dim", C.c_int32), ("pad", C.c_int32)] + [
+        (k, C.POINTER(C.c_double)) for k in ("pos", "vel", "force", "force_dis", "force_ran", "sigma", "rho", "theta",
+                                             "pressure")
+    ] + [("state", C.POINTER(C.c_int32)), ("t0", C.POINTER(C.c_int32)), ("cpu_time", C.c_double)]
+
+
+def _h5_check(L, st: int):
+    if st != 0:
+        buf = C.create_string_buffer(1024)
+        L.cil_h5_last_error(buf, 1024)
+        raise CilError(st, buf.value.decode())
+
+
+def h5_read(path: str, dataset: str) -> np.ndarray:
+    """A dataset of an HDF5 final-state file (the reference's <NAME>.Last.h5) as float64, read by
+    the library's own reader (cil_h5_read, include/cil_input.h)."""
+    L = lib()
+    rank = C.c_int32()
+    dims = (C.c_int64 * 8)()
+    _h5_check(L, L.cil_h5_shape(path.encode(), dataset.encode(), C.byref(rank), dims))
+    shape = tuple(int(dims[k]) for k in range(rank.value))
+    out = np.zeros(int(np.prod(shape)) if shape else 1)
+    _h5_check(L, L.cil_h5_read(path.encode(), dataset.encode(), _dp(out), out.size))
+    return out.reshape(shape)
+
+
+def h5_write_state(path: str, pos, sigma, vel=None, force=None, force_dis=None, force_ran=None, rho=None, theta=None,
+                   pressure=None, state=None, t0=None, cpu_time: float = 0.0):
+    """A final-state file as outputHDF5Frame writes it with id -1 (cil_h5_write_state). pos:
+    [cell][elem][dim]; sigma: [cell][elem]."""
+    L = lib()
+    pos = np.ascontiguousarray(pos, np.float64)
+    n, E, D = pos.shape
+    keep = [pos]
+
+    def d(a, shape):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64).reshape(shape), shape), np.float64)
+        keep.append(a)
+        return _dp(a)
+
+    def i(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, np.int32).reshape(n)
+        keep.append(a)
+        return _ip(a)
+
+    st = H5State(ncells=n, nelem=E, dim=D, pad=0, pos=_dp(pos), vel=d(vel, (n, E, D)), force=d(force, (n, E, D)),
+                 force_dis=d(force_dis, (n, E, D)), force_ran=d(force_ran, (n, E, D)), sigma=d(sigma, (n, E)),
+                 rho=d(rho, (n,)), theta=d(theta, (n,)), pressure=d(pressure, (n,)), state=i(state), t0=i(t0),
+                 cpu_time=cpu_time)
+    _h5_check(L, L.cil_h5_write_state(path.encode(), C.byref(st)))
 
 
 def cycle_params(**kw) -> CycleParams:
@@ -348,6 +408,14 @@ def lib():
         L.cil_cycle_timings.argtypes = [vp, dp, C.POINTER(C.c_int64)]
         L.cil_cycle_last_error.restype = None
         L.cil_cycle_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.cil_h5_shape.restype = i32
+        L.cil_h5_shape.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+        L.cil_h5_read.restype = i32
+        L.cil_h5_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64]
+        L.cil_h5_last_error.restype = None
+        L.cil_h5_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.cil_h5_write_state.restype = i32
+        L.cil_h5_write_state.argtypes = [C.c_char_p, C.POINTER(H5State)]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L
@@ -755,7 +823,8 @@ class RunInput:
         n, D = self.run["ncells"], self.params["dim"]
         a = {k: np.zeros(n) for k in ("sigma", "sigma_t", "theta", "rho", "angvel")}
         a["pos"] = np.zeros((n, D))
-        v = CycleView(ncells=0, capacity=n, ts=0, pad=0, vel=None, pressure=None, tpressure=None,
+        a["vel"] = np.zeros((n, D))  # INIT H5 ALL restarts the velocities; zero otherwise
+        v = CycleView(ncells=0, capacity=n, ts=0, pad=0, pressure=None, tpressure=None,
                       **{k: _dp(x) for k, x in a.items()})
         self._check(self.L.cil_input_cycle_initial_state(self.h, C.byref(v)))
         return a
@@ -833,11 +902,13 @@ class CycleEngine:
     def download(self) -> dict:
         cap, D = self.cap, self.dim
         a = {k: np.zeros(cap) for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure")}
-        a["pos"] = np.zeros((cap, D))
-        a["vel"] = np.zeros((cap, D))
+        for k in ("pos", "vel", "force", "force_dis", "force_ran"):
+            a[k] = np.zeros((cap, D))
         a["tpressure"] = np.zeros(cap, np.int32)
-        v = CycleView(ncells=0, capacity=cap, ts=0, pad=0, tpressure=_ip(a["tpressure"]),
-                      **{k: _dp(a[k]) for k in ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "pressure")})
+        a["t0"] = np.zeros(cap, np.int32)
+        v = CycleView(ncells=0, capacity=cap, ts=0, pad=0, tpressure=_ip(a["tpressure"]), t0=_ip(a["t0"]),
+                      **{k: _dp(a[k]) for k in ("pos", "vel", "sigma", "sigma_t", "theta", "rho", "angvel", "pressure",
+                                                "force", "force_dis", "force_ran")})
         self._check(self.L.cil_cycle_download(self.h, C.byref(v)))
         n = v.ncells
         out = {k: x[:n] for k, x in a.items()}

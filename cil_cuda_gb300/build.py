@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcilgpu.so")
 RUNNER = os.path.join(OUT, "cil_gpu_run")
 SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu",
-           "cil_frame.cu", "cil_input.cpp", "cil_cycle.cu"]
+           "cil_frame.cu", "cil_input.cpp", "cil_cycle.cu", "cil_h5.cpp"]
 # per-file flags: the single-element cycle model keeps FP64 products and sums separate (no FMA
 # contraction) so that it computes exactly what its host restatement computes
 EXTRA = {"cil_cycle.cu": ["--fmad=false"]}

@@ -24,6 +24,7 @@
 // restatement the tests compare with.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -1333,6 +1334,16 @@ cil_status cil_cycle_check_positions(cil_cycle *h) {
 cil_status cil_cycle_download(cil_cycle *h, cil_cycle_view *v) {
   if (!h || !v) return CIL_ERR_CONFIG;
   CY_TRY(h, cudaSetDevice(h->device));
+  if (h->uploaded && !h->C.dpd) {
+    const int64_t launches = h->launches;  // cil_cycle_timings reports the last cil_cycle_step
+    // the forces and pressures at the current state, which the reference's Euler step
+    // evaluates at its end (CIL.cu:1019) and writes out; the next step's force pass computes
+    // the same values again (same positions, velocities and step key)
+    bin_cells(h);
+    launch_force(h, h->set[h->cur], nullptr, h->frc, 1, 0);
+    h->launches = launches;
+    CY_TRY(h, cudaGetLastError());
+  }
   const cil_status st = read_counters(h);
   const int n = h->h_cnt->n, D = h->C.D;
   v->ncells = n;
@@ -1364,6 +1375,16 @@ cil_status cil_cycle_download(cil_cycle *h, cil_cycle_view *v) {
   CY_TRY(h, sca(v->angvel, S.om, sizeof(double)));
   CY_TRY(h, sca(v->pressure, S.p, sizeof(double)));
   CY_TRY(h, sca(v->tpressure, S.tp, sizeof(int)));
+  CY_TRY(h, sca(v->t0, S.t0, sizeof(int)));
+  if (h->C.dpd) {
+    CY_TRY(h, vec(v->force, S.fc));
+    CY_TRY(h, vec(v->force_dis, S.fd));
+    CY_TRY(h, vec(v->force_ran, S.fr));
+  } else {
+    CY_TRY(h, vec(v->force, h->frc));
+    for (double *f : {v->force_dis, v->force_ran})
+      if (f) std::fill(f, f + static_cast<size_t>(n) * D, 0.0);
+  }
   return st;
 }
 

@@ -33,6 +33,7 @@
 
 #include "cil_cycle.h"
 #include "cil_input.h"
+#include "cil_h5.hpp"
 #include "host_rng.h"
 
 namespace {
@@ -379,7 +380,11 @@ struct cil_input {
   double tau_div[2] = {0, 0}, tau_mig[2] = {0, 0};
   std::string init_kind;
   int ncells = 0;
-  std::vector<double> json_pos;  // INIT JSON: [cell][elements][dim]
+  std::vector<double> json_pos;  // INIT JSON or H5: [cell][elements][dim]
+  // INIT H5 ALL (Input.cpp:643-726): the cell status of the restart file
+  bool h5_all = false;
+  std::vector<double> h5_vel, h5_theta, h5_rho, h5_sigma;  // [cell][elem][dim], [cell], [cell], [cell][elem]
+  std::vector<int> h5_state;
   // MD keys of either model
   bool drain = false;
   double osm = 0.0;
@@ -391,11 +396,69 @@ struct cil_input {
 
 namespace {
 
+// INIT H5 (Input.cpp:610-726): LOCATION [file, dataset] reads the element positions; ALL [file,
+// R, Vel, State, Theta, RHO, SigmaCore] the cell status too. RANGE [first, end) selects cells
+// (negative values count from the end). The file is opened as given, relative to the working
+// directory, as the reference opens it.
+void read_h5_init(cil_input *in, const Node &h, int nelem) {
+  const std::string how = h.pick("SELECT", {"ALL", "LOCATION"});
+  const bool all = how == "ALL";
+  const auto names = h.strs(how);
+  if (names.size() != (all ? 7u : 2u))
+    key_error(h.path + "." + how, "vector should be of size " + std::to_string(all ? 7 : 2) + ". Got " +
+                                      std::to_string(names.size()));
+  cil::h5::Reader r;
+  std::string err;
+  if (!r.open(names[0], &err)) key_error(h.path + "." + how, err);
+  auto load = [&](const std::string &ds_name, std::vector<double> *out, uint64_t per_cell) -> uint64_t {
+    cil::h5::Dataset ds;
+    if (!r.dataset(ds_name, &ds, &err) || !r.read(ds, out, &err)) key_error(h.path + "." + how, err);
+    if (per_cell == 0 || out->size() % per_cell) key_error(h.path + "." + how, "Inconsistent H5 dataset dimensions");
+    return out->size() / per_cell;
+  };
+  const uint64_t D = static_cast<uint64_t>(in->dim), E = static_cast<uint64_t>(nelem);
+  std::vector<double> pos;
+  const long long ncells = static_cast<long long>(load(names[1], &pos, E * D));
+  long long lo = 0, hi = ncells;
+  if (h.has("RANGE")) {
+    const auto rg = h.nums("RANGE", 2);
+    lo = static_cast<long long>(rg[0]);
+    hi = static_cast<long long>(rg[1]);
+    if (lo < 0) lo += ncells;
+    if (hi < 0) hi += ncells;
+  }
+  if (lo < 0 || lo > ncells || hi < 0 || hi > ncells) key_error(h.path + ".RANGE", "Range out of bounds");
+  if (!(lo < hi)) key_error(h.path + ".RANGE", "Range is empty");
+  in->ncells = static_cast<int>(hi - lo);
+  in->json_pos.assign(pos.begin() + lo * E * D, pos.begin() + hi * E * D);
+  if (!all) return;
+  in->h5_all = true;
+  std::vector<double> vel, state, theta, rho, sigma;
+  auto same = [&](uint64_t n, const char *what) {
+    if (static_cast<long long>(n) != ncells)
+      key_error(h.path + ".ALL", std::string(what) + ": Inconsistent H5 dataset dimensions");
+  };
+  same(load(names[2], &vel, E * D), "Vel");
+  same(load(names[3], &state, 1), "State");
+  same(load(names[4], &theta, 1), "Theta");
+  same(load(names[5], &rho, 1), "RHO");
+  same(load(names[6], &sigma, E), "SigmaCore");
+  in->h5_vel.assign(vel.begin() + lo * E * D, vel.begin() + hi * E * D);
+  in->h5_theta.assign(theta.begin() + lo, theta.begin() + hi);
+  in->h5_rho.assign(rho.begin() + lo, rho.begin() + hi);
+  in->h5_sigma.assign(sigma.begin() + lo * E, sigma.begin() + hi * E);
+  in->h5_state.clear();
+  for (long long i = lo; i < hi; ++i) in->h5_state.push_back(static_cast<int>(state[i]));
+}
+
 // INIT block of either model: RANDOM cell count, or JSON element positions (rows of DIM)
 void read_init(cil_input *in, const Node &root, const std::string &cell, int nelem) {
   Node init = root.child("INIT").child(cell);
   in->init_kind = init.pick("SELECT", {"JSON", "H5", "RANDOM"});
-  if (in->init_kind == "H5") key_error(init.path + ".SELECT", "H5 restart needs libhdf5, which this build does not have");
+  if (in->init_kind == "H5") {
+    read_h5_init(in, init.child("H5"), nelem);
+    return;
+  }
   if (in->init_kind == "RANDOM") {
     const int n = init.child("RANDOM").integer("NUMBER");
     if (n < 0) key_error(init.path + ".RANDOM.NUMBER", "negative cell count");
@@ -824,6 +887,9 @@ cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *v) {
     }
   }
   if (in->init_kind == "RANDOM") random_positions(rng, in, v->pos);  // the second readInit
+  if (in->h5_all)  // the second readInit of H5 ALL: the file's diameters (velocities, phases and
+                   // activities have no place in the two-element step)
+    for (int i = 0; i < 2 * n; ++i) v->sigma[i] = in->h5_sigma[i];
   // initializeColony: positions must lie in the box along periodic axes (CIL.cuh:52-66)
   for (int i = 0; i < 2 * n; ++i)
     for (int d = 0; d < D; ++d) {
@@ -894,6 +960,22 @@ cil_status cil_input_cycle_initial_state(const cil_input *in, cil_cycle_view *v)
     }
   }
   if (in->init_kind == "RANDOM") positions();  // the second readInit
+  if (in->h5_all) {  // the second readInit of H5 ALL replaces the drawn status (Input.cpp:711-719)
+    for (int i = 0; i < n; ++i) {
+      if (q.divide && in->h5_state[i] != 0) {
+        m->err = "INIT H5: cell " + std::to_string(i) + " is not in the dividing state (crawling cells never "
+                 "re-enter the single-element cycle)";
+        return CIL_ERR_CONFIG;
+      }
+      v->sigma[i] = in->h5_sigma[i];
+      v->sigma_t[i] = in->h5_sigma[i];
+      v->theta[i] = in->h5_theta[i];
+      v->rho[i] = in->h5_rho[i];
+      if (v->vel)
+        for (int d = 0; d < D; ++d)
+          v->vel[static_cast<size_t>(i) * D + d] = in->h5_vel[static_cast<size_t>(i) * D + d];
+    }
+  }
   for (int i = 0; i < n; ++i)
     for (int d = 0; d < D; ++d) {
       const double r = v->pos[static_cast<size_t>(i) * D + d];

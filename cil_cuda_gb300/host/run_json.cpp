@@ -7,14 +7,17 @@
 // writes frame 0, then FRAMES times: GTS steps (one step call), checkPositions (with DRAIN),
 // a progress line in the reference's format, a GSD frame when OUTPUT.FORMAT lists GSD. At the
 // end the final state goes to <DIR>/Last/<NAME>.Last.gsd as one frame labelled step 0
-// (finalizeOutput, OutputWriter.cpp:724-745). Two-element species run the two-element step
-// with the device-fed frame writer (include/cil_gsd.h); single-element species, the shipped
-// runs, run the cell-cycle model (include/cil_cycle.h), whose frames are downloaded and
-// written with the GSD file layer (charge: the cycle activity rho, mass: the pressure, as
+// (finalizeOutput, OutputWriter.cpp:724-745), and with H5 in OUTPUT.FORMAT to
+// <DIR>/Last/<NAME>.Last.h5 (the H5 frame file is not written). Two-element species run the
+// two-element step with the device-fed frame writer (include/cil_gsd.h); single-element
+// species, the shipped runs, run the cell-cycle model (include/cil_cycle.h), whose frames are
+// downloaded and written with the GSD file layer (charge: the cycle activity rho, mass: the pressure, as
 // outputGSDParticles writes them, OutputWriter.cpp:522-615). The optional arguments replace
 // MD.FRAMES and MD.GTS. Failures print the library's message and exit 1, as run_assert does
 // (Utils.hpp:99-109).
 #include <sys/stat.h>
+
+#include <chrono>
 
 #include <cstdio>
 #include <stdexcept>
@@ -97,6 +100,55 @@ void cycle_frame(cil_gsd_file *f, const cil_cycle_params &p, const cil_run_info 
   if (cil_gsd_end_frame(f) != CIL_OK) throw std::runtime_error("GSD write failed");
 }
 
+// The final-state file <DIR>/Last/<NAME>.Last.h5 (outputHDF5Frame with id -1 and the move into
+// Last/, OutputWriter.cpp:388-441, 736-745) of a cell-cycle colony
+void cycle_last_h5(const std::string &path, const cil_cycle_params &p, cil_cycle *h, double cpu_time) {
+  cil_cycle_view v{};
+  cil_cycle_download(h, &v);  // cell count
+  const int n = v.ncells, D = p.dim;
+  std::vector<double> pos(static_cast<size_t>(n) * D), vel(pos.size()), fc(pos.size()), fd(pos.size()), fr(pos.size()),
+      sig(n), rho(n), th(n), pres(n);
+  std::vector<int32_t> t0(n), state(n, 0);  // every cell of the single-element cycle is dividing (0)
+  v = cil_cycle_view{};
+  v.capacity = n;
+  v.pos = pos.data();
+  v.vel = vel.data();
+  v.force = fc.data();
+  v.force_dis = fd.data();
+  v.force_ran = fr.data();
+  v.sigma = sig.data();
+  v.rho = rho.data();
+  v.theta = th.data();
+  v.pressure = pres.data();
+  v.t0 = t0.data();
+  if (cil_cycle_download(h, &v) != CIL_OK) throw std::runtime_error("cil_cycle_download failed");
+  cil_h5_state s{};
+  s.ncells = n;
+  s.nelem = 1;
+  s.dim = D;
+  s.pos = pos.data();
+  s.vel = vel.data();
+  s.force = fc.data();
+  s.force_dis = fd.data();
+  s.force_ran = fr.data();
+  s.sigma = sig.data();
+  s.rho = rho.data();
+  s.theta = th.data();
+  s.pressure = pres.data();
+  s.state = state.data();
+  s.t0 = t0.data();
+  s.cpu_time = cpu_time;
+  if (cil_h5_write_state(path.c_str(), &s) != CIL_OK) {
+    char buf[512] = {0};
+    cil_h5_last_error(buf, sizeof buf);
+    throw std::runtime_error(std::string("writing ") + path + ": " + buf);
+  }
+}
+
+double seconds_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 void cycle_check(cil_status s, const char *what, cil_cycle *h) {
   if (s == CIL_OK) return;
   char buf[1024] = {0};
@@ -111,12 +163,13 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
   check(cil_input_cycle_config(in, &p, &run), "cil_input_cycle_config", nullptr, in);
   if (frames_arg > 0) run.frames = frames_arg;
   if (gts_arg > 0) run.gts = gts_arg;
-  if (run.output_h5) std::fprintf(stderr, "# H5 output is not served by this build (no libhdf5); GSD only\n");
+  if (run.output_h5) std::fprintf(stderr, "# H5: the final state only (<NAME>.Last.h5); frames go to GSD\n");
   const int n = run.ncells, D = p.dim;
-  std::vector<double> pos(static_cast<size_t>(n) * D), sig(n), sigt(n), th(n), rho(n), om(n);
+  std::vector<double> pos(static_cast<size_t>(n) * D), vel(pos.size(), 0.0), sig(n), sigt(n), th(n), rho(n), om(n);
   cil_cycle_view v{};
   v.capacity = n;
   v.pos = pos.data();
+  v.vel = vel.data();  // INIT H5 ALL restarts the velocities
   v.sigma = sig.data();
   v.sigma_t = sigt.data();
   v.theta = th.data();
@@ -138,7 +191,9 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
       cycle_frame(f, p, run, h, 0);
     }
     int64_t ts = 0;
+    double cpu_time = 0.0;
     for (int iframe = 1; iframe <= run.frames; ++iframe) {
+      const auto t_frame = std::chrono::steady_clock::now();
       cycle_check(cil_cycle_step(h, run.gts, &ts), "cil_cycle_step", h);
       cycle_check(cil_cycle_check_positions(h), "checkPositions", h);
       cil_cycle_view c{};
@@ -146,6 +201,12 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
       std::fprintf(stderr, "# ts = %8lld time = %12.3e \t cells = %8d elements = %8d\n", static_cast<long long>(ts),
                    static_cast<double>(ts) * p.dt, c.ncells, c.ncells);
       if (f) cycle_frame(f, p, run, h, ts);
+      cpu_time = seconds_since(t_frame);
+    }
+    if (run.output_h5) {
+      mkdir(dir.c_str(), 0755);
+      mkdir((dir + "/Last").c_str(), 0733);
+      cycle_last_h5(dir + "/Last/" + name + ".Last.h5", p, h, cpu_time);
     }
     if (f) {
       cil_gsd_close(f);
@@ -191,7 +252,7 @@ int main(int argc, char **argv) {
     check(cil_input_config(in, &cfg, &p, &run), "cil_input_config", nullptr, in);
     if (frames_arg > 0) run.frames = frames_arg;
     if (gts_arg > 0) run.gts = gts_arg;
-    if (run.output_h5) std::fprintf(stderr, "# H5 output is not served by this build (no libhdf5); GSD only\n");
+    if (run.output_h5) std::fprintf(stderr, "# H5: the final state only (<NAME>.Last.h5); frames go to GSD\n");
     const int D = cfg.dim, cap = run.capacity > run.ncells ? run.capacity : run.ncells;
     std::vector<double> pos(static_cast<size_t>(cap) * 2 * D), sig(static_cast<size_t>(cap) * 2);
     std::vector<int> t0(cap), tsw(cap);
@@ -217,13 +278,50 @@ int main(int argc, char **argv) {
       check(cil_frame_write(w, 0, nullptr), "cil_frame_write", h);  // outputFrame(0, 0)
     }
     int64_t ts = 0;
+    double cpu_time = 0.0;
     for (int iframe = 1; iframe <= run.frames; ++iframe) {
+      const auto t_frame = std::chrono::steady_clock::now();
       check(cil_step(h, run.gts, &ts), "cil_step", h);  // GTS x mdStep(ts)
       cil_obs o{};
       check(cil_observables(h, 0, &o), "cil_observables", h);
       std::fprintf(stderr, "# ts = %8lld time = %12.3e \t cells = %8d elements = %8d\n", static_cast<long long>(ts),
                    static_cast<double>(ts) * p.dt, o.ncells, 2 * o.ncells);
       if (w) check(cil_frame_write(w, ts, nullptr), "cil_frame_write", h);
+      cpu_time = seconds_since(t_frame);
+    }
+    if (run.output_h5) {  // the final state of the two-element colony
+      std::vector<double> vel(static_cast<size_t>(cap) * 2 * D), frc(vel.size());
+      v = cil_colony_view{};
+      v.capacity = cap;
+      v.pos = pos.data();
+      v.sigma = sig.data();
+      v.vel = vel.data();
+      v.t0 = t0.data();
+      v.tswitch = tsw.data();
+      check(cil_download(h, 0, &v), "cil_download", h);
+      check(cil_forces(h, 0, frc.data()), "cil_forces", h);
+      const int n = v.ncells;
+      std::vector<double> rho(n, 1.0);  // initializeCellStatus's activity, which the step never changes
+      std::vector<int32_t> state(n, 0);
+      cil_h5_state s{};
+      s.ncells = n;
+      s.nelem = 2;
+      s.dim = D;
+      s.pos = pos.data();
+      s.vel = vel.data();
+      s.force = frc.data();
+      s.sigma = sig.data();
+      s.rho = rho.data();
+      s.state = state.data();
+      s.t0 = t0.data();
+      s.cpu_time = cpu_time;
+      mkdir(dir.c_str(), 0755);
+      mkdir((dir + "/Last").c_str(), 0733);
+      if (cil_h5_write_state((dir + "/Last/" + name + ".Last.h5").c_str(), &s) != CIL_OK) {
+        char buf[512] = {0};
+        cil_h5_last_error(buf, sizeof buf);
+        throw std::runtime_error(std::string("writing the final-state H5 file: ") + buf);
+      }
     }
     if (w) {
       check(cil_frame_close(w), "cil_frame_close", h);

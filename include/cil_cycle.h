@@ -141,8 +141,14 @@ typedef struct cil_cycle_view {
   double *theta;     /* cellTTheta, cycle phase */
   double *rho;       /* cellTRho, cycle activity */
   double *angvel;    /* cellAngVel, cycle speed per step */
-  double *pressure;  /* pressure of the last force evaluation */
+  double *pressure;  /* pressure at the cells' positions (download: evaluated at the current
+                      * state, as the reference's step leaves it for output) */
   int32_t *tpressure;/* cellTPressure */
+  /* download only (NULL where not wanted): the forces the reference writes to its final-state
+   * file (F, FD, FR): Euler, the force at the current state; DPD, Fc, Fd and Fr */
+  double *force, *force_dis, *force_ran;  /* [cell][dim] */
+  int32_t *t0;       /* cellT0, the step of the cell's birth (download only) */
+  int32_t pad2;
 } cil_cycle_view;
 
 typedef struct cil_cycle cil_cycle;

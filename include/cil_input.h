@@ -7,12 +7,14 @@
  *   UNITS       LENGTH, MOTILITY, FRICTION must be 1: the derived units need the reference's
  *               Units class, which is not part of its tree.
  *   MD          DIM, BOX, PBC, GTS, FRAMES; DT (MANUAL); INTEGRATOR EULER (no noise),
- *               STOCHASTIC_EULER (passive noise) or STOCHASTIC_HEUN (CIL_INTEGRATOR_HEUN;
- *               its active RADIAL/ANGULAR noise must be 0). AUTOSCALE and DPD are refused
- *               with a message.
+ *               STOCHASTIC_EULER (passive noise), STOCHASTIC_HEUN (CIL_INTEGRATOR_HEUN;
+ *               its active RADIAL/ANGULAR noise must be 0) or DPD (single-element cells:
+ *               CIL_CYCLE_DPD with INTEGRATOR.DPD DISSAMCEL / DISDIFCEL / DISBG, KBT and the
+ *               species' MASS). AUTOSCALE is refused with a message.
  *   RUNTIME     RNG.SEED (<= 0: the current time, as Random::init(time(NULL))).
- *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 needs libhdf5, which this
- *               build does not have, and is reported back as not served).
+ *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 by the final-state file
+ *               <NAME>.Last.h5, cil_h5_write_state below; the H5 frame file, whose groups
+ *               track link creation order, is not served).
  *   SPECIES     one species. Two-element cells (cil_gpu.h): NELEM, NAMES, MOTILITY, FRICTION,
  *               NOISE.PASSIVE, the element diameters of the selected pair force, FENE RMAX /
  *               KAPPA_PULL (for the steady-state length rss that INIT RANDOM uses),
@@ -21,7 +23,7 @@
  *               model, cil_cycle.h): PAIRFORCES.HZ (ELASTIC_MODULUS, POISSON_RATIO, SIGMA_CORE,
  *               ADHESION_CONSTANT), MOTILITY, FRICTION, P_FRICTION, P_FRICTION_BETA, NOISE,
  *               DIVISION (TAU_DIVISION, V1, CYCLE_*), APOPTOSIS (the Euler step's cycle-pressure
- *               law); MD.OSMOTIC_PRESSURE and MD.DRAIN.
+ *               law, or the DPD step's pressure-time law); MD.OSMOTIC_PRESSURE and MD.DRAIN.
  *   INTERACTIONS PAIRFORCES.SELECT "LJ" with ATTRACTION OFF is the reference's own law
  *               (WCA, cil_gpu.h CIL_FORCE_LJ_WCA, epsilon from the species' LJ EPSILON).
  *   GPU         (optional block, this library's own): PRECISION "FP64" | "MIXED", RNG
@@ -33,7 +35,12 @@
  *               WALLS {E, POS[], DIR[]}.
  *   INIT        per species: RANDOM (NUMBER) with the reference's draw sequence, so that the
  *               positions equal the reference's bit for bit for the same seed; JSON (element
- *               positions). H5 restart needs libhdf5 and is refused.
+ *               positions); H5 (Input.cpp:610-726): LOCATION [file, positions dataset] or ALL
+ *               [file, R, Vel, State, Theta, RHO, SigmaCore] with an optional RANGE of cells,
+ *               read from a final-state file (the reference's <NAME>.Last.h5) by this
+ *               library's own HDF5 reader; ALL replaces the drawn cell status by the file's
+ *               (positions, velocities, phases, activities, diameters); the file path is
+ *               taken relative to the working directory, as the reference opens it.
  *
  * Errors carry the JSON key that failed, as json_parser's std::domain_error messages do
  * (JsonParser.hpp:13-135).
@@ -104,6 +111,30 @@ cil_status cil_input_cycle_initial_state(const cil_input *in, cil_cycle_view *vi
 void cil_input_last_error(const cil_input *in, char *buf, size_t len);
 
 void cil_input_free(cil_input *in);
+
+/* ---- HDF5 final-state files, without libhdf5 (the subset libhdf5 writes for the reference's
+ * <NAME>.Last.h5: superblock 0, symbol-table groups, contiguous or compact numeric datasets).
+ * Errors: cil_h5_last_error (per thread). */
+
+/* Rank and dimensions (up to 8) of a dataset ("R", "/group/R"). */
+cil_status cil_h5_shape(const char *path, const char *dataset, int32_t *rank, int64_t dims[8]);
+/* The dataset converted to double, row-major; capacity in elements. */
+cil_status cil_h5_read(const char *path, const char *dataset, double *out, int64_t capacity);
+void cil_h5_last_error(char *buf, size_t len);
+
+/* One colony's final state as outputHDF5Frame writes it with id -1 (OutputWriter.cpp:388-441):
+ * datasets R, Vel, F, FD, FR [cell][elem][dim], SigmaCore [cell][elem], RHO, Theta, PR, State,
+ * T0 [cell], CpuTime [1], doubles stored as FP32 (SimIO.hpp:73) and integers as int32. NULL
+ * arrays are written as zeros. */
+typedef struct cil_h5_state {
+  int32_t ncells, nelem, dim, pad;
+  const double *pos, *vel, *force, *force_dis, *force_ran; /* [cell][elem][dim] */
+  const double *sigma;                                     /* [cell][elem] */
+  const double *rho, *theta, *pressure;                    /* [cell] */
+  const int32_t *state, *t0;                               /* [cell] */
+  double cpu_time;
+} cil_h5_state;
+cil_status cil_h5_write_state(const char *path, const cil_h5_state *s);
 
 #ifdef __cplusplus
 }

@@ -337,6 +337,19 @@ struct Model {
     }
   }
 
+  // Euler: the forces and pressures at the current state, which the reference's step evaluates
+  // at its end (CIL.cu:1019) and writes out; the next step computes the same values again
+  std::vector<double> out_f;  // [cell][3]
+  void refresh() {
+    if (p.integrator == 1) return;
+    const int n = static_cast<int>(c.size());
+    const Bins bins = bin_cells();
+    out_f.assign(static_cast<size_t>(n) * 3, 0.0);
+    std::vector<double> pn(n);
+    for (int i = 0; i < n; ++i) conservative(i, bins, ts, &out_f[static_cast<size_t>(i) * 3], &pn[i]);
+    for (int i = 0; i < n; ++i) c[i].p = pn[i];
+  }
+
   // ---- DPD (CIL.cu:1054-1066)
   double kick_div = 1, sqrt_dt = 1, sigma_r = 0;
 
@@ -647,9 +660,10 @@ int32_t cyo_check_positions(void *h) { return static_cast<Model *>(h)->check_pos
 
 int32_t cyo_num_cells(const void *h) { return static_cast<int32_t>(static_cast<const Model *>(h)->c.size()); }
 
-void cyo_get_state(const void *h, double *pos, double *vel, double *sigma, double *sigma_t, double *theta,
+void cyo_get_state(void *h, double *pos, double *vel, double *sigma, double *sigma_t, double *theta,
                    double *rho, double *angvel, double *pressure, int32_t *tpressure, int64_t *counts) {
-  const Model *m = static_cast<const Model *>(h);
+  Model *m = static_cast<Model *>(h);
+  m->refresh();
   const int n = static_cast<int>(m->c.size());
   for (int i = 0; i < n; ++i) {
     const Cell &c = m->c[i];
@@ -668,6 +682,22 @@ void cyo_get_state(const void *h, double *pos, double *vel, double *sigma, doubl
   counts[0] = m->ts;
   counts[1] = m->ndiv;
   counts[2] = m->napo;
+}
+
+// The forces a final-state file holds: Euler, the force at the current state (Fd, Fr zero);
+// DPD, Fc, Fd and Fr. Arrays [cell][dim].
+void cyo_get_forces(void *h, double *fc, double *fd, double *fr) {
+  Model *m = static_cast<Model *>(h);
+  m->refresh();
+  const int n = static_cast<int>(m->c.size());
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < m->D; ++d) {
+      const size_t k = static_cast<size_t>(i) * m->D + d;
+      const bool dpd = m->p.integrator == 1;
+      fc[k] = dpd ? m->c[i].fc[d] : m->out_f[static_cast<size_t>(i) * 3 + d];
+      fd[k] = dpd ? m->c[i].fd[d] : 0.0;
+      fr[k] = dpd ? m->c[i].fr[d] : 0.0;
+    }
 }
 
 }  // extern "C"

@@ -265,6 +265,7 @@ class CycleOracle:
         L.cyo_num_cells.restype = i32
         L.cyo_num_cells.argtypes = [vp]
         L.cyo_get_state.argtypes = [vp] + [dp] * 8 + [ip, C.POINTER(C.c_int64)]
+        L.cyo_get_forces.argtypes = [vp, dp, dp, dp]
         self.p = cycle_params(**params)
         self.dim = self.p.dim
         self.h = L.cyo_create(C.byref(self.p), capacity, seed)
@@ -299,6 +300,9 @@ class CycleOracle:
                              a["tpressure"].ctypes.data_as(C.POINTER(C.c_int32)),
                              counts.ctypes.data_as(C.POINTER(C.c_int64)))
         a.update(ncells=n, ts=int(counts[0]), ndiv=int(counts[1]), napo=int(counts[2]))
+        for k in ("force", "force_dis", "force_ran"):
+            a[k] = np.zeros((n, D))
+        self.L.cyo_get_forces(self.h, P(a["force"]), P(a["force_dis"]), P(a["force_ran"]))
         return a
 
     def close(self):

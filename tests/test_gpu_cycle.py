@@ -50,7 +50,7 @@ def compare(g, s, box):
     np.testing.assert_array_equal(g["tpressure"], s["tpressure"])
     L = np.asarray(box[:g["pos"].shape[1]])
     assert close(g["pos"], s["pos"], L)
-    for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure", "vel"):
+    for k in ("sigma", "sigma_t", "theta", "rho", "angvel", "pressure", "vel", "force", "force_dis", "force_ran"):
         assert close(g[k], s[k]), k
 
 

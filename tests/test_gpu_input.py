@@ -114,3 +114,85 @@ def test_runner_single_element_run(gpu_lib, tmp_path, integrator):
     np.testing.assert_array_equal(f.read(frames, "particles/charge"), s["rho"].astype(np.float32))
     np.testing.assert_array_equal(f.read(frames, "particles/mass"), s["pressure"].astype(np.float32))
     np.testing.assert_array_equal(last.read(0, "particles/diameter"), s["sigma"].astype(np.float32))
+
+
+@pytest.mark.parametrize("integrator", ["EULER", "DPD"])
+def test_runner_final_state_h5_and_restart(gpu_lib, tmp_path, integrator):
+    """OUTPUT.FORMAT with H5: cil_gpu_run writes <NAME>.Last.h5 beside the final GSD frame. Its
+    SigmaCore, RHO, PR and Vel are the FP32 values of the GSD file's diameter, charge, mass and
+    velocity, as in the reference's own pair of files; F is the force at the final state. A run
+    restarted from it with INIT H5 ALL starts from those values."""
+    G = gpu_lib
+    from cil_cuda_gb300 import build
+    doc = json.load(open(SINGLE))
+    doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
+    doc["OUTPUT"]["FORMAT"] = ["GSD", "H5"]
+    if integrator == "DPD":
+        doc["MD"]["INTEGRATOR"] = {"SELECT": "DPD", "DPD": {"DISSAMCEL": 0.0, "DISDIFCEL": 2.0, "DISBG": 0.5}}
+        doc["MD"]["KBT"] = 0.01
+    cfg = tmp_path / "run.json"
+    cfg.write_text(json.dumps(doc))
+    res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    name = doc["OUTPUT"]["NAME"]
+    h5 = str(tmp_path / "out" / "Last" / (name + ".Last.h5"))
+    f = GSDFile(str(tmp_path / "out" / "Last" / (name + ".Last.gsd")))
+    n = int(f.read(0, "particles/N")[0])
+    assert G.h5_read(h5, "R").shape == (n, 1, 2) and n > 20
+    np.testing.assert_array_equal(f.read(0, "particles/diameter"), G.h5_read(h5, "SigmaCore").ravel())
+    np.testing.assert_array_equal(f.read(0, "particles/charge"), G.h5_read(h5, "RHO"))
+    np.testing.assert_array_equal(f.read(0, "particles/mass"), G.h5_read(h5, "PR"))
+    np.testing.assert_array_equal(f.read(0, "particles/velocity")[:, :2], G.h5_read(h5, "Vel").reshape(n, 2))
+    # the same run through the binding: F is the force at the final state
+    r = G.RunInput(str(cfg))
+    eng = r.cycle_engine()
+    eng.upload(**r.cycle_initial_state())
+    for _ in range(doc["MD"]["FRAMES"]):
+        eng.step(doc["MD"]["GTS"])
+        eng.check_positions()
+    s = eng.download()
+    eng.close()
+    np.testing.assert_array_equal(G.h5_read(h5, "F").reshape(n, 2), s["force"].astype(np.float32))
+    np.testing.assert_array_equal(G.h5_read(h5, "T0"), s["t0"])
+    if integrator == "DPD":
+        np.testing.assert_array_equal(G.h5_read(h5, "FD").reshape(n, 2), s["force_dis"].astype(np.float32))
+    # restart from the file
+    c = doc["SPECIES"]["DEFINE"][0]
+    doc["INIT"][c] = {"SELECT": "H5", "H5": {"SELECT": "ALL",
+                                             "ALL": [h5, "R", "Vel", "State", "Theta", "RHO", "SigmaCore"]}}
+    doc["OUTPUT"]["DIR"] = str(tmp_path / "restart")
+    doc["MD"]["FRAMES"] = 2
+    cfg.write_text(json.dumps(doc))
+    st = G.RunInput(str(cfg)).cycle_initial_state()
+    np.testing.assert_array_equal(st["pos"], G.h5_read(h5, "R").reshape(n, 2))
+    res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    g = GSDFile(str(tmp_path / "restart" / (name + ".gsd")))
+    assert int(g.read(0, "particles/N")[0]) == n
+    np.testing.assert_array_equal(g.read(0, "particles/diameter"), f.read(0, "particles/diameter"))
+
+
+def test_runner_two_element_final_state_h5(gpu_lib, tmp_path):
+    G = gpu_lib
+    from cil_cuda_gb300 import build
+    doc = json.load(open(FIXTURE))
+    doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
+    doc["OUTPUT"]["FORMAT"] = ["GSD", "H5"]
+    cfg = tmp_path / "run.json"
+    cfg.write_text(json.dumps(doc))
+    res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    h5 = str(tmp_path / "out" / "Last" / "colony.Last.h5")
+    r = G.RunInput(str(cfg))
+    eng = r.engine()
+    eng.upload(0, **r.initial_state())
+    eng.step(doc["MD"]["GTS"] * doc["MD"]["FRAMES"])
+    g = eng.download(0)
+    frc = eng.forces(0)
+    eng.close()
+    n = g["ncells"]
+    np.testing.assert_array_equal(G.h5_read(h5, "R"), g["pos"].astype(np.float32))
+    np.testing.assert_array_equal(G.h5_read(h5, "SigmaCore"), g["sigma"].astype(np.float32))
+    np.testing.assert_array_equal(G.h5_read(h5, "T0"), g["t0"])
+    np.testing.assert_array_equal(G.h5_read(h5, "F"), frc.astype(np.float32))
+    assert G.h5_read(h5, "RHO").shape == (n,)

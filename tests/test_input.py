@@ -130,7 +130,9 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
     (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
     (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
     (lambda d: d["GPU"].pop("FORCE_LAW"), "GPU.FORCE_LAW"),
-    (lambda d: d["INIT"]["A"].update(SELECT="H5"), "libhdf5"),
+    (lambda d: d["INIT"]["A"].update(SELECT="H5"), "INIT.A.H5 : key not found"),
+    (lambda d: d["INIT"]["A"].update(SELECT="H5", H5={"SELECT": "LOCATION", "LOCATION": ["/nonexistent.h5", "R"]}),
+     "/nonexistent.h5: cannot open"),
     (lambda d: d["SPECIES"]["A"]["APOPTOSIS"].update(APOP_RATE=5000.0), "Apoptosis rate per time step >= 1"),
 ])
 def test_refusals_name_the_key(G, edit, needle):
