@@ -488,7 +488,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
     ap.add_argument("--no-frames", action="store_true", help="skip the frame-output leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
-    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle"], default=None,
+    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "dpd"], default=None,
                     help="run one form only (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -502,6 +502,9 @@ def main():
     if not os.path.exists(G.LIB_PATH):
         from cil_cuda_gb300 import build
         build.build()
+    if args.only == "dpd":
+        print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
+        return 0
     if args.only == "cycle":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1)))

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -919,6 +920,7 @@ struct cil_cycle {
   int *key = nullptr, *bcount = nullptr, *bstart = nullptr, *cursor = nullptr, *list = nullptr, *part = nullptr;
   int *flag = nullptr, *blk = nullptr;
   int nbins = 0, nparts = 0, nblocks = 0;
+  long long nbins_cap = 0;  // bins the arrays hold
   int64_t ts = 0;
   bool uploaded = false;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -978,6 +980,42 @@ cil_status check_params(const cil_cycle_params *p) {
 }
 
 int blocks_for(int n) { return n > 0 ? (n + kTile - 1) / kTile : 1; }
+
+int bins_along(double box, double width) {
+  const int ns = static_cast<int>(box / width);
+  return ns < 1 ? 1 : (ns > 4096 ? 4096 : ns);
+}
+
+// The bin grid of a step call: bins at least 1.05 x max(SIGMA_CORE, the colony's largest
+// diameter) wide, so that the pair search spans one bin on each side (3^D bins) unless cells
+// grow by more than 5 % within the call (the search then widens by itself). Narrower bins than
+// the diameter would make every search span two bins on each side (5^D bins). The host
+// restatement picks its grid by the same rule at the start of each call.
+void set_bins(cil_cycle *h, double smax) {
+  CyConst &C = h->C;
+  const double w = (smax > h->p.sigma_core ? smax : h->p.sigma_core) * 1.05;
+  h->nbins = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < h->p.dim) {
+      const int ns = bins_along(C.box[d], w);
+      C.ns[d] = ns;
+      C.bw[d] = C.box[d] / ns;
+      C.inv_bw[d] = ns / C.box[d];
+    } else {
+      C.ns[d] = 1;
+      C.bw[d] = 1.0;
+      C.inv_bw[d] = 1.0;
+    }
+    h->nbins *= C.ns[d];
+  }
+}
+
+double host_sigma_max(const cil_cycle *h) {
+  double s;
+  const unsigned long long b = h->h_cnt->sigma_max_bits;
+  std::memcpy(&s, &b, sizeof s);
+  return s;
+}
 
 // scan of count[0..m) into start[0..m] (start[m] = total)
 void scan_into(cil_cycle *h, const int *count, int m, int *start) {
@@ -1105,22 +1143,12 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     C.half[d] = 0.5 * C.box[d];
   }
   // bins: width at least the diameter of a new cell (the search widens as cells grow)
-  h->nbins = 1;
-  for (int d = 0; d < 3; ++d) {
-    if (d < p->dim) {
-      int ns = static_cast<int>(C.box[d] / p->sigma_core);
-      ns = ns < 1 ? 1 : (ns > 4096 ? 4096 : ns);
-      C.ns[d] = ns;
-      C.bw[d] = C.box[d] / ns;
-      C.inv_bw[d] = ns / C.box[d];
-    } else {
-      C.ns[d] = 1;
-      C.bw[d] = 1.0;
-      C.inv_bw[d] = 1.0;
-    }
-    h->nbins *= C.ns[d];
-  }
+  // bin arrays for the finest grid the colony can use (width SIGMA_CORE); set_bins picks the
+  // grid of each call
+  h->nbins_cap = 1;
+  for (int d = 0; d < p->dim; ++d) h->nbins_cap *= bins_along(C.box[d], p->sigma_core);
   C.sigma_core = p->sigma_core;
+  set_bins(h, p->sigma_core);
   C.hz_c = (1 - p->nu * p->nu) / p->E;
   C.adhesion = p->adhesion;
   C.motility = p->motility;
@@ -1194,16 +1222,16 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     ok = h->vs != nullptr;
   }
   h->nblocks = blocks_for(capacity);
-  h->nparts = (h->nbins + kScanTile - 1) / kScanTile + 1;
+  h->nparts = (h->nbins_cap + kScanTile - 1) / kScanTile + 1;
   if (ok) {
     h->xs = h->alloc<double>(D * cap);
     h->frc = h->alloc<double>(D * cap);
     h->cnt = h->alloc<CyCounters>(1);
     h->ts_dev = h->alloc<int>(1);
     h->key = h->alloc<int>(cap);
-    h->bcount = h->alloc<int>(h->nbins + 1);
-    h->bstart = h->alloc<int>(h->nbins + 1);
-    h->cursor = h->alloc<int>(h->nbins + 1);
+    h->bcount = h->alloc<int>(h->nbins_cap + 1);
+    h->bstart = h->alloc<int>(h->nbins_cap + 1);
+    h->cursor = h->alloc<int>(h->nbins_cap + 1);
     h->list = h->alloc<int>(cap);
     h->part = h->alloc<int>(h->nparts + 1);
     h->flag = h->alloc<int>(cap);
@@ -1282,11 +1310,15 @@ cil_status cil_cycle_upload(cil_cycle *h, const cil_cycle_view *v) {
     CY_TRY(h, cudaMemcpy(S.tp, v->tpressure, sizeof(int) * n, cudaMemcpyHostToDevice));
   }
   k_cy_sigma_max<<<blocks_for(h->cap), kTile, 0, h->stream>>>(h->C, S, h->cnt);
-  if (h->C.dpd) dpd_initial_forces(h);
   CY_TRY(h, cudaGetLastError());
-  CY_TRY(h, cudaStreamSynchronize(h->stream));
+  const cil_status st = read_counters(h);
+  if (st != CIL_OK) return st;
+  set_bins(h, host_sigma_max(h));
   h->uploaded = true;
-  return h->C.dpd ? read_counters(h) : CIL_OK;
+  if (!h->C.dpd) return CIL_OK;
+  dpd_initial_forces(h);
+  CY_TRY(h, cudaGetLastError());
+  return read_counters(h);
 }
 
 cil_status cil_cycle_step(cil_cycle *h, int32_t nsteps, int64_t *ts) {
@@ -1294,6 +1326,8 @@ cil_status cil_cycle_step(cil_cycle *h, int32_t nsteps, int64_t *ts) {
   if (!h->uploaded) return h->fail(CIL_ERR_STATE, "cil_cycle_step before cil_cycle_upload");
   if (nsteps < 0) return h->fail(CIL_ERR_CONFIG, "negative step count");
   CY_TRY(h, cudaSetDevice(h->device));
+  // the counters of the last call (every entry point ends by reading them)
+  set_bins(h, host_sigma_max(h));
   h->launches = 0;
   CY_TRY(h, cudaEventRecord(h->ev[0], h->stream));
   for (int k = 0; k < nsteps; ++k) {

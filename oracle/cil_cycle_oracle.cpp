@@ -152,14 +152,7 @@ struct Model {
     cap = capacity;
     k0 = static_cast<uint32_t>(seed);
     k1 = static_cast<uint32_t>(seed >> 32);
-    for (int d = 0; d < 3; ++d) {
-      if (d < D) {
-        int n = static_cast<int>(q.box[d] / q.sigma_core);
-        n = n < 1 ? 1 : (n > 4096 ? 4096 : n);
-        ns[d] = n;
-        inv_bw[d] = n / q.box[d];
-      }
-    }
+    rebin();
     tau_r = q.cycle_tau_r * q.tau_div_mu / q.dt;
     tau_v = q.cycle_tau_v * q.tau_div_mu / q.dt;
     tau_p = q.cycle_tau_p * q.tau_div_mu / q.dt;
@@ -174,6 +167,22 @@ struct Model {
     kick_div = 2 * (2 * q.mass);
     sqrt_dt = std::sqrt(q.dt);
     sigma_r = std::sqrt(2 * q.dis_diff * q.kbt);
+  }
+
+  // the bin grid of a call: width >= 1.05 x max(SIGMA_CORE, the largest diameter), the GPU
+  // model's rule
+  void rebin() {
+    const double w = (smax > p.sigma_core ? smax : p.sigma_core) * 1.05;
+    for (int d = 0; d < 3; ++d) {
+      ns[d] = 1;
+      inv_bw[d] = 1;
+      if (d < D) {
+        int n = static_cast<int>(p.box[d] / w);
+        n = n < 1 ? 1 : (n > 4096 ? 4096 : n);
+        ns[d] = n;
+        inv_bw[d] = n / p.box[d];
+      }
+    }
   }
 
   int bin_coord(double x, int d) const {
@@ -647,11 +656,13 @@ void cyo_set_state(void *h, int32_t n, int32_t ts, const double *pos, const doub
     c.tsw = -1;
     m->smax = std::fmax(m->smax, c.sig);
   }
+  m->rebin();
   if (m->p.integrator == 1) m->dpd_forces(ts, false);  // the forces before the first step (CIL.cu:1096)
 }
 
 int32_t cyo_step(void *h, int32_t nsteps) {
   Model *m = static_cast<Model *>(h);
+  m->rebin();
   for (int s = 0; s < nsteps; ++s) m->step();
   return m->err;
 }
