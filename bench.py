@@ -384,7 +384,8 @@ def run_cycle(G, device, steps, warmup, precision=0, dpd=False):
     out = {"value": (n0 + n1) / 2 * steps / dev_s, "unit": "cell-steps/s", "cells": n0, "cells_end": n1,
            "steps": steps, "ms_per_step": tm["total_ms"] / steps, "gpu_launches": tm["launches"],
            "config": "single-element cell-cycle model (PRX_MDCK_2D.json parameters), "
-                     + ("DPD, " if dpd else "") + ("FP32 contacts / FP64 state" if precision else "FP64")
+                     + ("DPD, " if dpd else "")
+                     + (("FP32 pair terms" if dpd else "FP32 contacts") + " / FP64 state" if precision else "FP64")
                      + ", 1M cells"}
     if precision or dpd:
         return out
@@ -504,6 +505,7 @@ def main():
         build.build()
     if args.only == "dpd":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
+        print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1, dpd=True)))
         return 0
     if args.only == "cycle":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
@@ -620,6 +622,8 @@ def main():
             line["cycle_model"] = run_cycle(G, device, min(args.steps, 200), args.warmup)
             line["cycle_model"]["fp32_contacts"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1)
             line["cycle_model"]["dpd"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 0, dpd=True)
+            line["cycle_model"]["dpd"]["fp32_pair_terms"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1,
+                                                                      dpd=True)
         except G.CilError as e:
             line["cycle_model"] = {"error": str(e)}
     if not args.no_e2e:

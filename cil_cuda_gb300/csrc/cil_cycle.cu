@@ -34,6 +34,10 @@
 #include "cil_cycle.h"
 #include "cil_internal.cuh"
 
+// Axis loops: unrolled to three with a guard, so that per-axis arrays stay in registers (the
+// dimension is a run-time value)
+#define CY_AXES(d, D) _Pragma("unroll") for (int d = 0; d < 3; ++d) if (d < (D))
+
 namespace {
 
 using cil::kTile;
@@ -167,7 +171,7 @@ __device__ inline double wrap(double t, double L) {  // fmod(t + L, L)
 
 __device__ inline int bin_of(const CyConst &C, const double *xd) {
   int b = 0;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     int v = static_cast<int>(xd[d] * C.inv_bw[d]);
     v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
     b = b * C.ns[d] + v;
@@ -184,7 +188,7 @@ struct Stencil {
 
 __device__ inline void stencil_of(const CyConst &C, const double *xi, double radius, Stencil &s) {
   for (int d = 0; d < 3; ++d) s.bi[d] = s.lo[d] = s.hi[d] = 0;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     int v = static_cast<int>(xi[d] * C.inv_bw[d]);
     v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
     s.bi[d] = v;
@@ -206,7 +210,7 @@ __device__ inline void stencil_of(const CyConst &C, const double *xi, double rad
 __device__ inline int stencil_bin(const CyConst &C, const Stencil &s, int o0, int o1, int o2) {
   const int oo[3] = {o0, o1, o2};
   int b = 0;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     int v = s.bi[d] + oo[d];
     if (v < 0) v += C.ns[d];
     if (v >= C.ns[d]) v -= C.ns[d];
@@ -220,7 +224,7 @@ __device__ inline int stencil_bin(const CyConst &C, const Stencil &s, int o0, in
 __device__ inline double separation(const CyConst &C, const CySet &S, const double *xi, int j, double *rij) {
   const size_t cap = C.capacity;
   double r2 = 0.0;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     double dd = S.x[d * cap + j] - xi[d];
     if (C.periodic[d]) {
       if (dd > C.half[d])
@@ -310,7 +314,7 @@ __global__ void k_cy_keys(CyConst C, CySet S, const CyCounters *cnt, int *key, i
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt->n) return;
   double xd[3];
-  for (int d = 0; d < C.D; ++d) xd[d] = S.x[static_cast<size_t>(d) * C.capacity + i];
+  CY_AXES(d, C.D) xd[d] = S.x[static_cast<size_t>(d) * C.capacity + i];
   const int b = bin_of(C, xd);
   key[i] = b;
   atomicAdd(count + b, 1);
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   const size_t cap = C.capacity;
   const int D = C.D;
   double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, F[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) {
+  CY_AXES(d, D) {
     xi[d] = S.x[d * cap + i];
     vi[d] = S.v[d * cap + i];
   }
@@ -372,7 +376,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   // ---- motility along the velocity (singleCellForce, MD.cu:600-646)
   {
     double v2 = 0.0;
-    for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+    CY_AXES(d, D) v2 += vi[d] * vi[d];
     double vl = sqrt(v2);
     if (vl == 0.0) {  // a direction at random, length 1e-11 (BIG_TOL_MP)
       const u32x4 r = draw(C, i, ts, kCyDir, 0);
@@ -389,17 +393,17 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
         vi[2] = 1e-11 * z;
       }
       v2 = 0.0;
-      for (int d = 0; d < D; ++d) v2 += vi[d] * vi[d];
+      CY_AXES(d, D) v2 += vi[d] * vi[d];
       vl = sqrt(v2);
     }
-    for (int d = 0; d < D; ++d) F[d] = C.motility * (vi[d] / vl);
+    CY_AXES(d, D) F[d] = C.motility * (vi[d] / vl);
   }
   // ---- passive noise (CIL.cu:84-97)
   if (C.noise_amp > 0.0) {
     double nz[4];
     normal2(draw(C, i, ts, kCyNoise, 0), &nz[0], &nz[1]);
     if (D == 3) normal2(draw(C, i, ts, kCyNoise, 1), &nz[2], &nz[3]);
-    for (int d = 0; d < D; ++d) F[d] += C.zeta * (C.noise_amp * nz[d]);
+    CY_AXES(d, D) F[d] += C.zeta * (C.noise_amp * nz[d]);
   }
   // ---- Hertz contacts with adhesion and the pressure (device draft, MD.cu:302-366)
   double pres = 0.0;
@@ -425,7 +429,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             if (MIXED) {
               float df[3] = {0.0f, 0.0f, 0.0f};
               float r2f = 0.0f;
-              for (int d = 0; d < D; ++d) {
+              CY_AXES(d, D) {
                 df[d] = static_cast<float>(rij[d]);
                 r2f += df[d] * df[d];
               }
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
               }
               const float f0 = -fel + adhf * A;
               if (vol != 0.0f) presf -= f0 / vol;
-              for (int d = 0; d < D; ++d) Ff[d] += f0 * df[d];
+              CY_AXES(d, D) Ff[d] += f0 * df[d];
               continue;
             }
             const double sj = S.sig[j];
@@ -475,20 +479,20 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             }
             const double f0 = -fel + C.adhesion * A;
             if (vol != 0.0) pres -= f0 / vol;
-            for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
+            CY_AXES(d, D) F[d] += f0 * rij[d];
           }
         }
     if (MIXED) {
       pres += static_cast<double>(presf);
-      for (int d = 0; d < D; ++d) F[d] += static_cast<double>(Ff[d]);
+      CY_AXES(d, D) F[d] += static_cast<double>(Ff[d]);
     }
   }
   bool finite = true;
-  for (int d = 0; d < D; ++d) finite = finite && isfinite(F[d]);
+  CY_AXES(d, D) finite = finite && isfinite(F[d]);
   S.p[i] = pres;
   if (!finite) atomicOr(&cnt->err, kErrNonFinite);
   if (mode == 1) {
-    for (int d = 0; d < D; ++d) frc[d * cap + i] = F[d];
+    CY_AXES(d, D) frc[d * cap + i] = F[d];
     return;
   }
   // ---- position update with the pressure-dependent friction (CIL.cu:902-939)
@@ -496,7 +500,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   // pow(x, 0) is 1 for every x
   const double pw = C.zeta_p_beta == 0.0 ? 1.0 : pow(pnd, C.zeta_p_beta);
   const double temp = C.dt * 1 / ((C.zeta + C.zeta_p * pw) * area_of(si));
-  for (int d = 0; d < D; ++d) {
+  CY_AXES(d, D) {
     const double t = xi[d] + temp * F[d];
     x_out[d * cap + i] = C.periodic[d] ? wrap(t, C.box[d]) : t;
     S.v[d * cap + i] = F[d] * (temp / C.dt);
@@ -514,7 +518,7 @@ __global__ void __launch_bounds__(kTile) k_dpd_kick_drift(CyConst C, CySet S, co
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt->n) return;
   const size_t cap = C.capacity;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     const size_t k = d * cap + i;
     const double v = kick(C, S.v[k], S.fc[k], S.fd[k], S.fr[k]);
     S.v[k] = v;
@@ -523,8 +527,24 @@ __global__ void __launch_bounds__(kTile) k_dpd_kick_drift(CyConst C, CySet S, co
   }
 }
 
+// Two standard normals in FP32 (Box-Muller on 24-bit uniforms) from the four words of one
+// Philox block, the FP32 counterpart of normal2: its uniforms are normal2's rounded to 24 bits
+// (1 - u from the first word, u from the third), so the two agree to FP32 rounding.
+__device__ inline void normal2f(const u32x4 &r, float *n0, float *n1) {
+  const float u1 = static_cast<float>((1u << 24) - (r.v[0] >> 8)) * 5.9604644775390625e-08f;  // (0, 1]
+  const float u2 = static_cast<float>(r.v[2] >> 8) * 5.9604644775390625e-08f;
+  const float rad = sqrtf(-2.0f * __logf(u1));
+  float sn, cs;
+  __sincosf(6.2831853071795865f * u2, &sn, &cs);
+  *n0 = rad * cs;
+  *n1 = rad * sn;
+}
+
 // Pair dissipative and random forces (cellCellDisRanForce, MD.cu:861-905) over the pairs closer
 // than the lower-index cell's diameter; then, with `kick`, the second half kick into v_out.
+// MIXED: the pair terms in FP32 on the FP64 separation and velocity difference, FP32 normals,
+// summed in FP32 per cell; the kick stays FP64.
+template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *v_out, CyCounters *cnt,
                                                     const int *start, const int *list, const int *ts_dev,
                                                     int key_off, int kick_on) {
@@ -535,11 +555,13 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
   const size_t cap = C.capacity;
   const int D = C.D;
   double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, Fd[3] = {0, 0, 0}, Fr[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) {
+  CY_AXES(d, D) {
     xi[d] = S.x[d * cap + i];
     vi[d] = S.v[d * cap + i];
   }
   const double si = S.sig[i];
+  const float gdf = static_cast<float>(C.gamma_d), srf = static_cast<float>(C.sigma_r);
+  float Fdf[3] = {0.0f, 0.0f, 0.0f}, Frf[3] = {0.0f, 0.0f, 0.0f};
   Stencil st;
   stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
   for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
@@ -550,7 +572,31 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
           const int j = list[q];
           if (j == i) continue;
           double rij[3] = {0, 0, 0};
-          const double r = sqrt(separation(C, S, xi, j, rij));
+          const double r2d = separation(C, S, xi, j, rij);
+          if (MIXED) {
+            float df[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
+            CY_AXES(d, D) {
+              df[d] = static_cast<float>(rij[d]);
+              r2 += df[d] * df[d];
+            }
+            const float rc = static_cast<float>(i < j ? si : S.sig[j]);
+            if (!(r2 < rc * rc) || r2 == 0.0f) continue;
+            const float rinv = rsqrtf(r2);
+            const float w = 1.0f - r2 * rinv / rc;
+            const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
+            float xf[4];
+            normal2f(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xf[0], &xf[1]);
+            if (D == 3) normal2f(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xf[2], &xf[3]);
+            const float sw = sqrtf(w);
+            CY_AXES(d, D) {
+              const float nd = df[d] * rinv;
+              const float dv = static_cast<float>(vi[d] - S.v[d * cap + j]);
+              Fdf[d] -= gdf * w * (dv * nd) * nd;
+              Frf[d] += srf * sw * nd * xf[d];
+            }
+            continue;
+          }
+          const double r = sqrt(r2d);
           const double rc = i < j ? si : S.sig[j];
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - (r / rc);
@@ -559,7 +605,7 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
           normal2(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xi_n[0], &xi_n[1]);
           if (D == 3) normal2(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xi_n[2], &xi_n[3]);
           const double sw = sqrt(w);
-          for (int d = 0; d < D; ++d) {
+          CY_AXES(d, D) {
             const double nd = rij[d] / r;
             const double vj = S.v[d * cap + j];
             Fd[d] -= C.gamma_d * w * ((vi[d] - vj) * nd) * nd;
@@ -567,8 +613,13 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
           }
         }
       }
+  if (MIXED)
+    CY_AXES(d, D) {
+      Fd[d] = static_cast<double>(Fdf[d]);
+      Fr[d] = static_cast<double>(Frf[d]);
+    }
   bool finite = true;
-  for (int d = 0; d < D; ++d) {
+  CY_AXES(d, D) {
     const size_t k = d * cap + i;
     S.fd[k] = Fd[d];
     S.fr[k] = Fr[d];
@@ -584,6 +635,7 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
 // Background and pair dissipation at the new velocities (calculDisForces, CIL.cu:294-364:
 // sameCellDisForce zeroes a single-element cell's Fd, cellBackDisForce subtracts gamma_bg v,
 // cellCellDisForce, MD.cu:951-985, with w = 1 - r^2 / sigma_core for r < sigma_core)
+template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyCounters *cnt, const int *start,
                                                    const int *list) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -592,13 +644,15 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
   const size_t cap = C.capacity;
   const int D = C.D;
   double xi[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, Fd[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) {
+  CY_AXES(d, D) {
     xi[d] = S.x[d * cap + i];
     vi[d] = S.v[d * cap + i];
     Fd[d] = 0;
     Fd[d] -= C.gamma_b * vi[d];
   }
   const double rc = C.sigma_core;
+  const float rcf = static_cast<float>(rc), gdf = static_cast<float>(C.gamma_d);
+  float Fdf[3] = {0.0f, 0.0f, 0.0f};
   const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
   Stencil st;
   stencil_of(C, xi, smax > rc ? smax : rc, st);
@@ -610,16 +664,33 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
           const int j = list[q];
           if (j == i) continue;
           double rij[3] = {0, 0, 0};
-          const double r = sqrt(separation(C, S, xi, j, rij));
+          const double r2d = separation(C, S, xi, j, rij);
+          if (MIXED) {
+            float df[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
+            CY_AXES(d, D) {
+              df[d] = static_cast<float>(rij[d]);
+              r2 += df[d] * df[d];
+            }
+            if (!(r2 < rcf * rcf) || r2 == 0.0f) continue;
+            const float rinv = rsqrtf(r2);
+            const float w = 1.0f - r2 / rcf;
+            CY_AXES(d, D) {
+              const float nd = -df[d] * rinv;
+              const float dv = static_cast<float>(vi[d] - S.v[d * cap + j]);
+              Fdf[d] -= gdf * w * (dv * nd) * nd;
+            }
+            continue;
+          }
+          const double r = sqrt(r2d);
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - ((r * r) / rc);
-          for (int d = 0; d < D; ++d) {
+          CY_AXES(d, D) {
             const double nd = -rij[d] / r;
             Fd[d] -= C.gamma_d * w * ((vi[d] - S.v[d * cap + j]) * nd) * nd;
           }
         }
       }
-  for (int d = 0; d < D; ++d) S.fd[d * cap + i] = Fd[d];
+  CY_AXES(d, D) S.fd[d * cap + i] = MIXED ? Fd[d] + static_cast<double>(Fdf[d]) : Fd[d];
 }
 
 // ---------------------------------------------------------------- cell cycle and divisions
@@ -721,7 +792,7 @@ __global__ void __launch_bounds__(kTile) k_cy_divide(CyConst C, CySet S, CyCount
         dr[1] = rr * sin(alpha) * sin(beta);
         dr[2] = rr * cos(alpha);
       }
-      for (int d = 0; d < D; ++d) {
+      CY_AXES(d, D) {
         const double m = S.x[d * cap + i];
         double xd = m + dr[d], xm = m + (-dr[d]);
         if (C.periodic[d]) {
@@ -809,7 +880,7 @@ __global__ void __launch_bounds__(kTile) k_cy_mark(CyConst C, CySet S, CyCounter
           k = 0;
       }
     } else {
-      for (int d = 0; d < C.D; ++d) {
+      CY_AXES(d, C.D) {
         const double x = S.x[static_cast<size_t>(d) * C.capacity + i];
         if (!(x >= 0.0 && x < C.box[d])) k = 0;
       }
@@ -830,7 +901,7 @@ __global__ void __launch_bounds__(kTile) k_cy_compact(CyConst C, CySet A, CySet 
   const int dst = block_start[blockIdx.x] + block_excl_scan(k, &tot);
   if (!k) return;
   const size_t cap = C.capacity;
-  for (int d = 0; d < C.D; ++d) {
+  CY_AXES(d, C.D) {
     B.x[d * cap + dst] = A.x[d * cap + i];
     B.v[d * cap + dst] = A.v[d * cap + i];
     if (A.fc) {
@@ -1063,14 +1134,23 @@ void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, 
   h->launches += 1;
 }
 
+void launch_dpd_pair(cil_cycle *h, CySet &S, int key_off, int kick_on) {
+  const int g = blocks_for(h->cap);
+  if (h->p.precision == 1)
+    k_dpd_pair<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
+                                                 kick_on);
+  else
+    k_dpd_pair<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
+                                                  kick_on);
+}
+
 // Fc, pressure, Fd and Fr at the current positions and velocities (the forces the reference
 // evaluates before its first step, CIL.cu:1096), draws keyed by the current step counter
 void dpd_initial_forces(cil_cycle *h) {
   CySet &S = h->set[h->cur];
-  const int g = blocks_for(h->cap);
   bin_cells(h);
   launch_force(h, S, nullptr, S.fc, 1, 0);
-  k_dpd_pair<<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, 0, 0);
+  launch_dpd_pair(h, S, 0, 0);
   h->launches += 1;
 }
 
@@ -1081,9 +1161,12 @@ cil_status enqueue_step(cil_cycle *h) {
     k_dpd_kick_drift<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt);
     bin_cells(h);
     launch_force(h, S, nullptr, S.fc, 1, 1);
-    k_dpd_pair<<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, 1, 1);
+    launch_dpd_pair(h, S, 1, 1);
     std::swap(S.v, h->vs);
-    k_dpd_dis<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
+    if (h->p.precision == 1)
+      k_dpd_dis<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
+    else
+      k_dpd_dis<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
     h->launches += 3;
   } else {
     bin_cells(h);

@@ -116,8 +116,10 @@ typedef struct cil_cycle_params {
   double apop_pressure, apop_duration, apop_rate, extr_gamma;
   int32_t drain;           /* MD.DRAIN: cil_cycle_check_positions removes cells off the box */
   int32_t precision;       /* 0: FP64 throughout (computes what the CPU restatement computes);
-                            * 1: FP32 contact arithmetic on the FP64 separations, FP64 positions,
-                            * forces of motility and noise, and cell state */
+                            * 1: FP32 pair arithmetic on the FP64 separations (the contacts; with
+                            * DPD also the dissipative and random pair terms, with FP32 normals
+                            * from the same counters), FP64 positions, velocities, forces of
+                            * motility and noise, and cell state */
   int32_t integrator;      /* CIL_CYCLE_EULER or CIL_CYCLE_DPD (MD.INTEGRATOR.SELECT) */
   int32_t pad;
   double mass;             /* MASS (DPD) */

@@ -234,3 +234,30 @@ def test_fp32_contacts_follow_fp64(gpu_lib):
     assert np.abs(d).max() < 1e-4
     assert np.abs(a["pressure"] - b["pressure"]).max() < 1e-3 * max(1.0, np.abs(a["pressure"]).max())
     np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
+
+
+def test_dpd_fp32_pair_terms_follow_fp64(gpu_lib):
+    """precision = 1 with DPD: the Hertz, dissipative and random pair terms in FP32 (normals
+    from the same Philox words by FP32 Box-Muller), velocities, positions and the cell state in
+    FP64. Over 100 steps the cells and events are the FP64 run's, the positions agree to 1e-4 and
+    the velocities to 1e-3 of their scale."""
+    G = gpu_lib
+    rng = np.random.default_rng(73)
+    box = [30.0, 30.0, 0.0]
+    prm = dict(DPD, box=box, dt=2e-4, motility=1.0, v1=15.0)
+    st = colony(rng, 400, box)
+    st["vel"] = rng.normal(0, 0.2, size=(400, 2))
+    out = []
+    for prec in (0, 1):
+        eng = G.CycleEngine(dict(prm, precision=prec), 20000, seed=11)
+        eng.upload(**st)
+        eng.step(100)
+        out.append(eng.download())
+        eng.close()
+    a, b = out
+    assert a["ncells"] == b["ncells"] > 400
+    d = a["pos"] - b["pos"]
+    d -= np.round(d / 30.0) * 30.0
+    assert np.abs(d).max() < 1e-4
+    assert np.abs(a["vel"] - b["vel"]).max() < 1e-3 * max(1.0, np.abs(a["vel"]).max())
+    np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
