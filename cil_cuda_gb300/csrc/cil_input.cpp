@@ -564,6 +564,9 @@ void read_single(cil_input *in, const Node &root, const Node &loc, const std::st
     if (!(q.apop_rate * q.dt < 1.0)) key_error(a.path + ".APOP_RATE", "Apoptosis rate per time step >= 1");
   }
   const bool has_gpu = root.has("GPU");
+  // GPU.PRECISION: FP64 (the default here: the reference's arithmetic) or MIXED (FP32 pair terms)
+  if (has_gpu && root.child("GPU").has("PRECISION"))
+    q.precision = root.child("GPU").pick("PRECISION", {"FP64", "MIXED"}) == "MIXED" ? 1 : 0;
   read_init(in, root, cell, 1);
   run.ncells = in->ncells;
   run.capacity = has_gpu && root.child("GPU").has("CAPACITY") ? root.child("GPU").integer("CAPACITY")

@@ -23,7 +23,8 @@
  *               model, cil_cycle.h): PAIRFORCES.HZ (ELASTIC_MODULUS, POISSON_RATIO, SIGMA_CORE,
  *               ADHESION_CONSTANT), MOTILITY, FRICTION, P_FRICTION, P_FRICTION_BETA, NOISE,
  *               DIVISION (TAU_DIVISION, V1, CYCLE_*), APOPTOSIS (the Euler step's cycle-pressure
- *               law, or the DPD step's pressure-time law); MD.OSMOTIC_PRESSURE and MD.DRAIN.
+ *               law, or the DPD step's pressure-time law); MD.OSMOTIC_PRESSURE and MD.DRAIN;
+ *               GPU.PRECISION FP64 (default) or MIXED (cil_cycle_params.precision 1).
  *   INTERACTIONS PAIRFORCES.SELECT "LJ" with ATTRACTION OFF is the reference's own law
  *               (WCA, cil_gpu.h CIL_FORCE_LJ_WCA, epsilon from the species' LJ EPSILON).
  *   GPU         (optional block, this library's own): PRECISION "FP64" | "MIXED", RNG

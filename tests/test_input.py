@@ -257,3 +257,14 @@ def test_single_element_dpd_is_read(G):
     with pytest.raises(G.CilError) as e:
         load(G, d)
     assert "MASS" in str(e.value)
+
+
+def test_single_element_precision_is_read(G):
+    d = json.load(open(SINGLE))
+    assert load(G, d).params["precision"] == 0  # FP64 unless asked
+    d["GPU"] = {"PRECISION": "MIXED"}
+    assert load(G, d).params["precision"] == 1
+    d["GPU"] = {"PRECISION": "FP16"}
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "GPU.PRECISION" in str(e.value)
