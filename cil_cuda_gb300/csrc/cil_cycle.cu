@@ -7,9 +7,11 @@
 //
 // A step (no host synchronisation; the cell count lives on the device):
 //   bins       k_cy_keys / scan / k_cy_scatter / k_cy_sort: a counting sort of the cells into
-//              bins of fixed width (the largest diameter at upload), ascending cell index
+//              bins (width set per call from the largest diameter), ascending cell index
 //              inside a bin; the pair search walks +-k bins with k from the colony's largest
-//              diameter of the previous step, so growing cells never outgrow the search;
+//              diameter of the previous step, so growing cells never outgrow the search; with
+//              FP32 pair arithmetic (precision 1), k_cy_pack writes the FP32 records of the bin
+//              order that the pair loops read instead of the FP64 positions;
 //   forces     k_cy_force: motility along the velocity, passive noise, Hertz contacts with
 //              adhesion and the pressure sum, then the position update with the pressure-
 //              dependent friction, in one thread per cell;
@@ -60,6 +62,7 @@ struct CyConst {
   double dt;
   int ns[3];
   double bw[3];       // bin width per axis
+  float bwf[3], boxf[3], halff[3];  // FP32 copies for the packed pair arithmetic
   double half[3];     // box / 2
   double inv_bw[3];
   double sigma_core;
@@ -91,6 +94,16 @@ struct CySet {
   double *sig, *sigt, *theta, *rho, *om, *p;
   int *tp, *t0, *tsw;
   double *fc, *fd, *fr;  // [D][cap], DPD only (conservative, dissipative, random forces)
+};
+
+// FP32 records of the cells in bin order, for the FP32 pair arithmetic (precision 1): the
+// position relative to the origin of the cell's bin with the diameter, the velocity (DPD), and
+// each cell's place in the bin order. Displacements are then formed in FP32 from bin offsets,
+// with no FP64 operation per candidate.
+struct CyPacked {
+  float4 *pk;  // [q]: x - bin origin per axis (z 0 in 2D), diameter
+  float4 *vk;  // [q]: velocity (DPD)
+  int *qpos;   // [cell]: its place q
 };
 
 struct CyCounters {
@@ -238,6 +251,28 @@ __device__ inline double separation(const CyConst &C, const CySet &S, const doub
   return r2;
 }
 
+__device__ inline float f4c(const float4 &v, int d) { return d == 0 ? v.x : (d == 1 ? v.y : v.z); }
+
+// FP32 displacement from the packed record pi to pj, whose bin lies at offset o from pi's, at
+// the nearest image on periodic axes; returns its square length
+__device__ inline float packed_sep(const CyConst &C, const float4 &pi, const float4 &pj, int o0, int o1, int o2,
+                                   float *df) {
+  const int o[3] = {o0, o1, o2};
+  float r2 = 0.0f;
+  CY_AXES(d, C.D) {
+    float v = f4c(pj, d) + static_cast<float>(o[d]) * C.bwf[d] - f4c(pi, d);
+    if (C.periodic[d]) {
+      if (v > C.halff[d])
+        v -= C.boxf[d];
+      else if (v < -C.halff[d])
+        v += C.boxf[d];
+    }
+    df[d] = v;
+    r2 += v * v;
+  }
+  return r2;
+}
+
 // ---------------------------------------------------------------- block scan
 __device__ inline int block_excl_scan(int v, int *total) {
   __shared__ int ws[kTile / 32];
@@ -349,6 +384,35 @@ __global__ void k_cy_sort(const int *start, int nbins, int *list, CyCounters *cn
   }
 }
 
+// The packed records of the bin order (CyPacked); vk only when velocities are wanted
+__global__ void k_cy_pack(CyConst C, CySet S, const CyCounters *cnt, const int *list, CyPacked P, int with_vel) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= cnt->n) return;
+  const int i = list[q];
+  const size_t cap = C.capacity;
+  float rel[3] = {0.0f, 0.0f, 0.0f}, vf[3] = {0.0f, 0.0f, 0.0f};
+  CY_AXES(d, C.D) {
+    const double x = S.x[d * cap + i];
+    int v = static_cast<int>(x * C.inv_bw[d]);
+    v = v < 0 ? 0 : (v >= C.ns[d] ? C.ns[d] - 1 : v);
+    rel[d] = static_cast<float>(x - v * C.bw[d]);
+    if (with_vel) vf[d] = static_cast<float>(S.v[d * cap + i]);
+  }
+  P.pk[q] = make_float4(rel[0], rel[1], rel[2], static_cast<float>(S.sig[i]));
+  if (with_vel) P.vk[q] = make_float4(vf[0], vf[1], vf[2], 0.0f);
+  P.qpos[i] = q;
+}
+
+__global__ void k_cy_pack_vel(CyConst C, CySet S, const CyCounters *cnt, const int *list, CyPacked P) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= cnt->n) return;
+  const int i = list[q];
+  const size_t cap = C.capacity;
+  float vf[3] = {0.0f, 0.0f, 0.0f};
+  CY_AXES(d, C.D) vf[d] = static_cast<float>(S.v[d * cap + i]);
+  P.vk[q] = make_float4(vf[0], vf[1], vf[2], 0.0f);
+}
+
 // ---------------------------------------------------------------- forces + update
 // MIXED: the candidate test and the contact arithmetic in FP32 on the FP64 separation (GB300
 // runs FP64 at a small fraction of its FP32 rate); the forces and the pressure are summed in
@@ -360,7 +424,7 @@ __global__ void k_cy_sort(const int *start, int nbins, int *list, CyCounters *cn
 template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
                                                     CyCounters *cnt, const int *start, const int *list,
-                                                    const int *ts_dev, int mode, int key_off) {
+                                                    const int *ts_dev, int mode, int key_off, CyPacked P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = cnt->n;
   if (i >= n) return;
@@ -416,26 +480,23 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
     const float sif = static_cast<float>(si), c2f = static_cast<float>(c2), adhf = static_cast<float>(C.adhesion);
     const float inv_rif = 2.0f / sif;
     float Ff[3] = {0.0f, 0.0f, 0.0f}, presf = 0.0f;
+    const int qi = MIXED ? P.qpos[i] : 0;
+    const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
       for (int o1 = (D > 1 ? st.lo[1] : 0); o1 <= (D > 1 ? st.hi[1] : 0); ++o1)
         for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
           const int b = stencil_bin(C, st, o0, o1, o2);
           const int e0 = start[b], e1 = start[b + 1];
           for (int q = e0; q < e1; ++q) {
-            const int j = list[q];
-            if (j == i) continue;
-            double rij[3] = {0, 0, 0};
-            const double r2 = separation(C, S, xi, j, rij);
             if (MIXED) {
+              if (q == qi) continue;
+              const float4 pj = P.pk[q];
               float df[3] = {0.0f, 0.0f, 0.0f};
-              float r2f = 0.0f;
-              CY_AXES(d, D) {
-                df[d] = static_cast<float>(rij[d]);
-                r2f += df[d] * df[d];
-              }
-              const float sjf = static_cast<float>(S.sig[j]);
+              const float r2f = packed_sep(C, pi4, pj, o0, o1, o2, df);
+              const float sjf = pj.w;
               const float cut = 0.5f * (sif + sjf);
               if (!(r2f <= cut * cut) || r2f == 0.0f) continue;
+              const int j = list[q];
               const float r = sqrtf(r2f);
               const float sa = i < j ? sif : sjf, sb = i < j ? sjf : sif;
               const float h = fmaxf(cut - r, 0.0f);
@@ -459,6 +520,10 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
               CY_AXES(d, D) Ff[d] += f0 * df[d];
               continue;
             }
+            const int j = list[q];
+            if (j == i) continue;
+            double rij[3] = {0, 0, 0};
+            const double r2 = separation(C, S, xi, j, rij);
             const double sj = S.sig[j];
             const double cut = (si + sj) / 2;
             if (r2 > 1.0000001 * (cut * cut)) continue;  // outside the contact distance (exact test below)
@@ -547,7 +612,7 @@ __device__ inline void normal2f(const u32x4 &r, float *n0, float *n1) {
 template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *v_out, CyCounters *cnt,
                                                     const int *start, const int *list, const int *ts_dev,
-                                                    int key_off, int kick_on) {
+                                                    int key_off, int kick_on, CyPacked P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = cnt->n;
   if (i >= n) return;
@@ -562,6 +627,9 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
   const double si = S.sig[i];
   const float gdf = static_cast<float>(C.gamma_d), srf = static_cast<float>(C.sigma_r);
   float Fdf[3] = {0.0f, 0.0f, 0.0f}, Frf[3] = {0.0f, 0.0f, 0.0f};
+  const int qi = MIXED ? P.qpos[i] : 0;
+  const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 vi4 = MIXED ? P.vk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   Stencil st;
   stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
   for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
@@ -571,16 +639,13 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
         for (int q = start[b]; q < start[b + 1]; ++q) {
           const int j = list[q];
           if (j == i) continue;
-          double rij[3] = {0, 0, 0};
-          const double r2d = separation(C, S, xi, j, rij);
           if (MIXED) {
-            float df[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
-            CY_AXES(d, D) {
-              df[d] = static_cast<float>(rij[d]);
-              r2 += df[d] * df[d];
-            }
-            const float rc = static_cast<float>(i < j ? si : S.sig[j]);
+            const float4 pj = P.pk[q];
+            float df[3] = {0.0f, 0.0f, 0.0f};
+            const float r2 = packed_sep(C, pi4, pj, o0, o1, o2, df);
+            const float rc = i < j ? pi4.w : pj.w;
             if (!(r2 < rc * rc) || r2 == 0.0f) continue;
+            const float4 vj4 = P.vk[q];
             const float rinv = rsqrtf(r2);
             const float w = 1.0f - r2 * rinv / rc;
             const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
@@ -590,13 +655,14 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
             const float sw = sqrtf(w);
             CY_AXES(d, D) {
               const float nd = df[d] * rinv;
-              const float dv = static_cast<float>(vi[d] - S.v[d * cap + j]);
+              const float dv = f4c(vi4, d) - f4c(vj4, d);
               Fdf[d] -= gdf * w * (dv * nd) * nd;
               Frf[d] += srf * sw * nd * xf[d];
             }
             continue;
           }
-          const double r = sqrt(r2d);
+          double rij[3] = {0, 0, 0};
+          const double r = sqrt(separation(C, S, xi, j, rij));
           const double rc = i < j ? si : S.sig[j];
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - (r / rc);
@@ -637,7 +703,7 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
 // cellCellDisForce, MD.cu:951-985, with w = 1 - r^2 / sigma_core for r < sigma_core)
 template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyCounters *cnt, const int *start,
-                                                   const int *list) {
+                                                   const int *list, CyPacked P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = cnt->n;
   if (i >= n) return;
@@ -653,6 +719,9 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
   const double rc = C.sigma_core;
   const float rcf = static_cast<float>(rc), gdf = static_cast<float>(C.gamma_d);
   float Fdf[3] = {0.0f, 0.0f, 0.0f};
+  const int qi = MIXED ? P.qpos[i] : 0;
+  const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 vi4 = MIXED ? P.vk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
   Stencil st;
   stencil_of(C, xi, smax > rc ? smax : rc, st);
@@ -661,27 +730,26 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
       for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
         const int b = stencil_bin(C, st, o0, o1, o2);
         for (int q = start[b]; q < start[b + 1]; ++q) {
-          const int j = list[q];
-          if (j == i) continue;
-          double rij[3] = {0, 0, 0};
-          const double r2d = separation(C, S, xi, j, rij);
           if (MIXED) {
-            float df[3] = {0.0f, 0.0f, 0.0f}, r2 = 0.0f;
-            CY_AXES(d, D) {
-              df[d] = static_cast<float>(rij[d]);
-              r2 += df[d] * df[d];
-            }
+            if (q == qi) continue;
+            const float4 pj = P.pk[q];
+            float df[3] = {0.0f, 0.0f, 0.0f};
+            const float r2 = packed_sep(C, pi4, pj, o0, o1, o2, df);
             if (!(r2 < rcf * rcf) || r2 == 0.0f) continue;
+            const float4 vj4 = P.vk[q];
             const float rinv = rsqrtf(r2);
             const float w = 1.0f - r2 / rcf;
             CY_AXES(d, D) {
               const float nd = -df[d] * rinv;
-              const float dv = static_cast<float>(vi[d] - S.v[d * cap + j]);
+              const float dv = f4c(vi4, d) - f4c(vj4, d);
               Fdf[d] -= gdf * w * (dv * nd) * nd;
             }
             continue;
           }
-          const double r = sqrt(r2d);
+          const int j = list[q];
+          if (j == i) continue;
+          double rij[3] = {0, 0, 0};
+          const double r = sqrt(separation(C, S, xi, j, rij));
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - ((r * r) / rc);
           CY_AXES(d, D) {
@@ -984,6 +1052,7 @@ struct cil_cycle {
   int cur = 0;
   double *xs = nullptr;   // position output buffer of the force pass
   double *vs = nullptr;   // velocity output buffer of the DPD pair pass
+  CyPacked P{};           // FP32 records of the bin order (precision 1)
   double *frc = nullptr;  // last forces (output only)
   CyCounters *cnt = nullptr;
   CyCounters *h_cnt = nullptr;  // pinned
@@ -1077,6 +1146,7 @@ void set_bins(cil_cycle *h, double smax) {
       C.bw[d] = 1.0;
       C.inv_bw[d] = 1.0;
     }
+    C.bwf[d] = static_cast<float>(C.bw[d]);
     h->nbins *= C.ns[d];
   }
 }
@@ -1107,6 +1177,10 @@ cil_status bin_cells(cil_cycle *h) {
   k_cy_scatter<<<g, kTile, 0, h->stream>>>(h->cnt, h->key, h->bstart, h->cursor, h->list);
   k_cy_sort<<<blocks_for(h->nbins), kTile, 0, h->stream>>>(h->bstart, h->nbins, h->list, h->cnt);
   h->launches += 5;
+  if (h->p.precision == 1) {
+    k_cy_pack<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->list, h->P, h->C.dpd);
+    h->launches += 1;
+  }
   return CIL_OK;
 }
 
@@ -1127,10 +1201,10 @@ void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, 
   const int g = blocks_for(h->cap);
   if (h->p.precision == 1)
     k_cy_force<true><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                 key_off);
+                                                 key_off, h->P);
   else
     k_cy_force<false><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                  key_off);
+                                                  key_off, h->P);
   h->launches += 1;
 }
 
@@ -1138,10 +1212,10 @@ void launch_dpd_pair(cil_cycle *h, CySet &S, int key_off, int kick_on) {
   const int g = blocks_for(h->cap);
   if (h->p.precision == 1)
     k_dpd_pair<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
-                                                 kick_on);
+                                                 kick_on, h->P);
   else
     k_dpd_pair<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
-                                                  kick_on);
+                                                  kick_on, h->P);
 }
 
 // Fc, pressure, Fd and Fr at the current positions and velocities (the forces the reference
@@ -1163,10 +1237,13 @@ cil_status enqueue_step(cil_cycle *h) {
     launch_force(h, S, nullptr, S.fc, 1, 1);
     launch_dpd_pair(h, S, 1, 1);
     std::swap(S.v, h->vs);
-    if (h->p.precision == 1)
-      k_dpd_dis<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
-    else
-      k_dpd_dis<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list);
+    if (h->p.precision == 1) {  // the records take the new velocities
+      k_cy_pack_vel<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->list, h->P);
+      k_dpd_dis<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
+      h->launches += 1;
+    } else {
+      k_dpd_dis<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
+    }
     h->launches += 3;
   } else {
     bin_cells(h);
@@ -1224,8 +1301,9 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     C.periodic[d] = d < p->dim ? p->periodic[d] : 0;
     C.box[d] = d < p->dim ? p->box[d] : 1.0;
     C.half[d] = 0.5 * C.box[d];
+    C.boxf[d] = static_cast<float>(C.box[d]);
+    C.halff[d] = static_cast<float>(C.half[d]);
   }
-  // bins: width at least the diameter of a new cell (the search widens as cells grow)
   // bin arrays for the finest grid the colony can use (width SIGMA_CORE); set_bins picks the
   // grid of each call
   h->nbins_cap = 1;
@@ -1303,6 +1381,12 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
   if (ok && C.dpd) {
     h->vs = h->alloc<double>(D * cap);
     ok = h->vs != nullptr;
+  }
+  if (ok && p->precision == 1) {
+    h->P.pk = h->alloc<float4>(cap);
+    h->P.qpos = h->alloc<int>(cap);
+    h->P.vk = C.dpd ? h->alloc<float4>(cap) : nullptr;
+    ok = h->P.pk && h->P.qpos && (!C.dpd || h->P.vk);
   }
   h->nblocks = blocks_for(capacity);
   h->nparts = (h->nbins_cap + kScanTile - 1) / kScanTile + 1;
