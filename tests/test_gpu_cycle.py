@@ -212,14 +212,20 @@ def test_shipped_configuration_grows_from_one_cell(gpu_lib):
     assert np.all(np.isfinite(s["pos"])) and np.all(np.isfinite(s["sigma"]))
 
 
-def test_fp32_contacts_follow_fp64(gpu_lib):
-    """precision = 1: FP32 contact arithmetic on the FP64 separations. Over 100 steps it keeps
-    the FP64 run's cells and events, and its positions and pressures to FP32 rounding."""
+FP32_CASES = [(2, 30.0, 400), (3, 12.0, 700), (2, 3.4, 6)]  # the last: 2 bins per axis, whole-axis searches
+
+
+@pytest.mark.parametrize("dim,L,n", FP32_CASES)
+def test_fp32_contacts_follow_fp64(gpu_lib, dim, L, n):
+    """precision = 1: FP32 contact arithmetic on packed FP32 records of the bin order. Over 100
+    steps it keeps the FP64 run's cells and events, and its positions and pressures to FP32
+    rounding; in 2D and 3D, and in a box of two bins per axis, where the search covers each
+    axis whole and the FP32 nearest-image fold applies."""
     G = gpu_lib
-    rng = np.random.default_rng(71)
-    box = [30.0, 30.0, 0.0]
-    prm = dict(box=box, dt=2e-4, motility=1.0, zeta=0.2, noise_D=0.002, v1=15.0)
-    st = colony(rng, 400, box)
+    rng = np.random.default_rng(71 + dim)
+    box = [L, L, L if dim == 3 else 0.0]
+    prm = dict(dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, zeta=0.2, noise_D=0.002, v1=15.0)
+    st = colony(rng, n, box, dim)
     out = []
     for prec in (0, 1):
         eng = G.CycleEngine(dict(prm, precision=prec), 20000, seed=11)
@@ -228,25 +234,27 @@ def test_fp32_contacts_follow_fp64(gpu_lib):
         out.append(eng.download())
         eng.close()
     a, b = out
-    assert a["ncells"] == b["ncells"] > 400
+    assert a["ncells"] == b["ncells"] >= n
     d = a["pos"] - b["pos"]
-    d -= np.round(d / 30.0) * 30.0
+    d -= np.round(d / L) * L
     assert np.abs(d).max() < 1e-4
     assert np.abs(a["pressure"] - b["pressure"]).max() < 1e-3 * max(1.0, np.abs(a["pressure"]).max())
+    assert np.abs(a["pressure"]).max() > 0
     np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
 
 
-def test_dpd_fp32_pair_terms_follow_fp64(gpu_lib):
+@pytest.mark.parametrize("dim,L,n", FP32_CASES)
+def test_dpd_fp32_pair_terms_follow_fp64(gpu_lib, dim, L, n):
     """precision = 1 with DPD: the Hertz, dissipative and random pair terms in FP32 (normals
     from the same Philox words by FP32 Box-Muller), velocities, positions and the cell state in
     FP64. Over 100 steps the cells and events are the FP64 run's, the positions agree to 1e-4 and
     the velocities to 1e-3 of their scale."""
     G = gpu_lib
-    rng = np.random.default_rng(73)
-    box = [30.0, 30.0, 0.0]
-    prm = dict(DPD, box=box, dt=2e-4, motility=1.0, v1=15.0)
-    st = colony(rng, 400, box)
-    st["vel"] = rng.normal(0, 0.2, size=(400, 2))
+    rng = np.random.default_rng(73 + dim)
+    box = [L, L, L if dim == 3 else 0.0]
+    prm = dict(DPD, dim=dim, box=box, periodic=[1, 1, 1], dt=2e-4, motility=1.0, v1=15.0)
+    st = colony(rng, n, box, dim)
+    st["vel"] = rng.normal(0, 0.2, size=(n, dim))
     out = []
     for prec in (0, 1):
         eng = G.CycleEngine(dict(prm, precision=prec), 20000, seed=11)
@@ -255,9 +263,9 @@ def test_dpd_fp32_pair_terms_follow_fp64(gpu_lib):
         out.append(eng.download())
         eng.close()
     a, b = out
-    assert a["ncells"] == b["ncells"] > 400
+    assert a["ncells"] == b["ncells"] >= n
     d = a["pos"] - b["pos"]
-    d -= np.round(d / 30.0) * 30.0
+    d -= np.round(d / L) * L
     assert np.abs(d).max() < 1e-4
     assert np.abs(a["vel"] - b["vel"]).max() < 1e-3 * max(1.0, np.abs(a["vel"]).max())
     np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
