@@ -410,6 +410,31 @@ def run_cycle(G, device, steps, warmup, precision=0, dpd=False):
     return out
 
 
+def run_cycle_small(G, device, steps=3000, warmup=3):
+    """The cell-cycle model at the sizes the shipped runs spend their time at (they start from
+    one or two cells): 1024 cells on the same lattice in a periodic 35.2^2 box, FP64, with the
+    step replayed as a captured CUDA graph (the default) and launched kernel by kernel."""
+    side = 32
+    rng = np.random.default_rng(19)
+    n = side * side
+    g = (np.arange(n) % side, np.arange(n) // side)
+    pos = np.stack([(g[0] + 0.5) * 1.1, (g[1] + 0.5) * 1.1], axis=1) + rng.uniform(-0.05, 0.05, size=(n, 2))
+    st = dict(pos=pos, sigma=np.full(n, 1.1283791670955126), theta=rng.uniform(0, 1, n), rho=np.ones(n),
+              angvel=np.full(n, 1e-5))
+    out = {"cells": n, "steps": steps, "unit": "ms per step"}
+    for name, flags in (("graphs", 0), ("launches", G.CYCLE_NO_GRAPH)):
+        prm = dict(box=[side * 1.1, side * 1.1, 0.0], dt=1e-5, motility=1.0, zeta=0.01, v1=15.0, flags=flags)
+        eng = G.CycleEngine(prm, 4 * n, seed=3, device=device)
+        eng.upload(**st)
+        eng.step(warmup)
+        eng.step(steps)
+        tm = eng.timings()
+        eng.close()
+        out[name] = tm["total_ms"] / steps
+    out["speedup"] = out["launches"] / out["graphs"]
+    return out
+
+
 def cpu_baseline(p, st, threads: int, budget_s: float = 20.0):
     """The oracle (race-free OpenMP variant of the reference's step) on the host cores on
     the same 2M-particle state, as many whole steps as fit the budget (at least 1)."""
@@ -508,6 +533,7 @@ def main():
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1, dpd=True)))
         return 0
     if args.only == "cycle":
+        print(json.dumps(run_cycle_small(G, device)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
@@ -621,6 +647,7 @@ def main():
         try:
             line["cycle_model"] = run_cycle(G, device, min(args.steps, 200), args.warmup)
             line["cycle_model"]["fp32_contacts"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1)
+            line["cycle_model"]["small_colony"] = run_cycle_small(G, device)
             line["cycle_model"]["dpd"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 0, dpd=True)
             line["cycle_model"]["dpd"]["fp32_pair_terms"] = run_cycle(G, device, min(args.steps, 200), args.warmup, 1,
                                                                       dpd=True)

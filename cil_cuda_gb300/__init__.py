@@ -187,6 +187,7 @@ class RunInfo(C.Structure):
 FRAME_TYPES_IN_FIRST = 1
 APOP_NONE, APOP_CYCLE_PRESSURE, APOP_PRESSURE_TIME, APOP_RATE, APOP_CYCLE, APOP_CYCLE_EXTRUDE = 0, 1, 2, 3, 4, 5
 CYCLE_EULER, CYCLE_DPD = 0, 1
+CYCLE_NO_GRAPH = 1
 
 CYCLE_FIELDS = [
     ("dim", C.c_int32), ("periodic", C.c_int32 * 3), ("box", C.c_double * 3), ("dt", C.c_double),
@@ -200,7 +201,7 @@ CYCLE_FIELDS = [
     ("cycle_p_shift", C.c_double), ("cycle_p_shift_tau", C.c_double), ("osmotic_pressure", C.c_double),
     ("apop_pressure", C.c_double), ("apop_duration", C.c_double), ("apop_rate", C.c_double),
     ("extr_gamma", C.c_double), ("drain", C.c_int32), ("precision", C.c_int32),
-    ("integrator", C.c_int32), ("pad", C.c_int32), ("mass", C.c_double), ("kbt", C.c_double),
+    ("integrator", C.c_int32), ("flags", C.c_int32), ("mass", C.c_double), ("kbt", C.c_double),
     ("dis_same", C.c_double), ("dis_diff", C.c_double), ("dis_bg", C.c_double), ("extr_rate", C.c_double),
 ]
 
@@ -282,7 +283,7 @@ def cycle_params(**kw) -> CycleParams:
                 cycle_tau_r=1.0, cycle_tau_v=1.0, cycle_tau_p=0.0, cycle_sigma_min=1.1283791670955126, cycle_p0=5.0,
                 cycle_beta_vs=0.0, cycle_rho_ratio=1.0, cycle_r_maxed=1.0, cycle_p_shift=0.0, cycle_p_shift_tau=0.0,
                 osmotic_pressure=0.0, apop_pressure=1.0, apop_duration=8.0, apop_rate=0.0, extr_gamma=0.0, drain=0,
-                precision=0, integrator=CYCLE_EULER, pad=0, mass=1.0, kbt=0.0, dis_same=0.0, dis_diff=0.0,
+                precision=0, integrator=CYCLE_EULER, flags=0, mass=1.0, kbt=0.0, dis_same=0.0, dis_diff=0.0,
                 dis_bg=0.0, extr_rate=0.0)
     base.update(kw)
     q = CycleParams()

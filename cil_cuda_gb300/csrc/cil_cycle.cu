@@ -1054,6 +1054,22 @@ struct cil_cycle {
   double *vs = nullptr;   // velocity output buffer of the DPD pair pass
   CyPacked P{};           // FP32 records of the bin order (precision 1)
   double *frc = nullptr;  // last forces (output only)
+  // captured steps: keyed by the buffer configuration before the step and the bin grid, each
+  // records the configuration after it (a step rotates x / xs, v / vs and the state sets)
+  struct Buffers {
+    CySet set[2];
+    double *xs, *vs;
+    int cur;
+  };
+  struct StepGraph {
+    Buffers before, after;
+    uint64_t grid;
+    cudaGraphExec_t exec;
+    int64_t nodes;
+  };
+  std::vector<StepGraph> graphs;
+  uint64_t grid_gen = 0;
+  int pair_bs = kTile;  // threads per block of the per-cell pair kernels (set per call)
   CyCounters *cnt = nullptr;
   CyCounters *h_cnt = nullptr;  // pinned
   int *ts_dev = nullptr;
@@ -1121,6 +1137,11 @@ cil_status check_params(const cil_cycle_params *p) {
 
 int blocks_for(int n) { return n > 0 ? (n + kTile - 1) / kTile : 1; }
 
+constexpr int kNumSMs = 152;  // GB300
+
+// grid of a per-cell pair kernel at h->pair_bs threads per block
+int pair_grid(const cil_cycle *h) { return (h->cap + h->pair_bs - 1) / h->pair_bs; }
+
 int bins_along(double box, double width) {
   const int ns = static_cast<int>(box / width);
   return ns < 1 ? 1 : (ns > 4096 ? 4096 : ns);
@@ -1131,9 +1152,18 @@ int bins_along(double box, double width) {
 // grow by more than 5 % within the call (the search then widens by itself). Narrower bins than
 // the diameter would make every search span two bins on each side (5^D bins). The host
 // restatement picks its grid by the same rule at the start of each call.
-void set_bins(cil_cycle *h, double smax) {
+void set_bins(cil_cycle *h, double smax, int ncells) {
   CyConst &C = h->C;
   const double w = (smax > h->p.sigma_core ? smax : h->p.sigma_core) * 1.05;
+  const int before[3] = {C.ns[0], C.ns[1], C.ns[2]};
+  // blocks of the per-cell pair kernels (FP64-heavy, no block cooperation): small enough that
+  // a small colony still spreads over every SM (two blocks per SM), 32 to kTile threads
+  const int bs_before = h->pair_bs;
+  h->pair_bs = 32;
+  while (h->pair_bs < kTile && static_cast<long long>(h->pair_bs) * 2 * kNumSMs < ncells) h->pair_bs *= 2;
+  // the grids cover the capacity: keep them at most 65536 blocks (a large capacity, few cells)
+  while (h->pair_bs < kTile && (h->cap + h->pair_bs - 1) / h->pair_bs > 65536) h->pair_bs *= 2;
+  if (h->pair_bs != bs_before) h->grid_gen += 1;
   h->nbins = 1;
   for (int d = 0; d < 3; ++d) {
     if (d < h->p.dim) {
@@ -1149,6 +1179,7 @@ void set_bins(cil_cycle *h, double smax) {
     C.bwf[d] = static_cast<float>(C.bw[d]);
     h->nbins *= C.ns[d];
   }
+  if (C.ns[0] != before[0] || C.ns[1] != before[1] || C.ns[2] != before[2]) h->grid_gen += 1;
 }
 
 double host_sigma_max(const cil_cycle *h) {
@@ -1198,23 +1229,23 @@ cil_status removals(cil_cycle *h, int mode) {
 }
 
 void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, int key_off) {
-  const int g = blocks_for(h->cap);
+  const int g = pair_grid(h), bs = h->pair_bs;
   if (h->p.precision == 1)
-    k_cy_force<true><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
+    k_cy_force<true><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
                                                  key_off, h->P);
   else
-    k_cy_force<false><<<g, kTile, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
+    k_cy_force<false><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
                                                   key_off, h->P);
   h->launches += 1;
 }
 
 void launch_dpd_pair(cil_cycle *h, CySet &S, int key_off, int kick_on) {
-  const int g = blocks_for(h->cap);
+  const int g = pair_grid(h), bs = h->pair_bs;
   if (h->p.precision == 1)
-    k_dpd_pair<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
+    k_dpd_pair<true><<<g, bs, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
                                                  kick_on, h->P);
   else
-    k_dpd_pair<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
+    k_dpd_pair<false><<<g, bs, 0, h->stream>>>(h->C, S, h->vs, h->cnt, h->bstart, h->list, h->ts_dev, key_off,
                                                   kick_on, h->P);
 }
 
@@ -1239,10 +1270,10 @@ cil_status enqueue_step(cil_cycle *h) {
     std::swap(S.v, h->vs);
     if (h->p.precision == 1) {  // the records take the new velocities
       k_cy_pack_vel<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->list, h->P);
-      k_dpd_dis<true><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
+      k_dpd_dis<true><<<pair_grid(h), h->pair_bs, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
       h->launches += 1;
     } else {
-      k_dpd_dis<false><<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
+      k_dpd_dis<false><<<pair_grid(h), h->pair_bs, 0, h->stream>>>(h->C, S, h->cnt, h->bstart, h->list, h->P);
     }
     h->launches += 3;
   } else {
@@ -1263,6 +1294,59 @@ cil_status enqueue_step(cil_cycle *h) {
   }
   if (h->C.apoptosis != CIL_APOP_NONE) removals(h, 1);
   CY_TRY(h, cudaGetLastError());
+  return CIL_OK;
+}
+
+constexpr size_t kMaxStepGraphs = 16;
+
+cil_cycle::Buffers buffers_of(const cil_cycle *h) {
+  cil_cycle::Buffers b{};
+  b.set[0] = h->set[0];
+  b.set[1] = h->set[1];
+  b.xs = h->xs;
+  b.vs = h->vs;
+  b.cur = h->cur;
+  return b;
+}
+
+bool same_buffers(const cil_cycle::Buffers &a, const cil_cycle::Buffers &b) {
+  return std::memcmp(&a.set[0], &b.set[0], sizeof(CySet)) == 0 &&
+         std::memcmp(&a.set[1], &b.set[1], sizeof(CySet)) == 0 && a.xs == b.xs && a.vs == b.vs && a.cur == b.cur;
+}
+
+// One step through the graph of its buffer configuration: captured from enqueue_step the first
+// time (the capture leaves the host state as the step leaves it), replayed afterwards
+cil_status graph_step(cil_cycle *h) {
+  const cil_cycle::Buffers b = buffers_of(h);
+  for (const auto &g : h->graphs)
+    if (g.grid == h->grid_gen && same_buffers(g.before, b)) {
+      CY_TRY(h, cudaGraphLaunch(g.exec, h->stream));
+      h->set[0] = g.after.set[0];
+      h->set[1] = g.after.set[1];
+      h->xs = g.after.xs;
+      h->vs = g.after.vs;
+      h->cur = g.after.cur;
+      h->ts += 1;
+      h->launches += g.nodes;
+      return CIL_OK;
+    }
+  if (h->graphs.size() >= kMaxStepGraphs) return enqueue_step(h);
+  const int64_t l0 = h->launches;
+  CY_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const cil_status st = enqueue_step(h);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+  if (st != CIL_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  CY_TRY(h, ce);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CY_TRY(h, ie);
+  h->graphs.push_back({b, buffers_of(h), h->grid_gen, exec, h->launches - l0});
+  CY_TRY(h, cudaGraphLaunch(exec, h->stream));
   return CIL_OK;
 }
 
@@ -1309,7 +1393,7 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
   h->nbins_cap = 1;
   for (int d = 0; d < p->dim; ++d) h->nbins_cap *= bins_along(C.box[d], p->sigma_core);
   C.sigma_core = p->sigma_core;
-  set_bins(h, p->sigma_core);
+  set_bins(h, p->sigma_core, capacity);
   C.hz_c = (1 - p->nu * p->nu) / p->E;
   C.adhesion = p->adhesion;
   C.motility = p->motility;
@@ -1423,6 +1507,7 @@ void cil_cycle_destroy(cil_cycle *h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto &g : h->graphs) cudaGraphExecDestroy(g.exec);
   for (void *q : h->allocs) cudaFree(q);
   if (h->h_cnt) cudaFreeHost(h->h_cnt);
   for (auto e : h->ev)
@@ -1480,7 +1565,7 @@ cil_status cil_cycle_upload(cil_cycle *h, const cil_cycle_view *v) {
   CY_TRY(h, cudaGetLastError());
   const cil_status st = read_counters(h);
   if (st != CIL_OK) return st;
-  set_bins(h, host_sigma_max(h));
+  set_bins(h, host_sigma_max(h), h->h_cnt->n);
   h->uploaded = true;
   if (!h->C.dpd) return CIL_OK;
   dpd_initial_forces(h);
@@ -1494,11 +1579,12 @@ cil_status cil_cycle_step(cil_cycle *h, int32_t nsteps, int64_t *ts) {
   if (nsteps < 0) return h->fail(CIL_ERR_CONFIG, "negative step count");
   CY_TRY(h, cudaSetDevice(h->device));
   // the counters of the last call (every entry point ends by reading them)
-  set_bins(h, host_sigma_max(h));
+  set_bins(h, host_sigma_max(h), h->h_cnt->n);
   h->launches = 0;
   CY_TRY(h, cudaEventRecord(h->ev[0], h->stream));
+  const bool graphs = !(h->p.flags & CIL_CYCLE_NO_GRAPH);
   for (int k = 0; k < nsteps; ++k) {
-    const cil_status st = enqueue_step(h);
+    const cil_status st = graphs ? graph_step(h) : enqueue_step(h);
     if (st != CIL_OK) return st;
   }
   CY_TRY(h, cudaEventRecord(h->ev[1], h->stream));

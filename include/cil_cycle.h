@@ -82,6 +82,12 @@ enum {
 
 enum { CIL_CYCLE_EULER = 0, CIL_CYCLE_DPD = 1 };
 
+/* cil_cycle_params.flags. By default a step is captured once as a CUDA graph per
+ * configuration of the device buffers it reads and writes (the buffers rotate from step to
+ * step) and of the bin grid, and replayed: one launch per step, what small colonies (the
+ * shipped runs start from one or two cells) are bound by. */
+#define CIL_CYCLE_NO_GRAPH 1
+
 /* Model parameters with the reference's JSON meaning (Input.cpp:6-262; Cell.cuh:236-260
  * defaults). Times in time units; cycle times in units of tau_div_mu as in the JSON. */
 typedef struct cil_cycle_params {
@@ -121,7 +127,7 @@ typedef struct cil_cycle_params {
                             * from the same counters), FP64 positions, velocities, forces of
                             * motility and noise, and cell state */
   int32_t integrator;      /* CIL_CYCLE_EULER or CIL_CYCLE_DPD (MD.INTEGRATOR.SELECT) */
-  int32_t pad;
+  int32_t flags;           /* CIL_CYCLE_NO_GRAPH: launch every kernel of every step */
   double mass;             /* MASS (DPD) */
   double kbt;              /* MD.KBT (DPD) */
   double dis_same;         /* DISSAMCEL: acts between the elements of one cell, none here */

@@ -46,7 +46,7 @@ typedef struct cyo_params {  // the layout of cil_cycle_params (include/cil_cycl
   int32_t drain;
   int32_t precision;  // read by the GPU model only: the restatement is FP64
   int32_t integrator;  // 0 Euler, 1 DPD
-  int32_t pad;
+  int32_t flags;       // read by the GPU model only
   double mass, kbt, dis_same, dis_diff, dis_bg, extr_rate;
 } cyo_params;
 

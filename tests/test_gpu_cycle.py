@@ -269,3 +269,31 @@ def test_dpd_fp32_pair_terms_follow_fp64(gpu_lib, dim, L, n):
     assert np.abs(d).max() < 1e-4
     assert np.abs(a["vel"] - b["vel"]).max() < 1e-3 * max(1.0, np.abs(a["vel"]).max())
     np.testing.assert_allclose(a["sigma"], b["sigma"], rtol=1e-5)
+
+
+@pytest.mark.parametrize("integrator,precision,apoptosis", [(0, 0, 1), (1, 0, 2), (0, 1, 0), (1, 1, 2)])
+def test_graph_replay_equals_launches(gpu_lib, integrator, precision, apoptosis):
+    """Captured steps (the default) compute what the same steps launched kernel by kernel
+    compute (CIL_CYCLE_NO_GRAPH), bit for bit, through divisions, removals (which rotate the
+    state sets), calls of different lengths and a download between calls."""
+    G = gpu_lib
+    rng = np.random.default_rng(81 + 2 * integrator + precision)
+    box = [30.0, 30.0, 0.0]
+    prm = dict(box=box, dt=2e-4, motility=1.0, zeta=0.2, v1=15.0, precision=precision, apoptosis=apoptosis,
+               apop_rate=40.0, apop_pressure=1.5, apop_duration=1.0, extr_gamma=0.5)
+    if integrator:
+        prm.update(DPD, apoptosis=apoptosis, apop_pressure=40.0, apop_duration=0.01)
+    st = colony(rng, 400, box)
+    out = []
+    for flags in (0, G.CYCLE_NO_GRAPH):
+        eng = G.CycleEngine(dict(prm, flags=flags), 20000, seed=11)
+        eng.upload(**st)
+        for n in (1, 7, 40, 1, 30):
+            eng.step(n)
+            eng.download()
+        out.append(eng.download())
+        eng.close()
+    a, b = out
+    assert a["ncells"] == b["ncells"] > 0
+    for k in ("pos", "vel", "sigma", "theta", "rho", "pressure", "tpressure", "force"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
