@@ -422,12 +422,18 @@ __global__ void k_cy_pack_vel(CyConst C, CySet S, const CyCounters *cnt, const i
 // and the velocity; mode 1 (DPD): the force goes to frc and nothing moves. Draws are keyed by
 // the device step counter + key_off.
 template <bool MIXED>
+// lane_bits: 2^lane_bits threads share a cell (small colonies): lane l takes the l-th of every
+// 2^lane_bits candidates of the flattened bin walk, and the lanes' contact sums are combined by
+// a fixed xor tree (the restatement combines them the same way); lane 0 writes.
 __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
                                                     CyCounters *cnt, const int *start, const int *list,
-                                                    const int *ts_dev, int mode, int key_off, CyPacked P) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                                                    const int *ts_dev, int mode, int key_off, CyPacked P,
+                                                    int lane_bits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = 1 << lane_bits;
+  const int i = t >> lane_bits, lane = t & (L - 1);
   const int n = cnt->n;
-  if (i >= n) return;
+  if (i >= n) return;  // a cell's lanes leave together (they share a warp)
   const int ts = *ts_dev + key_off;
   const size_t cap = C.capacity;
   const int D = C.D;
@@ -471,10 +477,12 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
   }
   // ---- Hertz contacts with adhesion and the pressure (device draft, MD.cu:302-366)
   double pres = 0.0;
+  double Fc[3] = {0.0, 0.0, 0.0};  // the contacts' share of the force
   {
     // bins to search on each side: the largest diameter of the colony over the bin width
     Stencil st;
     stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
+    int kflat = 0;  // candidates of the bins walked so far
     const double c2 = C.hz_c + C.hz_c;
     const double inv_ri = 1.0 / (si / 2);
     const float sif = static_cast<float>(si), c2f = static_cast<float>(c2), adhf = static_cast<float>(C.adhesion);
@@ -487,7 +495,9 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
         for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
           const int b = stencil_bin(C, st, o0, o1, o2);
           const int e0 = start[b], e1 = start[b + 1];
-          for (int q = e0; q < e1; ++q) {
+          const int first = e0 + ((lane - kflat) & (L - 1));
+          kflat += e1 - e0;
+          for (int q = first; q < e1; q += L) {
             if (MIXED) {
               if (q == qi) continue;
               const float4 pj = P.pk[q];
@@ -544,14 +554,28 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             }
             const double f0 = -fel + C.adhesion * A;
             if (vol != 0.0) pres -= f0 / vol;
-            CY_AXES(d, D) F[d] += f0 * rij[d];
+            CY_AXES(d, D) Fc[d] += f0 * rij[d];
           }
         }
+    if (L > 1) {  // lanes l and l ^ 2^k combine, k from the highest: a fixed tree
+      const unsigned gm = (L == 32 ? 0xffffffffu : ((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
+      for (int off = L >> 1; off > 0; off >>= 1) {
+        if (MIXED) {
+          presf += __shfl_xor_sync(gm, presf, off, L);
+          CY_AXES(d, D) Ff[d] += __shfl_xor_sync(gm, Ff[d], off, L);
+        } else {
+          pres += __shfl_xor_sync(gm, pres, off, L);
+          CY_AXES(d, D) Fc[d] += __shfl_xor_sync(gm, Fc[d], off, L);
+        }
+      }
+    }
+    CY_AXES(d, D) F[d] += Fc[d];
     if (MIXED) {
       pres += static_cast<double>(presf);
       CY_AXES(d, D) F[d] += static_cast<double>(Ff[d]);
     }
   }
+  if (lane != 0) return;
   bool finite = true;
   CY_AXES(d, D) finite = finite && isfinite(F[d]);
   S.p[i] = pres;
@@ -1070,6 +1094,7 @@ struct cil_cycle {
   std::vector<StepGraph> graphs;
   uint64_t grid_gen = 0;
   int pair_bs = kTile;  // threads per block of the per-cell pair kernels (set per call)
+  int lane_bits = 0;    // log2 of the threads per cell of the contact pass (set per call)
   CyCounters *cnt = nullptr;
   CyCounters *h_cnt = nullptr;  // pinned
   int *ts_dev = nullptr;
@@ -1142,6 +1167,15 @@ constexpr int kNumSMs = 152;  // GB300
 // grid of a per-cell pair kernel at h->pair_bs threads per block
 int pair_grid(const cil_cycle *h) { return (h->cap + h->pair_bs - 1) / h->pair_bs; }
 
+// Threads per cell of the contact pass: up to 8, while the colony gives fewer than two warps
+// per scheduler of every SM (152 SMs x 4 x 2 x 32 threads), and while the grid over the
+// capacity stays within 2^24 threads. The restatement uses the same rule.
+int contact_lane_bits(long long ncells, long long capacity) {
+  int b = 0;
+  while (b < 3 && ncells * (2LL << b) <= 2LL * kNumSMs * 4 * 32 && (capacity << (b + 1)) <= (1LL << 24)) ++b;
+  return b;
+}
+
 int bins_along(double box, double width) {
   const int ns = static_cast<int>(box / width);
   return ns < 1 ? 1 : (ns > 4096 ? 4096 : ns);
@@ -1158,7 +1192,9 @@ void set_bins(cil_cycle *h, double smax, int ncells) {
   const int before[3] = {C.ns[0], C.ns[1], C.ns[2]};
   // blocks of the per-cell pair kernels (FP64-heavy, no block cooperation): small enough that
   // a small colony still spreads over every SM (two blocks per SM), 32 to kTile threads
-  const int bs_before = h->pair_bs;
+  const int bs_before = h->pair_bs, lb_before = h->lane_bits;
+  h->lane_bits = contact_lane_bits(ncells, h->cap);
+  if (h->lane_bits != lb_before) h->grid_gen += 1;
   h->pair_bs = 32;
   while (h->pair_bs < kTile && static_cast<long long>(h->pair_bs) * 2 * kNumSMs < ncells) h->pair_bs *= 2;
   // the grids cover the capacity: keep them at most 65536 blocks (a large capacity, few cells)
@@ -1229,13 +1265,15 @@ cil_status removals(cil_cycle *h, int mode) {
 }
 
 void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, int key_off) {
-  const int g = pair_grid(h), bs = h->pair_bs;
+  const int bs = h->pair_bs;
+  const long long threads = static_cast<long long>(h->cap) << h->lane_bits;
+  const int g = static_cast<int>((threads + bs - 1) / bs);
   if (h->p.precision == 1)
     k_cy_force<true><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                 key_off, h->P);
+                                                 key_off, h->P, h->lane_bits);
   else
     k_cy_force<false><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                  key_off, h->P);
+                                                  key_off, h->P, h->lane_bits);
   h->launches += 1;
 }
 

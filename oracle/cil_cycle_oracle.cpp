@@ -169,9 +169,19 @@ struct Model {
     sigma_r = std::sqrt(2 * q.dis_diff * q.kbt);
   }
 
+  // threads per cell of the GPU model's contact pass (2^lane_bits), whose candidate split and
+  // combining tree conservative() follows; set per call by the GPU model's rule
+  int lane_bits = 0;
+
   // the bin grid of a call: width >= 1.05 x max(SIGMA_CORE, the largest diameter), the GPU
   // model's rule
   void rebin() {
+    {
+      const long long n = static_cast<long long>(c.size()), capl = cap;
+      int b = 0;
+      while (b < 3 && n * (2LL << b) <= 2LL * 152 * 4 * 32 && (capl << (b + 1)) <= (1LL << 24)) ++b;
+      lane_bits = b;
+    }
     const double w = (smax > p.sigma_core ? smax : p.sigma_core) * 1.05;
     for (int d = 0; d < 3; ++d) {
       ns[d] = 1;
@@ -205,7 +215,7 @@ struct Model {
 
   // every other cell in the bins within `radius` of cell i, in the GPU model's visiting order
   template <class Fn>
-  void each_neighbour(int i, double radius, const Bins &bins, Fn fn) const {
+  void each_neighbour(int i, double radius, const Bins &bins, Fn fn, bool with_self = false) const {
     int bi[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int d = 0; d < D; ++d) {
       bi[d] = bin_coord(c[i].x[d], d);
@@ -234,8 +244,14 @@ struct Model {
             b = b * ns[d] + v;
           }
           for (int j : bins[b])
-            if (j != i) fn(j);
+            if (j != i || with_self) fn(j);
         }
+  }
+
+  // every cell in the bins within `radius` of cell i, itself included, in the GPU model's order
+  template <class Fn>
+  void each_neighbour_all(int i, double radius, const Bins &bins, Fn fn) const {
+    each_neighbour(i, radius, bins, fn, true);
   }
 
   // r_j - r_i at the nearest image (Box::distance's Nint, |dd| < L); returns its square length
@@ -291,8 +307,15 @@ struct Model {
       if (D == 3) normal2(draw(i, key, kNoise, 1), &nz[2], &nz[3]);
       for (int d = 0; d < D; ++d) F[d] += p.zeta * (noise_amp * nz[d]);
     }
-    double pres = 0;
-    each_neighbour(i, smax, bins, [&](int j) {
+    // the candidates of the bin walk (self included) go to 2^lane_bits partial sums in turn
+    const int L = 1 << lane_bits;
+    double pl[8] = {0, 0, 0, 0, 0, 0, 0, 0}, Fl[8][3] = {};
+    int kflat = 0;
+    each_neighbour_all(i, smax, bins, [&](int j) {
+      const int lane = kflat++ & (L - 1);
+      if (j == i) return;
+      double *Fc = Fl[lane];
+      double &pres = pl[lane];
       double rij[3] = {0, 0, 0};
       const double r2 = separation(i, j, rij);
       const double si = ci.sig, sj = c[j].sig;
@@ -311,11 +334,23 @@ struct Model {
       }
       const double f0 = -fel + p.adhesion * A;
       if (vol != 0.0) pres -= f0 / vol;
-      for (int d = 0; d < D; ++d) F[d] += f0 * rij[d];
+      for (int d = 0; d < D; ++d) Fc[d] += f0 * rij[d];
     });
+    // the GPU model's xor tree: lane l adds lane l ^ off, off from L / 2 down to 1
+    for (int off = L >> 1; off > 0; off >>= 1)
+      for (int l = 0; l < L; ++l)
+        if (l < (l ^ off)) {
+          const double ps = pl[l] + pl[l ^ off];
+          pl[l] = pl[l ^ off] = ps;
+          for (int d = 0; d < D; ++d) {
+            const double fs = Fl[l][d] + Fl[l ^ off][d];
+            Fl[l][d] = Fl[l ^ off][d] = fs;
+          }
+        }
+    for (int d = 0; d < D; ++d) F[d] += Fl[0][d];
     for (int d = 0; d < D; ++d)
       if (!std::isfinite(F[d])) err |= 2;
-    *pres_out = pres;
+    *pres_out = pl[0];
   }
 
   // Euler: forces, then the position update with pressure-dependent friction (CIL.cu:902-939)
