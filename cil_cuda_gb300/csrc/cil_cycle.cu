@@ -274,9 +274,10 @@ __device__ inline float packed_sep(const CyConst &C, const float4 &pi, const flo
 }
 
 // ---------------------------------------------------------------- block scan
+// Exclusive scan over the block (any multiple of 32 threads up to kTile)
 __device__ inline int block_excl_scan(int v, int *total) {
   __shared__ int ws[kTile / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   int inc = v;
   for (int o = 1; o < 32; o <<= 1) {
     const int t = __shfl_up_sync(0xffffffffu, inc, o);
@@ -285,16 +286,16 @@ __device__ inline int block_excl_scan(int v, int *total) {
   if (lane == 31) ws[wid] = inc;
   __syncthreads();
   if (wid == 0) {
-    int w = lane < kTile / 32 ? ws[lane] : 0;
+    int w = lane < nw ? ws[lane] : 0;
     for (int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += t;
     }
-    if (lane < kTile / 32) ws[lane] = w;
+    if (lane < nw) ws[lane] = w;
   }
   __syncthreads();
   const int base = wid > 0 ? ws[wid - 1] : 0;
-  *total = ws[kTile / 32 - 1];
+  *total = ws[nw - 1];
   __syncthreads();
   return base + inc - v;
 }
@@ -1252,12 +1253,12 @@ cil_status bin_cells(cil_cycle *h) {
 }
 
 cil_status removals(cil_cycle *h, int mode) {
-  const int g = blocks_for(h->cap);
+  const int g = pair_grid(h), bs = h->pair_bs;
   CySet &A = h->set[h->cur];
   CySet &B = h->set[1 - h->cur];
-  k_cy_mark<<<g, kTile, 0, h->stream>>>(h->C, A, h->cnt, h->ts_dev, mode, h->flag, h->blk);
+  k_cy_mark<<<g, bs, 0, h->stream>>>(h->C, A, h->cnt, h->ts_dev, mode, h->flag, h->blk);
   k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
-  k_cy_compact<<<g, kTile, 0, h->stream>>>(h->C, A, B, h->cnt, h->flag, h->blk);
+  k_cy_compact<<<g, bs, 0, h->stream>>>(h->C, A, B, h->cnt, h->flag, h->blk);
   k_cy_commit_removals<<<1, 1, 0, h->stream>>>(h->cnt, h->blk, g, mode);
   h->launches += 4;
   h->cur = 1 - h->cur;
@@ -1323,11 +1324,12 @@ cil_status enqueue_step(cil_cycle *h) {
   h->ts += 1;
   h->launches += 1;
   if (h->C.divide) {
-    k_cy_cycle<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk);
-    k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
+    const int ge = pair_grid(h), bs = h->pair_bs;  // per-cell event kernels: the pair kernels' blocks
+    k_cy_cycle<<<ge, bs, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk);
+    k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, ge);
     k_cy_reset_smax<<<1, 1, 0, h->stream>>>(h->cnt);
-    k_cy_divide<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk, g);
-    k_cy_commit_divisions<<<1, 1, 0, h->stream>>>(h->cnt, h->blk, g, h->cap);
+    k_cy_divide<<<ge, bs, 0, h->stream>>>(h->C, S, h->cnt, h->ts_dev, h->flag, h->blk, ge);
+    k_cy_commit_divisions<<<1, 1, 0, h->stream>>>(h->cnt, h->blk, ge, h->cap);
     h->launches += 5;
   }
   if (h->C.apoptosis != CIL_APOP_NONE) removals(h, 1);
@@ -1510,7 +1512,7 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     h->P.vk = C.dpd ? h->alloc<float4>(cap) : nullptr;
     ok = h->P.pk && h->P.qpos && (!C.dpd || h->P.vk);
   }
-  h->nblocks = blocks_for(capacity);
+  h->nblocks = (capacity + 31) / 32;  // blocks of the per-cell event kernels at their smallest (32 threads)
   h->nparts = (h->nbins_cap + kScanTile - 1) / kScanTile + 1;
   if (ok) {
     h->xs = h->alloc<double>(D * cap);
@@ -1644,8 +1646,8 @@ cil_status cil_cycle_check_positions(cil_cycle *h) {
     return read_counters(h);
   }
   // without drain any cell off the box is an error (run_assert, CIL.cu:956)
-  const int g = blocks_for(h->cap);
-  k_cy_mark<<<g, kTile, 0, h->stream>>>(h->C, h->set[h->cur], h->cnt, h->ts_dev, 2, h->flag, h->blk);
+  const int g = pair_grid(h);
+  k_cy_mark<<<g, h->pair_bs, 0, h->stream>>>(h->C, h->set[h->cur], h->cnt, h->ts_dev, 2, h->flag, h->blk);
   k_cy_scan_small<<<1, kTile, 0, h->stream>>>(h->blk, g);
   CY_TRY(h, cudaGetLastError());
   cil_status st = read_counters(h);
