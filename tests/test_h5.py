@@ -211,3 +211,72 @@ def test_init_h5_from_the_reference_file(G, stem, L):
     np.testing.assert_array_equal(s["pos"], R.reshape(n, 2))
     np.testing.assert_array_equal(s["rho"], G.h5_read(h5, "RHO"))
     np.testing.assert_array_equal(s["vel"], G.h5_read(h5, "Vel").reshape(n, 2))
+
+
+def test_reader_follows_deeper_trees_and_continuations(G, tmp_path):
+    """Forms libhdf5 writes for larger files, built here by rewriting a written file: the
+    root group's B-tree under a level-1 node, and a dataset whose object header continues in a
+    second block (continuation message)."""
+    path = str(tmp_path / "x.Last.h5")
+    st = random_state(np.random.default_rng(3), 50, 1, 2)
+    G.h5_write_state(path, **st)
+    b = bytearray(open(path, "rb").read())
+    u = lambda f, o: struct.unpack_from("<" + f, b, o)  # noqa: E731
+    tree, heap = u("QQ", 80)
+    used = u("H", tree + 6)[0]
+    last_key = u("Q", tree + 24 + 16 * used)[0]
+    # a level-1 node whose one child is the original level-0 node
+    top = len(b)
+    node = bytearray(b"TREE") + bytes([0, 1]) + struct.pack("<H", 1) + struct.pack("<qq", -1, -1)
+    node += struct.pack("<QQQ", 0, tree, last_key)
+    b += node + bytes(24 + 33 * 8 + 32 * 8 - len(node))
+    struct.pack_into("<Q", b, 80, top)  # the superblock's cached B-tree address
+    root = u("Q", 64)[0]
+    struct.pack_into("<Q", b, root + 16 + 8, top)  # the root's symbol table message
+    # move the messages of dataset "R" after its dataspace into a continuation block
+    names = {}
+    for k in range(used):
+        snod = u("Q", tree + 24 + 16 * k + 8)[0]
+        for e in range(u("H", snod + 6)[0]):
+            off, oh = u("QQ", snod + 8 + 40 * e)
+            names[bytes(b[u("Q", heap + 24)[0] + off:]).split(b"\0")[0].decode()] = oh
+    oh = names["R"]
+    hsize = u("I", oh + 8)[0]
+    p = oh + 16
+    first = 8 + u("HH", p)[1]  # the dataspace message, kept
+    rest = bytes(b[p + first:p + hsize])
+    cont = len(b) + (-len(b)) % 8
+    b += bytes(cont - len(b)) + rest
+    nmsg = u("H", oh + 2)[0]
+    # the freed space: a continuation message, then a NIL message padding to the old size
+    cmsg = struct.pack("<HHB3x", 0x10, 16, 0) + struct.pack("<QQ", cont, len(rest))
+    pad = hsize - first - len(cmsg)
+    nil = struct.pack("<HHB3x", 0, pad - 8, 0) + bytes(pad - 8)
+    b[p + first:p + hsize] = cmsg + nil
+    struct.pack_into("<H", b, oh + 2, nmsg + 2)
+    open(path, "wb").write(bytes(b))
+    f32 = lambda a: np.asarray(a, np.float64).astype(np.float32).astype(np.float64)  # noqa: E731
+    np.testing.assert_array_equal(G.h5_read(path, "R"), f32(st["pos"]))
+    np.testing.assert_array_equal(G.h5_read(path, "/RHO"), f32(st["rho"]))
+    np.testing.assert_array_equal(G.h5_read(path, "T0"), st["t0"])
+    with pytest.raises(G.CilError) as e:
+        G.h5_read(path, "Missing")
+    assert "no object Missing" in str(e.value)
+
+
+def test_reader_refuses_malformed_files(G, tmp_path):
+    path = str(tmp_path / "x.Last.h5")
+    G.h5_write_state(path, **random_state(np.random.default_rng(4), 10, 1, 2))
+    good = open(path, "rb").read()
+    for cut, name in ((40, "R"), (200, "R"), (700, "R"), (len(good) - 10, "Vel")):  # Vel's data is written last
+        open(path, "wb").write(good[:cut])
+        with pytest.raises(G.CilError):
+            G.h5_read(path, name)
+    open(path, "wb").write(good[:len(good) - 10])
+    assert G.h5_read(path, "R").shape == (10, 1, 2)  # the datasets before the cut stay readable
+    b = bytearray(good)
+    b[8] = 2  # superblock version 2
+    open(path, "wb").write(bytes(b))
+    with pytest.raises(G.CilError) as e:
+        G.h5_read(path, "R")
+    assert "superblock version 2" in str(e.value)
