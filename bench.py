@@ -664,6 +664,9 @@ def main():
                                           mlp_skin if have_mlp else args.skin, have_mlp, tune)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(p, st, os.cpu_count() or 1)
+        # the same restatement on one host thread (a short sample: one or two steps)
+        one = cpu_baseline(p, st, 1, budget_s=8.0)
+        line["cpu_baseline"]["one_thread"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
