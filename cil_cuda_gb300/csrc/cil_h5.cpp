@@ -4,10 +4,13 @@
 #include "cil_h5.hpp"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <iterator>
 #include <limits>
+
+#include "cil_input.h"
 
 namespace cil {
 namespace h5 {
@@ -18,8 +21,8 @@ constexpr uint64_t kUndef = std::numeric_limits<uint64_t>::max();
 const uint8_t kSig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
 
 // message types
-constexpr uint16_t kNil = 0x00, kDataspace = 0x01, kDatatype = 0x03, kFillNew = 0x05, kLayout = 0x08,
-                   kFilters = 0x0B, kCont = 0x10, kSymtab = 0x11;
+constexpr uint16_t kDataspace = 0x01, kDatatype = 0x03, kFillNew = 0x05, kLayout = 0x08, kFilters = 0x0B,
+                   kCont = 0x10, kSymtab = 0x11;
 
 bool fail(std::string *err, const std::string &m) {
   if (err) *err = m;
@@ -531,8 +534,6 @@ bool Writer::save(const std::string &path, std::string *err) const {
 }  // namespace cil
 
 // ---------------------------------------------------------------------------- C ABI
-#include "cil_input.h"
-
 namespace {
 thread_local std::string g_h5_err;
 
