@@ -1371,20 +1371,30 @@ cil_status graph_step(cil_cycle *h) {
       return CIL_OK;
     }
   if (h->graphs.size() >= kMaxStepGraphs) return enqueue_step(h);
-  const int64_t l0 = h->launches;
-  CY_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t l0 = h->launches, ts0 = h->ts;
+  if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return enqueue_step(h);
+  }
   const cil_status st = enqueue_step(h);
   cudaGraph_t graph = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
-  if (st != CIL_OK) {
-    if (graph) cudaGraphDestroy(graph);
-    return st;
-  }
-  CY_TRY(h, ce);
   cudaGraphExec_t exec = nullptr;
-  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  CY_TRY(h, ie);
+  cudaError_t ie = cudaErrorUnknown;
+  if (st == CIL_OK && ce == cudaSuccess && graph) ie = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    // nothing ran: put the host state back as it was before the capture and launch the step
+    cudaGetLastError();
+    h->set[0] = b.set[0];
+    h->set[1] = b.set[1];
+    h->xs = b.xs;
+    h->vs = b.vs;
+    h->cur = b.cur;
+    h->ts = ts0;
+    h->launches = l0;
+    return enqueue_step(h);
+  }
   h->graphs.push_back({b, buffers_of(h), h->grid_gen, exec, h->launches - l0});
   CY_TRY(h, cudaGraphLaunch(exec, h->stream));
   return CIL_OK;
