@@ -98,3 +98,25 @@ def test_cycle_model_without_cells_and_with_one(gpu_lib):
     s = eng.download()
     eng.close()
     assert s["ncells"] == 1 and np.all(np.isfinite(s["pos"])) and s["pressure"][0] == 0.0
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_cycle_model_capacity_overflow(gpu_lib, flags):
+    """Divisions beyond the capacity inside replayed (or launched) steps: the call reports
+    CIL_ERR_CAPACITY, the colony never holds more cells than its capacity, and its state stays
+    finite."""
+    G = gpu_lib
+    rng = np.random.default_rng(5)
+    n, cap = 60, 80
+    prm = dict(box=[20.0, 20.0, 0.0], dt=2e-4, motility=1.0, zeta=0.2, flags=flags)
+    eng = G.CycleEngine(prm, cap, seed=2)
+    eng.upload(pos=rng.uniform(0, 20.0, size=(n, 2)), theta=np.full(n, 0.999), rho=np.ones(n),
+               angvel=np.full(n, 0.01), sigma=np.full(n, 1.1283791670955126))
+    with pytest.raises(G.CilError) as e:
+        eng.step(5)
+    assert e.value.status == 3
+    L = eng.L
+    v = G.CycleView(ncells=0, capacity=0)
+    L.cil_cycle_download(eng.h, v)  # the cell count, whatever the status
+    assert v.ncells == cap
+    eng.close()
