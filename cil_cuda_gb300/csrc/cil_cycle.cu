@@ -346,9 +346,12 @@ __global__ void k_cy_clear(int *a, int m) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) a[i] = 0;
 }
 
-__global__ void k_cy_keys(CyConst C, CySet S, const CyCounters *cnt, int *key, int *count) {
+// the bin of every cell, and 1 / (sigma / 2) for the contact pass (the same value it would
+// compute per contact)
+__global__ void k_cy_keys(CyConst C, CySet S, const CyCounters *cnt, int *key, int *count, double *inv_r) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt->n) return;
+  inv_r[i] = 1.0 / (S.sig[i] / 2);
   double xd[3];
   CY_AXES(d, C.D) xd[d] = S.x[static_cast<size_t>(d) * C.capacity + i];
   const int b = bin_of(C, xd);
@@ -429,7 +432,7 @@ template <bool MIXED>
 __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *x_out, double *frc,
                                                     CyCounters *cnt, const int *start, const int *list,
                                                     const int *ts_dev, int mode, int key_off, CyPacked P,
-                                                    int lane_bits) {
+                                                    int lane_bits, const double *inv_r) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int L = 1 << lane_bits;
   const int i = t >> lane_bits, lane = t & (L - 1);
@@ -544,7 +547,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             // symmetric in the two diameters)
             const double sa = i < j ? si : sj, sb = i < j ? sj : si;
             const double h = fmax((si + sj) / 2 - r, 0.0);
-            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(inv_ri + 1.0 / (sj / 2)));  // h^1.5
+            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(inv_ri + inv_r[j]));  // h^1.5
             double A, vol;
             if (D == 3) {
               A = contact_area(r, sa, sb);
@@ -1079,6 +1082,7 @@ struct cil_cycle {
   double *vs = nullptr;   // velocity output buffer of the DPD pair pass
   CyPacked P{};           // FP32 records of the bin order (precision 1)
   double *frc = nullptr;  // last forces (output only)
+  double *inv_r = nullptr;  // 1 / (sigma / 2) per cell, written with the bin keys
   // captured steps: keyed by the buffer configuration before the step and the bin grid, each
   // records the configuration after it (a step rotates x / xs, v / vs and the state sets)
   struct Buffers {
@@ -1239,7 +1243,7 @@ cil_status bin_cells(cil_cycle *h) {
   const CySet &S = h->set[h->cur];
   const int g = blocks_for(h->cap);
   k_cy_clear<<<256, kTile, 0, h->stream>>>(h->bcount, h->nbins);
-  k_cy_keys<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->key, h->bcount);
+  k_cy_keys<<<g, kTile, 0, h->stream>>>(h->C, S, h->cnt, h->key, h->bcount, h->inv_r);
   scan_into(h, h->bcount, h->nbins, h->bstart);
   k_cy_clear<<<256, kTile, 0, h->stream>>>(h->cursor, h->nbins);
   k_cy_scatter<<<g, kTile, 0, h->stream>>>(h->cnt, h->key, h->bstart, h->cursor, h->list);
@@ -1271,10 +1275,10 @@ void launch_force(cil_cycle *h, CySet &S, double *x_out, double *frc, int mode, 
   const int g = static_cast<int>((threads + bs - 1) / bs);
   if (h->p.precision == 1)
     k_cy_force<true><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                 key_off, h->P, h->lane_bits);
+                                                 key_off, h->P, h->lane_bits, h->inv_r);
   else
     k_cy_force<false><<<g, bs, 0, h->stream>>>(h->C, S, x_out, frc, h->cnt, h->bstart, h->list, h->ts_dev, mode,
-                                                  key_off, h->P, h->lane_bits);
+                                                  key_off, h->P, h->lane_bits, h->inv_r);
   h->launches += 1;
 }
 
@@ -1527,6 +1531,7 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
   if (ok) {
     h->xs = h->alloc<double>(D * cap);
     h->frc = h->alloc<double>(D * cap);
+    h->inv_r = h->alloc<double>(cap);
     h->cnt = h->alloc<CyCounters>(1);
     h->ts_dev = h->alloc<int>(1);
     h->key = h->alloc<int>(cap);
@@ -1537,7 +1542,7 @@ cil_status cil_cycle_create(const cil_cycle_params *p, int32_t capacity, uint64_
     h->part = h->alloc<int>(h->nparts + 1);
     h->flag = h->alloc<int>(cap);
     h->blk = h->alloc<int>(h->nblocks + 1);
-    ok = h->xs && h->frc && h->cnt && h->ts_dev && h->key && h->bcount && h->bstart && h->cursor && h->list &&
+    ok = h->xs && h->frc && h->inv_r && h->cnt && h->ts_dev && h->key && h->bcount && h->bstart && h->cursor && h->list &&
          h->part && h->flag && h->blk &&
          cudaHostAlloc(&h->h_cnt, sizeof(CyCounters), cudaHostAllocDefault) == cudaSuccess;
   }
