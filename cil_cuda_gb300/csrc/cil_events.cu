@@ -1,6 +1,6 @@
 // Division, apoptosis, state transfer and observables on the device.
 //
-// Division (calculDivisions, CIL.cu:369-455, with the BASELINE growth model: a cell
+// Division (calculDivisions, CIL.cu:369-455, with the linear-growth model: a cell
 // divides when its cycle ends, ts == tswitch): due cells are ranked by a deterministic
 // per-colony scan in slot order, the daughter takes cell index ncell + rank (addCell
 // appends, Colony.cpp:355-359) and both cells are re-placed as binaryCellDivision does

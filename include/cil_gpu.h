@@ -37,7 +37,8 @@ typedef enum cil_status {
 } cil_status;
 
 /* Pair-force laws (the reference's PairForceParams family, MD.cuh:23-344, with the
- * BASELINE forms). Force on element i from j is f0(r) * (r_j - r_i). */
+ * benchmark workloads' forms: WCA, the (1 - r/rc)^2 soft core, E h^1.5 Hertz). Force on element
+ * i from j is f0(r) * (r_j - r_i). */
 enum {
   CIL_FORCE_LJ_WCA = 0,   /* LJParams (MD.cuh:47-129): eps_ij = 24 eps, rc^2 = rcut_scale^2 sigma_ij^2 */
   CIL_FORCE_SOFTCORE = 1, /* F = eps (1 - r/rc)^2, rc = rcut_scale sigma_ij */

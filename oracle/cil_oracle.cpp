@@ -252,7 +252,7 @@ struct Oracle {
     return p.rest0 + (p.rest1 - p.rest0) * frac;
   }
 
-  // binaryCellForce (MD.cu:525-598) with the BASELINE bond: linear spring kappa (r - l)
+  // binaryCellForce (MD.cu:525-598) with the linear bond: spring kappa (r - l)
   // along the back->front axis, motility -m0 n on the back element and +m1 n on the front.
   // The reference's velocity-dependent friction term and FENE are not part of this model.
   // Assigns the force (the reference's migrationFunc assigns, MD.cu:595-596).
@@ -273,7 +273,7 @@ struct Oracle {
     }
   }
 
-  // One-sided flat Hertz walls normal to the last axis (BASELINE channel; the reference's
+  // One-sided flat Hertz walls normal to the last axis (the channel workload; the reference's
   // FlatWall::addHZForce, Wall.hpp:80-91, is the unused precursor). Overlap
   // delta = sigma/2 - dir*(x - x0); force +dir * E delta^1.5.
   void wall_force(int c, int j) {
@@ -470,7 +470,7 @@ struct Oracle {
     }
   }
 
-  // calculDivisions (CIL.cu:369-455) for the BASELINE growth model: a cell divides when its
+  // calculDivisions (CIL.cu:369-455) for the linear-growth model: a cell divides when its
   // cycle ends (ts == tswitch); binaryCellDivision (MD.cu:721-731) places both daughters
   // with half-separation rest0/2; random draws in the reference order: mother axis,
   // daughter axis, daughter cycle, mother cycle.

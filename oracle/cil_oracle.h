@@ -10,7 +10,7 @@
  * (golden vectors in tests/golden/). The reference ships no tests, fixtures or outputs of
  * this physics, and its step does not compile, so the force laws, binning, division and
  * apoptosis are "parity unpinned": they are restated from the reference source (cited per
- * function in cil_oracle.cpp) with the BASELINE force laws slotted into the reference's
+ * function in cil_oracle.cpp) with the benchmark workloads' force laws slotted into the reference's
  * PairForceParams / intraCellForce extension points.
  */
 #ifndef CIL_ORACLE_H

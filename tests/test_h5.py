@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("CIL_REFERENCE_DIR", "/root/reference")
 SINGLE = os.path.join(ROOT, "tests", "golden", "input_single_element_2d.json")
 TWO = os.path.join(ROOT, "tests", "golden", "input_two_element_2d.json")
 RUNS = ("z0.001t3.16_v2", "cil")
