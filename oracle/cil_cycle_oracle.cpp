@@ -1,5 +1,5 @@
 // ORACLE — test infrastructure only. A CPU restatement of the reference's single-element
-// cell-cycle model, the checker of the GPU model in cil_cuda_gb300/csrc/cil_cycle.cu.
+// cell-cycle model, the oracle the tests compare the GPU model (cil_cuda_gb300/csrc/cil_cycle.cu) with.
 //
 // Parity of this restatement with the reference is unpinned: the reference's host pair force
 // with pressure (cellCellForcePressure, declared MD.cuh:397-399, called CIL.cu:165,220,259)

@@ -2,7 +2,7 @@
  *
  * CPU restatement of the reference's overdamped cell-colony timestep (KokoroSinx/cil_cuda,
  * Euler integrator: CIL.cu:1013-1020 with calculForcesPressure CIL.cu:999-1007), used as
- * the checker for the CUDA library and as the timed CPU baseline. Only tests/,
+ * the oracle the tests compare the CUDA library with, and as the timed CPU baseline. Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU legs load it; the product never does.
  *
  * Pinning: the random-number layer (dSFMT-19937, Leva normals, onDSphere, uniform
