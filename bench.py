@@ -514,7 +514,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
     ap.add_argument("--no-frames", action="store_true", help="skip the frame-output leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
-    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "dpd"], default=None,
+    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd"], default=None,
                     help="run one form only (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -528,6 +528,9 @@ def main():
     if not os.path.exists(G.LIB_PATH):
         from cil_cuda_gb300 import build
         build.build()
+    if args.only == "cycle_small":
+        print(json.dumps(run_cycle_small(G, device, steps=args.steps, warmup=args.warmup)))
+        return 0
     if args.only == "dpd":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1, dpd=True)))
