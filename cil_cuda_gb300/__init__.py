@@ -37,7 +37,8 @@ EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step
             "cil_cycle_destroy", "cil_cycle_upload", "cil_cycle_step", "cil_cycle_check_positions",
             "cil_cycle_download", "cil_cycle_timings", "cil_cycle_last_error", "cil_input_elements",
             "cil_input_cycle_config", "cil_input_cycle_initial_state", "cil_h5_shape", "cil_h5_read",
-            "cil_h5_last_error", "cil_h5_write_state"]
+            "cil_h5_last_error", "cil_h5_write_state", "cil_h5_attr", "cil_h5_frames_create", "cil_h5_frames_write",
+            "cil_h5_frames_close"]
 
 
 class CilError(RuntimeError):
@@ -245,6 +246,63 @@ def h5_read(path: str, dataset: str) -> np.ndarray:
     return out.reshape(shape)
 
 
+def h5_attr(path: str, obj: str, name: str) -> np.ndarray:
+    """A numeric attribute of an HDF5 object (cil_h5_attr)."""
+    L = lib()
+    out = np.zeros(64)
+    n = C.c_int64()
+    _h5_check(L, L.cil_h5_attr(path.encode(), obj.encode(), name.encode(), _dp(out), out.size, C.byref(n)))
+    return out[:n.value].copy()
+
+
+class H5Frames:
+    """The HDF5 frame file (cil_h5_frames_*): /params, then /snapshots/t_<frame> per write."""
+
+    def __init__(self, path: str, box, dt: float, gts: int):
+        self.L = lib()
+        b = np.ascontiguousarray(box, np.float64)
+        h = C.c_void_p()
+        _h5_check(self.L, self.L.cil_h5_frames_create(path.encode(), len(b), _dp(b), dt, gts, C.byref(h)))
+        self.h = h
+
+    def write(self, frame: int, ts: int, **state):
+        keep, st = _h5_state(state)
+        _h5_check(self.L, self.L.cil_h5_frames_write(self.h, frame, ts, C.byref(st)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            h, self.h = self.h, None
+            _h5_check(self.L, self.L.cil_h5_frames_close(h))
+
+
+def _h5_state(state: dict):
+    pos = np.ascontiguousarray(state["pos"], np.float64)
+    n, E, D = pos.shape
+    keep = [pos]
+
+    def d(a, shape):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64).reshape(shape), shape), np.float64)
+        keep.append(a)
+        return _dp(a)
+
+    def i(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, np.int32).reshape(n)
+        keep.append(a)
+        return _ip(a)
+
+    g = state.get
+    st = H5State(ncells=n, nelem=E, dim=D, pad=0, pos=_dp(pos), vel=d(g("vel"), (n, E, D)),
+                 force=d(g("force"), (n, E, D)), force_dis=d(g("force_dis"), (n, E, D)),
+                 force_ran=d(g("force_ran"), (n, E, D)), sigma=d(g("sigma"), (n, E)), rho=d(g("rho"), (n,)),
+                 theta=d(g("theta"), (n,)), pressure=d(g("pressure"), (n,)), state=i(g("state")), t0=i(g("t0")),
+                 cpu_time=float(g("cpu_time", 0.0)))
+    return keep, st
+
+
 def h5_write_state(path: str, pos, sigma, vel=None, force=None, force_dis=None, force_ran=None, rho=None, theta=None,
                    pressure=None, state=None, t0=None, cpu_time: float = 0.0):
     """A final-state file as outputHDF5Frame writes it with id -1 (cil_h5_write_state). pos:
@@ -417,6 +475,15 @@ def lib():
         L.cil_h5_last_error.argtypes = [C.c_char_p, C.c_size_t]
         L.cil_h5_write_state.restype = i32
         L.cil_h5_write_state.argtypes = [C.c_char_p, C.POINTER(H5State)]
+        L.cil_h5_attr.restype = i32
+        L.cil_h5_attr.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64,
+                                  C.POINTER(C.c_int64)]
+        L.cil_h5_frames_create.restype = i32
+        L.cil_h5_frames_create.argtypes = [C.c_char_p, i32, C.POINTER(C.c_double), C.c_double, i32, C.POINTER(vp)]
+        L.cil_h5_frames_write.restype = i32
+        L.cil_h5_frames_write.argtypes = [vp, i32, i32, C.POINTER(H5State)]
+        L.cil_h5_frames_close.restype = i32
+        L.cil_h5_frames_close.argtypes = [vp]
         L.cil_host_rng_draw.restype = i32
         L.cil_host_rng_draw.argtypes = [C.c_uint32, i32, C.c_int64, dp]
         _lib = L

@@ -1258,7 +1258,11 @@ cil_status cil_forces(cil_handle *h, int32_t colony, double *frc) {
   const bool oracle = h->cfg.rng_mode == CIL_RNG_DSFMT;
   bool noise = false;
   if (oracle) {
+    // the noise the next step will draw: the host stream is put back after the draw, so that
+    // reading the forces leaves the run unchanged
+    const HostRng saved = h->rng;
     st = draw_oracle_noise(h, &noise);
+    h->rng = saved;
     if (st != CIL_OK) return st;
   } else {
     for (int c = 0; c < h->B; ++c) noise = noise || h->hc[c].p.noise_D > 0.0;

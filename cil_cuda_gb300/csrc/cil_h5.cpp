@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <iterator>
 #include <limits>
 
@@ -278,6 +279,62 @@ bool Reader::read(const Dataset &ds, std::vector<double> *out, std::string *err)
   return true;
 }
 
+bool Reader::attribute(const std::string &object, const std::string &name, std::vector<double> *out,
+                       std::string *err) const {
+  uint64_t oh;
+  if (!lookup(object, &oh, err)) return false;
+  std::vector<Msg> ms;
+  if (!messages(oh, &ms, err)) return false;
+  const std::string where = path_ + ": " + object + ": attribute " + name + ": ";
+  for (const Msg &m : ms) {
+    if (m.type != 0x0C || m.size < 8) continue;
+    const uint64_t d = m.off;
+    if (buf_[d] != 1) continue;  // version 1 (object headers of version 1)
+    const uint64_t nsz = u(d + 2, 2), tsz = u(d + 4, 2), ssz = u(d + 6, 2);
+    auto pad8 = [](uint64_t x) { return (x + 7) / 8 * 8; };
+    const uint64_t at_name = d + 8, at_type = at_name + pad8(nsz), at_space = at_type + pad8(tsz),
+                   at_data = at_space + pad8(ssz);
+    if (at_data > d + m.size || nsz == 0) return fail(err, where + "malformed attribute message");
+    const std::string an(reinterpret_cast<const char *>(buf_.data() + at_name), strnlen(
+        reinterpret_cast<const char *>(buf_.data() + at_name), nsz));
+    if (an != name) continue;
+    const int cls = buf_[at_type] & 0x0f, size = static_cast<int>(u(at_type + 4, 4));
+    const bool sgn = cls == 1 || (buf_[at_type + 1] & 0x08);
+    if ((cls != 0 && cls != 1) || (buf_[at_type + 1] & 0x01) || (cls == 1 && size != 4 && size != 8) ||
+        (cls == 0 && size != 1 && size != 2 && size != 4 && size != 8))
+      return fail(err, where + "not a little-endian number");
+    const int sver = buf_[at_space], rank = buf_[at_space + 1];
+    const uint64_t dims_at = sver == 1 ? at_space + 8 : at_space + 4;
+    uint64_t n = 1;
+    for (int k = 0; k < rank; ++k) n *= u(dims_at + 8 * k, 8);
+    if (at_data + n * size > d + m.size) return fail(err, where + "data outside its message");
+    out->assign(n, 0.0);
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint64_t q = at_data + i * size;
+      const uint64_t v = u(q, size);
+      double x;
+      if (cls == 1) {
+        if (size == 4) {
+          const uint32_t w = static_cast<uint32_t>(v);
+          float fl;
+          std::memcpy(&fl, &w, 4);
+          x = fl;
+        } else {
+          std::memcpy(&x, &v, 8);
+        }
+      } else if (sgn) {
+        const int sh = 64 - 8 * size;
+        x = static_cast<double>(static_cast<int64_t>(v << sh) >> sh);
+      } else {
+        x = static_cast<double>(v);
+      }
+      (*out)[i] = x;
+    }
+    return true;
+  }
+  return fail(err, where + "not found");
+}
+
 // ---------------------------------------------------------------------------- writer
 namespace {
 
@@ -533,6 +590,390 @@ bool Writer::save(const std::string &path, std::string *err) const {
 }  // namespace h5
 }  // namespace cil
 
+// ---------------------------------------------------------------------------- frame file
+namespace cil {
+namespace h5 {
+namespace {
+
+Buf space_v1(const std::vector<uint64_t> &dims) {  // dataspace v1, maximum dimensions = dimensions
+  Buf sp;
+  sp.put(1, 1);
+  sp.put(dims.size(), 1);
+  sp.put(1, 1);
+  sp.put(0, 5);
+  for (uint64_t d : dims) sp.put(d, 8);
+  for (uint64_t d : dims) sp.put(d, 8);
+  return sp;
+}
+
+Buf type_of(int cls, int size) {
+  Buf ty;
+  if (cls == 1 && size == 4) {  // IEEE binary32 little-endian
+    ty.put(0x11, 1);
+    ty.put(0x20, 1);
+    ty.put(31, 1);
+    ty.put(0, 1);
+    ty.put(4, 4);
+    ty.put(0, 2);
+    ty.put(32, 2);
+    ty.put(23, 1);
+    ty.put(8, 1);
+    ty.put(0, 1);
+    ty.put(23, 1);
+    ty.put(127, 4);
+  } else if (cls == 1) {  // IEEE binary64 little-endian
+    ty.put(0x11, 1);
+    ty.put(0x20, 1);
+    ty.put(63, 1);
+    ty.put(0, 1);
+    ty.put(8, 4);
+    ty.put(0, 2);
+    ty.put(64, 2);
+    ty.put(52, 1);
+    ty.put(11, 1);
+    ty.put(0, 1);
+    ty.put(52, 1);
+    ty.put(1023, 4);
+  } else {  // signed 32-bit little-endian
+    ty.put(0x10, 1);
+    ty.put(0x08, 1);
+    ty.put(0, 2);
+    ty.put(4, 4);
+    ty.put(0, 2);
+    ty.put(32, 2);
+  }
+  return ty;
+}
+
+}  // namespace
+
+struct FrameFile::Impl {
+  struct Attr {
+    std::string name;
+    int cls, size;
+    std::vector<uint8_t> bytes;
+    uint64_t n;
+  };
+  struct Data {
+    std::string name;
+    std::vector<uint64_t> dims;
+    int cls;
+    uint64_t addr, bytes;
+  };
+  struct Group {
+    std::string name;
+    std::vector<Group *> groups;
+    std::vector<Data> data;
+    std::vector<Attr> attrs;
+    uint64_t oh = 0, tree = 0, heap = 0;
+    ~Group() {
+      for (Group *g : groups) delete g;
+    }
+  };
+  std::string path;
+  std::FILE *f = nullptr;
+  uint64_t eof = 0;
+  Group root;
+
+  Group *group(const std::string &p) {
+    Group *g = &root;
+    size_t i = 0;
+    while (i < p.size()) {
+      while (i < p.size() && p[i] == '/') ++i;
+      if (i >= p.size()) break;
+      size_t j = p.find('/', i);
+      if (j == std::string::npos) j = p.size();
+      const std::string part = p.substr(i, j - i);
+      Group *next = nullptr;
+      for (Group *c : g->groups)
+        if (c->name == part) next = c;
+      if (!next) {
+        next = new Group();
+        next->name = part;
+        g->groups.push_back(next);
+      }
+      g = next;
+      i = j;
+    }
+    return g;
+  }
+
+  bool append(const void *p, size_t n, uint64_t *at, std::string *err) {
+    static const uint8_t zeros[8] = {0};
+    const uint64_t pad = (8 - eof % 8) % 8;
+    if (pad && std::fwrite(zeros, 1, pad, f) != pad) return fail(err, path + ": write failed");
+    eof += pad;
+    *at = eof;
+    if (n && std::fwrite(p, 1, n, f) != n) return fail(err, path + ": write failed");
+    eof += n;
+    return true;
+  }
+};
+
+bool FrameFile::create(const std::string &path, std::string *err) {
+  delete impl_;
+  impl_ = new Impl();
+  impl_->path = path;
+  impl_->f = std::fopen(path.c_str(), "wb");
+  if (!impl_->f) return fail(err, path + ": cannot create");
+  // the superblock and the root's entry, written again at close
+  static const uint8_t zeros[96] = {0};
+  if (std::fwrite(zeros, 1, 96, impl_->f) != 96) return fail(err, path + ": write failed");
+  impl_->eof = 96;
+  return true;
+}
+
+FrameFile::~FrameFile() {
+  if (impl_ && impl_->f) std::fclose(impl_->f);
+  delete impl_;
+}
+
+void FrameFile::make_group(const std::string &group) {
+  if (impl_) impl_->group(group);
+}
+
+bool FrameFile::attr_f64(const std::string &group, const std::string &name, const std::vector<double> &v,
+                         std::string *err) {
+  if (!impl_ || !impl_->f) return fail(err, "frame file not open");
+  Impl::Attr a{name, 1, 8, std::vector<uint8_t>(v.size() * 8), v.size()};
+  if (!v.empty()) std::memcpy(a.bytes.data(), v.data(), v.size() * 8);
+  impl_->group(group)->attrs.push_back(std::move(a));
+  return true;
+}
+
+bool FrameFile::attr_i32(const std::string &group, const std::string &name, const std::vector<int32_t> &v,
+                         std::string *err) {
+  if (!impl_ || !impl_->f) return fail(err, "frame file not open");
+  Impl::Attr a{name, 0, 4, std::vector<uint8_t>(v.size() * 4), v.size()};
+  if (!v.empty()) std::memcpy(a.bytes.data(), v.data(), v.size() * 4);
+  impl_->group(group)->attrs.push_back(std::move(a));
+  return true;
+}
+
+bool FrameFile::data_f32(const std::string &group, const std::string &name, const std::vector<uint64_t> &dims,
+                         const double *data, std::string *err) {
+  if (!impl_ || !impl_->f) return fail(err, "frame file not open");
+  uint64_t n = 1;
+  for (uint64_t d : dims) n *= d;
+  std::vector<float> v(n);
+  for (uint64_t i = 0; i < n; ++i) v[i] = static_cast<float>(data[i]);
+  uint64_t at;
+  if (!impl_->append(v.data(), n * 4, &at, err)) return false;
+  impl_->group(group)->data.push_back({name, dims, 1, at, n * 4});
+  return true;
+}
+
+bool FrameFile::data_i32(const std::string &group, const std::string &name, const std::vector<uint64_t> &dims,
+                         const int32_t *data, std::string *err) {
+  if (!impl_ || !impl_->f) return fail(err, "frame file not open");
+  uint64_t n = 1;
+  for (uint64_t d : dims) n *= d;
+  uint64_t at;
+  if (!impl_->append(data, n * 4, &at, err)) return false;
+  impl_->group(group)->data.push_back({name, dims, 0, at, n * 4});
+  return true;
+}
+
+bool FrameFile::close(std::string *err) {
+  if (!impl_ || !impl_->f) return fail(err, "frame file not open");
+  Impl &I = *impl_;
+  // one B-tree node per group: K large enough for the largest group
+  size_t most = 0;
+  std::vector<Impl::Group *> all{&I.root};
+  for (size_t k = 0; k < all.size(); ++k) {
+    most = std::max(most, all[k]->groups.size() + all[k]->data.size());
+    for (Impl::Group *c : all[k]->groups) all.push_back(c);
+  }
+  const size_t most_snod = (most + 2 * kLeafK - 1) / (2 * kLeafK);
+  const int K = static_cast<int>(std::max<size_t>(kInternalK, (most_snod + 1) / 2));
+  if (K > 65535) return fail(err, "too many entries in one group");
+  const uint64_t tree_size = 24 + (2 * static_cast<uint64_t>(K) + 1) * 8 + 2 * static_cast<uint64_t>(K) * 8;
+  const uint64_t snod_size = 8 + 2 * kLeafK * 40;
+  uint64_t at = (I.eof + 7) / 8 * 8;
+  Buf meta;  // written at `base`
+  const uint64_t base = at;
+  auto here = [&]() { return base + meta.b.size(); };
+  // post-order: children first, so that a group's entries know their object headers
+  std::function<bool(Impl::Group &)> emit = [&](Impl::Group &g) -> bool {
+    struct Entry {
+      std::string name;
+      uint64_t oh;
+      bool group;
+      Impl::Group *gp;
+    };
+    std::vector<Entry> es;
+    for (Impl::Group *c : g.groups) {
+      if (!emit(*c)) return false;
+      es.push_back({c->name, c->oh, true, c});
+    }
+    for (const Impl::Data &d : g.data) {
+      Buf msgs;
+      message(msgs, kDataspace, 0, space_v1(d.dims));
+      message(msgs, kDatatype, 1, type_of(d.cls, 4));
+      Buf fill;
+      fill.put(2, 1);
+      fill.put(2, 1);
+      fill.put(2, 1);
+      fill.put(1, 1);
+      fill.put(0, 4);
+      message(msgs, kFillNew, 1, fill);
+      Buf lay;
+      lay.put(3, 1);
+      lay.put(1, 1);
+      lay.put(d.addr, 8);
+      lay.put(d.bytes, 8);
+      message(msgs, kLayout, 0, lay);
+      meta.pad8();
+      const uint64_t oh = here();
+      meta.put(1, 1);
+      meta.put(0, 1);
+      meta.put(4, 2);
+      meta.put(1, 4);
+      meta.put(msgs.b.size(), 4);
+      meta.put(0, 4);
+      meta.bytes(msgs.b.data(), msgs.b.size());
+      es.push_back({d.name, oh, false, nullptr});
+    }
+    std::sort(es.begin(), es.end(), [](const Entry &a, const Entry &b) { return a.name < b.name; });
+    for (size_t k = 1; k < es.size(); ++k)
+      if (es[k].name == es[k - 1].name) return fail(err, "name " + es[k].name + " used twice in one group");
+    // local heap data: "" then the names
+    Buf heap;
+    heap.put(0, 8);
+    std::vector<uint64_t> off;
+    for (const Entry &e : es) {
+      off.push_back(heap.b.size());
+      heap.bytes(e.name.c_str(), e.name.size() + 1);
+      heap.pad8();
+    }
+    const size_t nsnod = (es.size() + 2 * kLeafK - 1) / (2 * kLeafK);
+    meta.pad8();
+    const uint64_t a_heap = here();
+    meta.bytes("HEAP", 4);
+    meta.put(0, 4);
+    meta.put(heap.b.size(), 8);
+    meta.put(1, 8);
+    meta.put(a_heap + 32, 8);
+    meta.bytes(heap.b.data(), heap.b.size());
+    std::vector<uint64_t> a_snod;
+    for (size_t sn = 0; sn < nsnod; ++sn) {
+      meta.pad8();
+      a_snod.push_back(here());
+      const size_t start = meta.b.size();
+      meta.bytes("SNOD", 4);
+      meta.put(1, 1);
+      meta.put(0, 1);
+      const size_t lo = sn * 2 * kLeafK, hi = std::min(es.size(), lo + 2 * kLeafK);
+      meta.put(hi - lo, 2);
+      for (size_t k = lo; k < hi; ++k) {
+        meta.put(off[k], 8);
+        meta.put(es[k].oh, 8);
+        if (es[k].group) {  // cache type 1: the group's B-tree and heap
+          meta.put(1, 4);
+          meta.put(0, 4);
+          meta.put(es[k].gp->tree, 8);
+          meta.put(es[k].gp->heap, 8);
+        } else {
+          meta.put(0, 4);
+          meta.put(0, 4);
+          meta.put(0, 16);
+        }
+      }
+      meta.b.resize(start + snod_size, 0);
+    }
+    meta.pad8();
+    const uint64_t a_tree = here();
+    {
+      const size_t start = meta.b.size();
+      meta.bytes("TREE", 4);
+      meta.put(0, 1);
+      meta.put(0, 1);
+      meta.put(nsnod, 2);
+      meta.put(kUndef, 8);
+      meta.put(kUndef, 8);
+      meta.put(0, 8);
+      for (size_t sn = 0; sn < nsnod; ++sn) {
+        const size_t last = std::min(es.size(), (sn + 1) * 2 * kLeafK) - 1;
+        meta.put(a_snod[sn], 8);
+        meta.put(off[last], 8);
+      }
+      meta.b.resize(start + tree_size, 0);
+    }
+    // the group's object header: its symbol table and its attributes
+    Buf msgs;
+    Buf st;
+    st.put(a_tree, 8);
+    st.put(a_heap, 8);
+    message(msgs, kSymtab, 0, st);
+    for (const Impl::Attr &a : g.attrs) {
+      Buf nm, ty = type_of(a.cls, a.size), sp = space_v1({a.n});
+      nm.bytes(a.name.c_str(), a.name.size() + 1);
+      Buf am;
+      am.put(1, 1);
+      am.put(0, 1);
+      am.put(a.name.size() + 1, 2);
+      am.put(ty.b.size(), 2);
+      am.put(sp.b.size(), 2);
+      nm.pad8();
+      ty.pad8();
+      sp.pad8();
+      am.bytes(nm.b.data(), nm.b.size());
+      am.bytes(ty.b.data(), ty.b.size());
+      am.bytes(sp.b.data(), sp.b.size());
+      am.bytes(a.bytes.data(), a.bytes.size());
+      message(msgs, 0x0C, 0, am);
+    }
+    meta.pad8();
+    g.oh = here();
+    g.tree = a_tree;
+    g.heap = a_heap;
+    meta.put(1, 1);
+    meta.put(0, 1);
+    meta.put(1 + g.attrs.size(), 2);
+    meta.put(1, 4);
+    meta.put(msgs.b.size(), 4);
+    meta.put(0, 4);
+    meta.bytes(msgs.b.data(), msgs.b.size());
+    return true;
+  };
+  if (!emit(I.root)) return false;
+  // the metadata after the data, then the superblock
+  static const uint8_t zeros[8] = {0};
+  const uint64_t pad = base - I.eof;
+  if ((pad && std::fwrite(zeros, 1, pad, I.f) != pad) ||
+      std::fwrite(meta.b.data(), 1, meta.b.size(), I.f) != meta.b.size())
+    return fail(err, I.path + ": write failed");
+  const uint64_t eof = base + meta.b.size();
+  Buf sb;
+  sb.bytes(kSig, 8);
+  sb.put(0, 4);
+  sb.put(0, 1);
+  sb.put(8, 1);
+  sb.put(8, 1);
+  sb.put(0, 1);
+  sb.put(kLeafK, 2);
+  sb.put(K, 2);
+  sb.put(0, 4);
+  sb.put(0, 8);
+  sb.put(kUndef, 8);
+  sb.put(eof, 8);
+  sb.put(kUndef, 8);
+  sb.put(0, 8);
+  sb.put(I.root.oh, 8);
+  sb.put(1, 4);
+  sb.put(0, 4);
+  sb.put(I.root.tree, 8);
+  sb.put(I.root.heap, 8);
+  const bool ok = std::fseek(I.f, 0, SEEK_SET) == 0 && std::fwrite(sb.b.data(), 1, sb.b.size(), I.f) == sb.b.size();
+  const bool closed = std::fclose(I.f) == 0;
+  I.f = nullptr;
+  if (!ok || !closed) return fail(err, I.path + ": write failed");
+  return true;
+}
+
+}  // namespace h5
+}  // namespace cil
+
 // ---------------------------------------------------------------------------- C ABI
 namespace {
 thread_local std::string g_h5_err;
@@ -575,6 +1016,93 @@ cil_status cil_h5_read(const char *path, const char *dataset, double *out, int64
 void cil_h5_last_error(char *buf, size_t len) {
   if (!buf || len == 0) return;
   snprintf(buf, len, "%s", g_h5_err.c_str());
+}
+
+}  // extern "C"
+
+namespace {
+
+// the datasets of one colony state (outputHDF5Frame), through `put(name, dims, f32 data)` and
+// `puti(name, dims, i32 data)`
+template <class F32, class I32>
+bool put_state(const cil_h5_state *s, F32 put, I32 puti) {
+  const uint64_t n = static_cast<uint64_t>(s->ncells), E = static_cast<uint64_t>(s->nelem),
+                 D = static_cast<uint64_t>(s->dim);
+  const std::vector<double> zv(n * E * D, 0.0), zs(n, 0.0), ze(n * E, 0.0);
+  const std::vector<int32_t> zi(n, 0);
+  auto pick = [](const double *p, const std::vector<double> &z) { return p ? p : z.data(); };
+  const std::vector<uint64_t> vec{n, E, D}, per_elem{n, E}, per_cell{n};
+  return put("R", vec, pick(s->pos, zv)) && put("Vel", vec, pick(s->vel, zv)) &&
+         put("SigmaCore", per_elem, pick(s->sigma, ze)) && put("F", vec, pick(s->force, zv)) &&
+         put("FD", vec, pick(s->force_dis, zv)) && put("FR", vec, pick(s->force_ran, zv)) &&
+         put("RHO", per_cell, pick(s->rho, zs)) && put("Theta", per_cell, pick(s->theta, zs)) &&
+         put("PR", per_cell, pick(s->pressure, zs)) && puti("State", per_cell, s->state ? s->state : zi.data()) &&
+         puti("T0", per_cell, s->t0 ? s->t0 : zi.data()) && put("CpuTime", std::vector<uint64_t>{1}, &s->cpu_time);
+}
+
+bool state_ok(const cil_h5_state *s) {
+  return s && s->ncells >= 0 && s->nelem >= 1 && (s->dim == 2 || s->dim == 3);
+}
+
+}  // namespace
+
+struct cil_h5_frames {
+  cil::h5::FrameFile file;
+};
+
+extern "C" {
+
+cil_status cil_h5_attr(const char *path, const char *object, const char *name, double *out, int64_t capacity,
+                       int64_t *n) {
+  if (!path || !object || !name || !n) return h5_fail("cil_h5_attr: NULL argument", CIL_ERR_CONFIG);
+  cil::h5::Reader r;
+  std::string err;
+  std::vector<double> v;
+  if (!r.open(path, &err) || !r.attribute(object, name, &v, &err)) return h5_fail(err);
+  *n = static_cast<int64_t>(v.size());
+  if (*n > capacity) return h5_fail(std::string(name) + ": " + std::to_string(v.size()) + " values", CIL_ERR_CAPACITY);
+  std::copy(v.begin(), v.end(), out);
+  return CIL_OK;
+}
+
+cil_status cil_h5_frames_create(const char *path, int32_t dim, const double *box, double dt, int32_t gts,
+                                cil_h5_frames **out) {
+  if (!path || !box || !out || (dim != 2 && dim != 3)) return h5_fail("cil_h5_frames_create: bad arguments", CIL_ERR_CONFIG);
+  *out = nullptr;
+  cil_h5_frames *w = new cil_h5_frames();
+  std::string err;
+  const bool ok = w->file.create(path, &err) && w->file.attr_f64("params", "dt", {dt}, &err) &&
+                  w->file.attr_f64("params", "L", std::vector<double>(box, box + dim), &err) &&
+                  w->file.attr_i32("params", "Tdump", {gts}, &err);
+  w->file.make_group("snapshots");
+  if (!ok) {
+    delete w;
+    return h5_fail(err);
+  }
+  *out = w;
+  return CIL_OK;
+}
+
+cil_status cil_h5_frames_write(cil_h5_frames *w, int32_t frame, int32_t ts, const cil_h5_state *s) {
+  if (!w || !state_ok(s) || frame < 0) return h5_fail("cil_h5_frames_write: bad arguments", CIL_ERR_CONFIG);
+  const std::string g = "snapshots/t_" + std::to_string(frame);
+  std::string err;
+  auto put = [&](const char *nm, const std::vector<uint64_t> &dims, const double *d) {
+    return w->file.data_f32(g, nm, dims, d, &err);
+  };
+  auto puti = [&](const char *nm, const std::vector<uint64_t> &dims, const int32_t *d) {
+    return w->file.data_i32(g, nm, dims, d, &err);
+  };
+  if (!w->file.attr_i32(g, "ts", {ts}, &err) || !put_state(s, put, puti)) return h5_fail(err);
+  return CIL_OK;
+}
+
+cil_status cil_h5_frames_close(cil_h5_frames *w) {
+  if (!w) return CIL_OK;
+  std::string err;
+  const bool ok = w->file.close(&err);
+  delete w;
+  return ok ? CIL_OK : h5_fail(err);
 }
 
 cil_status cil_h5_write_state(const char *path, const cil_h5_state *s) {

@@ -44,6 +44,9 @@ class Reader {
   bool read(const Dataset &ds, std::vector<double> *out, std::string *err) const;
   // Names in a group ("" or "/" for the root) in the group's name order.
   bool list(const std::string &group, std::vector<std::string> *names, std::string *err) const;
+  // A numeric attribute of an object (group or dataset), converted to double.
+  bool attribute(const std::string &object, const std::string &name, std::vector<double> *out,
+                 std::string *err) const;
 
  private:
   struct Msg {
@@ -83,6 +86,32 @@ class Writer {
     std::vector<uint8_t> data;
   };
   std::vector<Item> items_;
+};
+
+// Writes a frame file of the reference's layout (initHDF5Output / outputHDF5Frame,
+// OutputWriter.cpp:240-330, 388-441: /params with the run's attributes, /snapshots/t_<frame>
+// with the frame's datasets and its step as the attribute ts) incrementally: each dataset's
+// data is appended as it comes, and the metadata (groups as symbol tables, dataset headers as
+// Writer lays them out, one-dimensional numeric attributes as in H5LT's set_attribute) is written
+// at close, with the superblock. The reference's groups also track the creation order of their
+// links; these do not, which readers (h5py, libhdf5) only see when asked for that order.
+class FrameFile {
+ public:
+  bool create(const std::string &path, std::string *err);
+  // groups are paths from the root ("params", "snapshots/t_3"), created on first use
+  void make_group(const std::string &group);
+  bool attr_f64(const std::string &group, const std::string &name, const std::vector<double> &v, std::string *err);
+  bool attr_i32(const std::string &group, const std::string &name, const std::vector<int32_t> &v, std::string *err);
+  bool data_f32(const std::string &group, const std::string &name, const std::vector<uint64_t> &dims,
+                const double *data, std::string *err);
+  bool data_i32(const std::string &group, const std::string &name, const std::vector<uint64_t> &dims,
+                const int32_t *data, std::string *err);
+  bool close(std::string *err);
+  ~FrameFile();
+
+ private:
+  struct Impl;
+  Impl *impl_ = nullptr;
 };
 
 }  // namespace h5

@@ -8,7 +8,7 @@
 // a progress line in the reference's format, a GSD frame when OUTPUT.FORMAT lists GSD. At the
 // end the final state goes to <DIR>/Last/<NAME>.Last.gsd as one frame labelled step 0
 // (finalizeOutput, OutputWriter.cpp:724-745), and with H5 in OUTPUT.FORMAT to
-// <DIR>/Last/<NAME>.Last.h5 (the H5 frame file is not written). Two-element species run the
+// <DIR>/Last/<NAME>.Last.h5, single-element runs also to the frame file <DIR>/<NAME>.h5. Two-element species run the
 // two-element step with the device-fed frame writer (include/cil_gsd.h); single-element
 // species, the shipped runs, run the cell-cycle model (include/cil_cycle.h), whose frames are
 // downloaded and written with the GSD file layer (charge: the cycle activity rho, mass: the pressure, as
@@ -100,9 +100,14 @@ void cycle_frame(cil_gsd_file *f, const cil_cycle_params &p, const cil_run_info 
   if (cil_gsd_end_frame(f) != CIL_OK) throw std::runtime_error("GSD write failed");
 }
 
+// One snapshot of the frame file (outputHDF5Frame with id >= 0) of a cell-cycle colony
+void cycle_h5_frame(cil_h5_frames *hf, int32_t frame, int32_t ts, const cil_cycle_params &p, cil_cycle *h,
+                    double cpu_time);
+
 // The final-state file <DIR>/Last/<NAME>.Last.h5 (outputHDF5Frame with id -1 and the move into
-// Last/, OutputWriter.cpp:388-441, 736-745) of a cell-cycle colony
-void cycle_last_h5(const std::string &path, const cil_cycle_params &p, cil_cycle *h, double cpu_time) {
+// Last/, OutputWriter.cpp:388-441, 736-745) of a cell-cycle colony; with hf, a snapshot instead
+void cycle_last_h5(const std::string &path, const cil_cycle_params &p, cil_cycle *h, double cpu_time,
+                   cil_h5_frames *hf = nullptr, int32_t frame = 0, int32_t ts = 0) {
   cil_cycle_view v{};
   cil_cycle_download(h, &v);  // cell count
   const int n = v.ncells, D = p.dim;
@@ -138,11 +143,17 @@ void cycle_last_h5(const std::string &path, const cil_cycle_params &p, cil_cycle
   s.state = state.data();
   s.t0 = t0.data();
   s.cpu_time = cpu_time;
-  if (cil_h5_write_state(path.c_str(), &s) != CIL_OK) {
+  const cil_status st = hf ? cil_h5_frames_write(hf, frame, ts, &s) : cil_h5_write_state(path.c_str(), &s);
+  if (st != CIL_OK) {
     char buf[512] = {0};
     cil_h5_last_error(buf, sizeof buf);
-    throw std::runtime_error(std::string("writing ") + path + ": " + buf);
+    throw std::runtime_error(std::string("writing ") + (hf ? std::string("an H5 frame") : path) + ": " + buf);
   }
+}
+
+void cycle_h5_frame(cil_h5_frames *hf, int32_t frame, int32_t ts, const cil_cycle_params &p, cil_cycle *h,
+                    double cpu_time) {
+  cycle_last_h5(std::string(), p, h, cpu_time, hf, frame, ts);
 }
 
 double seconds_since(std::chrono::steady_clock::time_point t0) {
@@ -163,7 +174,6 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
   check(cil_input_cycle_config(in, &p, &run), "cil_input_cycle_config", nullptr, in);
   if (frames_arg > 0) run.frames = frames_arg;
   if (gts_arg > 0) run.gts = gts_arg;
-  if (run.output_h5) std::fprintf(stderr, "# H5: the final state only (<NAME>.Last.h5); frames go to GSD\n");
   const int n = run.ncells, D = p.dim;
   std::vector<double> pos(static_cast<size_t>(n) * D), vel(pos.size(), 0.0), sig(n), sigt(n), th(n), rho(n), om(n);
   cil_cycle_view v{};
@@ -190,6 +200,13 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
         throw std::runtime_error("cannot create " + dir + "/" + name + ".gsd");
       cycle_frame(f, p, run, h, 0);
     }
+    cil_h5_frames *hf = nullptr;  // the H5 frame file (outputHDF5Frame)
+    if (run.output_h5) {
+      mkdir(dir.c_str(), 0755);
+      if (cil_h5_frames_create((dir + "/" + name + ".h5").c_str(), p.dim, p.box, p.dt, run.gts, &hf) != CIL_OK)
+        throw std::runtime_error("cannot create " + dir + "/" + name + ".h5");
+      cycle_h5_frame(hf, 0, 0, p, h, 0.0);
+    }
     int64_t ts = 0;
     double cpu_time = 0.0;
     for (int iframe = 1; iframe <= run.frames; ++iframe) {
@@ -202,9 +219,10 @@ int run_cycle(cil_input *in, int frames_arg, int gts_arg) {
                    static_cast<double>(ts) * p.dt, c.ncells, c.ncells);
       if (f) cycle_frame(f, p, run, h, ts);
       cpu_time = seconds_since(t_frame);
+      if (hf) cycle_h5_frame(hf, iframe, static_cast<int32_t>(ts), p, h, cpu_time);
     }
+    if (hf && cil_h5_frames_close(hf) != CIL_OK) throw std::runtime_error("writing " + dir + "/" + name + ".h5");
     if (run.output_h5) {
-      mkdir(dir.c_str(), 0755);
       mkdir((dir + "/Last").c_str(), 0733);
       cycle_last_h5(dir + "/Last/" + name + ".Last.h5", p, h, cpu_time);
     }
@@ -252,7 +270,6 @@ int main(int argc, char **argv) {
     check(cil_input_config(in, &cfg, &p, &run), "cil_input_config", nullptr, in);
     if (frames_arg > 0) run.frames = frames_arg;
     if (gts_arg > 0) run.gts = gts_arg;
-    if (run.output_h5) std::fprintf(stderr, "# H5: the final state only (<NAME>.Last.h5); frames go to GSD\n");
     const int D = cfg.dim, cap = run.capacity > run.ncells ? run.capacity : run.ncells;
     std::vector<double> pos(static_cast<size_t>(cap) * 2 * D), sig(static_cast<size_t>(cap) * 2);
     std::vector<int> t0(cap), tsw(cap);
@@ -277,6 +294,51 @@ int main(int argc, char **argv) {
       check(cil_frame_open(h, 0, (dir + "/" + name + ".gsd").c_str(), &fo, &w), "cil_frame_open", h);
       check(cil_frame_write(w, 0, nullptr), "cil_frame_write", h);  // outputFrame(0, 0)
     }
+    // the state of the colony as outputHDF5Frame writes it: a snapshot of the frame file (hf) or
+    // the final-state file (path)
+    auto two_element_h5 = [&](cil_handle *hh, const char *path, cil_h5_frames *f5, int32_t frame, int32_t ts5,
+                              double cpu) {
+      std::vector<double> p5(static_cast<size_t>(cap) * 2 * D), s5(static_cast<size_t>(cap) * 2), v5(p5.size()),
+          f5f(p5.size());
+      std::vector<int> t05(cap), tw5(cap);
+      cil_colony_view w5{};
+      w5.capacity = cap;
+      w5.pos = p5.data();
+      w5.sigma = s5.data();
+      w5.vel = v5.data();
+      w5.t0 = t05.data();
+      w5.tswitch = tw5.data();
+      check(cil_download(hh, 0, &w5), "cil_download", hh);
+      check(cil_forces(hh, 0, f5f.data()), "cil_forces", hh);
+      const int n5 = w5.ncells;
+      std::vector<double> rho(n5, 1.0);  // initializeCellStatus's activity, which the step never changes
+      std::vector<int32_t> state(n5, 0);
+      cil_h5_state st5{};
+      st5.ncells = n5;
+      st5.nelem = 2;
+      st5.dim = D;
+      st5.pos = p5.data();
+      st5.vel = v5.data();
+      st5.force = f5f.data();
+      st5.sigma = s5.data();
+      st5.rho = rho.data();
+      st5.state = state.data();
+      st5.t0 = t05.data();
+      st5.cpu_time = cpu;
+      const cil_status r5 = f5 ? cil_h5_frames_write(f5, frame, ts5, &st5) : cil_h5_write_state(path, &st5);
+      if (r5 != CIL_OK) {
+        char buf[512] = {0};
+        cil_h5_last_error(buf, sizeof buf);
+        throw std::runtime_error(std::string("writing H5 output: ") + buf);
+      }
+    };
+    cil_h5_frames *hf = nullptr;
+    if (run.output_h5) {
+      mkdir(dir.c_str(), 0755);
+      if (cil_h5_frames_create((dir + "/" + name + ".h5").c_str(), D, p.box, p.dt, run.gts, &hf) != CIL_OK)
+        throw std::runtime_error("cannot create " + dir + "/" + name + ".h5");
+      two_element_h5(h, nullptr, hf, 0, 0, 0.0);
+    }
     int64_t ts = 0;
     double cpu_time = 0.0;
     for (int iframe = 1; iframe <= run.frames; ++iframe) {
@@ -288,40 +350,13 @@ int main(int argc, char **argv) {
                    static_cast<double>(ts) * p.dt, o.ncells, 2 * o.ncells);
       if (w) check(cil_frame_write(w, ts, nullptr), "cil_frame_write", h);
       cpu_time = seconds_since(t_frame);
+      if (hf) two_element_h5(h, nullptr, hf, iframe, static_cast<int32_t>(ts), cpu_time);
     }
+    if (hf && cil_h5_frames_close(hf) != CIL_OK) throw std::runtime_error("writing " + dir + "/" + name + ".h5");
+    hf = nullptr;
     if (run.output_h5) {  // the final state of the two-element colony
-      std::vector<double> vel(static_cast<size_t>(cap) * 2 * D), frc(vel.size());
-      v = cil_colony_view{};
-      v.capacity = cap;
-      v.pos = pos.data();
-      v.sigma = sig.data();
-      v.vel = vel.data();
-      v.t0 = t0.data();
-      v.tswitch = tsw.data();
-      check(cil_download(h, 0, &v), "cil_download", h);
-      check(cil_forces(h, 0, frc.data()), "cil_forces", h);
-      const int n = v.ncells;
-      std::vector<double> rho(n, 1.0);  // initializeCellStatus's activity, which the step never changes
-      std::vector<int32_t> state(n, 0);
-      cil_h5_state s{};
-      s.ncells = n;
-      s.nelem = 2;
-      s.dim = D;
-      s.pos = pos.data();
-      s.vel = vel.data();
-      s.force = frc.data();
-      s.sigma = sig.data();
-      s.rho = rho.data();
-      s.state = state.data();
-      s.t0 = t0.data();
-      s.cpu_time = cpu_time;
-      mkdir(dir.c_str(), 0755);
       mkdir((dir + "/Last").c_str(), 0733);
-      if (cil_h5_write_state((dir + "/Last/" + name + ".Last.h5").c_str(), &s) != CIL_OK) {
-        char buf[512] = {0};
-        cil_h5_last_error(buf, sizeof buf);
-        throw std::runtime_error(std::string("writing the final-state H5 file: ") + buf);
-      }
+      two_element_h5(h, (dir + "/Last/" + name + ".Last.h5").c_str(), nullptr, 0, 0, cpu_time);
     }
     if (w) {
       check(cil_frame_close(w), "cil_frame_close", h);

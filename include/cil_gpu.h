@@ -179,8 +179,9 @@ cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *view);
 cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts);
 
 /* Computes the forces of the current state without integrating (calculForcesPressure,
- * CIL.cu:999-1007), drawing the noise exactly as a step would, and copies them to frc
- * [cell][2][dim]. For parity checks and frame output. */
+ * CIL.cu:999-1007), with the noise the next step will draw, and copies them to frc
+ * [cell][2][dim]; the run is left unchanged (the host stream of the dSFMT mode is put back).
+ * For parity checks and frame output. */
 cil_status cil_forces(cil_handle *h, int32_t colony, double *frc);
 
 /* Bin structure of the current positions (LinkList::populate, Container.cpp:58-79;

@@ -137,6 +137,22 @@ typedef struct cil_h5_state {
 } cil_h5_state;
 cil_status cil_h5_write_state(const char *path, const cil_h5_state *s);
 
+/* A numeric attribute of an object ("params", "/snapshots/t_3") as doubles; *n receives its
+ * length. */
+cil_status cil_h5_attr(const char *path, const char *object, const char *name, double *out, int64_t capacity,
+                       int64_t *n);
+
+/* The frame file <NAME>.h5 (initHDF5Output and outputHDF5Frame, OutputWriter.cpp:240-330,
+ * 388-441): /params with the attributes dt, L (the box) and Tdump (GTS), then per frame the
+ * group /snapshots/t_<frame> with the datasets of cil_h5_write_state and the attribute ts.
+ * Frames are appended as written; the file is complete at cil_h5_frames_close. Groups are
+ * symbol tables: the reference's groups also track the creation order of their links. */
+typedef struct cil_h5_frames cil_h5_frames;
+cil_status cil_h5_frames_create(const char *path, int32_t dim, const double *box, double dt, int32_t gts,
+                                cil_h5_frames **out);
+cil_status cil_h5_frames_write(cil_h5_frames *w, int32_t frame, int32_t ts, const cil_h5_state *s);
+cil_status cil_h5_frames_close(cil_h5_frames *w);
+
 #ifdef __cplusplus
 }
 #endif

@@ -196,3 +196,40 @@ def test_runner_two_element_final_state_h5(gpu_lib, tmp_path):
     np.testing.assert_array_equal(G.h5_read(h5, "T0"), g["t0"])
     np.testing.assert_array_equal(G.h5_read(h5, "F"), frc.astype(np.float32))
     assert G.h5_read(h5, "RHO").shape == (n,)
+
+
+@pytest.mark.parametrize("fixture", ["two", "single"])
+def test_runner_h5_frame_file(gpu_lib, tmp_path, fixture):
+    """OUTPUT.FORMAT with H5: the frame file <NAME>.h5 (/params dt, L, Tdump; /snapshots/t_<k>
+    with R, F, ... and ts) holds the same frames as the GSD file, and writing it leaves the run
+    unchanged (the GSD frames equal those of a GSD-only run)."""
+    G = gpu_lib
+    from cil_cuda_gb300 import build
+    doc = json.load(open(FIXTURE if fixture == "two" else SINGLE))
+    name = doc["OUTPUT"]["NAME"]
+    outs = {}
+    for fmt in (["GSD"], ["GSD", "H5"]):
+        d = json.loads(json.dumps(doc))
+        d["OUTPUT"]["DIR"] = str(tmp_path / "_".join(fmt))
+        d["OUTPUT"]["FORMAT"] = fmt
+        cfg = tmp_path / ("run_%s.json" % "_".join(fmt))
+        cfg.write_text(json.dumps(d))
+        res = subprocess.run([build.RUNNER, str(cfg)], capture_output=True, text=True, timeout=300)
+        assert res.returncode == 0, res.stderr
+        outs["_".join(fmt)] = d["OUTPUT"]["DIR"]
+    g0 = GSDFile(os.path.join(outs["GSD"], name + ".gsd"))
+    g1 = GSDFile(os.path.join(outs["GSD_H5"], name + ".gsd"))
+    assert g0.nframes == g1.nframes == doc["MD"]["FRAMES"] + 1
+    h5 = os.path.join(outs["GSD_H5"], name + ".h5")
+    L = np.asarray(doc["MD"]["BOX"], float)
+    np.testing.assert_array_equal(G.h5_attr(h5, "params", "L"), L)
+    np.testing.assert_array_equal(G.h5_attr(h5, "params", "Tdump"), [doc["MD"]["GTS"]])
+    for k in range(g0.nframes):
+        np.testing.assert_array_equal(g0.read(k, "particles/position"), g1.read(k, "particles/position"))
+        step = int(g1.read(k, "configuration/step")[0])
+        np.testing.assert_array_equal(G.h5_attr(h5, "snapshots/t_%d" % k, "ts"), [step])
+        R = G.h5_read(h5, "snapshots/t_%d/R" % k)
+        n = R.shape[0] * R.shape[1]
+        assert int(g1.read(k, "particles/N")[0]) == n
+        d = g1.read(k, "particles/position")[:, :2].astype(np.float64) - (R.reshape(n, 2) - L / 2)
+        assert np.abs(d).max() <= 4 * np.spacing(np.float32(L.max()))

@@ -280,3 +280,49 @@ def test_reader_refuses_malformed_files(G, tmp_path):
     with pytest.raises(G.CilError) as e:
         G.h5_read(path, "R")
     assert "superblock version 2" in str(e.value)
+
+
+def test_frame_file_round_trip(G, tmp_path):
+    """The frame file (initHDF5Output / outputHDF5Frame): /params attributes dt, L, Tdump; per
+    frame /snapshots/t_<frame> with the datasets and the attribute ts, as the reference's
+    analysis (cil.py: f["snapshots/"], .get('R'), attrs['ts'][0], f["/params"].attrs['dt'][0])
+    reads them; frames of different sizes, 3D, and more frames than one symbol node holds."""
+    path = str(tmp_path / "run.h5")
+    w = G.H5Frames(path, box=[12.0, 13.0, 14.0], dt=1e-4, gts=200)
+    states = []
+    rng = np.random.default_rng(9)
+    for k in range(20):
+        st = random_state(rng, 5 + 3 * k, 1, 3)
+        states.append(st)
+        w.write(k, 200 * k, **st)
+    w.close()
+    np.testing.assert_array_equal(G.h5_attr(path, "params", "dt"), [1e-4])
+    np.testing.assert_array_equal(G.h5_attr(path, "/params", "L"), [12.0, 13.0, 14.0])
+    np.testing.assert_array_equal(G.h5_attr(path, "params", "Tdump"), [200])
+    f32 = lambda a: np.asarray(a, np.float64).astype(np.float32).astype(np.float64)  # noqa: E731
+    for k in (0, 7, 19):
+        g = "snapshots/t_%d/" % k
+        np.testing.assert_array_equal(G.h5_attr(path, "snapshots/t_%d" % k, "ts"), [200 * k])
+        np.testing.assert_array_equal(G.h5_read(path, g + "R"), f32(states[k]["pos"]))
+        np.testing.assert_array_equal(G.h5_read(path, g + "F"), f32(states[k]["force"]))
+        np.testing.assert_array_equal(G.h5_read(path, g + "T0"), states[k]["t0"])
+        np.testing.assert_array_equal(G.h5_read(path, g + "CpuTime"), [3.5])
+    # an empty run still has its groups
+    p2 = str(tmp_path / "empty.h5")
+    G.H5Frames(p2, box=[5.0, 5.0], dt=0.1, gts=1).close()
+    np.testing.assert_array_equal(G.h5_attr(p2, "params", "L"), [5.0, 5.0])
+    with pytest.raises(G.CilError):
+        G.h5_read(p2, "snapshots/t_0/R")
+
+
+def test_frame_file_with_many_frames(G, tmp_path):
+    """300 snapshots: more entries than a group B-tree node of K 16 holds (256), so the file's K
+    grows to hold them in one node."""
+    path = str(tmp_path / "long.h5")
+    w = G.H5Frames(path, box=[5.0, 5.0], dt=0.1, gts=1)
+    for k in range(300):
+        w.write(k, k, pos=np.full((1, 1, 2), 0.01 * k), sigma=np.ones((1, 1)))
+    w.close()
+    for k in (0, 150, 299):
+        np.testing.assert_array_equal(G.h5_attr(path, "snapshots/t_%d" % k, "ts"), [k])
+        assert G.h5_read(path, "snapshots/t_%d/R" % k)[0, 0, 0] == np.float32(0.01 * k)
