@@ -12,9 +12,9 @@
  *               CIL_CYCLE_DPD with INTEGRATOR.DPD DISSAMCEL / DISDIFCEL / DISBG, KBT and the
  *               species' MASS). AUTOSCALE is refused with a message.
  *   RUNTIME     RNG.SEED (<= 0: the current time, as Random::init(time(NULL))).
- *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 by the final-state file
- *               <NAME>.Last.h5, cil_h5_write_state below; the H5 frame file, whose groups
- *               track link creation order, is not served).
+ *   OUTPUT      DIR, NAME, FORMAT (GSD is served by cil_gsd.h; H5 by the frame file <NAME>.h5,
+ *               cil_h5_frames_* below, and the final-state file <NAME>.Last.h5,
+ *               cil_h5_write_state).
  *   SPECIES     one species. Two-element cells (cil_gpu.h): NELEM, NAMES, MOTILITY, FRICTION,
  *               NOISE.PASSIVE, the element diameters of the selected pair force, FENE RMAX /
  *               KAPPA_PULL (for the steady-state length rss that INIT RANDOM uses),
