@@ -614,7 +614,13 @@ void ora_get_state(const void *h, double *pos, double *sigma, double *vel, doubl
   if (tswitch) std::memcpy(tswitch, o->tsw.data(), sizeof(int32_t) * o->n);
 }
 
-void ora_compute_forces(void *h) { H(h)->compute_forces(); }
+// The forces of the current state with the noise the next step will draw; the random stream
+// is put back, as cil_forces does, so that reading them leaves the run unchanged.
+void ora_compute_forces(void *h) {
+  const Rng saved = H(h)->rng;
+  H(h)->compute_forces();
+  H(h)->rng = saved;
+}
 
 int32_t ora_step(void *h, int32_t nsteps) {
   Oracle *o = H(h);
