@@ -41,10 +41,37 @@ BOX = 2048.0
 CAP = 1_200_000
 GTS = 100  # steps per output frame in the end-to-end arm
 FRAME_CAP = 1_600_000  # cells: the frame-output leg grows the colony for 3000 steps
-# DRAM bytes per launch of k_force_list on this workload (learned scheduler, 2M particles) from one
-# ncu capture: dram__bytes_read.sum + dram__bytes_write.sum = 187.23 MB + 45.94 MB
-# (profiles/k_force_list_2d_softcore_2M.md)
-TRAFFIC_PER_LAUNCH = 233_163_008
+# ncu summary of the dominant kernel on this workload; roofline.traffic is read from its
+# dram__bytes_read.sum + dram__bytes_write.sum rows (one launch, one capture)
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_force_list_2d_softcore_2M.md")
+WORKLOAD = ("2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
+            "division+apoptosis on, dt=1e-4, 2048^2 periodic box")
+
+
+def bench_config(world: int) -> dict:
+    """The workload as both arms report it: the checkpoint's size before any step (the two arms
+    warm up differently, so counts taken later differ by the divisions in between)."""
+    return {"workload": WORKLOAD, "particles": 2 * NCELLS, "cells": NCELLS,
+            "l2": "working set ~230 MB per step > 126 MB L2, no flush",
+            "parallelism": f"replicas x{world}"}
+
+
+def profile_traffic(path: str = TRAFFIC_PROFILE):
+    """DRAM bytes of one launch from a committed ncu summary (markdown table rows
+    `| dram__bytes_read.sum | v | unit |`), or None when the file has no such rows."""
+    scale = {"byte": 1.0, "kbyte": 1e3, "mbyte": 1e6, "gbyte": 1e9}
+    got = {}
+    try:
+        with open(path) as f:
+            for line in f:
+                cells = [c.strip().strip("`") for c in line.strip().strip("|").split("|")]
+                if len(cells) >= 3 and cells[0] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                    got[cells[0]] = float(cells[1].replace(",", "")) * scale.get(cells[2].lower(), 1.0)
+    except OSError:
+        return None
+    if len(got) != 2:
+        return None
+    return got["dram__bytes_read.sum"] + got["dram__bytes_write.sum"]
 
 
 def peaks():
@@ -160,6 +187,7 @@ def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0, s
     if warmup:
         eng.step(warmup)
     n0 = eng.observables(0)["ncells"]
+    sk0 = eng.skin_stats(0) if skin > 0 else None
     barrier(dist)
     t0 = time.perf_counter()
     eng.step(steps)  # synchronises the handle's stream before returning
@@ -168,6 +196,9 @@ def run_form(G, p, st, precision, steps, warmup, device, seed, dist, skin=0.0, s
     gi = eng.graph_info()
     n1 = eng.observables(0)["ncells"]
     sk = eng.skin_stats(0) if skin > 0 else None
+    if sk is not None:
+        sk["rebuilds_in_timed_window"] = sk["nrebuild"] - sk0["nrebuild"]
+        sk["guard_trips_in_timed_window"] = sk["ntrip"] - sk0["ntrip"]
     eng.close()
     dev_s = tm["total_ms"] * 1e-3
     psteps = (n0 + n1) * steps  # 2 elements per cell, trapezoid over the (slow) growth
@@ -472,10 +503,13 @@ def reference_arm(args):
     o.set_state(**st)
     # bounded sample: each bench step is one full Euler step of the 2M-particle colony;
     # the number of timed steps is capped so that the run ends within a few minutes
+    # bounded sample: each bench step is one full Euler step of the 2M-particle colony; the
+    # warm-up is the requested one, and the number of timed steps is capped so that the run
+    # ends within a few minutes
     t0 = time.perf_counter()
     o.step(1)
     per = time.perf_counter() - t0
-    warm = min(args.warmup, 3)
+    warm = args.warmup
     if warm > 1:
         o.step(warm - 1)
     k = max(1, min(args.steps, int(90.0 / max(per, 1e-3))))
@@ -489,9 +523,8 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": k, "warmup": warm, "ms_per_step": wall / k * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
-                               "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
-                   "particles": 2 * n0, "cells": n0, "steps_requested": args.steps},
+        "config": bench_config(world),
+        "steps_requested": args.steps, "cells_timed": [n0, n1],
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{k} full Euler steps of the 2M-particle state on {threads} host threads "
                                    f"(oracle restatement; the reference's step does not compile)"},
@@ -514,8 +547,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
     ap.add_argument("--no-frames", action="store_true", help="skip the frame-output leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
-    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd"], default=None,
-                    help="run one form only (profiling)")
+    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd", "profile"],
+                    default=None, help="run one form only (profiling); profile: the headline form alone, "
+                                       "launched step by step, nothing else")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -543,6 +577,13 @@ def main():
         return 0
     p, st = workload(seed=1 + rank)
     hbm, peak_kind = peaks()
+    if args.only == "profile":
+        from cil_cuda_gb300 import skin_scheduler as SS
+        r = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist, skin=SS.load()[2],
+                     sched=True, graphs=False)
+        print(json.dumps({"profile_run": {"ms_per_step": r["dev_s"] / args.steps * 1e3, "timings": r["timings"],
+                                          "skin": r["skin"]}}))
+        return 0
 
     plain_steps = max(1, args.steps // 10)
     from cil_cuda_gb300 import skin_scheduler as SS
@@ -602,6 +643,7 @@ def main():
     achieved = bytes_per_elem * nelem / force_s / 1e9
     tp = plain["timings"]
     plain_force_s = tp["force_ms"] * 1e-3 / plain_steps
+    traffic = profile_traffic()
     form = ("mixed precision, Philox noise, Verlet skin with the learned scheduler" if have_mlp
             else f"mixed precision, Philox noise, Verlet skin {args.skin} sigma")
 
@@ -609,12 +651,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-force/f64-position", "data": "synthetic",
-        "config": {"workload": "2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
-                               "division+apoptosis on, dt=1e-4, 2048^2 periodic box",
-                   "particles": skinf["n0"] * 2, "cells": skinf["n0"], "cells_end": skinf["n1"],
-                   "form": form + ", CUDA-graph replay of steady steps",
-                   "l2": "working set ~230 MB per step > 126 MB L2, no flush",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(world),
+        "form": form + ", CUDA-graph replay of steady steps",
+        "cells_timed": [skinf["n0"], skinf["n1"]],
         "forms": {"mixed_skin_scheduled" if have_mlp else "mixed_skin": value,
                   "mixed_skin_fixed_0.3": fixed_value,
                   "mixed_rebuild_every_step": mixed_value, "plain_fp64": plain_value,
@@ -626,7 +665,9 @@ def main():
         "phases_ms_per_step": {k: tm[k] / psteps_ph for k in ("rebuild_ms", "force_ms", "events_ms")},
         "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": TRAFFIC_PER_LAUNCH, "traffic_unit": "bytes per launch (ncu)",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu: dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "traffic_source": os.path.relpath(TRAFFIC_PROFILE, ROOT),
                      "peak_kind": peak_kind,
                      "kernel": "k_force_list<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
                      "timed_on": f"{psteps_ph} individually launched steps (CUDA events around the force phase)",

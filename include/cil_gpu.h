@@ -281,10 +281,11 @@ cil_status cil_host_rng_draw(uint32_t seed, int32_t kind, int64_t n, double *out
 /* Element binning without any device allocation — no counterpart in the reference.
  *
  * For callers that cannot allocate device memory: a host framework that owns a budgeted
- * device pool and forbids outside cudaMalloc, code running while a CUDA graph is captured,
- * or a real-time loop that cannot risk an allocation. Same result as cil_bins for the same
+ * device pool and forbids outside cudaMalloc, or a real-time loop that cannot risk an
+ * allocation's latency or its failure mid-run. Same result as cil_bins for the same
  * positions and width (bins numbered as the reference's link list, ascending element ids
- * inside each bin), but the caller passes every buffer:
+ * inside each bin, in time linear in n_elems whatever the bins' occupancy), but the caller
+ * passes every buffer:
  *   pos        device, [n_elems][dim] FP64 positions inside [0, box)
  *   box        host, dim lengths;  width: minimum bin width
  *   ns         host out, bins per axis (1 on unused axes)
@@ -292,10 +293,12 @@ cil_status cil_host_rng_draw(uint32_t seed, int32_t kind, int64_t n, double *out
  *   elems      device out, n_elems element indices sorted by bin
  *   stream     cudaStream_t to run on (NULL = default stream)
  * Scratch lives in fixed device arrays inside the library: at most 1,048,576 elements and
- * 1,048,576 bins per call (about 8.3 MB held on every GPU that loads the library, until
- * exit). Larger inputs, or nbins > max_bins, return CIL_ERR_CAPACITY before any work. The
- * first call on a device resolves the scratch addresses; make it before any stream capture.
- * All calls share the scratch: calls that overlap on the GPU race, so serialise them. */
+ * 1,048,576 bins per call (about 14.7 MB held on every GPU that loads the library, until
+ * exit). Larger inputs, more than 1,048,576 bins along one axis, or nbins > max_bins return
+ * CIL_ERR_CAPACITY before any work is enqueued. The first call on a device resolves the
+ * scratch addresses (cudaGetSymbolAddress with that device current); make it before any
+ * stream capture. All calls share the scratch and each call overwrites what the last one
+ * left: calls that overlap on the GPU race, so serialise them. */
 cil_status cil_bin_elements_noalloc(const double *pos, int32_t n_elems, int32_t dim,
                                     const double *box, double width, int32_t *ns,
                                     int32_t *bin_start, int32_t *elems, int32_t max_bins,

@@ -156,6 +156,28 @@ struct LinkGrid {
   }
 };
 
+// BoundingBox::distance, Utils.hpp:536-544: r12 = r2 - r1, minus the nearest whole box along
+// periodic axes (Nint of r12 / L); returns |r12|^2
+double box_distance(int D, const double *box, const int32_t *periodic, double *r12, const double *r1,
+                    const double *r2) {
+  double ans = 0.0;
+  for (int d = 0; d < D; ++d) {
+    r12[d] = r2[d] - r1[d];
+    if (periodic[d]) r12[d] -= static_cast<double>(nint(r12[d] / box[d])) * box[d];
+    ans += r12[d] * r12[d];
+  }
+  return ans;
+}
+// BoundingBox::updatePos(r, v, dt), Utils.hpp:561-566
+void box_update_pos(int D, const double *box, const int32_t *periodic, double *r, const double *v, double dt) {
+  for (int d = 0; d < D; ++d)
+    r[d] = periodic[d] ? std::fmod(r[d] + dt * v[d] + box[d], box[d]) : r[d] + v[d] * dt;
+}
+// BoundingBox::updatePos(r, dr), Utils.hpp:556-559
+void box_update_pos(int D, const double *box, const int32_t *periodic, double *r, const double *dr) {
+  for (int d = 0; d < D; ++d) r[d] = periodic[d] ? std::fmod(r[d] + dr[d] + box[d], box[d]) : r[d] + dr[d];
+}
+
 // Half stencils including the own bin (Utils.hpp:700-704, DNS2D / DNS3D)
 const int kDns2d[5][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {-1, 1, 0}};
 const int kDns3d[14][3] = {{0, 0, 0},  {1, 0, 0},  {1, 1, 0},   {0, 1, 0},  {-1, 1, 0},
@@ -187,24 +209,12 @@ struct Oracle {
 
   // BoundingBox::distance, Utils.hpp:536-544: r12 = r2 - r1 with the minimum image
   double distance(double *r12, const double *r1, const double *r2) const {
-    double ans = 0.0;
-    for (int d = 0; d < D; ++d) {
-      r12[d] = r2[d] - r1[d];
-      if (p.periodic[d]) r12[d] -= static_cast<double>(nint(r12[d] / p.box[d])) * p.box[d];
-      ans += r12[d] * r12[d];
-    }
-    return ans;
+    return box_distance(D, p.box, p.periodic, r12, r1, r2);
   }
   // BoundingBox::updatePos(r, v, dt), Utils.hpp:561-566
-  void update_pos(double *r, const double *v, double dt) const {
-    for (int d = 0; d < D; ++d)
-      r[d] = p.periodic[d] ? std::fmod(r[d] + dt * v[d] + p.box[d], p.box[d]) : r[d] + v[d] * dt;
-  }
+  void update_pos(double *r, const double *v, double dt) const { box_update_pos(D, p.box, p.periodic, r, v, dt); }
   // BoundingBox::updatePos(r, dr), Utils.hpp:556-559
-  void update_pos(double *r, const double *dr) const {
-    for (int d = 0; d < D; ++d)
-      r[d] = p.periodic[d] ? std::fmod(r[d] + dr[d] + p.box[d], p.box[d]) : r[d] + dr[d];
-  }
+  void update_pos(double *r, const double *dr) const { box_update_pos(D, p.box, p.periodic, r, dr); }
 
   // Element pair force modulus f0 (force on i is f0 * rij with rij = rj - ri), in the
   // reference's PairForceParams::elemForce shape (MD.cuh:98-113). Laws:
@@ -706,6 +716,45 @@ void ora_observables(void *h, ora_obs *out) {
   out->vacf = v0 > 0.0 ? vv / v0 : 0.0;
   out->ndiv_total = o->ndiv_total;
   out->napo_total = o->napo_total;
+}
+
+int32_t ora_geom_nint(double a) { return nint(a); }
+
+void ora_geom_distance(int32_t dim, const double *box, const int32_t *periodic, int64_t n, const double *r1,
+                       const double *r2, double *r12, double *d2) {
+  for (int64_t i = 0; i < n; ++i)
+    d2[i] = box_distance(dim, box, periodic, r12 + i * dim, r1 + i * dim, r2 + i * dim);
+}
+
+void ora_geom_update_pos(int32_t dim, const double *box, const int32_t *periodic, int64_t n, double *r,
+                         const double *v, double dt) {
+  for (int64_t i = 0; i < n; ++i) {
+    if (dt == 0.0)
+      box_update_pos(dim, box, periodic, r + i * dim, v + i * dim);
+    else
+      box_update_pos(dim, box, periodic, r + i * dim, v + i * dim, dt);
+  }
+}
+
+int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const int32_t *periodic, int32_t n,
+                           const double *r, int32_t *ns, int32_t *head, int32_t *list, int32_t *coords,
+                           int32_t *neighbor_ids, int32_t max_bins) {
+  LinkGrid g;
+  g.init(dim, rcut, box, periodic);
+  for (int d = 0; d < 3; ++d) ns[d] = g.ns[d];
+  if (g.ncells > max_bins) return -g.ncells;
+  std::vector<int> hd, ls;
+  g.populate(r, n, hd, ls);
+  std::memcpy(head, hd.data(), sizeof(int32_t) * g.ncells);
+  if (n > 0) std::memcpy(list, ls.data(), sizeof(int32_t) * n);
+  const int nst = dim == 2 ? 5 : 14;
+  for (int b = 0; b < g.ncells; ++b) {
+    int c[3] = {0, 0, 0};
+    g.coord(b, c);
+    for (int d = 0; d < dim; ++d) coords[b * dim + d] = c[d];
+    for (int k = 0; k < nst; ++k) neighbor_ids[b * nst + k] = g.neighbor(c, dim == 2 ? kDns2d[k] : kDns3d[k]);
+  }
+  return g.ncells;
 }
 
 void ora_rng_seed(void *h, uint32_t seed) { H(h)->rng.init(seed); }

@@ -89,6 +89,25 @@ void ora_clear_events(void *h);
 void ora_obs_reset(void *h);
 void ora_observables(void *h, ora_obs *out);
 
+/* The restated box and link-list geometry on its own, for the checks against the reference's
+ * compiled Utils.hpp (golden vectors in tests/golden/geometry_golden.json):
+ *   Nint (Utils.hpp:173-175);
+ *   BoundingBox::distance over n pairs (Utils.hpp:536-544): r12[n][dim], d2[n];
+ *   BoundingBox::updatePos over n positions (Utils.hpp:556-566): dt == 0 takes v as the
+ *     displacement dr, otherwise r += dt v, both wrapped by fmod on periodic axes;
+ *   LinkListOrtho get_opt_size + init/reset + populate_list (Utils.hpp:872-1001) with
+ *     get_cellCoord and get_cellID over the half stencil (Utils.hpp:922-936, 1018-1069):
+ *     ns[3], head[nbins], list[n], coords[nbins][dim], neighbor_ids[nbins][5 or 14];
+ *     returns nbins, or -nbins when nbins > max_bins. */
+int32_t ora_geom_nint(double a);
+void ora_geom_distance(int32_t dim, const double *box, const int32_t *periodic, int64_t n, const double *r1,
+                       const double *r2, double *r12, double *d2);
+void ora_geom_update_pos(int32_t dim, const double *box, const int32_t *periodic, int64_t n, double *r,
+                         const double *v, double dt);
+int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const int32_t *periodic, int32_t n,
+                           const double *r, int32_t *ns, int32_t *head, int32_t *list, int32_t *coords,
+                           int32_t *neighbor_ids, int32_t max_bins);
+
 /* RNG access for golden-vector checks */
 void ora_rng_seed(void *h, uint32_t seed);
 double ora_rng_close_open(void *h);

@@ -4,9 +4,11 @@
 #   libref_random.so - its vendored dSFMT and Random.cpp, to cross-check the oracle's
 #                      restated RNG;
 #   libref_gsd.so    - its vendored GSD 1.0 library gsd.c, to read the files the frame writer
-#                      writes and to write the golden files it must reproduce byte for byte.
-# The rest of the reference does not build (missing Cell.hpp/MD.hpp/CIL.hpp/Units.hpp,
-# Boost, HDF5).
+#                      writes and to write the golden files it must reproduce byte for byte;
+#   libref_utils.so  - its Utils.hpp (Nint, BoundingBox, LinkListOrtho2D/3D), with
+#                      oracle/boost_shim standing in for the two Boost headers it includes, to
+#                      pin the oracle's box and link-list geometry.
+# The rest of the reference does not build (missing Cell.hpp/MD.hpp/CIL.hpp/Units.hpp, HDF5).
 set -euo pipefail
 REF=${CIL_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -16,11 +18,19 @@ if [ ! -f "$REF/mt/dSFMT.c" ] || [ ! -f "$REF/Random.hpp" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
+# where the tree was found, for the tests that read the reference's own files (oracle/refdir.py)
+(cd "$REF" && pwd) > "$OUT/reference_dir"
 gcc -O2 -fPIC -DDSFMT_MEXP=19937 -I"$REF/mt" -c "$REF/mt/dSFMT.c" -o "$OUT/dSFMT.o"
 g++ -O2 -fPIC -std=c++11 -DDSFMT_MEXP=19937 -I"$REF" -c "$REF/Random.cpp" -o "$OUT/Random.o"
 g++ -O2 -fPIC -std=c++11 -DDSFMT_MEXP=19937 -I"$REF" -c "$HERE/ref_random_shim.cpp" -o "$OUT/shim.o"
 g++ -shared -o "$OUT/libref_random.so" "$OUT/shim.o" "$OUT/Random.o" "$OUT/dSFMT.o"
 echo "built $OUT/libref_random.so"
+if [ -f "$REF/Utils.hpp" ]; then
+  # -DNDEBUG: the reference's asserts (positions inside the box) are not part of what is pinned
+  g++ -O2 -fPIC -shared -std=c++11 -DNDEBUG -ffp-contract=off -I"$HERE/boost_shim" -I"$REF" \
+      "$HERE/ref_utils_shim.cpp" -o "$OUT/libref_utils.so"
+  echo "built $OUT/libref_utils.so"
+fi
 if [ -f "$REF/gsd.c" ]; then
   gcc -O2 -fPIC -shared -I"$REF" "$REF/gsd.c" -o "$OUT/libref_gsd.so"
   echo "built $OUT/libref_gsd.so"

@@ -4,7 +4,7 @@ Runs oracle/ref_build.sh, which compiles the reference's vendored mt/dSFMT.c and
 header-only Random.hpp (Random.hpp:9-114) from the reference tree into oracle/_ref/, then
 records the outputs of those functions for a few seeds. The oracle's restated RNG and the
 library's host RNG (used in oracle mode) are checked against these files by
-tests/test_oracle_golden.py and tests/test_host_rng.py.
+tests/test_oracle.py and tests/test_abi.py.
 
 Usage: python tests/golden/make_golden.py   (needs the reference tree; not run by tests)
 """

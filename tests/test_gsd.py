@@ -16,8 +16,9 @@ sys.path.insert(0, GOLDEN)
 import gsd_sequence  # noqa: E402
 from cil_cuda_gb300.gsd import GSDFile  # noqa: E402
 from oracle import ref_gsd  # noqa: E402
+from oracle.refdir import reference_path  # noqa: E402
 
-REF_DIR = os.environ.get("CIL_REFERENCE_DIR", "/root/reference")
+REF_DIR = reference_path()
 REF_OUTPUTS = ["cil.Last.gsd", "z0.001t3.16_v2.Last.gsd"]  # final-state files shipped with the reference
 
 

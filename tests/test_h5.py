@@ -12,9 +12,10 @@ import struct
 
 import numpy as np
 import pytest
+from oracle.refdir import reference_path  # noqa: E402
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("CIL_REFERENCE_DIR", "/root/reference")
+REF = reference_path()
 SINGLE = os.path.join(ROOT, "tests", "golden", "input_single_element_2d.json")
 TWO = os.path.join(ROOT, "tests", "golden", "input_two_element_2d.json")
 RUNS = ("z0.001t3.16_v2", "cil")

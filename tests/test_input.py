@@ -16,9 +16,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 sys.path.insert(0, GOLDEN)
 
 import reference_init as R  # noqa: E402
+from oracle.refdir import reference_path  # noqa: E402
 
 FIXTURE = os.path.join(GOLDEN, "input_two_element_2d.json")
-REF_DIR = os.environ.get("CIL_REFERENCE_DIR", "/root/reference")
+REF_DIR = reference_path()
 
 
 @pytest.fixture(scope="module")

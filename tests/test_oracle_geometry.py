@@ -1,0 +1,90 @@
+"""The oracle's box and link-list geometry pinned on the reference's own code (no GPU).
+
+tests/golden/geometry_golden.json holds outputs of the reference's Utils.hpp compiled from its
+tree (tests/golden/make_geometry_golden.py): Nint (Utils.hpp:173-175), BoundingBox::distance
+and updatePos (Utils.hpp:536-566), LinkListOrtho2D/3D grid sizing, bin ids, LIFO head/link
+lists, bin coordinates and half-stencil neighbour ids (Utils.hpp:872-1069). The oracle's
+restatement (ora_geom_*, the same functions its step calls) must reproduce every value bit for
+bit. Where oracle/ref_build.sh has built the reference here, fresh random inputs are compared
+live as well."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "geometry_golden.json")
+
+
+def unhex(a):
+    return np.array([float.fromhex(x) for x in a], np.float64)
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def ora(oracle_lib):
+    from oracle import geometry as G
+    return G.oracle_geometry()
+
+
+def bits(a):
+    return np.asarray(a, np.float64).view(np.uint64)
+
+
+def test_nint_matches_reference(golden, ora):
+    a = unhex(golden["nint"]["a"])
+    np.testing.assert_array_equal(ora.nint(a), np.array(golden["nint"]["out"]))
+
+
+def test_minimum_image_distance_matches_reference(golden, ora):
+    for c in golden["distance"]:
+        dim = c["dim"]
+        r12, d2 = ora.distance(dim, unhex(c["box"]), c["periodic"], unhex(c["r1"]), unhex(c["r2"]))
+        np.testing.assert_array_equal(bits(r12.reshape(-1)), bits(unhex(c["r12"])))
+        np.testing.assert_array_equal(bits(d2), bits(unhex(c["d2"])))
+
+
+def test_position_update_and_wrap_match_reference(golden, ora):
+    for c in golden["update_pos"]:
+        dim = c["dim"]
+        out = ora.update_pos(dim, unhex(c["box"]), c["periodic"], unhex(c["r"]), unhex(c["v"]), float.fromhex(c["dt"]))
+        np.testing.assert_array_equal(bits(out.reshape(-1)), bits(unhex(c["out"])))
+
+
+def test_link_list_matches_reference(golden, ora):
+    for c in golden["link_list"]:
+        dim = c["dim"]
+        L = ora.link_list(dim, float.fromhex(c["rcut"]), unhex(c["box"]), c["periodic"], unhex(c["r"]))
+        assert L["ns"].tolist() == c["ns"]
+        np.testing.assert_array_equal(L["head"], c["head"])
+        np.testing.assert_array_equal(L["list"], c["list"])
+        np.testing.assert_array_equal(L["coords"].reshape(-1), c["coords"])
+        np.testing.assert_array_equal(L["neighbor_ids"].reshape(-1), c["neighbor_ids"])
+    # the collapsed grid is among the cases
+    assert any(c["ns"][:2] == [1, 1] for c in golden["link_list"])
+
+
+def test_live_against_reference_build(ora):
+    from oracle import geometry as G
+    ref = G.reference_geometry()
+    if ref is None:
+        pytest.skip("reference Utils.hpp not built here (oracle/ref_build.sh needs the reference tree)")
+    rng = np.random.default_rng(7)
+    for dim, box, per, rcut in ((2, np.array([61.7, 23.9]), [1, 1], 1.7), (3, np.array([14.1, 9.7, 30.3]), [1, 0, 1], 2.2)):
+        r1 = rng.uniform(0, 1, (3000, dim)) * box
+        r2 = rng.uniform(0, 1, (3000, dim)) * box
+        a = ora.distance(dim, box, per, r1, r2)
+        b = ref.distance(dim, box, per, r1, r2)
+        assert (bits(a[0]) == bits(b[0])).all() and (bits(a[1]) == bits(b[1])).all()
+        v = rng.normal(0, 30.0, r1.shape)
+        assert (bits(ora.update_pos(dim, box, per, r1, v, 1e-4)) == bits(ref.update_pos(dim, box, per, r1, v, 1e-4))).all()
+        La = ora.link_list(dim, rcut, box, per, r1)
+        Lb = ref.link_list(dim, rcut, box, per, r1)
+        for k in La:
+            np.testing.assert_array_equal(La[k], Lb[k])
