@@ -178,6 +178,43 @@ void box_update_pos(int D, const double *box, const int32_t *periodic, double *r
   for (int d = 0; d < D; ++d) r[d] = periodic[d] ? std::fmod(r[d] + dr[d] + box[d], box[d]) : r[d] + dr[d];
 }
 
+// Element pair force modulus f0 (force on i is f0 * rij with rij = rj - ri), in the
+// reference's PairForceParams::elemForce shape (MD.cuh:98-113). Laws:
+//  LJ-WCA: the reference LJ (MD.cuh:50-56), eps_ij = 24 sqrt(eps_i eps_j) (MD.cu:13),
+//          rc^2 = 2^(1/3) sigma_ij^2 (Input.cpp:296-301), inclusive cutoff.
+//  soft-core: F = eps (1 - r/rc)^2, rc = rcut_scale * sigma_ij.
+//  Hertz: F = E delta^1.5, delta = sigma_ij - r.
+bool pair_force_law(int law, double eps, double rcut_scale, double r2, double si, double sj, double &f0) {
+  const double sij = 0.5 * (si + sj);
+  f0 = 0.0;
+  if (law == ORA_FORCE_LJ_WCA) {
+    const double sij2 = sij * sij;
+    const double rc2 = sij2 * (rcut_scale * rcut_scale);
+    if (r2 <= rc2) {
+      const double ir2 = 1.0 / r2;
+      double sr2n = sij2 * ir2;
+      const double srn = sr2n * sr2n * sr2n;
+      sr2n = srn * srn;
+      f0 = (srn - 2.0 * sr2n) * ir2 * (24.0 * eps);
+      return true;
+    }
+    return false;
+  }
+  const double rc = rcut_scale * sij;
+  if (r2 < rc * rc && r2 > 0.0) {
+    const double r = std::sqrt(r2);
+    if (law == ORA_FORCE_SOFTCORE) {
+      const double w = 1.0 - r / rc;
+      f0 = -eps * w * w / r;
+    } else {
+      const double delta = sij - r;
+      f0 = -eps * delta * std::sqrt(delta) / r;
+    }
+    return true;
+  }
+  return false;
+}
+
 // Half stencils including the own bin (Utils.hpp:700-704, DNS2D / DNS3D)
 const int kDns2d[5][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {-1, 1, 0}};
 const int kDns3d[14][3] = {{0, 0, 0},  {1, 0, 0},  {1, 1, 0},   {0, 1, 0},  {-1, 1, 0},
@@ -216,41 +253,8 @@ struct Oracle {
   // BoundingBox::updatePos(r, dr), Utils.hpp:556-559
   void update_pos(double *r, const double *dr) const { box_update_pos(D, p.box, p.periodic, r, dr); }
 
-  // Element pair force modulus f0 (force on i is f0 * rij with rij = rj - ri), in the
-  // reference's PairForceParams::elemForce shape (MD.cuh:98-113). Laws:
-  //  LJ-WCA: the reference LJ (MD.cuh:50-56), eps_ij = 24 sqrt(eps_i eps_j) (MD.cu:13),
-  //          rc^2 = 2^(1/3) sigma_ij^2 (Input.cpp:296-301), inclusive cutoff.
-  //  soft-core: F = eps (1 - r/rc)^2, rc = rcut_scale * sigma_ij.
-  //  Hertz: F = E delta^1.5, delta = sigma_ij - r.
   bool elem_force(double r2, double si, double sj, double &f0) const {
-    const double sij = 0.5 * (si + sj);
-    f0 = 0.0;
-    if (p.force_law == ORA_FORCE_LJ_WCA) {
-      const double sij2 = sij * sij;
-      const double rc2 = sij2 * (p.rcut_scale * p.rcut_scale);
-      if (r2 <= rc2) {
-        const double ir2 = 1.0 / r2;
-        double sr2n = sij2 * ir2;
-        const double srn = sr2n * sr2n * sr2n;
-        sr2n = srn * srn;
-        f0 = (srn - 2.0 * sr2n) * ir2 * (24.0 * p.epsilon);
-        return true;
-      }
-      return false;
-    }
-    const double rc = p.rcut_scale * sij;
-    if (r2 < rc * rc && r2 > 0.0) {
-      const double r = std::sqrt(r2);
-      if (p.force_law == ORA_FORCE_SOFTCORE) {
-        const double w = 1.0 - r / rc;
-        f0 = -p.epsilon * w * w / r;
-      } else {
-        const double delta = sij - r;
-        f0 = -p.epsilon * delta * std::sqrt(delta) / r;
-      }
-      return true;
-    }
-    return false;
+    return pair_force_law(p.force_law, p.epsilon, p.rcut_scale, r2, si, sj, f0);
   }
 
   // Rest length of the intra-cell spring at step ts (linear growth over the cell cycle).
@@ -755,6 +759,11 @@ int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const in
     for (int k = 0; k < nst; ++k) neighbor_ids[b * nst + k] = g.neighbor(c, dim == 2 ? kDns2d[k] : kDns3d[k]);
   }
   return g.ncells;
+}
+
+void ora_geom_pair_force(int32_t law, double eps, double rcut_scale, int64_t n, const double *r2, const double *si,
+                         const double *sj, double *f0, int32_t *inside) {
+  for (int64_t k = 0; k < n; ++k) inside[k] = pair_force_law(law, eps, rcut_scale, r2[k], si[k], sj[k], f0[k]) ? 1 : 0;
 }
 
 void ora_rng_seed(void *h, uint32_t seed) { H(h)->rng.init(seed); }

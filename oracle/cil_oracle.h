@@ -7,11 +7,15 @@
  *
  * Pinning: the random-number layer (dSFMT-19937, Leva normals, onDSphere, uniform
  * variants) is pinned bit-for-bit against the reference's own mt/dSFMT.c + Random.hpp
- * (golden vectors in tests/golden/). The reference ships no tests, fixtures or outputs of
- * this physics, and its step does not compile, so the force laws, binning, division and
- * apoptosis are "parity unpinned": they are restated from the reference source (cited per
- * function in cil_oracle.cpp) with the benchmark workloads' force laws slotted into the reference's
- * PairForceParams / intraCellForce extension points.
+ * (golden vectors in tests/golden/dsfmt_random_golden.json). The box and link-list geometry
+ * (Nint, minimum image, the fmod wrap of updatePos, grid sizing, bin ids, LIFO lists, bin
+ * coordinates, half-stencil neighbours) and the Lennard-Jones law are pinned bit for bit
+ * against the reference's Utils.hpp and MD.cuh compiled from its tree
+ * (tests/golden/geometry_golden.json). The reference's step itself does not compile and ships
+ * no fixtures, so the soft-core and Hertz laws of the benchmark workloads (which have no
+ * reference counterpart), the cell-cell force assembly, division and apoptosis remain
+ * restated from the reference source (cited per function in cil_oracle.cpp) without a
+ * reference-produced number: "parity unpinned" for those parts.
  */
 #ifndef CIL_ORACLE_H
 #define CIL_ORACLE_H
@@ -98,7 +102,9 @@ void ora_observables(void *h, ora_obs *out);
  *   LinkListOrtho get_opt_size + init/reset + populate_list (Utils.hpp:872-1001) with
  *     get_cellCoord and get_cellID over the half stencil (Utils.hpp:922-936, 1018-1069):
  *     ns[3], head[nbins], list[n], coords[nbins][dim], neighbor_ids[nbins][5 or 14];
- *     returns nbins, or -nbins when nbins > max_bins. */
+ *     returns nbins, or -nbins when nbins > max_bins;
+ *   the element pair force modulus of a law (the one the step uses) for n (r2, si, sj):
+ *     f0[n] and inside[n] (PairForceParams::elemForce's value and return, MD.cuh:98-113). */
 int32_t ora_geom_nint(double a);
 void ora_geom_distance(int32_t dim, const double *box, const int32_t *periodic, int64_t n, const double *r1,
                        const double *r2, double *r12, double *d2);
@@ -107,6 +113,8 @@ void ora_geom_update_pos(int32_t dim, const double *box, const int32_t *periodic
 int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const int32_t *periodic, int32_t n,
                            const double *r, int32_t *ns, int32_t *head, int32_t *list, int32_t *coords,
                            int32_t *neighbor_ids, int32_t max_bins);
+void ora_geom_pair_force(int32_t law, double eps, double rcut_scale, int64_t n, const double *r2, const double *si,
+                         const double *sj, double *f0, int32_t *inside);
 
 /* RNG access for golden-vector checks */
 void ora_rng_seed(void *h, uint32_t seed);

@@ -1,12 +1,15 @@
 """ORACLE — test infrastructure only: numpy calls over the box and link-list geometry.
 
-Two libraries export the same five C signatures:
+Two libraries export the same C signatures:
   * the oracle's restatement (oracle/_build/liboracle.so, ora_geom_*);
   * the reference's own Utils.hpp compiled by oracle/ref_build.sh
     (oracle/_ref/libref_utils.so, ref_*): Nint (Utils.hpp:173-175), BoundingBox::distance /
     updatePos (Utils.hpp:536-566), LinkListOrtho2D/3D (Utils.hpp:872-1069).
 Geometry(lib, prefix) wraps either, so the golden vectors the reference produces
-(tests/golden/make_geometry_golden.py) and the oracle's outputs go through one code path."""
+(tests/golden/make_geometry_golden.py) and the oracle's outputs go through one code path.
+The Lennard-Jones element force has one wrapper per side: lj_force_oracle (the oracle's law
+table, ora_geom_pair_force) and lj_force_reference (the reference's LJParams::elemForce,
+MD.cuh:98-113, in oracle/_ref/libref_force.so)."""
 import ctypes as C
 import os
 
@@ -79,6 +82,39 @@ class Geometry:
             raise ValueError(f"{-nb} bins exceed max_bins={max_bins}")
         return dict(ns=ns, head=head[:nb].copy(), list=lst[:n].copy(), coords=coords[: nb * dim].reshape(nb, dim),
                     neighbor_ids=nbr[: nb * nst].reshape(nb, nst))
+
+
+def lj_force_oracle(eps, rcut_scale, r2, si, sj):
+    from oracle import oracle as O
+    L = O.lib()
+    f = L.ora_geom_pair_force
+    f.restype = None
+    f.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    f(0, float(eps), float(rcut_scale), r2.size, _dp(r2), _dp(si), _dp(sj), _dp(f0), _ip(inside))
+    return f0, inside
+
+
+REF_FORCE = os.path.join(HERE, "_ref", "libref_force.so")
+
+
+def lj_force_reference(eps, r2, si, sj):
+    """The reference's LJParams::elemForce with its WCA cutoff (pow(2, 1/3), Input.cpp:296-301),
+    or None when oracle/ref_build.sh has not built it here."""
+    if not os.path.exists(REF_FORCE):
+        return None
+    L = C.CDLL(REF_FORCE)
+    L.ref_lj_wca_rc2.restype = C.c_double
+    f = L.ref_lj_force
+    f.restype = None
+    f.argtypes = [C.c_double, C.c_double, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    f(float(eps), L.ref_lj_wca_rc2(), r2.size, _dp(r2), _dp(si), _dp(sj), _dp(f0), _ip(inside))
+    return f0, inside
 
 
 def oracle_geometry():

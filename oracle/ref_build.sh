@@ -7,8 +7,11 @@
 #                      writes and to write the golden files it must reproduce byte for byte;
 #   libref_utils.so  - its Utils.hpp (Nint, BoundingBox, LinkListOrtho2D/3D), with
 #                      oracle/boost_shim standing in for the two Boost headers it includes, to
-#                      pin the oracle's box and link-list geometry.
-# The rest of the reference does not build (missing Cell.hpp/MD.hpp/CIL.hpp/Units.hpp, HDF5).
+#                      pin the oracle's box and link-list geometry;
+#   libref_force.so  - its MD.cuh Lennard-Jones law (LJParams::elemForce) compiled as host C++
+#                      with the stand-ins of oracle/ref_stubs for the headers its tree lacks, to
+#                      pin the oracle's LJ force.
+# The rest of the reference does not build (its .cu files, the missing CIL.hpp, HDF5).
 set -euo pipefail
 REF=${CIL_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -30,6 +33,12 @@ if [ -f "$REF/Utils.hpp" ]; then
   g++ -O2 -fPIC -shared -std=c++11 -DNDEBUG -ffp-contract=off -I"$HERE/boost_shim" -I"$REF" \
       "$HERE/ref_utils_shim.cpp" -o "$OUT/libref_utils.so"
   echo "built $OUT/libref_utils.so"
+fi
+if [ -f "$REF/MD.cuh" ]; then
+  g++ -O2 -fPIC -shared -std=c++14 -DNDEBUG -ffp-contract=off -D__host__= -D__device__= -D__global__= \
+      -DSIMIO_HPP -I"$HERE/ref_stubs" -I"$HERE/boost_shim" -I"$REF" -w \
+      "$HERE/ref_force_shim.cpp" -o "$OUT/libref_force.so"
+  echo "built $OUT/libref_force.so"
 fi
 if [ -f "$REF/gsd.c" ]; then
   gcc -O2 -fPIC -shared -I"$REF" "$REF/gsd.c" -o "$OUT/libref_gsd.so"

@@ -1,4 +1,5 @@
-"""Generates tests/golden/geometry_golden.json from the reference's own box and link-list code.
+"""Generates tests/golden/geometry_golden.json from the reference's own box, link-list and
+Lennard-Jones code.
 
 Runs oracle/ref_build.sh, which compiles the reference's Utils.hpp (Nint, Utils.hpp:173-175;
 BoundingBox::distance and updatePos, Utils.hpp:536-566; LinkListOrtho2D/3D get_opt_size,
@@ -7,7 +8,10 @@ tree into oracle/_ref/libref_utils.so, with oracle/boost_shim standing in for th
 headers, then records its outputs on seeded inputs and edge cases: half-integer and near-half
 ratios for Nint, separations of exactly half a box and just around it, positions at 0 and just
 below L, displacements that wrap once either way, bin boundaries, grids that collapse to one
-bin, open and periodic axes in 2D and 3D. Doubles are stored as hex strings (bit-exact).
+bin, open and periodic axes in 2D and 3D. It also records the reference's LJParams::elemForce
+(MD.cuh:50-56, 98-113; compiled by the same recipe into oracle/_ref/libref_force.so) with its
+WCA cutoff, at three well depths, on polydisperse pairs and at the cutoff and one ulp around it.
+Doubles are stored as hex strings (bit-exact).
 tests/test_oracle_geometry.py checks the oracle's restatement (ora_geom_*) against this file.
 
 Usage: python tests/golden/make_geometry_golden.py   (needs the reference tree; not run by tests)
@@ -95,6 +99,20 @@ def link_cases(rng):
     return cases
 
 
+def lj_inputs(rng):
+    n = 400
+    si = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sj = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sij2 = (0.5 * (si + sj)) ** 2
+    r2 = sij2 * rng.uniform(0.55, 1.4, n)
+    # exactly at the WCA cutoff and one ulp either side (the cutoff is inclusive)
+    rc2 = sij2[:40] * (2.0 ** (1.0 / 3.0))
+    r2 = np.concatenate([r2, rc2, np.nextafter(rc2, 0), np.nextafter(rc2, np.inf)])
+    si = np.concatenate([si, si[:40], si[:40], si[:40]])
+    sj = np.concatenate([sj, sj[:40], sj[:40], sj[:40]])
+    return r2, si, sj
+
+
 def main():
     subprocess.run(["bash", os.path.join(ROOT, "oracle", "ref_build.sh")], check=True)
     from oracle import geometry as G
@@ -120,6 +138,12 @@ def main():
                                      head=L["head"].tolist(), list=L["list"].tolist(),
                                      coords=L["coords"].reshape(-1).tolist(),
                                      neighbor_ids=L["neighbor_ids"].reshape(-1).tolist()))
+    out["lj_force"] = []
+    r2, si, sj = lj_inputs(rng)
+    for eps in (1.0, 0.37, 5.0):
+        f0, inside = G.lj_force_reference(eps, r2, si, sj)
+        out["lj_force"].append(dict(eps=float(eps).hex(), r2=hexs(r2), si=hexs(si), sj=hexs(sj), f0=hexs(f0),
+                                    inside=inside.tolist()))
     path = os.path.join(HERE, "geometry_golden.json")
     with open(path, "w") as f:
         json.dump(out, f, separators=(",", ":"))

@@ -3,9 +3,10 @@
 tests/golden/geometry_golden.json holds outputs of the reference's Utils.hpp compiled from its
 tree (tests/golden/make_geometry_golden.py): Nint (Utils.hpp:173-175), BoundingBox::distance
 and updatePos (Utils.hpp:536-566), LinkListOrtho2D/3D grid sizing, bin ids, LIFO head/link
-lists, bin coordinates and half-stencil neighbour ids (Utils.hpp:872-1069). The oracle's
-restatement (ora_geom_*, the same functions its step calls) must reproduce every value bit for
-bit. Where oracle/ref_build.sh has built the reference here, fresh random inputs are compared
+lists, bin coordinates and half-stencil neighbour ids (Utils.hpp:872-1069), and of its
+Lennard-Jones element force LJParams::elemForce with the WCA cutoff (MD.cuh:50-56, 98-113;
+Input.cpp:296-301). The oracle's restatement (ora_geom_*, the same functions its step calls)
+must reproduce every value bit for bit. Where oracle/ref_build.sh has built the reference here, fresh random inputs are compared
 live as well."""
 import json
 import os
@@ -70,6 +71,17 @@ def test_link_list_matches_reference(golden, ora):
     assert any(c["ns"][:2] == [1, 1] for c in golden["link_list"])
 
 
+def test_lj_force_matches_reference(golden):
+    from oracle import geometry as G
+    assert len(golden["lj_force"]) == 3
+    for c in golden["lj_force"]:
+        f0, inside = G.lj_force_oracle(float.fromhex(c["eps"]), 2 ** (1 / 6), unhex(c["r2"]), unhex(c["si"]),
+                                       unhex(c["sj"]))
+        np.testing.assert_array_equal(inside, c["inside"])
+        np.testing.assert_array_equal(bits(f0), bits(unhex(c["f0"])))
+        assert 0 < np.sum(inside) < len(inside)
+
+
 def test_live_against_reference_build(ora):
     from oracle import geometry as G
     ref = G.reference_geometry()
@@ -88,3 +100,10 @@ def test_live_against_reference_build(ora):
         Lb = ref.link_list(dim, rcut, box, per, r1)
         for k in La:
             np.testing.assert_array_equal(La[k], Lb[k])
+    si = rng.uniform(0.7, 1.3, 5000)
+    sj = rng.uniform(0.7, 1.3, 5000)
+    r2 = (0.5 * (si + sj)) ** 2 * rng.uniform(0.5, 1.3, 5000)
+    a = G.lj_force_oracle(1.0, 2 ** (1 / 6), r2, si, sj)
+    b = G.lj_force_reference(1.0, r2, si, sj)
+    assert b is not None
+    assert (bits(a[0]) == bits(b[0])).all() and (a[1] == b[1]).all()
