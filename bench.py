@@ -547,6 +547,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 256-colony leg")
     ap.add_argument("--no-frames", action="store_true", help="skip the frame-output leg")
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
+    ap.add_argument("--staging", type=int, default=0, help="profile: list entries in flight (0: default)")
+    ap.add_argument("--occupancy", type=int, default=0, help="profile: CTAs per SM of the list kernel (0: default)")
     ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd", "profile"],
                     default=None, help="run one form only (profiling); profile: the headline form alone, "
                                        "launched step by step, nothing else")
@@ -579,8 +581,9 @@ def main():
     hbm, peak_kind = peaks()
     if args.only == "profile":
         from cil_cuda_gb300 import skin_scheduler as SS
+        tune = {"staging": args.staging, "occupancy": args.occupancy}
         r = run_form(G, p, st, G.PREC_MIXED, args.steps, args.warmup, device, 7 + rank, dist, skin=SS.load()[2],
-                     sched=True, graphs=False)
+                     sched=True, graphs=False, tune=tune)
         print(json.dumps({"profile_run": {"ms_per_step": r["dev_s"] / args.steps * 1e3, "timings": r["timings"],
                                           "skin": r["skin"]}}))
         return 0

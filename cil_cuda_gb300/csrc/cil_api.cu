@@ -69,7 +69,8 @@ struct cil_handle {
   int grid_slots = 0;  // persistent grid for slot kernels
   int grid_cells = 0;
   int grid_force = 0;
-  int stiles = 0;      // tiles over the slot capacity (grid of the list force kernel)
+  int stiles = 0;      // tiles over the slot capacity
+  int ptiles = 0;      // tiles over the slot pairs of the capacity (grid of the list force kernel)
   int list_variant = 0;  // list force kernel: staging depth and CTAs per SM (cil_config.staging/occupancy)
   int nsm = 0;
   bool geometry_ready = false;
@@ -121,6 +122,7 @@ struct cil_handle {
   int *d_slot_of = nullptr;
   int *d_t0 = nullptr, *d_tsw = nullptr;
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
+  int *d_tiles_pairs = nullptr;  // skin mode: tiles over slot pairs (the cell-major force kernel)
   int *d_tile_count = nullptr, *d_tile_off = nullptr;
   int *d_dead = nullptr;
   int *d_divq = nullptr;  // division queue [CC]
@@ -164,7 +166,7 @@ void free_all(cil_handle *h) {
                   h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
                   h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
-                  h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live,
+                  h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live, h->d_tiles_pairs,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_divq, h->d_obs,
                   h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
   for (void *p : ptrs)
@@ -288,6 +290,7 @@ RebuildArgs rebuild_args(cil_handle *h) {
   a.SS = h->SS;
   a.tiles_used = h->d_tiles_used;
   a.tiles_live = h->d_tiles_live;
+  a.tiles_cell = h->d_tiles_cell;
   a.scan_col = h->d_scan_col;
   a.nscan = h->nscan;
   const bool mixed = h->cfg.precision == CIL_PREC_MIXED;
@@ -356,6 +359,25 @@ cil_status do_rebuild(cil_handle *h, bool carry_vel = false, bool exact = false,
   return CIL_OK;
 }
 
+// Skin mode's slot re-sort: cells ranked by the bin of their back element, each cell's
+// elements moved into a slot pair (cell-major slots, the layout k_force_cells reads), tombstones
+// dropped. Re-anchors the FP32 records on the FP64 positions after an upload and every 32 steps,
+// like the permuting rebuild.
+cil_status do_cell_resort(cil_handle *h) {
+  RebuildArgs a = rebuild_args(h);
+  a.skin = nullptr;
+  a.any_rebuild = nullptr;
+  a.permute = 0;
+  launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
+  launch_cell_resort(a, h->grid_cells, h->stream);
+  h->cur = 1 - h->cur;
+  h->meta = 1 - h->meta;
+  h->pu = 1 - h->pu;
+  h->need_exact = false;
+  h->lists_stale = true;
+  return CIL_OK;
+}
+
 ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, double *frc) {
   ForceArgs a{};
   a.col = h->d_col;
@@ -370,7 +392,7 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
   a.pk = h->d_pk[h->pu];
   a.pk_next = h->d_pk[1 - h->pu];
   if (h->skin_mode) {
-    a.tiles = h->d_tiles_used;
+    a.tiles = h->d_tiles_pairs;
     a.skin = h->d_skin;
     a.nbr = h->d_nbr;
     a.ncnt = h->d_ncnt;
@@ -678,25 +700,24 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
         h->need_exact || h->lists_stale || (first && (h->ts % h->permute_period) == 0);
     launch_skin_begin(skin_args(h, permute ? 1 : 0), h->stream);
     if (permute) {
-      st = do_rebuild(h);
+      // cell-major re-sort; every colony then rebuilds its bin index and lists (host request)
+      st = do_cell_resort(h);
       if (st != CIL_OK) return st;
-      // the re-sort compacted the slots: tile tables for the list build
-      launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
-    } else {
-      launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream);
-      launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
-      RebuildArgs ra = rebuild_args(h);
-      ra.permute = 0;
-      ra.skin = h->d_skin;  // only colonies with rebuild_now
-      ra.any_rebuild = h->d_anyreb;
-      ra.ts_dev = h->d_ts;
-      ra.state_out = nullptr;
-      launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
     }
+    // tile tables over the slots (list build) and the slot pairs (force kernel)
+    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs);
+    launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
+    RebuildArgs ra = rebuild_args(h);
+    ra.permute = 0;
+    ra.skin = h->d_skin;  // only colonies with rebuild_now
+    ra.any_rebuild = h->d_anyreb;
+    ra.ts_dev = h->d_ts;
+    ra.state_out = nullptr;
+    launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
     launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
-    h->launches += permute ? 15 : 8;
+    h->launches += permute ? 17 : 8;
   } else {
     // the second half step of a Heun step reads the first half's velocities: carried through
     // the re-sort (only when velocities are written, i.e. the last step of a cil_step call)
@@ -723,7 +744,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
   if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
   fa.heun = heun;
-  launch_force_list(fa, h->D, h->cfg.force_law, h->stiles, h->list_variant, h->stream);  // skin mode
+  launch_force_list(fa, h->D, h->cfg.force_law, h->ptiles, h->list_variant, h->stream);  // skin mode
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
   return CIL_OK;
@@ -874,11 +895,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->integrator != CIL_INTEGRATOR_EULER && cfg->integrator != CIL_INTEGRATOR_HEUN) return CIL_ERR_CONFIG;
   int list_variant = -1;
   {
-    const int st = cfg->staging == 0 ? 4 : cfg->staging, oc = cfg->occupancy == 0 ? 4 : cfg->occupancy;
-    if (st == 4 && oc == 4) list_variant = 0;
-    if (st == 2 && oc == 4) list_variant = 1;
-    if (st == 8 && oc == 3) list_variant = 2;
-    if (st == 8 && oc == 2) list_variant = 3;
+    const int st = cfg->staging == 0 ? 4 : cfg->staging, oc = cfg->occupancy == 0 ? 2 : cfg->occupancy;
+    if (st == 4 && oc == 2) list_variant = 0;
+    if (st == 2 && oc == 3) list_variant = 1;
+    if (st == 1 && oc == 3) list_variant = 2;
+    if (st == 2 && oc == 2) list_variant = 3;
     if (list_variant < 0) return CIL_ERR_CONFIG;
   }
   auto *h = new cil_handle();
@@ -1039,10 +1060,13 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_tiles_used = dalloc<int>(h->B + 1);
   h->d_tiles_live = dalloc<int>(h->B + 1);
   h->d_tiles_cell = dalloc<int>(h->B + 1);
+  h->d_tiles_pairs = dalloc<int>(h->B + 1);
   h->ctiles = 0;
   for (int c = 0; c < h->B; ++c) h->ctiles += (h->hc[c].cap + kTile - 1) / kTile;
   h->stiles = 0;
   for (int c = 0; c < h->B; ++c) h->stiles += (h->cc[c].slot_cap + kTile - 1) / kTile;
+  h->ptiles = 0;
+  for (int c = 0; c < h->B; ++c) h->ptiles += (h->cc[c].slot_cap + 2 * kTile - 1) / (2 * kTile);
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
@@ -1050,6 +1074,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_eid[0] && h->d_eid[1] && h->d_sbin[0] &&
             h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
             h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
+            h->d_tiles_pairs &&
             h->d_tile_count && h->d_tile_off && h->d_dead && h->d_divq && h->d_ts &&
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
             skin_ok;

@@ -45,25 +45,37 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
   return base + inc - v;
 }
 
-// tiles[c] = sum over colonies < c of ceil(count_c / kTile); tiles[B] = total.
-// which: 0 = nslot, 1 = nlive, 2 = ncell
-__global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which,
-                        int *__restrict__ tiles) {
-  int carry = 0;
+// tiles[c] = sum over colonies < c of ceil(count_c / per); tiles[B] = total.
+// which: 0 = nslot (per kTile), 1 = nlive (kTile), 2 = ncell (kCellTile), 3 = nslot in slot
+// pairs (2 kTile: the cell-major force kernel, one thread per pair). A second table (which2,
+// tiles2) can be written by the same launch.
+__device__ __forceinline__ int tile_count(const ColonyCounters &k, int which) {
+  const int n = which == 1 ? k.nlive : (which == 2 ? k.ncell : k.nslot);
+  const int per = which == 2 ? kCellTile : (which == 3 ? 2 * kTile : kTile);
+  return (n + per - 1) / per;
+}
+
+__global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which, int *__restrict__ tiles,
+                        int which2, int *__restrict__ tiles2) {
+  int carry = 0, carry2 = 0;
   for (int base = 0; base < B; base += kTile) {
     const int c = base + threadIdx.x;
-    int v = 0;
-    if (c < B) {
-      const int n = which == 0 ? cnt[c].nslot : (which == 1 ? cnt[c].nlive : cnt[c].ncell);
-      const int per = which == 2 ? kCellTile : kTile;
-      v = (n + per - 1) / per;
-    }
-    int total;
+    const int v = c < B ? tile_count(cnt[c], which) : 0;
+    const int v2 = (tiles2 && c < B) ? tile_count(cnt[c], which2) : 0;
+    int total, total2;
     const int ex = block_excl_scan(v, &total);
-    if (c < B) tiles[c] = carry + ex;
+    const int ex2 = block_excl_scan(v2, &total2);
+    if (c < B) {
+      tiles[c] = carry + ex;
+      if (tiles2) tiles2[c] = carry2 + ex2;
+    }
     carry += total;
+    carry2 += total2;
   }
-  if (threadIdx.x == 0) tiles[B] = carry;
+  if (threadIdx.x == 0) {
+    tiles[B] = carry;
+    if (tiles2) tiles2[B] = carry2;
+  }
 }
 
 // New bin of a slot in the mixed form from FP32 data only: the home bin plus the whole
@@ -316,11 +328,139 @@ __global__ void __launch_bounds__(kTile) k_clear_tail_keys(RebuildArgs a) {
     if (i < C.slot_cap) a.key[C.slot_base + i] = -1;
 }
 
+// ---------------------------------------------------------------- cell-major slot re-sort
+// Skin mode re-sorts its slots by cell: cells are ranked by the bin of their back element (a
+// counting sort over the same bins and scan kernels), and the two elements of the cell of rank
+// r move into the slot pair (slot_base + 2 r, + 1), back element first. Tombstones are dropped
+// (nslot = 2 ncell). Each element keeps its own home bin, so the Verlet lists (built next from
+// the element bins) do not depend on the slot order; only the force kernel, one thread per slot
+// pair, does.
+
+// cell c-local index i of thread (tile t, item q) over tiles_cell
+__device__ __forceinline__ int cell_of(const RebuildArgs &a, int t, int c, int q) {
+  return (t - a.tiles_cell[c]) * kCellTile + q * kTile + threadIdx.x;
+}
+
+template <int D>
+__device__ __forceinline__ int cell_bin(const RebuildArgs &a, const ColonyConst &C, int s) {
+  int b[D];
+  if (a.exact) {
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[d] = a.x_in[d * a.SS + s];
+    bin_coords<D>(C, x, b);
+  } else {
+    int sh[D];
+    fast_bin<D>(C, a.sbin_in[s], a.pk_in[s], b, sh);
+  }
+  return bin_id<D>(C, b);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_cell_keys(RebuildArgs a) {
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int n = a.cnt[c].ncell;
+#pragma unroll
+    for (int q = 0; q < kCellItems; ++q) {
+      const int i = cell_of(a, t, c, q);
+      if (i >= n) continue;
+      const int g = C.cell_base + i;
+      const int k = C.bin_base + cell_bin<D>(a, C, a.slot_of[2 * g]);
+      a.key[g] = k;
+      atomicAdd(a.bcount + k, 1);
+    }
+  }
+}
+
+// rank of every cell inside its bin's range (bcount counts back down to zero); perm[slot_base
+// + rank] = cell
+__global__ void __launch_bounds__(kTile) k_cell_scatter(RebuildArgs a) {
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int n = a.cnt[c].ncell;
+#pragma unroll
+    for (int q = 0; q < kCellItems; ++q) {
+      const int i = cell_of(a, t, c, q);
+      if (i >= n) continue;
+      const int g = C.cell_base + i;
+      const int k = a.key[g];
+      const int pos = a.range[k].x + atomicSub(a.bcount + k, 1) - 1;  // slot_base + rank
+      a.perm[pos] = static_cast<unsigned long long>(static_cast<uint32_t>(g));
+    }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTile) k_cell_gather(RebuildArgs a) {
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    const int n = a.cnt[c].ncell;
+#pragma unroll
+    for (int q = 0; q < kCellItems; ++q) {
+      const int r = cell_of(a, t, c, q);
+      if (r >= n) continue;
+      const int g = static_cast<int>(a.perm[C.slot_base + r] & 0xffffffffu);
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int e = 2 * g + j;
+        const int src = a.slot_of[e];
+        const int dst = C.slot_base + 2 * r + j;
+        double x[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          x[d] = a.x_in[d * a.SS + src];
+          a.x_out[d * a.SS + dst] = x[d];
+        }
+        if (a.vel_out) {
+#pragma unroll
+          for (int d = 0; d < D; ++d) a.vel_out[d * a.SS + dst] = a.vel_in[d * a.SS + src];
+        }
+        a.eid_out[dst] = e;
+        a.slot_of[e] = dst;
+        a.state_out[dst] = kSlotNormal;
+        if (a.sig_out) a.sig_out[dst] = a.sig_in[src];
+        int b[D];
+        float4 p;
+        if (a.exact) {
+          // re-anchored on the FP64 position: home bin and local coordinate from x
+          a.cyc_out[dst] = make_int2(a.t0c[g], a.tswc[g]);
+          bin_coords<D>(C, x, b);
+          p = make_float4(0.0f, 0.0f, 0.0f, static_cast<float>(a.sigma_c[e]));
+#pragma unroll
+          for (int d = 0; d < D; ++d) pk_set(p, d, static_cast<float>(x[d] - static_cast<double>(b[d]) * C.bw[d]));
+        } else {
+          a.cyc_out[dst] = a.cyc_in[src];
+          int sh[D];
+          const float4 qv = a.pk_in[src];
+          fast_bin<D>(C, a.sbin_in[src], qv, b, sh);
+          p = make_float4(0.0f, 0.0f, 0.0f, fabsf(qv.w));  // every element is normal after a re-sort
+#pragma unroll
+          for (int d = 0; d < D; ++d) pk_set(p, d, pk_c(qv, d) - static_cast<float>(sh[d]) * C.bwf[d]);
+        }
+        a.pk_out[dst] = p;
+        a.sbin_out[dst] = bin_id<D>(C, b);
+      }
+    }
+  }
+}
+
+// per colony: the slot pairs in use after the re-sort
+__global__ void k_cell_finish(RebuildArgs a) {
+  for (int c = threadIdx.x; c < a.B; c += blockDim.x) a.cnt[c].nslot = 2 * a.cnt[c].ncell;
+}
+
 }  // namespace
 
 void launch_tiles(const ColonyConst *, ColonyCounters *cnt, int B, int which, int *tiles,
-                  cudaStream_t s) {
-  k_tiles<<<1, kTile, 0, s>>>(cnt, B, which, tiles);
+                  cudaStream_t s, int which2, int *tiles2) {
+  k_tiles<<<1, kTile, 0, s>>>(cnt, B, which, tiles, which2, tiles2);
 }
 
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
@@ -340,11 +480,27 @@ void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
   if (!a.permute) return;  // the bin index (range + perm) is all a list rebuild needs
   if (a.skin == nullptr)   // bin order by element id: deterministic sums (FP64 / plain forms)
     k_sort_bins<<<(a.nscan * kScanItems + kTile - 1) / kTile, kTile, 0, s>>>(a, a.nscan * kScanItems);
-  k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live));
+  k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live), 0, nullptr);
   if (a.dim == 2)
     k_gather<2><<<grid_slots, kTile, 0, s>>>(a);
   else
     k_gather<3><<<grid_slots, kTile, 0, s>>>(a);
+}
+
+void launch_cell_resort(const RebuildArgs &a, int grid_cells, cudaStream_t s) {
+  if (a.dim == 2)
+    k_cell_keys<2><<<grid_cells, kTile, 0, s>>>(a);
+  else
+    k_cell_keys<3><<<grid_cells, kTile, 0, s>>>(a);
+  k_scan_partial<<<a.nscan, kTile, 0, s>>>(a);
+  k_scan_colony<<<a.B, kTile, 0, s>>>(a);
+  k_scan_final<<<a.nscan, kTile, 0, s>>>(a);
+  k_cell_scatter<<<grid_cells, kTile, 0, s>>>(a);
+  if (a.dim == 2)
+    k_cell_gather<2><<<grid_cells, kTile, 0, s>>>(a);
+  else
+    k_cell_gather<3><<<grid_cells, kTile, 0, s>>>(a);
+  k_cell_finish<<<1, kTile, 0, s>>>(a);
 }
 
 }  // namespace cil

@@ -131,9 +131,8 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
 #pragma unroll
       for (int d = 0; d < D; ++d) F[d] += C.zeta[j] * a.noise[base + d];
     } else if (a.noise_mode == 1) {
-      const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
       uint32_t w[4];
-      noise_words<D>(id, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
+      noise_words<D>(e, C.noise_per_cell, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
       float n[4];
       box_muller(w[0], w[1], n[0], n[1]);
       if (D == 3) box_muller(w[2], w[3], n[2], n[3]);
@@ -289,9 +288,8 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
   }
   if (a.noise_mode == 1) {
     // Box-Muller with the fast log / sincos
-    const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
     uint32_t w[4];
-    noise_words<D>(id, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
+    noise_words<D>(e, C.noise_per_cell, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
     const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
     for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -333,18 +331,19 @@ __device__ __forceinline__ void mixed_integrate(const ForceArgs &a, const Colony
   for (int d = 0; d < D; ++d) {
     const float dxf = temp * F[d];
     double xn = a.x_in[d * a.SS + s] + f2d_exact(dxf);
-    long long xb = __double_as_longlong(xn);
+    const long long xb = __double_as_longlong(xn);
     const long long lb = __double_as_longlong(C.box[d]);
+    const bool lo = xb < 0, hi = xb >= lb;
     if (C.periodic[d]) {
       // non-negative doubles order like their bit patterns: wrap tests without FP64
-      // compares; a tiny negative x + L that rounds to L ends at 0 like fmod(x + L, L)
-      if (xb < 0) {
-        xn = (xb & 0x7fffffffffffffffll) ? xn + C.box[d] : 0.0;
-        xb = __double_as_longlong(xn);
+      // compares; a tiny negative x + L that rounds to L ends at 0 like fmod(x + L, L). The
+      // wrap runs only in warps where some element crossed 0 or L.
+      if (__any_sync(__activemask(), lo || hi)) {
+        if (lo) xn = (xb & 0x7fffffffffffffffll) ? xn + C.box[d] : 0.0;
+        if (__double_as_longlong(xn) >= lb) xn -= C.box[d];
       }
-      if (xb >= lb) xn -= C.box[d];
     } else {
-      inside = inside && xb >= 0 && xb < lb;
+      inside = inside && !lo && !hi;
     }
     a.x_out[d * a.SS + s] = xn;
     pk_set(pn, d, ui[d] + dxf);
@@ -708,9 +707,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
     }
     // ---- passive noise
     if (a.noise_mode == 1) {
-      const uint32_t id = static_cast<uint32_t>(C.noise_per_cell ? g : e);
       uint32_t w[4];
-      noise_words<D>(id, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w);
+      noise_words<D>(e, C.noise_per_cell, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w);
       const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
       for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -856,17 +854,355 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
   }
 }
 
+// Skin-mode step over cell-major slots, one thread per cell. Between slot re-sorts a cell's
+// two elements sit in adjacent slots, back element first (s0 = slot_base + 2 p, s1 = s0 + 1):
+// the re-sort ranks cells, division appends daughters as slot pairs, apoptosis leaves pairs of
+// tombstones. So a thread reads both records, the cycle and the FP64 positions of its cell
+// with coalesced loads, evaluates the intra-cell spring once, draws the noise of both elements
+// from one Philox block (2D), and walks the two Verlet lists in lockstep, BATCH entries of each
+// in flight. Per element it computes what k_force_list computes: the spring, wall and noise
+// terms are the same expressions; the pair terms are summed in list order.
+template <int D, int LAW, int BATCH, int MINB>
+__global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) {
+  __shared__ ColonyConst sC;
+  __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
+  __shared__ float s_ssum;
+  __shared__ float s_half2;
+  __shared__ int s_warps_done;
+  const int t = blockIdx.x;
+  if (t >= a.tiles[a.B]) return;  // uniform per block (tiles over slot pairs)
+  const int tid = threadIdx.x;
+  const int c = colony_of_tile(a.tiles, a.B, t);
+  {
+    const int *src = reinterpret_cast<const int *>(a.col + c);
+    int *dst = reinterpret_cast<int *>(&sC);
+    for (int i = tid; i < static_cast<int>(sizeof(ColonyConst) / sizeof(int)); i += kTile) dst[i] = __ldg(src + i);
+    if (tid == 0) {
+      s_dmax = 0u;
+      s_smax = 0u;
+      s_ssum = 0.0f;
+      s_half2 = a.skin[c].half2;
+      s_warps_done = 0;
+    }
+  }
+  __syncthreads();
+  const ColonyConst &C = sC;
+  const int ts = __ldg(a.ts_dev);
+  const size_t SS = a.SS;
+  const int s0 = C.slot_base + 2 * ((t - a.tiles[c]) * kTile + tid);
+  const bool used = s0 < C.slot_base + a.cnt[c].nslot;
+  const int2 ee = used ? __ldg(reinterpret_cast<const int2 *>(a.eid + s0)) : make_int2(-1, -1);
+  // fresh-pair contributions: one bit per slot; slot bases are 32-aligned and s0 is even, so
+  // both bits of the cell sit in one word (16 cells per word)
+  const unsigned tword = a.ftouch[s0 >> 5];
+  const unsigned tbits = (tword >> (s0 & 31)) & 3u;
+  float d2 = 0.0f, st2[2] = {0.0f, 0.0f};
+  if (ee.x >= 0) {
+    // ---- loads (both elements; every load before the first store)
+    const int g = ee.x >> 1;
+    float4 pr[2];
+    pr[0] = __ldg(a.pk + s0);
+    pr[1] = __ldg(a.pk + s0 + 1);
+    const int2 sb = __ldg(reinterpret_cast<const int2 *>(a.sbin + s0));
+    const int2 nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
+    int2 cy = make_int2(0, 0);
+    if (C.divide) cy = __ldg(a.cyc + s0);
+    double xin[2][D];
+    float uref[2][D], F[2][D], fa[2][D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double2 xv = __ldg(reinterpret_cast<const double2 *>(a.x_in + d * SS + s0));
+      xin[0][d] = xv.x;
+      xin[1][d] = xv.y;
+      fa[0][d] = (tbits & 1u) ? a.facc[d * SS + s0] : 0.0f;
+      fa[1][d] = (tbits & 2u) ? a.facc[d * SS + s0 + 1] : 0.0f;
+      F[0][d] = 0.0f;
+      F[1][d] = 0.0f;
+    }
+    if (D == 2) {
+      uref_unpack2(C.uq_inv, pr[0].z, uref[0]);
+      uref_unpack2(C.uq_inv, pr[1].z, uref[1]);
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const float2 uv = __ldg(reinterpret_cast<const float2 *>(a.uref + d * SS + s0));
+        uref[0][d] = uv.x;
+        uref[1][d] = uv.y;
+      }
+    }
+    float ui[2][D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      ui[0][d] = pk_c(pr[0], d);
+      ui[1][d] = pk_c(pr[1], d);
+    }
+    const float si[2] = {fabsf(pr[0].w), fabsf(pr[1].w)};
+    int bi[2][D];
+    bin_decode<D>(C, sb.x, bi[0]);
+    bin_decode<D>(C, sb.y, bi[1]);
+    // ---- intra-cell spring + motility (the back element's view r1 - r0; the front
+    // element's is the same vector, as -(r0 - r1) is exact)
+    {
+      float rij[D];
+      float r2 = 0.0f;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        float v = ui[1][d] - ui[0][d];
+        if (C.single_bin) {
+          if (C.periodic[d]) v -= rintf(v * C.inv_bwf[d]) * C.bwf[d];
+        } else {
+          int db = bi[1][d] - bi[0][d];
+          if (C.periodic[d]) {
+            if (db > (C.ns[d] >> 1)) db -= C.ns[d];
+            if (db < -(C.ns[d] >> 1)) db += C.ns[d];
+          }
+          v += static_cast<float>(db) * C.bwf[d];
+        }
+        rij[d] = v;
+        r2 += v * v;
+      }
+      if (r2 > 0.0f) {
+        const float rinv = rsqrtf(r2);
+        float rest = C.rest0_f;
+        if (C.divide) {
+          const int span = cy.y - cy.x;
+          float frac = span > 0 ? __fdividef(static_cast<float>(ts - cy.x), static_cast<float>(span)) : 1.0f;
+          frac = fminf(1.0f, fmaxf(0.0f, frac));
+          rest = C.rest0_f + (C.rest1_f - C.rest0_f) * frac;
+        }
+        const float sp = C.kappa_f * (r2 * rinv - rest);
+        const float coef0 = (sp - C.motility_f[0]) * rinv;
+        const float coef1 = (C.motility_f[1] - sp) * rinv;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          F[0][d] += coef0 * rij[d];
+          F[1][d] += coef1 * rij[d];
+        }
+      }
+    }
+    // ---- walls
+    if (C.nwalls > 0) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const float z = static_cast<float>(bi[j][D - 1]) * C.bwf[D - 1] + ui[j][D - 1];
+        const float rad = 0.5f * si[j];
+        for (int w = 0; w < C.nwalls; ++w) {
+          const float dir = static_cast<float>(C.wall_dir[w]);
+          const float delta = rad - dir * (z - C.wall_pos_f[w]);
+          if (delta > 0.0f) F[j][D - 1] += dir * C.wall_E_f * delta * (delta * rsqrtf(delta));
+        }
+      }
+    }
+    // ---- passive noise
+    if (a.noise_mode == 1) {
+      uint32_t w[2][4];
+      noise_words_cell<D>(g, C.noise_per_cell, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w[0], w[1]);
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const float amp = C.zeta_f[j] * C.amp_f;
+#pragma unroll
+        for (int h = 0; h < (D + 1) / 2; ++h) {
+          const float u1 = static_cast<float>((w[j][2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;
+          const float u2 = static_cast<float>(w[j][2 * h + 1] >> 8) * 5.9604644775390625e-08f;
+          const float m = fmaxf(-2.0f * __logf(u1), 0.0f);
+          const float rad = m * rsqrtf(fmaxf(m, 1e-30f));  // sqrt(m), 0 when u1 == 1
+          float sn, cs;
+          __sincosf(6.2831853071795865f * u2, &sn, &cs);
+          F[j][2 * h] += amp * rad * cs;
+          if (2 * h + 1 < D) F[j][2 * h + 1] += amp * rad * sn;
+        }
+      }
+    } else if (a.noise_mode == 2) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const size_t base = static_cast<size_t>(C.noise_per_cell ? g : 2 * g + j) * D;
+#pragma unroll
+        for (int d = 0; d < D; ++d) F[j][d] += C.zeta_f[j] * static_cast<float>(__ldg(a.noise + base + d));
+      }
+    }
+    // ---- pair forces: both lists in lockstep, BATCH entries of each in flight
+    const float eps = C.eps_f, rcs = C.rcs_f;
+    float tab[2][D][3];  // partner offset from each element for bin offset -1, 0, +1
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        tab[j][d][0] = -C.bwf[d] - ui[j][d];
+        tab[j][d][1] = -ui[j][d];
+        tab[j][d][2] = C.bwf[d] - ui[j][d];
+      }
+    const int nmax = nn.x > nn.y ? nn.x : nn.y;
+    const int *lp = a.nbr + s0;
+    for (int k0 = 0; k0 < nmax; k0 += BATCH) {
+      unsigned ent[2][BATCH];
+      float4 pj[2][BATCH];
+#pragma unroll
+      for (int q = 0; q < BATCH; ++q) {
+        const int k = k0 + q;
+        const int2 ev = k < nmax ? __ldg(reinterpret_cast<const int2 *>(lp + static_cast<size_t>(k) * SS))
+                                 : make_int2(-1, -1);
+        ent[0][q] = k < nn.x ? static_cast<unsigned>(ev.x) : 0xffffffffu;
+        ent[1][q] = k < nn.y ? static_cast<unsigned>(ev.y) : 0xffffffffu;
+      }
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < BATCH; ++q)
+          pj[j][q] = ent[j][q] != 0xffffffffu ? __ldg(a.pk + (ent[j][q] & ((1u << kListSlotBits) - 1u)))
+                                              : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int q = 0; q < BATCH; ++q) {
+          const unsigned code = ent[j][q] >> kListSlotBits;
+          float dx[D];
+          float r2 = 0.0f;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const unsigned k = (code >> (2 * d)) & 3u;
+            dx[d] = pk_c(pj[j][q], d) + (k == 0u ? tab[j][d][0] : (k == 1u ? tab[j][d][1] : tab[j][d][2]));
+            r2 += dx[d] * dx[d];
+          }
+          const float f0 = pair_f0_fast<LAW>(r2, si[j], pj[j][q].w, eps, rcs, pj[j][q].w > 0.0f);
+#pragma unroll
+          for (int d = 0; d < D; ++d) F[j][d] += f0 * dx[d];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[j][d] += fa[j][d];
+    // ---- checks, update (one FP64 add per axis, integer wrap tests), stores
+    bool finite = true;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int d = 0; d < D; ++d) finite = finite && isfinite(F[j][d]);
+    if (!finite) atomicOr(&a.cnt[c].err, kErrNan);
+    if (a.frc) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        *reinterpret_cast<double2 *>(a.frc + d * SS + s0) =
+            make_double2(static_cast<double>(F[0][d]), static_cast<double>(F[1][d]));
+    }
+    if (tbits) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) *reinterpret_cast<float2 *>(a.facc + d * SS + s0) = make_float2(0.0f, 0.0f);
+    }
+    if (a.integrate) {
+      bool inside = true;
+      float4 pn[2];
+      double xo[2][D];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const float temp = a.heun ? 0.5f * C.temp_f[j] : C.temp_f[j];
+        // 2D: z carries the packed list reference to the next record
+        pn[j] = make_float4(0.0f, 0.0f, D == 2 ? pr[j].z : 0.0f, pr[j].w);
+        float dj2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const float dxf = temp * F[j][d];
+          double xn = xin[j][d] + f2d_exact(dxf);
+          const long long xb = __double_as_longlong(xn);
+          const long long lb = __double_as_longlong(C.box[d]);
+          const bool lo = xb < 0, hi = xb >= lb;  // negative (incl. -0) / at or past L
+          if (C.periodic[d]) {
+            // the wrap, taken by the few warps with an element that crossed 0 or L (an FP64
+            // add predicated into every thread would cost the FP64 pipe on all of them)
+            if (__any_sync(__activemask(), lo || hi)) {
+              if (lo) xn = (xb & 0x7fffffffffffffffll) ? xn + C.box[d] : 0.0;
+              if (__double_as_longlong(xn) >= lb) xn -= C.box[d];
+            }
+          } else {
+            inside = inside && !lo && !hi;
+          }
+          xo[j][d] = xn;
+          const float un = ui[j][d] + dxf;
+          pk_set(pn[j], d, un);
+          const float dr = un - uref[j][d];
+          dj2 += dr * dr;
+          st2[j] += dxf * dxf;
+        }
+        d2 = fmaxf(d2, dj2);
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        *reinterpret_cast<double2 *>(a.x_out + d * SS + s0) = make_double2(xo[0][d], xo[1][d]);
+      a.pk_next[s0] = pn[0];
+      a.pk_next[s0 + 1] = pn[1];
+      if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
+      if (D == 2) {
+        // guard with the fixed-point rounding allowed for: trips no later than |u - uref| > skin/2
+        const float h = fmaxf(sqrtf(s_half2) - (C.uq_inv[0] + C.uq_inv[1]), 0.0f);
+        if (d2 > h * h) atomicOr(&a.skin[c].need, 1);
+      } else if (d2 > s_half2) {
+        atomicOr(&a.skin[c].need, 1);
+      }
+      if (a.vel) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          double v[2];
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const double vj = static_cast<double>(F[j][d] * C.mu_f[j]);
+            v[j] = a.heun == 2 ? 0.5 * ((a.vel_prev ? a.vel_prev : a.vel)[d * SS + s0 + j] + vj) : vj;
+          }
+          *reinterpret_cast<double2 *>(a.vel + d * SS + s0) = make_double2(v[0], v[1]);
+        }
+      }
+    }
+  } else if (used && a.integrate) {
+    // tombstones: the next records must keep w < 0 too, or the lists of others would see the
+    // stale records of two steps ago in the other buffer
+    a.pk_next[s0] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    a.pk_next[s0 + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+  }
+  __syncwarp();  // every lane has read its touch word
+  if (tword != 0u && (tid & 15) == 0) a.ftouch[s0 >> 5] = 0u;
+  if (a.integrate) {
+    // displacement statistics: warp reductions and shared atomics; the last warp of the block
+    // to finish adds the block's values to the colony (no block barrier: warps with short
+    // lists do not wait for the others)
+    const unsigned dmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    const float stp0 = sqrtf(st2[0]), stp1 = sqrtf(st2[1]);
+    const unsigned smax = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(stp0, stp1)));
+    float ssum = stp0 + stp1;
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, q);
+    if ((tid & 31) == 0) {
+      atomicMax(&s_dmax, dmax);
+      atomicMax(&s_smax, smax);
+      atomicAdd(&s_ssum, ssum);
+      __threadfence_block();
+      if (atomicAdd(&s_warps_done, 1) == kTile / 32 - 1) {
+        __threadfence_block();
+        atomicMax(&a.skin[c].maxdisp2, atomicOr(&s_dmax, 0u));
+        if (a.sched) {
+          atomicMax(reinterpret_cast<unsigned *>(&a.sched[c].step_max), atomicOr(&s_smax, 0u));
+          atomicAdd(&a.sched[c].step_sum, atomicAdd(&s_ssum, 0.0f));
+        }
+      }
+    }
+  }
+}
+
 template <int D, int LAW>
 void launch_list_dl(const ForceArgs &a, int grid, int variant, cudaStream_t s) {
-  // variants (staging depth, CTAs per SM): 0 (4, 4), 1 (2, 4), 2 (8, 3), 3 (8, 2); 3D runs (4, 4)
-  if (D == 3 || variant == 0) {
-    k_force_list<D, LAW, 4, 4><<<grid, kTile, 0, s>>>(a);
-  } else if (variant == 1) {
-    k_force_list<D, LAW, 2, 4><<<grid, kTile, 0, s>>>(a);
-  } else if (variant == 2) {
-    k_force_list<D, LAW, 8, 3><<<grid, kTile, 0, s>>>(a);
+  // cell-major slots, one thread per cell; variants (list entries of each element in flight,
+  // CTAs per SM): 0 (4, 2), 1 (2, 3), 2 (1, 3), 3 (2, 2); 3D runs (2, 2)
+  if constexpr (D == 3) {
+    (void)variant;
+    k_force_cells<D, LAW, 2, 2><<<grid, kTile, 0, s>>>(a);
   } else {
-    k_force_list<D, LAW, 8, 2><<<grid, kTile, 0, s>>>(a);
+    if (variant == 0) {
+      k_force_cells<D, LAW, 4, 2><<<grid, kTile, 0, s>>>(a);
+    } else if (variant == 1) {
+      k_force_cells<D, LAW, 2, 3><<<grid, kTile, 0, s>>>(a);
+    } else if (variant == 2) {
+      k_force_cells<D, LAW, 1, 3><<<grid, kTile, 0, s>>>(a);
+    } else {
+      k_force_cells<D, LAW, 2, 2><<<grid, kTile, 0, s>>>(a);
+    }
   }
 }
 

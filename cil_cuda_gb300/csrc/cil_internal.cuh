@@ -243,15 +243,15 @@ __device__ __forceinline__ void bin_decode(const ColonyConst &C, int id, int *b)
 }
 
 // Exact float -> double conversion with integer operations only (no FP64 pipe): finite
-// normal values are re-biased bit for bit; zeros, subnormals, inf and NaN take the
-// conversion instruction.
+// normal values are re-biased bit for bit; zeros and subnormals give a signed zero (a
+// displacement below 1.2e-38 leaves any position unchanged); inf and NaN keep their class.
 __device__ __forceinline__ double f2d_exact(float f) {
   const uint32_t b = __float_as_uint(f);
   const uint32_t ex = (b >> 23) & 0xffu;
-  if (ex == 0u || ex == 0xffu) return static_cast<double>(f);
-  const uint64_t d = (static_cast<uint64_t>(b & 0x80000000u) << 32) |
-                     (static_cast<uint64_t>(ex - 127u + 1023u) << 52) |
-                     (static_cast<uint64_t>(b & 0x7fffffu) << 29);
+  const uint64_t sign = static_cast<uint64_t>(b & 0x80000000u) << 32;
+  const uint64_t mant = static_cast<uint64_t>(b & 0x7fffffu) << 29;
+  const uint64_t e64 = ex == 0u ? 0u : (ex == 0xffu ? 0x7ffu : ex - 127u + 1023u);
+  const uint64_t d = sign | (e64 << 52) | (ex == 0u ? 0u : mant);
   return __longlong_as_double(static_cast<long long>(d));
 }
 
@@ -317,20 +317,56 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float &n0, fl
   n1 = r * s;
 }
 
-// Philox words of the passive noise of one element (or cell) at step ts. In 2D one block of
-// four words serves two consecutive steps (the even step takes words 0-1, the odd one 2-3,
-// one Box-Muller pair each); in 3D each step takes a block of its own (two pairs).
+// Philox words of the passive noise of element e = 2 g + j at step ts.
+//   per element (noise_per_cell 0): in 2D one block keyed by the cell, (g, ts, noise, 1),
+//     serves both of its elements: element j takes words 2j and 2j + 1 (one Box-Muller pair);
+//     in 3D each element takes a block of its own, (e, ts, noise, 0) (two pairs).
+//   per cell (noise_per_cell 1, the reference's passiveWiener[cell][dim]): in 2D one block
+//     (g, ts / 2, noise, 0) serves two consecutive steps (the even step takes words 0-1, the odd
+//     one 2-3); in 3D each step takes the block (g, ts, noise, 0).
+// Every force kernel draws through these two functions, so the forms agree on the noise.
 template <int D>
-__device__ __forceinline__ void noise_words(uint32_t id, int ts, uint32_t klo, uint32_t khi, uint32_t *w) {
+__device__ __forceinline__ void noise_words(int e, int per_cell, int ts, uint32_t klo, uint32_t khi, uint32_t *w) {
+  const uint32_t g = static_cast<uint32_t>(e) >> 1;
   if (D == 2) {
-    const u32x4 r = philox4x32_10(id, static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi);
-    const bool odd = (ts & 1) != 0;
-    w[0] = odd ? r.v[2] : r.v[0];
-    w[1] = odd ? r.v[3] : r.v[1];
+    const bool sel = per_cell ? (ts & 1) != 0 : (e & 1) != 0;
+    const u32x4 r = per_cell ? philox4x32_10(g, static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi)
+                             : philox4x32_10(g, static_cast<uint32_t>(ts), kRngNoise, 1u, klo, khi);
+    w[0] = sel ? r.v[2] : r.v[0];
+    w[1] = sel ? r.v[3] : r.v[1];
   } else {
-    const u32x4 r = philox4x32_10(id, static_cast<uint32_t>(ts), kRngNoise, 0u, klo, khi);
+    const u32x4 r = philox4x32_10(per_cell ? g : static_cast<uint32_t>(e), static_cast<uint32_t>(ts), kRngNoise, 0u,
+                                  klo, khi);
 #pragma unroll
     for (int q = 0; q < 4; ++q) w[q] = r.v[q];
+  }
+}
+
+// The words of both elements of cell g at once (w0: back element, w1: front element), one
+// Philox block per cell and step in 2D; the same values noise_words gives each element.
+template <int D>
+__device__ __forceinline__ void noise_words_cell(int g, int per_cell, int ts, uint32_t klo, uint32_t khi,
+                                                 uint32_t *w0, uint32_t *w1) {
+  if (D == 2) {
+    if (per_cell) {
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi);
+      const bool odd = (ts & 1) != 0;
+      w0[0] = w1[0] = odd ? r.v[2] : r.v[0];
+      w0[1] = w1[1] = odd ? r.v[3] : r.v[1];
+    } else {
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts), kRngNoise, 1u, klo, khi);
+      w0[0] = r.v[0];
+      w0[1] = r.v[1];
+      w1[0] = r.v[2];
+      w1[1] = r.v[3];
+    }
+  } else if (per_cell) {
+    noise_words<D>(2 * g, 1, ts, klo, khi, w0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w1[q] = w0[q];
+  } else {
+    noise_words<D>(2 * g, 0, ts, klo, khi, w0);
+    noise_words<D>(2 * g + 1, 0, ts, klo, khi, w1);
   }
 }
 
@@ -412,6 +448,7 @@ struct RebuildArgs {
   size_t SS;               // slot stride of SoA arrays
   const int *tiles_used;   // [B+1] tiles over nslot (before the rebuild)
   const int *tiles_live;   // [B+1] tiles over nlive (after the scan)
+  const int *tiles_cell;   // [B+1] tiles over ncell (cell re-sort of skin mode)
   const int *scan_col;     // scan block -> colony
   int nscan;               // scan blocks
   const double *x_in;
@@ -464,7 +501,7 @@ struct ForceArgs {
   const int2 *range;
   const int *slot_of;
   // skin mode (null otherwise)
-  const int *tiles;        // tiles over nslot
+  const int *tiles;        // tiles over nslot (k_force_list) or over slot pairs (k_force_cells)
   ColonySkin *skin;
   const int *nbr;          // Verlet lists [kListCap][SS]
   const int *ncnt;
@@ -606,8 +643,12 @@ __device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ w, co
 
 // ---------------------------------------------------------------- launchers (host side)
 void launch_tiles(const ColonyConst *col, ColonyCounters *cnt, int B, int which, int *tiles,
-                  cudaStream_t s);
+                  cudaStream_t s, int which2 = 0, int *tiles2 = nullptr);
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s);
+// skin mode: slots re-sorted by cell (cells ranked by the bin of their back element, a cell's
+// elements in the slot pair slot_base + 2 rank, + 1; tombstones dropped); a.tiles_cell must be
+// current; leaves bcount at zero and nslot = 2 ncell
+void launch_cell_resort(const RebuildArgs &a, int grid_cells, cudaStream_t s);
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block,
                   cudaStream_t s);
 void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, cudaStream_t s);

@@ -97,9 +97,10 @@ typedef struct cil_config {
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
   int32_t block_size;     /* threads per block of the force kernels: 0 or 256 */
   int32_t flags;          /* CIL_FLAG_* bits */
-  /* Verlet-list force kernel (skin mode): list entries in flight per thread (0 = 4; 2, 4, 8)
-   * and CTAs per SM it is compiled for (0 = 4; 2, 3, 4). Supported pairs: (2, 4), (4, 4),
-   * (8, 3), (8, 2); 3D always runs (4, 4). cil_cuda_gb300/autotune.py picks them. */
+  /* Verlet-list force kernel (skin mode, one thread per cell): list entries of each element in
+   * flight per thread (0 = 4; 1, 2, 4) and CTAs per SM it is compiled for (0 = 2; 2, 3).
+   * Supported pairs: (4, 2), (2, 3), (1, 3), (2, 2); 3D always runs (2, 2).
+   * cil_cuda_gb300/autotune.py picks them. */
   int32_t staging;
   int32_t occupancy;
   int32_t integrator;     /* CIL_INTEGRATOR_*: 0 = Euler */
