@@ -2,9 +2,9 @@
 
 Tries, on the caller's own colonies, every combination of
   * bin size: the bin width as a factor of the smallest allowed one (largest cutoff + skin),
-  * the Verlet-list force kernel's variant: list entries of each of the cell's two elements in
-    flight per thread (staging depth) and CTAs per SM it is compiled for (which sets its
-    register budget, hence block residency),
+  * the Verlet-list force kernel's variant: chunks of 32 flattened list entries in flight per
+    warp (staging depth) and CTAs per SM it is compiled for (which sets its register budget,
+    hence block residency),
 and times a short run of each with CUDA events (graph-replayed steps, as in production).
 Every candidate runs the same physics; only the time differs. Returns the fastest settings
 as keyword arguments for Engine and the table of all trials.
@@ -16,7 +16,7 @@ import itertools
 from . import Engine, PREC_MIXED, RNG_PHILOX
 
 BIN_FACTORS = (1.0, 1.15, 1.3)
-VARIANTS = ((4, 2), (2, 3), (1, 3), (2, 2))  # (list entries of each element in flight, CTAs per SM)
+VARIANTS = ((2, 3), (1, 3), (2, 2), (1, 4))  # (chunks of 32 list entries in flight per warp, CTAs per SM)
 
 
 def needed_width(params, states, skin):

@@ -19,8 +19,10 @@ RUNNER = os.path.join(OUT, "cil_gpu_run")
 SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_skin.cu", "cil_mlp.cu", "cil_noalloc.cu",
            "cil_frame.cu", "cil_input.cpp", "cil_cycle.cu", "cil_h5.cpp"]
 # per-file flags: the single-element cycle model keeps FP64 products and sums separate (no FMA
-# contraction) so that it computes exactly what its host restatement computes
-EXTRA = {"cil_cycle.cu": ["--fmad=false"]}
+# contraction) so that it computes exactly what its host restatement computes; the force kernels
+# flush FP32 denormals (no denormal fix-up code around the reciprocal square roots of the FP32
+# pair laws; the FP64 paths are unaffected)
+EXTRA = {"cil_cycle.cu": ["--fmad=false"], "cil_force.cu": ["-ftz=true"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

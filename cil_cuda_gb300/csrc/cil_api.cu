@@ -895,11 +895,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->integrator != CIL_INTEGRATOR_EULER && cfg->integrator != CIL_INTEGRATOR_HEUN) return CIL_ERR_CONFIG;
   int list_variant = -1;
   {
-    const int st = cfg->staging == 0 ? 4 : cfg->staging, oc = cfg->occupancy == 0 ? 2 : cfg->occupancy;
-    if (st == 4 && oc == 2) list_variant = 0;
-    if (st == 2 && oc == 3) list_variant = 1;
-    if (st == 1 && oc == 3) list_variant = 2;
-    if (st == 2 && oc == 2) list_variant = 3;
+    const int st = cfg->staging == 0 ? 2 : cfg->staging, oc = cfg->occupancy == 0 ? 3 : cfg->occupancy;
+    if (st == 2 && oc == 3) list_variant = 0;
+    if (st == 1 && oc == 3) list_variant = 1;
+    if (st == 2 && oc == 2) list_variant = 2;
+    if (st == 1 && oc == 4) list_variant = 3;
     if (list_variant < 0) return CIL_ERR_CONFIG;
   }
   auto *h = new cil_handle();

@@ -854,16 +854,115 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
   }
 }
 
+// Per-warp shared memory of the cell kernel's pair pass: the records of the warp's 64 elements,
+// and for one segment of kPairSeg flattened list entries the owner of each entry (element | list
+// index << 6) and its pair force.
+constexpr int kPairSeg = 512;
+template <int D>
+__host__ __device__ constexpr int pair_smem_warp() {
+  return 64 * 16 + kPairSeg * 2 + kPairSeg * D * 4;
+}
+
+// The pair forces of a warp's 32 cells (64 elements), whole warp: the elements' Verlet-list
+// entries are taken as one flattened range (element by element, each list in order), so every
+// lane evaluates a real entry whatever the lengths of the lists; each lane then adds its two
+// elements' pair forces in list order (the sums do not depend on scheduling). Every lane calls
+// it; lanes without a live cell pass n = (0, 0). sw0: the warp's first slot.
+template <int D, int LAW, int UNROLL>
+__device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst &C, int sw0, int2 nn,
+                                           const float4 *pr, float (*F)[D], unsigned char *wsm) {
+  const int lane = threadIdx.x & 31;
+  float4 *s_rec = reinterpret_cast<float4 *>(wsm);
+  unsigned short *s_own = reinterpret_cast<unsigned short *>(wsm + 64 * 16);
+  float *s_c = reinterpret_cast<float *>(wsm + 64 * 16 + kPairSeg * 2);
+  s_rec[2 * lane] = pr[0];
+  s_rec[2 * lane + 1] = pr[1];
+  const int cnt = nn.x + nn.y;
+  int inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const int T = __shfl_sync(0xffffffffu, inc, 31);
+  const int st0 = inc - cnt, st1 = st0 + nn.x, en1 = inc;
+  // list entry k of element i of the warp sits at nbr[k * SS + sw0 + i]: 32-bit offsets from the
+  // warp's first slot (k < 64 and, in skin mode, SS < 2^26: list entries address slots in 26
+  // bits, checked when the handle is created, so k * SS + i < 2^32)
+  const int *lw = a.nbr + sw0;
+  const unsigned ss = static_cast<unsigned>(a.SS);
+  const float eps = C.eps_f, rcs = C.rcs_f;
+  float bw[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) bw[d] = C.bwf[d];
+  for (int S = 0; S < T; S += kPairSeg) {  // uniform
+    const int E = min(T, S + kPairSeg);
+    __syncwarp();  // the last segment's sums are read; the records are written
+    // owner of every entry of the segment
+    for (int f = max(st0, S); f < min(st1, E); ++f)
+      s_own[f - S] = static_cast<unsigned short>((2 * lane) | ((f - st0) << 6));
+    for (int f = max(st1, S); f < min(en1, E); ++f)
+      s_own[f - S] = static_cast<unsigned short>((2 * lane + 1) | ((f - st1) << 6));
+    __syncwarp();
+    for (int base = S; base < E; base += 32 * UNROLL) {  // uniform
+      unsigned ent[UNROLL];
+      int own[UNROLL];
+      float4 pj[UNROLL];
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const int f = base + 32 * u + lane;
+        own[u] = f < E ? s_own[f - S] : -1;
+        ent[u] = own[u] >= 0
+                     ? __ldg(lw + (static_cast<unsigned>(own[u] >> 6) * ss + static_cast<unsigned>(own[u] & 63)))
+                     : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u)
+        pj[u] = own[u] >= 0 ? __ldg(a.pk + (ent[u] & ((1u << kListSlotBits) - 1u)))
+                            : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        if (own[u] < 0) continue;
+        const float4 me = s_rec[own[u] & 63];
+        const unsigned code = ent[u] >> kListSlotBits;
+        float dx[D];
+        float r2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          // bin offset code k in {0, 1, 2}: (k - 1) as a float, exactly, without a conversion
+          const float off = __int_as_float(0x4B000000 | ((code >> (2 * d)) & 3u)) - 8388609.0f;
+          dx[d] = pk_c(pj[u], d) + (off * bw[d] - pk_c(me, d));
+          r2 += dx[d] * dx[d];
+        }
+        const float f0 = pair_f0_fast<LAW>(r2, fabsf(me.w), pj[u].w, eps, rcs, pj[u].w > 0.0f);
+        float *cf = s_c + (base + 32 * u + lane - S) * D;
+#pragma unroll
+        for (int d = 0; d < D; ++d) cf[d] = f0 * dx[d];
+      }
+    }
+    __syncwarp();
+    // each element adds its entries of the segment, in list order
+    for (int f = max(st0, S); f < min(st1, E); ++f)
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[0][d] += s_c[(f - S) * D + d];
+    for (int f = max(st1, S); f < min(en1, E); ++f)
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[1][d] += s_c[(f - S) * D + d];
+  }
+}
+
 // Skin-mode step over cell-major slots, one thread per cell. Between slot re-sorts a cell's
 // two elements sit in adjacent slots, back element first (s0 = slot_base + 2 p, s1 = s0 + 1):
 // the re-sort ranks cells, division appends daughters as slot pairs, apoptosis leaves pairs of
 // tombstones. So a thread reads both records, the cycle and the FP64 positions of its cell
-// with coalesced loads, evaluates the intra-cell spring once, draws the noise of both elements
-// from one Philox block (2D), and walks the two Verlet lists in lockstep, BATCH entries of each
-// in flight. Per element it computes what k_force_list computes: the spring, wall and noise
-// terms are the same expressions; the pair terms are summed in list order.
-template <int D, int LAW, int BATCH, int MINB>
+// with coalesced loads, evaluates the intra-cell spring once and draws the noise of both
+// elements from one Philox block (2D); the warp then evaluates its 64 elements' Verlet-list
+// entries as one flattened range (cell_pairs). Per element it computes what k_force_list
+// computes: the spring, wall and noise terms are the same expressions, the pair terms are
+// summed in list order. UNROLL flattened chunks of 32 entries are in flight per warp.
+template <int D, int LAW, int UNROLL, int MINB>
 __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) {
+  extern __shared__ __align__(16) unsigned char s_pairs[];
   __shared__ ColonyConst sC;
   __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
   __shared__ float s_ssum;
@@ -897,27 +996,32 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
   const unsigned tword = a.ftouch[s0 >> 5];
   const unsigned tbits = (tword >> (s0 & 31)) & 3u;
   float d2 = 0.0f, st2[2] = {0.0f, 0.0f};
-  if (ee.x >= 0) {
-    // ---- loads (both elements; every load before the first store)
+  const bool live = ee.x >= 0;
+  // ---- loads and the per-element terms (live cells; every load before the first store)
+  float4 pr[2] = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+  int2 nn = make_int2(0, 0);
+  double xin[2][D];
+  float uref[2][D], F[2][D], fa[2][D], ui[2][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    F[0][d] = F[1][d] = 0.0f;
+    fa[0][d] = fa[1][d] = 0.0f;
+  }
+  if (live) {
     const int g = ee.x >> 1;
-    float4 pr[2];
     pr[0] = __ldg(a.pk + s0);
     pr[1] = __ldg(a.pk + s0 + 1);
     const int2 sb = __ldg(reinterpret_cast<const int2 *>(a.sbin + s0));
-    const int2 nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
+    nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
     int2 cy = make_int2(0, 0);
     if (C.divide) cy = __ldg(a.cyc + s0);
-    double xin[2][D];
-    float uref[2][D], F[2][D], fa[2][D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       const double2 xv = __ldg(reinterpret_cast<const double2 *>(a.x_in + d * SS + s0));
       xin[0][d] = xv.x;
       xin[1][d] = xv.y;
-      fa[0][d] = (tbits & 1u) ? a.facc[d * SS + s0] : 0.0f;
-      fa[1][d] = (tbits & 2u) ? a.facc[d * SS + s0 + 1] : 0.0f;
-      F[0][d] = 0.0f;
-      F[1][d] = 0.0f;
+      if (tbits & 1u) fa[0][d] = a.facc[d * SS + s0];
+      if (tbits & 2u) fa[1][d] = a.facc[d * SS + s0 + 1];
     }
     if (D == 2) {
       uref_unpack2(C.uq_inv, pr[0].z, uref[0]);
@@ -930,7 +1034,6 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
         uref[1][d] = uv.y;
       }
     }
-    float ui[2][D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       ui[0][d] = pk_c(pr[0], d);
@@ -1020,54 +1123,10 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
         for (int d = 0; d < D; ++d) F[j][d] += C.zeta_f[j] * static_cast<float>(__ldg(a.noise + base + d));
       }
     }
-    // ---- pair forces: both lists in lockstep, BATCH entries of each in flight
-    const float eps = C.eps_f, rcs = C.rcs_f;
-    float tab[2][D][3];  // partner offset from each element for bin offset -1, 0, +1
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        tab[j][d][0] = -C.bwf[d] - ui[j][d];
-        tab[j][d][1] = -ui[j][d];
-        tab[j][d][2] = C.bwf[d] - ui[j][d];
-      }
-    const int nmax = nn.x > nn.y ? nn.x : nn.y;
-    const int *lp = a.nbr + s0;
-    for (int k0 = 0; k0 < nmax; k0 += BATCH) {
-      unsigned ent[2][BATCH];
-      float4 pj[2][BATCH];
-#pragma unroll
-      for (int q = 0; q < BATCH; ++q) {
-        const int k = k0 + q;
-        const int2 ev = k < nmax ? __ldg(reinterpret_cast<const int2 *>(lp + static_cast<size_t>(k) * SS))
-                                 : make_int2(-1, -1);
-        ent[0][q] = k < nn.x ? static_cast<unsigned>(ev.x) : 0xffffffffu;
-        ent[1][q] = k < nn.y ? static_cast<unsigned>(ev.y) : 0xffffffffu;
-      }
-#pragma unroll
-      for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int q = 0; q < BATCH; ++q)
-          pj[j][q] = ent[j][q] != 0xffffffffu ? __ldg(a.pk + (ent[j][q] & ((1u << kListSlotBits) - 1u)))
-                                              : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-#pragma unroll
-      for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int q = 0; q < BATCH; ++q) {
-          const unsigned code = ent[j][q] >> kListSlotBits;
-          float dx[D];
-          float r2 = 0.0f;
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            const unsigned k = (code >> (2 * d)) & 3u;
-            dx[d] = pk_c(pj[j][q], d) + (k == 0u ? tab[j][d][0] : (k == 1u ? tab[j][d][1] : tab[j][d][2]));
-            r2 += dx[d] * dx[d];
-          }
-          const float f0 = pair_f0_fast<LAW>(r2, si[j], pj[j][q].w, eps, rcs, pj[j][q].w > 0.0f);
-#pragma unroll
-          for (int d = 0; d < D; ++d) F[j][d] += f0 * dx[d];
-        }
-    }
+  }
+  // ---- pair forces from the Verlet lists: the whole warp
+  cell_pairs<D, LAW, UNROLL>(a, C, s0 - 2 * (tid & 31), nn, pr, F, s_pairs + (tid >> 5) * pair_smem_warp<D>());
+  if (live) {
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
@@ -1186,22 +1245,34 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
   }
 }
 
+template <int D, int LAW, int UNROLL, int MINB>
+void launch_cells(const ForceArgs &a, int grid, cudaStream_t s) {
+  constexpr int bytes = (kTile / 32) * pair_smem_warp<D>();
+  static bool attr_set = false;  // per instantiation; the attribute is per function
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_force_cells<D, LAW, UNROLL, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    attr_set = true;
+  }
+  k_force_cells<D, LAW, UNROLL, MINB><<<grid, kTile, bytes, s>>>(a);
+}
+
 template <int D, int LAW>
 void launch_list_dl(const ForceArgs &a, int grid, int variant, cudaStream_t s) {
-  // cell-major slots, one thread per cell; variants (list entries of each element in flight,
-  // CTAs per SM): 0 (4, 2), 1 (2, 3), 2 (1, 3), 3 (2, 2); 3D runs (2, 2)
+  // cell-major slots, one thread per cell, the warp's list entries flattened; variants
+  // (chunks of 32 entries in flight per warp, CTAs per SM): 0 (2, 3), 1 (1, 3), 2 (2, 2),
+  // 3 (1, 4); 3D runs (1, 2)
   if constexpr (D == 3) {
     (void)variant;
-    k_force_cells<D, LAW, 2, 2><<<grid, kTile, 0, s>>>(a);
+    launch_cells<D, LAW, 1, 2>(a, grid, s);
   } else {
     if (variant == 0) {
-      k_force_cells<D, LAW, 4, 2><<<grid, kTile, 0, s>>>(a);
+      launch_cells<D, LAW, 2, 3>(a, grid, s);
     } else if (variant == 1) {
-      k_force_cells<D, LAW, 2, 3><<<grid, kTile, 0, s>>>(a);
+      launch_cells<D, LAW, 1, 3>(a, grid, s);
     } else if (variant == 2) {
-      k_force_cells<D, LAW, 1, 3><<<grid, kTile, 0, s>>>(a);
+      launch_cells<D, LAW, 2, 2>(a, grid, s);
     } else {
-      k_force_cells<D, LAW, 2, 2><<<grid, kTile, 0, s>>>(a);
+      launch_cells<D, LAW, 1, 4>(a, grid, s);
     }
   }
 }

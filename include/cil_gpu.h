@@ -97,10 +97,10 @@ typedef struct cil_config {
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
   int32_t block_size;     /* threads per block of the force kernels: 0 or 256 */
   int32_t flags;          /* CIL_FLAG_* bits */
-  /* Verlet-list force kernel (skin mode, one thread per cell): list entries of each element in
-   * flight per thread (0 = 4; 1, 2, 4) and CTAs per SM it is compiled for (0 = 2; 2, 3).
-   * Supported pairs: (4, 2), (2, 3), (1, 3), (2, 2); 3D always runs (2, 2).
-   * cil_cuda_gb300/autotune.py picks them. */
+  /* Verlet-list force kernel (skin mode: one thread per cell, each warp's list entries taken as
+   * one flattened range): chunks of 32 entries in flight per warp (0 = 2; 1, 2) and CTAs per SM
+   * it is compiled for (0 = 3; 2, 3, 4). Supported pairs: (2, 3), (1, 3), (2, 2), (1, 4); 3D
+   * always runs (1, 2). cil_cuda_gb300/autotune.py picks them. */
   int32_t staging;
   int32_t occupancy;
   int32_t integrator;     /* CIL_INTEGRATOR_*: 0 = Euler */

@@ -14,7 +14,7 @@ def test_variants_agree_and_tuner_picks_one(gpu_lib):
     st = S.disk_colony(20000, p, seed=8)
     cap = 26000
     outs = []
-    for f, (stg, occ) in [(1.0, (2, 3)), (1.3, (1, 3)), (1.15, (4, 2)), (1.0, (2, 2))]:
+    for f, (stg, occ) in [(1.0, (2, 3)), (1.3, (1, 3)), (1.15, (2, 2)), (1.0, (1, 4))]:
         w = 0.0 if f == 1.0 else f * AT.needed_width([p], [st], 0.3)
         eng = gpu_lib.Engine([p], [cap], precision=gpu_lib.PREC_MIXED, rng=gpu_lib.RNG_PHILOX, seed=4, skin=0.3,
                              bin_width=w, staging=stg, occupancy=occ)
