@@ -260,12 +260,33 @@ def run_batched(G, device, steps, warmup, sched):
     dev_s = tm["total_ms"] * 1e-3
     psteps = (sum(n0) + sum(n1)) * steps
     sizes = np.array([len(s["sigma"]) for s in sts])
+    batch_ms = dev_s / steps * 1e3
+    # per colony: five colonies (smallest, quartiles, largest) run alone on their own random
+    # streams with the same settings, against their share of the batched step (by particles)
+    order = np.argsort(sizes)
+    picks = [int(order[int(round(q * (len(order) - 1)))]) for q in (0.0, 0.25, 0.5, 0.75, 1.0)]
+    tot = float(sum(n0) + sum(n1))
+    alone = []
+    for c in picks:
+        e1 = G.Engine([ps[c]], [caps[c]], precision=G.PREC_MIXED, rng=G.RNG_PHILOX, seed=11, device=device, skin=skin,
+                      rng_stream_base=c, **tune)
+        e1.upload(0, **sts[c])
+        if sched:
+            SS.install(e1)
+        e1.step(warmup)
+        e1.step(steps)
+        ms1 = e1.timings()["total_ms"] / steps
+        e1.close()
+        share = (n0[c] + n1[c]) / tot * batch_ms
+        alone.append({"colony": c, "cells": int(sizes[c]), "ms_per_step_alone": ms1,
+                      "ms_per_step_share_in_batch": share, "speedup_in_batch": ms1 / share})
     return {"value": psteps / dev_s, "unit": UNIT, "colonies": len(ps), "steps": steps,
             "particles": 2 * int(sum(n0)), "cells_min_median_max": [int(sizes.min()), int(np.median(sizes)),
                                                                     int(sizes.max())],
-            "ms_per_step": dev_s / steps * 1e3, "per_colony_ms_per_step": dev_s / steps * 1e3,
+            "ms_per_step": batch_ms, "ms_per_colony_step": batch_ms / len(ps),
+            "per_colony": alone,
             "form": "mixed precision, Verlet skin" + (" + learned scheduler" if sched else " 0.3 sigma"),
-            "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}":
+            "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}/{t['block_size']}":
                                                               round(t["ms_per_step"], 4) for t in trials},
             "graph_steps": gi["graph_steps"], "gpu_launches": tm["launches"]}
 
@@ -466,6 +487,43 @@ def run_cycle_small(G, device, steps=3000, warmup=3):
     return out
 
 
+def run_c1(G, device, steps, warmup, threads):
+    """The first configuration at its stated size: 4096 two-element cells (8192 particles), WCA LJ,
+    packing 0.8 in a periodic square (relaxed from uniform centres), D = 0.01, dt = 1e-4, no
+    division or apoptosis; `steps` steps on the GPU (plain FP64 and mixed with lists, device
+    time) and on the host cores (the oracle restatement on all threads and on one)."""
+    from cil_cuda_gb300 import synthetic as S
+    from oracle import oracle as O
+    p, st = S.config1(4096, seed=12345)
+    st = S.relax(p, st, device=device)
+    n = len(st["sigma"])
+    out = {"particles": 2 * n, "steps": steps, "unit": UNIT}
+    for name, prec, skin in (("plain_fp64", G.PREC_FP64, 0.0), ("mixed_skin_0.3", G.PREC_MIXED, 0.3)):
+        eng = G.Engine([p], [n], precision=prec, rng=G.RNG_PHILOX, seed=5, device=device, skin=skin)
+        eng.upload(0, **st)
+        eng.step(warmup)
+        eng.step(steps)
+        ms = eng.timings()["total_ms"]
+        eng.close()
+        out[name] = {"value": 2 * n * steps / (ms * 1e-3), "ms_per_step": ms / steps}
+    if not os.path.exists(O.LIB_PATH):
+        O.build()
+    for key, th in (("cpu_all_threads", threads), ("cpu_one_thread", 1)):
+        o = O.Oracle(p, n, 1, threads=th)
+        o.set_state(**st)
+        t0 = time.perf_counter()
+        k = 0
+        while k < steps and time.perf_counter() - t0 < 12.0:
+            o.step(50)
+            k += 50
+        wall = time.perf_counter() - t0
+        o.close()
+        out[key] = {"value": 2 * n * k / wall, "cores": th, "kind": "port",
+                    "sample": f"{k} Euler steps of the 8192-particle configuration, {wall:.1f} s"}
+    out["config"] = "4096 cells x 2 elements, WCA LJ eps=1, packing 0.8, periodic, D=0.01, dt=1e-4"
+    return out
+
+
 def cpu_baseline(p, st, threads: int, budget_s: float = 20.0):
     """The oracle (race-free OpenMP variant of the reference's step) on the host cores on
     the same 2M-particle state, as many whole steps as fit the budget (at least 1)."""
@@ -663,7 +721,7 @@ def main():
                   "speedup_vs_plain_fp64": value / plain_value},
         "skin_stats": skinf["skin"],
         "graph_steps": skinf["graphs"]["graph_steps"],
-        "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}":
+        "autotuned": tune, "autotune_trials_ms_per_step": {f"{t['bin_factor']}/{t['staging']}/{t['occupancy']}/{t['block_size']}":
                                                           round(t["ms_per_step"], 4) for t in trials},
         "phases_ms_per_step": {k: tm[k] / psteps_ph for k in ("rebuild_ms", "force_ms", "events_ms")},
         "plain_fp64_phases_ms_per_step": {k: tp[k] / plain_steps for k in ("rebuild_ms", "force_ms", "events_ms")},
@@ -706,6 +764,12 @@ def main():
         line["e2e"] = {"value": allreduce_sum(dist, e2e["value"]), "unit": UNIT,
                        "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
                        "frames": e2e["frames"], "frame_every": GTS, "gsd_file_bytes": e2e["file_bytes"]}
+    if args.only is None and not args.no_batched:
+        try:
+            line["first_configuration"] = run_c1(G, device, min(args.steps, 1000), args.warmup,
+                                                 os.cpu_count() or 1)
+        except G.CilError as e:
+            line["first_configuration"] = {"error": str(e)}
     if args.only is None and not args.no_frames:
         line["frame_output"] = run_frames(G, p, st, 3000, device, 7 + rank,
                                           mlp_skin if have_mlp else args.skin, have_mlp, tune)

@@ -90,6 +90,7 @@ class Config(C.Structure):
         ("staging", C.c_int32),
         ("occupancy", C.c_int32),
         ("integrator", C.c_int32),
+        ("rng_stream_base", C.c_int32),
     ]
 
 
@@ -516,16 +517,16 @@ class Engine:
     def __init__(self, params: list, caps: list, *, precision: int = PREC_FP64, rng: int = RNG_PHILOX,
                  seed: int = 0, device: int = 0, bin_width: float = 0.0, skin: float = 0.0,
                  graphs: bool = True, staging: int = 0, occupancy: int = 0, integrator: int = INTEGRATOR_EULER,
-                 deferred_status: bool = False):
+                 deferred_status: bool = False, rng_stream_base: int = 0, block_size: int = 0):
         self.L = lib()
         self.B = len(params)
         self.dim = params[0]["dim"]
         self.caps = [int(c) for c in caps]
         cfg = Config(dim=self.dim, force_law=params[0]["force_law"], precision=precision, rng_mode=rng,
                      seed=seed, num_colonies=self.B, device=device, bin_width=bin_width, skin=skin,
-                     block_size=0, flags=(0 if graphs else FLAG_NO_GRAPH) | (FLAG_DEFERRED_STATUS if deferred_status else 0),
+                     block_size=block_size, flags=(0 if graphs else FLAG_NO_GRAPH) | (FLAG_DEFERRED_STATUS if deferred_status else 0),
                      staging=staging,
-                     occupancy=occupancy, integrator=integrator)
+                     occupancy=occupancy, integrator=integrator, rng_stream_base=rng_stream_base)
         arr = (ColonyParams * self.B)(*[make_params(**p) for p in params])
         caps_a = np.array(self.caps, np.int32)
         h = C.c_void_p()

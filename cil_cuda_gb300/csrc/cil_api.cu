@@ -71,6 +71,7 @@ struct cil_handle {
   int grid_force = 0;
   int stiles = 0;      // tiles over the slot capacity
   int ptiles = 0;      // tiles over the slot pairs of the capacity (grid of the list force kernel)
+  int cell_block = 256;  // threads (cells) per block of the list force kernel
   int list_variant = 0;  // list force kernel: staging depth and CTAs per SM (cil_config.staging/occupancy)
   int nsm = 0;
   bool geometry_ready = false;
@@ -705,7 +706,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
       if (st != CIL_OK) return st;
     }
     // tile tables over the slots (list build) and the slot pairs (force kernel)
-    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs);
+    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs, 2 * h->cell_block);
     launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
     RebuildArgs ra = rebuild_args(h);
     ra.permute = 0;
@@ -744,7 +745,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
   if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
   fa.heun = heun;
-  launch_force_list(fa, h->D, h->cfg.force_law, h->ptiles, h->list_variant, h->stream);  // skin mode
+  launch_force_list(fa, h->D, h->cfg.force_law, h->ptiles, h->list_variant, h->cell_block, h->stream);  // skin mode
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
   return CIL_OK;
@@ -891,7 +892,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (cfg->rng_mode != CIL_RNG_PHILOX && cfg->rng_mode != CIL_RNG_DSFMT) return CIL_ERR_CONFIG;
   if (cfg->skin < 0.0 || (cfg->skin > 0.0 && cfg->precision != CIL_PREC_MIXED)) return CIL_ERR_CONFIG;
   if (cfg->skin > 0.0 && cfg->num_colonies > kMaxSkinColonies) return CIL_ERR_CONFIG;
-  if (cfg->block_size != 0 && cfg->block_size != kTile) return CIL_ERR_CONFIG;
+  // block size: the list force kernel of skin mode takes 128, 256 or 512 threads; the other
+  // kernels run 256
+  if (cfg->block_size != 0 && cfg->block_size != kTile &&
+      !(cfg->skin > 0.0 && (cfg->block_size == 128 || cfg->block_size == 512)))
+    return CIL_ERR_CONFIG;
   if (cfg->integrator != CIL_INTEGRATOR_EULER && cfg->integrator != CIL_INTEGRATOR_HEUN) return CIL_ERR_CONFIG;
   int list_variant = -1;
   {
@@ -946,6 +951,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.slot_cap = static_cast<int>(((want + kSlotAlign - 1) / kSlotAlign) * kSlotAlign);
     C.force_law = p.force_law;
     C.noise_per_cell = p.noise_per_cell;
+    C.rng_stream = static_cast<uint32_t>(cfg->rng_stream_base + c);
     C.divide = p.divide;
     C.nwalls = p.nwalls;
     for (int w = 0; w < 2; ++w) {
@@ -1065,8 +1071,9 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   for (int c = 0; c < h->B; ++c) h->ctiles += (h->hc[c].cap + kTile - 1) / kTile;
   h->stiles = 0;
   for (int c = 0; c < h->B; ++c) h->stiles += (h->cc[c].slot_cap + kTile - 1) / kTile;
+  h->cell_block = cfg->block_size ? cfg->block_size : kTile;
   h->ptiles = 0;
-  for (int c = 0; c < h->B; ++c) h->ptiles += (h->cc[c].slot_cap + 2 * kTile - 1) / (2 * kTile);
+  for (int c = 0; c < h->B; ++c) h->ptiles += (h->cc[c].slot_cap + 2 * h->cell_block - 1) / (2 * h->cell_block);
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);

@@ -46,22 +46,22 @@ __device__ __forceinline__ int block_excl_scan(int v, int *total) {
 }
 
 // tiles[c] = sum over colonies < c of ceil(count_c / per); tiles[B] = total.
-// which: 0 = nslot (per kTile), 1 = nlive (kTile), 2 = ncell (kCellTile), 3 = nslot in slot
-// pairs (2 kTile: the cell-major force kernel, one thread per pair). A second table (which2,
-// tiles2) can be written by the same launch.
-__device__ __forceinline__ int tile_count(const ColonyCounters &k, int which) {
+// which: 0 = nslot (per kTile), 1 = nlive (kTile), 2 = ncell (kCellTile), 3 = nslot in tiles of
+// `per3` slots (slot pairs of the cell-major force kernel: twice its block size). A second table
+// (which2, tiles2) can be written by the same launch.
+__device__ __forceinline__ int tile_count(const ColonyCounters &k, int which, int per3) {
   const int n = which == 1 ? k.nlive : (which == 2 ? k.ncell : k.nslot);
-  const int per = which == 2 ? kCellTile : (which == 3 ? 2 * kTile : kTile);
+  const int per = which == 2 ? kCellTile : (which == 3 ? per3 : kTile);
   return (n + per - 1) / per;
 }
 
 __global__ void k_tiles(const ColonyCounters *__restrict__ cnt, int B, int which, int *__restrict__ tiles,
-                        int which2, int *__restrict__ tiles2) {
+                        int which2, int *__restrict__ tiles2, int per3) {
   int carry = 0, carry2 = 0;
   for (int base = 0; base < B; base += kTile) {
     const int c = base + threadIdx.x;
-    const int v = c < B ? tile_count(cnt[c], which) : 0;
-    const int v2 = (tiles2 && c < B) ? tile_count(cnt[c], which2) : 0;
+    const int v = c < B ? tile_count(cnt[c], which, per3) : 0;
+    const int v2 = (tiles2 && c < B) ? tile_count(cnt[c], which2, per3) : 0;
     int total, total2;
     const int ex = block_excl_scan(v, &total);
     const int ex2 = block_excl_scan(v2, &total2);
@@ -459,8 +459,8 @@ __global__ void k_cell_finish(RebuildArgs a) {
 }  // namespace
 
 void launch_tiles(const ColonyConst *, ColonyCounters *cnt, int B, int which, int *tiles,
-                  cudaStream_t s, int which2, int *tiles2) {
-  k_tiles<<<1, kTile, 0, s>>>(cnt, B, which, tiles, which2, tiles2);
+                  cudaStream_t s, int which2, int *tiles2, int per2) {
+  k_tiles<<<1, kTile, 0, s>>>(cnt, B, which, tiles, which2, tiles2, per2);
 }
 
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
@@ -480,7 +480,7 @@ void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s) {
   if (!a.permute) return;  // the bin index (range + perm) is all a list rebuild needs
   if (a.skin == nullptr)   // bin order by element id: deterministic sums (FP64 / plain forms)
     k_sort_bins<<<(a.nscan * kScanItems + kTile - 1) / kTile, kTile, 0, s>>>(a, a.nscan * kScanItems);
-  k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live), 0, nullptr);
+  k_tiles<<<1, kTile, 0, s>>>(a.cnt, a.B, 1, const_cast<int *>(a.tiles_live), 0, nullptr, 2 * kTile);
   if (a.dim == 2)
     k_gather<2><<<grid_slots, kTile, 0, s>>>(a);
   else

@@ -205,15 +205,16 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
   }
 }
 
-// random axis and cycle length of a division in Philox mode
+// random axis and cycle length of a division in Philox mode (i: the mother's colony-local index;
+// the colony's stream in the fourth counter word)
 template <int D>
-__device__ void division_draws(const EventArgs &a, int g, double *dir_m, double *dir_d,
+__device__ void division_draws(const EventArgs &a, int i, double *dir_m, double *dir_d,
                                int &span_d, int &span_m, const ColonyConst &C) {
   // fast mode: FP32 draws (the FP64 placement arithmetic stays in place / divide_cell); the
   // axes are FP32 unit vectors widened exactly to FP64
-  const u32x4 r1 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv, 0u,
+  const u32x4 r1 = philox4x32_10(static_cast<uint32_t>(i), static_cast<uint32_t>(a.ts), kRngDiv, C.rng_stream,
                                  a.seed_lo, a.seed_hi);
-  const u32x4 r2 = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(a.ts), kRngDiv2, 0u,
+  const u32x4 r2 = philox4x32_10(static_cast<uint32_t>(i), static_cast<uint32_t>(a.ts), kRngDiv2, C.rng_stream,
                                  a.seed_lo, a.seed_hi);
   const float k24 = 5.9604644775390625e-08f;  // 2^-24
   if (D == 2) {
@@ -342,7 +343,7 @@ __global__ void __launch_bounds__(128) k_div_exec(EventArgs a_) {
     const int i = a.divq[C.cell_base + r];
     double dm[D], dd[D];
     int span_d, span_m;
-    division_draws<D>(a, C.cell_base + i, dm, dd, span_d, span_m, C);
+    division_draws<D>(a, i, dm, dd, span_d, span_m, C);
     divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
   }
 }
@@ -380,8 +381,8 @@ __device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, Colon
   for (int attempt = 0; attempt < 16; ++attempt) {
     if (need) {
       const u32x4 r = philox4x32_10(static_cast<uint32_t>(lane) | (static_cast<uint32_t>(attempt) << 24),
-                                    static_cast<uint32_t>(a.ts), kRngApoPick, static_cast<uint32_t>(c),
-                                    a.seed_lo, a.seed_hi);
+                                    static_cast<uint32_t>(a.ts), kRngApoPick, C.rng_stream, a.seed_lo,
+                                    a.seed_hi);
       const int x = static_cast<int>(uniform53(r.v[0], r.v[1]) * n1);
       v = x < n1 ? x : n1 - 1;
     }
@@ -461,8 +462,7 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
     // k-subset, the same distribution without a draw per cell
     int k = 0;
     if (C.apop_p > 0.0 && s_n1 > 0) {
-      const u32x4 r = philox4x32_10(static_cast<uint32_t>(c), static_cast<uint32_t>(a.ts), kRngApo, 0u,
-                                    a.seed_lo, a.seed_hi);
+      const u32x4 r = philox4x32_10(C.rng_stream, static_cast<uint32_t>(a.ts), kRngApo, 0u, a.seed_lo, a.seed_hi);
       const float nn = static_cast<float>(s_n1), p = static_cast<float>(C.apop_p);
       const float mean = nn * p;
       if (mean < 30.0f) {
@@ -510,8 +510,8 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
     for (int i = threadIdx.x; i < k; i += blockDim.x) {
       if (sd[i] == -1) {
         const u32x4 r = philox4x32_10(static_cast<uint32_t>(i) | (static_cast<uint32_t>(attempt) << 24),
-                                      static_cast<uint32_t>(a.ts), kRngApoPick, static_cast<uint32_t>(c),
-                                      a.seed_lo, a.seed_hi);
+                                      static_cast<uint32_t>(a.ts), kRngApoPick, C.rng_stream, a.seed_lo,
+                                      a.seed_hi);
         const int v = static_cast<int>(uniform53(r.v[0], r.v[1]) * n1);
         sd[i] = v < n1 ? v : n1 - 1;
       }

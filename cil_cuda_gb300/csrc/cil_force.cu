@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       for (int d = 0; d < D; ++d) F[d] += C.zeta[j] * a.noise[base + d];
     } else if (a.noise_mode == 1) {
       uint32_t w[4];
-      noise_words<D>(e, C.noise_per_cell, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
+      noise_words<D>(e - 2 * C.cell_base, C.noise_per_cell, noise_index(a.ts, a.heun), C.rng_stream, a.seed_lo, a.seed_hi, w);
       float n[4];
       box_muller(w[0], w[1], n[0], n[1]);
       if (D == 3) box_muller(w[2], w[3], n[2], n[3]);
@@ -289,7 +289,7 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
   if (a.noise_mode == 1) {
     // Box-Muller with the fast log / sincos
     uint32_t w[4];
-    noise_words<D>(e, C.noise_per_cell, noise_index(a.ts, a.heun), a.seed_lo, a.seed_hi, w);
+    noise_words<D>(e - 2 * C.cell_base, C.noise_per_cell, noise_index(a.ts, a.heun), C.rng_stream, a.seed_lo, a.seed_hi, w);
     const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
     for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
     // ---- passive noise
     if (a.noise_mode == 1) {
       uint32_t w[4];
-      noise_words<D>(e, C.noise_per_cell, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w);
+      noise_words<D>(e - 2 * C.cell_base, C.noise_per_cell, noise_index(ts, a.heun), C.rng_stream, a.seed_lo, a.seed_hi, w);
       const float amp = C.zeta_f[j] * C.amp_f;
 #pragma unroll
       for (int h = 0; h < (D + 1) / 2; ++h) {
@@ -960,8 +960,8 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
 // entries as one flattened range (cell_pairs). Per element it computes what k_force_list
 // computes: the spring, wall and noise terms are the same expressions, the pair terms are
 // summed in list order. UNROLL flattened chunks of 32 entries are in flight per warp.
-template <int D, int LAW, int UNROLL, int MINB>
-__global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) {
+template <int D, int LAW, int UNROLL, int MINB, int TILE>
+__global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   extern __shared__ __align__(16) unsigned char s_pairs[];
   __shared__ ColonyConst sC;
   __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
@@ -975,7 +975,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
   {
     const int *src = reinterpret_cast<const int *>(a.col + c);
     int *dst = reinterpret_cast<int *>(&sC);
-    for (int i = tid; i < static_cast<int>(sizeof(ColonyConst) / sizeof(int)); i += kTile) dst[i] = __ldg(src + i);
+    for (int i = tid; i < static_cast<int>(sizeof(ColonyConst) / sizeof(int)); i += TILE) dst[i] = __ldg(src + i);
     if (tid == 0) {
       s_dmax = 0u;
       s_smax = 0u;
@@ -988,7 +988,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
   const ColonyConst &C = sC;
   const int ts = __ldg(a.ts_dev);
   const size_t SS = a.SS;
-  const int s0 = C.slot_base + 2 * ((t - a.tiles[c]) * kTile + tid);
+  const int s0 = C.slot_base + 2 * ((t - a.tiles[c]) * TILE + tid);
   const bool used = s0 < C.slot_base + a.cnt[c].nslot;
   const int2 ee = used ? __ldg(reinterpret_cast<const int2 *>(a.eid + s0)) : make_int2(-1, -1);
   // fresh-pair contributions: one bit per slot; slot bases are 32-aligned and s0 is even, so
@@ -1099,7 +1099,8 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
     // ---- passive noise
     if (a.noise_mode == 1) {
       uint32_t w[2][4];
-      noise_words_cell<D>(g, C.noise_per_cell, noise_index(ts, a.heun), a.seed_lo, a.seed_hi, w[0], w[1]);
+      noise_words_cell<D>(g - C.cell_base, C.noise_per_cell, noise_index(ts, a.heun), C.rng_stream, a.seed_lo, a.seed_hi,
+                              w[0], w[1]);
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const float amp = C.zeta_f[j] * C.amp_f;
@@ -1233,7 +1234,7 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
       atomicMax(&s_smax, smax);
       atomicAdd(&s_ssum, ssum);
       __threadfence_block();
-      if (atomicAdd(&s_warps_done, 1) == kTile / 32 - 1) {
+      if (atomicAdd(&s_warps_done, 1) == TILE / 32 - 1) {
         __threadfence_block();
         atomicMax(&a.skin[c].maxdisp2, atomicOr(&s_dmax, 0u));
         if (a.sched) {
@@ -1245,49 +1246,62 @@ __global__ void __launch_bounds__(kTile, MINB) k_force_cells(const ForceArgs a) 
   }
 }
 
-template <int D, int LAW, int UNROLL, int MINB>
-void launch_cells(const ForceArgs &a, int grid, cudaStream_t s) {
-  constexpr int bytes = (kTile / 32) * pair_smem_warp<D>();
+template <int D, int LAW, int UNROLL, int MINB, int TILE>
+void launch_cells_t(const ForceArgs &a, int grid, cudaStream_t s) {
+  constexpr int bytes = (TILE / 32) * pair_smem_warp<D>();
   static bool attr_set = false;  // per instantiation; the attribute is per function
   if (!attr_set) {
-    cudaFuncSetAttribute(k_force_cells<D, LAW, UNROLL, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force_cells<D, LAW, UNROLL, MINB, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         bytes);
     attr_set = true;
   }
-  k_force_cells<D, LAW, UNROLL, MINB><<<grid, kTile, bytes, s>>>(a);
+  k_force_cells<D, LAW, UNROLL, MINB, TILE><<<grid, TILE, bytes, s>>>(a);
+}
+
+// MINB is the CTAs per SM at 256 threads; 128-thread blocks keep its threads per SM (hence the
+// register budget per thread), 512-thread blocks take at most as many threads per SM
+template <int D, int LAW, int UNROLL, int MINB>
+void launch_cells(const ForceArgs &a, int grid, int block, cudaStream_t s) {
+  if (block == 128)
+    launch_cells_t<D, LAW, UNROLL, 2 * MINB, 128>(a, grid, s);
+  else if (block == 512)
+    launch_cells_t<D, LAW, UNROLL, (MINB / 2 > 0 ? MINB / 2 : 1), 512>(a, grid, s);
+  else
+    launch_cells_t<D, LAW, UNROLL, MINB, 256>(a, grid, s);
 }
 
 template <int D, int LAW>
-void launch_list_dl(const ForceArgs &a, int grid, int variant, cudaStream_t s) {
+void launch_list_dl(const ForceArgs &a, int grid, int variant, int block, cudaStream_t s) {
   // cell-major slots, one thread per cell, the warp's list entries flattened; variants
-  // (chunks of 32 entries in flight per warp, CTAs per SM): 0 (2, 3), 1 (1, 3), 2 (2, 2),
-  // 3 (1, 4); 3D runs (1, 2)
+  // (chunks of 32 entries in flight per warp, CTAs per SM at 256 threads): 0 (2, 3), 1 (1, 3),
+  // 2 (2, 2), 3 (1, 4); 3D runs (1, 2); block: 128, 256 or 512 threads (cells per block)
   if constexpr (D == 3) {
     (void)variant;
-    launch_cells<D, LAW, 1, 2>(a, grid, s);
+    launch_cells<D, LAW, 1, 2>(a, grid, block, s);
   } else {
     if (variant == 0) {
-      launch_cells<D, LAW, 2, 3>(a, grid, s);
+      launch_cells<D, LAW, 2, 3>(a, grid, block, s);
     } else if (variant == 1) {
-      launch_cells<D, LAW, 1, 3>(a, grid, s);
+      launch_cells<D, LAW, 1, 3>(a, grid, block, s);
     } else if (variant == 2) {
-      launch_cells<D, LAW, 2, 2>(a, grid, s);
+      launch_cells<D, LAW, 2, 2>(a, grid, block, s);
     } else {
-      launch_cells<D, LAW, 1, 4>(a, grid, s);
+      launch_cells<D, LAW, 1, 4>(a, grid, block, s);
     }
   }
 }
 
 template <int D>
-void launch_list_d(const ForceArgs &a, int law, int grid, int variant, cudaStream_t s) {
+void launch_list_d(const ForceArgs &a, int law, int grid, int variant, int block, cudaStream_t s) {
   switch (law) {
     case CIL_FORCE_LJ_WCA:
-      launch_list_dl<D, CIL_FORCE_LJ_WCA>(a, grid, variant, s);
+      launch_list_dl<D, CIL_FORCE_LJ_WCA>(a, grid, variant, block, s);
       break;
     case CIL_FORCE_SOFTCORE:
-      launch_list_dl<D, CIL_FORCE_SOFTCORE>(a, grid, variant, s);
+      launch_list_dl<D, CIL_FORCE_SOFTCORE>(a, grid, variant, block, s);
       break;
     default:
-      launch_list_dl<D, CIL_FORCE_HERTZ>(a, grid, variant, s);
+      launch_list_dl<D, CIL_FORCE_HERTZ>(a, grid, variant, block, s);
       break;
   }
 }
@@ -1330,11 +1344,11 @@ void launch_d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s) {
 
 }  // namespace
 
-void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, cudaStream_t s) {
+void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, int block, cudaStream_t s) {
   if (dim == 2)
-    launch_list_d<2>(a, law, grid, variant, s);
+    launch_list_d<2>(a, law, grid, variant, block, s);
   else
-    launch_list_d<3>(a, law, grid, variant, s);
+    launch_list_d<3>(a, law, grid, variant, block, s);
 }
 
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block, cudaStream_t s) {

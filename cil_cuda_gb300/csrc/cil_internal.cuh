@@ -136,6 +136,7 @@ struct ColonyConst {
   int ctile_cap;     // cell tiles reserved
   int force_law;
   int noise_per_cell;
+  uint32_t rng_stream;  // the colony's Philox stream (cil_config.rng_stream_base + colony index)
   int divide;
   int nwalls;
   int wall_dir[2];
@@ -317,56 +318,62 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float &n0, fl
   n1 = r * s;
 }
 
-// Philox words of the passive noise of element e = 2 g + j at step ts.
-//   per element (noise_per_cell 0): in 2D one block keyed by the cell, (g, ts, noise, 1),
+// Philox words of the passive noise of element e = 2 g + j (colony-local ids) at step ts; the
+// fourth counter word carries the colony's random stream (stream << 1, plus 1 for the 2D
+// per-element blocks), so a colony draws the same numbers whether it runs alone or in a batch.
+//   per element (noise_per_cell 0): in 2D one block keyed by the cell, (g, ts, noise, 2 stream + 1),
 //     serves both of its elements: element j takes words 2j and 2j + 1 (one Box-Muller pair);
-//     in 3D each element takes a block of its own, (e, ts, noise, 0) (two pairs).
+//     in 3D each element takes a block of its own, (e, ts, noise, 2 stream) (two pairs).
 //   per cell (noise_per_cell 1, the reference's passiveWiener[cell][dim]): in 2D one block
-//     (g, ts / 2, noise, 0) serves two consecutive steps (the even step takes words 0-1, the odd
-//     one 2-3); in 3D each step takes the block (g, ts, noise, 0).
+//     (g, ts / 2, noise, 2 stream) serves two consecutive steps (the even step takes words 0-1,
+//     the odd one 2-3); in 3D each step takes the block (g, ts, noise, 2 stream).
 // Every force kernel draws through these two functions, so the forms agree on the noise.
 template <int D>
-__device__ __forceinline__ void noise_words(int e, int per_cell, int ts, uint32_t klo, uint32_t khi, uint32_t *w) {
+__device__ __forceinline__ void noise_words(int e, int per_cell, int ts, uint32_t stream, uint32_t klo, uint32_t khi,
+                                            uint32_t *w) {
   const uint32_t g = static_cast<uint32_t>(e) >> 1;
   if (D == 2) {
     const bool sel = per_cell ? (ts & 1) != 0 : (e & 1) != 0;
-    const u32x4 r = per_cell ? philox4x32_10(g, static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi)
-                             : philox4x32_10(g, static_cast<uint32_t>(ts), kRngNoise, 1u, klo, khi);
+    const u32x4 r = per_cell ? philox4x32_10(g, static_cast<uint32_t>(ts) >> 1, kRngNoise, stream << 1, klo, khi)
+                             : philox4x32_10(g, static_cast<uint32_t>(ts), kRngNoise, (stream << 1) | 1u, klo, khi);
     w[0] = sel ? r.v[2] : r.v[0];
     w[1] = sel ? r.v[3] : r.v[1];
   } else {
-    const u32x4 r = philox4x32_10(per_cell ? g : static_cast<uint32_t>(e), static_cast<uint32_t>(ts), kRngNoise, 0u,
-                                  klo, khi);
+    const u32x4 r = philox4x32_10(per_cell ? g : static_cast<uint32_t>(e), static_cast<uint32_t>(ts), kRngNoise,
+                                  stream << 1, klo, khi);
 #pragma unroll
     for (int q = 0; q < 4; ++q) w[q] = r.v[q];
   }
 }
 
-// The words of both elements of cell g at once (w0: back element, w1: front element), one
-// Philox block per cell and step in 2D; the same values noise_words gives each element.
+// The words of both elements of cell g (colony-local) at once (w0: back element, w1: front
+// element), one Philox block per cell and step in 2D; the same values noise_words gives each
+// element.
 template <int D>
-__device__ __forceinline__ void noise_words_cell(int g, int per_cell, int ts, uint32_t klo, uint32_t khi,
-                                                 uint32_t *w0, uint32_t *w1) {
+__device__ __forceinline__ void noise_words_cell(int g, int per_cell, int ts, uint32_t stream, uint32_t klo,
+                                                 uint32_t khi, uint32_t *w0, uint32_t *w1) {
   if (D == 2) {
     if (per_cell) {
-      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts) >> 1, kRngNoise, 0u, klo, khi);
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts) >> 1, kRngNoise, stream << 1,
+                                    klo, khi);
       const bool odd = (ts & 1) != 0;
       w0[0] = w1[0] = odd ? r.v[2] : r.v[0];
       w0[1] = w1[1] = odd ? r.v[3] : r.v[1];
     } else {
-      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts), kRngNoise, 1u, klo, khi);
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(g), static_cast<uint32_t>(ts), kRngNoise,
+                                    (stream << 1) | 1u, klo, khi);
       w0[0] = r.v[0];
       w0[1] = r.v[1];
       w1[0] = r.v[2];
       w1[1] = r.v[3];
     }
   } else if (per_cell) {
-    noise_words<D>(2 * g, 1, ts, klo, khi, w0);
+    noise_words<D>(2 * g, 1, ts, stream, klo, khi, w0);
 #pragma unroll
     for (int q = 0; q < 4; ++q) w1[q] = w0[q];
   } else {
-    noise_words<D>(2 * g, 0, ts, klo, khi, w0);
-    noise_words<D>(2 * g + 1, 0, ts, klo, khi, w1);
+    noise_words<D>(2 * g, 0, ts, stream, klo, khi, w0);
+    noise_words<D>(2 * g + 1, 0, ts, stream, klo, khi, w1);
   }
 }
 
@@ -642,8 +649,9 @@ __device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ w, co
 
 
 // ---------------------------------------------------------------- launchers (host side)
+// which2 / tiles2: a second table in the same launch; per2: slots per tile of a which2 = 3 table
 void launch_tiles(const ColonyConst *col, ColonyCounters *cnt, int B, int which, int *tiles,
-                  cudaStream_t s, int which2 = 0, int *tiles2 = nullptr);
+                  cudaStream_t s, int which2 = 0, int *tiles2 = nullptr, int per2 = 2 * kTile);
 void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s);
 // skin mode: slots re-sorted by cell (cells ranked by the bin of their back element, a cell's
 // elements in the slot pair slot_base + 2 rank, + 1; tombstones dropped); a.tiles_cell must be
@@ -651,7 +659,9 @@ void launch_rebuild(const RebuildArgs &a, int grid_slots, cudaStream_t s);
 void launch_cell_resort(const RebuildArgs &a, int grid_cells, cudaStream_t s);
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block,
                   cudaStream_t s);
-void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, cudaStream_t s);
+// skin mode: the cell kernel (one thread per slot pair); block = cells per block (128, 256, 512);
+// a.tiles must be the pair tiles of that block size
+void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, int block, cudaStream_t s);
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);

@@ -95,7 +95,8 @@ typedef struct cil_config {
   int32_t device;         /* CUDA device ordinal */
   double bin_width;       /* 0: cutoff of the largest element (+ skin); else at least this */
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
-  int32_t block_size;     /* threads per block of the force kernels: 0 or 256 */
+  int32_t block_size;     /* threads per block of the force kernels: 0 or 256; in skin mode the
+                           * list force kernel also takes 128 or 512 (cells per block) */
   int32_t flags;          /* CIL_FLAG_* bits */
   /* Verlet-list force kernel (skin mode: one thread per cell, each warp's list entries taken as
    * one flattened range): chunks of 32 entries in flight per warp (0 = 2; 1, 2) and CTAs per SM
@@ -104,6 +105,10 @@ typedef struct cil_config {
   int32_t staging;
   int32_t occupancy;
   int32_t integrator;     /* CIL_INTEGRATOR_*: 0 = Euler */
+  /* Philox mode: colony c draws from random stream rng_stream_base + c. The draws of a colony
+   * depend only on the seed, its stream and its own (colony-local) cell indices, so a colony
+   * run alone with rng_stream_base = c draws what it draws as colony c of a batch. */
+  int32_t rng_stream_base;
 } cil_config;
 
 /* cil_config.integrator. EULER is the reference's Euler (CIL.cu:1013-1020). HEUN is its
