@@ -43,7 +43,7 @@ GTS = 100  # steps per output frame in the end-to-end arm
 FRAME_CAP = 1_600_000  # cells: the frame-output leg grows the colony for 3000 steps
 # ncu summary of the dominant kernel on this workload; roofline.traffic is read from its
 # dram__bytes_read.sum + dram__bytes_write.sum rows (one launch, one capture)
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_force_list_2d_softcore_2M.md")
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_force_cells_2d_softcore_2M.md")
 WORKLOAD = ("2D colony growth, soft-core eps=5, 1M cells / 2M particles checkpoint, "
             "division+apoptosis on, dt=1e-4, 2048^2 periodic box")
 
@@ -730,7 +730,7 @@ def main():
                      "traffic_unit": "bytes per launch (ncu: dram__bytes_read.sum + dram__bytes_write.sum)",
                      "traffic_source": os.path.relpath(TRAFFIC_PROFILE, ROOT),
                      "peak_kind": peak_kind,
-                     "kernel": "k_force_list<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
+                     "kernel": "k_force_cells<2, softcore>", "algorithmic_bytes_per_element": bytes_per_elem,
                      "timed_on": f"{psteps_ph} individually launched steps (CUDA events around the force phase)",
                      "plain_fp64_kernel_GBps": 44 * nelem / plain_force_s / 1e9},
         "gpu_launches": skinf["timings"]["launches"],

@@ -580,280 +580,6 @@ __global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
   }
 }
 
-// Skin-mode step, one thread per slot, one tile per CTA. Each element walks its Verlet list
-// (entries: slot | neighbour-bin index << 27), loading a batch of entries and then the
-// batch's packed partners; a partner with w < 0 (fresh or dead) is skipped. Fresh elements
-// (ncnt 0) take their pair force from facc, written by k_fresh_pairs; normal elements add
-// the reactions found there. After the update the displacement guard |u - uref| > skin/2
-// requests a list rebuild for the next step; the tile's largest displacement and step
-// statistics go to the colony once.
-//
-// Every global load of the element (position, record, cycle, list reference, facc, list
-// length) is issued at the top, before any store, so that the compiler can keep them in
-// flight together; the colony's constants are staged in shared memory once per CTA.
-// BATCH list entries are in flight per thread ("staging depth"); MINB is the CTAs per SM the
-// kernel is compiled for (registers: 65536 / (256 * MINB)). Both are picked per handle.
-template <int D, int LAW, int BATCH, int MINB>
-__global__ void __launch_bounds__(kTile, MINB) k_force_list(const ForceArgs a) {
-  constexpr int kListBatch = BATCH;
-  __shared__ ColonyConst sC;
-  __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
-  __shared__ float s_ssum;
-  __shared__ float s_half2;
-  const int t = blockIdx.x;
-  if (t >= a.tiles[a.B]) return;  // uniform per block
-  const int tid = threadIdx.x;
-  const int c = colony_of_tile(a.tiles, a.B, t);
-  {
-    const int *src = reinterpret_cast<const int *>(a.col + c);
-    int *dst = reinterpret_cast<int *>(&sC);
-    for (int i = tid; i < static_cast<int>(sizeof(ColonyConst) / sizeof(int)); i += kTile) dst[i] = __ldg(src + i);
-    if (tid == 0) {
-      s_dmax = 0u;
-      s_smax = 0u;
-      s_ssum = 0.0f;
-      s_half2 = a.skin[c].half2;
-    }
-  }
-  __syncthreads();
-  const ColonyConst &C = sC;
-  const int ts = __ldg(a.ts_dev);
-  const size_t SS = a.SS;
-  const int s = C.slot_base + (t - a.tiles[c]) * kTile + tid;
-  const bool used = s < C.slot_base + a.cnt[c].nslot;
-  const int e = used ? __ldg(a.eid + s) : -1;
-  // fresh-pair contributions: one bit per slot, one word per warp (slot bases are 32-aligned)
-  const unsigned tword = a.ftouch[s >> 5];
-  const bool touched = (tword >> (s & 31)) & 1u;
-  float d2 = 0.0f, st2 = 0.0f;
-  if (e >= 0) {
-    // ---- loads
-    const int j = e & 1;
-    const int g = e >> 1;
-    const float4 pi = __ldg(a.pk + s);
-    const int sb = __ldg(a.sbin + s);
-    const int n = __ldg(a.ncnt + s);
-    const int ps = __ldg(a.slot_of + (e ^ 1));
-    int2 cy = make_int2(0, 0);
-    if (C.divide) cy = __ldg(a.cyc + s);
-    double xin[D];
-    float uref[D], fa[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      xin[d] = __ldg(a.x_in + d * SS + s);
-      fa[d] = touched ? a.facc[d * SS + s] : 0.0f;
-    }
-    if (D == 2) {
-      uref_unpack2(C.uq_inv, pi.z, uref);
-    } else {
-#pragma unroll
-      for (int d = 0; d < D; ++d) uref[d] = __ldg(a.uref + d * SS + s);
-    }
-    const float4 pp = __ldg(a.pk + ps);
-    const int sbp = __ldg(a.sbin + ps);
-    float ui[D], F[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) ui[d] = pk_c(pi, d);
-    const float si = fabsf(pi.w);
-    int bi[D], bp[D];
-    bin_decode<D>(C, sb, bi);
-    bin_decode<D>(C, sbp, bp);
-    // ---- intra-cell spring + motility (assigns)
-    {
-      float rij[D];
-      float r2 = 0.0f;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        float v = pk_c(pp, d) - ui[d];
-        if (C.single_bin) {
-          if (C.periodic[d]) v -= rintf(v * C.inv_bwf[d]) * C.bwf[d];
-        } else {
-          int db = bp[d] - bi[d];
-          if (C.periodic[d]) {
-            if (db > (C.ns[d] >> 1)) db -= C.ns[d];
-            if (db < -(C.ns[d] >> 1)) db += C.ns[d];
-          }
-          v += static_cast<float>(db) * C.bwf[d];
-        }
-        rij[d] = (j == 0) ? v : -v;  // r1 - r0
-        r2 += rij[d] * rij[d];
-      }
-#pragma unroll
-      for (int d = 0; d < D; ++d) F[d] = 0.0f;
-      if (r2 > 0.0f) {
-        const float rinv = rsqrtf(r2);
-        float rest = C.rest0_f;
-        if (C.divide) {
-          const int span = cy.y - cy.x;
-          float frac = span > 0 ? __fdividef(static_cast<float>(ts - cy.x), static_cast<float>(span)) : 1.0f;
-          frac = fminf(1.0f, fmaxf(0.0f, frac));
-          rest = C.rest0_f + (C.rest1_f - C.rest0_f) * frac;
-        }
-        const float sp = C.kappa_f * (r2 * rinv - rest);
-        const float coef = ((j == 0) ? (sp - C.motility_f[0]) : (C.motility_f[1] - sp)) * rinv;
-#pragma unroll
-        for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
-      }
-    }
-    // ---- walls
-    if (C.nwalls > 0) {
-      const float z = static_cast<float>(bi[D - 1]) * C.bwf[D - 1] + ui[D - 1];
-      const float rad = 0.5f * si;
-      for (int w = 0; w < C.nwalls; ++w) {
-        const float dir = static_cast<float>(C.wall_dir[w]);
-        const float delta = rad - dir * (z - C.wall_pos_f[w]);
-        if (delta > 0.0f) F[D - 1] += dir * C.wall_E_f * delta * (delta * rsqrtf(delta));
-      }
-    }
-    // ---- passive noise
-    if (a.noise_mode == 1) {
-      uint32_t w[4];
-      noise_words<D>(e - 2 * C.cell_base, C.noise_per_cell, noise_index(ts, a.heun), C.rng_stream, a.seed_lo, a.seed_hi, w);
-      const float amp = C.zeta_f[j] * C.amp_f;
-#pragma unroll
-      for (int h = 0; h < (D + 1) / 2; ++h) {
-        const float u1 = static_cast<float>((w[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;
-        const float u2 = static_cast<float>(w[2 * h + 1] >> 8) * 5.9604644775390625e-08f;
-        const float m = fmaxf(-2.0f * __logf(u1), 0.0f);
-        const float rad = m * rsqrtf(fmaxf(m, 1e-30f));  // sqrt(m), 0 when u1 == 1
-        float sn, cs;
-        __sincosf(6.2831853071795865f * u2, &sn, &cs);
-        F[2 * h] += amp * rad * cs;
-        if (2 * h + 1 < D) F[2 * h + 1] += amp * rad * sn;
-      }
-    } else if (a.noise_mode == 2) {
-      const size_t base = static_cast<size_t>(C.noise_per_cell ? g : e) * D;
-#pragma unroll
-      for (int d = 0; d < D; ++d) F[d] += C.zeta_f[j] * static_cast<float>(__ldg(a.noise + base + d));
-    }
-    // ---- pair forces from the list, kListBatch entries in flight at a time
-    const float eps = C.eps_f, rcs = C.rcs_f;
-    float tab[D][3];  // partner offset from this element for bin offset -1, 0, +1
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      tab[d][0] = -C.bwf[d] - ui[d];
-      tab[d][1] = -ui[d];
-      tab[d][2] = C.bwf[d] - ui[d];
-    }
-    const int *lp = a.nbr + s;
-    for (int k0 = 0; k0 < n; k0 += kListBatch) {
-      unsigned ent[kListBatch];
-      float4 pj[kListBatch];
-#pragma unroll
-      for (int q = 0; q < kListBatch; ++q) {
-        ent[q] = k0 + q < n ? static_cast<unsigned>(__ldg(lp)) : 0xffffffffu;
-        lp += SS;
-      }
-#pragma unroll
-      for (int q = 0; q < kListBatch; ++q)
-        pj[q] = ent[q] != 0xffffffffu ? __ldg(a.pk + (ent[q] & ((1u << kListSlotBits) - 1u)))
-                                      : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-#pragma unroll
-      for (int q = 0; q < kListBatch; ++q) {
-        const unsigned code = ent[q] >> kListSlotBits;
-        float dx[D];
-        float r2 = 0.0f;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          const unsigned k = (code >> (2 * d)) & 3u;
-          dx[d] = pk_c(pj[q], d) + (k == 0u ? tab[d][0] : (k == 1u ? tab[d][1] : tab[d][2]));
-          r2 += dx[d] * dx[d];
-        }
-        const float f0 = pair_f0_fast<LAW>(r2, si, pj[q].w, eps, rcs, pj[q].w > 0.0f);
-#pragma unroll
-        for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
-      }
-    }
-#pragma unroll
-    for (int d = 0; d < D; ++d) F[d] += fa[d];
-    // ---- checks, update (one FP64 add per axis, integer wrap tests), stores
-    bool finite = true;
-#pragma unroll
-    for (int d = 0; d < D; ++d) finite = finite && isfinite(F[d]);
-    if (!finite) atomicOr(&a.cnt[c].err, kErrNan);
-    if (a.frc) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) a.frc[d * SS + s] = static_cast<double>(F[d]);
-    }
-    if (touched) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) a.facc[d * SS + s] = 0.0f;
-    }
-    if (a.integrate) {
-      const float temp = a.heun ? 0.5f * C.temp_f[j] : C.temp_f[j];
-      bool inside = true;
-      // 2D: z carries the packed list reference to the next record
-      float4 pn = make_float4(0.0f, 0.0f, D == 2 ? pi.z : 0.0f, pi.w);
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const float dxf = temp * F[d];
-        double xn = xin[d] + f2d_exact(dxf);
-        long long xb = __double_as_longlong(xn);
-        const long long lb = __double_as_longlong(C.box[d]);
-        if (C.periodic[d]) {
-          if (xb < 0) {
-            xn = (xb & 0x7fffffffffffffffll) ? xn + C.box[d] : 0.0;
-            xb = __double_as_longlong(xn);
-          }
-          if (xb >= lb) xn -= C.box[d];
-        } else {
-          inside = inside && xb >= 0 && xb < lb;
-        }
-        a.x_out[d * SS + s] = xn;
-        const float un = ui[d] + dxf;
-        pk_set(pn, d, un);
-        const float dr = un - uref[d];
-        d2 += dr * dr;
-        st2 += dxf * dxf;
-      }
-      a.pk_next[s] = pn;
-      if (!inside) atomicOr(&a.cnt[c].err, kErrBox);
-      if (D == 2) {
-        // guard with the fixed-point rounding allowed for: trips no later than |u - uref| > skin/2
-        const float h = fmaxf(sqrtf(s_half2) - (C.uq_inv[0] + C.uq_inv[1]), 0.0f);
-        if (d2 > h * h) atomicOr(&a.skin[c].need, 1);
-      } else if (d2 > s_half2) {
-        atomicOr(&a.skin[c].need, 1);
-      }
-      if (a.vel) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          const double v = static_cast<double>(F[d] * C.mu_f[j]);
-          a.vel[d * SS + s] = a.heun == 2 ? 0.5 * ((a.vel_prev ? a.vel_prev : a.vel)[d * SS + s] + v) : v;
-        }
-      }
-    }
-  } else if (used && a.integrate) {
-    // tombstone: the next record must keep w < 0 too, or the lists of others would see the
-    // stale record of two steps ago in the other buffer
-    a.pk_next[s] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-  }
-  __syncwarp();  // every lane has read the touch word
-  if (tword != 0u && (tid & 31) == 0) a.ftouch[s >> 5] = 0u;
-  if (a.integrate) {
-    // displacement statistics: warp reductions, shared atomics, one global atomic each
-    const unsigned dmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    const float stp = sqrtf(st2);
-    const unsigned smax = __reduce_max_sync(0xffffffffu, __float_as_uint(stp));
-    float ssum = stp;
-#pragma unroll
-    for (int q = 16; q > 0; q >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, q);
-    if ((tid & 31) == 0) {
-      atomicMax(&s_dmax, dmax);
-      atomicMax(&s_smax, smax);
-      atomicAdd(&s_ssum, ssum);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      atomicMax(&a.skin[c].maxdisp2, s_dmax);
-      if (a.sched) {
-        atomicMax(reinterpret_cast<unsigned *>(&a.sched[c].step_max), s_smax);
-        atomicAdd(&a.sched[c].step_sum, s_ssum);
-      }
-    }
-  }
-}
-
 // Per-warp shared memory of the cell kernel's pair pass: the records of the warp's 64 elements,
 // and for one segment of kPairSeg flattened list entries the owner of each entry (element | list
 // index << 6) and its pair force.
@@ -957,9 +683,10 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
 // tombstones. So a thread reads both records, the cycle and the FP64 positions of its cell
 // with coalesced loads, evaluates the intra-cell spring once and draws the noise of both
 // elements from one Philox block (2D); the warp then evaluates its 64 elements' Verlet-list
-// entries as one flattened range (cell_pairs). Per element it computes what k_force_list
-// computes: the spring, wall and noise terms are the same expressions, the pair terms are
-// summed in list order. UNROLL flattened chunks of 32 entries are in flight per warp.
+// entries as one flattened range (cell_pairs). Per element: the spring, wall and noise terms
+// are the expressions of the other force kernels, the pair terms are summed in list order, and
+// pairs with fresh elements (created or moved by a division since the last list build, in no
+// list) arrive through facc from k_fresh_pairs. UNROLL flattened chunks of 32 entries are in flight per warp.
 template <int D, int LAW, int UNROLL, int MINB, int TILE>
 __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   extern __shared__ __align__(16) unsigned char s_pairs[];

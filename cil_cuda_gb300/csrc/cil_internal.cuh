@@ -508,7 +508,7 @@ struct ForceArgs {
   const int2 *range;
   const int *slot_of;
   // skin mode (null otherwise)
-  const int *tiles;        // tiles over nslot (k_force_list) or over slot pairs (k_force_cells)
+  const int *tiles;        // skin mode: tiles over slot pairs (k_force_cells)
   ColonySkin *skin;
   const int *nbr;          // Verlet lists [kListCap][SS]
   const int *ncnt;
