@@ -664,7 +664,9 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
                                              timed && pass == 0 ? pool_event(h, e0 + 1) : nullptr);
     if (st != CIL_OK) return st;
   }
-  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream);
+  const bool philox = h->cfg.rng_mode != CIL_RNG_DSFMT;
+  // the step counter, and in Philox mode the cell tile table of the device events
+  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream, h->d_cnt, h->B, philox ? h->d_tiles_cell : nullptr);
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
   h->ts += 1;
   if (h->cfg.rng_mode == CIL_RNG_DSFMT) {
@@ -672,9 +674,8 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     if (st != CIL_OK) return st;
     h->launches += 2;
   } else {
-    launch_tiles(h->d_col, h->d_cnt, h->B, 2, h->d_tiles_cell, h->stream);
     launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
-    h->launches += 8;
+    h->launches += 3;
   }
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
   CUDA_TRY(h, cudaGetLastError());
@@ -699,14 +700,21 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     // re-sorts the slots on a fixed schedule and after uploads
     const bool permute =
         h->need_exact || h->lists_stale || (first && (h->ts % h->permute_period) == 0);
-    launch_skin_begin(skin_args(h, permute ? 1 : 0), h->stream);
+    // the rebuild decision; without a re-sort the same launch writes the tile tables over the
+    // slots (list build) and the slot pairs (force kernel)
+    SkinArgs sb = skin_args(h, permute ? 1 : 0);
+    if (!permute) {
+      sb.tiles_used_out = h->d_tiles_used;
+      sb.tiles_pairs_out = h->d_tiles_pairs;
+      sb.pair_tile = 2 * h->cell_block;
+    }
+    launch_skin_begin(sb, h->stream);
     if (permute) {
       // cell-major re-sort; every colony then rebuilds its bin index and lists (host request)
       st = do_cell_resort(h);
       if (st != CIL_OK) return st;
+      launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs, 2 * h->cell_block);
     }
-    // tile tables over the slots (list build) and the slot pairs (force kernel)
-    launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs, 2 * h->cell_block);
     launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
     RebuildArgs ra = rebuild_args(h);
     ra.permute = 0;
@@ -718,7 +726,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
-    h->launches += permute ? 17 : 8;
+    h->launches += permute ? 17 : 7;
   } else {
     // the second half step of a Heun step reads the first half's velocities: carried through
     // the re-sort (only when velocities are written, i.e. the last step of a cil_step call)

@@ -269,37 +269,10 @@ __global__ void __launch_bounds__(kTile) k_div_count(EventArgs a_) {
   }
 }
 
-__global__ void __launch_bounds__(kTile) k_div_scan(EventArgs a) {
-  const int c = blockIdx.x;
-  const ColonyConst &C = a.col[c];
-  const int t0 = a.tiles_cell[c], t1 = a.tiles_cell[c + 1];
-  int carry = 0;
-  for (int base = t0; base < t1; base += kTile) {
-    const int t = base + threadIdx.x;
-    const int v = t < t1 ? a.tile_count[t] : 0;
-    int total;
-    const int ex = block_excl_scan_ev(v, &total);
-    if (t < t1) a.tile_off[t] = carry + ex;
-    carry += total;
-  }
-  if (threadIdx.x == 0) {
-    ColonyCounters &K = a.cnt[c];
-    // room for the cells and for their two element slots each (skin mode appends daughters
-    // behind removed elements until the next slot re-sort)
-    const int room_cells = C.cell_cap - K.ncell;
-    const int room_slots = (C.slot_cap - K.nslot) / 2;
-    const int room = room_cells < room_slots ? room_cells : room_slots;
-    int allowed = carry < room ? carry : room;
-    if (allowed < 0) allowed = 0;
-    if (allowed < carry) K.err |= kErrCap;
-    K.ndiv_step = carry;
-    K.ndiv_allowed = allowed;
-    K.ndead = 0;
-  }
-}
-
 // due cells of the step, ranked in cell order: the first ndiv_allowed go to the colony's
-// division queue (the placement work runs in k_div_exec, so this scan stays light)
+// division queue. Each block sums its colony's tile counts itself (those before its tile give
+// its offset, all of them the colony's total for the capacity check), so no scan pass runs in
+// between; the block of the colony's first tile records the step's counts.
 __global__ void __launch_bounds__(kTile) k_div_rank(EventArgs a_) {
   const EventArgs &a = a_;
   const int ts = *a.ts_dev;
@@ -307,9 +280,32 @@ __global__ void __launch_bounds__(kTile) k_div_rank(EventArgs a_) {
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles_cell, a.B, t);
     const ColonyConst &C = a.col[c];
-    const ColonyCounters &K = a.cnt[c];
+    ColonyCounters &K = a.cnt[c];
     const int n = K.ncell;
-    const int i0 = (t - a.tiles_cell[c]) * kCellTile + threadIdx.x * kCellItems;
+    const int tc0 = a.tiles_cell[c], tc1 = a.tiles_cell[c + 1];
+    int before = 0, all = 0;
+    for (int u = tc0 + static_cast<int>(threadIdx.x); u < tc1; u += kTile) {
+      const int v = a.tile_count[u];
+      all += v;
+      before += u < t ? v : 0;
+    }
+    int off, cnt_all;
+    block_excl_scan_ev(before, &off);
+    block_excl_scan_ev(all, &cnt_all);
+    // room for the cells and for their two element slots each (skin mode appends daughters
+    // behind removed elements until the next slot re-sort)
+    const int room_cells = C.cell_cap - n;
+    const int room_slots = (C.slot_cap - K.nslot) / 2;
+    const int room = room_cells < room_slots ? room_cells : room_slots;
+    int allowed = cnt_all < room ? cnt_all : room;
+    if (allowed < 0) allowed = 0;
+    if (t == tc0 && threadIdx.x == 0) {
+      if (allowed < cnt_all) K.err |= kErrCap;
+      K.ndiv_step = cnt_all;
+      K.ndiv_allowed = allowed;
+      K.ndead = 0;
+    }
+    const int i0 = (t - tc0) * kCellTile + threadIdx.x * kCellItems;
     bool due[kCellItems];
     int cnt = 0;
 #pragma unroll
@@ -318,33 +314,13 @@ __global__ void __launch_bounds__(kTile) k_div_rank(EventArgs a_) {
       cnt += due[q] ? 1 : 0;
     }
     int tot;
-    int rank = a.tile_off[t] + block_excl_scan_ev(cnt, &tot);
-    const int allowed = K.ndiv_allowed;
+    int rank = off + block_excl_scan_ev(cnt, &tot);
 #pragma unroll
     for (int q = 0; q < kCellItems; ++q) {
       if (!due[q]) continue;
       if (rank < allowed) a.divq[C.cell_base + rank] = i0 + q;
       ++rank;
     }
-  }
-}
-
-// one thread per division of the queue: draws, FP64 placement of the four elements, new
-// cycles; daughters take cells n + rank and slots nslot + 2 rank
-template <int D>
-__global__ void __launch_bounds__(128) k_div_exec(EventArgs a_) {
-  EventArgs a = a_;
-  a.ts = *a_.ts_dev;
-  const int c = blockIdx.y;
-  const ColonyConst &C = a.col[c];
-  const ColonyCounters &K = a.cnt[c];
-  const int nd = K.ndiv_allowed, n = K.ncell, nslot = K.nslot;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nd; r += gridDim.x * blockDim.x) {
-    const int i = a.divq[C.cell_base + r];
-    double dm[D], dd[D];
-    int span_d, span_m;
-    division_draws<D>(a, i, dm, dd, span_d, span_m, C);
-    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
   }
 }
 
@@ -369,7 +345,7 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
 }
 
 // one block per colony: commit the divisions, then swap-with-last removal of the dead
-// warp-level path of k_apo_apply for k <= 32 deaths among n1 cells: distinct uniform picks
+// warp-level path of apo_colony for k <= 32 deaths among n1 cells: distinct uniform picks
 // (redrawn while duplicated, at most 16 rounds), tombstones, then the live cells of the tail
 // [n1 - k, n1) move into the holes below it in ascending order (removeCell's swap-with-last,
 // Colony.cpp:365-399, for a sorted set of victims)
@@ -443,12 +419,12 @@ __device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, Colon
   }
 }
 
-__global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
-  EventArgs a = a_;
-  a.ts = *a_.ts_dev;
+// The step's apoptoses of colony c by one block (any multiple of 32 threads), after its
+// divisions: commits the divisions' counts, draws the number of deaths, picks distinct victims,
+// leaves tombstones and moves tail cells into the holes.
+__device__ void apo_colony(const EventArgs &a, int c, int D) {
   __shared__ int sd[kDeadCap];
   __shared__ int s_n1, s_k;
-  const int c = blockIdx.x;
   const ColonyConst &C = a.col[c];
   ColonyCounters &K = a.cnt[c];
   if (threadIdx.x == 0) {
@@ -622,6 +598,28 @@ __global__ void __launch_bounds__(1024) k_apo_apply(EventArgs a_, int D) {
   }
 }
 
+// One block per colony: the divisions of the queue, one thread each (draws, FP64 placement of
+// the four elements, new cycles; daughters take cells n + rank and slots nslot + 2 rank), then
+// the colony's apoptoses (apo_colony) once every division is placed.
+template <int D>
+__global__ void __launch_bounds__(kTile) k_events_exec(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
+  const int c = blockIdx.x;
+  const ColonyConst &C = a.col[c];
+  const ColonyCounters &K = a.cnt[c];
+  const int nd = K.ndiv_allowed, n = K.ncell, nslot = K.nslot;
+  for (int r = threadIdx.x; r < nd; r += blockDim.x) {
+    const int i = a.divq[C.cell_base + r];
+    double dm[D], dd[D];
+    int span_d, span_m;
+    division_draws<D>(a, i, dm, dd, span_d, span_m, C);
+    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
+  }
+  __syncthreads();  // every division is placed, and visible to the whole block
+  apo_colony(a, c, D);
+}
+
 // oracle mode: divisions in the host's order with host-drawn axes and cycle lengths
 template <int D>
 __global__ void k_div_list(EventArgs a_, int c, int n0, int ndiv, const int *mothers, const double *dirs,
@@ -760,29 +758,43 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
     for (int q = 0; q < 4; ++q) partials[blockIdx.x * 4 + q] = red[q][0];
 }
 
-// the device step counter moves past the force step (before the events read it)
-// (skin mode: also clears the next step's any-rebuild flag)
-__global__ void k_advance_ts(int *ts, int *any_rebuild) {
-  if (any_rebuild) any_rebuild[(*ts + 1) & 1] = 0;
-  *ts += 1;
+// the device step counter moves past the force step (before the events read it); skin mode
+// also clears the next step's any-rebuild flag. With tiles_cell, the same block writes the tile
+// table over the cells that the event kernels of the step read (the cell counts do not change
+// between the force pass and the events).
+__global__ void __launch_bounds__(kTile) k_step_end(int *ts, int *any_rebuild, const ColonyCounters *cnt, int B,
+                                                    int *tiles_cell) {
+  if (threadIdx.x == 0) {
+    if (any_rebuild) any_rebuild[(*ts + 1) & 1] = 0;
+    *ts += 1;
+  }
+  if (!tiles_cell) return;  // uniform
+  int carry = 0;
+  for (int base = 0; base < B; base += kTile) {
+    const int c = base + static_cast<int>(threadIdx.x);
+    const int v = c < B ? (cnt[c].ncell + kCellTile - 1) / kCellTile : 0;
+    int total;
+    const int ex = block_excl_scan_ev(v, &total);
+    if (c < B) tiles_cell[c] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) tiles_cell[B] = carry;
 }
 
 }  // namespace
 
-void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s) {
-  k_advance_ts<<<1, 1, 0, s>>>(ts_dev, any_rebuild);
+void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s, const ColonyCounters *cnt, int B,
+                       int *tiles_cell) {
+  k_step_end<<<1, kTile, 0, s>>>(ts_dev, any_rebuild, cnt, B, tiles_cell);
 }
 
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
   k_div_count<<<grid_cells, kTile, 0, s>>>(a);
-  k_div_scan<<<a.B, kTile, 0, s>>>(a);
   k_div_rank<<<grid_cells, kTile, 0, s>>>(a);
-  const dim3 g(8, a.B);
   if (dim == 2)
-    k_div_exec<2><<<g, 128, 0, s>>>(a);
+    k_events_exec<2><<<a.B, kTile, 0, s>>>(a);
   else
-    k_div_exec<3><<<g, 128, 0, s>>>(a);
-  k_apo_apply<<<a.B, 1024, 0, s>>>(a, dim);
+    k_events_exec<3><<<a.B, kTile, 0, s>>>(a);
 }
 
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,

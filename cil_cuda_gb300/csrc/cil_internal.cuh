@@ -599,6 +599,11 @@ struct SkinArgs {
   int grid;                // blocks of the fresh-pair kernel
   const int *ts_dev;       // device step counter
   int *any_rebuild;        // [2]: some colony rebuilds at step ts (index ts & 1), or null
+  // k_skin_begin also writes the step's tile tables over the slots and the slot pairs when these
+  // are set (pair tiles of pair_tile slots), or null
+  int *tiles_used_out;
+  int *tiles_pairs_out;
+  int pair_tile;
   // learned scheduler (null: skin and cadence stay as set)
   const float *mlp;
   int use_interval;
@@ -666,7 +671,10 @@ void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
 void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
-void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s);
+// the device step counter advance; with tiles_cell also the tile table over the cells of the
+// step's events
+void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s, const ColonyCounters *cnt = nullptr, int B = 0,
+                       int *tiles_cell = nullptr);
 int mlp_param_count();
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,

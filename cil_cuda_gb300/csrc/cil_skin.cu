@@ -121,6 +121,49 @@ __device__ __forceinline__ int skin_begin_colony(const SkinArgs &a, int c) {
 // one warp per colony: the decision, then (rebuilding colony, scheduler installed) the
 // network on the colony's features sets the skin of the new lists and the cadence
 __global__ void k_skin_begin(SkinArgs a) {
+  if (blockIdx.x == 0 && a.tiles_used_out) {
+    // the step's tile tables (slots: kTile per tile; slot pairs: pair_tile slots per tile),
+    // block 0, before any thread returns
+    __shared__ int ws[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int carry0 = 0, carry1 = 0;
+    for (int base = 0; base < a.B; base += blockDim.x) {
+      const int cc = base + static_cast<int>(threadIdx.x);
+      const int ns = cc < a.B ? a.cnt[cc].nslot : 0;
+      int v[2] = {(ns + kTile - 1) / kTile, (ns + a.pair_tile - 1) / a.pair_tile};
+      int inc[2] = {v[0], v[1]};
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int t = __shfl_up_sync(0xffffffffu, inc[q], o);
+          if (lane >= o) inc[q] += t;
+        }
+      if (lane == 31) {
+        ws[0][wid] = inc[0];
+        ws[1][wid] = inc[1];
+      }
+      __syncthreads();
+      int before[2] = {0, 0}, tot[2] = {0, 0};
+      for (int w = 0; w < nw; ++w)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          before[q] += w < wid ? ws[q][w] : 0;
+          tot[q] += ws[q][w];
+        }
+      if (cc < a.B) {
+        a.tiles_used_out[cc] = carry0 + before[0] + inc[0] - v[0];
+        a.tiles_pairs_out[cc] = carry1 + before[1] + inc[1] - v[1];
+      }
+      carry0 += tot[0];
+      carry1 += tot[1];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      a.tiles_used_out[a.B] = carry0;
+      a.tiles_pairs_out[a.B] = carry1;
+    }
+  }
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= a.B) return;  // uniform per warp
   const int lane = threadIdx.x & 31;
