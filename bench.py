@@ -226,8 +226,11 @@ def run_channel(G, device, steps, warmup):
         eng.close()
         out[name] = (n0 + n1) * k / (tm["total_ms"] * 1e-3)
         out[name + "_ms_per_step"] = tm["total_ms"] / k
+        if name == "mixed_skin":
+            phases = {key: v / k for key, v in tm.items() if key.endswith("_ms") and key != "total_ms"}
     return {"value": out["mixed_skin"], "unit": UNIT, "particles": 2 * len(st["sigma"]), "steps": steps,
             "forms": out, "speedup_vs_plain_fp64": out["mixed_skin"] / out["plain_fp64"],
+            "mixed_skin_phase_ms_per_step": phases,
             "config": "3D Hertz E=100, walls z=0 and 20, periodic 1024^2, phi=0.6 slab, dt=5e-5, D=0.005, division on"}
 
 
@@ -607,7 +610,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
     ap.add_argument("--staging", type=int, default=0, help="profile: list entries in flight (0: default)")
     ap.add_argument("--occupancy", type=int, default=0, help="profile: CTAs per SM of the list kernel (0: default)")
-    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd", "profile"],
+    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd", "profile", "channel"],
                     default=None, help="run one form only (profiling); profile: the headline form alone, "
                                        "launched step by step, nothing else")
     args = ap.parse_args()
@@ -622,6 +625,9 @@ def main():
     if not os.path.exists(G.LIB_PATH):
         from cil_cuda_gb300 import build
         build.build()
+    if args.only == "channel":
+        print(json.dumps(run_channel(G, device, args.steps, args.warmup)))
+        return 0
     if args.only == "cycle_small":
         print(json.dumps(run_cycle_small(G, device, steps=args.steps, warmup=args.warmup)))
         return 0

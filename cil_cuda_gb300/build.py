@@ -23,6 +23,9 @@ SOURCES = ["cil_api.cu", "cil_bins.cu", "cil_force.cu", "cil_events.cu", "cil_sk
 # flush FP32 denormals (no denormal fix-up code around the reciprocal square roots of the FP32
 # pair laws; the FP64 paths are unaffected)
 EXTRA = {"cil_cycle.cu": ["--fmad=false"], "cil_force.cu": ["-ftz=true"]}
+# sources compiled a second time into another object with extra defines: the force kernels'
+# 3D instances build in parallel with the 2D ones
+SECOND = {"cil_force.cu": ("cil_force3.o", ["-DCIL_FORCE_DIM=3"])}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -46,8 +49,10 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     extra = ["-Xptxas", "-v"] if ptxas_info else []
     procs = []
     objs = []
-    for src in SOURCES:
-        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+    units = [(src, os.path.splitext(src)[0] + ".o", []) for src in SOURCES]
+    units += [(src, o, d) for src, (o, d) in SECOND.items()]
+    for src, obj_name, defines in units:
+        obj = os.path.join(OUT, obj_name)
         objs.append(obj)
         src_path = os.path.join(CSRC, src)
         deps = [src_path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
@@ -55,8 +60,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         if (not ptxas_info and os.path.exists(obj)
                 and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
             continue
-        cmd = [nvcc(), *flags(extra), *EXTRA.get(src, []), "-c", src_path, "-o", obj]
-        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+        cmd = [nvcc(), *flags(extra), *EXTRA.get(src, []), *defines, "-c", src_path, "-o", obj]
+        procs.append((obj_name, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     failed = []
     for src, p in procs:
         out, _ = p.communicate()

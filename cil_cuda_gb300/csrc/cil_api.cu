@@ -913,6 +913,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     if (st == 1 && oc == 3) list_variant = 1;
     if (st == 2 && oc == 2) list_variant = 2;
     if (st == 1 && oc == 4) list_variant = 3;
+    if (st == 1 && oc == 2) list_variant = 4;
     if (list_variant < 0) return CIL_ERR_CONFIG;
   }
   auto *h = new cil_handle();

@@ -580,29 +580,89 @@ __global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
   }
 }
 
-// Per-warp shared memory of the cell kernel's pair pass: the records of the warp's 64 elements,
-// and for one segment of kPairSeg flattened list entries the owner of each entry (element | list
-// index << 6) and its pair force.
-constexpr int kPairSeg = 512;
-template <int D>
+// Asynchronous global -> shared copies (cp.async, sm_80 and later): issued early, waited for
+// where the data is used, so their latency overlaps the work in between. Each thread waits
+// for its own copies; a __syncwarp after the wait publishes them to the warp.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Per-warp shared memory of the cell kernel, for segments of SEG flattened list entries:
+//   records of the warp's 64 elements             64 x 16 B
+//   FP64 positions of the 64 elements (staged)    64 x D x 8 B, axis-major
+//   list entries of the segment                   SEG x 4 B
+//   owner (element of the warp) of each entry     SEG x 1 B
+//   pair force of each entry                      SEG x D x 4 B
+// SEG is the largest multiple of 32 (at most 1024) with which MINB blocks of TILE threads fit
+// in the 228 KB of shared memory of an SM, leaving 2 KB per block for the static variables
+// and the per-block reservation.
+template <int D, int MINB, int TILE>
+__host__ __device__ constexpr int pair_seg() {
+  return ((233472 / MINB - 2048) / (TILE / 32) - (64 * 16 + 64 * D * 8)) / (5 + 4 * D) / 32 * 32 > 1024
+             ? 1024
+             : ((233472 / MINB - 2048) / (TILE / 32) - (64 * 16 + 64 * D * 8)) / (5 + 4 * D) / 32 * 32;
+}
+template <int D, int SEG>
 __host__ __device__ constexpr int pair_smem_warp() {
-  return 64 * 16 + kPairSeg * 2 + kPairSeg * D * 4;
+  return 64 * 16 + 64 * D * 8 + SEG * (4 + 1 + 4 * D);
+}
+template <int D, int SEG>
+struct PairSmem {
+  float4 *rec;
+  double *x;
+  unsigned *ent;
+  unsigned char *own;
+  float *c;
+  __device__ __forceinline__ explicit PairSmem(unsigned char *w)
+      : rec(reinterpret_cast<float4 *>(w)),
+        x(reinterpret_cast<double *>(w + 64 * 16)),
+        ent(reinterpret_cast<unsigned *>(w + 64 * 16 + 64 * D * 8)),
+        own(w + 64 * 16 + 64 * D * 8 + SEG * 4),
+        c(reinterpret_cast<float *>(w + 64 * 16 + 64 * D * 8 + SEG * 5)) {}
+};
+
+// The warp's flattened list range: element 2 lane owns [st0, st1), element 2 lane + 1 owns
+// [st1, en1) of the T entries of the warp's 64 elements.
+struct PairRange {
+  int st0, st1, en1, T;
+};
+
+// One segment [S, E) of the flattened range: every lane writes the owners of its entries and
+// starts the copies of the entries themselves (list entry k of element i of the warp sits at
+// nbr[k * SS + sw0 + i]; 32-bit offsets from the warp's first slot: k < 64 and, in skin mode,
+// SS < 2^26, checked when the handle is created, so k * SS + i < 2^32).
+template <int D, int SEG>
+__device__ __forceinline__ void pairs_segment_start(const ForceArgs &a, int sw0, const PairRange &R, int S,
+                                                    const PairSmem<D, SEG> &sm) {
+  const int lane = threadIdx.x & 31;
+  const int E = min(R.T, S + SEG);
+  const int *lw = a.nbr + sw0;
+  const unsigned ss = static_cast<unsigned>(a.SS);
+  for (int f = max(R.st0, S); f < min(R.st1, E); ++f) {
+    sm.own[f - S] = static_cast<unsigned char>(2 * lane);
+    cp_async4(sm.ent + (f - S), lw + (static_cast<unsigned>(f - R.st0) * ss + static_cast<unsigned>(2 * lane)));
+  }
+  for (int f = max(R.st1, S); f < min(R.en1, E); ++f) {
+    sm.own[f - S] = static_cast<unsigned char>(2 * lane + 1);
+    cp_async4(sm.ent + (f - S), lw + (static_cast<unsigned>(f - R.st1) * ss + static_cast<unsigned>(2 * lane + 1)));
+  }
 }
 
-// The pair forces of a warp's 32 cells (64 elements), whole warp: the elements' Verlet-list
-// entries are taken as one flattened range (element by element, each list in order), so every
-// lane evaluates a real entry whatever the lengths of the lists; each lane then adds its two
-// elements' pair forces in list order (the sums do not depend on scheduling). Every lane calls
-// it; lanes without a live cell pass n = (0, 0). sw0: the warp's first slot.
-template <int D, int LAW, int UNROLL>
-__device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst &C, int sw0, int2 nn,
-                                           const float4 *pr, float (*F)[D], unsigned char *wsm) {
+// The start of the pair pass, right after the cell's own loads: the records of the warp's 64
+// elements into shared memory, the flattened range, and the copies of the first segment.
+// Every lane calls it; lanes without a live cell pass n = (0, 0).
+template <int D, int SEG>
+__device__ __forceinline__ PairRange pairs_begin(const ForceArgs &a, int sw0, int2 nn, const float4 *pr,
+                                                 const PairSmem<D, SEG> &sm) {
   const int lane = threadIdx.x & 31;
-  float4 *s_rec = reinterpret_cast<float4 *>(wsm);
-  unsigned short *s_own = reinterpret_cast<unsigned short *>(wsm + 64 * 16);
-  float *s_c = reinterpret_cast<float *>(wsm + 64 * 16 + kPairSeg * 2);
-  s_rec[2 * lane] = pr[0];
-  s_rec[2 * lane + 1] = pr[1];
+  sm.rec[2 * lane] = pr[0];
+  sm.rec[2 * lane + 1] = pr[1];
   const int cnt = nn.x + nn.y;
   int inc = cnt;
 #pragma unroll
@@ -610,26 +670,36 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
     const int t = __shfl_up_sync(0xffffffffu, inc, o);
     if (lane >= o) inc += t;
   }
-  const int T = __shfl_sync(0xffffffffu, inc, 31);
-  const int st0 = inc - cnt, st1 = st0 + nn.x, en1 = inc;
-  // list entry k of element i of the warp sits at nbr[k * SS + sw0 + i]: 32-bit offsets from the
-  // warp's first slot (k < 64 and, in skin mode, SS < 2^26: list entries address slots in 26
-  // bits, checked when the handle is created, so k * SS + i < 2^32)
-  const int *lw = a.nbr + sw0;
-  const unsigned ss = static_cast<unsigned>(a.SS);
+  PairRange R;
+  R.T = __shfl_sync(0xffffffffu, inc, 31);
+  R.st0 = inc - cnt;
+  R.st1 = R.st0 + nn.x;
+  R.en1 = inc;
+  pairs_segment_start<D, SEG>(a, sw0, R, 0, sm);
+  return R;
+}
+
+// The pair forces of a warp's 32 cells (64 elements), whole warp: the elements' Verlet-list
+// entries are taken as one flattened range (element by element, each list in order), so every
+// lane evaluates a real entry whatever the lengths of the lists; each lane then adds its two
+// elements' pair forces in list order (the sums do not depend on scheduling). UNROLL chunks of
+// 32 entries have their partner records in flight together.
+template <int D, int LAW, int UNROLL, int SEG>
+__device__ __forceinline__ void pairs_finish(const ForceArgs &a, const ColonyConst &C, int sw0, const PairRange &R,
+                                             float (*F)[D], const PairSmem<D, SEG> &sm) {
+  const int lane = threadIdx.x & 31;
   const float eps = C.eps_f, rcs = C.rcs_f;
   float bw[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) bw[d] = C.bwf[d];
-  for (int S = 0; S < T; S += kPairSeg) {  // uniform
-    const int E = min(T, S + kPairSeg);
-    __syncwarp();  // the last segment's sums are read; the records are written
-    // owner of every entry of the segment
-    for (int f = max(st0, S); f < min(st1, E); ++f)
-      s_own[f - S] = static_cast<unsigned short>((2 * lane) | ((f - st0) << 6));
-    for (int f = max(st1, S); f < min(en1, E); ++f)
-      s_own[f - S] = static_cast<unsigned short>((2 * lane + 1) | ((f - st1) << 6));
-    __syncwarp();
+  for (int S = 0; S < R.T; S += SEG) {  // uniform
+    const int E = min(R.T, S + SEG);
+    if (S > 0) {
+      __syncwarp();  // the last segment's sums are read
+      pairs_segment_start<D, SEG>(a, sw0, R, S, sm);
+    }
+    cp_async_wait_all();
+    __syncwarp();  // every lane's copies (entries, records, owners) are visible to the warp
     for (int base = S; base < E; base += 32 * UNROLL) {  // uniform
       unsigned ent[UNROLL];
       int own[UNROLL];
@@ -637,10 +707,8 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const int f = base + 32 * u + lane;
-        own[u] = f < E ? s_own[f - S] : -1;
-        ent[u] = own[u] >= 0
-                     ? __ldg(lw + (static_cast<unsigned>(own[u] >> 6) * ss + static_cast<unsigned>(own[u] & 63)))
-                     : 0u;
+        own[u] = f < E ? sm.own[f - S] : -1;
+        ent[u] = f < E ? sm.ent[f - S] : 0u;
       }
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u)
@@ -649,7 +717,7 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         if (own[u] < 0) continue;
-        const float4 me = s_rec[own[u] & 63];
+        const float4 me = sm.rec[own[u]];
         const unsigned code = ent[u] >> kListSlotBits;
         float dx[D];
         float r2 = 0.0f;
@@ -661,20 +729,21 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
           r2 += dx[d] * dx[d];
         }
         const float f0 = pair_f0_fast<LAW>(r2, fabsf(me.w), pj[u].w, eps, rcs, pj[u].w > 0.0f);
-        float *cf = s_c + (base + 32 * u + lane - S) * D;
+        float *cf = sm.c + (base + 32 * u + lane - S) * D;
 #pragma unroll
         for (int d = 0; d < D; ++d) cf[d] = f0 * dx[d];
       }
     }
     __syncwarp();
     // each element adds its entries of the segment, in list order
-    for (int f = max(st0, S); f < min(st1, E); ++f)
+    for (int f = max(R.st0, S); f < min(R.st1, E); ++f)
 #pragma unroll
-      for (int d = 0; d < D; ++d) F[0][d] += s_c[(f - S) * D + d];
-    for (int f = max(st1, S); f < min(en1, E); ++f)
+      for (int d = 0; d < D; ++d) F[0][d] += sm.c[(f - S) * D + d];
+    for (int f = max(R.st1, S); f < min(R.en1, E); ++f)
 #pragma unroll
-      for (int d = 0; d < D; ++d) F[1][d] += s_c[(f - S) * D + d];
+      for (int d = 0; d < D; ++d) F[1][d] += sm.c[(f - S) * D + d];
   }
+  cp_async_wait_all();  // a warp without list entries has waited for nothing yet
 }
 
 // Skin-mode step over cell-major slots, one thread per cell. Between slot re-sorts a cell's
@@ -682,13 +751,17 @@ __device__ __forceinline__ void cell_pairs(const ForceArgs &a, const ColonyConst
 // the re-sort ranks cells, division appends daughters as slot pairs, apoptosis leaves pairs of
 // tombstones. So a thread reads both records, the cycle and the FP64 positions of its cell
 // with coalesced loads, evaluates the intra-cell spring once and draws the noise of both
-// elements from one Philox block (2D); the warp then evaluates its 64 elements' Verlet-list
-// entries as one flattened range (cell_pairs). Per element: the spring, wall and noise terms
-// are the expressions of the other force kernels, the pair terms are summed in list order, and
-// pairs with fresh elements (created or moved by a division since the last list build, in no
-// list) arrive through facc from k_fresh_pairs. UNROLL flattened chunks of 32 entries are in flight per warp.
+// elements from one Philox block (2D); the warp evaluates its 64 elements' Verlet-list
+// entries as one flattened range (pairs_begin / pairs_finish). The list entries and the FP64
+// positions are copied into shared memory asynchronously at the start, so they arrive while
+// the spring, wall and noise terms are evaluated; in the pair pass only the partner records
+// are gathered (UNROLL chunks of 32 entries in flight per warp). Per element: the spring, wall
+// and noise terms are the expressions of the other force kernels, the pair terms are summed in
+// list order, and pairs with fresh elements (created or moved by a division since the last
+// list build, in no list) arrive through facc from k_fresh_pairs.
 template <int D, int LAW, int UNROLL, int MINB, int TILE>
 __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
+  constexpr int SEG = pair_seg<D, MINB, TILE>();
   extern __shared__ __align__(16) unsigned char s_pairs[];
   __shared__ ColonyConst sC;
   __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
@@ -716,51 +789,43 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   const int ts = __ldg(a.ts_dev);
   const size_t SS = a.SS;
   const int s0 = C.slot_base + 2 * ((t - a.tiles[c]) * TILE + tid);
-  const bool used = s0 < C.slot_base + a.cnt[c].nslot;
-  const int2 ee = used ? __ldg(reinterpret_cast<const int2 *>(a.eid + s0)) : make_int2(-1, -1);
+  // every load of the cell is issued at once, guarded by the colony's slot capacity only (the
+  // memory is there; what lies past the used slots is not used), so none waits on another
+  const bool incap = s0 < C.slot_base + C.slot_cap;
+  int2 ee = make_int2(-1, -1), sb = make_int2(0, 0), nn = make_int2(0, 0), cy = make_int2(0, 0);
+  float4 pr[2] = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+  if (incap) {
+    ee = __ldg(reinterpret_cast<const int2 *>(a.eid + s0));
+    pr[0] = __ldg(a.pk + s0);
+    pr[1] = __ldg(a.pk + s0 + 1);
+    sb = __ldg(reinterpret_cast<const int2 *>(a.sbin + s0));
+    nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
+    if (C.divide) cy = __ldg(a.cyc + s0);
+  }
   // fresh-pair contributions: one bit per slot; slot bases are 32-aligned and s0 is even, so
   // both bits of the cell sit in one word (16 cells per word)
   const unsigned tword = a.ftouch[s0 >> 5];
   const unsigned tbits = (tword >> (s0 & 31)) & 3u;
+  const bool used = s0 < C.slot_base + a.cnt[c].nslot;
+  const bool live = used && ee.x >= 0;
+  if (!live) nn = make_int2(0, 0);
   float d2 = 0.0f, st2[2] = {0.0f, 0.0f};
-  const bool live = ee.x >= 0;
-  // ---- loads and the per-element terms (live cells; every load before the first store)
-  float4 pr[2] = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
-  int2 nn = make_int2(0, 0);
-  double xin[2][D];
-  float uref[2][D], F[2][D], fa[2][D], ui[2][D];
+  // ---- the pair pass starts: the warp's records, its flattened list range, and asynchronous
+  // copies of its list entries and of the cells' FP64 positions, which arrive while the
+  // per-element terms below are evaluated
+  PairSmem<D, SEG> sm(s_pairs + (tid >> 5) * pair_smem_warp<D, SEG>());
+  const int sw0 = s0 - 2 * (tid & 31);
+  const PairRange R = pairs_begin<D, SEG>(a, sw0, nn, pr, sm);
+  if (live) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    F[0][d] = F[1][d] = 0.0f;
-    fa[0][d] = fa[1][d] = 0.0f;
+    for (int d = 0; d < D; ++d) cp_async16(sm.x + d * 64 + 2 * (tid & 31), a.x_in + d * SS + s0);
   }
+  // ---- the per-element terms (live cells)
+  float F[2][D], ui[2][D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) F[0][d] = F[1][d] = 0.0f;
   if (live) {
     const int g = ee.x >> 1;
-    pr[0] = __ldg(a.pk + s0);
-    pr[1] = __ldg(a.pk + s0 + 1);
-    const int2 sb = __ldg(reinterpret_cast<const int2 *>(a.sbin + s0));
-    nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
-    int2 cy = make_int2(0, 0);
-    if (C.divide) cy = __ldg(a.cyc + s0);
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      const double2 xv = __ldg(reinterpret_cast<const double2 *>(a.x_in + d * SS + s0));
-      xin[0][d] = xv.x;
-      xin[1][d] = xv.y;
-      if (tbits & 1u) fa[0][d] = a.facc[d * SS + s0];
-      if (tbits & 2u) fa[1][d] = a.facc[d * SS + s0 + 1];
-    }
-    if (D == 2) {
-      uref_unpack2(C.uq_inv, pr[0].z, uref[0]);
-      uref_unpack2(C.uq_inv, pr[1].z, uref[1]);
-    } else {
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const float2 uv = __ldg(reinterpret_cast<const float2 *>(a.uref + d * SS + s0));
-        uref[0][d] = uv.x;
-        uref[1][d] = uv.y;
-      }
-    }
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       ui[0][d] = pk_c(pr[0], d);
@@ -853,12 +918,30 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
     }
   }
   // ---- pair forces from the Verlet lists: the whole warp
-  cell_pairs<D, LAW, UNROLL>(a, C, s0 - 2 * (tid & 31), nn, pr, F, s_pairs + (tid >> 5) * pair_smem_warp<D>());
+  pairs_finish<D, LAW, UNROLL, SEG>(a, C, sw0, R, F, sm);
   if (live) {
+    double xin[2][D];
+    float uref[2][D];
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int d = 0; d < D; ++d) {
+      // this lane's own staged copies (complete: pairs_finish waited for them)
+      const double2 xv = *reinterpret_cast<const double2 *>(sm.x + d * 64 + 2 * (tid & 31));
+      xin[0][d] = xv.x;
+      xin[1][d] = xv.y;
+      if (tbits & 1u) F[0][d] += a.facc[d * SS + s0];
+      if (tbits & 2u) F[1][d] += a.facc[d * SS + s0 + 1];
+    }
+    if (D == 2) {
+      uref_unpack2(C.uq_inv, pr[0].z, uref[0]);
+      uref_unpack2(C.uq_inv, pr[1].z, uref[1]);
+    } else {
 #pragma unroll
-      for (int d = 0; d < D; ++d) F[j][d] += fa[j][d];
+      for (int d = 0; d < D; ++d) {
+        const float2 uv = __ldg(reinterpret_cast<const float2 *>(a.uref + d * SS + s0));
+        uref[0][d] = uv.x;
+        uref[1][d] = uv.y;
+      }
+    }
     // ---- checks, update (one FP64 add per axis, integer wrap tests), stores
     bool finite = true;
 #pragma unroll
@@ -975,7 +1058,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
 
 template <int D, int LAW, int UNROLL, int MINB, int TILE>
 void launch_cells_t(const ForceArgs &a, int grid, cudaStream_t s) {
-  constexpr int bytes = (TILE / 32) * pair_smem_warp<D>();
+  constexpr int bytes = (TILE / 32) * pair_smem_warp<D, pair_seg<D, MINB, TILE>()>();
   static bool attr_set = false;  // per instantiation; the attribute is per function
   if (!attr_set) {
     cudaFuncSetAttribute(k_force_cells<D, LAW, UNROLL, MINB, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1001,20 +1084,17 @@ template <int D, int LAW>
 void launch_list_dl(const ForceArgs &a, int grid, int variant, int block, cudaStream_t s) {
   // cell-major slots, one thread per cell, the warp's list entries flattened; variants
   // (chunks of 32 entries in flight per warp, CTAs per SM at 256 threads): 0 (2, 3), 1 (1, 3),
-  // 2 (2, 2), 3 (1, 4); 3D runs (1, 2); block: 128, 256 or 512 threads (cells per block)
-  if constexpr (D == 3) {
-    (void)variant;
-    launch_cells<D, LAW, 1, 2>(a, grid, block, s);
+  // 2 (2, 2), 3 (1, 4), 4 (1, 2); block: 128, 256 or 512 threads (cells per block)
+  if (variant == 0) {
+    launch_cells<D, LAW, 2, 3>(a, grid, block, s);
+  } else if (variant == 1) {
+    launch_cells<D, LAW, 1, 3>(a, grid, block, s);
+  } else if (variant == 2) {
+    launch_cells<D, LAW, 2, 2>(a, grid, block, s);
+  } else if (variant == 3) {
+    launch_cells<D, LAW, 1, 4>(a, grid, block, s);
   } else {
-    if (variant == 0) {
-      launch_cells<D, LAW, 2, 3>(a, grid, block, s);
-    } else if (variant == 1) {
-      launch_cells<D, LAW, 1, 3>(a, grid, block, s);
-    } else if (variant == 2) {
-      launch_cells<D, LAW, 2, 2>(a, grid, block, s);
-    } else {
-      launch_cells<D, LAW, 1, 4>(a, grid, block, s);
-    }
+    launch_cells<D, LAW, 1, 2>(a, grid, block, s);
   }
 }
 
@@ -1071,11 +1151,25 @@ void launch_d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s) {
 
 }  // namespace
 
+// This file is compiled twice: with CIL_FORCE_DIM=3 it holds the 3D kernels alone, otherwise
+// the 2D kernels and the dispatch (two translation units that build in parallel).
+#if defined(CIL_FORCE_DIM) && CIL_FORCE_DIM == 3
+void launch_force_list_3d(const ForceArgs &a, int law, int grid, int variant, int block, cudaStream_t s) {
+  launch_list_d<3>(a, law, grid, variant, block, s);
+}
+
+void launch_force_3d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s) {
+  launch_d<3>(a, law, prec, grid, s);
+}
+#else
+void launch_force_list_3d(const ForceArgs &a, int law, int grid, int variant, int block, cudaStream_t s);
+void launch_force_3d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s);
+
 void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int variant, int block, cudaStream_t s) {
   if (dim == 2)
     launch_list_d<2>(a, law, grid, variant, block, s);
   else
-    launch_list_d<3>(a, law, grid, variant, block, s);
+    launch_force_list_3d(a, law, grid, variant, block, s);
 }
 
 void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int block, cudaStream_t s) {
@@ -1083,7 +1177,8 @@ void launch_force(const ForceArgs &a, int dim, int law, int prec, int grid, int 
   if (dim == 2)
     launch_d<2>(a, law, prec, grid, s);
   else
-    launch_d<3>(a, law, prec, grid, s);
+    launch_force_3d(a, law, prec, grid, s);
 }
+#endif
 
 }  // namespace cil
