@@ -627,6 +627,13 @@ struct PairSmem {
         c(reinterpret_cast<float *>(w + 64 * 16 + 64 * D * 8 + SEG * 5)) {}
 };
 
+// Bin-origin offsets by list-entry code (2 bits per axis: bin offset + 1), per block:
+// entry k holds ((k >> 2d) & 3) - 1 times the bin width on axis d (exact products).
+template <int D>
+constexpr int kOffStride = D == 2 ? 2 : 4;
+template <int D>
+constexpr int kOffCodes = D == 2 ? 16 : 64;
+
 // The warp's flattened list range: element 2 lane owns [st0, st1), element 2 lane + 1 owns
 // [st1, en1) of the T entries of the warp's 64 elements.
 struct PairRange {
@@ -686,12 +693,9 @@ __device__ __forceinline__ PairRange pairs_begin(const ForceArgs &a, int sw0, in
 // 32 entries have their partner records in flight together.
 template <int D, int LAW, int UNROLL, int SEG>
 __device__ __forceinline__ void pairs_finish(const ForceArgs &a, const ColonyConst &C, int sw0, const PairRange &R,
-                                             float (*F)[D], const PairSmem<D, SEG> &sm) {
+                                             float (*F)[D], const PairSmem<D, SEG> &sm, const float *s_off) {
   const int lane = threadIdx.x & 31;
   const float eps = C.eps_f, rcs = C.rcs_f;
-  float bw[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) bw[d] = C.bwf[d];
   for (int S = 0; S < R.T; S += SEG) {  // uniform
     const int E = min(R.T, S + SEG);
     if (S > 0) {
@@ -718,14 +722,13 @@ __device__ __forceinline__ void pairs_finish(const ForceArgs &a, const ColonyCon
       for (int u = 0; u < UNROLL; ++u) {
         if (own[u] < 0) continue;
         const float4 me = sm.rec[own[u]];
-        const unsigned code = ent[u] >> kListSlotBits;
+        // the offset between the two home bins' origins, from the entry's bin offset code
+        const float *ov = s_off + (ent[u] >> kListSlotBits) * kOffStride<D>;
         float dx[D];
         float r2 = 0.0f;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          // bin offset code k in {0, 1, 2}: (k - 1) as a float, exactly, without a conversion
-          const float off = __int_as_float(0x4B000000 | ((code >> (2 * d)) & 3u)) - 8388609.0f;
-          dx[d] = pk_c(pj[u], d) + (off * bw[d] - pk_c(me, d));
+          dx[d] = pk_c(pj[u], d) + (ov[d] - pk_c(me, d));
           r2 += dx[d] * dx[d];
         }
         const float f0 = pair_f0_fast<LAW>(r2, fabsf(me.w), pj[u].w, eps, rcs, pj[u].w > 0.0f);
@@ -768,6 +771,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   __shared__ float s_ssum;
   __shared__ float s_half2;
   __shared__ int s_warps_done;
+  __shared__ __align__(16) float s_off[kOffCodes<D> * kOffStride<D>];
   const int t = blockIdx.x;
   if (t >= a.tiles[a.B]) return;  // uniform per block (tiles over slot pairs)
   const int tid = threadIdx.x;
@@ -776,6 +780,11 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
     const int *src = reinterpret_cast<const int *>(a.col + c);
     int *dst = reinterpret_cast<int *>(&sC);
     for (int i = tid; i < static_cast<int>(sizeof(ColonyConst) / sizeof(int)); i += TILE) dst[i] = __ldg(src + i);
+    if (tid < kOffCodes<D>) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        s_off[tid * kOffStride<D> + d] = static_cast<float>(((tid >> (2 * d)) & 3) - 1) * __ldg(&a.col[c].bwf[d]);
+    }
     if (tid == 0) {
       s_dmax = 0u;
       s_smax = 0u;
@@ -918,7 +927,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
     }
   }
   // ---- pair forces from the Verlet lists: the whole warp
-  pairs_finish<D, LAW, UNROLL, SEG>(a, C, sw0, R, F, sm);
+  pairs_finish<D, LAW, UNROLL, SEG>(a, C, sw0, R, F, sm, s_off);
   if (live) {
     double xin[2][D];
     float uref[2][D];

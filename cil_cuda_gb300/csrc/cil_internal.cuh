@@ -431,18 +431,21 @@ __device__ __forceinline__ float pair_f0_fast(float r2, float si, float sj, floa
     const float sr6 = sr2 * sr2 * sr2;
     const float f0 = (sr6 - 2.0f * sr6 * sr6) * ir2 * (24.0f * eps);
     return in ? f0 : 0.0f;
+  } else if (LAW == CIL_FORCE_SOFTCORE) {
+    // -eps (1 - r/rc)^2 / r from one reciprocal square root: q = 1 / (r rc) gives
+    // r / rc = r2 q and 1 / r = rc q
+    const float rc2 = rc * rc;
+    const bool in = ok && r2 < rc2 && r2 > 0.0f;
+    const float q = rsqrtf(r2 * rc2);
+    const float w = 1.0f - r2 * q;
+    return in ? -eps * w * w * (rc * q) : 0.0f;
   } else {
     const bool in = ok && r2 < rc * rc && r2 > 0.0f;
     const float rinv = rsqrtf(r2);
     const float r = r2 * rinv;
-    if (LAW == CIL_FORCE_SOFTCORE) {
-      const float w = 1.0f - __fdividef(r, rc);
-      return in ? -eps * w * w * rinv : 0.0f;
-    } else {
-      const float delta = fmaxf(sij - r, 0.0f);
-      const float sq = delta * rsqrtf(fmaxf(delta, 1e-30f));
-      return in ? -eps * delta * sq * rinv : 0.0f;
-    }
+    const float delta = fmaxf(sij - r, 0.0f);
+    const float sq = delta * rsqrtf(fmaxf(delta, 1e-30f));
+    return in ? -eps * delta * sq * rinv : 0.0f;
   }
 }
 
