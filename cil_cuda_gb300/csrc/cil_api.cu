@@ -101,7 +101,10 @@ struct cil_handle {
   unsigned *d_ftouch = nullptr;  // one bit per slot: facc holds a fresh-pair contribution
   ColonySkin *d_skin = nullptr;
   int *d_ts = nullptr;           // device step counter (kernels read the step from here)
-  int *d_anyreb = nullptr;       // skin mode: [2] some colony rebuilds at step ts (ts & 1)
+  int *d_anyreb = nullptr;       // skin mode: [4] some colony rebuilds at step ts ([ts & 1]),
+                                 // colonies decided ([2]), rebuild nodes run ([3])
+  cudaStream_t side = nullptr;   // skin mode: captures the bodies of the rebuild nodes
+  bool cond_capture = false;     // a steady-step capture: rebuild kernels in a conditional node
   // CUDA graphs of two steady steps, one per buffer parity (graph_gen: invalidation)
   std::vector<GraphSlot> graphs;
   uint64_t graph_gen = 0;
@@ -125,6 +128,9 @@ struct cil_handle {
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
   int *d_tiles_pairs = nullptr;  // skin mode: tiles over slot pairs (the cell-major force kernel)
   int *d_tile_count = nullptr, *d_tile_off = nullptr;
+  int *d_dueq = nullptr;      // skin mode, Philox: cells due to divide, per colony (due_base)
+  size_t due_total = 0;
+  int *d_evdone = nullptr;    // skin mode, Philox: colonies whose events are done this step
   int *d_dead = nullptr;
   int *d_divq = nullptr;  // division queue [CC]
   double *d_obs = nullptr;  // com_prev, disp, vref: 3 * D * CC
@@ -168,7 +174,7 @@ void free_all(cil_handle *h) {
                   h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live, h->d_tiles_pairs,
-                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dead, h->d_divq, h->d_obs,
+                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dueq, h->d_evdone, h->d_dead, h->d_divq, h->d_obs,
                   h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -181,6 +187,7 @@ void free_all(cil_handle *h) {
     if (e) cudaEventDestroy(e);
   for (auto e : h->evpool) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->side) cudaStreamDestroy(h->side);
 }
 
 // bins per axis as LinkListOrtho::get_opt_size + reset (Utils.hpp:872-908)
@@ -392,6 +399,7 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
   a.eid = h->d_eid[h->meta];
   a.pk = h->d_pk[h->pu];
   a.pk_next = h->d_pk[1 - h->pu];
+  a.dueq = h->d_dueq;
   if (h->skin_mode) {
     a.tiles = h->d_tiles_pairs;
     a.skin = h->d_skin;
@@ -446,6 +454,9 @@ EventArgs event_args(cil_handle *h) {
   a.tsw = h->d_tsw;
   a.tile_count = h->d_tile_count;
   a.tile_off = h->d_tile_off;
+  a.dueq = h->d_dueq;
+  a.ev_done = h->d_evdone;
+  a.any_rebuild = h->d_anyreb;
   a.dead = h->d_dead;
   a.divq = h->d_divq;
   if (h->d_obs) {
@@ -665,14 +676,23 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     if (st != CIL_OK) return st;
   }
   const bool philox = h->cfg.rng_mode != CIL_RNG_DSFMT;
-  // the step counter, and in Philox mode the cell tile table of the device events
-  launch_advance_ts(h->d_ts, h->d_anyreb, h->stream, h->d_cnt, h->B, philox ? h->d_tiles_cell : nullptr);
+  // skin mode, Philox: one event kernel over the force kernel's due-cell queues, which also
+  // moves the step counter; otherwise a step-end launch (the step counter and, in Philox mode,
+  // the cell tile table) and the tile-wise event kernels
+  const bool due_events = philox && h->skin_mode;
+  if (!due_events) {
+    launch_advance_ts(h->d_ts, h->d_anyreb, h->stream, h->d_cnt, h->B, philox ? h->d_tiles_cell : nullptr);
+    h->launches += 1;
+  }
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 2), h->stream));
   h->ts += 1;
   if (h->cfg.rng_mode == CIL_RNG_DSFMT) {
     const cil_status st = oracle_events(h);
     if (st != CIL_OK) return st;
     h->launches += 2;
+  } else if (due_events) {
+    launch_events_due(event_args(h), h->D, h->stream);
+    h->launches += 1;
   } else {
     launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
     h->launches += 3;
@@ -708,6 +728,18 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
       sb.tiles_pairs_out = h->d_tiles_pairs;
       sb.pair_tile = 2 * h->cell_block;
     }
+    // in a steady-step capture the rebuild kernels go into a conditional (IF) node that
+    // k_skin_begin sets: steps on which no colony rebuilds launch none of them (the kernels
+    // still check the rebuild flags themselves, so the node only saves launches)
+    const bool use_cond = h->cond_capture && !permute;
+    cudaGraph_t cg = nullptr;
+    if (use_cond) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      CUDA_TRY(h, cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &cg));
+      if (cs != cudaStreamCaptureStatusActive || !cg) return fail(h, CIL_ERR_CUDA, "rebuild node: stream not capturing");
+      CUDA_TRY(h, cudaGraphConditionalHandleCreate(&sb.cond, cg, 1, cudaGraphCondAssignDefault));
+      sb.use_cond = 1;
+    }
     launch_skin_begin(sb, h->stream);
     if (permute) {
       // cell-major re-sort; every colony then rebuilds its bin index and lists (host request)
@@ -715,18 +747,42 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
       if (st != CIL_OK) return st;
       launch_tiles(h->d_col, h->d_cnt, h->B, 0, h->d_tiles_used, h->stream, 3, h->d_tiles_pairs, 2 * h->cell_block);
     }
-    launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, h->stream);
+    cudaStream_t rs = h->stream;
+    if (use_cond) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      const cudaGraphNode_t *deps = nullptr;
+      const cudaGraphEdgeData *edges = nullptr;
+      size_t ndeps = 0;
+      CUDA_TRY(h, cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &deps, &edges, &ndeps));
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = sb.cond;
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      CUDA_TRY(h, cudaGraphAddNode(&node, cg, deps, edges, ndeps, &cp));
+      CUDA_TRY(h, cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+      CUDA_TRY(h, cudaStreamBeginCaptureToGraph(h->side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+      rs = h->side;
+    }
+    launch_skin_rebin(skin_args(h, 0), h->D, h->grid_slots, rs);
     RebuildArgs ra = rebuild_args(h);
     ra.permute = 0;
     ra.skin = h->d_skin;  // only colonies with rebuild_now
     ra.any_rebuild = h->d_anyreb;
     ra.ts_dev = h->d_ts;
     ra.state_out = nullptr;
-    launch_rebuild(ra, h->grid_slots, h->stream);  // slot count unchanged: tile tables stay
-    launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, h->stream);
+    launch_rebuild(ra, h->grid_slots, rs);  // slot count unchanged: tile tables stay
+    launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, rs);
+    if (use_cond) {
+      cudaGraph_t body = nullptr;
+      CUDA_TRY(h, cudaStreamEndCapture(h->side, &body));
+    }
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
-    h->launches += permute ? 17 : 7;
+    // kernels of the rebuild node: counted when the node runs (cil_timings)
+    h->launches += permute ? 17 : (use_cond ? 2 : 8);
   } else {
     // the second half step of a Heun step reads the first half's velocities: carried through
     // the re-sort (only when velocities are written, i.e. the last step of a cil_step call)
@@ -746,6 +802,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     fa.heun = heun;
     fa.vel_prev = vel_prev;
     launch_force(fa, h->D, h->cfg.force_law, h->cfg.precision, h->grid_force, kTile, h->stream);
+    h->launches += 1;
     h->cur = 1 - h->cur;
     if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
     return CIL_OK;
@@ -753,7 +810,9 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
   if (before_force) CUDA_TRY(h, cudaEventRecord(before_force, h->stream));
   ForceArgs fa = force_args(h, noise ? (oracle ? 2 : 1) : 0, 1, last ? h->d_vel : nullptr, nullptr);
   fa.heun = heun;
+  fa.collect_due = (!oracle && heun != 1) ? 1 : 0;  // the step's events read the due-cell queue
   launch_force_list(fa, h->D, h->cfg.force_law, h->ptiles, h->list_variant, h->cell_block, h->stream);  // skin mode
+  h->launches += 1;
   h->cur = 1 - h->cur;
   if (h->cfg.precision == CIL_PREC_MIXED) h->pu = 1 - h->pu;
   return CIL_OK;
@@ -836,7 +895,17 @@ cudaGraphExec_t steady_graph(cil_handle *h, int nsteps, bool last, int64_t *laun
     return nullptr;
   }
   cil_status sc = CIL_OK;
+  h->cond_capture = h->skin_mode && h->side != nullptr;
   for (int i = 0; i < nsteps && sc == CIL_OK; ++i) sc = enqueue_step(h, last && i == nsteps - 1, false, 0);
+  h->cond_capture = false;
+  {
+    // a failure inside a rebuild node's body leaves the side stream capturing: end it
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (h->side && cudaStreamIsCapturing(h->side, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t body = nullptr;
+      cudaStreamEndCapture(h->side, &body);
+    }
+  }
   const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
   HostStepState expect = before;
   for (int i = 0; i < nsteps; ++i) advance_host_state(h, &expect);
@@ -924,6 +993,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->hc.resize(h->B);
   h->cc.resize(h->B);
   long long cells = 0, slots = 0;
+  long long due_acc = 0;  // the due-cell queue: a power of two >= the cell capacity per colony
   for (int c = 0; c < h->B; ++c) {
     const cil_colony_params &p = params[c];
     if (p.dim != cfg->dim || p.force_law != cfg->force_law || cap_cells[c] <= 0 || !(p.dt > 0.0) ||
@@ -1001,6 +1071,12 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.eps_f = static_cast<float>(C.epsilon);
     C.rcs_f = static_cast<float>(C.rcut_scale);
     C.wall_E_f = static_cast<float>(C.wall_E);
+    C.due_base = static_cast<int>(due_acc);
+    {
+      long long p2 = 1;
+      while (p2 < cap_cells[c]) p2 <<= 1;
+      due_acc += p2;
+    }
     cells += cap_cells[c];
     slots += C.slot_cap;
     if (cells > (1ll << 29) || slots > (1ll << 30)) {
@@ -1015,10 +1091,12 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   }
   h->CC = static_cast<int>(cells);
   h->SS = static_cast<size_t>(slots);
+  h->due_total = static_cast<size_t>(due_acc);
   h->obs_ready.assign(h->B, 0);
 
   cudaError_t e = cudaSetDevice(cfg->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && cfg->skin > 0.0) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, cfg->device);
   if (e != cudaSuccess) {
     h->err = cudaGetErrorString(e);
@@ -1056,10 +1134,12 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_ftouch = dalloc<unsigned>((SS + 31) / 32);
     h->d_fresh = dalloc<int>(static_cast<size_t>(h->B) * kFreshCap);
     h->d_fnext = dalloc<unsigned long long>(SS);
-    h->d_anyreb = dalloc<int>(2);
+    h->d_anyreb = dalloc<int>(4);
+    h->d_dueq = dalloc<int>(h->due_total);
     h->d_skin = dalloc<ColonySkin>(h->B);
     h->d_sched = dalloc<SchedState>(h->B);
     skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_ftouch &&
+              h->d_dueq &&
               h->d_fresh &&
               h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
@@ -1085,13 +1165,14 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   for (int c = 0; c < h->B; ++c) h->ptiles += (h->cc[c].slot_cap + 2 * h->cell_block - 1) / (2 * h->cell_block);
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
+  h->d_evdone = dalloc<int>(1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
   h->d_divq = dalloc<int>(static_cast<size_t>(h->CC));
   bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_eid[0] && h->d_eid[1] && h->d_sbin[0] &&
             h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
             h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
             h->d_tiles_pairs &&
-            h->d_tile_count && h->d_tile_off && h->d_dead && h->d_divq && h->d_ts &&
+            h->d_tile_count && h->d_tile_off && h->d_evdone && h->d_dead && h->d_divq && h->d_ts &&
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
             skin_ok;
   if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {
@@ -1106,6 +1187,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     delete h;
     return CIL_ERR_CUDA;
   }
+  cudaMemsetAsync(h->d_evdone, 0, sizeof(int), h->stream);
   // static parts of the colony table (bases, capacities, physics); the bin geometry is
   // filled in once every colony has been uploaded
   cudaMemcpyAsync(h->d_col, h->cc.data(), sizeof(ColonyConst) * h->B, cudaMemcpyHostToDevice, h->stream);
@@ -1125,7 +1207,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     }
     cudaMemcpy(h->d_skin, sk.data(), sizeof(ColonySkin) * h->B, cudaMemcpyHostToDevice);
     cudaMemsetAsync(h->d_sched, 0, sizeof(SchedState) * h->B, h->stream);
-    cudaMemsetAsync(h->d_anyreb, 0, 2 * sizeof(int), h->stream);
+    cudaMemsetAsync(h->d_anyreb, 0, 4 * sizeof(int), h->stream);
     cudaMemsetAsync(h->d_facc, 0, sizeof(float) * D * SS, h->stream);
     cudaMemsetAsync(h->d_ftouch, 0, sizeof(unsigned) * ((SS + 31) / 32), h->stream);
     cudaMemsetAsync(h->d_ncnt, 0, sizeof(int) * SS, h->stream);
@@ -1222,6 +1304,7 @@ cil_status cil_step(cil_handle *h, int32_t nsteps, int64_t *ts_out) {
   h->t_rebuild = h->t_force = h->t_events = 0.0;
   h->launches = 0;
   h->graph_steps = 0;
+  if (h->skin_mode) CUDA_TRY(h, cudaMemsetAsync(h->d_anyreb + 3, 0, sizeof(int), h->stream));
   std::vector<char> seg_graph;  // per segment of 4 events: 1 = a graph of two steps
   int k = 0;
   while (k < nsteps) {
@@ -1593,7 +1676,15 @@ cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, doub
   if (force_ms) *force_ms = h->t_force;
   if (events_ms) *events_ms = h->t_events;
   if (total_ms) *total_ms = h->t_total;
-  if (launches) *launches = h->launches;
+  if (launches) {
+    // plus the six kernels of every rebuild node that ran in the last cil_step call
+    int runs = 0;
+    if (h->skin_mode) {
+      CUDA_TRY(h, cudaMemcpyAsync(&runs, h->d_anyreb + 3, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    }
+    *launches = h->launches + 6 * static_cast<int64_t>(runs);
+  }
   return CIL_OK;
 }
 

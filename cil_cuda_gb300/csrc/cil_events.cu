@@ -620,6 +620,97 @@ __global__ void __launch_bounds__(kTile) k_events_exec(EventArgs a_) {
   apo_colony(a, c, D);
 }
 
+// Ascending bitonic sort of v[0, P) (P a power of two) by the whole block; v in shared or
+// global memory (a block barrier orders both within the block).
+__device__ void block_bitonic_sort(int *v, int P) {
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int l = i ^ stride;
+        if (l > i) {
+          const bool up = (i & size) == 0;
+          const int x = v[i], y = v[l];
+          if ((x > y) == up) {
+            v[i] = y;
+            v[l] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+constexpr int kDueSort = 2048;  // due cells sorted in shared memory (more: in the queue itself)
+
+// Skin mode, Philox: the step's events from the due-cell queues, one block per colony. The
+// force pass appended the cells whose cycle ends at this step (in no particular order); the
+// block sorts them by cell index, so the first ndiv_allowed in cell order divide (within the
+// colony's cell and slot room; the ranking of the tile-wise kernels), places the divisions
+// (one thread each: draws, FP64 placement of the four elements, new cycles; daughters take
+// cells n + rank and slots nslot + 2 rank), then the colony's apoptoses (apo_colony). The
+// kernel reads the step as *ts_dev + 1; the block that finishes last writes it back and
+// clears the next step's any-rebuild flag (in place of a step-counter launch).
+template <int D>
+__global__ void __launch_bounds__(kTile) k_events_due(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev + 1;
+  const int c = blockIdx.x;
+  const ColonyConst &C = a.col[c];
+  ColonyCounters &K = a.cnt[c];
+  __shared__ int s_key[kDueSort];
+  __shared__ int s_allowed;
+  const int n = K.ncell;
+  const int nd = min(K.ndue, n);
+  int P = 1;
+  while (P < nd) P <<= 1;
+  int *q = a.dueq + C.due_base;  // capacity: a power of two >= cell_cap >= P
+  int *keys = s_key;
+  if (P <= kDueSort) {
+    for (int i = threadIdx.x; i < P; i += blockDim.x) s_key[i] = i < nd ? q[i] : 0x7fffffff;
+  } else {
+    for (int i = nd + static_cast<int>(threadIdx.x); i < P; i += blockDim.x) q[i] = 0x7fffffff;
+    keys = q;
+  }
+  __syncthreads();
+  if (nd > 1) block_bitonic_sort(keys, P);
+  if (threadIdx.x == 0) {
+    // room for the cells and for their two element slots each (skin mode appends daughters
+    // behind removed elements until the next slot re-sort)
+    const int room_cells = C.cell_cap - n;
+    const int room_slots = (C.slot_cap - K.nslot) / 2;
+    const int room = room_cells < room_slots ? room_cells : room_slots;
+    int allowed = nd < room ? nd : room;
+    if (allowed < 0) allowed = 0;
+    if (allowed < nd) K.err |= kErrCap;
+    K.ndiv_step = nd;
+    K.ndiv_allowed = allowed;
+    K.ndead = 0;
+    K.ndue = 0;  // for the next step's force pass
+    s_allowed = allowed;
+  }
+  __syncthreads();
+  const int allowed = s_allowed, nslot = K.nslot;
+  for (int r = threadIdx.x; r < allowed; r += blockDim.x) {
+    const int i = keys[r];
+    double dm[D], dd[D];
+    int span_d, span_m;
+    division_draws<D>(a, i, dm, dd, span_d, span_m, C);
+    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
+  }
+  __syncthreads();  // every division is placed, and visible to the whole block
+  apo_colony(a, c, D);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // the last colony's block moves the step counter (every block has read it by then)
+    __threadfence();
+    if (atomicAdd(a.ev_done, 1) == a.B - 1) {
+      a.any_rebuild[a.ts & 1] = 0;
+      *a.ts_dev = a.ts;
+      *a.ev_done = 0;
+    }
+  }
+}
+
 // oracle mode: divisions in the host's order with host-drawn axes and cycle lengths
 template <int D>
 __global__ void k_div_list(EventArgs a_, int c, int n0, int ndiv, const int *mothers, const double *dirs,
@@ -688,6 +779,7 @@ __global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, c
     cnt[c].ndead = 0;
     cnt[c].ndiv_step = 0;
     cnt[c].ndiv_allowed = 0;
+    cnt[c].ndue = 0;
   }
 }
 
@@ -795,6 +887,13 @@ void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_
     k_events_exec<2><<<a.B, kTile, 0, s>>>(a);
   else
     k_events_exec<3><<<a.B, kTile, 0, s>>>(a);
+}
+
+void launch_events_due(const EventArgs &a, int dim, cudaStream_t s) {
+  if (dim == 2)
+    k_events_due<2><<<a.B, kTile, 0, s>>>(a);
+  else
+    k_events_due<3><<<a.B, kTile, 0, s>>>(a);
 }
 
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,

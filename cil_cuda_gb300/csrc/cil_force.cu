@@ -818,6 +818,19 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   const bool used = s0 < C.slot_base + a.cnt[c].nslot;
   const bool live = used && ee.x >= 0;
   if (!live) nn = make_int2(0, 0);
+  if (a.collect_due && C.divide) {  // uniform
+    // cells whose cycle ends at the coming events (step ts + 1) join the colony's due-cell
+    // queue: one atomic per warp
+    const bool due = live && cy.y == ts + 1;
+    const unsigned dm = __ballot_sync(0xffffffffu, due);
+    if (dm) {
+      const int lane = tid & 31, leader = __ffs(dm) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&a.cnt[c].ndue, __popc(dm));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (due) a.dueq[C.due_base + base + __popc(dm & ((1u << lane) - 1u))] = (ee.x >> 1) - C.cell_base;
+    }
+  }
   float d2 = 0.0f, st2[2] = {0.0f, 0.0f};
   // ---- the pair pass starts: the warp's records, its flattened list range, and asynchronous
   // copies of its list entries and of the cells' FP64 positions, which arrive while the

@@ -132,8 +132,7 @@ struct ColonyConst {
   int scan_base;     // first scan block
   int slot_base, slot_cap;
   int cell_base, cell_cap;
-  int ctile_base;    // first cell tile (static, from capacity)
-  int ctile_cap;     // cell tiles reserved
+  int due_base;      // the colony's part of the due-cell queue (a power of two >= cell_cap)
   int force_law;
   int noise_per_cell;
   uint32_t rng_stream;  // the colony's Philox stream (cil_config.rng_stream_base + colony index)
@@ -173,7 +172,7 @@ struct ColonyCounters {
   int ndiv_step;      // divisions this step
   int ndead;          // apoptoses recorded this step (list length, may exceed kDeadCap)
   int ndiv_allowed;   // divisions that fit the capacity this step
-  int pad;
+  int ndue;           // skin mode, Philox: cells due to divide at the coming events (force kernel)
   long long ndiv_total;
   long long napo_total;
 };
@@ -529,6 +528,10 @@ struct ForceArgs {
   int noise_mode;          // 0 none, 1 philox, 2 uploaded
   int integrate;
   int heun;                // 0 Euler step; 1, 2: first, second half step of a Heun step
+  // skin mode, Philox, the step's last force pass: cells due to divide at step ts + 1 are
+  // appended to the colony's due-cell queue (dueq + col[c].due_base, count cnt[c].ndue)
+  int collect_due;
+  int *dueq;
 };
 
 // Half-step helpers of the Heun integrator (CIL_INTEGRATOR_HEUN): the Philox noise index of
@@ -563,13 +566,18 @@ struct EventArgs {
   int *tsw;
   int *tile_count;
   int *tile_off;
+  // skin mode, Philox: the cells due to divide, appended by the force kernel (colony c's at
+  // dueq + col[c].due_base, count cnt[c].ndue), and the event kernel's finished-colony count
+  int *dueq;
+  int *ev_done;
+  int *any_rebuild;        // the any-rebuild flags (the next step's is cleared)
   int *dead;               // [B * kDeadCap]
   int *divq;               // [CC] per colony: the cells dividing this step, in rank order
   double *obs_com_prev;    // [D * CC] or null
   double *obs_disp;
   double *obs_vref;
   size_t CC;
-  const int *ts_dev;       // device step counter, already advanced past the force step
+  int *ts_dev;             // device step counter (advanced past the force step, or by k_events_due)
   int ts;                  // filled from *ts_dev at kernel entry
   uint32_t seed_lo, seed_hi;
 };
@@ -601,7 +609,12 @@ struct SkinArgs {
   int force_rebuild;       // host request for every colony this step
   int grid;                // blocks of the fresh-pair kernel
   const int *ts_dev;       // device step counter
-  int *any_rebuild;        // [2]: some colony rebuilds at step ts (index ts & 1), or null
+  int *any_rebuild;        // [4]: [ts & 1] some colony rebuilds at step ts; [2] colonies decided
+                           // this step; [3] steps whose rebuild node ran (or null)
+  // graph replay: the conditional (IF) node around the rebuild kernels of the step; the
+  // colony that decides last sets it to "some colony rebuilds" (use_cond 0: no node)
+  int use_cond;
+  cudaGraphConditionalHandle cond;
   // k_skin_begin also writes the step's tile tables over the slots and the slot pairs when these
   // are set (pair tiles of pair_tile slots), or null
   int *tiles_used_out;
@@ -680,6 +693,7 @@ void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s, const Colo
                        int *tiles_cell = nullptr);
 int mlp_param_count();
 void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);
+void launch_events_due(const EventArgs &a, int dim, cudaStream_t s);
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,
                            const double *dirs, const int *spans, int dim, cudaStream_t s);
 void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops, const int *ops, int dim,

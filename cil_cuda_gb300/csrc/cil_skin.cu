@@ -171,6 +171,17 @@ __global__ void k_skin_begin(SkinArgs a) {
   if (lane == 0) {
     now = skin_begin_colony(a, c);
     if (now && a.any_rebuild) atomicOr(&a.any_rebuild[*a.ts_dev & 1], 1);
+    if (a.use_cond) {
+      // the last colony to decide sets the step's rebuild node (one caller: no racing sets)
+      __threadfence();
+      if (atomicAdd(&a.any_rebuild[2], 1) == a.B - 1) {
+        __threadfence();
+        const int any = atomicOr(&a.any_rebuild[*a.ts_dev & 1], 0);
+        cudaGraphSetConditional(a.cond, any != 0 ? 1u : 0u);
+        if (any) atomicAdd(&a.any_rebuild[3], 1);
+        atomicExch(&a.any_rebuild[2], 0);
+      }
+    }
   }
   now = __shfl_sync(0xffffffffu, now, 0);
   if (!now || !a.mlp) return;  // uniform per warp
