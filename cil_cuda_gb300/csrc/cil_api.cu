@@ -895,7 +895,7 @@ cudaGraphExec_t steady_graph(cil_handle *h, int nsteps, bool last, int64_t *laun
     return nullptr;
   }
   cil_status sc = CIL_OK;
-  h->cond_capture = h->skin_mode && h->side != nullptr;
+  h->cond_capture = h->skin_mode && h->side != nullptr && !(h->cfg.flags & CIL_FLAG_NO_REBUILD_NODE);
   for (int i = 0; i < nsteps && sc == CIL_OK; ++i) sc = enqueue_step(h, last && i == nsteps - 1, false, 0);
   h->cond_capture = false;
   {

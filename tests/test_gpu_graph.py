@@ -55,6 +55,34 @@ def test_mixed_graph_matches_launches(gpu_lib, growth, skin):
     assert np.abs(d).max() < 1e-4
 
 
+def test_rebuild_node_and_plain_launches_agree(gpu_lib, growth):
+    """Skin mode with graphs: the list-rebuild kernels in a conditional graph node (run on
+    rebuild steps only) and the same kernels launched every step (returning at once when no
+    colony rebuilds) give the same run: the same rebuilds, divisions and apoptoses, positions
+    to FP32 summation order; the node saves the six launches on steps without a rebuild."""
+    p, st = growth
+    n = len(st["sigma"])
+    res = []
+    for node in (True, False):
+        eng = gpu_lib.Engine([p], [3 * n], precision=gpu_lib.PREC_MIXED, rng=gpu_lib.RNG_PHILOX, seed=5, skin=0.3,
+                             rebuild_node=node)
+        eng.upload(0, **st)
+        eng.step(STEPS)
+        launches = eng.timings()["launches"]
+        res.append((eng.download(0), launches, eng.skin_stats(0), eng.graph_info(), eng.observables(0)))
+        eng.close()
+    (a, la, ska, ga, oa), (b, lb, skb, gb, ob) = res
+    assert ga["graph_steps"] > 0 and gb["graph_steps"] == ga["graph_steps"]
+    assert ska["nrebuild"] == skb["nrebuild"] and 1 <= ska["nrebuild"] < STEPS // 2
+    assert a["ncells"] == b["ncells"] and oa["ndiv_total"] == ob["ndiv_total"] > 0
+    np.testing.assert_array_equal(a["tswitch"], b["tswitch"])
+    d = np.asarray(a["pos"]) - np.asarray(b["pos"])
+    d -= np.round(d / p["box"][0]) * p["box"][0]
+    assert np.abs(d).max() < 1e-4
+    # replayed steps without a rebuild launch six kernels fewer with the node
+    assert 6 * (ga["graph_steps"] - ska["nrebuild"]) <= lb - la <= 6 * ga["graph_steps"]
+
+
 def test_graphs_follow_buffers_allocated_between_calls(gpu_lib, growth):
     """Observables are allocated at the first obs_reset; steps captured before it must not be
     replayed after it (they would hold no observable arrays and divisions would not carry the
