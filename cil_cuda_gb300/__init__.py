@@ -20,7 +20,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 RNG_PHILOX, RNG_DSFMT = 0, 1
 FLAG_NO_GRAPH = 1
 FLAG_DEFERRED_STATUS = 2
-FLAG_NO_REBUILD_NODE = 4
+FLAG_REBUILD_NODE = 4
 INTEGRATOR_EULER, INTEGRATOR_HEUN = 0, 1
 
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
@@ -519,7 +519,7 @@ class Engine:
                  seed: int = 0, device: int = 0, bin_width: float = 0.0, skin: float = 0.0,
                  graphs: bool = True, staging: int = 0, occupancy: int = 0, integrator: int = INTEGRATOR_EULER,
                  deferred_status: bool = False, rng_stream_base: int = 0, block_size: int = 0,
-                 rebuild_node: bool = True):
+                 rebuild_node: bool = False):
         self.L = lib()
         self.B = len(params)
         self.dim = params[0]["dim"]
@@ -528,7 +528,7 @@ class Engine:
                      seed=seed, num_colonies=self.B, device=device, bin_width=bin_width, skin=skin,
                      block_size=block_size,
                      flags=(0 if graphs else FLAG_NO_GRAPH) | (FLAG_DEFERRED_STATUS if deferred_status else 0)
-                     | (0 if rebuild_node else FLAG_NO_REBUILD_NODE),
+                     | (FLAG_REBUILD_NODE if rebuild_node else 0),
                      staging=staging,
                      occupancy=occupancy, integrator=integrator, rng_stream_base=rng_stream_base)
         arr = (ColonyParams * self.B)(*[make_params(**p) for p in params])

@@ -728,9 +728,10 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
       sb.tiles_pairs_out = h->d_tiles_pairs;
       sb.pair_tile = 2 * h->cell_block;
     }
-    // in a steady-step capture the rebuild kernels go into a conditional (IF) node that
-    // k_skin_begin sets: steps on which no colony rebuilds launch none of them (the kernels
-    // still check the rebuild flags themselves, so the node only saves launches)
+    // with CIL_FLAG_REBUILD_NODE, a steady-step capture puts the rebuild kernels into a
+    // conditional (IF) node that k_skin_begin sets: steps on which no colony rebuilds launch
+    // none of them (the kernels still check the rebuild flags themselves, so the node only
+    // saves launches)
     const bool use_cond = h->cond_capture && !permute;
     cudaGraph_t cg = nullptr;
     if (use_cond) {
@@ -895,7 +896,7 @@ cudaGraphExec_t steady_graph(cil_handle *h, int nsteps, bool last, int64_t *laun
     return nullptr;
   }
   cil_status sc = CIL_OK;
-  h->cond_capture = h->skin_mode && h->side != nullptr && !(h->cfg.flags & CIL_FLAG_NO_REBUILD_NODE);
+  h->cond_capture = h->skin_mode && h->side != nullptr && (h->cfg.flags & CIL_FLAG_REBUILD_NODE) != 0;
   for (int i = 0; i < nsteps && sc == CIL_OK; ++i) sc = enqueue_step(h, last && i == nsteps - 1, false, 0);
   h->cond_capture = false;
   {

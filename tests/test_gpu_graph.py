@@ -57,9 +57,10 @@ def test_mixed_graph_matches_launches(gpu_lib, growth, skin):
 
 def test_rebuild_node_and_plain_launches_agree(gpu_lib, growth):
     """Skin mode with graphs: the list-rebuild kernels in a conditional graph node (run on
-    rebuild steps only) and the same kernels launched every step (returning at once when no
-    colony rebuilds) give the same run: the same rebuilds, divisions and apoptoses, positions
-    to FP32 summation order; the node saves the six launches on steps without a rebuild."""
+    rebuild steps only, CIL_FLAG_REBUILD_NODE) and the same kernels launched every step
+    (returning at once when no colony rebuilds) give the same run: the same rebuilds, divisions
+    and apoptoses, positions to FP32 summation order; the node saves the six launches on steps
+    without a rebuild."""
     p, st = growth
     n = len(st["sigma"])
     res = []
