@@ -247,8 +247,19 @@ __global__ void __launch_bounds__(kTile) k_skin_rebin(SkinArgs a) {
   }
 }
 
+// Latency-bound (two dependent loads per batch of candidates): many resident warps with short
+// batches beat few warps with long ones. One list build (with the rebin and scan launches) of
+// the 2M-particle 2D colony took 0.603 ms with batches of 8 at 2 CTAs per SM (108 registers),
+// 0.440 ms with 4 at 4 CTAs and 0.420 ms with 2 at 8 CTAs (32 registers); of the 4M-particle
+// 3D channel, 2.64 ms with 8 at 1 CTA, 1.55 ms with 2 at 2 CTAs and 1.43 ms with 2 at 3 CTAs
+// (3D keeps the 27 bin ranges in registers, so it runs fewer CTAs per SM).
+template <int D>
+constexpr int kListBatch = 2;
+template <int D>
+constexpr int kListMinBlocks = D == 2 ? 8 : 3;
+
 template <int D, int LAW>
-__global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
+__global__ void __launch_bounds__(kTile, kListMinBlocks<D>) k_skin_lists(SkinArgs a) {
   constexpr int NB = (D == 2) ? 9 : 27;
   if (a.any_rebuild && a.any_rebuild[*a.ts_dev & 1] == 0) return;  // uniform, before any barrier
   __shared__ unsigned s_occ_sum, s_occ_max, s_cnt;
@@ -288,7 +299,7 @@ __global__ void __launch_bounds__(kTile) k_skin_lists(SkinArgs a) {
         bin_decode<D>(C, a.sbin[s], bi);
         // the 3^d bin ranges, loaded together; candidates are then taken as one flattened
         // range in batches of kLB, so each batch costs two round trips (slots, then records)
-        constexpr int kLB = 8;
+        constexpr int kLB = kListBatch<D>;
         int start[NB], pre[NB + 1];
         pre[0] = 0;
 #pragma unroll
