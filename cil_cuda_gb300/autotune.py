@@ -17,8 +17,8 @@ import itertools
 from . import Engine, PREC_MIXED, RNG_PHILOX
 
 BIN_FACTORS = (1.0, 1.15, 1.3)
-BLOCK_SIZES = (128, 256, 512)  # threads (cells) per block of the list force kernel
-VARIANTS = ((2, 3), (1, 3), (2, 2), (1, 4))  # (chunks of 32 list entries in flight per warp, CTAs per SM)
+BLOCK_SIZES = (128, 256, 512)  # threads (cells) per block of the list force kernel; stage 1 runs the first
+VARIANTS = ((4, 3), (2, 3), (1, 3), (1, 4))  # (chunks of 32 list entries in flight per warp, CTAs per SM)
 
 
 def needed_width(params, states, skin):
@@ -46,19 +46,17 @@ def _trial(params, states, caps, *, skin, steps, warmup, seed, device, scheduler
 def autotune(params, states, caps, *, skin=0.3, steps=40, warmup=10, seed=3, device=0, scheduler=None,
              bin_factors=BIN_FACTORS, variants=VARIANTS, block_sizes=BLOCK_SIZES):
     """scheduler: None, or a callable installing the learned scheduler into an engine.
-    Stage 1 tries every bin size x list-kernel variant at 256 threads per block; stage 2 tries
-    the other block sizes with the stage-1 winner."""
+    Stage 1 tries every bin size x list-kernel variant at the first block size (128 threads);
+    stage 2 tries the other block sizes with the stage-1 winner."""
     base = needed_width(params, states, skin)
     common = dict(skin=skin, steps=steps, warmup=warmup, seed=seed, device=device, scheduler=scheduler)
     trials = []
     for f, (stg, occ) in itertools.product(bin_factors, variants):
-        ms = _trial(params, states, caps, bin_width=0.0 if f == 1.0 else f * base, stg=stg, occ=occ, block=256,
-                    **common)
-        trials.append(dict(bin_factor=f, staging=stg, occupancy=occ, block_size=256, ms_per_step=ms))
+        ms = _trial(params, states, caps, bin_width=0.0 if f == 1.0 else f * base, stg=stg, occ=occ,
+                    block=block_sizes[0], **common)
+        trials.append(dict(bin_factor=f, staging=stg, occupancy=occ, block_size=block_sizes[0], ms_per_step=ms))
     best = min(trials, key=lambda t: t["ms_per_step"])
-    for b in block_sizes:
-        if b == 256:
-            continue
+    for b in block_sizes[1:]:
         f = best["bin_factor"]
         ms = _trial(params, states, caps, bin_width=0.0 if f == 1.0 else f * base, stg=best["staging"],
                     occ=best["occupancy"], block=b, **common)

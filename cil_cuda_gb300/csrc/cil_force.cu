@@ -1105,18 +1105,16 @@ void launch_cells(const ForceArgs &a, int grid, int block, cudaStream_t s) {
 template <int D, int LAW>
 void launch_list_dl(const ForceArgs &a, int grid, int variant, int block, cudaStream_t s) {
   // cell-major slots, one thread per cell, the warp's list entries flattened; variants
-  // (chunks of 32 entries in flight per warp, CTAs per SM at 256 threads): 0 (2, 3), 1 (1, 3),
-  // 2 (2, 2), 3 (1, 4), 4 (1, 2); block: 128, 256 or 512 threads (cells per block)
+  // (chunks of 32 entries in flight per warp, CTAs per SM at 256 threads): 0 (4, 3), 1 (2, 3),
+  // 2 (1, 3), 3 (1, 4); block: 128, 256 or 512 threads (cells per block)
   if (variant == 0) {
-    launch_cells<D, LAW, 2, 3>(a, grid, block, s);
+    launch_cells<D, LAW, 4, 3>(a, grid, block, s);
   } else if (variant == 1) {
-    launch_cells<D, LAW, 1, 3>(a, grid, block, s);
+    launch_cells<D, LAW, 2, 3>(a, grid, block, s);
   } else if (variant == 2) {
-    launch_cells<D, LAW, 2, 2>(a, grid, block, s);
-  } else if (variant == 3) {
-    launch_cells<D, LAW, 1, 4>(a, grid, block, s);
+    launch_cells<D, LAW, 1, 3>(a, grid, block, s);
   } else {
-    launch_cells<D, LAW, 1, 2>(a, grid, block, s);
+    launch_cells<D, LAW, 1, 4>(a, grid, block, s);
   }
 }
 

@@ -96,12 +96,13 @@ typedef struct cil_config {
   double bin_width;       /* 0: cutoff of the largest element (+ skin); else at least this */
   double skin;            /* Verlet skin of the binned structure (0 = rebuild every step) */
   int32_t block_size;     /* threads per block of the force kernels: 0 or 256; in skin mode the
-                           * list force kernel also takes 128 or 512 (cells per block) */
+                           * list force kernel takes 128 (the default there), 256 or 512
+                           * (cells per block) */
   int32_t flags;          /* CIL_FLAG_* bits */
   /* Verlet-list force kernel (skin mode: one thread per cell, each warp's list entries taken as
-   * one flattened range): chunks of 32 entries in flight per warp (0 = 2; 1, 2) and CTAs per SM
-   * it is compiled for (0 = 3; 2, 3, 4). Supported pairs: (2, 3), (1, 3), (2, 2), (1, 4); 3D
-   * always runs (1, 2). cil_cuda_gb300/autotune.py picks them. */
+   * one flattened range): chunks of 32 entries in flight per warp (0 = 4; 1, 2) and CTAs per SM
+   * of 256 threads it is compiled for (0 = 3; 4). Supported pairs: (4, 3), (2, 3), (1, 3),
+   * (1, 4). cil_cuda_gb300/autotune.py picks them. */
   int32_t staging;
   int32_t occupancy;
   int32_t integrator;     /* CIL_INTEGRATOR_*: 0 = Euler */

@@ -14,7 +14,7 @@ def test_variants_agree_and_tuner_picks_one(gpu_lib):
     st = S.disk_colony(20000, p, seed=8)
     cap = 26000
     outs = []
-    for f, (stg, occ) in [(1.0, (2, 3)), (1.3, (1, 3)), (1.15, (2, 2)), (1.0, (1, 4))]:
+    for f, (stg, occ) in [(1.0, (4, 3)), (1.3, (1, 3)), (1.15, (2, 3)), (1.0, (1, 4))]:
         w = 0.0 if f == 1.0 else f * AT.needed_width([p], [st], 0.3)
         eng = gpu_lib.Engine([p], [cap], precision=gpu_lib.PREC_MIXED, rng=gpu_lib.RNG_PHILOX, seed=4, skin=0.3,
                              bin_width=w, staging=stg, occupancy=occ)
@@ -59,8 +59,9 @@ def test_block_sizes_agree(gpu_lib):
 
 def test_invalid_variant_rejected(gpu_lib):
     p = S.growth_params(box=64.0)
-    with pytest.raises(gpu_lib.CilError):
-        gpu_lib.Engine([p], [100], precision=gpu_lib.PREC_MIXED, skin=0.3, staging=8, occupancy=4)
+    for stg, occ in ((8, 4), (2, 2)):  # (2, 2): a pair no longer compiled
+        with pytest.raises(gpu_lib.CilError):
+            gpu_lib.Engine([p], [100], precision=gpu_lib.PREC_MIXED, skin=0.3, staging=stg, occupancy=occ)
     with pytest.raises(gpu_lib.CilError):
         gpu_lib.Engine([p], [100], precision=gpu_lib.PREC_MIXED, skin=0.3, block_size=384)
     with pytest.raises(gpu_lib.CilError):  # other block sizes only for the list kernel of skin mode
