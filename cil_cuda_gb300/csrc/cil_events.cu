@@ -792,6 +792,10 @@ __global__ void k_gather_canonical(int ncells, int dim, size_t SS, int cell_base
   (void)dim;
 }
 
+// nint(t / L) (Utils.hpp:173-175): 0 without a division when |t| < L / 4 (t / L then lies in
+// (-0.25, 0.25) whatever its rounding), the division otherwise (a minimum image across the box)
+__device__ __forceinline__ int nint_small(double t, double L) { return fabs(t) < 0.25 * L ? 0 : nint(t / L); }
+
 template <int D>
 __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, int reset, double *partials) {
   const ColonyConst &C = a.col[c];
@@ -805,9 +809,10 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
     for (int d = 0; d < D; ++d) {
       const double r0 = a.x[d * a.SS + s0], r1 = a.x[d * a.SS + s1];
       double rel = r1 - r0;
-      if (C.periodic[d]) rel -= static_cast<double>(nint(rel / C.box[d])) * C.box[d];
+      if (C.periodic[d]) rel -= static_cast<double>(nint_small(rel, C.box[d])) * C.box[d];
       const double m = (0.0 + rel) / 2.0;  // calculComs, Colony.cpp:409-432
-      com[d] = C.periodic[d] ? fmod(m + r0 + C.box[d], C.box[d]) : m + r0;
+      // fmod(m + r0 + L, L) with m + r0 in [-L, 2L): the exact division-free form
+      com[d] = C.periodic[d] ? wrap_like_fmod(m + r0, C.box[d]) : m + r0;
       v[d] = a.vel ? 0.5 * (a.vel[d * a.SS + s0] + a.vel[d * a.SS + s1]) : 0.0;
     }
     const double q0 = a.sigma_c[2 * g] * 0.5, q1 = a.sigma_c[2 * g + 1] * 0.5;
@@ -823,7 +828,7 @@ __global__ void __launch_bounds__(kTile) k_obs(EventArgs a, int c, int ncells, i
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         double dr = com[d] - a.obs_com_prev[d * a.CC + g];
-        if (C.periodic[d]) dr -= static_cast<double>(nint(dr / C.box[d])) * C.box[d];
+        if (C.periodic[d]) dr -= static_cast<double>(nint_small(dr, C.box[d])) * C.box[d];
         const double acc = a.obs_disp[d * a.CC + g] + dr;
         a.obs_disp[d * a.CC + g] = acc;
         a.obs_com_prev[d * a.CC + g] = com[d];

@@ -502,10 +502,11 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
       for (int d = 0; d < D; ++d) of[d] = __shfl_sync(0xffffffffu, ofs[d], o);
       if (k >= total) continue;
       const int tt = static_cast<int>(a.perm[st + (k - base)] & 0xffffffffu);
-      if (a.state[tt] != kSlotNormal) continue;
+      // the candidate's state, element id and record: independent loads, issued together
+      const unsigned char stt = a.state[tt];
       const int ej = a.eid[tt];
-      if (ej < 0 || (ej >> 1) == gf) continue;
       const float4 pj = a.pk[tt];
+      if (stt != kSlotNormal || ej < 0 || (ej >> 1) == gf) continue;
       float dx[D];
       float r2 = 0.0f;
 #pragma unroll
@@ -529,10 +530,10 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
       for (int guard = 0; guard < kFreshCap && static_cast<unsigned>(ent >> 32) == epoch; ++guard) {
         const int q = static_cast<int>(ent & 0xffffffffu);
         ent = a.fnext[q];
-        if (q == f || a.state[q] != kSlotFresh) continue;
+        const unsigned char sq = a.state[q];
         const int eq = a.eid[q];
-        if (eq < 0 || (eq >> 1) == gf) continue;
         const float4 pq = a.pk[q];
+        if (q == f || sq != kSlotFresh || eq < 0 || (eq >> 1) == gf) continue;
         float dx[D];
         float r2 = 0.0f;
 #pragma unroll
