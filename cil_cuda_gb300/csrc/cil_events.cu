@@ -344,13 +344,14 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
   }
 }
 
-// one block per colony: commit the divisions, then swap-with-last removal of the dead
-// warp-level path of apo_colony for k <= 32 deaths among n1 cells: distinct uniform picks
-// (redrawn while duplicated, at most 16 rounds), tombstones, then the live cells of the tail
-// [n1 - k, n1) move into the holes below it in ascending order (removeCell's swap-with-last,
-// Colony.cpp:365-399, for a sorted set of victims)
-__device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, ColonyCounters &K, int k, int n1,
-                          int D) {
+// warp-level path of apo_colony for k <= 32 deaths among n1 cells. apo_small_pick: distinct
+// uniform picks (redrawn while duplicated, at most 16 rounds), ascending in lanes 0..kk-1 (the
+// return value kk; duplicates left after 16 rounds, practically impossible, are dropped).
+// apo_small_apply: tombstones, then the live cells of the tail [n1 - kk, n1) move into the holes
+// below it in ascending order (removeCell's swap-with-last, Colony.cpp:365-399, for a sorted
+// set of victims). The picks depend only on n1, so they can be drawn before the divisions are
+// placed; the apply reads the victims' slots, so it comes after.
+__device__ int apo_small_pick(const EventArgs &a, const ColonyConst &C, int k, int n1, int *sdv_out) {
   const int lane = threadIdx.x & 31;
   int v = 0x7fffffff;
   bool need = lane < k;
@@ -387,6 +388,13 @@ __device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, Colon
     const int val = __shfl_sync(0xffffffffu, v, src);
     if (((km >> src) & 1u) && __popc(km & ((1u << src) - 1u)) == lane) sdv = val;
   }
+  *sdv_out = sdv;
+  return kk;
+}
+
+__device__ void apo_small_apply(const EventArgs &a, const ColonyConst &C, ColonyCounters &K, int sdv, int kk,
+                                int n1, int D) {
+  const int lane = threadIdx.x & 31;
   if (lane < kk) {
     const int g = C.cell_base + sdv;
     const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
@@ -419,53 +427,61 @@ __device__ void apo_small(const EventArgs &a, const ColonyConst &C, int c, Colon
   }
 }
 
+// The number of deaths among n1 cells this step (thread-level). Philox mode: every cell
+// (daughters included) dies with probability p this step (CIL.cu:627-649); drawn as
+// k ~ Binomial(n1, p) by inversion and a uniformly random k-subset, the same distribution
+// without a draw per cell.
+__device__ int apo_count(const EventArgs &a, const ColonyConst &C, ColonyCounters &K, int n1) {
+  int k = 0;
+  if (C.apop_p > 0.0 && n1 > 0) {
+    const u32x4 r = philox4x32_10(C.rng_stream, static_cast<uint32_t>(a.ts), kRngApo, 0u, a.seed_lo, a.seed_hi);
+    const float nn = static_cast<float>(n1), p = static_cast<float>(C.apop_p);
+    const float mean = nn * p;
+    if (mean < 30.0f) {
+      // inversion of the binomial CDF from k = 0 (FP32: P(0) = exp(n log(1 - p)) >= e^-30);
+      // at most 200 terms (P(k > 200) is below FP32 resolution for a mean under 30)
+      const float u = static_cast<float>(r.v[0] >> 8) * 5.9604644775390625e-08f;
+      const float ratio = p / (1.0f - p);
+      float pk = __expf(nn * C.apop_log1m_p), cdf = pk;
+      while (u > cdf && k < n1 && k < kDeadCap && k < 200) {
+        pk *= (nn - static_cast<float>(k)) / static_cast<float>(k + 1) * ratio;
+        cdf += pk;
+        ++k;
+      }
+    } else {
+      // large means: normal approximation with continuity rounding
+      float z0, z1;
+      box_muller(r.v[0], r.v[1], z0, z1);
+      const float kf = rintf(mean + sqrtf(mean * (1.0f - p)) * z0);
+      k = kf < 0.0f ? 0 : static_cast<int>(fminf(kf, nn));
+    }
+    if (k >= kDeadCap) {
+      K.err |= kErrCap;
+      k = kDeadCap - 1;
+    }
+  }
+  return k;
+}
+
 // The step's apoptoses of colony c by one block (any multiple of 32 threads), after its
 // divisions: commits the divisions' counts, draws the number of deaths, picks distinct victims,
-// leaves tombstones and moves tail cells into the holes.
-__device__ void apo_colony(const EventArgs &a, int c, int D) {
+// leaves tombstones and moves tail cells into the holes. With planned (k_events_due), the
+// counts are committed and k (and, for k <= 32, warp 0's victims sdv / kk) were drawn already.
+__device__ void apo_colony(const EventArgs &a, int c, int D, bool planned = false, int k_planned = 0,
+                           int sdv_planned = 0, int kk_planned = 0) {
   __shared__ int sd[kDeadCap];
   __shared__ int s_n1, s_k;
   const ColonyConst &C = a.col[c];
   ColonyCounters &K = a.cnt[c];
   if (threadIdx.x == 0) {
-    const int add = K.ndiv_allowed;
-    K.ncell += add;
-    K.nslot += 2 * add;
-    K.ndiv_total += add;
-    s_n1 = K.ncell;
-    // Philox mode: every cell (daughters included) dies with probability p this step
-    // (CIL.cu:627-649); drawn as k ~ Binomial(n, p) by inversion and a uniformly random
-    // k-subset, the same distribution without a draw per cell
-    int k = 0;
-    if (C.apop_p > 0.0 && s_n1 > 0) {
-      const u32x4 r = philox4x32_10(C.rng_stream, static_cast<uint32_t>(a.ts), kRngApo, 0u, a.seed_lo, a.seed_hi);
-      const float nn = static_cast<float>(s_n1), p = static_cast<float>(C.apop_p);
-      const float mean = nn * p;
-      if (mean < 30.0f) {
-        // inversion of the binomial CDF from k = 0 (FP32: P(0) = exp(n log(1 - p)) >= e^-30);
-        // at most 200 terms (P(k > 200) is below FP32 resolution for a mean under 30)
-        const float u = static_cast<float>(r.v[0] >> 8) * 5.9604644775390625e-08f;
-        const float ratio = p / (1.0f - p);
-        float pk = __expf(nn * C.apop_log1m_p), cdf = pk;
-        while (u > cdf && k < s_n1 && k < kDeadCap && k < 200) {
-          pk *= (nn - static_cast<float>(k)) / static_cast<float>(k + 1) * ratio;
-          cdf += pk;
-          ++k;
-        }
-      } else {
-        // large means: normal approximation with continuity rounding
-        float z0, z1;
-        box_muller(r.v[0], r.v[1], z0, z1);
-        const float kf = rintf(mean + sqrtf(mean * (1.0f - p)) * z0);
-        k = kf < 0.0f ? 0 : static_cast<int>(fminf(kf, nn));
-      }
-      if (k >= kDeadCap) {
-        K.err |= kErrCap;
-        k = kDeadCap - 1;
-      }
+    if (!planned) {
+      const int add = K.ndiv_allowed;
+      K.ncell += add;
+      K.nslot += 2 * add;
+      K.ndiv_total += add;
     }
-    s_k = k;
-
+    s_n1 = K.ncell;
+    s_k = planned ? k_planned : apo_count(a, C, K, K.ncell);
   }
   __syncthreads();
   const int k = s_k, n1 = s_n1;
@@ -473,7 +489,9 @@ __device__ void apo_colony(const EventArgs &a, int c, int D) {
   if (k <= 32) {
     // few deaths (the usual case): one warp, no block barriers
     if (threadIdx.x >= 32) return;
-    apo_small(a, C, c, K, k, n1, D);
+    int sdv = sdv_planned, kk = kk_planned;
+    if (!planned) kk = apo_small_pick(a, C, k, n1, &sdv);
+    apo_small_apply(a, C, K, sdv, kk, n1, D);
     return;
   }
   int P = 1;
@@ -690,6 +708,22 @@ __global__ void __launch_bounds__(kTile) k_events_due(EventArgs a_) {
   }
   __syncthreads();
   const int allowed = s_allowed, nslot = K.nslot;
+  // the apoptosis draws depend only on the cell count after the divisions: the last warp draws
+  // them (and, for k <= 32, picks the victims) while the other warps place the divisions
+  __shared__ int s_k, s_kk, s_vic[32];
+  if (threadIdx.x >= kTile - 32) {
+    const int lane = threadIdx.x & 31;
+    int k = 0;
+    if (lane == 0) k = apo_count(a, C, K, n + allowed);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    int sdv = 0, kk = 0;
+    if (k > 0 && k <= 32) kk = apo_small_pick(a, C, k, n + allowed, &sdv);
+    s_vic[lane] = sdv;
+    if (lane == 0) {
+      s_k = k;
+      s_kk = kk;
+    }
+  }
   for (int r = threadIdx.x; r < allowed; r += blockDim.x) {
     const int i = keys[r];
     double dm[D], dd[D];
@@ -698,7 +732,13 @@ __global__ void __launch_bounds__(kTile) k_events_due(EventArgs a_) {
     divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
   }
   __syncthreads();  // every division is placed, and visible to the whole block
-  apo_colony(a, c, D);
+  if (threadIdx.x == 0) {
+    K.ncell = n + allowed;
+    K.nslot = nslot + 2 * allowed;
+    K.ndiv_total += allowed;
+  }
+  __syncthreads();
+  apo_colony(a, c, D, true, s_k, s_vic[threadIdx.x & 31], s_kk);
   __syncthreads();
   if (threadIdx.x == 0) {
     // the last colony's block moves the step counter (every block has read it by then)
