@@ -96,6 +96,9 @@ struct cil_handle {
   bool skin_mode = false;
   unsigned char *d_state[2] = {nullptr, nullptr};
   int *d_nbr = nullptr, *d_ncnt = nullptr, *d_fresh = nullptr;
+  int *d_lflat = nullptr, *d_lwarp = nullptr;  // the lists flattened per warp of 32 cells
+  unsigned char *d_oflat = nullptr;
+  unsigned short *d_lstart = nullptr;
   unsigned long long *d_fhead = nullptr, *d_fnext = nullptr;  // per-bin fresh lists
   float *d_uref = nullptr, *d_facc = nullptr;
   unsigned *d_ftouch = nullptr;  // one bit per slot: facc holds a fresh-pair contribution
@@ -171,7 +174,7 @@ void free_all(cil_handle *h) {
   void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
                   h->d_eid[1], h->d_pk[0], h->d_pk[1], h->d_sbin[0], h->d_sbin[1],
                   h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
-                  h->d_ncnt, h->d_fresh, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_ncnt, h->d_fresh, h->d_lflat, h->d_lwarp, h->d_oflat, h->d_lstart, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live, h->d_tiles_pairs,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dueq, h->d_evdone, h->d_dead, h->d_divq, h->d_obs,
@@ -405,6 +408,10 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
     a.skin = h->d_skin;
     a.nbr = h->d_nbr;
     a.ncnt = h->d_ncnt;
+    a.lflat = h->d_lflat;
+    a.oflat = h->d_oflat;
+    a.lstart = h->d_lstart;
+    a.lwarp = h->d_lwarp;
     a.uref = h->d_uref;
     a.facc = h->d_facc;
     a.ftouch = h->d_ftouch;
@@ -489,6 +496,10 @@ SkinArgs skin_args(cil_handle *h, int force_rebuild) {
   a.perm = h->d_perm;
   a.nbr = h->d_nbr;
   a.ncnt = h->d_ncnt;
+  a.lflat = h->d_lflat;
+  a.oflat = h->d_oflat;
+  a.lstart = h->d_lstart;
+  a.lwarp = h->d_lwarp;
   a.fresh = h->d_fresh;
   a.fhead = h->d_fhead;
   a.fnext = h->d_fnext;
@@ -776,6 +787,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     ra.state_out = nullptr;
     launch_rebuild(ra, h->grid_slots, rs);  // slot count unchanged: tile tables stay
     launch_skin_lists(skin_args(h, 0), h->D, h->cfg.force_law, h->grid_slots, rs);
+    launch_list_flatten(skin_args(h, 0), h->grid_slots, rs);
     if (use_cond) {
       cudaGraph_t body = nullptr;
       CUDA_TRY(h, cudaStreamEndCapture(h->side, &body));
@@ -783,7 +795,7 @@ cil_status enqueue_force_pass(cil_handle *h, bool last, int heun, bool first, cu
     launch_fresh_pairs(skin_args(h, 0), h->D, h->cfg.force_law, h->stream);
     h->lists_stale = false;
     // kernels of the rebuild node: counted when the node runs (cil_timings)
-    h->launches += permute ? 17 : (use_cond ? 2 : 8);
+    h->launches += permute ? 18 : (use_cond ? 2 : 9);
   } else {
     // the second half step of a Heun step reads the first half's velocities: carried through
     // the re-sort (only when velocities are written, i.e. the last step of a cil_step call)
@@ -1129,6 +1141,10 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     for (int b = 0; b < 2; ++b) h->d_state[b] = dalloc<unsigned char>(SS);
     h->d_nbr = dalloc<int>(static_cast<size_t>(kListCap) * SS);
     h->d_ncnt = dalloc<int>(SS);
+    h->d_lflat = dalloc<int>(static_cast<size_t>(kListCap) * SS);
+    h->d_oflat = dalloc<unsigned char>(static_cast<size_t>(kListCap) * SS);
+    h->d_lstart = dalloc<unsigned short>(SS);
+    h->d_lwarp = dalloc<int>(SS / 64 + 1);
     h->d_uref = dalloc<float>(D * SS);
     h->d_facc = dalloc<float>(D * SS);
     h->d_ftouch = dalloc<unsigned>((SS + 31) / 32);
@@ -1139,7 +1155,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_skin = dalloc<ColonySkin>(h->B);
     h->d_sched = dalloc<SchedState>(h->B);
     skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_ftouch &&
-              h->d_dueq &&
+              h->d_dueq && h->d_lflat && h->d_oflat && h->d_lstart && h->d_lwarp &&
               h->d_fresh &&
               h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
@@ -1213,6 +1229,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     cudaMemsetAsync(h->d_facc, 0, sizeof(float) * D * SS, h->stream);
     cudaMemsetAsync(h->d_ftouch, 0, sizeof(unsigned) * ((SS + 31) / 32), h->stream);
     cudaMemsetAsync(h->d_ncnt, 0, sizeof(int) * SS, h->stream);
+    // flattened lists: every entry a valid slot and every count 0 before the first build
+    cudaMemsetAsync(h->d_lflat, 0, sizeof(int) * kListCap * SS, h->stream);
+    cudaMemsetAsync(h->d_oflat, 0, static_cast<size_t>(kListCap) * SS, h->stream);
+    cudaMemsetAsync(h->d_lstart, 0, sizeof(unsigned short) * SS, h->stream);
+    cudaMemsetAsync(h->d_lwarp, 0, sizeof(int) * (SS / 64 + 1), h->stream);
     cudaMemsetAsync(h->d_state[0], kSlotDead, SS, h->stream);
     cudaMemsetAsync(h->d_state[1], kSlotDead, SS, h->stream);
   }
@@ -1679,13 +1700,13 @@ cil_status cil_timings(cil_handle *h, double *rebuild_ms, double *force_ms, doub
   if (events_ms) *events_ms = h->t_events;
   if (total_ms) *total_ms = h->t_total;
   if (launches) {
-    // plus the six kernels of every rebuild node that ran in the last cil_step call
+    // plus the seven kernels of every rebuild node that ran in the last cil_step call
     int runs = 0;
     if (h->skin_mode) {
       CUDA_TRY(h, cudaMemcpyAsync(&runs, h->d_anyreb + 3, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
       CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     }
-    *launches = h->launches + 6 * static_cast<int64_t>(runs);
+    *launches = h->launches + 7 * static_cast<int64_t>(runs);
   }
   return CIL_OK;
 }

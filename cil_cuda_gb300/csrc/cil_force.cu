@@ -583,10 +583,6 @@ __global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
 // Asynchronous global -> shared copies (cp.async, sm_80 and later): issued early, waited for
 // where the data is used, so their latency overlaps the work in between. Each thread waits
 // for its own copies; a __syncwarp after the wait publishes them to the warp.
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
@@ -634,54 +630,46 @@ constexpr int kOffStride = D == 2 ? 2 : 4;
 template <int D>
 constexpr int kOffCodes = D == 2 ? 16 : 64;
 
-// The warp's flattened list range: element 2 lane owns [st0, st1), element 2 lane + 1 owns
-// [st1, en1) of the T entries of the warp's 64 elements.
+// The warp's range of flattened list entries (k_list_flatten): element 2 lane owns [st0, en0),
+// element 2 lane + 1 owns [st1, en1) of the warp's T entries. T and the starts are those of the
+// last list build; an element that became fresh or dead since has an empty range (its entries
+// are still evaluated, and dropped).
 struct PairRange {
-  int st0, st1, en1, T;
+  int st0, en0, st1, en1, T;
 };
 
-// One segment [S, E) of the flattened range: every lane writes the owners of its entries and
-// starts the copies of the entries themselves (list entry k of element i of the warp sits at
-// nbr[k * SS + sw0 + i]; 32-bit offsets from the warp's first slot: k < 64 and, in skin mode,
-// SS < 2^26, checked when the handle is created, so k * SS + i < 2^32).
+// One segment [S, E) of the warp's range: 16-byte copies of its list entries and their owners
+// from the flattened lists. The warp's range starts 16 KB aligned and S is a multiple of 32, so
+// every copy is aligned; the copies round E up to 4 entries and 16 owners, which stays inside
+// the warp's 64 kListCap entries and inside the segment's shared arrays (SEG is a multiple of 32).
 template <int D, int SEG>
 __device__ __forceinline__ void pairs_segment_start(const ForceArgs &a, int sw0, const PairRange &R, int S,
                                                     const PairSmem<D, SEG> &sm) {
   const int lane = threadIdx.x & 31;
   const int E = min(R.T, S + SEG);
-  const int *lw = a.nbr + sw0;
-  const unsigned ss = static_cast<unsigned>(a.SS);
-  for (int f = max(R.st0, S); f < min(R.st1, E); ++f) {
-    sm.own[f - S] = static_cast<unsigned char>(2 * lane);
-    cp_async4(sm.ent + (f - S), lw + (static_cast<unsigned>(f - R.st0) * ss + static_cast<unsigned>(2 * lane)));
-  }
-  for (int f = max(R.st1, S); f < min(R.en1, E); ++f) {
-    sm.own[f - S] = static_cast<unsigned char>(2 * lane + 1);
-    cp_async4(sm.ent + (f - S), lw + (static_cast<unsigned>(f - R.st1) * ss + static_cast<unsigned>(2 * lane + 1)));
-  }
+  const int *le = a.lflat + static_cast<size_t>(sw0) * kListCap + S;
+  const unsigned char *lo = a.oflat + static_cast<size_t>(sw0) * kListCap + S;
+  const int ne = (E - S + 3) >> 2, no = (E - S + 15) >> 4;
+  for (int i = lane; i < ne; i += 32) cp_async16(sm.ent + 4 * i, le + 4 * i);
+  for (int i = lane; i < no; i += 32) cp_async16(sm.own + 16 * i, lo + 16 * i);
 }
 
 // The start of the pair pass, right after the cell's own loads: the records of the warp's 64
-// elements into shared memory, the flattened range, and the copies of the first segment.
-// Every lane calls it; lanes without a live cell pass n = (0, 0).
+// elements into shared memory, the warp's range, and the copies of the first segment. Every
+// lane calls it; lanes without a live cell pass n = (0, 0). ls: the two elements' starts;
+// Tw: the warp's entry count at the last build.
 template <int D, int SEG>
-__device__ __forceinline__ PairRange pairs_begin(const ForceArgs &a, int sw0, int2 nn, const float4 *pr,
-                                                 const PairSmem<D, SEG> &sm) {
+__device__ __forceinline__ PairRange pairs_begin(const ForceArgs &a, int sw0, int2 nn, ushort2 ls, int Tw,
+                                                 const float4 *pr, const PairSmem<D, SEG> &sm) {
   const int lane = threadIdx.x & 31;
   sm.rec[2 * lane] = pr[0];
   sm.rec[2 * lane + 1] = pr[1];
-  const int cnt = nn.x + nn.y;
-  int inc = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
-  }
   PairRange R;
-  R.T = __shfl_sync(0xffffffffu, inc, 31);
-  R.st0 = inc - cnt;
-  R.st1 = R.st0 + nn.x;
-  R.en1 = inc;
+  R.T = min(Tw, 64 * kListCap);
+  R.st0 = ls.x;
+  R.en0 = ls.x + nn.x;
+  R.st1 = ls.y;
+  R.en1 = ls.y + nn.y;
   pairs_segment_start<D, SEG>(a, sw0, R, 0, sm);
   return R;
 }
@@ -739,7 +727,7 @@ __device__ __forceinline__ void pairs_finish(const ForceArgs &a, const ColonyCon
     }
     __syncwarp();
     // each element adds its entries of the segment, in list order
-    for (int f = max(R.st0, S); f < min(R.st1, E); ++f)
+    for (int f = max(R.st0, S); f < min(R.en0, E); ++f)
 #pragma unroll
       for (int d = 0; d < D; ++d) F[0][d] += sm.c[(f - S) * D + d];
     for (int f = max(R.st1, S); f < min(R.en1, E); ++f)
@@ -770,6 +758,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   __shared__ unsigned s_dmax, s_smax;  // float bits of non-negative values
   __shared__ float s_ssum;
   __shared__ float s_half2;
+  __shared__ int s_nbuilt;
   __shared__ int s_warps_done;
   __shared__ __align__(16) float s_off[kOffCodes<D> * kOffStride<D>];
   const int t = blockIdx.x;
@@ -790,6 +779,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
       s_smax = 0u;
       s_ssum = 0.0f;
       s_half2 = a.skin[c].half2;
+      s_nbuilt = a.skin[c].nslot_built;
       s_warps_done = 0;
     }
   }
@@ -803,14 +793,19 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   const bool incap = s0 < C.slot_base + C.slot_cap;
   int2 ee = make_int2(-1, -1), sb = make_int2(0, 0), nn = make_int2(0, 0), cy = make_int2(0, 0);
   float4 pr[2] = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+  ushort2 ls = make_ushort2(0, 0);
   if (incap) {
     ee = __ldg(reinterpret_cast<const int2 *>(a.eid + s0));
     pr[0] = __ldg(a.pk + s0);
     pr[1] = __ldg(a.pk + s0 + 1);
     sb = __ldg(reinterpret_cast<const int2 *>(a.sbin + s0));
     nn = __ldg(reinterpret_cast<const int2 *>(a.ncnt + s0));
+    ls = __ldg(reinterpret_cast<const ushort2 *>(a.lstart + s0));
     if (C.divide) cy = __ldg(a.cyc + s0);
   }
+  // the warp's entry count at the last build (warps past the slots of that build have none)
+  const int sw0 = s0 - 2 * (tid & 31);
+  const int Tw = sw0 < C.slot_base + s_nbuilt ? __ldg(a.lwarp + (sw0 >> 6)) : 0;
   // fresh-pair contributions: one bit per slot; slot bases are 32-aligned and s0 is even, so
   // both bits of the cell sit in one word (16 cells per word)
   const unsigned tword = a.ftouch[s0 >> 5];
@@ -836,8 +831,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
   // copies of its list entries and of the cells' FP64 positions, which arrive while the
   // per-element terms below are evaluated
   PairSmem<D, SEG> sm(s_pairs + (tid >> 5) * pair_smem_warp<D, SEG>());
-  const int sw0 = s0 - 2 * (tid & 31);
-  const PairRange R = pairs_begin<D, SEG>(a, sw0, nn, pr, sm);
+  const PairRange R = pairs_begin<D, SEG>(a, sw0, nn, ls, Tw, pr, sm);
   if (live) {
 #pragma unroll
     for (int d = 0; d < D; ++d) cp_async16(sm.x + d * 64 + 2 * (tid & 31), a.x_in + d * SS + s0);

@@ -62,6 +62,7 @@ struct ColonySkin {
   int list_overflow;   // elements whose list was truncated at the last build
   int last_interval;   // steps between the last two rebuilds
   long long npairs;    // list entries at the last build
+  int nslot_built;     // used slots at the last build (the flattened lists cover these)
 };
 
 // Inputs of the learned skin scheduler, maintained on the device per colony in skin mode.
@@ -514,6 +515,12 @@ struct ForceArgs {
   ColonySkin *skin;
   const int *nbr;          // Verlet lists [kListCap][SS]
   const int *ncnt;
+  // the lists per warp of 32 cells (64 slots from w0), flattened: entries and their owners
+  // (element of the warp) at w0 * kListCap, element starts per slot, entries per warp
+  const int *lflat;
+  const unsigned char *oflat;
+  const unsigned short *lstart;
+  const int *lwarp;
   const float *uref;       // 3D only (2D: packed in the record's z word)
   float *facc;             // pair forces of fresh elements / reactions [D][SS], consumed and zeroed
   unsigned *ftouch;        // one bit per slot: facc holds a contribution
@@ -599,6 +606,10 @@ struct SkinArgs {
   const unsigned long long *perm;
   int *nbr;
   int *ncnt;
+  int *lflat;              // flattened lists per warp of 32 cells (see ForceArgs)
+  unsigned char *oflat;
+  unsigned short *lstart;
+  int *lwarp;
   const int *fresh;
   const unsigned long long *fhead;
   const unsigned long long *fnext;
@@ -686,6 +697,7 @@ void launch_force_list(const ForceArgs &a, int dim, int law, int grid, int varia
 void launch_skin_begin(const SkinArgs &a, cudaStream_t s);
 void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s);
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s);
+void launch_list_flatten(const SkinArgs &a, int grid, cudaStream_t s);
 void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
 // the device step counter advance; with tiles_cell also the tile table over the cells of the
 // step's events

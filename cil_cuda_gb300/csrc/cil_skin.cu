@@ -398,6 +398,63 @@ __global__ void __launch_bounds__(kTile, kListMinBlocks<D>) k_skin_lists(SkinArg
   }
 }
 
+// After a list build, the lists of each warp of the force kernel (32 cells = 64 slots from a
+// 64-aligned first slot w0) as one contiguous range in the warp's flattened order (element by
+// element, each list in order) at w0 * kListCap, with the owner (element of the warp) of every
+// entry, each element's start in the range (lstart) and the warp's entry count (lwarp): the force
+// kernel then copies a warp's entries and owners with a few 16-byte copies per lane. One block of
+// 128 threads per tile of kTile slots (4 warps of 64 slots), rebuilding colonies only.
+__global__ void __launch_bounds__(128) k_list_flatten(SkinArgs a) {
+  const int total = a.tiles[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles, a.B, t);
+    if (!a.skin[c].rebuild_now) continue;  // uniform per block
+    const ColonyConst &C = a.col[c];
+    const int lane = threadIdx.x & 31;
+    const int s0 = C.slot_base + (t - a.tiles[c]) * kTile + 2 * threadIdx.x;
+    const int nslot = a.cnt[c].nslot;
+    const int2 n = s0 < C.slot_base + nslot ? *reinterpret_cast<const int2 *>(a.ncnt + s0) : make_int2(0, 0);
+    const int cnt = n.x + n.y;
+    int inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += v;
+    }
+    const int st0 = inc - cnt, st1 = st0 + n.x;
+    const int w0 = s0 - 2 * lane;
+    if (s0 < C.slot_base + C.slot_cap)
+      *reinterpret_cast<ushort2 *>(a.lstart + s0) =
+          make_ushort2(static_cast<unsigned short>(st0), static_cast<unsigned short>(st1));
+    if (lane == 31) a.lwarp[w0 >> 6] = inc;
+    if (t == a.tiles[c] && threadIdx.x == 0) a.skin[c].nslot_built = nslot;
+    int *dst = a.lflat + static_cast<size_t>(w0) * kListCap;
+    unsigned char *dso = a.oflat + static_cast<size_t>(w0) * kListCap;
+    // both elements' entries in batches of 8 loads in flight (the list rows are SS apart)
+    const int nmax = n.x > n.y ? n.x : n.y;
+    for (int k0 = 0; k0 < nmax; k0 += 4) {
+      int v[2][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const size_t row = static_cast<size_t>(k0 + q) * a.SS + s0;
+        v[0][q] = k0 + q < n.x ? __ldg(a.nbr + row) : 0;
+        v[1][q] = k0 + q < n.y ? __ldg(a.nbr + row + 1) : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (k0 + q < n.x) {
+          dst[st0 + k0 + q] = v[0][q];
+          dso[st0 + k0 + q] = static_cast<unsigned char>(2 * lane);
+        }
+        if (k0 + q < n.y) {
+          dst[st1 + k0 + q] = v[1][q];
+          dso[st1 + k0 + q] = static_cast<unsigned char>(2 * lane + 1);
+        }
+      }
+    }
+  }
+}
+
 // Fresh elements (created or moved by divisions since the last build) against the normal
 // elements in the bins of the last build (with Newton's third law onto them through facc)
 // and against the other fresh elements through the per-bin fresh lists. One warp per fresh
@@ -600,6 +657,8 @@ void launch_skin_rebin(const SkinArgs &a, int dim, int grid, cudaStream_t s) {
   else
     k_skin_rebin<3><<<grid, kTile, 0, s>>>(a);
 }
+
+void launch_list_flatten(const SkinArgs &a, int grid, cudaStream_t s) { k_list_flatten<<<grid, 128, 0, s>>>(a); }
 
 void launch_skin_lists(const SkinArgs &a, int dim, int law, int grid, cudaStream_t s) {
   if (dim == 2)
