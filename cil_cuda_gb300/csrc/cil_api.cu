@@ -97,6 +97,7 @@ struct cil_handle {
   unsigned char *d_state[2] = {nullptr, nullptr};
   int *d_nbr = nullptr, *d_ncnt = nullptr, *d_fresh = nullptr;
   int *d_lflat = nullptr, *d_lwarp = nullptr;  // the lists flattened per warp of 32 cells
+  StatPart *d_spart = nullptr;                 // displacement statistics slots [B][kStatSlots]
   unsigned char *d_oflat = nullptr;
   unsigned short *d_lstart = nullptr;
   unsigned long long *d_fhead = nullptr, *d_fnext = nullptr;  // per-bin fresh lists
@@ -174,7 +175,7 @@ void free_all(cil_handle *h) {
   void *ptrs[] = {h->d_col, h->d_cnt, h->d_x[0], h->d_x[1], h->d_sig[0], h->d_sig[1], h->d_eid[0],
                   h->d_eid[1], h->d_pk[0], h->d_pk[1], h->d_sbin[0], h->d_sbin[1],
                   h->d_cyc[0], h->d_cyc[1], h->d_sigma_c, h->d_state[0], h->d_state[1], h->d_nbr,
-                  h->d_ncnt, h->d_fresh, h->d_lflat, h->d_lwarp, h->d_oflat, h->d_lstart, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
+                  h->d_ncnt, h->d_fresh, h->d_spart, h->d_lflat, h->d_lwarp, h->d_oflat, h->d_lstart, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live, h->d_tiles_pairs,
                   h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dueq, h->d_evdone, h->d_dead, h->d_divq, h->d_obs,
@@ -412,6 +413,7 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
     a.oflat = h->d_oflat;
     a.lstart = h->d_lstart;
     a.lwarp = h->d_lwarp;
+    a.spart = h->d_spart;
     a.uref = h->d_uref;
     a.facc = h->d_facc;
     a.ftouch = h->d_ftouch;
@@ -500,6 +502,7 @@ SkinArgs skin_args(cil_handle *h, int force_rebuild) {
   a.oflat = h->d_oflat;
   a.lstart = h->d_lstart;
   a.lwarp = h->d_lwarp;
+  a.spart = h->d_spart;
   a.fresh = h->d_fresh;
   a.fhead = h->d_fhead;
   a.fnext = h->d_fnext;
@@ -1145,6 +1148,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_oflat = dalloc<unsigned char>(static_cast<size_t>(kListCap) * SS);
     h->d_lstart = dalloc<unsigned short>(SS);
     h->d_lwarp = dalloc<int>(SS / 64 + 1);
+    h->d_spart = dalloc<StatPart>(static_cast<size_t>(h->B) * kStatSlots);
     h->d_uref = dalloc<float>(D * SS);
     h->d_facc = dalloc<float>(D * SS);
     h->d_ftouch = dalloc<unsigned>((SS + 31) / 32);
@@ -1155,7 +1159,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     h->d_skin = dalloc<ColonySkin>(h->B);
     h->d_sched = dalloc<SchedState>(h->B);
     skin_ok = h->d_state[0] && h->d_state[1] && h->d_nbr && h->d_ncnt && h->d_uref && h->d_facc && h->d_ftouch &&
-              h->d_dueq && h->d_lflat && h->d_oflat && h->d_lstart && h->d_lwarp &&
+              h->d_dueq && h->d_spart && h->d_lflat && h->d_oflat && h->d_lstart && h->d_lwarp &&
               h->d_fresh &&
               h->d_fnext && h->d_anyreb && h->d_skin && h->d_sched;
   }
@@ -1234,6 +1238,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     cudaMemsetAsync(h->d_oflat, 0, static_cast<size_t>(kListCap) * SS, h->stream);
     cudaMemsetAsync(h->d_lstart, 0, sizeof(unsigned short) * SS, h->stream);
     cudaMemsetAsync(h->d_lwarp, 0, sizeof(int) * (SS / 64 + 1), h->stream);
+    cudaMemsetAsync(h->d_spart, 0, sizeof(StatPart) * h->B * kStatSlots, h->stream);
     cudaMemsetAsync(h->d_state[0], kSlotDead, SS, h->stream);
     cudaMemsetAsync(h->d_state[1], kSlotDead, SS, h->stream);
   }
@@ -1606,10 +1611,17 @@ cil_status cil_skin_stats(cil_handle *h, int32_t colony, cil_skin_info *out) {
   if (colony < 0 || colony >= h->B || !out) return fail(h, CIL_ERR_CONFIG, "cil_skin_stats: bad arguments");
   if (!h->skin_mode) return fail(h, CIL_ERR_CONFIG, "cil_skin_stats: the handle has no skin");
   ColonySkin k;
+  StatPart part[kStatSlots];
   CUDA_TRY(h, cudaMemcpyAsync(&k, h->d_skin + colony, sizeof k, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(part, h->d_spart + static_cast<size_t>(colony) * kStatSlots, sizeof part,
+                              cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  // the largest displacement of the last force pass: its statistics slots (folded and cleared
+  // at the start of the next step)
+  unsigned bits = k.maxdisp2;
+  for (const StatPart &q : part) bits = q.dmax > bits ? q.dmax : bits;
   float md2;
-  std::memcpy(&md2, &k.maxdisp2, sizeof md2);
+  std::memcpy(&md2, &bits, sizeof md2);
   out->skin = k.skin;
   out->interval = k.interval;
   out->nrebuild = k.nrebuild;

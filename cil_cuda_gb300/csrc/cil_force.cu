@@ -1062,10 +1062,11 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
       __threadfence_block();
       if (atomicAdd(&s_warps_done, 1) == TILE / 32 - 1) {
         __threadfence_block();
-        atomicMax(&a.skin[c].maxdisp2, atomicOr(&s_dmax, 0u));
+        StatPart &P = a.spart[c * kStatSlots + (blockIdx.x & (kStatSlots - 1))];
+        atomicMax(&P.dmax, atomicOr(&s_dmax, 0u));
         if (a.sched) {
-          atomicMax(reinterpret_cast<unsigned *>(&a.sched[c].step_max), atomicOr(&s_smax, 0u));
-          atomicAdd(&a.sched[c].step_sum, atomicAdd(&s_ssum, 0.0f));
+          atomicMax(&P.smax, atomicOr(&s_smax, 0u));
+          atomicAdd(&P.ssum, atomicAdd(&s_ssum, 0.0f));
         }
       }
     }

@@ -65,6 +65,17 @@ struct ColonySkin {
   int nslot_built;     // used slots at the last build (the flattened lists cover these)
 };
 
+// The force pass's displacement statistics of a colony, spread over kStatSlots slots (slot =
+// block index mod kStatSlots) so that the blocks' closing atomics do not all meet on one
+// address; k_skin_begin folds and clears them at the next step.
+constexpr int kStatSlots = 32;
+struct StatPart {
+  unsigned dmax;  // largest |u - uref|^2 (float bits)
+  unsigned smax;  // largest |step displacement| (float bits)
+  float ssum;     // sum of |step displacement|
+  int pad;
+};
+
 // Inputs of the learned skin scheduler, maintained on the device per colony in skin mode.
 // The 12 features are formed by k_skin_begin at every list rebuild (before the statistics
 // of the new build are reset); the scheduler network (k_skin_begin) turns them into the colony's next skin and
@@ -525,6 +536,7 @@ struct ForceArgs {
   float *facc;             // pair forces of fresh elements / reactions [D][SS], consumed and zeroed
   unsigned *ftouch;        // one bit per slot: facc holds a contribution
   SchedState *sched;       // speed statistics for the scheduler
+  StatPart *spart;         // [B][kStatSlots] displacement statistics of this pass
   const double *noise;     // oracle mode: uploaded normals (already scaled), canonical order
   double *vel;             // slot order, may be null
   const double *vel_prev;  // Heun second half step: the first half's velocities (null: vel itself)
@@ -594,6 +606,7 @@ struct SkinArgs {
   ColonyCounters *cnt;
   ColonySkin *skin;
   SchedState *sched;       // scheduler inputs (always maintained in skin mode)
+  StatPart *spart;         // [B][kStatSlots] the last force pass's displacement statistics
   int B;
   size_t SS;
   const int *tiles;        // tiles over nslot

@@ -168,6 +168,23 @@ __global__ void k_skin_begin(SkinArgs a) {
   if (c >= a.B) return;  // uniform per warp
   const int lane = threadIdx.x & 31;
   int now = 0;
+  {
+    // the last force pass's displacement statistics, folded from the colony's slots
+    StatPart &P = a.spart[c * kStatSlots + lane];
+    const unsigned dmax = __reduce_max_sync(0xffffffffu, P.dmax);
+    const unsigned smax = __reduce_max_sync(0xffffffffu, P.smax);
+    float ssum = P.ssum;
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) ssum += __shfl_xor_sync(0xffffffffu, ssum, q);
+    P.dmax = 0u;
+    P.smax = 0u;
+    P.ssum = 0.0f;
+    if (lane == 0) {
+      a.skin[c].maxdisp2 = dmax;
+      a.sched[c].step_max = __uint_as_float(smax);
+      a.sched[c].step_sum = ssum;
+    }
+  }
   if (lane == 0) {
     now = skin_begin_colony(a, c);
     if (now && a.any_rebuild) atomicOr(&a.any_rebuild[*a.ts_dev & 1], 1);
