@@ -309,6 +309,12 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
                    deferred_status=True, **(tune or {}))
     h2d = st["pos"].nbytes + st["sigma"].nbytes + st["t0"].nbytes + st["tswitch"].nbytes
     d2h = 0
+    # the step's inputs sit in pinned host memory (registered before the timed region)
+    types = {"pos": np.float64, "sigma": np.float64, "t0": np.int32, "tswitch": np.int32}
+    st = {k: np.ascontiguousarray(v, types.get(k)) for k, v in st.items()}
+    pinned = [v for k, v in st.items() if k in ("pos", "sigma", "t0", "tswitch") and v.nbytes]
+    for v in pinned:
+        G.host_register(v)
     with tempfile.TemporaryDirectory() as tmp:
         # the output file and its staging are opened before the run, as the reference's
         # initializeOutput is (outside its simulation timer)
@@ -328,6 +334,8 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
         fs = w.last_stats
     n1 = eng.observables(0)["ncells"]
     eng.close()
+    for v in pinned:
+        G.host_unregister(v)
     d2h += fs["d2h_bytes"]
     return dict(value=(n + n1) * steps / wall, wall_s=wall, h2d=h2d / steps, d2h=d2h / steps,
                 frames=fs["frames_written"], file_bytes=fs["file_bytes"])

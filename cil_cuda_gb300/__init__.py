@@ -26,7 +26,8 @@ INTEGRATOR_EULER, INTEGRATOR_HEUN = 0, 1
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
           5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE", 8: "CIL_ERR_IO"}
 
-EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces",
+EXPORTED = ["cil_create", "cil_destroy", "cil_upload", "cil_download", "cil_step", "cil_forces", "cil_host_register",
+            "cil_host_unregister",
             "cil_bins", "cil_obs_reset", "cil_observables", "cil_timings", "cil_last_error",
             "cil_version", "cil_host_rng_draw", "cil_bin_elements_noalloc", "cil_skin_stats",
             "cil_set_skin", "cil_set_scheduler", "cil_sched_state", "cil_mlp_num_params",
@@ -391,6 +392,10 @@ def lib():
         L.cil_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
         L.cil_version.restype = C.c_char_p
         L.cil_version.argtypes = []
+        L.cil_host_register.restype = i32
+        L.cil_host_register.argtypes = [vp, C.c_size_t]
+        L.cil_host_unregister.restype = i32
+        L.cil_host_unregister.argtypes = [vp]
         L.cil_bin_elements_noalloc.restype = i32
         L.cil_bin_elements_noalloc.argtypes = [vp, i32, i32, dp, C.c_double, ip, vp, vp, i32, vp]
         L.cil_skin_stats.restype = i32
@@ -666,6 +671,22 @@ class Engine:
         self._check(self.L.cil_timings(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(t), C.byref(n)))
         return dict(rebuild_ms=a.value, force_ms=b.value, events_ms=c.value, total_ms=t.value,
                     launches=n.value)
+
+
+def host_register(arr: np.ndarray):
+    """Pins a C-contiguous numpy array's memory (cil_host_register), so uploads from it and
+    downloads into it are direct copies; release it with host_unregister before it is freed."""
+    if not arr.flags["C_CONTIGUOUS"] or arr.nbytes == 0:
+        raise ValueError("host_register: a non-empty C-contiguous array is needed")
+    st = lib().cil_host_register(arr.ctypes.data_as(C.c_void_p), arr.nbytes)
+    if st != 0:
+        raise CilError(st, "cil_host_register failed")
+
+
+def host_unregister(arr: np.ndarray):
+    st = lib().cil_host_unregister(arr.ctypes.data_as(C.c_void_p))
+    if st != 0:
+        raise CilError(st, "cil_host_unregister failed")
 
 
 def host_rng_draw(seed: int, kind: str, n: int) -> np.ndarray:

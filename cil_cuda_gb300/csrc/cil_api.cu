@@ -132,6 +132,7 @@ struct cil_handle {
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
   int *d_tiles_pairs = nullptr;  // skin mode: tiles over slot pairs (the cell-major force kernel)
   int *d_tile_count = nullptr, *d_tile_off = nullptr;
+  int *d_upchk = nullptr;     // upload checks: bad-value bits, largest diameter (double bits)
   int *d_dueq = nullptr;      // skin mode, Philox: cells due to divide, per colony (due_base)
   size_t due_total = 0;
   int *d_evdone = nullptr;    // skin mode, Philox: colonies whose events are done this step
@@ -178,7 +179,7 @@ void free_all(cil_handle *h) {
                   h->d_ncnt, h->d_fresh, h->d_spart, h->d_lflat, h->d_lwarp, h->d_oflat, h->d_lstart, h->d_uref, h->d_facc, h->d_ftouch, h->d_skin, h->d_sched, h->d_mlp, h->d_fhead, h->d_fnext, h->d_ts, h->d_anyreb, h->d_vel, h->d_vel2, h->d_frc, h->d_key, h->d_perm,
                   h->d_bcount, h->d_range, h->d_scan_sum, h->d_scan_off, h->d_scan_col,
                   h->d_slot_of, h->d_t0, h->d_tsw, h->d_tiles_used, h->d_tiles_live, h->d_tiles_pairs,
-                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_dueq, h->d_evdone, h->d_dead, h->d_divq, h->d_obs,
+                  h->d_tiles_cell, h->d_tile_count, h->d_tile_off, h->d_upchk, h->d_dueq, h->d_evdone, h->d_dead, h->d_divq, h->d_obs,
                   h->d_partials, h->d_stage, h->d_noise, h->d_oracle_i, h->d_oracle_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -950,6 +951,16 @@ extern "C" {
 
 const char *cil_version(void) { return "cil-gb300 0.1 (sm_103a)"; }
 
+cil_status cil_host_register(void *ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return CIL_ERR_CONFIG;
+  return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? CIL_OK : CIL_ERR_CUDA;
+}
+
+cil_status cil_host_unregister(void *ptr) {
+  if (!ptr) return CIL_ERR_CONFIG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? CIL_OK : CIL_ERR_CUDA;
+}
+
 cil_status cil_host_rng_draw(uint32_t seed, int32_t kind, int64_t n, double *out) {
   if (!out || n < 0 || kind < 0 || kind > 5) return CIL_ERR_CONFIG;
   HostRng r;
@@ -1187,6 +1198,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   for (int c = 0; c < h->B; ++c) h->ptiles += (h->cc[c].slot_cap + 2 * h->cell_block - 1) / (2 * h->cell_block);
   h->d_tile_count = dalloc<int>(h->ctiles + 1);
   h->d_tile_off = dalloc<int>(h->ctiles + 1);
+  h->d_upchk = dalloc<int>(4);
   h->d_evdone = dalloc<int>(1);
   h->d_dead = dalloc<int>(static_cast<size_t>(h->B) * kDeadCap);
   h->d_divq = dalloc<int>(static_cast<size_t>(h->CC));
@@ -1194,7 +1206,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
             h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
             h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
             h->d_tiles_pairs &&
-            h->d_tile_count && h->d_tile_off && h->d_evdone && h->d_dead && h->d_divq && h->d_ts &&
+            h->d_tile_count && h->d_tile_off && h->d_upchk && h->d_evdone && h->d_dead && h->d_divq && h->d_ts &&
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
             skin_ok;
   if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {
@@ -1245,6 +1257,21 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->grid_slots = std::max(1, std::min(h->nsm * 8, static_cast<int>((SS + kTile - 1) / kTile)));
   h->grid_cells = std::max(1, std::min(h->nsm * 8, h->ctiles));
   h->grid_force = h->grid_slots;
+  {
+    // the upload and download staging, sized for the largest colony here rather than at the
+    // first upload (an allocation would otherwise sit inside the first cil_upload)
+    size_t need = 0;
+    for (int c = 0; c < h->B; ++c) {
+      const size_t ne = 2 * static_cast<size_t>(h->hc[c].cap);
+      need = std::max(need, std::max(ne * D + ne + ne / 2 + 1, ne * 2 * D));
+    }
+    if (ensure_stage(h, need) != CIL_OK) {
+      h->err = "out of device memory (staging)";
+      free_all(h);
+      delete h;
+      return CIL_ERR_CUDA;
+    }
+  }
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
     h->err = "initialisation failed";
     free_all(h);
@@ -1273,33 +1300,29 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
   CUDA_TRY(h, cudaSetDevice(h->cfg.device));
   const int D = h->D;
   const ColonyConst &C = h->cc[colony];
-  double smax = 0.0;
-  for (int e = 0; e < 2 * n; ++e) {
-    const double s = v->sigma[e];
-    if (!(s > 0.0) || !std::isfinite(s)) return fail(h, CIL_ERR_CONFIG, "cil_upload: diameters must be positive");
-    smax = std::max(smax, s);
-  }
-  for (long long i = 0; i < 2ll * n * D; ++i) {
-    const int d = static_cast<int>(i % D);
-    const double x = v->pos[i];
-    if (!std::isfinite(x) || x < 0.0 || x >= hc.p.box[d])
-      return fail(h, CIL_ERR_OUT_OF_BOX, "cil_upload: position outside the box (CIL.cuh:54-66)");
-  }
-  const cil_status sst = ensure_stage(h, static_cast<size_t>(2 * n) * D);
+  // everything is staged and checked on the device (diameters positive and finite, positions
+  // finite and inside the box, CIL.cuh:54-66) before any of the colony's arrays is written, so a
+  // refused upload changes nothing
+  const size_t ne = 2 * static_cast<size_t>(n);
+  const cil_status sst = ensure_stage(h, ne * D + ne + static_cast<size_t>(n) + 1);
   if (sst != CIL_OK) return sst;
-  // the positions are re-binned by the first rebuild; the fresh slots follow the current
-  // buffers
-  CUDA_TRY(h, cudaMemcpyAsync(h->d_stage, v->pos, sizeof(double) * 2 * n * D, cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(h->d_sigma_c + 2 * static_cast<size_t>(C.cell_base), v->sigma, sizeof(double) * 2 * n,
-                              cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(h->d_t0 + C.cell_base, v->t0, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemcpyAsync(h->d_tsw + C.cell_base, v->tswitch, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
-  CUDA_TRY(h, cudaMemsetAsync(h->d_vel + 0, 0, sizeof(double) * D * h->SS, h->stream));
-  CUDA_TRY(h, cudaMemsetAsync(h->d_eid[h->meta] + C.slot_base, 0xff, sizeof(int) * C.slot_cap, h->stream));
-  launch_upload_scatter(h->d_col, colony, n, D, h->SS, h->d_stage, h->d_x[h->cur], h->d_eid[h->meta],
-                        h->d_slot_of, h->d_cnt, h->stream);
+  double *st_pos = h->d_stage, *st_sig = h->d_stage + ne * D;
+  int *st_t0 = reinterpret_cast<int *>(st_sig + ne), *st_tsw = st_t0 + n;
+  CUDA_TRY(h, cudaMemcpyAsync(st_pos, v->pos, sizeof(double) * ne * D, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(st_sig, v->sigma, sizeof(double) * ne, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(st_t0, v->t0, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemcpyAsync(st_tsw, v->tswitch, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(h, cudaMemsetAsync(h->d_upchk, 0, 4 * sizeof(int), h->stream));
+  launch_upload(h->d_col, colony, n, D, h->SS, h->d_stage, h->d_x[h->cur], h->d_sigma_c, h->d_t0, h->d_tsw,
+                h->d_vel, h->d_eid[h->meta], h->d_slot_of, h->d_cnt, h->d_upchk, h->stream);
   CUDA_TRY(h, cudaGetLastError());
+  int chk[4] = {0, 0, 0, 0};
+  CUDA_TRY(h, cudaMemcpyAsync(chk, h->d_upchk, sizeof chk, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+  if (chk[0] & 1) return fail(h, CIL_ERR_CONFIG, "cil_upload: diameters must be positive");
+  if (chk[0] & 2) return fail(h, CIL_ERR_OUT_OF_BOX, "cil_upload: position outside the box (CIL.cuh:54-66)");
+  double smax = 0.0;
+  std::memcpy(&smax, chk + 2, sizeof smax);
   hc.uploaded = true;
   hc.sigma_max = smax;
   hc.n = n;
@@ -1308,19 +1331,14 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
   hc.t0.resize(hc.cap);
   hc.tsw.resize(hc.cap);
   h->ts = v->ts;
-  {
-    const int tsi = static_cast<int>(v->ts);
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_ts, &tsi, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-  }
+  const int tsi = static_cast<int>(v->ts);
+  CUDA_TRY(h, cudaMemcpyAsync(h->d_ts, &tsi, sizeof(int), cudaMemcpyHostToDevice, h->stream));
   h->obs_ready[colony] = 0;
   h->geometry_ready = false;
   h->need_exact = true;
-  if (h->skin_mode) {
-    // the scheduler's statistics restart with the new state; the event counters restart too
-    CUDA_TRY(h, cudaMemsetAsync(h->d_sched + colony, 0, sizeof(SchedState), h->stream));
-    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-  }
+  // the scheduler's statistics restart with the new state
+  if (h->skin_mode) CUDA_TRY(h, cudaMemsetAsync(h->d_sched + colony, 0, sizeof(SchedState), h->stream));
+  CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return CIL_OK;
 }
 

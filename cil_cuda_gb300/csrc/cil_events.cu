@@ -799,19 +799,56 @@ __global__ void k_apo_ops(EventArgs a, int c, int ndiv, int nops, const int *ops
   }
 }
 
+// Upload, step 1: every staged diameter positive and finite (bit 1 of chk[0] otherwise) and
+// every staged position finite and in [0, L) on its axis (bit 2, CIL.cuh:54-66); the largest
+// diameter (positive doubles order like their bit patterns) into chk[1..2].
 template <int D>
-__global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, const double *pos, double *x,
-                         int *eid, int *slot_of, ColonyCounters *cnt) {
+__global__ void k_upload_check(const ColonyConst *col, int c, int ncells, const double *pos, const double *sig,
+                               int *chk) {
   const ColonyConst &C = col[c];
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < 2 * ncells) {
-    const int slot = C.slot_base + e;
+  if (e >= 2 * ncells) return;
+  const double s = sig[e];
+  int bad = (s > 0.0 && isfinite(s)) ? 0 : 1;
 #pragma unroll
-    for (int d = 0; d < D; ++d) x[d * SS + slot] = pos[static_cast<size_t>(e) * D + d];
-    eid[slot] = 2 * C.cell_base + e;
-    slot_of[2 * C.cell_base + e] = slot;
+  for (int d = 0; d < D; ++d) {
+    const double x = pos[static_cast<size_t>(e) * D + d];
+    if (!(isfinite(x) && x >= 0.0 && x < C.box[d])) bad |= 2;
   }
-  if (e == 0) {
+  if (bad) atomicOr(chk, bad);
+  if (!(bad & 1))
+    atomicMax(reinterpret_cast<unsigned long long *>(chk + 2), static_cast<unsigned long long>(__double_as_longlong(s)));
+}
+
+// Upload, step 2 (nothing happens when step 1 found a bad value): the staged positions into the
+// colony's first slots, the staged diameters and cycles into the cell arrays, element ids and
+// slots, zero velocities, every other slot of the colony empty, the counters.
+template <int D>
+__global__ void k_upload(const ColonyConst *col, int c, int ncells, size_t SS, const double *pos, const double *sig,
+                         const int *t0s, const int *tsws, double *x, double *sig_c, int *t0, int *tsw, double *vel,
+                         int *eid, int *slot_of, ColonyCounters *cnt, const int *chk) {
+  if (*chk != 0) return;  // uniform
+  const ColonyConst &C = col[c];
+  for (int slot = C.slot_base + blockIdx.x * blockDim.x + threadIdx.x; slot < C.slot_base + C.slot_cap;
+       slot += gridDim.x * blockDim.x) {
+    const int e = slot - C.slot_base;
+    if (e < 2 * ncells) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) x[d * SS + slot] = pos[static_cast<size_t>(e) * D + d];
+      eid[slot] = 2 * C.cell_base + e;
+      slot_of[2 * C.cell_base + e] = slot;
+      sig_c[2 * static_cast<size_t>(C.cell_base) + e] = sig[e];
+      if (e < ncells) {
+        t0[C.cell_base + e] = t0s[e];
+        tsw[C.cell_base + e] = tsws[e];
+      }
+    } else {
+      eid[slot] = -1;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) vel[d * SS + slot] = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     cnt[c].ncell = ncells;
     cnt[c].nslot = 2 * ncells;
     cnt[c].nlive = 0;
@@ -956,15 +993,23 @@ void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops,
   k_apo_ops<<<1, 32, 0, s>>>(a, colony, ndiv, nops, ops, dim);
 }
 
-void launch_upload_scatter(const ColonyConst *col, int colony, int ncells, int dim, size_t SS,
-                           const double *pos, double *x, int *eid, int *slot_of, ColonyCounters *cnt,
-                           cudaStream_t s) {
-  const int n = 2 * ncells > 0 ? 2 * ncells : 1;
-  const int blocks = (n + kTile - 1) / kTile;
-  if (dim == 2)
-    k_upload<2><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, x, eid, slot_of, cnt);
-  else
-    k_upload<3><<<blocks, kTile, 0, s>>>(col, colony, ncells, SS, pos, x, eid, slot_of, cnt);
+void launch_upload(const ColonyConst *col, int colony, int ncells, int dim, size_t SS, const double *stage,
+                   double *x, double *sig_c, int *t0, int *tsw, double *vel, int *eid, int *slot_of,
+                   ColonyCounters *cnt, int *chk, cudaStream_t s) {
+  // stage: positions [2n][dim], diameters [2n], then t0 and tswitch [n] each as int
+  const size_t ne = 2 * static_cast<size_t>(ncells);
+  const double *pos = stage, *sig = stage + ne * dim;
+  const int *t0s = reinterpret_cast<const int *>(sig + ne), *tsws = t0s + ncells;
+  const int blocks = static_cast<int>((ne + kTile - 1) / kTile);
+  if (dim == 2) {
+    if (ne) k_upload_check<2><<<blocks, kTile, 0, s>>>(col, colony, ncells, pos, sig, chk);
+    k_upload<2><<<1024, kTile, 0, s>>>(col, colony, ncells, SS, pos, sig, t0s, tsws, x, sig_c, t0, tsw, vel, eid,
+                                       slot_of, cnt, chk);
+  } else {
+    if (ne) k_upload_check<3><<<blocks, kTile, 0, s>>>(col, colony, ncells, pos, sig, chk);
+    k_upload<3><<<1024, kTile, 0, s>>>(col, colony, ncells, SS, pos, sig, t0s, tsws, x, sig_c, t0, tsw, vel, eid,
+                                       slot_of, cnt, chk);
+  }
 }
 
 void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,

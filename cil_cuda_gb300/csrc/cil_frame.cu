@@ -383,7 +383,7 @@ struct cil_frame_writer {
   std::string err;
   // thread-owned scratch
   std::vector<uint32_t> typeid_buf;
-  std::vector<float> fill_buf;
+  std::vector<float> charge_buf, mass_buf;  // the constant chunks, filled when the count grows
   // counters
   int64_t queued = 0, done = 0, d2h_bytes = 0, file_bytes = 0;
   double enqueue_ms = 0, slot_wait_ms = 0, write_ms = 0, pack_ms = 0, copy_ms = 0;
@@ -426,13 +426,13 @@ struct cil_frame_writer {
         CIL_W(cil_gsd_write_chunk(f, "particles/typeid", CIL_GSD_UINT32, E, 1, typeid_buf.data()));
       }
       if (j.charge) {
-        fill_buf.assign(E, -1.0f);  // cellTRho, never set by the two-element model
-        CIL_W(cil_gsd_write_chunk(f, "particles/charge", CIL_GSD_FLOAT, E, 1, fill_buf.data()));
+        if (charge_buf.size() < E) charge_buf.assign(E, -1.0f);  // cellTRho, never set by the two-element model
+        CIL_W(cil_gsd_write_chunk(f, "particles/charge", CIL_GSD_FLOAT, E, 1, charge_buf.data()));
       }
       CIL_W(cil_gsd_write_chunk(f, "particles/position", CIL_GSD_FLOAT, E, 3, pos));
       CIL_W(cil_gsd_write_chunk(f, "particles/velocity", CIL_GSD_FLOAT, E, 3, vel));
-      fill_buf.assign(E, 0.0f);  // pressure
-      CIL_W(cil_gsd_write_chunk(f, "particles/mass", CIL_GSD_FLOAT, E, 1, fill_buf.data()));
+      if (mass_buf.size() < E) mass_buf.assign(E, 0.0f);  // pressure
+      CIL_W(cil_gsd_write_chunk(f, "particles/mass", CIL_GSD_FLOAT, E, 1, mass_buf.data()));
     }
 #undef CIL_W
     return cil_gsd_end_frame(f);

@@ -723,9 +723,9 @@ void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, con
                            const double *dirs, const int *spans, int dim, cudaStream_t s);
 void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops, const int *ops, int dim,
                              cudaStream_t s);
-void launch_upload_scatter(const ColonyConst *col, int colony, int ncells, int dim, size_t SS,
-                           const double *pos, double *x, int *eid, int *slot_of, ColonyCounters *cnt,
-                           cudaStream_t s);
+void launch_upload(const ColonyConst *col, int colony, int ncells, int dim, size_t SS, const double *stage,
+                   double *x, double *sig_c, int *t0, int *tsw, double *vel, int *eid, int *slot_of,
+                   ColonyCounters *cnt, int *chk, cudaStream_t s);
 void launch_gather_canonical(int ncells, int dim, size_t SS, int cell_base, const int *slot_of,
                              const double *src, int width, double *dst, cudaStream_t s);
 void launch_observables(const EventArgs &a, int colony, int ncells, int dim, int reset,

@@ -321,6 +321,14 @@ cil_status cil_bin_elements_noalloc(const double *pos, int32_t n_elems, int32_t 
 /* Last error message of the handle (empty if none). */
 void cil_last_error(const cil_handle *h, char *buf, size_t len);
 
+/* Pins (page-locks) a host range for DMA with the GPUs (cudaHostRegister), so that cil_upload
+ * and cil_download from and into it run as direct copies instead of through a staging buffer
+ * (the reference's CellColony arrays, for instance, registered once after they are sized).
+ * cil_host_unregister releases it; ranges must not overlap a registered range. No counterpart in
+ * the reference. */
+cil_status cil_host_register(void *ptr, size_t bytes);
+cil_status cil_host_unregister(void *ptr);
+
 /* Library version string. */
 const char *cil_version(void);
 

@@ -260,3 +260,46 @@ def test_error_capacity_and_box(gpu_lib):
         eng.upload(0, **bad)
     assert e.value.status == 5
     eng.close()
+
+
+def test_refused_upload_changes_nothing_and_pinned_upload(gpu_lib):
+    """cil_upload checks its input on the device before writing any of the colony's arrays: a
+    refused upload (a position outside the box, a non-positive diameter) leaves the colony as it
+    was, and stepping goes on; an upload from registered (pinned) host arrays gives the same
+    state as one from ordinary arrays."""
+    p = S.growth_params(box=30.0, dt=1e-3)
+    st = S.disk_colony(50, p, seed=2)
+    eng = engine(gpu_lib, p, 200)
+    eng.upload(0, **st)
+    eng.step(3)
+    before = eng.download(0)
+    bad_box = dict(st, pos=st["pos"].copy())
+    bad_box["pos"][7, 1, 0] = -1e-9
+    bad_sigma = dict(st, sigma=st["sigma"].copy())
+    bad_sigma["sigma"][3, 0] = 0.0
+    for bad, status in ((bad_box, 5), (bad_sigma, 1)):
+        with pytest.raises(gpu_lib.CilError) as e:
+            eng.upload(0, **bad)
+        assert e.value.status == status
+        after = eng.download(0)
+        for k in ("pos", "sigma", "t0", "tswitch"):
+            np.testing.assert_array_equal(after[k], before[k])
+    eng.step(3)
+    eng.close()
+    outs = []
+    for pin in (False, True):
+        arrs = {"pos": np.ascontiguousarray(st["pos"], np.float64), "sigma": np.ascontiguousarray(st["sigma"], np.float64),
+                "t0": np.ascontiguousarray(st["t0"], np.int32), "tswitch": np.ascontiguousarray(st["tswitch"], np.int32)}
+        if pin:
+            for v in arrs.values():
+                gpu_lib.host_register(v)
+        e2 = engine(gpu_lib, p, 200)
+        e2.upload(0, **arrs)
+        e2.step(5)
+        outs.append(e2.download(0))
+        e2.close()
+        if pin:
+            for v in arrs.values():
+                gpu_lib.host_unregister(v)
+    for k in ("pos", "sigma", "t0", "tswitch"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
