@@ -420,14 +420,19 @@ __global__ void __launch_bounds__(kTile, kListMinBlocks<D>) k_skin_lists(SkinArg
 // element, each list in order) at w0 * kListCap, with the owner (element of the warp) of every
 // entry, each element's start in the range (lstart) and the warp's entry count (lwarp): the force
 // kernel then copies a warp's entries and owners with a few 16-byte copies per lane. One block of
-// 128 threads per tile of kTile slots (4 warps of 64 slots), rebuilding colonies only.
+// 128 threads per tile of kTile slots (4 warps of 64 slots), rebuilding colonies only; each warp
+// assembles segments of kFlatSeg entries in shared memory and stores them with 16-byte stores.
+constexpr int kFlatSeg = 1024;
+
 __global__ void __launch_bounds__(128) k_list_flatten(SkinArgs a) {
+  __shared__ __align__(16) int s_ent[4][kFlatSeg];
+  __shared__ __align__(16) unsigned char s_own[4][kFlatSeg];
   const int total = a.tiles[a.B];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     const int c = colony_of_tile(a.tiles, a.B, t);
     if (!a.skin[c].rebuild_now) continue;  // uniform per block
     const ColonyConst &C = a.col[c];
-    const int lane = threadIdx.x & 31;
     const int s0 = C.slot_base + (t - a.tiles[c]) * kTile + 2 * threadIdx.x;
     const int nslot = a.cnt[c].nslot;
     const int2 n = s0 < C.slot_base + nslot ? *reinterpret_cast<const int2 *>(a.ncnt + s0) : make_int2(0, 0);
@@ -438,6 +443,7 @@ __global__ void __launch_bounds__(128) k_list_flatten(SkinArgs a) {
       const int v = __shfl_up_sync(0xffffffffu, inc, o);
       if (lane >= o) inc += v;
     }
+    const int T = __shfl_sync(0xffffffffu, inc, 31);
     const int st0 = inc - cnt, st1 = st0 + n.x;
     const int w0 = s0 - 2 * lane;
     if (s0 < C.slot_base + C.slot_cap)
@@ -447,27 +453,37 @@ __global__ void __launch_bounds__(128) k_list_flatten(SkinArgs a) {
     if (t == a.tiles[c] && threadIdx.x == 0) a.skin[c].nslot_built = nslot;
     int *dst = a.lflat + static_cast<size_t>(w0) * kListCap;
     unsigned char *dso = a.oflat + static_cast<size_t>(w0) * kListCap;
-    // both elements' entries in batches of 8 loads in flight (the list rows are SS apart)
-    const int nmax = n.x > n.y ? n.x : n.y;
-    for (int k0 = 0; k0 < nmax; k0 += 4) {
-      int v[2][4];
+    int *se = s_ent[wid];
+    unsigned char *so = s_own[wid];
+    for (int S = 0; S < T; S += kFlatSeg) {  // uniform per warp
+      const int E = min(T, S + kFlatSeg);
+      // this lane's entries of the segment, read row by row (the list rows are SS apart)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const size_t row = static_cast<size_t>(k0 + q) * a.SS + s0;
-        v[0][q] = k0 + q < n.x ? __ldg(a.nbr + row) : 0;
-        v[1][q] = k0 + q < n.y ? __ldg(a.nbr + row + 1) : 0;
-      }
+      for (int j = 0; j < 2; ++j) {
+        const int st = j ? st1 : st0, nj = j ? n.y : n.x;
+        const int k0 = max(S - st, 0), k1 = min(E - st, nj);
+        for (int k = k0; k < k1; k += 4) {
+          int v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (k0 + q < n.x) {
-          dst[st0 + k0 + q] = v[0][q];
-          dso[st0 + k0 + q] = static_cast<unsigned char>(2 * lane);
-        }
-        if (k0 + q < n.y) {
-          dst[st1 + k0 + q] = v[1][q];
-          dso[st1 + k0 + q] = static_cast<unsigned char>(2 * lane + 1);
+          for (int q = 0; q < 4; ++q) v[q] = k + q < k1 ? __ldg(a.nbr + static_cast<size_t>(k + q) * a.SS + s0 + j) : 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (k + q < k1) {
+              se[st + k + q - S] = v[q];
+              so[st + k + q - S] = static_cast<unsigned char>(2 * lane + j);
+            }
+          }
         }
       }
+      __syncwarp();
+      // 16-byte stores of the segment (rounded up to 4 entries / 16 owners: within the warp's
+      // 64 kListCap entries and within the shared segment)
+      const int ne = (E - S + 3) >> 2, no = (E - S + 15) >> 4;
+      for (int i = lane; i < ne; i += 32)
+        *reinterpret_cast<int4 *>(dst + S + 4 * i) = *reinterpret_cast<const int4 *>(se + 4 * i);
+      for (int i = lane; i < no; i += 32)
+        *reinterpret_cast<int4 *>(dso + S + 16 * i) = *reinterpret_cast<const int4 *>(so + 16 * i);
+      __syncwarp();
     }
   }
 }
