@@ -659,6 +659,7 @@ __device__ void block_bitonic_sort(int *v, int P) {
 }
 
 constexpr int kDueSort = 2048;  // due cells sorted in shared memory (more: in the queue itself)
+constexpr int kDueRank = 512;   // up to this many: sorted by ranks instead of a sorting network
 
 // Skin mode, Philox: the step's events from the due-cell queues, one block per colony. The
 // force pass appended the cells whose cycle ends at this step (in no particular order); the
@@ -675,22 +676,36 @@ __global__ void __launch_bounds__(kTile) k_events_due(EventArgs a_) {
   const int c = blockIdx.x;
   const ColonyConst &C = a.col[c];
   ColonyCounters &K = a.cnt[c];
-  __shared__ int s_key[kDueSort];
+  __shared__ int s_key[kDueSort], s_sorted[kDueRank];
   __shared__ int s_allowed;
   const int n = K.ncell;
   const int nd = min(K.ndue, n);
-  int P = 1;
-  while (P < nd) P <<= 1;
-  int *q = a.dueq + C.due_base;  // capacity: a power of two >= cell_cap >= P
+  int *q = a.dueq + C.due_base;  // capacity: a power of two >= cell_cap
   int *keys = s_key;
-  if (P <= kDueSort) {
-    for (int i = threadIdx.x; i < P; i += blockDim.x) s_key[i] = i < nd ? q[i] : 0x7fffffff;
+  if (nd <= kDueRank) {
+    // the keys are distinct cell indices: each one's rank is the number of smaller keys, so
+    // one pass over the shared keys (and two barriers) sorts them
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) s_key[i] = q[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+      const int v = s_key[i];
+      int r = 0;
+      for (int j = 0; j < nd; ++j) r += s_key[j] < v ? 1 : 0;
+      s_sorted[r] = v;
+    }
+    keys = s_sorted;
   } else {
-    for (int i = nd + static_cast<int>(threadIdx.x); i < P; i += blockDim.x) q[i] = 0x7fffffff;
-    keys = q;
+    int P = 1;
+    while (P < nd) P <<= 1;
+    if (P <= kDueSort) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) s_key[i] = i < nd ? q[i] : 0x7fffffff;
+    } else {
+      for (int i = nd + static_cast<int>(threadIdx.x); i < P; i += blockDim.x) q[i] = 0x7fffffff;
+      keys = q;
+    }
+    __syncthreads();
+    block_bitonic_sort(keys, P);
   }
-  __syncthreads();
-  if (nd > 1) block_bitonic_sort(keys, P);
   if (threadIdx.x == 0) {
     // room for the cells and for their two element slots each (skin mode appends daughters
     // behind removed elements until the next slot re-sort)
