@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
     stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
     int kflat = 0;  // candidates of the bins walked so far
     const double c2 = C.hz_c + C.hz_c;
+    const double inv_hz = 1.0 / (0.75 * c2);
     const double inv_ri = 1.0 / (si / 2);
     const float sif = static_cast<float>(si), c2f = static_cast<float>(c2), adhf = static_cast<float>(C.adhesion);
     const float inv_rif = 2.0f / sif;
@@ -547,7 +548,8 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             // symmetric in the two diameters)
             const double sa = i < j ? si : sj, sb = i < j ? sj : si;
             const double h = fmax((si + sj) / 2 - r, 0.0);
-            const double fel = (h * sqrt(h)) / (0.75 * c2 * sqrt(inv_ri + inv_r[j]));  // h^1.5
+            // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2): one square root fewer
+            const double fel = h * sqrt(h / (inv_ri + inv_r[j])) * inv_hz;
             double A, vol;
             if (D == 3) {
               A = contact_area(r, sa, sb);
@@ -693,14 +695,15 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
           const double r = sqrt(separation(C, S, xi, j, rij));
           const double rc = i < j ? si : S.sig[j];
           if (!(r < rc) || r == 0.0) continue;
-          const double w = 1 - (r / rc);
+          const double ir = 1.0 / r;  // one division for the weight and the unit vector
+          const double w = 1 - r / rc;
           const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
           double xi_n[4];
           normal2(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xi_n[0], &xi_n[1]);
           if (D == 3) normal2(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xi_n[2], &xi_n[3]);
           const double sw = sqrt(w);
           CY_AXES(d, D) {
-            const double nd = rij[d] / r;
+            const double nd = rij[d] * ir;
             const double vj = S.v[d * cap + j];
             Fd[d] -= C.gamma_d * w * ((vi[d] - vj) * nd) * nd;
             Fr[d] += C.sigma_r * sw * nd * xi_n[d];

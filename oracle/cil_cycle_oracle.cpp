@@ -323,7 +323,8 @@ struct Model {
       if (!(r <= (si + sj) / 2) || r == 0.0) return;
       const double sa = i < j ? si : sj, sb = i < j ? sj : si;
       const double h = std::fmax((si + sj) / 2 - r, 0.0);
-      const double fel = (h * std::sqrt(h)) / (0.75 * c2 * std::sqrt(1.0 / (si / 2) + 1.0 / (sj / 2)));
+      // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2), the GPU model's expression
+      const double fel = h * std::sqrt(h / (1.0 / (si / 2) + 1.0 / (sj / 2))) * (1.0 / (0.75 * c2));
       double A, vol;
       if (D == 3) {
         A = contact_area(r, sa, sb);
@@ -426,8 +427,9 @@ struct Model {
         normal2(philox(a, static_cast<uint32_t>(key), kDpd0, z, k0, k1), &xi[0], &xi[1]);
         if (D == 3) normal2(philox(a, static_cast<uint32_t>(key), kDpd1, z, k0, k1), &xi[2], &xi[3]);
         const double sw = std::sqrt(w);
+        const double ir = 1.0 / r;  // the GPU model's one division per pair
         for (int d = 0; d < D; ++d) {
-          const double nd = rij[d] / r;
+          const double nd = rij[d] * ir;
           Fd[d] -= p.dis_diff * w * ((c[i].v[d] - c[j].v[d]) * nd) * nd;
           Fr[d] += sigma_r * sw * nd * xi[d];
         }
