@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcilgpu.so")
 
-FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ = 0, 1, 2
+FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ, FORCE_SC = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 RNG_PHILOX, RNG_DSFMT = 0, 1
 FLAG_NO_GRAPH = 1
@@ -73,6 +73,10 @@ class ColonyParams(C.Structure):
         ("div_tau_mu", C.c_double),
         ("div_tau_sigma", C.c_double),
         ("apop_rate", C.c_double),
+        ("well_epsilon", C.c_double),
+        ("well_sigma", C.c_double),
+        ("force_shifted", C.c_int32),
+        ("pad_sc", C.c_int32),
     ]
 
 

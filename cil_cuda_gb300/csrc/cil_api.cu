@@ -215,7 +215,9 @@ void grid_geometry(const cil_colony_params &p, double width, int *ns, bool *sing
 double bin_width_for(const cil_handle *h, const HostColony &c) {
   // a colony without cells stays without (nothing divides): one bin
   if (!(c.sigma_max > 0.0)) return std::max(c.p.box[0], std::max(c.p.box[1], c.p.box[2]));
-  const double need = c.p.rcut_scale * c.sigma_max + h->cfg.skin;
+  // the law's reach for the largest diameter (the soft-core well reaches xi past contact)
+  const double reach = c.p.force_law == CIL_FORCE_SC ? c.sigma_max + c.p.well_sigma : c.sigma_max;
+  const double need = c.p.rcut_scale * reach + h->cfg.skin;
   return h->cfg.bin_width > need ? h->cfg.bin_width : need;
 }
 
@@ -991,7 +993,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   if (!cfg || !params || !cap_cells) return CIL_ERR_CONFIG;
   if (cfg->dim != 2 && cfg->dim != 3) return CIL_ERR_CONFIG;
   if (cfg->num_colonies <= 0) return CIL_ERR_CONFIG;
-  if (cfg->force_law < 0 || cfg->force_law > 2) return CIL_ERR_CONFIG;
+  if (cfg->force_law < 0 || cfg->force_law > 3) return CIL_ERR_CONFIG;
   if (cfg->precision != CIL_PREC_FP64 && cfg->precision != CIL_PREC_MIXED) return CIL_ERR_CONFIG;
   if (cfg->rng_mode != CIL_RNG_PHILOX && cfg->rng_mode != CIL_RNG_DSFMT) return CIL_ERR_CONFIG;
   if (cfg->skin < 0.0 || (cfg->skin > 0.0 && cfg->precision != CIL_PREC_MIXED)) return CIL_ERR_CONFIG;
@@ -1024,7 +1026,8 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     const cil_colony_params &p = params[c];
     if (p.dim != cfg->dim || p.force_law != cfg->force_law || cap_cells[c] <= 0 || !(p.dt > 0.0) ||
         !(p.zeta[0] > 0.0) || !(p.zeta[1] > 0.0) || p.nwalls < 0 || p.nwalls > 2 ||
-        !(p.rcut_scale > 0.0)) {
+        !(p.rcut_scale > 0.0) ||
+        (p.force_law == CIL_FORCE_SC && (!(p.well_sigma > 0.0) || !(p.well_epsilon >= 0.0)))) {
       delete h;
       return CIL_ERR_CONFIG;
     }
@@ -1096,6 +1099,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.amp_f = static_cast<float>(C.noise_amp);
     C.eps_f = static_cast<float>(C.epsilon);
     C.rcs_f = static_cast<float>(C.rcut_scale);
+    C.well_eps = p.force_law == CIL_FORCE_SC ? p.well_epsilon : 0.0;
+    C.well_sigma = p.force_law == CIL_FORCE_SC ? p.well_sigma : 0.0;
+    C.well_eps_f = static_cast<float>(C.well_eps);
+    C.well_sigma_f = static_cast<float>(C.well_sigma);
+    C.force_shifted = (p.force_law == CIL_FORCE_SC || p.force_law == CIL_FORCE_LJ_WCA) && p.force_shifted ? 1 : 0;
     C.wall_E_f = static_cast<float>(C.wall_E);
     C.due_base = static_cast<int>(due_acc);
     {

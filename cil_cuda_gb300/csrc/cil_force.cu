@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
           r2 += v * v;
         }
         double f0;
-        if (pair_force<LAW, double>(r2, si, a.sig[tt], eps, rcs, f0)) {
+        if (pair_force<LAW, double>(r2, si, a.sig[tt], eps, rcs, f0, C.well_eps, C.well_sigma, C.force_shifted)) {
 #pragma unroll
           for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
         }
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
                 r2 += dx[d] * dx[d];
               }
               double f0;
-              if (pair_force<LAW, double>(r2, si, __ldg(a.sig + tt), eps, rcs, f0)) {
+              if (pair_force<LAW, double>(r2, si, __ldg(a.sig + tt), eps, rcs, f0, C.well_eps, C.well_sigma, C.force_shifted)) {
 #pragma unroll
                 for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
               }
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
             dx[d] = pk_c(pj, d) + offv[d];
             r2 += dx[d] * dx[d];
           }
-          const float f0 = pair_f0_fast<LAW>(r2, sh, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != gh);
+          const float f0 = pair_f0_fast<LAW>(r2, sh, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != gh, C.well_eps_f, C.well_sigma_f, C.force_shifted);
 #pragma unroll
           for (int d = 0; d < D; ++d) acc[d] += f0 * dx[d];
           if (++p >= p1) break;
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kTile) k_force_mixed(ForceArgs a_) {
             dx[d] = v;
             r2 += v * v;
           }
-          const float f0 = pair_f0_fast<LAW>(r2, si, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != g);
+          const float f0 = pair_f0_fast<LAW>(r2, si, pj.w, eps, rcs, ej >= 0 && (ej >> 1) != g, C.well_eps_f, C.well_sigma_f, C.force_shifted);
 #pragma unroll
           for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
         }
@@ -719,7 +719,7 @@ __device__ __forceinline__ void pairs_finish(const ForceArgs &a, const ColonyCon
           dx[d] = pk_c(pj[u], d) + (ov[d] - pk_c(me, d));
           r2 += dx[d] * dx[d];
         }
-        const float f0 = pair_f0_fast<LAW>(r2, fabsf(me.w), pj[u].w, eps, rcs, pj[u].w > 0.0f);
+        const float f0 = pair_f0_fast<LAW>(r2, fabsf(me.w), pj[u].w, eps, rcs, pj[u].w > 0.0f, C.well_eps_f, C.well_sigma_f, C.force_shifted);
         float *cf = sm.c + (base + 32 * u + lane - S) * D;
 #pragma unroll
         for (int d = 0; d < D; ++d) cf[d] = f0 * dx[d];
@@ -1101,15 +1101,18 @@ template <int D, int LAW>
 void launch_list_dl(const ForceArgs &a, int grid, int variant, int block, cudaStream_t s) {
   // cell-major slots, one thread per cell, the warp's list entries flattened; variants
   // (chunks of 32 entries in flight per warp, CTAs per SM at 256 threads): 0 (4, 3), 1 (2, 3),
-  // 2 (1, 3), 3 (1, 4); block: 128, 256 or 512 threads (cells per block)
-  if (variant == 0) {
+  // 2 (1, 3), 3 (1, 4); block: 128, 256 or 512 threads (cells per block). The reference's
+  // soft-core well is compiled in the default variant only.
+  if (LAW == CIL_FORCE_SC || variant == 0) {
     launch_cells<D, LAW, 4, 3>(a, grid, block, s);
-  } else if (variant == 1) {
-    launch_cells<D, LAW, 2, 3>(a, grid, block, s);
-  } else if (variant == 2) {
-    launch_cells<D, LAW, 1, 3>(a, grid, block, s);
-  } else {
-    launch_cells<D, LAW, 1, 4>(a, grid, block, s);
+  } else if constexpr (LAW != CIL_FORCE_SC) {
+    if (variant == 1) {
+      launch_cells<D, LAW, 2, 3>(a, grid, block, s);
+    } else if (variant == 2) {
+      launch_cells<D, LAW, 1, 3>(a, grid, block, s);
+    } else {
+      launch_cells<D, LAW, 1, 4>(a, grid, block, s);
+    }
   }
 }
 
@@ -1121,6 +1124,9 @@ void launch_list_d(const ForceArgs &a, int law, int grid, int variant, int block
       break;
     case CIL_FORCE_SOFTCORE:
       launch_list_dl<D, CIL_FORCE_SOFTCORE>(a, grid, variant, block, s);
+      break;
+    case CIL_FORCE_SC:
+      launch_list_dl<D, CIL_FORCE_SC>(a, grid, variant, block, s);
       break;
     default:
       launch_list_dl<D, CIL_FORCE_HERTZ>(a, grid, variant, block, s);
@@ -1157,6 +1163,9 @@ void launch_d(const ForceArgs &a, int law, int prec, int grid, cudaStream_t s) {
       break;
     case CIL_FORCE_SOFTCORE:
       launch_dl<D, CIL_FORCE_SOFTCORE>(a, prec, grid, s);
+      break;
+    case CIL_FORCE_SC:
+      launch_dl<D, CIL_FORCE_SC>(a, prec, grid, s);
       break;
     default:
       launch_dl<D, CIL_FORCE_HERTZ>(a, prec, grid, s);

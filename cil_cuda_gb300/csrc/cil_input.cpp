@@ -29,6 +29,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <utility>
 #include <vector>
 
 #include "cil_cycle.h"
@@ -346,6 +347,39 @@ struct Node {
     for (const auto &e : a) {
       if (e.kind != JVal::kStr) key_error(c.path, "expected strings");
       out.push_back(e.str);
+    }
+    return out;
+  }
+  // [[a, b], ...]: pairs of strings (the DOMAIN SPECIES list, Input.cpp:318-322)
+  std::vector<std::pair<std::string, std::string>> str_pairs(const std::string &k) const {
+    Node c{nullptr, ""};
+    const auto &a = array(k, &c);
+    std::vector<std::pair<std::string, std::string>> out;
+    for (const auto &e : a) {
+      if (e.kind != JVal::kArr || e.arr.size() != 2) key_error(c.path, "Wrong cell pair specification");
+      for (const auto &q : e.arr)
+        if (q.kind != JVal::kStr) key_error(c.path, "expected strings");
+      out.emplace_back(e.arr[0].str, e.arr[1].str);
+    }
+    return out;
+  }
+  // [[[cell, elem], [cell, elem]], ...]: pairs of (cell, element) names (the DOMAIN ELEMENTS
+  // list, Input.cpp:330-345)
+  std::vector<std::pair<std::pair<std::string, std::string>, std::pair<std::string, std::string>>> elem_pairs(
+      const std::string &k) const {
+    Node c{nullptr, ""};
+    const auto &a = array(k, &c);
+    std::vector<std::pair<std::pair<std::string, std::string>, std::pair<std::string, std::string>>> out;
+    for (const auto &e : a) {
+      if (e.kind != JVal::kArr || e.arr.size() != 2) key_error(c.path, "Wrong element pair specification");
+      std::pair<std::string, std::string> ce[2];
+      for (int q = 0; q < 2; ++q) {
+        const JVal &x = e.arr[q];
+        if (x.kind != JVal::kArr || x.arr.size() != 2 || x.arr[0].kind != JVal::kStr || x.arr[1].kind != JVal::kStr)
+          key_error(c.path, "Wrong element pair specification");
+        ce[q] = {x.arr[0].str, x.arr[1].str};
+      }
+      out.emplace_back(ce[0], ce[1]);
     }
     return out;
   }
@@ -728,14 +762,82 @@ void read_all(cil_input *in) {
     p.epsilon = gpu.num("EPSILON");
     p.rcut_scale = gnum("RCUT_SCALE", law == "LJ_WCA" ? std::pow(2.0, 1.0 / 6.0) : 1.0);
   } else if (pair == "LJ") {
+    // readInteractionsLJ (Input.cpp:294-352): the WCA cutoff rc2 = 2^(1/3), or with ATTRACTION ON
+    // rc2 = RCUT^2 over the pairs its DOMAIN names and SHIFT FORCE -> OPT::FORCE_SHIFTED
     Node att = root.child("INTERACTIONS").child("PAIRFORCES").child("LJ").child("ATTRACTION");
-    if (att.pick("SELECT", {"ON", "OFF"}) != "OFF")
-      key_error(att.path + ".SELECT", "LJ attraction is not modelled by the GPU step (WCA only)");
     if (eps_lj[0] != eps_lj[1])
       key_error(loc.path + ".PAIRFORCES.LJ.EPSILON", "the GPU step uses one epsilon per species");
     cfg.force_law = CIL_FORCE_LJ_WCA;
     p.epsilon = eps_lj[0];
     p.rcut_scale = std::pow(2.0, 1.0 / 6.0);
+    p.force_shifted = 0;
+    if (att.pick("SELECT", {"ON", "OFF"}) == "ON") {
+      Node on = att.child("ON");
+      const double rcut = on.num("RCUT");
+      if (on.pick("SHIFT", {"FORCE", "POTENTIAL"}) == "FORCE") p.force_shifted = 1;
+      if (!(rcut * rcut >= std::pow(2.0, 1.0 / 3.0))) key_error(on.path + ".RCUT", "Invalid LJ cutoff");
+      Node dom = on.child("DOMAIN");
+      const std::string sel = dom.pick("SELECT", {"ALL", "SPECIES", "ELEMENTS"});
+      // one species of two elements: the domain covers all three element pairs or none of them
+      int covered = 0;
+      if (sel == "ALL") {
+        covered = 3;
+      } else if (sel == "SPECIES") {
+        for (const auto &pr : dom.str_pairs("SPECIES")) {
+          if (pr.first != cell || pr.second != cell)
+            key_error(dom.path + ".SPECIES", "unknown cell type in " + pr.first + ", " + pr.second);
+          covered = 3;
+        }
+      } else {
+        bool pairs[2][2] = {{false, false}, {false, false}};
+        for (const auto &pr : dom.elem_pairs("ELEMENTS")) {
+          int e[2];
+          for (int k = 0; k < 2; ++k) {
+            const auto &ce = k == 0 ? pr.first : pr.second;
+            if (ce.first != cell) key_error(dom.path + ".ELEMENTS", "Unknown cell type " + ce.first);
+            if (ce.second == enames[0]) {
+              e[k] = 0;
+            } else if (ce.second == enames[1]) {
+              e[k] = 1;
+            } else {
+              key_error(dom.path + ".ELEMENTS", "Unknown element name " + ce.second + " for cell type " + ce.first);
+            }
+          }
+          pairs[e[0]][e[1]] = pairs[e[1]][e[0]] = true;
+        }
+        covered = (pairs[0][0] ? 1 : 0) + (pairs[0][1] ? 1 : 0) + (pairs[1][1] ? 1 : 0);
+      }
+      if (covered == 3) {
+        p.rcut_scale = rcut;
+      } else if (covered != 0) {
+        key_error(dom.path + ".ELEMENTS", "the GPU step uses one cutoff per species (the attraction must cover "
+                                          "all element pairs of the cell or none)");
+      }
+    }
+  } else if (pair == "SC") {
+    // the cubic well of SCParams (MD.cuh:134-232) with the element values of Input.cpp:48-62
+    // (xi = SIGMA_RATIO * SIGMA_CORE, Em = EPSILON_RATIO * EPSILON_CORE) and rc2 = 1
+    // (Input.cpp:354-357); MD.cu:57-75 averages the per-element values into per-pair ones,
+    // which the GPU step holds as one value per colony, so the two elements must agree.
+    Node sc = pf.child("SC");
+    const auto e0 = sc.nums("EPSILON_CORE", 2);
+    const auto sr = sc.nums("SIGMA_RATIO", 2);
+    const auto er = sc.nums("EPSILON_RATIO", 2);
+    for (int j = 0; j < 2; ++j)
+      if (!(sr[j] <= 1.0)) key_error(sc.path + ".SIGMA_RATIO", "Sigma Ratio > 1 !!!");
+    const double xi0 = sr[0] * in->sigma[0], xi1 = sr[1] * in->sigma[1];
+    if (e0[0] != e0[1]) key_error(sc.path + ".EPSILON_CORE", "the GPU step uses one core energy per species");
+    if (xi0 != xi1)
+      key_error(sc.path + ".SIGMA_RATIO", "the GPU step uses one well width per species (SIGMA_RATIO x SIGMA_CORE "
+                                          "equal for both elements)");
+    if (er[0] * e0[0] != er[1] * e0[1])
+      key_error(sc.path + ".EPSILON_RATIO", "the GPU step uses one well depth per species");
+    cfg.force_law = CIL_FORCE_SC;
+    p.epsilon = e0[0];
+    p.well_epsilon = er[0] * e0[0];
+    p.well_sigma = xi0;
+    p.rcut_scale = 1.0;
+    p.force_shifted = 0;  // FORCE_SHIFTED is set only by the LJ attraction block (Input.cpp:306)
   } else {
     key_error("GPU.FORCE_LAW", "the reference's " + pair +
                                    " law differs from the GPU step's; set GPU.FORCE_LAW, EPSILON (and RCUT_SCALE)");

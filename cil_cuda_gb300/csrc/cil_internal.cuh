@@ -173,6 +173,10 @@ struct ColonyConst {
   float inv_bwf[3];  // 1 / bin width
   float zeta_f[2], temp_f[2], mu_f[2], motility_f[2];
   float kappa_f, rest0_f, rest1_f, amp_f, eps_f, rcs_f, wall_E_f;
+  // CIL_FORCE_SC: well depth and width, shifted force (FP64 and FP32 copies)
+  double well_eps, well_sigma;
+  float well_eps_f, well_sigma_f;
+  int force_shifted;
   float wall_pos_f[2];
 };
 
@@ -397,18 +401,46 @@ __device__ __forceinline__ double uniform53(uint32_t a, uint32_t b) {
 // ---------------------------------------------------------------- pair force laws
 // Force modulus f0 with F_i += f0 * (r_j - r_i); returns false outside the cutoff.
 // LJ-WCA is the reference's LJParams::elemForce0 form (MD.cuh:50-56, 98-113).
+// The reference soft-core cubic well's elemForce0 (MD.cuh:144-162): y = r - sigma_ij,
+// t'(y, xi) = 6 y (xi - y) / xi^3.
+template <typename R>
+__device__ __forceinline__ R sc_force0(R r, R sij, R e0, R em, R xi) {
+  const R y = r - sij;
+  if (y <= -xi) return R(0);
+  if (y < R(0)) return -(e0 + em) * (R(6) * (-y) * (y + xi) / (xi * xi * xi)) / r;
+  if (y < xi) return em * (R(6) * y * (-y + xi) / (xi * xi * xi)) / r;
+  return R(0);
+}
+
+// The bare Lennard-Jones modulus (s^6 - 2 s^12) / r^2 with s^2 = sij2 / r2 (MD.cuh:50-56).
+template <typename R>
+__device__ __forceinline__ R lj_force0(R sij2, R r2) {
+  const R ir2 = R(1) / r2;
+  R sr2n = sij2 * ir2;
+  const R srn = sr2n * sr2n * sr2n;
+  sr2n = srn * srn;
+  return (srn - R(2) * sr2n) * ir2;
+}
+
 template <int LAW, typename R>
-__device__ __forceinline__ bool pair_force(R r2, R si, R sj, R eps, R rcs, R &f0) {
+__device__ __forceinline__ bool pair_force(R r2, R si, R sj, R eps, R rcs, R &f0, R em = R(0), R xi = R(0),
+                                           int shifted = 0) {
   const R sij = R(0.5) * (si + sj);
+  if (LAW == CIL_FORCE_SC) {
+    // SCParams::elemForce (MD.cuh:199-214): rcut2 (sigma_ij -+ xi)^2 bound the force
+    const R rc2 = rcs * rcs * ((sij + xi) * (sij + xi));
+    if (r2 > rcs * rcs * ((sij - xi) * (sij - xi)) && r2 <= rc2) {
+      f0 = sc_force0(sqrt(r2), sij, eps, em, xi) - (shifted ? sc_force0(sqrt(rc2), sij, eps, em, xi) * sqrt(rc2 / r2) : R(0));
+      return true;
+    }
+    return false;
+  }
   if (LAW == CIL_FORCE_LJ_WCA) {
+    // LJParams::elemForce (MD.cuh:72-92): (f(r2) - [shifted] f(rc2) sqrt(rc2 / r2)) 24 eps
     const R sij2 = sij * sij;
     const R rc2 = sij2 * (rcs * rcs);
     if (r2 <= rc2) {
-      const R ir2 = R(1) / r2;
-      R sr2n = sij2 * ir2;
-      const R srn = sr2n * sr2n * sr2n;
-      sr2n = srn * srn;
-      f0 = (srn - R(2) * sr2n) * ir2 * (R(24) * eps);
+      f0 = (lj_force0(sij2, r2) - (shifted ? lj_force0(sij2, rc2) * sqrt(rc2 / r2) : R(0))) * (R(24) * eps);
       return true;
     }
     return false;
@@ -432,16 +464,32 @@ __device__ __forceinline__ bool pair_force(R r2, R si, R sj, R eps, R rcs, R &f0
 // FP32 pair force, branch-free: the law is evaluated for every candidate and masked
 // (fast reciprocal / reciprocal square root; the mixed form's tolerance is FP32-level)
 template <int LAW>
-__device__ __forceinline__ float pair_f0_fast(float r2, float si, float sj, float eps, float rcs, bool ok) {
+__device__ __forceinline__ float pair_f0_fast(float r2, float si, float sj, float eps, float rcs, bool ok,
+                                              float em = 0.0f, float xi = 0.0f, int shifted = 0) {
   const float sij = 0.5f * (si + sj);
   const float rc = rcs * sij;
+  if (LAW == CIL_FORCE_SC) {
+    const float rc2 = rcs * rcs * ((sij + xi) * (sij + xi));
+    const bool in = ok && r2 > rcs * rcs * ((sij - xi) * (sij - xi)) && r2 <= rc2 && r2 > 0.0f;
+    const float rinv = rsqrtf(r2);
+    float f = sc_force0(r2 * rinv, sij, eps, em, xi);
+    if (shifted) f -= sc_force0(sqrtf(rc2), sij, eps, em, xi) * sqrtf(rc2) * rinv;
+    return in ? f : 0.0f;
+  }
   if (LAW == CIL_FORCE_LJ_WCA) {
     const bool in = ok && r2 <= rc * rc;
     const float ir2 = __fdividef(1.0f, r2);  // fast reciprocal (about 2 ulp)
     const float sr2 = sij * sij * ir2;
     const float sr6 = sr2 * sr2 * sr2;
-    const float f0 = (sr6 - 2.0f * sr6 * sr6) * ir2 * (24.0f * eps);
-    return in ? f0 : 0.0f;
+    float f = sr6 - 2.0f * sr6 * sr6;
+    if (shifted) {
+      // f(rc) sqrt(rc^2 / r^2) / r^2 with (sigma / rc)^2 = 1 / rcs^2:
+      // (c6 - 2 c6^2) / (rc r^3), the r^-2 factor taken out below
+      const float c2 = __fdividef(1.0f, rcs * rcs);
+      const float c6 = c2 * c2 * c2;
+      f -= (c6 - 2.0f * c6 * c6) * sqrtf(r2) * __fdividef(1.0f, rc);
+    }
+    return in ? f * ir2 * (24.0f * eps) : 0.0f;
   } else if (LAW == CIL_FORCE_SOFTCORE) {
     // -eps (1 - r/rc)^2 / r from one reciprocal square root: q = 1 / (r rc) gives
     // r / rc = r2 q and 1 / r = rc q
@@ -458,6 +506,14 @@ __device__ __forceinline__ float pair_f0_fast(float r2, float si, float sj, floa
     const float sq = delta * rsqrtf(fmaxf(delta, 1e-30f));
     return in ? -eps * delta * sq * rinv : 0.0f;
   }
+}
+
+// The largest distance at which the law acts between elements of diameters si, sj (the Verlet
+// lists add the skin to it).
+template <int LAW>
+__device__ __forceinline__ float law_cutoff_f(const ColonyConst &C, float si, float sj) {
+  const float sij = 0.5f * (si + sj);
+  return LAW == CIL_FORCE_SC ? C.rcs_f * (sij + C.well_sigma_f) : C.rcs_f * sij;
 }
 
 // ---------------------------------------------------------------- kernel argument packs

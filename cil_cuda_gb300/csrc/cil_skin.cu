@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kTile, kListMinBlocks<D>) k_skin_lists(SkinArg
               const float dx = pk_c(pj[q], d) + (static_cast<float>(off[d]) * C.bwf[d] - ui[d]);
               r2 += dx * dx;
             }
-            const float cut = C.rcs_f * 0.5f * (si + fabsf(pj[q].w)) + skin;
+            const float cut = law_cutoff_f<LAW>(C, si, fabsf(pj[q].w)) + skin;
             if (r2 < cut * cut) {
               if (n < kListCap)
                 a.nbr[static_cast<size_t>(n) * SS + s] =
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
         dx[d] = pk_c(pj, d) + of[d];
         r2 += dx[d] * dx[d];
       }
-      const float f0 = pair_f0_fast<LAW>(r2, sf, fabsf(pj.w), eps, rcs, true);
+      const float f0 = pair_f0_fast<LAW>(r2, sf, fabsf(pj.w), eps, rcs, true, C.well_eps_f, C.well_sigma_f, C.force_shifted);
       if (f0 != 0.0f) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
           dx[d] = pk_c(pq, d) + ofs[d];
           r2 += dx[d] * dx[d];
         }
-        const float f0 = pair_f0_fast<LAW>(r2, sf, fabsf(pq.w), eps, rcs, true);
+        const float f0 = pair_f0_fast<LAW>(r2, sf, fabsf(pq.w), eps, rcs, true, C.well_eps_f, C.well_sigma_f, C.force_shifted);
 #pragma unroll
         for (int d = 0; d < D; ++d) acc[d] += f0 * dx[d];
       }
@@ -656,6 +656,9 @@ void lists_d(const SkinArgs &a, int law, int grid, cudaStream_t s) {
     case CIL_FORCE_SOFTCORE:
       k_skin_lists<D, CIL_FORCE_SOFTCORE><<<grid, kTile, 0, s>>>(a);
       break;
+    case CIL_FORCE_SC:
+      k_skin_lists<D, CIL_FORCE_SC><<<grid, kTile, 0, s>>>(a);
+      break;
     default:
       k_skin_lists<D, CIL_FORCE_HERTZ><<<grid, kTile, 0, s>>>(a);
       break;
@@ -671,6 +674,9 @@ void fresh_d(const SkinArgs &a, int law, cudaStream_t s) {
       break;
     case CIL_FORCE_SOFTCORE:
       k_fresh_pairs<D, CIL_FORCE_SOFTCORE><<<grid, kFreshBlock, 0, s>>>(a);
+      break;
+    case CIL_FORCE_SC:
+      k_fresh_pairs<D, CIL_FORCE_SC><<<grid, kFreshBlock, 0, s>>>(a);
       break;
     default:
       k_fresh_pairs<D, CIL_FORCE_HERTZ><<<grid, kFreshBlock, 0, s>>>(a);

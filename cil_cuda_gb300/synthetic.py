@@ -27,9 +27,20 @@ def base_params(dim: int, force_law: int, box, **over) -> dict:
              nwalls=0, wall_dir=[1, -1], wall_pos=[0.0, 0.0], wall_E=0.0,
              epsilon=1.0, rcut_scale=2 ** (1 / 6), zeta=[1.0, 1.0], motility=[0.0, 1.0],
              kappa=10.0, rest0=0.5, rest1=1.0, noise_D=0.01, dt=1e-4,
-             div_tau_mu=1.0, div_tau_sigma=0.1, apop_rate=0.0)
+             div_tau_mu=1.0, div_tau_sigma=0.1, apop_rate=0.0,
+             well_epsilon=0.0, well_sigma=0.0, force_shifted=0)
     p.update(over)
     return p
+
+
+def sc_params(box=60.0, **over) -> dict:
+    """The reference's soft-core cubic well (SCParams, MD.cuh:134-232) in a 2D colony: core
+    energy E0 = 10, well depth Em = 0.5, well width xi = 0.3 (its SIGMA_RATIO times a unit
+    diameter), the reference's rc2 = 1."""
+    from . import FORCE_SC
+    kw = dict(epsilon=10.0, well_epsilon=0.5, well_sigma=0.3, rcut_scale=1.0)
+    kw.update(over)
+    return base_params(2, FORCE_SC, [box, box], **kw)
 
 
 def polydisperse(rng, n, mu=1.0, sd=0.1, lo=0.7, hi=1.3):

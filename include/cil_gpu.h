@@ -37,12 +37,21 @@ typedef enum cil_status {
 } cil_status;
 
 /* Pair-force laws (the reference's PairForceParams family, MD.cuh:23-344, with the
- * benchmark workloads' forms: WCA, the (1 - r/rc)^2 soft core, E h^1.5 Hertz). Force on element
- * i from j is f0(r) * (r_j - r_i). */
+ * benchmark workloads' forms: WCA, the (1 - r/rc)^2 soft core, E h^1.5 Hertz; and the
+ * reference's own soft-core cubic well). Force on element i from j is f0(r) * (r_j - r_i). */
 enum {
-  CIL_FORCE_LJ_WCA = 0,   /* LJParams (MD.cuh:47-129): eps_ij = 24 eps, rc^2 = rcut_scale^2 sigma_ij^2 */
+  CIL_FORCE_LJ_WCA = 0,   /* LJParams (MD.cuh:47-129): eps_ij = 24 eps, rc^2 = rcut_scale^2 sigma_ij^2
+                             (rcut_scale 2^(1/6): WCA; larger: the attractive tail, the reference's
+                             ATTRACTION ON with RCUT = rcut_scale); with force_shifted, minus
+                             f0(rc) sqrt(rc^2 / r^2) (SHIFT FORCE, OPT::FORCE_SHIFTED) */
   CIL_FORCE_SOFTCORE = 1, /* F = eps (1 - r/rc)^2, rc = rcut_scale sigma_ij */
-  CIL_FORCE_HERTZ = 2     /* F = E delta^1.5, delta = sigma_ij - r */
+  CIL_FORCE_HERTZ = 2,    /* F = E delta^1.5, delta = sigma_ij - r */
+  CIL_FORCE_SC = 3        /* SCParams (MD.cuh:134-232), one species: y = r - sigma_ij, xi = well_sigma;
+                             f0 = -(E0 + Em) t'(-y, xi) / r for -xi <= y < 0, Em t'(y, xi) / r for
+                             0 <= y < xi, t'(y, xi) = 6 y (xi - y) / xi^3, E0 = epsilon,
+                             Em = well_epsilon; acting for rcut_scale^2 (sigma_ij - xi)^2 < r^2 <=
+                             rcut_scale^2 (sigma_ij + xi)^2 (the reference's rc2 is 1); with
+                             force_shifted, minus f0(rc) sqrt(rc^2 / r^2) (OPT::FORCE_SHIFTED) */
 };
 
 /* Arithmetic of the pair forces. */
@@ -83,6 +92,10 @@ typedef struct cil_colony_params {
   double div_tau_mu;      /* division time ~ N(mu, sigma) */
   double div_tau_sigma;
   double apop_rate;       /* apoptosis rate per unit time */
+  double well_epsilon;    /* CIL_FORCE_SC: well depth Em (other laws: unused) */
+  double well_sigma;      /* CIL_FORCE_SC: well width xi, absolute (other laws: unused) */
+  int32_t force_shifted;  /* CIL_FORCE_SC and CIL_FORCE_LJ_WCA: 1 = the reference's shifted force */
+  int32_t pad_sc;
 } cil_colony_params;
 
 typedef struct cil_config {

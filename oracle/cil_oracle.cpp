@@ -184,18 +184,54 @@ void box_update_pos(int D, const double *box, const int32_t *periodic, double *r
 //          rc^2 = 2^(1/3) sigma_ij^2 (Input.cpp:296-301), inclusive cutoff.
 //  soft-core: F = eps (1 - r/rc)^2, rc = rcut_scale * sigma_ij.
 //  Hertz: F = E delta^1.5, delta = sigma_ij - r.
-bool pair_force_law(int law, double eps, double rcut_scale, double r2, double si, double sj, double &f0) {
+// The reference soft-core cubic well (SCParams, MD.cuh:134-232), one species: the pair
+// coefficients of SCParams::init (MD.cu:57-77) reduce to eps_core, eps_well, xi and rcut2 for a
+// single element type. elemForce0 (MD.cuh:144-162) with t'(y, xi) = 6 y (-y + xi) / xi^3
+// (MD.cuh:135-137), in the reference's operation order.
+double sc_force0(double r2, double sig_core, double e0, double em, double xi) {
+  const double r = std::sqrt(r2);
+  const double y = r - sig_core;
+  if (y <= -xi) return 0.0;
+  if (-xi <= y && y < 0.0) {
+    const double yy = -y;
+    return -(e0 + em) * (6.0 * yy * (-yy + xi) / (xi * xi * xi)) / r;
+  }
+  if (0 <= y && y < xi) return em * (6.0 * y * (-y + xi) / (xi * xi * xi)) / r;
+  return 0.0;
+}
+
+// LJParams::elemForce0 (MD.cuh:50-56): (s^6 - 2 s^12) / r2 with s^2 = sij2 / r2
+static double lj_force0(double sij2, double r2) {
+  const double ir2 = 1.0 / r2;
+  double sr2n = sij2 * ir2;
+  const double srn = sr2n * sr2n * sr2n;
+  sr2n = srn * srn;
+  return (srn - 2.0 * sr2n) * ir2;
+}
+
+bool pair_force_law(int law, double eps, double rcut_scale, double r2, double si, double sj, double &f0,
+                    double well_eps, double well_sigma, int shifted) {
   const double sij = 0.5 * (si + sj);
   f0 = 0.0;
+  if (law == ORA_FORCE_SC) {
+    // SCParams::elemForce (MD.cuh:199-214): the force acts for rcut2 (sigCore - xi)^2 < r2 <=
+    // rcut2 (sigCore + xi)^2, minus its value at the cutoff with OPT::FORCE_SHIFTED
+    const double rcut2 = rcut_scale * rcut_scale;
+    const double rc2 = rcut2 * ((sij + well_sigma) * (sij + well_sigma));
+    if (r2 > rcut2 * ((sij - well_sigma) * (sij - well_sigma)) && r2 <= rc2) {
+      f0 = sc_force0(r2, sij, eps, well_eps, well_sigma) -
+           (shifted ? sc_force0(rc2, sij, eps, well_eps, well_sigma) * std::sqrt(rc2 / r2) : 0.0);
+      return true;
+    }
+    return false;
+  }
   if (law == ORA_FORCE_LJ_WCA) {
+    // LJParams::elemForce (MD.cuh:72-92): eps_ij = 24 eps (one species), rc2 = sij2 rcut2,
+    // minus the modulus at the cutoff times sqrt(rc2 / r2) with OPT::FORCE_SHIFTED
     const double sij2 = sij * sij;
     const double rc2 = sij2 * (rcut_scale * rcut_scale);
     if (r2 <= rc2) {
-      const double ir2 = 1.0 / r2;
-      double sr2n = sij2 * ir2;
-      const double srn = sr2n * sr2n * sr2n;
-      sr2n = srn * srn;
-      f0 = (srn - 2.0 * sr2n) * ir2 * (24.0 * eps);
+      f0 = (lj_force0(sij2, r2) - (shifted ? lj_force0(sij2, rc2) * std::sqrt(rc2 / r2) : 0.0)) * (24.0 * eps);
       return true;
     }
     return false;
@@ -254,7 +290,8 @@ struct Oracle {
   void update_pos(double *r, const double *dr) const { box_update_pos(D, p.box, p.periodic, r, dr); }
 
   bool elem_force(double r2, double si, double sj, double &f0) const {
-    return pair_force_law(p.force_law, p.epsilon, p.rcut_scale, r2, si, sj, f0);
+    return pair_force_law(p.force_law, p.epsilon, p.rcut_scale, r2, si, sj, f0, p.well_epsilon, p.well_sigma,
+                          p.force_shifted);
   }
 
   // Rest length of the intra-cell spring at step ts (linear growth over the cell cycle).
@@ -360,7 +397,8 @@ struct Oracle {
       smax = std::max(smax, std::max(sig[static_cast<size_t>(c) * 2], sig[static_cast<size_t>(c) * 2 + 1]));
       ext = std::max(ext, std::sqrt(distance(rij, P(c, 0), P(c, 1))));
     }
-    const double width = p.rcut_scale * smax + ext;
+    const double reach = p.force_law == ORA_FORCE_SC ? smax + p.well_sigma : smax;  // the well reaches xi further
+    const double width = p.rcut_scale * reach + ext;
     grid.init(D, width, p.box, p.periodic);
     calc_coms();
     grid.populate(com.data(), n, head, list);
@@ -763,7 +801,24 @@ int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const in
 
 void ora_geom_pair_force(int32_t law, double eps, double rcut_scale, int64_t n, const double *r2, const double *si,
                          const double *sj, double *f0, int32_t *inside) {
-  for (int64_t k = 0; k < n; ++k) inside[k] = pair_force_law(law, eps, rcut_scale, r2[k], si[k], sj[k], f0[k]) ? 1 : 0;
+  for (int64_t k = 0; k < n; ++k)
+    inside[k] = pair_force_law(law, eps, rcut_scale, r2[k], si[k], sj[k], f0[k], 0.0, 0.0, 0) ? 1 : 0;
+}
+
+void ora_geom_lj_force(double eps, double rcut_scale, int32_t shifted, int64_t n, const double *r2, const double *si,
+                       const double *sj, double *f0, int32_t *inside) {
+  for (int64_t k = 0; k < n; ++k)
+    inside[k] =
+        pair_force_law(ORA_FORCE_LJ_WCA, eps, rcut_scale, r2[k], si[k], sj[k], f0[k], 0.0, 0.0, shifted) ? 1 : 0;
+}
+
+void ora_geom_sc_force(double eps_core, double eps_well, double well_sigma, double rcut_scale, int32_t shifted,
+                       int64_t n, const double *r2, const double *si, const double *sj, double *f0, int32_t *inside) {
+  for (int64_t k = 0; k < n; ++k)
+    inside[k] = pair_force_law(ORA_FORCE_SC, eps_core, rcut_scale, r2[k], si[k], sj[k], f0[k], eps_well, well_sigma,
+                               shifted)
+                    ? 1
+                    : 0;
 }
 
 void ora_rng_seed(void *h, uint32_t seed) { H(h)->rng.init(seed); }

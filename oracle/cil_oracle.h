@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-enum { ORA_FORCE_LJ_WCA = 0, ORA_FORCE_SOFTCORE = 1, ORA_FORCE_HERTZ = 2 };
+enum { ORA_FORCE_LJ_WCA = 0, ORA_FORCE_SOFTCORE = 1, ORA_FORCE_HERTZ = 2, ORA_FORCE_SC = 3 };
 
 typedef struct ora_params {
   int32_t dim;            /* 2 or 3 */
@@ -49,6 +49,10 @@ typedef struct ora_params {
   double dt;
   double div_tau_mu, div_tau_sigma; /* division time ~ N(mu, sigma), time units */
   double apop_rate;                 /* per unit time */
+  double well_epsilon;              /* ORA_FORCE_SC: well depth Em */
+  double well_sigma;                /* ORA_FORCE_SC: well width xi (absolute) */
+  int32_t force_shifted;            /* ORA_FORCE_SC: OPT::FORCE_SHIFTED */
+  int32_t pad_sc;
 } ora_params;
 
 typedef struct ora_event {
@@ -115,6 +119,12 @@ int32_t ora_geom_link_list(int32_t dim, double rcut, const double *box, const in
                            int32_t *neighbor_ids, int32_t max_bins);
 void ora_geom_pair_force(int32_t law, double eps, double rcut_scale, int64_t n, const double *r2, const double *si,
                          const double *sj, double *f0, int32_t *inside);
+/* the Lennard-Jones law (ORA_FORCE_LJ_WCA) with any cutoff, shifted or not */
+void ora_geom_lj_force(double eps, double rcut_scale, int32_t shifted, int64_t n, const double *r2, const double *si,
+                       const double *sj, double *f0, int32_t *inside);
+/* the soft-core cubic well (ORA_FORCE_SC) with its well parameters */
+void ora_geom_sc_force(double eps_core, double eps_well, double well_sigma, double rcut_scale, int32_t shifted,
+                       int64_t n, const double *r2, const double *si, const double *sj, double *f0, int32_t *inside);
 
 /* RNG access for golden-vector checks */
 void ora_rng_seed(void *h, uint32_t seed);

@@ -9,6 +9,7 @@ Geometry(lib, prefix) wraps either, so the golden vectors the reference produces
 (tests/golden/make_geometry_golden.py) and the oracle's outputs go through one code path.
 The Lennard-Jones element force has one wrapper per side: lj_force_oracle (the oracle's law
 table, ora_geom_pair_force) and lj_force_reference (the reference's LJParams::elemForce,
+likewise the soft-core cubic well: sc_force_oracle and sc_force_reference (SCParams),
 MD.cuh:98-113, in oracle/_ref/libref_force.so)."""
 import ctypes as C
 import os
@@ -114,6 +115,70 @@ def lj_force_reference(eps, r2, si, sj):
     f0 = np.zeros(r2.size)
     inside = np.zeros(r2.size, np.int32)
     f(float(eps), L.ref_lj_wca_rc2(), r2.size, _dp(r2), _dp(si), _dp(sj), _dp(f0), _ip(inside))
+    return f0, inside
+
+
+def lj_attr_force_oracle(eps, rcut, shifted, r2, si, sj):
+    """The oracle's Lennard-Jones law with cutoff rcut (in sigma_ij) and the optional force shift
+    (ora_geom_lj_force)."""
+    from oracle import oracle as O
+    L = O.lib()
+    f = L.ora_geom_lj_force
+    f.restype = None
+    f.argtypes = [C.c_double, C.c_double, C.c_int32, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    f(float(eps), float(rcut), int(shifted), r2.size, _dp(r2), _dp(si), _dp(sj), _dp(f0), _ip(inside))
+    return f0, inside
+
+
+def lj_attr_force_reference(eps, rcut, shifted, r2, si, sj):
+    """The reference's LJParams::elemForce with ATTRACTION ON (rcut2 = RCUT^2, SHIFT FORCE when
+    shifted), or None when oracle/ref_build.sh has not built it here."""
+    if not os.path.exists(REF_FORCE):
+        return None
+    L = C.CDLL(REF_FORCE)
+    f = L.ref_lj_attr_force
+    f.restype = None
+    f.argtypes = [C.c_double, C.c_double, C.c_int32, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    f(float(eps), float(rcut), int(shifted), r2.size, _dp(r2), _dp(si), _dp(sj), _dp(f0), _ip(inside))
+    return f0, inside
+
+
+def sc_force_oracle(eps_core, eps_well, xi, rcut_scale, shifted, r2, si, sj):
+    """The oracle's restatement of the reference's soft-core cubic well (ora_geom_sc_force)."""
+    from oracle import oracle as O
+    L = O.lib()
+    f = L.ora_geom_sc_force
+    f.restype = None
+    f.argtypes = [C.c_double] * 4 + [C.c_int32, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    f(float(eps_core), float(eps_well), float(xi), float(rcut_scale), int(shifted), r2.size, _dp(r2), _dp(si), _dp(sj),
+      _dp(f0), _ip(inside))
+    return f0, inside
+
+
+def sc_force_reference(eps_core, eps_well, xi, rcut_scale, shifted, r2, si, sj):
+    """The reference's SCParams::elemForce (one element type, rcut2 = rcut_scale^2), or None when
+    oracle/ref_build.sh has not built it here."""
+    if not os.path.exists(REF_FORCE):
+        return None
+    L = C.CDLL(REF_FORCE)
+    f = L.ref_sc_force
+    f.restype = None
+    f.argtypes = [C.c_double] * 4 + [C.c_int32, C.c_int64] + [C.POINTER(C.c_double)] * 4 + [C.POINTER(C.c_int32)]
+    r2, si, sj = (np.ascontiguousarray(a, np.float64) for a in (r2, si, sj))
+    f0 = np.zeros(r2.size)
+    inside = np.zeros(r2.size, np.int32)
+    rcs = float(rcut_scale)
+    f(float(eps_core), float(eps_well), float(xi), rcs * rcs, int(shifted), r2.size, _dp(r2), _dp(si), _dp(sj),
+      _dp(f0), _ip(inside))
     return f0, inside
 
 

@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ = 0, 1, 2
+FORCE_LJ_WCA, FORCE_SOFTCORE, FORCE_HERTZ, FORCE_SC = 0, 1, 2, 3
 
 
 class OraParams(C.Structure):
@@ -43,6 +43,10 @@ class OraParams(C.Structure):
         ("div_tau_mu", C.c_double),
         ("div_tau_sigma", C.c_double),
         ("apop_rate", C.c_double),
+        ("well_epsilon", C.c_double),
+        ("well_sigma", C.c_double),
+        ("force_shifted", C.c_int32),
+        ("pad_sc", C.c_int32),
     ]
 
 

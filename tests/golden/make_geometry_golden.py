@@ -8,9 +8,11 @@ tree into oracle/_ref/libref_utils.so, with oracle/boost_shim standing in for th
 headers, then records its outputs on seeded inputs and edge cases: half-integer and near-half
 ratios for Nint, separations of exactly half a box and just around it, positions at 0 and just
 below L, displacements that wrap once either way, bin boundaries, grids that collapse to one
-bin, open and periodic axes in 2D and 3D. It also records the reference's LJParams::elemForce
+bin, open and periodic axes in 2D and 3D. It also records the reference's SCParams::elemForce
+(the soft-core cubic well, plain and shifted) and its LJParams::elemForce
 (MD.cuh:50-56, 98-113; compiled by the same recipe into oracle/_ref/libref_force.so) with its
-WCA cutoff, at three well depths, on polydisperse pairs and at the cutoff and one ulp around it.
+WCA cutoff, at three well depths, on polydisperse pairs and at the cutoff and one ulp around it,
+and with the attraction's cutoff (rcut2 = RCUT^2), plain and force-shifted.
 Doubles are stored as hex strings (bit-exact).
 tests/test_oracle_geometry.py checks the oracle's restatement (ora_geom_*) against this file.
 
@@ -113,6 +115,46 @@ def lj_inputs(rng):
     return r2, si, sj
 
 
+LJ_ATTR_CASES = ((1.0, 2.5, 0), (1.0, 2.5, 1), (0.6, 1.5, 1))
+
+
+def lj_attr_inputs(rng, rcut):
+    n = 400
+    si = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sj = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sij2 = (0.5 * (si + sj)) ** 2
+    r2 = sij2 * rng.uniform(0.55, 1.1 * rcut * rcut, n)
+    # exactly at the cutoff sij2 RCUT^2 and one ulp either side (the cutoff is inclusive)
+    rc2 = sij2[:40] * (rcut * rcut)
+    r2 = np.concatenate([r2, rc2, np.nextafter(rc2, 0), np.nextafter(rc2, np.inf)])
+    si = np.concatenate([si, si[:40], si[:40], si[:40]])
+    sj = np.concatenate([sj, sj[:40], sj[:40], sj[:40]])
+    return r2, si, sj
+
+
+SC_CASES = ((10.0, 0.5, 0.3, 1.0, 0), (10.0, 0.5, 0.3, 1.1, 1), (3.0, 1.2, 0.15, 1.0, 1))
+
+
+def sc_inputs(rng, xi, rcs):
+    n = 400
+    si = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sj = np.clip(rng.normal(1.0, 0.1, n), 0.5, None)
+    sij = 0.5 * (si + sj)
+    r = sij + rng.uniform(-1.5 * xi, 1.5 * xi, n)
+    r2 = r * r
+    # the branch points y = -xi, 0, xi and the two bounds of the window, with one ulp either side
+    k = 25
+    pts = [(sij[:k] - xi) ** 2, sij[:k] ** 2, (sij[:k] + xi) ** 2, (rcs * (sij[:k] - xi)) ** 2,
+           (rcs * rcs) * ((sij[:k] + xi) * (sij[:k] + xi))]
+    extra = []
+    for q in pts:
+        extra += [q, np.nextafter(q, 0), np.nextafter(q, np.inf)]
+    r2 = np.concatenate([r2] + extra)
+    si = np.concatenate([si] + [si[:k]] * len(extra))
+    sj = np.concatenate([sj] + [sj[:k]] * len(extra))
+    return r2, si, sj
+
+
 def main():
     subprocess.run(["bash", os.path.join(ROOT, "oracle", "ref_build.sh")], check=True)
     from oracle import geometry as G
@@ -144,6 +186,19 @@ def main():
         f0, inside = G.lj_force_reference(eps, r2, si, sj)
         out["lj_force"].append(dict(eps=float(eps).hex(), r2=hexs(r2), si=hexs(si), sj=hexs(sj), f0=hexs(f0),
                                     inside=inside.tolist()))
+    out["lj_attr_force"] = []
+    for eps, rcut, shifted in LJ_ATTR_CASES:
+        r2, si, sj = lj_attr_inputs(rng, rcut)
+        f0, inside = G.lj_attr_force_reference(eps, rcut, shifted, r2, si, sj)
+        out["lj_attr_force"].append(dict(eps=float(eps).hex(), rcut=float(rcut).hex(), shifted=shifted, r2=hexs(r2),
+                                         si=hexs(si), sj=hexs(sj), f0=hexs(f0), inside=inside.tolist()))
+    out["sc_force"] = []
+    for e0, em, xi, rcs, shifted in SC_CASES:
+        r2, si, sj = sc_inputs(rng, xi, rcs)
+        f0, inside = G.sc_force_reference(e0, em, xi, rcs, shifted, r2, si, sj)
+        out["sc_force"].append(dict(eps_core=float(e0).hex(), eps_well=float(em).hex(), xi=float(xi).hex(),
+                                    rcut_scale=float(rcs).hex(), shifted=shifted, r2=hexs(r2), si=hexs(si),
+                                    sj=hexs(sj), f0=hexs(f0), inside=inside.tolist()))
     path = os.path.join(HERE, "geometry_golden.json")
     with open(path, "w") as f:
         json.dump(out, f, separators=(",", ":"))

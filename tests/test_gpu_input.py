@@ -16,9 +16,21 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIXTURE = os.path.join(ROOT, "tests", "golden", "input_two_element_2d.json")
 
 
-def test_run_from_json_matches_oracle(gpu_lib, oracle_lib):
+def sc_document():
+    """The fixture with INTERACTIONS SELECT SC read as the reference's cubic well (no
+    GPU.FORCE_LAW): xi = 0.3, Em = 0.5, E0 = 5; dt = 1e-4 for the stiff well."""
+    d = json.load(open(FIXTURE))
+    del d["GPU"]["FORCE_LAW"]
+    d["SPECIES"]["A"]["PAIRFORCES"]["SC"].update(SIGMA_RATIO=[0.3, 0.3 / 0.9], EPSILON_RATIO=[0.1, 0.1])
+    d["MD"]["DT"]["MANUAL"] = 1e-4
+    return json.dumps(d)
+
+
+@pytest.mark.parametrize("law", ["softcore", "sc"])
+def test_run_from_json_matches_oracle(gpu_lib, oracle_lib, law):
     G = gpu_lib
-    r = G.RunInput(FIXTURE)
+    r = G.RunInput(FIXTURE) if law == "softcore" else G.RunInput(sc_document(), is_path=False)
+    assert r.params["force_law"] == (G.FORCE_SOFTCORE if law == "softcore" else G.FORCE_SC)
     st = r.initial_state()
     eng = r.engine()
     eng.upload(0, **st)
@@ -30,7 +42,7 @@ def test_run_from_json_matches_oracle(gpu_lib, oracle_lib):
     o.set_state(**st)
     assert o.step(steps) == 0
     s = o.state()
-    assert g["ncells"] == len(s["sigma"]) and g["ncells"] != r.run["ncells"]
+    assert g["ncells"] == len(s["sigma"]) and (law == "sc" or g["ncells"] != r.run["ncells"])
     np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
     d = g["pos"] - s["pos"]
     d -= np.round(d / 60.0) * 60.0

@@ -51,6 +51,14 @@ def growth(gpu_lib):
 
 
 @pytest.fixture(scope="module")
+def sc(gpu_lib):
+    """The soft-core cubic well: a dense disk, so pairs sit in the core and in the well."""
+    p = S.sc_params(box=90.0)
+    st = S.disk_colony(1500, p, seed=13)
+    return p, st
+
+
+@pytest.fixture(scope="module")
 def channel(gpu_lib):
     p = S.channel_params(lxy=40.0, height=10.0)
     st = S.channel_colony(1500, p, seed=5)
@@ -111,11 +119,21 @@ def forces_pair(G, O, p, st, seed=42, **kw):
     return fg, fo
 
 
-@pytest.mark.parametrize("case", ["lj", "growth", "channel", "lj_cellnoise"])
-def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, case):
-    p, st = {"lj": lj, "growth": growth, "channel": channel, "lj_cellnoise": lj}[case]
+def lj_attraction(lj, shifted=1):
+    """The LJ law with the reference's ATTRACTION ON: cutoff 2.5 sigma_ij, SHIFT FORCE."""
+    p, st = lj
+    return dict(p, rcut_scale=2.5, force_shifted=shifted), st
+
+
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "lj_cellnoise", "sc", "sc_shifted", "lj_attr",
+                                  "lj_attr_plain"])
+def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, sc, case):
+    p, st = {"lj": lj, "growth": growth, "channel": channel, "lj_cellnoise": lj,
+             "sc": sc, "sc_shifted": sc, "lj_attr": lj_attraction(lj), "lj_attr_plain": lj_attraction(lj, 0)}[case]
     if case == "lj_cellnoise":
         p = dict(p, noise_per_cell=1)
+    if case == "sc_shifted":
+        p = dict(p, force_shifted=1)
     fg, fo = forces_pair(gpu_lib, oracle_lib, p, st)
     assert np.isfinite(fo).all()
     scale = np.abs(fo).max()
@@ -123,8 +141,8 @@ def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, case):
     assert err <= FORCE_TOL * scale, (err, scale)
 
 
-def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth):
-    for p, st in (lj, growth):
+def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth, sc):
+    for p, st in (lj, growth, sc, (dict(sc[0], force_shifted=1), sc[1]), lj_attraction(lj), lj_attraction(lj, 0)):
         p = dict(p, noise_D=0.0)
         fg, fo = forces_pair(gpu_lib, oracle_lib, p, st, precision=gpu_lib.PREC_MIXED)
         err = np.abs(fg - fo).max() / np.abs(fo).max()
@@ -164,9 +182,41 @@ def test_trajectory_100_steps_3d_channel(gpu_lib, oracle_lib, channel):
     assert err <= TRAJ_TOL, err
 
 
-@pytest.mark.parametrize("case", ["lj", "growth", "channel"])
-def test_mixed_precision_trajectory(gpu_lib, oracle_lib, lj, growth, channel, case):
-    p, st = {"lj": lj, "growth": growth, "channel": channel}[case]
+def test_trajectory_100_steps_soft_core_well(gpu_lib, oracle_lib, sc):
+    p, st = sc
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100, cap=2 * len(st["sigma"]))
+    assert rc == 0
+    assert g["ncells"] == len(s["sigma"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
+def test_trajectory_100_steps_lj_attraction(gpu_lib, oracle_lib, lj):
+    p, st = lj_attraction(lj)
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100)
+    assert rc == 0
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
+def test_soft_core_well_events_fp64(gpu_lib, oracle_lib):
+    """The cubic well with division and apoptosis over 300 steps: events exact, FP64 positions."""
+    p = S.sc_params(box=80.0, dt=1e-4, divide=1, div_tau_mu=0.05, div_tau_sigma=0.005, apop_rate=2.0)
+    st = S.disk_colony(1200, p, seed=9)
+    g, s, rc, o = run_pair(gpu_lib, oracle_lib, p, st, 300, seed=11, cap=4 * len(st["sigma"]))
+    assert rc == 0
+    ev = o.events()
+    assert (ev[:, 1] == 0).sum() > 100 and (ev[:, 1] == 1).sum() > 5
+    assert g["ncells"] == len(s["sigma"])
+    np.testing.assert_array_equal(g["t0"], s["t0"])
+    np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr"])
+def test_mixed_precision_trajectory(gpu_lib, oracle_lib, lj, growth, channel, sc, case):
+    p, st = {"lj": lj, "growth": growth, "channel": channel, "sc": sc, "lj_attr": lj_attraction(lj)}[case]
     g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100, cap=2 * len(st["sigma"]),
                            precision=gpu_lib.PREC_MIXED)
     assert rc == 0

@@ -10,6 +10,7 @@ from cil_cuda_gb300 import synthetic as S
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
+SC_TOL = 1e-4
 STEPS = 300
 
 
@@ -29,7 +30,16 @@ def cases():
     g_st = S.disk_colony(1200, g_p, seed=3)
     c_p = S.channel_params(lxy=40.0, height=10.0)
     c_st = S.channel_colony(1500, c_p, seed=5)
-    return {"lj": (lj_p, lj_st), "growth": (g_p, g_st), "channel": (c_p, c_st)}
+    # the cubic well is stiff (about 6 (E0 + Em) / xi^2 = 700 at contact): at dt = 1e-3 a 1e-7
+    # displacement grows to 0.6 in 300 steps of the oracle alone, at dt = 1e-4 it still grows
+    # 200-900x once cells divide or die (50x for the growth colony), so this case is held to
+    # SC_TOL; its FP64 form matches the oracle to 1e-9 (test_gpu_parity.py)
+    s_p = S.sc_params(box=80.0, dt=1e-4, divide=1, div_tau_mu=0.05, div_tau_sigma=0.005, apop_rate=2.0)
+    s_st = S.disk_colony(1200, s_p, seed=9)
+    # the reference's LJ attraction: cutoff 2.5 sigma_ij, SHIFT FORCE (lists of about 25 entries)
+    a_p = dict(lj_p, rcut_scale=2.5, force_shifted=1)
+    return {"lj": (lj_p, lj_st), "growth": (g_p, g_st), "channel": (c_p, c_st), "sc": (s_p, s_st),
+            "lj_attr": (a_p, lj_st)}
 
 
 @pytest.fixture(scope="module")
@@ -37,7 +47,7 @@ def states(gpu_lib):
     return cases()
 
 
-@pytest.mark.parametrize("case", ["lj", "growth", "channel"])
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr"])
 def test_skin_trajectory_matches_oracle(gpu_lib, oracle_lib, states, case):
     p, st = states[case]
     n = len(st["sigma"])
@@ -55,7 +65,7 @@ def test_skin_trajectory_matches_oracle(gpu_lib, oracle_lib, states, case):
     assert g["ncells"] == len(s["sigma"])
     np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
     err = np.abs(minimage(g["pos"], s["pos"], p)).max()
-    assert err <= TOL, err
+    assert err <= (SC_TOL if case == "sc" else TOL), err
     # the lists were reused: fewer rebuilds than steps, and never truncated
     assert info["list_overflow"] == 0
     assert 1 <= info["nrebuild"] < STEPS, info

@@ -130,7 +130,8 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
     (lambda d: d["SPECIES"]["A"].update(NELEM=1), "SPECIES.A.NAMES : vector should be of size 1"),
     (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
     (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
-    (lambda d: d["GPU"].pop("FORCE_LAW"), "GPU.FORCE_LAW"),
+    (lambda d: (d["GPU"].pop("FORCE_LAW"), d["INTERACTIONS"]["PAIRFORCES"].update(SELECT="HZ"),
+                d["SPECIES"]["A"]["PAIRFORCES"].update(HZ={"SIGMA_CORE": [1.0, 0.9]})), "GPU.FORCE_LAW"),
     (lambda d: d["INIT"]["A"].update(SELECT="H5"), "INIT.A.H5 : key not found"),
     (lambda d: d["INIT"]["A"].update(SELECT="H5", H5={"SELECT": "LOCATION", "LOCATION": ["/nonexistent.h5", "R"]}),
      "/nonexistent.h5: cannot open"),
@@ -151,10 +152,83 @@ def test_lj_is_the_reference_law(G):
     r = load(G, d)
     assert r.params["force_law"] == G.FORCE_LJ_WCA and r.params["epsilon"] == 1.0
     assert abs(r.params["rcut_scale"] - 2 ** (1 / 6)) < 1e-15
-    d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["SELECT"] = "ON"
+    assert r.params["force_shifted"] == 0
+
+
+def lj_attraction_doc(shift="FORCE", domain=None, rcut=2.5):
+    d = copy.deepcopy(doc())
+    del d["GPU"]["FORCE_LAW"]
+    on = {"RCUT": rcut, "SHIFT": shift, "DOMAIN": domain or {"SELECT": "ALL"}}
+    d["INTERACTIONS"]["PAIRFORCES"] = {"SELECT": "LJ", "LJ": {"ATTRACTION": {"SELECT": "ON", "ON": on}}}
+    return d
+
+
+@pytest.mark.parametrize("shift,domain,rcs", [
+    ("FORCE", None, 2.5),
+    ("POTENTIAL", None, 2.5),
+    ("FORCE", {"SELECT": "SPECIES", "SPECIES": [["A", "A"]]}, 2.5),
+    ("FORCE", {"SELECT": "SPECIES", "SPECIES": []}, 2 ** (1 / 6)),
+    ("POTENTIAL", {"SELECT": "ELEMENTS", "ELEMENTS": [[["A", "BACK"], ["A", "BACK"]], [["A", "FRONT"], ["A", "BACK"]],
+                                                       [["A", "FRONT"], ["A", "FRONT"]]]}, 2.5),
+])
+def test_lj_attraction_is_read(G, shift, domain, rcs):
+    """ATTRACTION ON (readInteractionsLJ, Input.cpp:294-352): rc2 = RCUT^2 over the pairs of its
+    DOMAIN, SHIFT FORCE -> the force-shifted law (OPT::FORCE_SHIFTED, which also applies to
+    pairs left at the WCA cutoff)."""
+    r = load(G, lj_attraction_doc(shift, domain))
+    p = r.params
+    assert p["force_law"] == G.FORCE_LJ_WCA and p["epsilon"] == 1.0
+    assert abs(p["rcut_scale"] - rcs) < 1e-15
+    assert p["force_shifted"] == (1 if shift == "FORCE" else 0)
+
+
+@pytest.mark.parametrize("edit,needle", [
+    (lambda d: d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["ON"].update(RCUT=1.0), "Invalid LJ cutoff"),
+    (lambda d: d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["ON"].update(
+        DOMAIN={"SELECT": "ELEMENTS", "ELEMENTS": [[["A", "BACK"], ["A", "FRONT"]]]}), "one cutoff per species"),
+    (lambda d: d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["ON"].update(
+        DOMAIN={"SELECT": "ELEMENTS", "ELEMENTS": [[["A", "MID"], ["A", "FRONT"]]]}), "Unknown element name MID"),
+    (lambda d: d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["ON"].update(
+        DOMAIN={"SELECT": "SPECIES", "SPECIES": [["A"]]}), "Wrong cell pair specification"),
+    (lambda d: d["INTERACTIONS"]["PAIRFORCES"]["LJ"]["ATTRACTION"]["ON"].update(SHIFT="NONE"), "not one of"),
+])
+def test_lj_attraction_refusals(G, edit, needle):
+    d = lj_attraction_doc()
+    edit(d)
     with pytest.raises(G.CilError) as e:
         load(G, d)
-    assert "ATTRACTION" in str(e.value)
+    assert needle in str(e.value)
+
+
+def sc_doc():
+    d = copy.deepcopy(doc())
+    del d["GPU"]["FORCE_LAW"]
+    d["SPECIES"]["A"]["PAIRFORCES"]["SC"].update(SIGMA_RATIO=[0.3, 0.3 / 0.9], EPSILON_RATIO=[0.1, 0.1])
+    return d
+
+
+def test_sc_is_the_reference_law(G):
+    """SELECT SC without GPU.FORCE_LAW runs the reference's cubic well: xi = SIGMA_RATIO x
+    SIGMA_CORE and Em = EPSILON_RATIO x EPSILON_CORE (Input.cpp:48-62), rc2 = 1."""
+    r = load(G, sc_doc())
+    p = r.params
+    assert p["force_law"] == r.config["force_law"] == G.FORCE_SC
+    assert (p["epsilon"], p["rcut_scale"], p["force_shifted"]) == (5.0, 1.0, 0)
+    assert p["well_epsilon"] == 0.1 * 5.0 and p["well_sigma"] == 0.3
+
+
+@pytest.mark.parametrize("key,value,needle", [
+    ("SIGMA_RATIO", [0.3, 0.3], "one well width per species"),
+    ("SIGMA_RATIO", [1.2, 1.2], "Sigma Ratio > 1"),
+    ("EPSILON_CORE", [5, 6], "one core energy per species"),
+    ("EPSILON_RATIO", [0.1, 0.2], "one well depth per species"),
+])
+def test_sc_refusals(G, key, value, needle):
+    d = sc_doc()
+    d["SPECIES"]["A"]["PAIRFORCES"]["SC"][key] = value
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert needle in str(e.value) and "SPECIES.A.PAIRFORCES.SC." + key in str(e.value)
 
 
 def test_parse_errors(G):

@@ -82,6 +82,39 @@ def test_lj_force_matches_reference(golden):
         assert 0 < np.sum(inside) < len(inside)
 
 
+def test_lj_attraction_matches_reference(golden):
+    """The LJ law with ATTRACTION ON (LJParams::elemForce, MD.cuh:72-92, rcut2 = RCUT^2 as
+    Input.cpp:303-315 sets it), plain and with SHIFT FORCE, at the cutoff and one ulp around it,
+    bit for bit."""
+    from oracle import geometry as G
+    assert len(golden["lj_attr_force"]) == 3
+    for c in golden["lj_attr_force"]:
+        f0, inside = G.lj_attr_force_oracle(float.fromhex(c["eps"]), float.fromhex(c["rcut"]), c["shifted"],
+                                            unhex(c["r2"]), unhex(c["si"]), unhex(c["sj"]))
+        np.testing.assert_array_equal(inside, c["inside"])
+        np.testing.assert_array_equal(bits(f0), bits(unhex(c["f0"])))
+        assert 0 < np.sum(inside) < len(inside)
+        f = unhex(c["f0"])
+        assert (f > 0).any() and (f < 0).any()  # the attractive tail and the repulsive core
+
+
+def test_sc_force_matches_reference(golden):
+    """The soft-core cubic well (SCParams::elemForce, MD.cuh:134-232): the reference's values at
+    its branch points (y = -xi, 0, xi), at both bounds of its window with one ulp either side,
+    with and without OPT::FORCE_SHIFTED, bit for bit."""
+    from oracle import geometry as G
+    assert len(golden["sc_force"]) == 3
+    for c in golden["sc_force"]:
+        f0, inside = G.sc_force_oracle(float.fromhex(c["eps_core"]), float.fromhex(c["eps_well"]),
+                                       float.fromhex(c["xi"]), float.fromhex(c["rcut_scale"]), c["shifted"],
+                                       unhex(c["r2"]), unhex(c["si"]), unhex(c["sj"]))
+        np.testing.assert_array_equal(inside, c["inside"])
+        np.testing.assert_array_equal(bits(f0), bits(unhex(c["f0"])))
+        assert 0 < np.sum(inside) < len(inside)
+        f = unhex(c["f0"])
+        assert (f > 0).any() and (f < 0).any()  # both the attractive well and the repulsive core
+
+
 def test_live_against_reference_build(ora):
     from oracle import geometry as G
     ref = G.reference_geometry()
@@ -107,3 +140,13 @@ def test_live_against_reference_build(ora):
     b = G.lj_force_reference(1.0, r2, si, sj)
     assert b is not None
     assert (bits(a[0]) == bits(b[0])).all() and (a[1] == b[1]).all()
+    r2a = (0.5 * (si + sj)) ** 2 * rng.uniform(0.5, 7.0, 5000)
+    for shifted, rcut in ((0, 2.5), (1, 2.5), (1, 1.3)):
+        a = G.lj_attr_force_oracle(1.3, rcut, shifted, r2a, si, sj)
+        b = G.lj_attr_force_reference(1.3, rcut, shifted, r2a, si, sj)
+        assert (bits(a[0]) == bits(b[0])).all() and (a[1] == b[1]).all()
+    r2 = (0.5 * (si + sj) + rng.uniform(-0.5, 0.5, 5000)) ** 2
+    for shifted, rcs in ((0, 1.0), (1, 1.07)):
+        a = G.sc_force_oracle(7.0, 0.8, 0.35, rcs, shifted, r2, si, sj)
+        b = G.sc_force_reference(7.0, 0.8, 0.35, rcs, shifted, r2, si, sj)
+        assert (bits(a[0]) == bits(b[0])).all() and (a[1] == b[1]).all()
