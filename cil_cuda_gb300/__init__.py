@@ -22,6 +22,7 @@ FLAG_NO_GRAPH = 1
 FLAG_DEFERRED_STATUS = 2
 FLAG_REBUILD_NODE = 4
 INTEGRATOR_EULER, INTEGRATOR_HEUN = 0, 1
+INTRA_SPRING, INTRA_FENE = 0, 1
 
 STATUS = {0: "CIL_OK", 1: "CIL_ERR_CONFIG", 2: "CIL_ERR_CUDA", 3: "CIL_ERR_CAPACITY", 4: "CIL_ERR_NAN",
           5: "CIL_ERR_OUT_OF_BOX", 6: "CIL_ERR_TIMEOUT", 7: "CIL_ERR_STATE", 8: "CIL_ERR_IO"}
@@ -76,7 +77,12 @@ class ColonyParams(C.Structure):
         ("well_epsilon", C.c_double),
         ("well_sigma", C.c_double),
         ("force_shifted", C.c_int32),
-        ("pad_sc", C.c_int32),
+        ("intra_law", C.c_int32),
+        ("cil", C.c_int32),
+        ("fene_kappa", C.c_double),
+        ("fene_kappa_push", C.c_double),
+        ("fene_spring_ratio", C.c_double),
+        ("fene_rmax", C.c_double),
     ]
 
 

@@ -212,6 +212,15 @@ void grid_geometry(const cil_colony_params &p, double width, int *ns, bool *sing
   *single = overkill;
 }
 
+// Steady-state length of the reference's bond (Input.cpp:139-144): sqrt(r2max (1 - alpha / beta
+// kappa)) with alpha = 1/zeta0 + 1/zeta1, beta = m0/zeta0 + m1/zeta1, r2max = RMAX^2.
+double fene_rss(const cil_colony_params &p) {
+  const double zi0 = 1.0 / p.zeta[0], zi1 = 1.0 / p.zeta[1];
+  const double alpha = zi0 + zi1;
+  const double beta = p.motility[0] * zi0 + p.motility[1] * zi1;
+  return std::sqrt(p.fene_rmax * p.fene_rmax * (1.0 - alpha / beta * p.fene_kappa));
+}
+
 double bin_width_for(const cil_handle *h, const HostColony &c) {
   // a colony without cells stays without (nothing divides): one bin
   if (!(c.sigma_max > 0.0)) return std::max(c.p.box[0], std::max(c.p.box[1], c.p.box[2]));
@@ -1027,7 +1036,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     if (p.dim != cfg->dim || p.force_law != cfg->force_law || cap_cells[c] <= 0 || !(p.dt > 0.0) ||
         !(p.zeta[0] > 0.0) || !(p.zeta[1] > 0.0) || p.nwalls < 0 || p.nwalls > 2 ||
         !(p.rcut_scale > 0.0) ||
-        (p.force_law == CIL_FORCE_SC && (!(p.well_sigma > 0.0) || !(p.well_epsilon >= 0.0)))) {
+        (p.force_law == CIL_FORCE_SC && (!(p.well_sigma > 0.0) || !(p.well_epsilon >= 0.0))) ||
+        (p.intra_law != CIL_INTRA_SPRING && p.intra_law != CIL_INTRA_FENE) ||
+        (p.intra_law == CIL_INTRA_FENE &&
+         (p.divide || !(p.fene_rmax > 0.0) || !(p.fene_spring_ratio >= 0.0 && p.fene_spring_ratio < 1.0) ||
+          !(p.fene_kappa >= 0.0) || !(p.fene_kappa_push >= 0.0) || (!p.cil && !(fene_rss(p) > 0.0))))) {
       delete h;
       return CIL_ERR_CONFIG;
     }
@@ -1078,6 +1091,18 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.kappa = p.kappa;
     C.rest0 = p.rest0;
     C.rest1 = p.rest1;
+    C.intra_fene = p.intra_law == CIL_INTRA_FENE ? 1 : 0;
+    C.cil = p.cil ? 1 : 0;
+    C.fene_kappa = p.fene_kappa;
+    C.fene_kappa_push = p.fene_kappa_push;
+    C.fene_ratio = p.fene_spring_ratio;
+    C.fene_r2max = p.fene_rmax * p.fene_rmax;
+    C.fene_rss = C.intra_fene ? fene_rss(p) : 0.0;
+    C.fene_kappa_f = static_cast<float>(C.fene_kappa);
+    C.fene_kappa_push_f = static_cast<float>(C.fene_kappa_push);
+    C.fene_ratio_f = static_cast<float>(C.fene_ratio);
+    C.fene_r2max_f = static_cast<float>(C.fene_r2max);
+    C.fene_rss_f = static_cast<float>(C.fene_rss);
     C.noise_amp = p.noise_D > 0.0 ? std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt)) : 0.0;
     C.dt = p.dt;
     C.div_tau_mu = p.div_tau_mu;

@@ -98,6 +98,16 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       if (r2 == 0.0) {
 #pragma unroll
         for (int d = 0; d < D; ++d) F[d] = 0.0;
+      } else if (C.intra_fene) {
+        const double r = sqrt(r2);
+        double spring, sc;
+        fene_bond<double>(r2, r, fmax(si, a.sig[ps]), C.fene_r2max, C.fene_kappa, C.fene_kappa_push, C.fene_ratio,
+                          C.fene_rss, C.cil, spring, sc);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const double nd = C.cil ? rij[d] : rij[d] * sc;
+          F[d] = (j == 0) ? -(C.motility[0] * nd + spring * rij[d] * 2.0) : C.motility[1] * nd + spring * rij[d] * 2.0;
+        }
       } else {
         const double r = sqrt(r2);
         double rest = C.rest0;
@@ -261,7 +271,15 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
     }
 #pragma unroll
     for (int d = 0; d < D; ++d) F[d] = 0.0f;
-    if (r2 > 0.0f) {
+    if (r2 > 0.0f && C.intra_fene) {
+      const float rinv = rsqrtf(r2);
+      float spring, sc;
+      fene_bond<float>(r2, r2 * rinv, fmaxf(si, fabsf(pp.w)), C.fene_r2max_f, C.fene_kappa_f, C.fene_kappa_push_f,
+                       C.fene_ratio_f, C.fene_rss_f, C.cil, spring, sc);
+      const float coef = (j == 0) ? -(C.motility_f[0] * sc + 2.0f * spring) : C.motility_f[1] * sc + 2.0f * spring;
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
+    } else if (r2 > 0.0f) {
       const float rinv = rsqrtf(r2);
       float rest = C.rest0_f;
       if (C.divide) {
@@ -872,7 +890,19 @@ __global__ void __launch_bounds__(TILE, MINB) k_force_cells(const ForceArgs a) {
         rij[d] = v;
         r2 += v * v;
       }
-      if (r2 > 0.0f) {
+      if (r2 > 0.0f && C.intra_fene) {
+        const float rinv = rsqrtf(r2);
+        float spring, sc;
+        fene_bond<float>(r2, r2 * rinv, fmaxf(si[0], si[1]), C.fene_r2max_f, C.fene_kappa_f, C.fene_kappa_push_f,
+                         C.fene_ratio_f, C.fene_rss_f, C.cil, spring, sc);
+        const float coef0 = -(C.motility_f[0] * sc + 2.0f * spring);
+        const float coef1 = C.motility_f[1] * sc + 2.0f * spring;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          F[0][d] += coef0 * rij[d];
+          F[1][d] += coef1 * rij[d];
+        }
+      } else if (r2 > 0.0f) {
         const float rinv = rsqrtf(r2);
         float rest = C.rest0_f;
         if (C.divide) {

@@ -842,13 +842,28 @@ void read_all(cil_input *in) {
     key_error("GPU.FORCE_LAW", "the reference's " + pair +
                                    " law differs from the GPU step's; set GPU.FORCE_LAW, EPSILON (and RCUT_SCALE)");
   }
-  if (!has_gpu || !gpu.has("SPRING"))
-    key_error("GPU.SPRING", "the GPU step's intra-cell force is a linear spring (the reference's FENE law differs); "
-                            "set GPU.SPRING {KAPPA, REST0, REST1}");
-  Node spring = gpu.child("SPRING");
-  p.kappa = spring.num("KAPPA");
-  p.rest0 = spring.num("REST0");
-  p.rest1 = spring.has("REST1") ? spring.num("REST1") : p.rest0;
+  if (has_gpu && gpu.has("SPRING")) {  // the linear spring with the rest length growing over the cycle
+    Node spring = gpu.child("SPRING");
+    p.kappa = spring.num("KAPPA");
+    p.rest0 = spring.num("REST0");
+    p.rest1 = spring.has("REST1") ? spring.num("REST1") : p.rest0;
+  } else {
+    // the reference's own bond (binaryCellForce, MD.cu:525-598) from the species' FENE block
+    // (Input.cpp:115-136) and its CIL flag (Input.cpp:22), for cells that do not divide
+    if (in->divide)
+      key_error("GPU.SPRING", "dividing two-element cells run the reference's crawling/dividing state machine "
+                              "(CIL.cu:369-455), which the GPU step does not model; set GPU.SPRING {KAPPA, REST0, "
+                              "REST1} for the linear spring with growth");
+    Node fene = loc.child("FENE");
+    p.intra_law = CIL_INTRA_FENE;
+    p.cil = loc.boolean("CIL") ? 1 : 0;
+    p.fene_kappa = fene.nums("KAPPA_PULL", 1)[0];
+    p.fene_kappa_push = fene.nums("KAPPA_PUSH", 1)[0];
+    p.fene_spring_ratio = fene.nums("SPRING_RATIO", 1)[0];
+    p.fene_rmax = fene.nums("RMAX", 1)[0];
+    if (!(p.fene_spring_ratio >= 0.0 && p.fene_spring_ratio < 1.0))
+      key_error(fene.path + ".SPRING_RATIO", "the GPU step needs 0 <= SPRING_RATIO < 1");
+  }
   p.noise_per_cell = has_gpu && gpu.has("NOISE_PER_CELL") ? gpu.boolean("NOISE_PER_CELL") : 0;
   if (has_gpu && gpu.has("WALLS")) {
     Node w = gpu.child("WALLS");

@@ -178,7 +178,34 @@ struct ColonyConst {
   float well_eps_f, well_sigma_f;
   int force_shifted;
   float wall_pos_f[2];
+  // CIL_INTRA_FENE: the reference's bond of a crawling cell (FP64 and FP32 copies); rss is the
+  // steady-state length of Input.cpp:139-144
+  int intra_fene, cil;
+  double fene_kappa, fene_kappa_push, fene_ratio, fene_r2max, fene_rss;
+  float fene_kappa_f, fene_kappa_push_f, fene_ratio_f, fene_r2max_f, fene_rss_f;
 };
+
+// The reference's bond of a crawling two-element cell (binaryCellForce, MD.cu:525-598): the
+// magnitude `spring` of the bond term spring * rij * 2 (rij = r_front - r_back, strongContract
+// = 2) and the scale s of the motility direction nij = rij * s. r2max = max(RMAX^2, the larger
+// element diameter) (MD.cu:547-548); below spring_ratio * r2max the push spring
+// kappa_push |r2 - r2max ratio| (Spring, MD.cu:263-265), above it FENE(kappa, r2max (1 - ratio),
+// r2 - r2max ratio) = -kappa / (1 - q^2) (MD.cu:255-257, 553-558); s = 1 with contact inhibition,
+// rss / r without (MD.cu:568-571). The forces are F_back = -(m0 nij + spring rij 2) and
+// F_front = m1 nij + spring rij 2.
+template <typename R>
+__device__ __forceinline__ void fene_bond(R r2, R r, R smax, R r2max0, R kappa, R kpush, R ratio, R rss, int cil,
+                                          R &spring, R &s) {
+  const R r2max = r2max0 > smax ? r2max0 : smax;
+  const R lim = r2max * ratio;
+  if (r2 <= lim) {
+    spring = kpush * fabs(r2 - lim);
+  } else {
+    const R q = (r2 - lim) / (r2max * (R(1) - ratio));
+    spring = -kappa / (R(1) - q * q);
+  }
+  s = cil ? R(1) : rss / r;
+}
 
 struct ColonyCounters {
   int ncell;          // live cells

@@ -43,6 +43,24 @@ def sc_params(box=60.0, **over) -> dict:
     return base_params(2, FORCE_SC, [box, box], **kw)
 
 
+def fene_params(box=60.0, **over) -> dict:
+    """Two-element cells held by the reference's own bond (binaryCellForce, MD.cu:525-598): FENE
+    above half of RMAX^2 = 1.44, the push spring below it, no contact inhibition (motility
+    along the axis scaled by rss / r), the front element pulling; soft-core contacts (eps 5,
+    cutoff at contact), no division. rest0 is the steady-state length rss, used only to place
+    the elements."""
+    from . import FORCE_SOFTCORE, INTRA_FENE
+    kw = dict(epsilon=5.0, rcut_scale=1.0, intra_law=INTRA_FENE, cil=0, fene_kappa=0.2, fene_kappa_push=0.5,
+              fene_spring_ratio=0.5, fene_rmax=1.2, motility=[0.0, 1.0], zeta=[1.0, 1.0])
+    kw.update(over)
+    p = base_params(2, FORCE_SOFTCORE, [box, box], **kw)
+    zi = [1.0 / z for z in p["zeta"]]
+    beta = p["motility"][0] * zi[0] + p["motility"][1] * zi[1]
+    rss = math.sqrt(p["fene_rmax"] ** 2 * (1.0 - (zi[0] + zi[1]) / beta * p["fene_kappa"]))
+    p.update(rest0=rss, rest1=rss)
+    return p
+
+
 def polydisperse(rng, n, mu=1.0, sd=0.1, lo=0.7, hi=1.3):
     """Gaussian diameters, redrawn outside [lo, hi]."""
     s = rng.normal(mu, sd, size=n)

@@ -54,6 +54,12 @@ enum {
                              force_shifted, minus f0(rc) sqrt(rc^2 / r^2) (OPT::FORCE_SHIFTED) */
 };
 
+/* Intra-cell bond of the two-element cells (cil_colony_params.intra_law). */
+enum {
+  CIL_INTRA_SPRING = 0, /* linear spring kappa (r - l) with the rest length growing over the cycle */
+  CIL_INTRA_FENE = 1    /* the reference's FENE / push bond of a crawling cell (no division) */
+};
+
 /* Arithmetic of the pair forces. */
 enum {
   CIL_PREC_FP64 = 0, /* everything in FP64 */
@@ -95,7 +101,19 @@ typedef struct cil_colony_params {
   double well_epsilon;    /* CIL_FORCE_SC: well depth Em (other laws: unused) */
   double well_sigma;      /* CIL_FORCE_SC: well width xi, absolute (other laws: unused) */
   int32_t force_shifted;  /* CIL_FORCE_SC and CIL_FORCE_LJ_WCA: 1 = the reference's shifted force */
-  int32_t pad_sc;
+  int32_t intra_law;      /* CIL_INTRA_SPRING (0) or CIL_INTRA_FENE (1) */
+  /* CIL_INTRA_FENE: the reference's bond for a crawling cell (binaryCellForce, MD.cu:525-598):
+   * below spring_ratio * r2max the push spring kappa_push |r^2 - r2max spring_ratio|
+   * (MD.cu:263-265), above it the FENE law -kappa / (1 - ((r^2 - r2max ratio) /
+   * (r2max (1 - ratio)))^2) (MD.cu:255-257), acting twice along r_front - r_back, with
+   * r2max = max(fene_rmax^2, the larger element diameter) (MD.cu:547-548); motility m_j along the
+   * axis, scaled by rss / r without contact inhibition (cil = 0; rss from Input.cpp:139-144).
+   * kappa, rest0, rest1 are unused; divide must be 0. */
+  int32_t cil;            /* CIL_INTRA_FENE: the species' CIL flag */
+  double fene_kappa;      /* KAPPA_PULL */
+  double fene_kappa_push; /* KAPPA_PUSH */
+  double fene_spring_ratio; /* SPRING_RATIO, in [0, 1) */
+  double fene_rmax;       /* RMAX */
 } cil_colony_params;
 
 typedef struct cil_config {

@@ -263,6 +263,7 @@ struct Oracle {
   int cap = 0, n = 0, ts = 0;
   int nthreads = 0;
   int integrator = 0;  // 0 Euler, 1 Heun
+  double fene_r2max = 0.0, fene_rss = 0.0;  // intra_law 1: RMAX^2, steady-state length
   std::vector<double> pos, vel, frc, sig, wiener;
   std::vector<int> t0, tsw;
   Rng rng;
@@ -316,6 +317,31 @@ struct Oracle {
       return;
     }
     const double r = std::sqrt(r2);
+    if (p.intra_law == 1) {
+      // binaryCellForce (MD.cu:525-598) for a crawling cell: r2max = max(RMAX^2, the larger
+      // diameter) (MD.cu:547-548); push spring below spring_ratio r2max (MD.cu:263-265, 553-554),
+      // FENE above it (MD.cu:255-257, 553-558); motility along nij = rij, or rij rss / r
+      // without CIL (MD.cu:568-571); the bond acts twice (strongContract = 2). The reference's
+      // velocity-squared friction (MD.cu:592-596) is left out: its two-element integrator
+      // (StochasticHeun) never updates the velocities, which stay 0, and the NaN guard drops it.
+      const double smax = std::max(sig[2 * c], sig[2 * c + 1]);
+      const double r2max = fene_r2max > smax ? fene_r2max : smax;
+      const double lim = r2max * p.fene_spring_ratio;
+      double spring;
+      if (r2 <= lim) {
+        spring = p.fene_kappa_push * std::fabs(r2 - lim);
+      } else {
+        const double q = (r2 - lim) / (r2max * (1.0 - p.fene_spring_ratio));
+        spring = -p.fene_kappa / (1.0 - q * q);
+      }
+      const double scaling = p.cil ? 1.0 : fene_rss / r;
+      for (int d = 0; d < D; ++d) {
+        const double nd = p.cil ? rij[d] : rij[d] * scaling;
+        f0[d] = -(p.motility[0] * nd + spring * rij[d] * 2.0);
+        f1[d] = p.motility[1] * nd + spring * rij[d] * 2.0;
+      }
+      return;
+    }
     const double s = p.kappa * (r - rest_length(c));
     for (int d = 0; d < D; ++d) {
       const double nd = rij[d] / r;
@@ -625,6 +651,13 @@ void *ora_create(const ora_params *p, int32_t cap_cells, uint32_t seed) {
   o->disp.assign(static_cast<size_t>(cap_cells) * o->D, 0.0);
   o->vref.assign(static_cast<size_t>(cap_cells) * o->D, 0.0);
   o->rng.init(seed);  // Random::init, Random.hpp:12-14
+  if (p->intra_law == 1) {
+    // params.r2max and the steady-state length rss of Input.cpp:123-144
+    o->fene_r2max = p->fene_rmax * p->fene_rmax;
+    const double zi0 = 1.0 / p->zeta[0], zi1 = 1.0 / p->zeta[1];
+    const double alpha = zi0 + zi1, beta = p->motility[0] * zi0 + p->motility[1] * zi1;
+    o->fene_rss = std::sqrt(o->fene_r2max * (1.0 - alpha / beta * p->fene_kappa));
+  }
   return o;
 }
 

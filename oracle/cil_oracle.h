@@ -52,7 +52,9 @@ typedef struct ora_params {
   double well_epsilon;              /* ORA_FORCE_SC: well depth Em */
   double well_sigma;                /* ORA_FORCE_SC: well width xi (absolute) */
   int32_t force_shifted;            /* ORA_FORCE_SC: OPT::FORCE_SHIFTED */
-  int32_t pad_sc;
+  int32_t intra_law;                /* 0: linear spring with growth, 1: the reference's FENE / push bond */
+  int32_t cil;                      /* intra_law 1: the species' CIL flag */
+  double fene_kappa, fene_kappa_push, fene_spring_ratio, fene_rmax; /* intra_law 1 */
 } ora_params;
 
 typedef struct ora_event {

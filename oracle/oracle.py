@@ -46,7 +46,12 @@ class OraParams(C.Structure):
         ("well_epsilon", C.c_double),
         ("well_sigma", C.c_double),
         ("force_shifted", C.c_int32),
-        ("pad_sc", C.c_int32),
+        ("intra_law", C.c_int32),
+        ("cil", C.c_int32),
+        ("fene_kappa", C.c_double),
+        ("fene_kappa_push", C.c_double),
+        ("fene_spring_ratio", C.c_double),
+        ("fene_rmax", C.c_double),
     ]
 
 

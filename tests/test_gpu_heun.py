@@ -40,6 +40,24 @@ def test_heun_oracle_mode_matches_oracle(gpu_lib, oracle_lib):
     assert np.abs(g["vel"] - s["vel"]).max() <= 1e-7 * max(1.0, np.abs(s["vel"]).max())
 
 
+def test_heun_fene_bond_oracle_mode(gpu_lib, oracle_lib):
+    """The reference's two-element integrator with its own bond (binaryCellForce, FENE / push
+    spring, no division) against the oracle, oracle-mode noise, FP64."""
+    G = gpu_lib
+    p = S.fene_params(box=80.0, dt=1e-3, noise_D=0.002)
+    st = S.disk_colony(1200, p, seed=23)
+    eng = G.Engine([p], [1200], precision=G.PREC_FP64, rng=G.RNG_DSFMT, seed=19, integrator=G.INTEGRATOR_HEUN)
+    eng.upload(0, **st)
+    eng.step(150)
+    g = eng.download(0)
+    eng.close()
+    o = oracle_lib.Oracle(p, 1200, 19, integrator=1)
+    o.set_state(**st)
+    assert o.step(150) == 0
+    s = o.state()
+    assert np.abs(wrapdiff(g["pos"], s["pos"], 80.0)).max() <= 1e-9
+
+
 def test_heun_is_two_half_euler_steps(gpu_lib):
     G = gpu_lib
     p = S.growth_params(box=60.0, dt=1e-3, divide=0, apop_rate=0.0, noise_D=0.0)

@@ -59,6 +59,14 @@ def sc(gpu_lib):
 
 
 @pytest.fixture(scope="module")
+def fene(gpu_lib):
+    """Two-element cells held by the reference's FENE / push bond, soft-core contacts."""
+    p = S.fene_params(box=90.0)
+    st = S.disk_colony(2000, p, seed=4)
+    return p, st
+
+
+@pytest.fixture(scope="module")
 def channel(gpu_lib):
     p = S.channel_params(lxy=40.0, height=10.0)
     st = S.channel_colony(1500, p, seed=5)
@@ -126,10 +134,11 @@ def lj_attraction(lj, shifted=1):
 
 
 @pytest.mark.parametrize("case", ["lj", "growth", "channel", "lj_cellnoise", "sc", "sc_shifted", "lj_attr",
-                                  "lj_attr_plain"])
-def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, sc, case):
+                                  "lj_attr_plain", "fene", "fene_cil"])
+def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, sc, fene, case):
     p, st = {"lj": lj, "growth": growth, "channel": channel, "lj_cellnoise": lj,
-             "sc": sc, "sc_shifted": sc, "lj_attr": lj_attraction(lj), "lj_attr_plain": lj_attraction(lj, 0)}[case]
+             "sc": sc, "sc_shifted": sc, "lj_attr": lj_attraction(lj), "lj_attr_plain": lj_attraction(lj, 0),
+             "fene": fene, "fene_cil": (dict(fene[0], cil=1), fene[1])}[case]
     if case == "lj_cellnoise":
         p = dict(p, noise_per_cell=1)
     if case == "sc_shifted":
@@ -141,8 +150,9 @@ def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, sc, case)
     assert err <= FORCE_TOL * scale, (err, scale)
 
 
-def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth, sc):
-    for p, st in (lj, growth, sc, (dict(sc[0], force_shifted=1), sc[1]), lj_attraction(lj), lj_attraction(lj, 0)):
+def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth, sc, fene):
+    for p, st in (lj, growth, sc, (dict(sc[0], force_shifted=1), sc[1]), lj_attraction(lj), lj_attraction(lj, 0),
+                  fene, (dict(fene[0], cil=1), fene[1])):
         p = dict(p, noise_D=0.0)
         fg, fo = forces_pair(gpu_lib, oracle_lib, p, st, precision=gpu_lib.PREC_MIXED)
         err = np.abs(fg - fo).max() / np.abs(fo).max()
@@ -199,6 +209,14 @@ def test_trajectory_100_steps_lj_attraction(gpu_lib, oracle_lib, lj):
     assert err <= TRAJ_TOL, err
 
 
+def test_trajectory_100_steps_fene_bond(gpu_lib, oracle_lib, fene):
+    p, st = fene
+    g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100)
+    assert rc == 0
+    err = np.abs(minimage(g["pos"], s["pos"], p)).max()
+    assert err <= TRAJ_TOL, err
+
+
 def test_soft_core_well_events_fp64(gpu_lib, oracle_lib):
     """The cubic well with division and apoptosis over 300 steps: events exact, FP64 positions."""
     p = S.sc_params(box=80.0, dt=1e-4, divide=1, div_tau_mu=0.05, div_tau_sigma=0.005, apop_rate=2.0)
@@ -214,9 +232,9 @@ def test_soft_core_well_events_fp64(gpu_lib, oracle_lib):
     assert err <= TRAJ_TOL, err
 
 
-@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr"])
-def test_mixed_precision_trajectory(gpu_lib, oracle_lib, lj, growth, channel, sc, case):
-    p, st = {"lj": lj, "growth": growth, "channel": channel, "sc": sc, "lj_attr": lj_attraction(lj)}[case]
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr", "fene"])
+def test_mixed_precision_trajectory(gpu_lib, oracle_lib, lj, growth, channel, sc, fene, case):
+    p, st = {"lj": lj, "growth": growth, "channel": channel, "sc": sc, "lj_attr": lj_attraction(lj), "fene": fene}[case]
     g, s, rc, _ = run_pair(gpu_lib, oracle_lib, p, st, 100, cap=2 * len(st["sigma"]),
                            precision=gpu_lib.PREC_MIXED)
     assert rc == 0

@@ -38,8 +38,10 @@ def cases():
     s_st = S.disk_colony(1200, s_p, seed=9)
     # the reference's LJ attraction: cutoff 2.5 sigma_ij, SHIFT FORCE (lists of about 25 entries)
     a_p = dict(lj_p, rcut_scale=2.5, force_shifted=1)
+    f_p = S.fene_params(box=80.0, dt=1e-3, apop_rate=0.5)
+    f_st = S.disk_colony(1200, f_p, seed=8)
     return {"lj": (lj_p, lj_st), "growth": (g_p, g_st), "channel": (c_p, c_st), "sc": (s_p, s_st),
-            "lj_attr": (a_p, lj_st)}
+            "lj_attr": (a_p, lj_st), "fene": (f_p, f_st)}
 
 
 @pytest.fixture(scope="module")
@@ -47,7 +49,7 @@ def states(gpu_lib):
     return cases()
 
 
-@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr"])
+@pytest.mark.parametrize("case", ["lj", "growth", "channel", "sc", "lj_attr", "fene"])
 def test_skin_trajectory_matches_oracle(gpu_lib, oracle_lib, states, case):
     p, st = states[case]
     n = len(st["sigma"])

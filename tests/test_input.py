@@ -200,6 +200,28 @@ def test_lj_attraction_refusals(G, edit, needle):
     assert needle in str(e.value)
 
 
+def test_fene_bond_is_read_without_division(G):
+    """Without GPU.SPRING and with DIVISION off, the species' FENE block and CIL flag select the
+    reference's own bond (binaryCellForce, MD.cu:525-598; Input.cpp:22, 115-136)."""
+    d = copy.deepcopy(doc())
+    del d["GPU"]["SPRING"]
+    d["SPECIES"]["A"]["DIVISION"]["ENABLED"] = False
+    p = load(G, d).params
+    assert p["intra_law"] == G.INTRA_FENE and p["cil"] == 0
+    assert (p["fene_kappa"], p["fene_kappa_push"], p["fene_spring_ratio"], p["fene_rmax"]) == (0.2, 0.5, 0.5, 1.2)
+    d["SPECIES"]["A"]["CIL"] = True
+    assert load(G, d).params["cil"] == 1
+    d["SPECIES"]["A"]["FENE"]["SPRING_RATIO"] = [1.0]
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "SPECIES.A.FENE.SPRING_RATIO" in str(e.value)
+    d = copy.deepcopy(doc())
+    del d["GPU"]["SPRING"]
+    with pytest.raises(G.CilError) as e:  # dividing: the state machine is not modelled
+        load(G, d)
+    assert "GPU.SPRING" in str(e.value) and "state machine" in str(e.value)
+
+
 def sc_doc():
     d = copy.deepcopy(doc())
     del d["GPU"]["FORCE_LAW"]

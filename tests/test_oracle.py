@@ -101,6 +101,35 @@ def test_spring_and_motility(oracle_lib):
     assert f[0, 0, 1] == 0.0 and f[0, 1, 1] == 0.0
 
 
+@pytest.mark.parametrize("sep,cil", [(0.7, 0), (1.05, 0), (1.05, 1), (0.3, 1)])
+def test_fene_bond_known_answers(oracle_lib, sep, cil):
+    """binaryCellForce (MD.cu:525-598) for a crawling cell, worked by hand: r2max = max(RMAX^2,
+    larger diameter); push spring kappa_push |r^2 - r2max ratio| below r2max ratio, FENE
+    -kappa / (1 - q^2), q = (r^2 - r2max ratio) / (r2max (1 - ratio)), above; the bond acts twice;
+    motility along rij, scaled by rss / r without CIL."""
+    kappa, kpush, ratio, rmax = 0.2, 0.5, 0.5, 1.2
+    p = small_params(noise_D=0.0, motility=[0.25, 1.0], intra_law=1, cil=cil, fene_kappa=kappa,
+                     fene_kappa_push=kpush, fene_spring_ratio=ratio, fene_rmax=rmax)
+    o = make(oracle_lib, p)
+    pos = np.array([[[5.0, 5.0], [5.0 + sep * 0.8, 5.0 + sep * 0.6]]])
+    sig = np.array([[1.3, 0.9]])
+    o.set_state(pos, sig, np.zeros(1, np.int32), np.full(1, S.NEVER, np.int32))
+    f = o.compute_forces()
+    rij = pos[0, 1] - pos[0, 0]
+    r2 = float(rij @ rij)
+    r2max = max(rmax * rmax, 1.3)
+    if r2 <= r2max * ratio:
+        spring = kpush * abs(r2 - r2max * ratio)
+        assert spring > 0.0  # pushes the elements apart
+    else:
+        q = (r2 - r2max * ratio) / (r2max * (1.0 - ratio))
+        spring = -kappa / (1.0 - q * q)
+    rss = math.sqrt(rmax * rmax * (1.0 - 2.0 / 1.25 * kappa))  # alpha = 2, beta = 0.25 + 1
+    nij = rij if cil else rij * (rss / math.sqrt(r2))
+    np.testing.assert_allclose(f[0, 0], -(0.25 * nij + 2.0 * spring * rij), rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(f[0, 1], 1.0 * nij + 2.0 * spring * rij, rtol=1e-14, atol=1e-15)
+
+
 def test_binning_formula_known_answers(oracle_lib):
     """min((int)((r * (1/L)) * Ns), Ns-1) with Ns = (int)(L / (w + 1e-8 min L)), ids
     ls0 * Ns1 + ls1 (Utils.hpp:872-876, 990, 1020-1022)."""
