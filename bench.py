@@ -308,10 +308,11 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
     colony from pinned host memory, one cil_step per Euler step (the reference's mdStep
     call; every step's counters are read back to the host, and with CIL_FLAG_DEFERRED_STATUS
     each call returns the previous call's status, so the host queues the next step while the
-    GPU runs this one), and a GSD
-    frame every GTS steps written by the device-fed frame writer (outputFrame,
-    OutputWriter.cpp:640-644; its copy to the host and its file writes overlap the next
-    steps). The file is flushed and closed inside the timed region."""
+    GPU runs this one), a GSD frame after every GTS steps written by the device-fed frame
+    writer (outputFrame, OutputWriter.cpp:640-644; its copy to the host and its file writes
+    overlap the next steps; none in a run shorter than GTS steps), and the final state
+    downloaded into pinned host arrays. The frame file is flushed and closed inside the timed
+    region."""
     import tempfile
     n = len(st["sigma"])
     eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
@@ -322,6 +323,10 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
     types = {"pos": np.float64, "sigma": np.float64, "t0": np.int32, "tswitch": np.int32}
     st = {k: np.ascontiguousarray(v, types.get(k)) for k, v in st.items()}
     pinned = [v for k, v in st.items() if k in ("pos", "sigma", "t0", "tswitch") and v.nbytes]
+    # the result: the final state, into pinned host arrays of the run's capacity
+    res = dict(pos=np.zeros((CAP, 2, p["dim"])), sigma=np.zeros((CAP, 2)), t0=np.zeros(CAP, np.int32),
+               tswitch=np.zeros(CAP, np.int32))
+    pinned += list(res.values())
     for v in pinned:
         G.host_register(v)
     with tempfile.TemporaryDirectory() as tmp:
@@ -336,12 +341,14 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
         for k in range(steps):
             eng.step(1)
             d2h += 56  # the per-call status read of the colony counters
-            if (k + 1) % GTS == 0 or k == steps - 1:
+            if (k + 1) % GTS == 0:
                 w.write()
         w.close()
+        fin = eng.download(0, want=("pos", "sigma", "t0", "tswitch"), out=res)
         wall = time.perf_counter() - t0
         fs = w.last_stats
-    n1 = eng.observables(0)["ncells"]
+    n1 = fin["ncells"]
+    d2h += n1 * (res["pos"][0].nbytes + res["sigma"][0].nbytes + 8)
     eng.close()
     for v in pinned:
         G.host_unregister(v)

@@ -612,27 +612,41 @@ class Engine:
         start = start[: nb + 1].copy()
         return ns, start, elems[: start[-1]].copy()
 
-    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch"), strict: bool = True) -> dict:
+    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch"), strict: bool = True,
+                 out: dict = None) -> dict:
         """The colony's state. strict=False keeps the state that a failed step left (its status
-        under "status") instead of raising."""
-        cap = self.caps[colony]
+        under "status") instead of raising. out: caller-owned C-contiguous arrays to fill
+        (pos [cap][2][dim] and sigma [cap][2] float64, t0 and tswitch [cap] int32, vel optional;
+        cap = their first dimension), e.g. pinned with host_register; views of them come back."""
         D = self.dim
-        pos = np.zeros((cap, 2, D))
-        sig = np.zeros((cap, 2))
-        vel = np.zeros((cap, 2, D))
-        t0 = np.zeros(cap, np.int32)
-        tsw = np.zeros(cap, np.int32)
-        v = ColonyView(ncells=0, capacity=cap, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig), vel=_dp(vel),
-                       t0=_ip(t0), tswitch=_ip(tsw))
+        if out is None:
+            cap = self.caps[colony]
+            pos = np.zeros((cap, 2, D))
+            sig = np.zeros((cap, 2))
+            vel = np.zeros((cap, 2, D))
+            t0 = np.zeros(cap, np.int32)
+            tsw = np.zeros(cap, np.int32)
+        else:
+            pos, sig, t0, tsw, vel = out["pos"], out["sigma"], out["t0"], out["tswitch"], out.get("vel")
+            cap = len(pos)
+            for a, dt in ((pos, np.float64), (sig, np.float64), (t0, np.int32), (tsw, np.int32)) + \
+                    (((vel, np.float64),) if vel is not None else ()):
+                if a.dtype != dt or not a.flags["C_CONTIGUOUS"] or len(a) != cap:
+                    raise ValueError("download: out arrays must be C-contiguous, of one capacity and typed")
+            if pos.shape[1:] != (2, D) or sig.shape[1:] != (2,) or (vel is not None and vel.shape[1:] != (2, D)):
+                raise ValueError("download: out arrays have the wrong shape")
+        v = ColonyView(ncells=0, capacity=cap, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig),
+                       vel=_dp(vel) if vel is not None else None, t0=_ip(t0), tswitch=_ip(tsw))
         st = self.L.cil_download(self.h, colony, C.byref(v))
         if strict or st not in (3, 4, 5) or v.ncells > cap:
             self._check(st)
         n = v.ncells
-        out = dict(ncells=n, ts=v.ts, pos=pos[:n], sigma=sig[:n], vel=vel[:n], t0=t0[:n], tswitch=tsw[:n])
-        out = {k: out[k] for k in out if k in want or k in ("ncells", "ts")}
+        res = dict(ncells=n, ts=v.ts, pos=pos[:n], sigma=sig[:n], vel=vel[:n] if vel is not None else None,
+                   t0=t0[:n], tswitch=tsw[:n])
+        res = {k: res[k] for k in res if k in want or k in ("ncells", "ts")}
         if st != 0:
-            out["status"] = st
-        return out
+            res["status"] = st
+        return res
 
     def obs_reset(self, colony: int = 0):
         self._check(self.L.cil_obs_reset(self.h, colony))

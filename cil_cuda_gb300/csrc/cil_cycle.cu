@@ -548,18 +548,28 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             // symmetric in the two diameters)
             const double sa = i < j ? si : sj, sb = i < j ? sj : si;
             const double h = fmax((si + sj) / 2 - r, 0.0);
+            const double Sr = inv_ri + inv_r[j];
             // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2): one square root fewer
-            const double fel = h * sqrt(h / (inv_ri + inv_r[j])) * inv_hz;
-            double A, vol;
+            double fel, f0;
             if (D == 3) {
-              A = contact_area(r, sa, sb);
-              vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+              fel = h * sqrt(h / Sr) * inv_hz;
+              const double A = contact_area(r, sa, sb);
+              const double vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+              f0 = -fel + C.adhesion * A;
+              if (vol != 0.0) pres -= f0 / vol;
             } else {
-              A = contact_length(sa, sb, h);
-              vol = A;
+              const double A = contact_length(sa, sb, h);  // also the contact's volume in 2D
+              if (A != 0.0) {
+                // one reciprocal u = 1 / (S A) gives both h / S = h A u and f0 / A = f0 S u
+                const double u = 1.0 / (Sr * A);
+                fel = h * sqrt(h * (A * u)) * inv_hz;
+                f0 = -fel + C.adhesion * A;
+                pres -= f0 * (Sr * u);
+              } else {
+                fel = h * sqrt(h / Sr) * inv_hz;
+                f0 = -fel;
+              }
             }
-            const double f0 = -fel + C.adhesion * A;
-            if (vol != 0.0) pres -= f0 / vol;
             CY_AXES(d, D) Fc[d] += f0 * rij[d];
           }
         }

@@ -323,18 +323,29 @@ struct Model {
       if (!(r <= (si + sj) / 2) || r == 0.0) return;
       const double sa = i < j ? si : sj, sb = i < j ? sj : si;
       const double h = std::fmax((si + sj) / 2 - r, 0.0);
-      // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2), the GPU model's expression
-      const double fel = h * std::sqrt(h / (1.0 / (si / 2) + 1.0 / (sj / 2))) * (1.0 / (0.75 * c2));
-      double A, vol;
+      const double Sr = 1.0 / (si / 2) + 1.0 / (sj / 2);
+      const double inv_hz = 1.0 / (0.75 * c2);
+      // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2), the GPU model's expression;
+      // in 2D one reciprocal u = 1 / (S A) gives both h / S = h A u and f0 / A = f0 S u
+      double fel, f0;
       if (D == 3) {
-        A = contact_area(r, sa, sb);
-        vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+        fel = h * std::sqrt(h / Sr) * inv_hz;
+        const double A = contact_area(r, sa, sb);
+        const double vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+        f0 = -fel + p.adhesion * A;
+        if (vol != 0.0) pres -= f0 / vol;
       } else {
-        A = contact_length(sa, sb, h);
-        vol = A;
+        const double A = contact_length(sa, sb, h);
+        if (A != 0.0) {
+          const double u = 1.0 / (Sr * A);
+          fel = h * std::sqrt(h * (A * u)) * inv_hz;
+          f0 = -fel + p.adhesion * A;
+          pres -= f0 * (Sr * u);
+        } else {
+          fel = h * std::sqrt(h / Sr) * inv_hz;
+          f0 = -fel;
+        }
       }
-      const double f0 = -fel + p.adhesion * A;
-      if (vol != 0.0) pres -= f0 / vol;
       for (int d = 0; d < D; ++d) Fc[d] += f0 * rij[d];
     });
     // the GPU model's xor tree: lane l adds lane l ^ off, off from L / 2 down to 1
