@@ -634,7 +634,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch parameters (no autotuner)")
     ap.add_argument("--staging", type=int, default=0, help="profile: list entries in flight (0: default)")
     ap.add_argument("--occupancy", type=int, default=0, help="profile: CTAs per SM of the list kernel (0: default)")
-    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_small", "dpd", "profile", "channel"],
+    ap.add_argument("--only", choices=["mixed", "plain", "skin", "cycle", "cycle_fp64", "cycle_small", "dpd", "profile",
+                                       "channel"],
                     default=None, help="run one form only (profiling); profile: the headline form alone, "
                                        "launched step by step, nothing else")
     args = ap.parse_args()
@@ -658,6 +659,9 @@ def main():
     if args.only == "dpd":
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 0, dpd=True)))
         print(json.dumps(run_cycle(G, device, args.steps, args.warmup, 1, dpd=True)))
+        return 0
+    if args.only == "cycle_fp64":  # the 1M-cell FP64 form alone (profiling)
+        print(json.dumps(run_cycle(G, device, args.steps, args.warmup)))
         return 0
     if args.only == "cycle":
         print(json.dumps(run_cycle_small(G, device)))

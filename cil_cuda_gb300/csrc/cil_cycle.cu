@@ -495,6 +495,49 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
     float Ff[3] = {0.0f, 0.0f, 0.0f}, presf = 0.0f;
     const int qi = MIXED ? P.qpos[i] : 0;
     const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // FP64: the candidates that pass the cheap distance test, in walk order (kNear at a time)
+    constexpr int kNear = 16;
+    int near[kNear];
+    int nnear = 0;
+    auto contacts = [&]() {
+      for (int k = 0; k < nnear; ++k) {
+        const int j = near[k];
+        double rij[3] = {0, 0, 0};
+        const double r2 = separation(C, S, xi, j, rij);
+        const double sj = S.sig[j];
+        const double cut = (si + sj) / 2;
+        const double r = sqrt(r2);
+        if (!(r <= cut) || r == 0.0) continue;
+        // the pair's first cell is the one of lower index (the contact length is not
+        // symmetric in the two diameters)
+        const double sa = i < j ? si : sj, sb = i < j ? sj : si;
+        const double h = fmax((si + sj) / 2 - r, 0.0);
+        const double Sr = inv_ri + inv_r[j];
+        // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2): one square root fewer
+        double fel, f0;
+        if (D == 3) {
+          fel = h * sqrt(h / Sr) * inv_hz;
+          const double A = contact_area(r, sa, sb);
+          const double vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
+          f0 = -fel + C.adhesion * A;
+          if (vol != 0.0) pres -= f0 / vol;
+        } else {
+          const double A = contact_length(sa, sb, h);  // also the contact's volume in 2D
+          if (A != 0.0) {
+            // one reciprocal u = 1 / (S A) gives both h / S = h A u and f0 / A = f0 S u
+            const double u = 1.0 / (Sr * A);
+            fel = h * sqrt(h * (A * u)) * inv_hz;
+            f0 = -fel + C.adhesion * A;
+            pres -= f0 * (Sr * u);
+          } else {
+            fel = h * sqrt(h / Sr) * inv_hz;
+            f0 = -fel;
+          }
+        }
+        CY_AXES(d, D) Fc[d] += f0 * rij[d];
+      }
+      nnear = 0;
+    };
     for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
       for (int o1 = (D > 1 ? st.lo[1] : 0); o1 <= (D > 1 ? st.hi[1] : 0); ++o1)
         for (int o2 = (D > 2 ? st.lo[2] : 0); o2 <= (D > 2 ? st.hi[2] : 0); ++o2) {
@@ -539,40 +582,15 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             if (j == i) continue;
             double rij[3] = {0, 0, 0};
             const double r2 = separation(C, S, xi, j, rij);
-            const double sj = S.sig[j];
-            const double cut = (si + sj) / 2;
+            const double cut = (si + S.sig[j]) / 2;
             if (r2 > 1.0000001 * (cut * cut)) continue;  // outside the contact distance (exact test below)
-            const double r = sqrt(r2);
-            if (!(r <= cut) || r == 0.0) continue;
-            // the pair's first cell is the one of lower index (the contact length is not
-            // symmetric in the two diameters)
-            const double sa = i < j ? si : sj, sb = i < j ? sj : si;
-            const double h = fmax((si + sj) / 2 - r, 0.0);
-            const double Sr = inv_ri + inv_r[j];
-            // h^1.5 / (0.75 c2 sqrt(S)) as h sqrt(h / S) / (0.75 c2): one square root fewer
-            double fel, f0;
-            if (D == 3) {
-              fel = h * sqrt(h / Sr) * inv_hz;
-              const double A = contact_area(r, sa, sb);
-              const double vol = (A == 0 ? 0 : (4 * kPi * ((sa / 2) * (sa / 2)) / 3));
-              f0 = -fel + C.adhesion * A;
-              if (vol != 0.0) pres -= f0 / vol;
-            } else {
-              const double A = contact_length(sa, sb, h);  // also the contact's volume in 2D
-              if (A != 0.0) {
-                // one reciprocal u = 1 / (S A) gives both h / S = h A u and f0 / A = f0 S u
-                const double u = 1.0 / (Sr * A);
-                fel = h * sqrt(h * (A * u)) * inv_hz;
-                f0 = -fel + C.adhesion * A;
-                pres -= f0 * (Sr * u);
-              } else {
-                fel = h * sqrt(h / Sr) * inv_hz;
-                f0 = -fel;
-              }
-            }
-            CY_AXES(d, D) Fc[d] += f0 * rij[d];
+            // near candidates are evaluated together after the walk (contacts), so the warp runs
+            // the FP64 contact arithmetic with its lanes converged instead of once per candidate
+            near[nnear++] = j;
+            if (nnear == kNear) contacts();
           }
         }
+    if (!MIXED) contacts();
     if (L > 1) {  // lanes l and l ^ 2^k combine, k from the highest: a fixed tree
       const unsigned gm = (L == 32 ? 0xffffffffu : ((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
       for (int off = L >> 1; off > 0; off >>= 1) {
@@ -670,6 +688,34 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
   const int qi = MIXED ? P.qpos[i] : 0;
   const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   const float4 vi4 = MIXED ? P.vk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  // FP64: the candidates in range, in walk order, evaluated kNear at a time after the cheap
+  // distance test, so the warp runs the pair terms (draws, normals, square roots) converged
+  constexpr int kNear = 16;
+  int near[kNear];
+  int nnear = 0;
+  auto pairs = [&]() {
+    for (int k = 0; k < nnear; ++k) {
+      const int j = near[k];
+      double rij[3] = {0, 0, 0};
+      const double r = sqrt(separation(C, S, xi, j, rij));
+      const double rc = i < j ? si : S.sig[j];
+      if (!(r < rc) || r == 0.0) continue;
+      const double ir = 1.0 / r;  // one division for the weight and the unit vector
+      const double w = 1 - r / rc;
+      const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
+      double xi_n[4];
+      normal2(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xi_n[0], &xi_n[1]);
+      if (D == 3) normal2(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xi_n[2], &xi_n[3]);
+      const double sw = sqrt(w);
+      CY_AXES(d, D) {
+        const double nd = rij[d] * ir;
+        const double vj = S.v[d * cap + j];
+        Fd[d] -= C.gamma_d * w * ((vi[d] - vj) * nd) * nd;
+        Fr[d] += C.sigma_r * sw * nd * xi_n[d];
+      }
+    }
+    nnear = 0;
+  };
   Stencil st;
   stencil_of(C, xi, __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits)), st);
   for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
@@ -702,24 +748,14 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
             continue;
           }
           double rij[3] = {0, 0, 0};
-          const double r = sqrt(separation(C, S, xi, j, rij));
+          const double r2 = separation(C, S, xi, j, rij);
           const double rc = i < j ? si : S.sig[j];
-          if (!(r < rc) || r == 0.0) continue;
-          const double ir = 1.0 / r;  // one division for the weight and the unit vector
-          const double w = 1 - r / rc;
-          const uint32_t a = static_cast<uint32_t>(i < j ? i : j), z = static_cast<uint32_t>(i < j ? j : i);
-          double xi_n[4];
-          normal2(philox4x32_10(a, ts, kCyDpd0, z, C.seed_lo, C.seed_hi), &xi_n[0], &xi_n[1]);
-          if (D == 3) normal2(philox4x32_10(a, ts, kCyDpd1, z, C.seed_lo, C.seed_hi), &xi_n[2], &xi_n[3]);
-          const double sw = sqrt(w);
-          CY_AXES(d, D) {
-            const double nd = rij[d] * ir;
-            const double vj = S.v[d * cap + j];
-            Fd[d] -= C.gamma_d * w * ((vi[d] - vj) * nd) * nd;
-            Fr[d] += C.sigma_r * sw * nd * xi_n[d];
-          }
+          if (r2 > 1.0000001 * (rc * rc)) continue;  // out of range (exact test in pairs())
+          near[nnear++] = j;
+          if (nnear == kNear) pairs();
         }
       }
+  if (!MIXED) pairs();
   if (MIXED)
     CY_AXES(d, D) {
       Fd[d] = static_cast<double>(Fdf[d]);
@@ -790,7 +826,9 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
           const int j = list[q];
           if (j == i) continue;
           double rij[3] = {0, 0, 0};
-          const double r = sqrt(separation(C, S, xi, j, rij));
+          const double r2 = separation(C, S, xi, j, rij);
+          if (r2 > 1.0000001 * (rc * rc)) continue;  // out of range (exact test below)
+          const double r = sqrt(r2);
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - ((r * r) / rc);
           CY_AXES(d, D) {

@@ -839,8 +839,14 @@ void read_all(cil_input *in) {
     p.rcut_scale = 1.0;
     p.force_shifted = 0;  // FORCE_SHIFTED is set only by the LJ attraction block (Input.cpp:306)
   } else {
-    key_error("GPU.FORCE_LAW", "the reference's " + pair +
-                                   " law differs from the GPU step's; set GPU.FORCE_LAW, EPSILON (and RCUT_SCALE)");
+    // HZ: cellCellForce (MD.cu:757-790) calls the overload of HZParams::elemForce that passes
+    // zero diameters (MD.cuh:265-270), so its force is -0 for every pair; EA: -Ei r^2 on every
+    // link-list candidate (MD.cuh:297-304, 317-322), so it depends on the bin size
+    key_error("GPU.FORCE_LAW", "the reference's two-element " + pair +
+                                   (pair == "HZ" ? " force is zero for every pair (HZParams::elemForce with zero "
+                                                   "diameters)"
+                                                 : " force acts on every link-list candidate (bin-size dependent)") +
+                                   "; set GPU.FORCE_LAW, EPSILON (and RCUT_SCALE)");
   }
   if (has_gpu && gpu.has("SPRING")) {  // the linear spring with the rest length growing over the cycle
     Node spring = gpu.child("SPRING");

@@ -150,6 +150,32 @@ def test_forces_match_oracle(gpu_lib, oracle_lib, lj, growth, channel, sc, fene,
     assert err <= FORCE_TOL * scale, (err, scale)
 
 
+def channel_variants():
+    """The 3D walled channel with the other laws: the cubic well, and the FENE / push bond (the
+    colony placed at its steady-state length), divisions off."""
+    import cil_cuda_gb300 as CG
+    base = S.channel_params(lxy=40.0, height=10.0, divide=0)
+    sc = dict(base, force_law=CG.FORCE_SC, epsilon=10.0, well_epsilon=0.5, well_sigma=0.3, rcut_scale=1.0)
+    fp = S.fene_params(box=40.0)
+    fene = dict(base, intra_law=fp["intra_law"], cil=0, fene_kappa=fp["fene_kappa"],
+                fene_kappa_push=fp["fene_kappa_push"], fene_spring_ratio=fp["fene_spring_ratio"],
+                fene_rmax=fp["fene_rmax"], motility=fp["motility"], zeta=fp["zeta"], rest0=fp["rest0"],
+                rest1=fp["rest0"])
+    lja = dict(base, force_law=CG.FORCE_LJ_WCA, epsilon=1.0, rcut_scale=2.5, force_shifted=1)
+    return {"sc3": (sc, S.channel_colony(1500, sc, seed=6)), "fene3": (fene, S.channel_colony(1500, fene, seed=7)),
+            "lj_attr3": (lja, S.channel_colony(1500, lja, seed=8))}
+
+
+@pytest.mark.parametrize("case", ["sc3", "fene3", "lj_attr3"])
+def test_forces_3d_other_laws(gpu_lib, oracle_lib, case):
+    p, st = channel_variants()[case]
+    fg, fo = forces_pair(gpu_lib, oracle_lib, p, st)
+    scale = np.abs(fo).max()
+    assert np.isfinite(fo).all() and np.abs(fg - fo).max() <= FORCE_TOL * scale
+    fg, fo = forces_pair(gpu_lib, oracle_lib, dict(p, noise_D=0.0), st, precision=gpu_lib.PREC_MIXED)
+    assert np.abs(fg - fo).max() / np.abs(fo).max() <= MIXED_TOL
+
+
 def test_mixed_precision_forces(gpu_lib, oracle_lib, lj, growth, sc, fene):
     for p, st in (lj, growth, sc, (dict(sc[0], force_shifted=1), sc[1]), lj_attraction(lj), lj_attraction(lj, 0),
                   fene, (dict(fene[0], cil=1), fene[1])):

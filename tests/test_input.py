@@ -131,7 +131,8 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
     (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
     (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
     (lambda d: (d["GPU"].pop("FORCE_LAW"), d["INTERACTIONS"]["PAIRFORCES"].update(SELECT="HZ"),
-                d["SPECIES"]["A"]["PAIRFORCES"].update(HZ={"SIGMA_CORE": [1.0, 0.9]})), "GPU.FORCE_LAW"),
+                d["SPECIES"]["A"]["PAIRFORCES"].update(HZ={"SIGMA_CORE": [1.0, 0.9]})),
+     "GPU.FORCE_LAW : the reference's two-element HZ force is zero for every pair"),
     (lambda d: d["INIT"]["A"].update(SELECT="H5"), "INIT.A.H5 : key not found"),
     (lambda d: d["INIT"]["A"].update(SELECT="H5", H5={"SELECT": "LOCATION", "LOCATION": ["/nonexistent.h5", "R"]}),
      "/nonexistent.h5: cannot open"),
