@@ -175,6 +175,36 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
     } else {
       int bi[D];
       bin_decode<D>(C, a.sbin[s], bi);
+      // the partners inside the cutoff, in walk order with their neighbour bin: their pair
+      // forces are evaluated kNear at a time after the walk, so the warp runs the FP64 law with
+      // its lanes converged instead of once per candidate (the sums keep the walk order)
+      constexpr int kNear = 16;
+      int near_t[kNear];
+      unsigned char near_o[kNear];
+      int nnear = 0;
+      auto pairs = [&]() {
+        for (int k = 0; k < nnear; ++k) {
+          const int tt = near_t[k], code = near_o[k];
+          const int oo[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+          int nb[D];
+          double shift[D];
+          neighbor_bin<D>(C, bi, oo, nb, shift);
+          double dx[D];
+          double r2 = 0.0;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            dx[d] = (__ldg(a.x_in + d * SS + tt) + shift[d]) - xi[d];
+            r2 += dx[d] * dx[d];
+          }
+          double f0;
+          if (pair_force<LAW, double>(r2, si, __ldg(a.sig + tt), eps, rcs, f0, C.well_eps, C.well_sigma,
+                                      C.force_shifted)) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
+          }
+        }
+        nnear = 0;
+      };
       int o[3] = {-1, -1, -1};
       for (o[0] = -1; o[0] <= 1; ++o[0])
         for (o[1] = -1; o[1] <= 1; ++o[1])
@@ -183,23 +213,23 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
             double shift[D];
             if (!neighbor_bin<D>(C, bi, o, nb, shift)) continue;
             const int2 r = a.range[C.bin_base + bin_id<D>(C, nb)];
+            const unsigned char code = static_cast<unsigned char>((o[0] + 1) + 3 * (o[1] + 1) + 9 * (o[2] + 1));
             for (int tt = r.x; tt < r.y; ++tt) {
               const int ej = __ldg(a.eid + tt);
               if (ej < 0 || (ej >> 1) == g) continue;
-              double dx[D];
               double r2 = 0.0;
 #pragma unroll
               for (int d = 0; d < D; ++d) {
-                dx[d] = (__ldg(a.x_in + d * SS + tt) + shift[d]) - xi[d];
-                r2 += dx[d] * dx[d];
+                const double dx = (__ldg(a.x_in + d * SS + tt) + shift[d]) - xi[d];
+                r2 += dx * dx;
               }
-              double f0;
-              if (pair_force<LAW, double>(r2, si, __ldg(a.sig + tt), eps, rcs, f0, C.well_eps, C.well_sigma, C.force_shifted)) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) F[d] += f0 * dx[d];
-              }
+              if (!pair_in_range<LAW, double>(r2, si, __ldg(a.sig + tt), rcs, C.well_sigma)) continue;
+              near_t[nnear] = tt;
+              near_o[nnear] = code;
+              if (++nnear == kNear) pairs();
             }
           }
+      pairs();
     }
 
     // ---- checks, integration, outputs

@@ -488,6 +488,17 @@ __device__ __forceinline__ bool pair_force(R r2, R si, R sj, R eps, R rcs, R &f0
   }
 }
 
+// The range test of pair_force alone (the same expressions, so the same answer).
+template <int LAW, typename R>
+__device__ __forceinline__ bool pair_in_range(R r2, R si, R sj, R rcs, R xi) {
+  const R sij = R(0.5) * (si + sj);
+  if (LAW == CIL_FORCE_SC)
+    return r2 > rcs * rcs * ((sij - xi) * (sij - xi)) && r2 <= rcs * rcs * ((sij + xi) * (sij + xi));
+  if (LAW == CIL_FORCE_LJ_WCA) return r2 <= (sij * sij) * (rcs * rcs);
+  const R rc = rcs * sij;
+  return r2 < rc * rc && r2 > R(0);
+}
+
 // FP32 pair force, branch-free: the law is evaluated for every candidate and masked
 // (fast reciprocal / reciprocal square root; the mixed form's tolerance is FP32-level)
 template <int LAW>
