@@ -178,6 +178,8 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       // the partners inside the cutoff, in walk order with their neighbour bin: their pair
       // forces are evaluated kNear at a time after the walk, so the warp runs the FP64 law with
       // its lanes converged instead of once per candidate (the sums keep the walk order)
+      const float sif = static_cast<float>(si), rcsf = static_cast<float>(rcs);
+      const float xif = static_cast<float>(C.well_sigma);
       constexpr int kNear = 16;
       int near_t[kNear];
       unsigned char near_o[kNear];
@@ -217,13 +219,15 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
             for (int tt = r.x; tt < r.y; ++tt) {
               const int ej = __ldg(a.eid + tt);
               if (ej < 0 || (ej >> 1) == g) continue;
-              double r2 = 0.0;
+              // a conservative FP32 range test on the FP64 separation (pair_force repeats the
+              // exact test): one FP64 subtraction per axis per candidate, the rest in FP32
+              float r2f = 0.0f;
 #pragma unroll
               for (int d = 0; d < D; ++d) {
-                const double dx = (__ldg(a.x_in + d * SS + tt) + shift[d]) - xi[d];
-                r2 += dx * dx;
+                const float dx = static_cast<float>((__ldg(a.x_in + d * SS + tt) + shift[d]) - xi[d]);
+                r2f += dx * dx;
               }
-              if (!pair_in_range<LAW, double>(r2, si, __ldg(a.sig + tt), rcs, C.well_sigma)) continue;
+              if (!pair_maybe_in_range<LAW>(r2f, sif, static_cast<float>(__ldg(a.sig + tt)), rcsf, xif)) continue;
               near_t[nnear] = tt;
               near_o[nnear] = code;
               if (++nnear == kNear) pairs();

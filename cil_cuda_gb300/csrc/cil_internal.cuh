@@ -499,6 +499,18 @@ __device__ __forceinline__ bool pair_in_range(R r2, R si, R sj, R rcs, R xi) {
   return r2 < rc * rc && r2 > R(0);
 }
 
+// A superset of pair_in_range in FP32, for a squared separation r2f within a relative 1e-6 of
+// the FP64 one: the bounds are widened by 1e-5, so every pair that pair_force accepts passes.
+template <int LAW>
+__device__ __forceinline__ bool pair_maybe_in_range(float r2f, float si, float sj, float rcs, float xi) {
+  const float sij = 0.5f * (si + sj);
+  constexpr float up = 1.00001f, dn = 0.99999f;
+  if (LAW == CIL_FORCE_SC)
+    return r2f >= dn * (rcs * rcs * ((sij - xi) * (sij - xi))) && r2f <= up * (rcs * rcs * ((sij + xi) * (sij + xi)));
+  const float rc = rcs * sij;
+  return r2f <= up * (rc * rc);
+}
+
 // FP32 pair force, branch-free: the law is evaluated for every candidate and masked
 // (fast reciprocal / reciprocal square root; the mixed form's tolerance is FP32-level)
 template <int LAW>
