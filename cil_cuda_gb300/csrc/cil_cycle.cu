@@ -273,6 +273,26 @@ __device__ inline float packed_sep(const CyConst &C, const float4 &pi, const flo
   return r2;
 }
 
+// The squared minimum-image separation in FP32 from the FP64 difference, for the walks' range
+// tests: within a relative 1e-6 of separation()'s (a pair near half a box may wrap the other
+// way, and is out of range either way), so bounds widened by 1e-5 let every pair in range pass
+// to the exact FP64 test.
+__device__ inline float separation_f(const CyConst &C, const CySet &S, const double *xi, int j) {
+  const size_t cap = C.capacity;
+  float r2 = 0.0f;
+  CY_AXES(d, C.D) {
+    float v = static_cast<float>(S.x[d * cap + j] - xi[d]);
+    if (C.periodic[d]) {
+      if (v > C.halff[d])
+        v -= C.boxf[d];
+      else if (v < -C.halff[d])
+        v += C.boxf[d];
+    }
+    r2 += v * v;
+  }
+  return r2;
+}
+
 // ---------------------------------------------------------------- block scan
 // Exclusive scan over the block (any multiple of 32 threads up to kTile)
 __device__ inline int block_excl_scan(int v, int *total) {
@@ -580,10 +600,8 @@ __global__ void __launch_bounds__(kTile) k_cy_force(CyConst C, CySet S, double *
             }
             const int j = list[q];
             if (j == i) continue;
-            double rij[3] = {0, 0, 0};
-            const double r2 = separation(C, S, xi, j, rij);
-            const double cut = (si + S.sig[j]) / 2;
-            if (r2 > 1.0000001 * (cut * cut)) continue;  // outside the contact distance (exact test below)
+            const float cutf = 0.5f * (sif + static_cast<float>(S.sig[j]));
+            if (separation_f(C, S, xi, j) > 1.00001f * (cutf * cutf)) continue;  // out of contact (exact test in contacts())
             // near candidates are evaluated together after the walk (contacts), so the warp runs
             // the FP64 contact arithmetic with its lanes converged instead of once per candidate
             near[nnear++] = j;
@@ -747,10 +765,8 @@ __global__ void __launch_bounds__(kTile) k_dpd_pair(CyConst C, CySet S, double *
             }
             continue;
           }
-          double rij[3] = {0, 0, 0};
-          const double r2 = separation(C, S, xi, j, rij);
-          const double rc = i < j ? si : S.sig[j];
-          if (r2 > 1.0000001 * (rc * rc)) continue;  // out of range (exact test in pairs())
+          const float rcf = static_cast<float>(i < j ? si : S.sig[j]);
+          if (separation_f(C, S, xi, j) > 1.00001f * (rcf * rcf)) continue;  // out of range (exact test in pairs())
           near[nnear++] = j;
           if (nnear == kNear) pairs();
         }
@@ -825,10 +841,9 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
           }
           const int j = list[q];
           if (j == i) continue;
+          if (separation_f(C, S, xi, j) > 1.00001f * (rcf * rcf)) continue;  // out of range (exact test below)
           double rij[3] = {0, 0, 0};
-          const double r2 = separation(C, S, xi, j, rij);
-          if (r2 > 1.0000001 * (rc * rc)) continue;  // out of range (exact test below)
-          const double r = sqrt(r2);
+          const double r = sqrt(separation(C, S, xi, j, rij));
           if (!(r < rc) || r == 0.0) continue;
           const double w = 1 - ((r * r) / rc);
           CY_AXES(d, D) {
