@@ -816,6 +816,25 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
   const float4 pi4 = MIXED ? P.pk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   const float4 vi4 = MIXED ? P.vk[qi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   const double smax = __longlong_as_double(static_cast<long long>(cnt->sigma_max_bits));
+  // FP64: the candidates in range, in walk order, evaluated kNear at a time after the walk with
+  // the warp's lanes converged (same terms in the same order)
+  constexpr int kNear = 16;
+  int near[kNear];
+  int nnear = 0;
+  auto pairs = [&]() {
+    for (int k = 0; k < nnear; ++k) {
+      const int j = near[k];
+      double rij[3] = {0, 0, 0};
+      const double r = sqrt(separation(C, S, xi, j, rij));
+      if (!(r < rc) || r == 0.0) continue;
+      const double w = 1 - ((r * r) / rc);
+      CY_AXES(d, D) {
+        const double nd = -rij[d] / r;
+        Fd[d] -= C.gamma_d * w * ((vi[d] - S.v[d * cap + j]) * nd) * nd;
+      }
+    }
+    nnear = 0;
+  };
   Stencil st;
   stencil_of(C, xi, smax > rc ? smax : rc, st);
   for (int o0 = st.lo[0]; o0 <= st.hi[0]; ++o0)
@@ -841,17 +860,12 @@ __global__ void __launch_bounds__(kTile) k_dpd_dis(CyConst C, CySet S, const CyC
           }
           const int j = list[q];
           if (j == i) continue;
-          if (separation_f(C, S, xi, j) > 1.00001f * (rcf * rcf)) continue;  // out of range (exact test below)
-          double rij[3] = {0, 0, 0};
-          const double r = sqrt(separation(C, S, xi, j, rij));
-          if (!(r < rc) || r == 0.0) continue;
-          const double w = 1 - ((r * r) / rc);
-          CY_AXES(d, D) {
-            const double nd = -rij[d] / r;
-            Fd[d] -= C.gamma_d * w * ((vi[d] - S.v[d * cap + j]) * nd) * nd;
-          }
+          if (separation_f(C, S, xi, j) > 1.00001f * (rcf * rcf)) continue;  // out of range (exact test in pairs())
+          near[nnear++] = j;
+          if (nnear == kNear) pairs();
         }
       }
+  if (!MIXED) pairs();
   CY_AXES(d, D) S.fd[d * cap + i] = MIXED ? Fd[d] + static_cast<double>(Fdf[d]) : Fd[d];
 }
 
