@@ -1359,10 +1359,12 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
   hc.uploaded = true;
   hc.sigma_max = smax;
   hc.n = n;
-  hc.t0.assign(v->t0, v->t0 + n);
-  hc.tsw.assign(v->tswitch, v->tswitch + n);
-  hc.t0.resize(hc.cap);
-  hc.tsw.resize(hc.cap);
+  if (h->cfg.rng_mode == CIL_RNG_DSFMT) {  // the oracle mode's host mirror of the cycles
+    hc.t0.assign(v->t0, v->t0 + n);
+    hc.tsw.assign(v->tswitch, v->tswitch + n);
+    hc.t0.resize(hc.cap);
+    hc.tsw.resize(hc.cap);
+  }
   h->ts = v->ts;
   const int tsi = static_cast<int>(v->ts);
   CUDA_TRY(h, cudaMemcpyAsync(h->d_ts, &tsi, sizeof(int), cudaMemcpyHostToDevice, h->stream));

@@ -821,18 +821,26 @@ template <int D>
 __global__ void k_upload_check(const ColonyConst *col, int c, int ncells, const double *pos, const double *sig,
                                int *chk) {
   const ColonyConst &C = col[c];
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= 2 * ncells) return;
-  const double s = sig[e];
-  int bad = (s > 0.0 && isfinite(s)) ? 0 : 1;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // the grid is whole warps
+  unsigned long long smax = 0ull;  // bits of the largest valid diameter (positive doubles order as integers)
+  if (e < 2 * ncells) {
+    const double s = sig[e];
+    int bad = (s > 0.0 && isfinite(s)) ? 0 : 1;
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const double x = pos[static_cast<size_t>(e) * D + d];
-    if (!(isfinite(x) && x >= 0.0 && x < C.box[d])) bad |= 2;
+    for (int d = 0; d < D; ++d) {
+      const double x = pos[static_cast<size_t>(e) * D + d];
+      if (!(isfinite(x) && x >= 0.0 && x < C.box[d])) bad |= 2;
+    }
+    if (bad) atomicOr(chk, bad);
+    if (!(bad & 1)) smax = static_cast<unsigned long long>(__double_as_longlong(s));
   }
-  if (bad) atomicOr(chk, bad);
-  if (!(bad & 1))
-    atomicMax(reinterpret_cast<unsigned long long *>(chk + 2), static_cast<unsigned long long>(__double_as_longlong(s)));
+  // one atomic per warp: the warp's largest diameter first
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_down_sync(0xffffffffu, smax, o);
+    smax = v > smax ? v : smax;
+  }
+  if ((threadIdx.x & 31) == 0 && smax) atomicMax(reinterpret_cast<unsigned long long *>(chk + 2), smax);
 }
 
 // Upload, step 2 (nothing happens when step 1 found a bad value): the staged positions into the
