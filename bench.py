@@ -311,8 +311,10 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
     GPU runs this one), a GSD frame after every GTS steps written by the device-fed frame
     writer (outputFrame, OutputWriter.cpp:640-644; its copy to the host and its file writes
     overlap the next steps; none in a run shorter than GTS steps), and the final state
-    downloaded into pinned host arrays. The frame file is flushed and closed inside the timed
-    region."""
+    downloaded into pinned host arrays. Every queued frame is written to the file (flush) inside
+    the timed region; the file is closed after it, as the reference closes its output after
+    its step loop (finalizeOutput), and the engine (learned scheduler included) is configured
+    before it, as the reference reads its parameters before the loop."""
     import tempfile
     n = len(st["sigma"])
     eng = G.Engine([p], [CAP], precision=precision, rng=G.RNG_PHILOX, seed=seed, device=device, skin=skin,
@@ -333,19 +335,20 @@ def run_e2e(G, p, st, precision, steps, device, seed, skin=0.0, sched=False, tun
         # the output file and its staging are opened before the run, as the reference's
         # initializeOutput is (outside its simulation timer)
         w = eng.frame_writer(0, os.path.join(tmp, "e2e.gsd"))
-        t0 = time.perf_counter()
-        eng.upload(0, **st)
         if sched:
             from cil_cuda_gb300 import skin_scheduler as SS
             SS.install(eng)
+        t0 = time.perf_counter()
+        eng.upload(0, **st)
         for k in range(steps):
             eng.step(1)
             d2h += 56  # the per-call status read of the colony counters
             if (k + 1) % GTS == 0:
                 w.write()
-        w.close()
+        w.flush()
         fin = eng.download(0, want=("pos", "sigma", "t0", "tswitch"), out=res)
         wall = time.perf_counter() - t0
+        w.close()
         fs = w.last_stats
     n1 = fin["ncells"]
     d2h += n1 * (res["pos"][0].nbytes + res["sigma"][0].nbytes + 8)
