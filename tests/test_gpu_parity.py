@@ -327,6 +327,38 @@ def test_batched_colonies_equal_single(gpu_lib):
         np.testing.assert_array_equal(batched[c]["pos"], single["pos"])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_colonies_with_different_bonds(gpu_lib, precision):
+    """One handle holding a colony with the linear spring and one with the reference's FENE /
+    push bond (the bond is a per-colony parameter) gives each the state it has alone."""
+    ps, sts = [], []
+    for i, n in enumerate((500, 900)):
+        p = S.growth_params(box=0.0, noise_D=0.0, divide=0, apop_rate=0.0)
+        if i == 1:
+            f = S.fene_params()
+            p.update({k: f[k] for k in ("intra_law", "cil", "fene_kappa", "fene_kappa_push", "fene_spring_ratio",
+                                        "fene_rmax", "motility", "zeta", "rest0", "rest1")})
+        p, st = S.square_colony(n, p, seed=10 + i)
+        ps.append(p)
+        sts.append(st)
+    eng = gpu_lib.Engine(ps, [len(s["sigma"]) for s in sts], precision=precision)
+    for c, st in enumerate(sts):
+        eng.upload(c, **st)
+    eng.step(20)
+    batched = [eng.download(c) for c in range(2)]
+    eng.close()
+    for c in range(2):
+        e1 = engine(gpu_lib, ps[c], len(sts[c]["sigma"]), precision=precision)
+        e1.upload(0, **sts[c])
+        e1.step(20)
+        single = e1.download(0)
+        e1.close()
+        if precision == 0:
+            np.testing.assert_array_equal(batched[c]["pos"], single["pos"])
+        else:  # the mixed kernel may sum a cell's FP32 pair terms in another order in a batch
+            assert np.abs(minimage(batched[c]["pos"], single["pos"], ps[c])).max() <= 1e-6
+
+
 def test_error_nan(gpu_lib):
     p = S.base_params(2, gpu_lib.FORCE_LJ_WCA, [10.0, 10.0], noise_D=0.0)
     pos = np.array([[[5.0, 5.0], [5.5, 5.0]], [[5.0, 5.0], [4.5, 5.0]]])  # coincident back elements
