@@ -499,7 +499,7 @@ template <int D, int LAW>
 __global__ void __launch_bounds__(kFreshBlock) k_fresh_pairs(SkinArgs a) {
   constexpr int NB = (D == 2) ? 9 : 27;
   // the fresh sets of all colonies as one flattened range (inclusive prefix of their sizes)
-  __shared__ int s_pref[kMaxSkinColonies];
+  extern __shared__ int s_pref[];  // [B], sized at launch (all blocks resident in one wave)
   __shared__ int s_warp[kFreshWarps];
   __shared__ int s_run;
   const int nb_col = a.B;  // <= kMaxSkinColonies (checked at create)
@@ -670,16 +670,16 @@ void fresh_d(const SkinArgs &a, int law, cudaStream_t s) {
   const int grid = a.grid;
   switch (law) {
     case CIL_FORCE_LJ_WCA:
-      k_fresh_pairs<D, CIL_FORCE_LJ_WCA><<<grid, kFreshBlock, 0, s>>>(a);
+      k_fresh_pairs<D, CIL_FORCE_LJ_WCA><<<grid, kFreshBlock, sizeof(int) * a.B, s>>>(a);
       break;
     case CIL_FORCE_SOFTCORE:
-      k_fresh_pairs<D, CIL_FORCE_SOFTCORE><<<grid, kFreshBlock, 0, s>>>(a);
+      k_fresh_pairs<D, CIL_FORCE_SOFTCORE><<<grid, kFreshBlock, sizeof(int) * a.B, s>>>(a);
       break;
     case CIL_FORCE_SC:
-      k_fresh_pairs<D, CIL_FORCE_SC><<<grid, kFreshBlock, 0, s>>>(a);
+      k_fresh_pairs<D, CIL_FORCE_SC><<<grid, kFreshBlock, sizeof(int) * a.B, s>>>(a);
       break;
     default:
-      k_fresh_pairs<D, CIL_FORCE_HERTZ><<<grid, kFreshBlock, 0, s>>>(a);
+      k_fresh_pairs<D, CIL_FORCE_HERTZ><<<grid, kFreshBlock, sizeof(int) * a.B, s>>>(a);
       break;
   }
 }
