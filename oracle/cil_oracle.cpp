@@ -257,6 +257,9 @@ const int kDns3d[14][3] = {{0, 0, 0},  {1, 0, 0},  {1, 1, 0},   {0, 1, 0},  {-1,
                            {0, 0, 1},  {1, 0, 1},  {1, 1, 1},   {0, 1, 1},  {-1, 1, 1},
                            {-1, 0, 1}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1}};
 
+// CellState (Cell.cuh:26-30)
+constexpr int kDividing = 0, kCrawling = 1, kUndefined = 2;
+
 struct Oracle {
   ora_params p{};
   int D = 2;
@@ -264,6 +267,8 @@ struct Oracle {
   int nthreads = 0;
   int integrator = 0;  // 0 Euler, 1 Heun
   double fene_r2max = 0.0, fene_rss = 0.0;  // intra_law 1: RMAX^2, steady-state length
+  double fene_r2max_div = 0.0;                // intra_law 1: RMAX_DIVISION^2 (RMAX^2 without it)
+  std::vector<int> cst;                       // CellState per cell (Cell.cuh:26-30)
   std::vector<double> pos, vel, frc, sig, wiener;
   std::vector<int> t0, tsw;
   Rng rng;
@@ -324,8 +329,10 @@ struct Oracle {
       // without CIL (MD.cu:568-571); the bond acts twice (strongContract = 2). The reference's
       // velocity-squared friction (MD.cu:592-596) is left out: its two-element integrator
       // (StochasticHeun) never updates the velocities, which stay 0, and the NaN guard drops it.
+      const bool dividing = cst[c] == kDividing;
       const double smax = std::max(sig[2 * c], sig[2 * c + 1]);
-      const double r2max = fene_r2max > smax ? fene_r2max : smax;
+      const double r2max0 = dividing ? fene_r2max_div : fene_r2max;
+      const double r2max = r2max0 > smax ? r2max0 : smax;
       const double lim = r2max * p.fene_spring_ratio;
       double spring;
       if (r2 <= lim) {
@@ -333,6 +340,19 @@ struct Oracle {
       } else {
         const double q = (r2 - lim) / (r2max * (1.0 - p.fene_spring_ratio));
         spring = -p.fene_kappa / (1.0 - q * q);
+      }
+      if (dividing) {
+        // MD.cu:559-567: the growth activity along rij against the FENE force at the division
+        // length (feneDivMax, with divisionR2min = Rmin^2), the bond acting once
+        const double qd = p.div_rmin * p.div_rmin / r2max;
+        const double fdm = -p.fene_kappa / (1.0 - qd * qd);
+        double act[2];
+        for (int j = 0; j < 2; ++j) act[j] = -p.growth_k0[j] * fdm + p.growth_k1[j] + p.growth_k2[j] * (r2 * r2);
+        for (int d = 0; d < D; ++d) {
+          f0[d] = -(act[0] * rij[d] + spring * rij[d] * 1.0);
+          f1[d] = act[1] * rij[d] + spring * rij[d] * 1.0;
+        }
+        return;
       }
       const double scaling = p.cil ? 1.0 : fene_rss / r;
       for (int d = 0; d < D; ++d) {
@@ -541,6 +561,7 @@ struct Oracle {
     }
     t0[dst] = t0[src];
     tsw[dst] = tsw[src];
+    cst[dst] = cst[src];
     for (int d = 0; d < D; ++d) {
       com_prev[static_cast<size_t>(dst) * D + d] = com_prev[static_cast<size_t>(src) * D + d];
       disp[static_cast<size_t>(dst) * D + d] = disp[static_cast<size_t>(src) * D + d];
@@ -552,8 +573,82 @@ struct Oracle {
   // cycle ends (ts == tswitch); binaryCellDivision (MD.cu:721-731) places both daughters
   // with half-separation rest0/2; random draws in the reference order: mother axis,
   // daughter axis, daughter cycle, mother cycle.
+  // randomTimeSpan (MD.cuh:434-436) of the migration time
+  int mig_span() {
+    const int s = nint(rng.normal(p.mig_tau_mu, p.mig_tau_sigma) / p.dt);
+    return s >= 1 ? s : 1;
+  }
+
+  void reset_motion(int c) {
+    for (int j = 0; j < 2; ++j)
+      for (int d = 0; d < D; ++d) V(c, j)[d] = F(c, j)[d] = 0.0;
+  }
+
+  // calculDivisions (CIL.cu:369-455) for the reference's two-element cells with the FENE bond:
+  // a crawling cell whose time ends starts dividing (time += span(TAU_DIVISION)); a dividing
+  // cell whose elements are Rmin apart (binaryCellDivisionCriteria, MD.cuh:426-433) divides
+  // (binaryCellDivision with radius R0, MD.cu:721-731; both cells crawl, their times from
+  // TAU_MIGRATION, the mother's added to her own), and one whose time ends without that fails
+  // (binaryCellDivisionFail, MD.cu:736-752). Diameters return to SIGMA_CORE.
+  int state_divisions() {
+    const int n0 = n;
+    int err = 0;
+    for (int i = 0; i < n0; ++i) {
+      if (cst[i] == kDividing) {
+        double rij[3] = {0, 0, 0};
+        const double r2 = distance(rij, P(i, 1), P(i, 0));
+        const bool ok = p.div_rmin_ratio != 0.0 ? r2 >= p.div_rmin_ratio * sig[2 * static_cast<size_t>(i)]
+                                                : r2 >= p.div_rmin * p.div_rmin;
+        if (ok) {
+          if (n >= cap) {
+            err = -2;
+            continue;
+          }
+          const int k = n++;
+          copy_cell(k, i);
+          for (int d = 0; d < D; ++d) P(k, 0)[d] = P(i, 0)[d];
+          reorient(P(i, 0), P(i, 1), p.div_r0);
+          reorient(P(k, 1), P(k, 0), p.div_r0);
+          t0[k] = ts;
+          t0[i] = ts;
+          tsw[k] = ts + mig_span();
+          cst[k] = kCrawling;
+          sig[2 * static_cast<size_t>(k)] = p.sigma_core[0];
+          sig[2 * static_cast<size_t>(k) + 1] = p.sigma_core[1];
+          reset_motion(k);
+          reset_motion(i);
+          tsw[i] += mig_span();
+          cst[i] = kCrawling;
+          sig[2 * static_cast<size_t>(i)] = p.sigma_core[0];
+          sig[2 * static_cast<size_t>(i) + 1] = p.sigma_core[1];
+          events.push_back({ts, 0, i, k});
+          ++ndiv_total;
+        } else if (tsw[i] == ts) {
+          // back element to the centre (a plain add, MD.cu:744-746), then both reoriented
+          double dr[3] = {0, 0, 0};
+          distance(dr, P(i, 0), P(i, 1));
+          for (int d = 0; d < D; ++d) P(i, 0)[d] += dr[d] * 0.5;
+          reorient(P(i, 1), P(i, 0), p.div_r0);
+          reset_motion(i);
+          tsw[i] += mig_span();
+          cst[i] = kCrawling;
+          sig[2 * static_cast<size_t>(i)] = p.sigma_core[0];
+          sig[2 * static_cast<size_t>(i) + 1] = p.sigma_core[1];
+          events.push_back({ts, 2, i, i});
+        }
+      } else if (tsw[i] == ts) {
+        cst[i] = kDividing;
+        tsw[i] += time_span();
+        reset_motion(i);
+        events.push_back({ts, 3, i, i});
+      }
+    }
+    return err;
+  }
+
   int divisions() {
     if (!p.divide) return 0;
+    if (p.intra_law == 1) return state_divisions();
     const int n0 = n;
     const double radius = 0.5 * p.rest0;
     int err = 0;
@@ -657,7 +752,9 @@ void *ora_create(const ora_params *p, int32_t cap_cells, uint32_t seed) {
     const double zi0 = 1.0 / p->zeta[0], zi1 = 1.0 / p->zeta[1];
     const double alpha = zi0 + zi1, beta = p->motility[0] * zi0 + p->motility[1] * zi1;
     o->fene_rss = std::sqrt(o->fene_r2max * (1.0 - alpha / beta * p->fene_kappa));
+    o->fene_r2max_div = p->fene_rmax_division > 0.0 ? p->fene_rmax_division * p->fene_rmax_division : o->fene_r2max;
   }
+  o->cst.assign(cap_cells, kUndefined);
   return o;
 }
 
@@ -680,8 +777,19 @@ int32_t ora_set_state(void *h, int32_t ncells, const double *pos, const double *
   std::memcpy(o->tsw.data(), tswitch, sizeof(int32_t) * ncells);
   std::fill(o->vel.begin(), o->vel.end(), 0.0);
   std::fill(o->frc.begin(), o->frc.end(), 0.0);
+  std::fill(o->cst.begin(), o->cst.end(), kUndefined);
   o->obs_ready = false;
   return 0;
+}
+
+void ora_set_cell_states(void *h, int32_t n, const int32_t *states) {
+  Oracle *o = H(h);
+  for (int i = 0; i < n && i < o->cap; ++i) o->cst[i] = states[i];
+}
+
+void ora_get_cell_states(const void *h, int32_t *states) {
+  const Oracle *o = H(h);
+  for (int i = 0; i < o->n; ++i) states[i] = o->cst[i];
 }
 
 int32_t ora_num_cells(const void *h) { return H(h)->n; }

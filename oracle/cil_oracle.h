@@ -55,6 +55,14 @@ typedef struct ora_params {
   int32_t intra_law;                /* 0: linear spring with growth, 1: the reference's FENE / push bond */
   int32_t cil;                      /* intra_law 1: the species' CIL flag */
   double fene_kappa, fene_kappa_push, fene_spring_ratio, fene_rmax; /* intra_law 1 */
+  /* intra_law 1 with divide: the reference's crawling/dividing cells (calculDivisions,
+   * CIL.cu:369-455): RMAX_DIVISION (0: RMAX), GROWTHK0/1/2 per element, R0, Rmin, Rmin_RATIO,
+   * TAU_MIGRATION, the diameters a division resets to (SIGMA_CORE) */
+  double fene_rmax_division;
+  double growth_k0[2], growth_k1[2], growth_k2[2];
+  double div_r0, div_rmin, div_rmin_ratio;
+  double mig_tau_mu, mig_tau_sigma;
+  double sigma_core[2];
 } ora_params;
 
 typedef struct ora_event {
@@ -83,6 +91,10 @@ int32_t ora_set_state(void *h, int32_t ncells, const double *pos, const double *
                       const int32_t *t0, const int32_t *tswitch, int32_t ts);
 int32_t ora_num_cells(const void *h);
 int32_t ora_timestep(const void *h);
+/* cell states of the reference's two-element cells (CellState: 0 dividing, 1 crawling,
+ * 2 undefined), [cell]; set after ora_set_state (which leaves every cell undefined) */
+void ora_set_cell_states(void *h, int32_t n, const int32_t *states);
+void ora_get_cell_states(const void *h, int32_t *states);
 void ora_get_state(const void *h, double *pos, double *sigma, double *vel, double *frc,
                    int32_t *t0, int32_t *tswitch);
 /* forces at the current state (draws the noise like calculForcesPressure) into frc */

@@ -52,6 +52,16 @@ class OraParams(C.Structure):
         ("fene_kappa_push", C.c_double),
         ("fene_spring_ratio", C.c_double),
         ("fene_rmax", C.c_double),
+        ("fene_rmax_division", C.c_double),
+        ("growth_k0", C.c_double * 2),
+        ("growth_k1", C.c_double * 2),
+        ("growth_k2", C.c_double * 2),
+        ("div_r0", C.c_double),
+        ("div_rmin", C.c_double),
+        ("div_rmin_ratio", C.c_double),
+        ("mig_tau_mu", C.c_double),
+        ("mig_tau_sigma", C.c_double),
+        ("sigma_core", C.c_double * 2),
     ]
 
 
@@ -99,6 +109,10 @@ def lib():
         L.ora_timestep.restype = i32
         L.ora_timestep.argtypes = [vp]
         L.ora_get_state.argtypes = [vp, dp, dp, dp, dp, ip, ip]
+        L.ora_set_cell_states.restype = None
+        L.ora_set_cell_states.argtypes = [vp, i32, ip]
+        L.ora_get_cell_states.restype = None
+        L.ora_get_cell_states.argtypes = [vp, ip]
         L.ora_compute_forces.argtypes = [vp]
         L.ora_step.restype = i32
         L.ora_step.argtypes = [vp, i32]
@@ -163,7 +177,7 @@ class Oracle:
         except Exception:
             pass
 
-    def set_state(self, pos, sigma, t0, tswitch, ts=0):
+    def set_state(self, pos, sigma, t0, tswitch, ts=0, cell_state=None):
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         sigma = np.ascontiguousarray(sigma, dtype=np.float64)
         t0 = np.ascontiguousarray(t0, dtype=np.int32)
@@ -172,6 +186,9 @@ class Oracle:
         rc = self.L.ora_set_state(self.h, n, _dp(pos), _dp(sigma), _ip(t0), _ip(tswitch), ts)
         if rc != 0:
             raise ValueError(f"ora_set_state rc={rc}")
+        if cell_state is not None:
+            cs = np.ascontiguousarray(cell_state, dtype=np.int32)
+            self.L.ora_set_cell_states(self.h, n, _ip(cs))
 
     @property
     def ncells(self) -> int:
@@ -190,7 +207,9 @@ class Oracle:
         t0 = np.zeros(n, np.int32)
         tsw = np.zeros(n, np.int32)
         self.L.ora_get_state(self.h, _dp(pos), _dp(sig), _dp(vel), _dp(frc), _ip(t0), _ip(tsw))
-        return dict(pos=pos, sigma=sig, vel=vel, frc=frc, t0=t0, tswitch=tsw)
+        cs = np.zeros(n, np.int32)
+        self.L.ora_get_cell_states(self.h, _ip(cs))
+        return dict(pos=pos, sigma=sig, vel=vel, frc=frc, t0=t0, tswitch=tsw, cell_state=cs)
 
     def compute_forces(self) -> np.ndarray:
         self.L.ora_compute_forces(self.h)

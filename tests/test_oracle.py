@@ -130,6 +130,66 @@ def test_fene_bond_known_answers(oracle_lib, sep, cil):
     np.testing.assert_allclose(f[0, 1], 1.0 * nij + 2.0 * spring * rij, rtol=1e-14, atol=1e-15)
 
 
+def cell_machine_params(**kw):
+    """Two-element cells with the reference's bond and its crawling/dividing states; spans exact
+    (sigma 0): division 30 steps, migration 50."""
+    p = small_params(noise_D=0.0, motility=[0.0, 1.0], intra_law=1, cil=1, fene_kappa=0.2, fene_kappa_push=0.5,
+                     fene_spring_ratio=0.5, fene_rmax=1.2, fene_rmax_division=1.6, divide=1, dt=1e-3,
+                     div_tau_mu=0.03, div_tau_sigma=0.0, mig_tau_mu=0.05, mig_tau_sigma=0.0,
+                     growth_k0=[0.0, 0.0], growth_k1=[1.0, 1.0], growth_k2=[0.0, 0.0], div_r0=0.25,
+                     div_rmin=1.05, sigma_core=[1.0, 0.9])
+    p.update(kw)
+    return p
+
+
+def test_cell_state_machine_transitions(oracle_lib):
+    """calculDivisions (CIL.cu:369-455) for the reference's two-element cells, worked by hand on
+    three isolated cells after one step: a crawling cell whose time ends starts dividing
+    (time += 30); a dividing cell whose elements are Rmin apart divides (a daughter appended,
+    both crawling, both born now, the daughter's time now + 50 and the mother's own + 50, the
+    elements 2 R0 apart, the diameters reset to SIGMA_CORE); a dividing cell short of Rmin whose
+    time ends fails (crawling, time += 50, elements 2 R0 apart)."""
+    p = cell_machine_params()
+    o = make(oracle_lib, p)
+    pos = np.array([[[3.0, 3.0], [3.9, 3.0]],     # crawling, time ends
+                    [[10.0, 10.0], [11.3, 10.0]],  # dividing, 1.3 apart
+                    [[16.0, 16.0], [16.9, 16.0]]])  # dividing, 0.9 apart, time ends
+    sig = np.array([[1.0, 1.0], [1.1, 1.0], [1.0, 1.0]])
+    o.set_state(pos, sig, np.zeros(3, np.int32), np.array([1, 500, 1], np.int32), cell_state=[1, 0, 0])
+    assert o.step(1) == 0
+    s = o.state()
+    assert o.ncells == 4
+    np.testing.assert_array_equal(s["cell_state"], [0, 1, 1, 1])
+    np.testing.assert_array_equal(s["tswitch"], [1 + 30, 500 + 50, 1 + 50, 1 + 50])
+    np.testing.assert_array_equal(s["t0"], [0, 1, 0, 1])
+    for c in (1, 2, 3):
+        d = s["pos"][c, 1] - s["pos"][c, 0]
+        assert np.sqrt(d @ d) == pytest.approx(0.5, abs=1e-12)
+    np.testing.assert_array_equal(s["sigma"][1], [1.0, 0.9])
+    np.testing.assert_array_equal(s["sigma"][3], [1.0, 0.9])
+    ev = o.events()
+    assert sorted(ev[:, 1].tolist()) == [0, 2, 3]
+
+
+def test_dividing_bond_known_answer(oracle_lib):
+    """binaryCellForce (MD.cu:545-567) for a dividing cell: r2max from RMAX_DIVISION, the growth
+    activity -k0 feneDivMax + k1 + k2 r^4 along rij (no rss scaling), the bond acting once."""
+    p = cell_machine_params(growth_k0=[0.3, 0.1], growth_k1=[0.2, 0.7], growth_k2=[0.05, 0.02], divide=0)
+    o = make(oracle_lib, p)
+    pos = np.array([[[5.0, 5.0], [5.0 + 0.8 * 1.1, 5.0 + 0.6 * 1.1]]])
+    o.set_state(pos, np.ones((1, 2)), np.zeros(1, np.int32), np.full(1, S.NEVER, np.int32), cell_state=[0])
+    f = o.compute_forces()
+    rij = pos[0, 1] - pos[0, 0]
+    r2 = float(rij @ rij)
+    r2max = 1.6 * 1.6
+    lim = 0.5 * r2max
+    spring = 0.5 * abs(r2 - lim) if r2 <= lim else -0.2 / (1 - ((r2 - lim) / (0.5 * r2max)) ** 2)
+    fdm = -0.2 / (1 - (1.05 * 1.05 / r2max) ** 2)
+    act = [-0.3 * fdm + 0.2 + 0.05 * r2 * r2, -0.1 * fdm + 0.7 + 0.02 * r2 * r2]
+    np.testing.assert_allclose(f[0, 0], -(act[0] * rij + spring * rij), rtol=1e-14)
+    np.testing.assert_allclose(f[0, 1], act[1] * rij + spring * rij, rtol=1e-14)
+
+
 def test_binning_formula_known_answers(oracle_lib):
     """min((int)((r * (1/L)) * Ns), Ns-1) with Ns = (int)(L / (w + 1e-8 min L)), ids
     ls0 * Ns1 + ls1 (Utils.hpp:872-876, 990, 1020-1022)."""
