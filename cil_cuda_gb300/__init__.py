@@ -83,6 +83,16 @@ class ColonyParams(C.Structure):
         ("fene_kappa_push", C.c_double),
         ("fene_spring_ratio", C.c_double),
         ("fene_rmax", C.c_double),
+        ("fene_rmax_division", C.c_double),
+        ("growth_k0", C.c_double * 2),
+        ("growth_k1", C.c_double * 2),
+        ("growth_k2", C.c_double * 2),
+        ("div_r0", C.c_double),
+        ("div_rmin", C.c_double),
+        ("div_rmin_ratio", C.c_double),
+        ("mig_tau_mu", C.c_double),
+        ("mig_tau_sigma", C.c_double),
+        ("sigma_core", C.c_double * 2),
     ]
 
 
@@ -117,6 +127,7 @@ class ColonyView(C.Structure):
         ("vel", C.POINTER(C.c_double)),
         ("t0", C.POINTER(C.c_int32)),
         ("tswitch", C.POINTER(C.c_int32)),
+        ("cell_state", C.POINTER(C.c_int32)),
     ]
 
 
@@ -582,13 +593,15 @@ class Engine:
         except Exception:
             pass
 
-    def upload(self, colony: int, pos, sigma, t0, tswitch, ts: int = 0):
+    def upload(self, colony: int, pos, sigma, t0, tswitch, ts: int = 0, cell_state=None):
         pos = np.ascontiguousarray(pos, np.float64)
         sigma = np.ascontiguousarray(sigma, np.float64)
         t0 = np.ascontiguousarray(t0, np.int32)
         tswitch = np.ascontiguousarray(tswitch, np.int32)
+        cs = None if cell_state is None else np.ascontiguousarray(cell_state, np.int32)
         v = ColonyView(ncells=sigma.shape[0], capacity=sigma.shape[0], ts=ts, pad=0, pos=_dp(pos),
-                       sigma=_dp(sigma), vel=None, t0=_ip(t0), tswitch=_ip(tswitch))
+                       sigma=_dp(sigma), vel=None, t0=_ip(t0), tswitch=_ip(tswitch),
+                       cell_state=_ip(cs) if cs is not None else None)
         self._check(self.L.cil_upload(self.h, colony, C.byref(v)))
 
     def step(self, n: int = 1) -> int:
@@ -612,7 +625,7 @@ class Engine:
         start = start[: nb + 1].copy()
         return ns, start, elems[: start[-1]].copy()
 
-    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch"), strict: bool = True,
+    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch", "cell_state"), strict: bool = True,
                  out: dict = None) -> dict:
         """The colony's state. strict=False keeps the state that a failed step left (its status
         under "status") instead of raising. out: caller-owned C-contiguous arrays to fill
@@ -626,8 +639,10 @@ class Engine:
             vel = np.zeros((cap, 2, D))
             t0 = np.zeros(cap, np.int32)
             tsw = np.zeros(cap, np.int32)
+            cst = np.zeros(cap, np.int32) if "cell_state" in want else None
         else:
             pos, sig, t0, tsw, vel = out["pos"], out["sigma"], out["t0"], out["tswitch"], out.get("vel")
+            cst = out.get("cell_state")
             cap = len(pos)
             for a, dt in ((pos, np.float64), (sig, np.float64), (t0, np.int32), (tsw, np.int32)) + \
                     (((vel, np.float64),) if vel is not None else ()):
@@ -636,13 +651,14 @@ class Engine:
             if pos.shape[1:] != (2, D) or sig.shape[1:] != (2,) or (vel is not None and vel.shape[1:] != (2, D)):
                 raise ValueError("download: out arrays have the wrong shape")
         v = ColonyView(ncells=0, capacity=cap, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig),
-                       vel=_dp(vel) if vel is not None else None, t0=_ip(t0), tswitch=_ip(tsw))
+                       vel=_dp(vel) if vel is not None else None, t0=_ip(t0), tswitch=_ip(tsw),
+                       cell_state=_ip(cst) if cst is not None else None)
         st = self.L.cil_download(self.h, colony, C.byref(v))
         if strict or st not in (3, 4, 5) or v.ncells > cap:
             self._check(st)
         n = v.ncells
         res = dict(ncells=n, ts=v.ts, pos=pos[:n], sigma=sig[:n], vel=vel[:n] if vel is not None else None,
-                   t0=t0[:n], tswitch=tsw[:n])
+                   t0=t0[:n], tswitch=tsw[:n], cell_state=cst[:n] if cst is not None else None)
         res = {k: res[k] for k in res if k in want or k in ("ncells", "ts")}
         if st != 0:
             res["status"] = st

@@ -41,6 +41,7 @@ struct HostColony {
   // oracle-mode mirror
   int n = 0;
   std::vector<int> t0, tsw;
+  std::vector<int> cst;  // cell states (crawling/dividing cells)
 };
 
 }  // namespace
@@ -129,6 +130,8 @@ struct cil_handle {
   int *d_scan_sum = nullptr, *d_scan_off = nullptr, *d_scan_col = nullptr;
   int *d_slot_of = nullptr;
   int *d_t0 = nullptr, *d_tsw = nullptr;
+  int *d_cst = nullptr;     // cell states [CC] (crawling/dividing cells)
+  unsigned char *d_smflag = nullptr;  // per cell: division criterion met (oracle mode, state machine)
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
   int *d_tiles_pairs = nullptr;  // skin mode: tiles over slot pairs (the cell-major force kernel)
   int *d_tile_count = nullptr, *d_tile_off = nullptr;
@@ -408,6 +411,7 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
   a.cnt = h->d_cnt;
   a.B = h->B;
   a.SS = h->SS;
+  a.cst = h->d_cst;
   a.tiles_live = h->d_tiles_live;
   a.x_in = h->d_x[h->cur];
   a.x_out = h->d_x[1 - h->cur];
@@ -473,6 +477,8 @@ EventArgs event_args(cil_handle *h) {
   a.slot_of = h->d_slot_of;
   a.t0 = h->d_t0;
   a.tsw = h->d_tsw;
+  a.cst = h->d_cst;
+  a.smflag = h->d_smflag;
   a.tile_count = h->d_tile_count;
   a.tile_off = h->d_tile_off;
   a.dueq = h->d_dueq;
@@ -578,8 +584,65 @@ cil_status oracle_events(cil_handle *h) {
     const int D = h->D;
     std::vector<int> mothers, tsws;
     std::vector<double> dirs;
+    std::vector<int> smops;      // crawling/dividing cells: cell, kind (1 start, 2 failed), new time
+    std::vector<double> smdirs;  // the failed divisions' axes
     const int n0 = hc.n;
-    if (hc.p.divide) {
+    const bool sm = hc.p.divide && hc.p.intra_law == CIL_INTRA_FENE;
+    if (sm) {
+      // calculDivisions (CIL.cu:369-455) on the host mirror, in cell order; which dividing
+      // cells have their elements Rmin apart is read from the device (this step's positions)
+      std::vector<unsigned char> flags(static_cast<size_t>(n0));
+      if (n0 > 0) {
+        launch_sm_flags(event_args(h), c, n0, D, h->stream);
+        CUDA_TRY(h, cudaMemcpyAsync(flags.data(), h->d_smflag + h->cc[c].cell_base, static_cast<size_t>(n0),
+                                    cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        h->launches += 1;
+      }
+      auto span = [&](double mu, double sd) {
+        const int s = nint(h->rng.normal(mu, sd) / hc.p.dt);
+        return s >= 1 ? s : 1;
+      };
+      for (int i = 0; i < n0; ++i) {
+        if (hc.cst[i] == 0) {  // dividing
+          if (flags[i]) {
+            if (hc.n >= hc.cap) {
+              cap_hit = c;
+              continue;
+            }
+            const int k = hc.n++;
+            double dm[3] = {0, 0, 0}, dd[3] = {0, 0, 0};
+            h->rng.on_dsphere(D, dm);
+            h->rng.on_dsphere(D, dd);
+            const int td = ts + span(hc.p.mig_tau_mu, hc.p.mig_tau_sigma);
+            const int tm = hc.tsw[i] + span(hc.p.mig_tau_mu, hc.p.mig_tau_sigma);
+            hc.t0[k] = ts;
+            hc.tsw[k] = td;
+            hc.cst[k] = 1;
+            hc.t0[i] = ts;
+            hc.tsw[i] = tm;
+            hc.cst[i] = 1;
+            mothers.push_back(i);
+            tsws.push_back(td);
+            tsws.push_back(tm);
+            for (int d = 0; d < D; ++d) dirs.push_back(dm[d]);
+            for (int d = 0; d < D; ++d) dirs.push_back(dd[d]);
+          } else if (hc.tsw[i] == ts) {  // failed division
+            double df[3] = {0, 0, 0};
+            h->rng.on_dsphere(D, df);
+            hc.tsw[i] += span(hc.p.mig_tau_mu, hc.p.mig_tau_sigma);
+            hc.cst[i] = 1;
+            smops.insert(smops.end(), {i, 2, hc.tsw[i]});
+            for (int d = 0; d < D; ++d) smdirs.push_back(df[d]);
+          }
+        } else if (hc.tsw[i] == ts) {  // starts dividing
+          hc.tsw[i] += span(hc.p.div_tau_mu, hc.p.div_tau_sigma);
+          hc.cst[i] = 0;
+          smops.insert(smops.end(), {i, 1, hc.tsw[i]});
+          for (int d = 0; d < D; ++d) smdirs.push_back(0.0);
+        }
+      }
+    } else if (hc.p.divide) {
       for (int i = 0; i < n0; ++i) {
         if (hc.tsw[i] != ts) continue;
         if (hc.n >= hc.cap) {  // skipped, as the oracle does, and reported after the step
@@ -616,6 +679,7 @@ cil_status oracle_events(cil_handle *h) {
           const int last = hc.n - 1;
           hc.t0[i] = hc.t0[last];
           hc.tsw[i] = hc.tsw[last];
+          if (sm) hc.cst[i] = hc.cst[last];
           hc.n -= 1;
           ops.push_back(i);
         } else {
@@ -624,23 +688,28 @@ cil_status oracle_events(cil_handle *h) {
       }
     }
     const int ndiv = static_cast<int>(mothers.size());
-    if (ndiv == 0 && ops.empty()) continue;
-    const size_t ni = mothers.size() + tsws.size() + ops.size();
-    cil_status st = ensure_oracle_buffers(h, ni, dirs.size());
+    const int nsm = static_cast<int>(smops.size() / 3);
+    if (ndiv == 0 && ops.empty() && nsm == 0) continue;
+    const size_t ni = mothers.size() + tsws.size() + ops.size() + smops.size();
+    cil_status st = ensure_oracle_buffers(h, ni, dirs.size() + smdirs.size());
     if (st != CIL_OK) return st;
     std::vector<int> packed;
     packed.insert(packed.end(), mothers.begin(), mothers.end());
     packed.insert(packed.end(), tsws.begin(), tsws.end());
     packed.insert(packed.end(), ops.begin(), ops.end());
+    packed.insert(packed.end(), smops.begin(), smops.end());
+    dirs.insert(dirs.end(), smdirs.begin(), smdirs.end());
     CUDA_TRY(h, cudaMemcpyAsync(h->d_oracle_i, packed.data(), sizeof(int) * packed.size(), cudaMemcpyHostToDevice, h->stream));
     if (!dirs.empty())
       CUDA_TRY(h, cudaMemcpyAsync(h->d_oracle_d, dirs.data(), sizeof(double) * dirs.size(), cudaMemcpyHostToDevice, h->stream));
     // the staged host vectors must stay alive until the copies ran
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     EventArgs a = event_args(h);
+    launch_sm_ops(a, c, nsm, h->d_oracle_i + 3 * ndiv + ops.size(), h->d_oracle_d + static_cast<size_t>(ndiv) * 2 * D,
+                  D, h->stream);
     launch_divisions_list(a, c, n0, ndiv, h->d_oracle_i, h->d_oracle_d, h->d_oracle_i + ndiv, D, h->stream);
     launch_apo_ops_with_div(a, c, ndiv, static_cast<int>(ops.size()), h->d_oracle_i + 3 * ndiv, D, h->stream);
-    h->launches += (ndiv > 0 ? 1 : 0) + 1;
+    h->launches += (ndiv > 0 ? 1 : 0) + (nsm > 0 ? 1 : 0) + 1;
   }
   if (cap_hit >= 0) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(cap_hit));
   return CIL_OK;
@@ -1039,8 +1108,14 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
         (p.force_law == CIL_FORCE_SC && (!(p.well_sigma > 0.0) || !(p.well_epsilon >= 0.0))) ||
         (p.intra_law != CIL_INTRA_SPRING && p.intra_law != CIL_INTRA_FENE) ||
         (p.intra_law == CIL_INTRA_FENE &&
-         (p.divide || !(p.fene_rmax > 0.0) || !(p.fene_spring_ratio >= 0.0 && p.fene_spring_ratio < 1.0) ||
-          !(p.fene_kappa >= 0.0) || !(p.fene_kappa_push >= 0.0) || (!p.cil && !(fene_rss(p) > 0.0))))) {
+         (!(p.fene_rmax > 0.0) || !(p.fene_spring_ratio >= 0.0 && p.fene_spring_ratio < 1.0) ||
+          !(p.fene_kappa >= 0.0) || !(p.fene_kappa_push >= 0.0) || (!p.cil && !(fene_rss(p) > 0.0)))) ||
+        // the crawling/dividing cells: oracle-mode draws (their outcomes are read back each step),
+        // bins rebuilt every step (no Verlet skin), positive spans and radius
+        (p.intra_law == CIL_INTRA_FENE && p.divide &&
+         (cfg->rng_mode != CIL_RNG_DSFMT || cfg->skin > 0.0 || !(p.dt > 0.0) || !(p.div_r0 >= 0.0) ||
+          !(p.div_rmin >= 0.0) || !(p.mig_tau_mu > 0.0) || !(p.mig_tau_sigma >= 0.0) ||
+          !(p.sigma_core[0] > 0.0) || !(p.sigma_core[1] > 0.0) || !(p.fene_rmax_division >= 0.0)))) {
       delete h;
       return CIL_ERR_CONFIG;
     }
@@ -1103,6 +1178,22 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.fene_ratio_f = static_cast<float>(C.fene_ratio);
     C.fene_r2max_f = static_cast<float>(C.fene_r2max);
     C.fene_rss_f = static_cast<float>(C.fene_rss);
+    C.cell_sm = C.intra_fene && p.divide ? 1 : 0;
+    C.fene_r2max_div = p.fene_rmax_division > 0.0 ? p.fene_rmax_division * p.fene_rmax_division : C.fene_r2max;
+    C.fene_r2max_div_f = static_cast<float>(C.fene_r2max_div);
+    for (int j = 0; j < 2; ++j) {
+      C.growth_k0[j] = p.growth_k0[j];
+      C.growth_k1[j] = p.growth_k1[j];
+      C.growth_k2[j] = p.growth_k2[j];
+      C.growth_k0_f[j] = static_cast<float>(p.growth_k0[j]);
+      C.growth_k1_f[j] = static_cast<float>(p.growth_k1[j]);
+      C.growth_k2_f[j] = static_cast<float>(p.growth_k2[j]);
+      C.sigma_core[j] = p.sigma_core[j];
+    }
+    C.div_r2min = p.div_rmin * p.div_rmin;
+    C.div_r2min_f = static_cast<float>(C.div_r2min);
+    C.div_rmin_ratio = p.div_rmin_ratio;
+    C.div_radius = C.cell_sm ? p.div_r0 : 0.5 * p.rest0;
     C.noise_amp = p.noise_D > 0.0 ? std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt)) : 0.0;
     C.dt = p.dt;
     C.div_tau_mu = p.div_tau_mu;
@@ -1216,6 +1307,8 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_slot_of = dalloc<int>(2 * static_cast<size_t>(h->CC));
   h->d_t0 = dalloc<int>(h->CC);
   h->d_tsw = dalloc<int>(h->CC);
+  h->d_cst = dalloc<int>(h->CC);
+  h->d_smflag = dalloc<unsigned char>(h->CC);
   h->d_tiles_used = dalloc<int>(h->B + 1);
   h->d_tiles_live = dalloc<int>(h->B + 1);
   h->d_tiles_cell = dalloc<int>(h->B + 1);
@@ -1237,7 +1330,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
   h->d_divq = dalloc<int>(static_cast<size_t>(h->CC));
   bool ok = h->d_col && h->d_cnt && h->d_x[0] && h->d_x[1] && h->d_eid[0] && h->d_eid[1] && h->d_sbin[0] &&
             h->d_sbin[1] && h->d_cyc[0] && h->d_cyc[1] && h->d_sigma_c && h->d_vel && h->d_key && h->d_perm &&
-            h->d_slot_of && h->d_t0 && h->d_tsw && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
+            h->d_slot_of && h->d_t0 && h->d_tsw && h->d_cst && h->d_smflag && h->d_tiles_used && h->d_tiles_live && h->d_tiles_cell &&
             h->d_tiles_pairs &&
             h->d_tile_count && h->d_tile_off && h->d_upchk && h->d_evdone && h->d_dead && h->d_divq && h->d_ts &&
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
@@ -1364,6 +1457,18 @@ cil_status cil_upload(cil_handle *h, int32_t colony, const cil_colony_view *v) {
     hc.tsw.assign(v->tswitch, v->tswitch + n);
     hc.t0.resize(hc.cap);
     hc.tsw.resize(hc.cap);
+    if (v->cell_state)
+      hc.cst.assign(v->cell_state, v->cell_state + n);
+    else
+      hc.cst.assign(n, 2);
+    hc.cst.resize(hc.cap, 2);
+  }
+  // cell states: given, or every cell undefined (CellState::Undefined, Colony.cpp:248)
+  if (v->cell_state) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_cst + C.cell_base, v->cell_state, sizeof(int) * n, cudaMemcpyHostToDevice,
+                                h->stream));
+  } else if (n > 0) {
+    launch_fill_int(h->d_cst + C.cell_base, n, 2, h->stream);
   }
   h->ts = v->ts;
   const int tsi = static_cast<int>(v->ts);
@@ -1548,6 +1653,8 @@ cil_status cil_download(cil_handle *h, int32_t colony, cil_colony_view *v) {
   if (v->vel) CUDA_TRY(h, cudaMemcpyAsync(v->vel, sv, sizeof(double) * 2 * n * D, cudaMemcpyDeviceToHost, h->stream));
   if (v->t0) CUDA_TRY(h, cudaMemcpyAsync(v->t0, h->d_t0 + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
   if (v->tswitch) CUDA_TRY(h, cudaMemcpyAsync(v->tswitch, h->d_tsw + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  if (v->cell_state)
+    CUDA_TRY(h, cudaMemcpyAsync(v->cell_state, h->d_cst + C.cell_base, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   return st;
 }

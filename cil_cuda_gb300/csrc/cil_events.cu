@@ -86,7 +86,7 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
     xb[d] = a.x[d * SS + sb];
     xf[d] = a.x[d * SS + sf];
   }
-  const double sgb = a.sigma_c[2 * g], sgf = a.sigma_c[2 * g + 1];
+  double sgb = a.sigma_c[2 * g], sgf = a.sigma_c[2 * g + 1];
   double sigb = 0.0, sigf = 0.0;
   if (a.sig) {
     sigb = a.sig[sb];
@@ -96,6 +96,12 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
   if (a.pk) {
     wb = fabsf(a.pk[sb].w);
     wf = fabsf(a.pk[sf].w);
+  }
+  if (C.cell_sm) {  // crawling/dividing cells: both cells' diameters return to SIGMA_CORE (CIL.cu:408, 427)
+    sgb = sigb = C.sigma_core[0];
+    sgf = sigf = C.sigma_core[1];
+    wb = static_cast<float>(sgb);
+    wf = static_cast<float>(sgf);
   }
   const bool skin = a.state != nullptr;
   bool was_fresh_b = false, was_fresh_f = false;
@@ -113,7 +119,7 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
     }
   }
   // ---- placement (FP64), bins and records
-  const double radius = 0.5 * C.rest0;
+  const double radius = C.div_radius;  // half the birth rest length, or the reference's R0
   double xs[4][D];
   place<D>(C, xf, dir_m, radius, xs[1], xs[0]);  // mother: master = front element
   place<D>(C, xb, dir_d, radius, xs[2], xs[3]);  // daughter: master = back element
@@ -186,6 +192,16 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
   if (a.sig) {
     a.sig[s0] = sigb;
     a.sig[s0 + 1] = sigf;
+  }
+  if (C.cell_sm) {  // the mother's reset diameters; both cells crawl
+    a.sigma_c[2 * g] = sgb;
+    a.sigma_c[2 * g + 1] = sgf;
+    if (a.sig) {
+      a.sig[sb] = sigb;
+      a.sig[sf] = sigf;
+    }
+    a.cst[g] = kCellCrawling;
+    a.cst[gk] = kCellCrawling;
   }
   a.eid[s0] = 2 * gk;
   a.eid[s0 + 1] = 2 * gk + 1;
@@ -328,6 +344,7 @@ __device__ void move_cell(const EventArgs &a, const ColonyConst &C, int dst, int
   const int gd = C.cell_base + dst, gs = C.cell_base + src;
   a.t0[gd] = a.t0[gs];
   a.tsw[gd] = a.tsw[gs];
+  a.cst[gd] = a.cst[gs];
   a.sigma_c[2 * gd] = a.sigma_c[2 * gs];
   a.sigma_c[2 * gd + 1] = a.sigma_c[2 * gs + 1];
   for (int j = 0; j < 2; ++j) {
@@ -999,6 +1016,108 @@ void launch_events_due(const EventArgs &a, int dim, cudaStream_t s) {
     k_events_due<2><<<a.B, kTile, 0, s>>>(a);
   else
     k_events_due<3><<<a.B, kTile, 0, s>>>(a);
+}
+
+// The crawling/dividing cells, oracle mode: per cell of the colony, whether a dividing cell's
+// elements are far enough apart to divide (binaryCellDivisionCriteria, MD.cuh:426-433; the
+// squared separation of BoundingBox::distance, Utils.hpp:536-544, without fused arithmetic, as
+// the restatement computes it). The host reads the flags and decides the step's events.
+template <int D>
+__global__ void k_sm_flags(EventArgs a, int c, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ColonyConst &C = a.col[c];
+  const int g = C.cell_base + i;
+  unsigned char f = 0;
+  if (a.cst[g] == kCellDividing) {
+    const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+    double r2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double v = __dsub_rn(a.x[d * a.SS + s0], a.x[d * a.SS + s1]);  // r0 - r1
+      if (C.periodic[d]) v = __dsub_rn(v, __dmul_rn(static_cast<double>(nint(v / C.box[d])), C.box[d]));
+      r2 = __dadd_rn(r2, __dmul_rn(v, v));
+    }
+    const bool ok = C.div_rmin_ratio != 0.0 ? r2 >= __dmul_rn(C.div_rmin_ratio, a.sigma_c[2 * g]) : r2 >= C.div_r2min;
+    f = ok ? 1 : 0;
+  }
+  a.smflag[g] = f;
+}
+
+// The crawling/dividing cells, oracle mode: the step's non-dividing transitions in the host's
+// order, ops[3 r] = cell, kind, new time; kind 1: the cell starts dividing; kind 2: a failed
+// division (binaryCellDivisionFail, MD.cu:736-752: the back element moved half the bond
+// towards the front, a plain add, then both reoriented about it at R0 along dirs[r]), the cell
+// crawls again with its diameters reset. Velocities of the cell are zeroed (CIL.cu:432, 444).
+template <int D>
+__global__ void k_sm_ops(EventArgs a, int c, int nops, const int *ops, const double *dirs) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nops) return;
+  const ColonyConst &C = a.col[c];
+  const int i = ops[3 * r], kind = ops[3 * r + 1], tsw_new = ops[3 * r + 2];
+  const int g = C.cell_base + i;
+  const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+  const size_t SS = a.SS;
+  if (kind == 2) {
+    double x0[D], x1[D], m[D], sl[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      x0[d] = a.x[d * SS + s0];
+      x1[d] = a.x[d * SS + s1];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double v = __dsub_rn(x1[d], x0[d]);  // r1 - r0
+      if (C.periodic[d]) v = __dsub_rn(v, __dmul_rn(static_cast<double>(nint(v / C.box[d])), C.box[d]));
+      x0[d] = __dadd_rn(x0[d], __dmul_rn(v, 0.5));
+    }
+    place<D>(C, x0, dirs + static_cast<size_t>(r) * D, C.div_radius, m, sl);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      a.x[d * SS + s0] = m[d];
+      a.x[d * SS + s1] = sl[d];
+    }
+    a.sigma_c[2 * g] = C.sigma_core[0];
+    a.sigma_c[2 * g + 1] = C.sigma_core[1];
+    if (a.sig) {
+      a.sig[s0] = C.sigma_core[0];
+      a.sig[s1] = C.sigma_core[1];
+    }
+    a.cst[g] = kCellCrawling;
+  } else {
+    a.cst[g] = kCellDividing;
+  }
+  a.tsw[g] = tsw_new;
+  if (a.vel) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) a.vel[d * SS + s0] = a.vel[d * SS + s1] = 0.0;
+  }
+}
+
+__global__ void k_fill_int(int *dst, int n, int value) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = value;
+}
+
+void launch_fill_int(int *dst, int n, int value, cudaStream_t s) {
+  if (n > 0) k_fill_int<<<(n + 255) / 256, 256, 0, s>>>(dst, n, value);
+}
+
+void launch_sm_flags(const EventArgs &a, int colony, int n, int dim, cudaStream_t s) {
+  if (n <= 0) return;
+  if (dim == 2)
+    k_sm_flags<2><<<(n + 255) / 256, 256, 0, s>>>(a, colony, n);
+  else
+    k_sm_flags<3><<<(n + 255) / 256, 256, 0, s>>>(a, colony, n);
+}
+
+void launch_sm_ops(const EventArgs &a, int colony, int nops, const int *ops, const double *dirs, int dim,
+                   cudaStream_t s) {
+  if (nops <= 0) return;
+  if (dim == 2)
+    k_sm_ops<2><<<(nops + 127) / 128, 128, 0, s>>>(a, colony, nops, ops, dirs);
+  else
+    k_sm_ops<3><<<(nops + 127) / 128, 128, 0, s>>>(a, colony, nops, ops, dirs);
 }
 
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,

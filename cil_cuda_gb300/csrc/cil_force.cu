@@ -98,6 +98,13 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
       if (r2 == 0.0) {
 #pragma unroll
         for (int d = 0; d < D; ++d) F[d] = 0.0;
+      } else if (C.cell_sm && a.cst[g] == kCellDividing) {
+        double spring, act[2];
+        fene_bond_dividing<double>(r2, fmax(si, a.sig[ps]), C.fene_r2max_div, C.fene_kappa, C.fene_kappa_push,
+                                   C.fene_ratio, C.div_r2min, C.growth_k0, C.growth_k1, C.growth_k2, spring, act);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          F[d] = (j == 0) ? -(act[0] * rij[d] + spring * rij[d] * 1.0) : act[1] * rij[d] + spring * rij[d] * 1.0;
       } else if (C.intra_fene) {
         const double r = sqrt(r2);
         double spring, sc;
@@ -305,7 +312,14 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
     }
 #pragma unroll
     for (int d = 0; d < D; ++d) F[d] = 0.0f;
-    if (r2 > 0.0f && C.intra_fene) {
+    if (r2 > 0.0f && C.cell_sm && a.cst[g] == kCellDividing) {
+      float spring, act[2];
+      fene_bond_dividing<float>(r2, fmaxf(si, fabsf(pp.w)), C.fene_r2max_div_f, C.fene_kappa_f, C.fene_kappa_push_f,
+                                C.fene_ratio_f, C.div_r2min_f, C.growth_k0_f, C.growth_k1_f, C.growth_k2_f, spring, act);
+      const float coef = (j == 0) ? -(act[0] + spring) : act[1] + spring;
+#pragma unroll
+      for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
+    } else if (r2 > 0.0f && C.intra_fene) {
       const float rinv = rsqrtf(r2);
       float spring, sc;
       fene_bond<float>(r2, r2 * rinv, fmaxf(si, fabsf(pp.w)), C.fene_r2max_f, C.fene_kappa_f, C.fene_kappa_push_f,

@@ -183,7 +183,37 @@ struct ColonyConst {
   int intra_fene, cil;
   double fene_kappa, fene_kappa_push, fene_ratio, fene_r2max, fene_rss;
   float fene_kappa_f, fene_kappa_push_f, fene_ratio_f, fene_r2max_f, fene_rss_f;
+  // the reference's crawling/dividing cells (CIL_INTRA_FENE with divide): RMAX_DIVISION^2,
+  // growth activities, Rmin^2 and its ratio form, the reorientation radius of a division
+  // (R0; half the birth rest length otherwise) and the diameters a division resets to
+  int cell_sm;
+  double fene_r2max_div, growth_k0[2], growth_k1[2], growth_k2[2], div_r2min, div_rmin_ratio;
+  float fene_r2max_div_f, growth_k0_f[2], growth_k1_f[2], growth_k2_f[2], div_r2min_f;
+  double div_radius, sigma_core[2];
 };
+
+// Cell states of the reference's two-element cells (CellState, Cell.cuh:26-30)
+constexpr int kCellDividing = 0, kCellCrawling = 1, kCellUndefined = 2;
+
+// The bond of a dividing cell (binaryCellForce, MD.cu:545-567): r2max from RMAX_DIVISION, the
+// growth activities act_j = -k0_j feneDivMax + k1_j + k2_j r^4 with feneDivMax = FENE(r2max,
+// Rmin^2), the bond acting once: F_back = -(act_0 + spring) rij, F_front = (act_1 + spring) rij.
+template <typename R>
+__device__ __forceinline__ void fene_bond_dividing(R r2, R smax, R r2max_div, R kappa, R kpush, R ratio, R r2min,
+                                                   const R *k0, const R *k1, const R *k2, R &spring, R *act) {
+  const R r2max = r2max_div > smax ? r2max_div : smax;
+  const R lim = r2max * ratio;
+  if (r2 <= lim) {
+    spring = kpush * fabs(r2 - lim);
+  } else {
+    const R q = (r2 - lim) / (r2max * (R(1) - ratio));
+    spring = -kappa / (R(1) - q * q);
+  }
+  const R qd = r2min / r2max;
+  const R fdm = -kappa / (R(1) - qd * qd);
+  act[0] = -k0[0] * fdm + k1[0] + k2[0] * (r2 * r2);
+  act[1] = -k0[1] * fdm + k1[1] + k2[1] * (r2 * r2);
+}
 
 // The reference's bond of a crawling two-element cell (binaryCellForce, MD.cu:525-598): the
 // magnitude `spring` of the bond term spring * rij * 2 (rij = r_front - r_back, strongContract
@@ -616,6 +646,7 @@ struct ForceArgs {
   ColonyCounters *cnt;
   int B;
   size_t SS;
+  const int *cst;          // cell states (the crawling/dividing cells' bond)
   const int *tiles_live;
   const double *x_in;      // sorted positions
   double *x_out;           // integrated positions (same slots)
@@ -689,6 +720,8 @@ struct EventArgs {
   int *slot_of;
   int *t0;
   int *tsw;
+  int *cst;                // cell states (crawling/dividing cells)
+  unsigned char *smflag;   // per cell: the division criterion is met (oracle mode, state machine)
   int *tile_count;
   int *tile_off;
   // skin mode, Philox: the cells due to divide, appended by the force kernel (colony c's at
@@ -829,6 +862,10 @@ void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, con
                            const double *dirs, const int *spans, int dim, cudaStream_t s);
 void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops, const int *ops, int dim,
                              cudaStream_t s);
+void launch_fill_int(int *dst, int n, int value, cudaStream_t s);
+void launch_sm_flags(const EventArgs &a, int colony, int n, int dim, cudaStream_t s);
+void launch_sm_ops(const EventArgs &a, int colony, int nops, const int *ops, const double *dirs, int dim,
+                   cudaStream_t s);
 void launch_upload(const ColonyConst *col, int colony, int ncells, int dim, size_t SS, const double *stage,
                    double *x, double *sig_c, int *t0, int *tsw, double *vel, int *eid, int *slot_of,
                    ColonyCounters *cnt, int *chk, cudaStream_t s);

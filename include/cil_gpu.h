@@ -114,6 +114,23 @@ typedef struct cil_colony_params {
   double fene_kappa_push; /* KAPPA_PUSH */
   double fene_spring_ratio; /* SPRING_RATIO, in [0, 1) */
   double fene_rmax;       /* RMAX */
+  /* CIL_INTRA_FENE with divide = 1: the reference's crawling/dividing cells (calculDivisions,
+   * CIL.cu:369-455; oracle-mode draws, FP64 or mixed, no Verlet skin). A crawling cell whose
+   * time ends starts dividing (time += N(div_tau_mu, div_tau_sigma) / dt); a dividing cell whose
+   * elements are div_rmin apart (or, with div_rmin_ratio != 0, whose r^2 reaches
+   * div_rmin_ratio x its back diameter) divides: binaryCellDivision at radius div_r0, both cells
+   * crawling, born now, the daughter's time now + N(mig_tau_mu, mig_tau_sigma) / dt and the
+   * mother's own time plus another such span, diameters reset to sigma_core; one that does
+   * not get there by its time fails (binaryCellDivisionFail: the back element to the centre,
+   * both reoriented at div_r0; crawling; time += a migration span). While dividing, the bond uses
+   * RMAX_DIVISION and the growth activity -k0 FENE(r2max, Rmin^2) + k1 + k2 r^4 (MD.cu:545-567). */
+  double fene_rmax_division; /* RMAX_DIVISION (0: RMAX) */
+  double growth_k0[2], growth_k1[2], growth_k2[2]; /* GROWTHK0/1/2 of the two elements */
+  double div_r0;          /* DIVISION.R0 */
+  double div_rmin;        /* DIVISION.Rmin */
+  double div_rmin_ratio;  /* DIVISION.Rmin_RATIO (0: Rmin decides) */
+  double mig_tau_mu, mig_tau_sigma; /* TAU_MIGRATION */
+  double sigma_core[2];   /* SIGMA_CORE of the two elements (what a division resets to) */
 } cil_colony_params;
 
 typedef struct cil_config {
@@ -187,6 +204,9 @@ typedef struct cil_colony_view {
   double *vel;      /* [cell][2][dim], download only, may be NULL */
   int32_t *t0;      /* [cell] birth step (cellT0) */
   int32_t *tswitch; /* [cell] division step (cellTSwitch) */
+  int32_t *cell_state; /* [cell] CellState (0 dividing, 1 crawling, 2 undefined); may be NULL
+                          (upload: undefined; download: not copied); used by the crawling/
+                          dividing cells of CIL_INTRA_FENE with divide */
 } cil_colony_view;
 
 /* Observables reduced on the device (per colony). */
