@@ -625,8 +625,8 @@ class Engine:
         start = start[: nb + 1].copy()
         return ns, start, elems[: start[-1]].copy()
 
-    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch", "cell_state"), strict: bool = True,
-                 out: dict = None) -> dict:
+    def download(self, colony: int = 0, want=("pos", "sigma", "vel", "t0", "tswitch", "cell_state"),
+                 strict: bool = True, out: dict = None) -> dict:
         """The colony's state. strict=False keeps the state that a failed step left (its status
         under "status") instead of raising. out: caller-owned C-contiguous arrays to fill
         (pos [cap][2][dim] and sigma [cap][2] float64, t0 and tswitch [cap] int32, vel optional;
@@ -947,10 +947,11 @@ class RunInput:
         sig = np.zeros((n, 2))
         t0 = np.zeros(n, np.int32)
         tsw = np.zeros(n, np.int32)
+        cst = np.zeros(n, np.int32)
         v = ColonyView(ncells=0, capacity=n, ts=0, pad=0, pos=_dp(pos), sigma=_dp(sig), vel=None, t0=_ip(t0),
-                       tswitch=_ip(tsw))
+                       tswitch=_ip(tsw), cell_state=_ip(cst))
         self._check(self.L.cil_input_initial_state(self.h, C.byref(v)))
-        return dict(pos=pos, sigma=sig, t0=t0, tswitch=tsw)
+        return dict(pos=pos, sigma=sig, t0=t0, tswitch=tsw, cell_state=cst)
 
     def cycle_initial_state(self) -> dict:
         """INIT and the cell status of a single-element run (cil_input_cycle_initial_state)."""

@@ -855,12 +855,33 @@ void read_all(cil_input *in) {
     p.rest1 = spring.has("REST1") ? spring.num("REST1") : p.rest0;
   } else {
     // the reference's own bond (binaryCellForce, MD.cu:525-598) from the species' FENE block
-    // (Input.cpp:115-136) and its CIL flag (Input.cpp:22), for cells that do not divide
-    if (in->divide)
-      key_error("GPU.SPRING", "dividing two-element cells run the reference's crawling/dividing state machine "
-                              "(CIL.cu:369-455), which the GPU step does not model; set GPU.SPRING {KAPPA, REST0, "
-                              "REST1} for the linear spring with growth");
+    // (Input.cpp:115-136) and its CIL flag (Input.cpp:22); dividing cells run the reference's
+    // crawling/dividing states (calculDivisions, CIL.cu:369-455) with the DIVISION block's R0,
+    // Rmin, Rmin_RATIO and TAU_MIGRATION, the species' GROWTHK0/1/2 (Input.cpp:36-38, 153-243)
     Node fene = loc.child("FENE");
+    if (in->divide) {
+      Node dv = loc.child("DIVISION");
+      p.div_r0 = dv.num("R0");
+      p.div_rmin = dv.num("Rmin");
+      p.div_rmin_ratio = dv.num("Rmin_RATIO");
+      p.mig_tau_mu = in->tau_mig[0];
+      p.mig_tau_sigma = in->tau_mig[1];
+      const auto k0 = loc.nums("GROWTHK0", 2), k1 = loc.nums("GROWTHK1", 2), k2 = loc.nums("GROWTHK2", 2);
+      for (int j = 0; j < 2; ++j) {
+        p.growth_k0[j] = k0[j];
+        p.growth_k1[j] = k1[j];
+        p.growth_k2[j] = k2[j];
+        p.sigma_core[j] = in->sigma[j];
+      }
+      p.fene_rmax_division = fene.has("RMAX_DIVISION") ? fene.nums("RMAX_DIVISION", 1)[0] : 0.0;
+      if (dv.has("SWELLING") && dv.boolean("SWELLING"))
+        key_error(dv.path + ".SWELLING", "swelling of dividing cells is not modelled by the GPU step");
+      // the outcomes of the divisions are read back each step to draw the reference's stream
+      cfg.rng_mode = CIL_RNG_DSFMT;
+      cfg.skin = 0.0;
+      if (has_gpu && gpu.has("RNG") && gpu.pick("RNG", {"PHILOX", "DSFMT"}) != "DSFMT")
+        key_error("GPU.RNG", "dividing two-element cells with the reference's bond run with the reference's draws (DSFMT)");
+    }
     p.intra_law = CIL_INTRA_FENE;
     p.cil = loc.boolean("CIL") ? 1 : 0;
     p.fene_kappa = fene.nums("KAPPA_PULL", 1)[0];
@@ -1000,13 +1021,23 @@ cil_status cil_input_initial_state(const cil_input *in, cil_colony_view *v) {
     v->sigma[2 * i] = in->sigma[0];
     v->sigma[2 * i + 1] = in->sigma[1];
   }
+  // cell states: what INIT read, else undefined (Colony.cpp:248); a dividing species turns an
+  // undefined cell crawling or dividing with its time span (CIL.cuh:279-290)
+  if (v->cell_state)
+    for (int i = 0; i < n; ++i)
+      v->cell_state[i] = static_cast<size_t>(i) < in->h5_state.size() ? in->h5_state[i] : 2;
   if (in->divide) {
     const double p_mig = in->tau_mig[0] / (in->tau_mig[0] + in->tau_div[0]);
     for (int i = 0; i < n; ++i) {
       int span;
+      bool crawl = true;
       if (in->const_force) span = time_span(rng, in->tau_mig, in->dt);
       else if (rng.uniform0x(1.0) <= p_mig) span = time_span(rng, in->tau_mig, in->dt);
-      else span = time_span(rng, in->tau_div, in->dt);
+      else {
+        span = time_span(rng, in->tau_div, in->dt);
+        crawl = false;
+      }
+      if (v->cell_state && v->cell_state[i] == 2) v->cell_state[i] = crawl ? 1 : 0;
       (void)rng.uniform0x(1);  // theta, the cycle phase of the single-element model
       span -= nint(rng.uniform0x(static_cast<double>(span))) - 1;
       v->tswitch[i] = v->t0[i] + span;

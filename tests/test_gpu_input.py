@@ -26,11 +26,24 @@ def sc_document():
     return json.dumps(d)
 
 
-@pytest.mark.parametrize("law", ["softcore", "sc"])
+def machine_document():
+    """The fixture's dividing cells with the reference's own bond and crawling/dividing states (no
+    GPU.SPRING): R0, Rmin and the growth activities added, as the reference requires them."""
+    d = json.load(open(FIXTURE))
+    del d["GPU"]["SPRING"]
+    del d["GPU"]["RNG"]
+    d["SPECIES"]["A"]["DIVISION"].update(R0=0.25, Rmin=1.05, Rmin_RATIO=0.0, SWELLING=False)
+    d["SPECIES"]["A"].update(GROWTHK0=[0.0, 0.0], GROWTHK1=[1.0, 1.0], GROWTHK2=[0.0, 0.0])
+    d["SPECIES"]["A"]["FENE"]["RMAX_DIVISION"] = [1.6]
+    return json.dumps(d)
+
+
+@pytest.mark.parametrize("law", ["softcore", "sc", "machine"])
 def test_run_from_json_matches_oracle(gpu_lib, oracle_lib, law):
     G = gpu_lib
-    r = G.RunInput(FIXTURE) if law == "softcore" else G.RunInput(sc_document(), is_path=False)
-    assert r.params["force_law"] == (G.FORCE_SOFTCORE if law == "softcore" else G.FORCE_SC)
+    docs = {"softcore": None, "sc": sc_document, "machine": machine_document}
+    r = G.RunInput(FIXTURE) if law == "softcore" else G.RunInput(docs[law](), is_path=False)
+    assert r.params["force_law"] == (G.FORCE_SC if law == "sc" else G.FORCE_SOFTCORE)
     st = r.initial_state()
     eng = r.engine()
     eng.upload(0, **st)
@@ -44,6 +57,8 @@ def test_run_from_json_matches_oracle(gpu_lib, oracle_lib, law):
     s = o.state()
     assert g["ncells"] == len(s["sigma"]) and (law == "sc" or g["ncells"] != r.run["ncells"])
     np.testing.assert_array_equal(g["tswitch"], s["tswitch"])
+    if law == "machine":
+        np.testing.assert_array_equal(g["cell_state"], s["cell_state"])
     d = g["pos"] - s["pos"]
     d -= np.round(d / 60.0) * 60.0
     assert np.abs(d).max() <= 1e-9

@@ -129,7 +129,7 @@ def test_random_init_3d_out_of_bounds_is_refused(G):
     (lambda d: d["SPECIES"]["A"].update(NELEM=3), "SPECIES.A.NELEM"),
     (lambda d: d["SPECIES"]["A"].update(NELEM=1), "SPECIES.A.NAMES : vector should be of size 1"),
     (lambda d: d["SPECIES"]["A"].pop("MOTILITY"), "SPECIES.A.MOTILITY : key not found"),
-    (lambda d: d["GPU"].pop("SPRING"), "GPU.SPRING"),
+    (lambda d: d["GPU"].pop("SPRING"), "SPECIES.A.DIVISION.R0 : key not found"),
     (lambda d: (d["GPU"].pop("FORCE_LAW"), d["INTERACTIONS"]["PAIRFORCES"].update(SELECT="HZ"),
                 d["SPECIES"]["A"]["PAIRFORCES"].update(HZ={"SIGMA_CORE": [1.0, 0.9]})),
      "GPU.FORCE_LAW : the reference's two-element HZ force is zero for every pair"),
@@ -216,11 +216,44 @@ def test_fene_bond_is_read_without_division(G):
     with pytest.raises(G.CilError) as e:
         load(G, d)
     assert "SPECIES.A.FENE.SPRING_RATIO" in str(e.value)
+
+
+
+def machine_doc():
     d = copy.deepcopy(doc())
     del d["GPU"]["SPRING"]
-    with pytest.raises(G.CilError) as e:  # dividing: the state machine is not modelled
+    del d["GPU"]["RNG"]
+    d["SPECIES"]["A"]["DIVISION"].update(R0=0.25, Rmin=1.05, Rmin_RATIO=0.0, SWELLING=False)
+    d["SPECIES"]["A"].update(GROWTHK0=[0.0, 0.1], GROWTHK1=[1.0, 0.9], GROWTHK2=[0.0, 0.01])
+    d["SPECIES"]["A"]["FENE"]["RMAX_DIVISION"] = [1.6]
+    return d
+
+
+def test_dividing_cells_with_the_reference_bond_are_read(G):
+    """Dividing cells without GPU.SPRING: the reference's crawling/dividing cells with the DIVISION
+    block's R0, Rmin, Rmin_RATIO, TAU_MIGRATION, the species' GROWTHK0/1/2 and RMAX_DIVISION
+    (Input.cpp:36-38, 153-243), drawn with the reference's stream and without a Verlet skin; the
+    initial states follow initializeCellStatus (CIL.cuh:279-290)."""
+    r = load(G, machine_doc())
+    p, c = r.params, r.config
+    assert p["intra_law"] == G.INTRA_FENE and p["divide"] == 1
+    assert (p["div_r0"], p["div_rmin"], p["div_rmin_ratio"], p["fene_rmax_division"]) == (0.25, 1.05, 0.0, 1.6)
+    assert (p["mig_tau_mu"], p["mig_tau_sigma"]) == (0.08, 0.01)
+    assert list(p["growth_k0"]) == [0.0, 0.1] and list(p["growth_k1"]) == [1.0, 0.9]
+    assert list(p["growth_k2"]) == [0.0, 0.01] and list(p["sigma_core"]) == [1.0, 0.9]
+    assert c["rng_mode"] == G.RNG_DSFMT and c["skin"] == 0.0
+    st = r.initial_state()
+    assert set(np.unique(st["cell_state"]).tolist()) == {0, 1}
+    d = machine_doc()
+    d["GPU"]["RNG"] = "PHILOX"
+    with pytest.raises(G.CilError) as e:
         load(G, d)
-    assert "GPU.SPRING" in str(e.value) and "state machine" in str(e.value)
+    assert "GPU.RNG" in str(e.value)
+    d = machine_doc()
+    d["SPECIES"]["A"]["DIVISION"]["SWELLING"] = True
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "SWELLING" in str(e.value)
 
 
 def sc_doc():
