@@ -272,13 +272,14 @@ int main(int argc, char **argv) {
     if (gts_arg > 0) run.gts = gts_arg;
     const int D = cfg.dim, cap = run.capacity > run.ncells ? run.capacity : run.ncells;
     std::vector<double> pos(static_cast<size_t>(cap) * 2 * D), sig(static_cast<size_t>(cap) * 2);
-    std::vector<int> t0(cap), tsw(cap);
+    std::vector<int> t0(cap), tsw(cap), cst(cap, 2);
     cil_colony_view v{};
     v.capacity = cap;
     v.pos = pos.data();
     v.sigma = sig.data();
     v.t0 = t0.data();
     v.tswitch = tsw.data();
+    v.cell_state = cst.data();  // initializeCellStatus's states (the crawling/dividing cells use them)
     check(cil_input_initial_state(in, &v), "INIT", nullptr, in);
     int32_t capacity = cap;
     check(cil_create(&cfg, &p, &capacity, &h), "cil_create");
@@ -300,7 +301,7 @@ int main(int argc, char **argv) {
                               double cpu) {
       std::vector<double> p5(static_cast<size_t>(cap) * 2 * D), s5(static_cast<size_t>(cap) * 2), v5(p5.size()),
           f5f(p5.size());
-      std::vector<int> t05(cap), tw5(cap);
+      std::vector<int> t05(cap), tw5(cap), cs5(cap, 0);
       cil_colony_view w5{};
       w5.capacity = cap;
       w5.pos = p5.data();
@@ -308,11 +309,12 @@ int main(int argc, char **argv) {
       w5.vel = v5.data();
       w5.t0 = t05.data();
       w5.tswitch = tw5.data();
+      w5.cell_state = cs5.data();
       check(cil_download(hh, 0, &w5), "cil_download", hh);
       check(cil_forces(hh, 0, f5f.data()), "cil_forces", hh);
       const int n5 = w5.ncells;
       std::vector<double> rho(n5, 1.0);  // initializeCellStatus's activity, which the step never changes
-      std::vector<int32_t> state(n5, 0);
+      std::vector<int32_t> state(cs5.begin(), cs5.begin() + n5);  // the cells' states
       cil_h5_state st5{};
       st5.ncells = n5;
       st5.nelem = 2;

@@ -199,10 +199,11 @@ def test_runner_final_state_h5_and_restart(gpu_lib, tmp_path, integrator):
     np.testing.assert_array_equal(g.read(0, "particles/diameter"), f.read(0, "particles/diameter"))
 
 
-def test_runner_two_element_final_state_h5(gpu_lib, tmp_path):
+@pytest.mark.parametrize("model", ["spring", "machine"])
+def test_runner_two_element_final_state_h5(gpu_lib, tmp_path, model):
     G = gpu_lib
     from cil_cuda_gb300 import build
-    doc = json.load(open(FIXTURE))
+    doc = json.load(open(FIXTURE)) if model == "spring" else json.loads(machine_document())
     doc["OUTPUT"]["DIR"] = str(tmp_path / "out")
     doc["OUTPUT"]["FORMAT"] = ["GSD", "H5"]
     cfg = tmp_path / "run.json"
@@ -222,6 +223,7 @@ def test_runner_two_element_final_state_h5(gpu_lib, tmp_path):
     np.testing.assert_array_equal(G.h5_read(h5, "SigmaCore"), g["sigma"].astype(np.float32))
     np.testing.assert_array_equal(G.h5_read(h5, "T0"), g["t0"])
     np.testing.assert_array_equal(G.h5_read(h5, "F"), frc.astype(np.float32))
+    np.testing.assert_array_equal(G.h5_read(h5, "State"), g["cell_state"])
     assert G.h5_read(h5, "RHO").shape == (n,)
 
 
