@@ -57,7 +57,7 @@ enum {
 /* Intra-cell bond of the two-element cells (cil_colony_params.intra_law). */
 enum {
   CIL_INTRA_SPRING = 0, /* linear spring kappa (r - l) with the rest length growing over the cycle */
-  CIL_INTRA_FENE = 1    /* the reference's FENE / push bond of a crawling cell (no division) */
+  CIL_INTRA_FENE = 1    /* the reference's FENE / push bond, and with divide its crawling/dividing cells */
 };
 
 /* Arithmetic of the pair forces. */
@@ -108,7 +108,7 @@ typedef struct cil_colony_params {
    * (r2max (1 - ratio)))^2) (MD.cu:255-257), acting twice along r_front - r_back, with
    * r2max = max(fene_rmax^2, the larger element diameter) (MD.cu:547-548); motility m_j along the
    * axis, scaled by rss / r without contact inhibition (cil = 0; rss from Input.cpp:139-144).
-   * kappa, rest0, rest1 are unused; divide must be 0. */
+   * kappa, rest0, rest1 are unused; with divide, the crawling/dividing cells below. */
   int32_t cil;            /* CIL_INTRA_FENE: the species' CIL flag */
   double fene_kappa;      /* KAPPA_PULL */
   double fene_kappa_push; /* KAPPA_PUSH */
