@@ -93,6 +93,8 @@ class ColonyParams(C.Structure):
         ("mig_tau_mu", C.c_double),
         ("mig_tau_sigma", C.c_double),
         ("sigma_core", C.c_double * 2),
+        ("noise_radial", C.c_double),
+        ("noise_angular", C.c_double),
     ]
 
 

@@ -440,6 +440,8 @@ ForceArgs force_args(cil_handle *h, int noise_mode, int integrate, double *vel, 
   a.range = h->d_range;
   a.slot_of = h->d_slot_of;
   a.noise = h->d_noise;
+  a.noise_act = h->d_noise ? h->d_noise + 2 * static_cast<size_t>(h->CC) * h->D : nullptr;
+  a.noise_act_t = a.noise_act ? a.noise_act + h->CC : nullptr;
   a.vel = vel;
   a.frc = frc;
   a.ts_dev = h->d_ts;
@@ -547,19 +549,38 @@ cil_status draw_oracle_noise(cil_handle *h, bool *any) {
   // the pinned buffer may still be the source of the previous step's copy
   CUDA_TRY(h, cudaStreamSynchronize(h->stream));
   size_t total = 0;
+  bool active = false;
+  const size_t act_off = 2 * static_cast<size_t>(h->CC) * h->D;  // the bond's active noise: radial, angular [CC]
   for (int c = 0; c < h->B; ++c) {
     const HostColony &hc = h->hc[c];
-    if (!(hc.p.noise_D > 0.0)) continue;
+    const bool act = h->cc[c].act_noise != 0;
+    if (!(hc.p.noise_D > 0.0) && !act) continue;
     *any = true;
-    const double amp = std::sqrt(2.0 * hc.p.noise_D) * (1.0 / std::sqrt(hc.p.dt));
     const int per = hc.p.noise_per_cell ? 1 : 2;
     const size_t base = static_cast<size_t>(h->cc[c].cell_base) * per * h->D;
     const size_t m = static_cast<size_t>(hc.n) * per * h->D;
-    for (size_t i = 0; i < m; ++i) h->h_noise[base + i] = amp * h->rng.normal();
+    if (hc.p.noise_D > 0.0) {
+      const double amp = std::sqrt(2.0 * hc.p.noise_D) * (1.0 / std::sqrt(hc.p.dt));
+      for (size_t i = 0; i < m; ++i) h->h_noise[base + i] = amp * h->rng.normal();
+    } else {
+      std::fill(h->h_noise + base, h->h_noise + base + m, 0.0);
+    }
     total = std::max(total, base + m);
+    if (act) {
+      // CIL.cu:803-815: radial for every cell, then angular; a zero amplitude draws nothing
+      active = true;
+      double *wr = h->h_noise + act_off + h->cc[c].cell_base, *wt = wr + h->CC;
+      const double ar = std::sqrt(2.0 * hc.p.noise_radial) * (1.0 / std::sqrt(hc.p.dt));
+      const double at = std::sqrt(2.0 * hc.p.noise_angular) * (1.0 / std::sqrt(hc.p.dt));
+      for (int i = 0; i < hc.n; ++i) wr[i] = hc.p.noise_radial > 0.0 ? ar * h->rng.normal() : 0.0;
+      for (int i = 0; i < hc.n; ++i) wt[i] = hc.p.noise_angular > 0.0 ? at * h->rng.normal() : 0.0;
+    }
   }
   if (*any && total > 0)
     CUDA_TRY(h, cudaMemcpyAsync(h->d_noise, h->h_noise, sizeof(double) * total, cudaMemcpyHostToDevice, h->stream));
+  if (active)
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_noise + act_off, h->h_noise + act_off, sizeof(double) * 2 * h->CC,
+                                cudaMemcpyHostToDevice, h->stream));
   return CIL_OK;
 }
 
@@ -1115,7 +1136,11 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
         (p.intra_law == CIL_INTRA_FENE && p.divide &&
          (cfg->rng_mode != CIL_RNG_DSFMT || cfg->skin > 0.0 || !(p.dt > 0.0) || !(p.div_r0 >= 0.0) ||
           !(p.div_rmin >= 0.0) || !(p.mig_tau_mu > 0.0) || !(p.mig_tau_sigma >= 0.0) ||
-          !(p.sigma_core[0] > 0.0) || !(p.sigma_core[1] > 0.0) || !(p.fene_rmax_division >= 0.0)))) {
+          !(p.sigma_core[0] > 0.0) || !(p.sigma_core[1] > 0.0) || !(p.fene_rmax_division >= 0.0))) ||
+        // the bond's active noise: 2D, the reference's bond, oracle-mode draws, no Verlet skin
+        ((p.noise_radial != 0.0 || p.noise_angular != 0.0) &&
+         (!(p.noise_radial >= 0.0) || !(p.noise_angular >= 0.0) || p.intra_law != CIL_INTRA_FENE || cfg->dim != 2 ||
+          cfg->rng_mode != CIL_RNG_DSFMT || cfg->skin > 0.0))) {
       delete h;
       return CIL_ERR_CONFIG;
     }
@@ -1194,6 +1219,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.div_r2min_f = static_cast<float>(C.div_r2min);
     C.div_rmin_ratio = p.div_rmin_ratio;
     C.div_radius = C.cell_sm ? p.div_r0 : 0.5 * p.rest0;
+    C.act_noise = p.intra_law == CIL_INTRA_FENE && (p.noise_radial > 0.0 || p.noise_angular > 0.0) ? 1 : 0;
     C.noise_amp = p.noise_D > 0.0 ? std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt)) : 0.0;
     C.dt = p.dt;
     C.div_tau_mu = p.div_tau_mu;
@@ -1336,7 +1362,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
             (mixed ? (h->d_pk[0] && h->d_pk[1]) : (h->d_sig[0] && h->d_sig[1])) &&
             skin_ok;
   if (ok && cfg->rng_mode == CIL_RNG_DSFMT) {
-    const size_t nn = 2 * static_cast<size_t>(h->CC) * D;
+    const size_t nn = 2 * static_cast<size_t>(h->CC) * D + 2 * static_cast<size_t>(h->CC);  // passive, active
     h->d_noise = dalloc<double>(nn);
     ok = h->d_noise && cudaMallocHost(&h->h_noise, sizeof(double) * nn) == cudaSuccess;
     h->rng.seed(static_cast<uint32_t>(cfg->seed));

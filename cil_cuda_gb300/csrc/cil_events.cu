@@ -193,16 +193,17 @@ __device__ void divide_cell(const EventArgs &a, const ColonyConst &C, int c, int
     a.sig[s0] = sigb;
     a.sig[s0 + 1] = sigf;
   }
-  if (C.cell_sm) {  // the mother's reset diameters; both cells crawl
+  if (C.cell_sm) {  // the mother's reset diameters
     a.sigma_c[2 * g] = sgb;
     a.sigma_c[2 * g + 1] = sgf;
     if (a.sig) {
       a.sig[sb] = sigb;
       a.sig[sf] = sigf;
     }
-    a.cst[g] = kCellCrawling;
-    a.cst[gk] = kCellCrawling;
   }
+  // both cells crawl after a division (CIL.cu:403, 425)
+  a.cst[g] = kCellCrawling;
+  a.cst[gk] = kCellCrawling;
   a.eid[s0] = 2 * gk;
   a.eid[s0 + 1] = 2 * gk + 1;
   a.slot_of[2 * gk] = s0;

@@ -102,18 +102,24 @@ __global__ void __launch_bounds__(kTile) k_force_fp64(ForceArgs a_) {
         double spring, act[2];
         fene_bond_dividing<double>(r2, fmax(si, a.sig[ps]), C.fene_r2max_div, C.fene_kappa, C.fene_kappa_push,
                                    C.fene_ratio, C.div_r2min, C.growth_k0, C.growth_k1, C.growth_k2, spring, act);
+        double rnd[3] = {0.0, 0.0, 0.0};
+        if (C.act_noise && a.noise_mode == 2) bond_noise<D, double>(a.noise_act[g], a.noise_act_t[g], rij, sqrt(r2), rnd);
 #pragma unroll
         for (int d = 0; d < D; ++d)
-          F[d] = (j == 0) ? -(act[0] * rij[d] + spring * rij[d] * 1.0) : act[1] * rij[d] + spring * rij[d] * 1.0;
+          F[d] = (j == 0) ? -(act[0] * rij[d] + spring * rij[d] * 1.0 + rnd[d] * rij[d])
+                          : act[1] * rij[d] + spring * rij[d] * 1.0 + rnd[d] * rij[d];
       } else if (C.intra_fene) {
         const double r = sqrt(r2);
         double spring, sc;
         fene_bond<double>(r2, r, fmax(si, a.sig[ps]), C.fene_r2max, C.fene_kappa, C.fene_kappa_push, C.fene_ratio,
                           C.fene_rss, C.cil, spring, sc);
+        double rnd[3] = {0.0, 0.0, 0.0};
+        if (C.act_noise && a.noise_mode == 2) bond_noise<D, double>(a.noise_act[g], a.noise_act_t[g], rij, r, rnd);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           const double nd = C.cil ? rij[d] : rij[d] * sc;
-          F[d] = (j == 0) ? -(C.motility[0] * nd + spring * rij[d] * 2.0) : C.motility[1] * nd + spring * rij[d] * 2.0;
+          F[d] = (j == 0) ? -(C.motility[0] * nd + spring * rij[d] * 2.0 + rnd[d] * rij[d])
+                          : C.motility[1] * nd + spring * rij[d] * 2.0 + rnd[d] * rij[d];
         }
       } else {
         const double r = sqrt(r2);
@@ -317,16 +323,22 @@ __device__ __forceinline__ void mixed_own_forces(const ForceArgs &a, const Colon
       fene_bond_dividing<float>(r2, fmaxf(si, fabsf(pp.w)), C.fene_r2max_div_f, C.fene_kappa_f, C.fene_kappa_push_f,
                                 C.fene_ratio_f, C.div_r2min_f, C.growth_k0_f, C.growth_k1_f, C.growth_k2_f, spring, act);
       const float coef = (j == 0) ? -(act[0] + spring) : act[1] + spring;
+      float rnd[3] = {0.0f, 0.0f, 0.0f};
+      if (C.act_noise && a.noise_mode == 2)
+        bond_noise<D, float>(static_cast<float>(a.noise_act[g]), static_cast<float>(a.noise_act_t[g]), rij, sqrtf(r2), rnd);
 #pragma unroll
-      for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
+      for (int d = 0; d < D; ++d) F[d] = coef * rij[d] + (j == 0 ? -rnd[d] : rnd[d]) * rij[d];
     } else if (r2 > 0.0f && C.intra_fene) {
       const float rinv = rsqrtf(r2);
       float spring, sc;
       fene_bond<float>(r2, r2 * rinv, fmaxf(si, fabsf(pp.w)), C.fene_r2max_f, C.fene_kappa_f, C.fene_kappa_push_f,
                        C.fene_ratio_f, C.fene_rss_f, C.cil, spring, sc);
       const float coef = (j == 0) ? -(C.motility_f[0] * sc + 2.0f * spring) : C.motility_f[1] * sc + 2.0f * spring;
+      float rnd[3] = {0.0f, 0.0f, 0.0f};
+      if (C.act_noise && a.noise_mode == 2)
+        bond_noise<D, float>(static_cast<float>(a.noise_act[g]), static_cast<float>(a.noise_act_t[g]), rij, r2 * rinv, rnd);
 #pragma unroll
-      for (int d = 0; d < D; ++d) F[d] = coef * rij[d];
+      for (int d = 0; d < D; ++d) F[d] = coef * rij[d] + (j == 0 ? -rnd[d] : rnd[d]) * rij[d];
     } else if (r2 > 0.0f) {
       const float rinv = rsqrtf(r2);
       float rest = C.rest0_f;

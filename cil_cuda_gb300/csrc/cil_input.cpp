@@ -707,13 +707,18 @@ void read_all(cil_input *in) {
   } else {
     key_error("INTERACTIONS.PAIRFORCES.SELECT", "GHOSTS is not modelled by the GPU step");
   }
-  double noise_D = 0.0;
+  double noise_D = 0.0, noise_r = 0.0, noise_a = 0.0;
+  std::string noise_path;
   if (integrator != "EULER") {  // NOISE_ON (Input.cpp:527-535, 99-111)
     Node nz = loc.child("NOISE");
     noise_D = nz.num("PASSIVE");
-    if (integrator == "STOCHASTIC_HEUN")  // NOISE_ACTIVE: radial and angular noise of the cell axis
-      for (const char *k : {"RADIAL", "ANGULAR"})
-        if (nz.num(k) != 0.0) key_error(nz.path + "." + k, "active cell noise is not modelled by the GPU step");
+    noise_path = nz.path;
+    if (integrator == "STOCHASTIC_HEUN") {  // NOISE_ACTIVE: radial and angular noise of the cell axis
+      noise_r = nz.num("RADIAL");
+      noise_a = nz.num("ANGULAR");
+      if ((noise_r != 0.0 || noise_a != 0.0) && in->dim == 3)
+        key_error("MD.INTEGRATOR.SELECT", "Active noise not yet implemented for 3D systems");
+    }
   }
   {  // steady-state length (Input.cpp:139-144) for INIT RANDOM
     Node fene = loc.child("FENE");
@@ -849,6 +854,9 @@ void read_all(cil_input *in) {
                                    "; set GPU.FORCE_LAW, EPSILON (and RCUT_SCALE)");
   }
   if (has_gpu && gpu.has("SPRING")) {  // the linear spring with the rest length growing over the cycle
+    for (const auto &kv : {std::make_pair("RADIAL", noise_r), std::make_pair("ANGULAR", noise_a)})
+      if (kv.second != 0.0)
+        key_error(noise_path + "." + kv.first, "the active noise acts on the reference's bond (no GPU.SPRING)");
     Node spring = gpu.child("SPRING");
     p.kappa = spring.num("KAPPA");
     p.rest0 = spring.num("REST0");
@@ -890,6 +898,15 @@ void read_all(cil_input *in) {
     p.fene_rmax = fene.nums("RMAX", 1)[0];
     if (!(p.fene_spring_ratio >= 0.0 && p.fene_spring_ratio < 1.0))
       key_error(fene.path + ".SPRING_RATIO", "the GPU step needs 0 <= SPRING_RATIO < 1");
+    if (noise_r != 0.0 || noise_a != 0.0) {
+      // the bond's active noise (CIL.cu:803-815, MD.cu:573-579): drawn with the reference's stream
+      p.noise_radial = noise_r;
+      p.noise_angular = noise_a;
+      cfg.rng_mode = CIL_RNG_DSFMT;
+      cfg.skin = 0.0;
+      if (has_gpu && gpu.has("RNG") && gpu.pick("RNG", {"PHILOX", "DSFMT"}) != "DSFMT")
+        key_error("GPU.RNG", "the bond's active noise runs with the reference's draws (DSFMT)");
+    }
   }
   p.noise_per_cell = has_gpu && gpu.has("NOISE_PER_CELL") ? gpu.boolean("NOISE_PER_CELL") : 0;
   if (has_gpu && gpu.has("WALLS")) {

@@ -190,10 +190,20 @@ struct ColonyConst {
   double fene_r2max_div, growth_k0[2], growth_k1[2], growth_k2[2], div_r2min, div_rmin_ratio;
   float fene_r2max_div_f, growth_k0_f[2], growth_k1_f[2], growth_k2_f[2], div_r2min_f;
   double div_radius, sigma_core[2];
+  int act_noise;  // the bond's active noise (2D, uploaded with the passive noise)
 };
 
 // Cell states of the reference's two-element cells (CellState, Cell.cuh:26-30)
 constexpr int kCellDividing = 0, kCellCrawling = 1, kCellUndefined = 2;
+
+// The bond's active noise (binaryCellForce, MD.cu:573-579; 2D): rnd = (Wr r_x / r - Wt r_y,
+// Wr r_y / r + Wt r_x) / 2, which the bond term adds as rnd_d r_ij,d.
+template <int D, typename R>
+__device__ __forceinline__ void bond_noise(R wr, R wt, const R *rij, R r, R *rnd) {
+  if (D != 2) return;
+  rnd[0] = R(0.5) * (wr * rij[0] / r - wt * rij[1]);
+  rnd[1] = R(0.5) * (wr * rij[1] / r + wt * rij[0]);
+}
 
 // The bond of a dividing cell (binaryCellForce, MD.cu:545-567): r2max from RMAX_DIVISION, the
 // growth activities act_j = -k0_j feneDivMax + k1_j + k2_j r^4 with feneDivMax = FENE(r2max,
@@ -675,6 +685,8 @@ struct ForceArgs {
   SchedState *sched;       // speed statistics for the scheduler
   StatPart *spart;         // [B][kStatSlots] displacement statistics of this pass
   const double *noise;     // oracle mode: uploaded normals (already scaled), canonical order
+  const double *noise_act; // oracle mode: the bond's active noise per cell, radial
+  const double *noise_act_t;  //   and angular
   double *vel;             // slot order, may be null
   const double *vel_prev;  // Heun second half step: the first half's velocities (null: vel itself)
   double *frc;             // slot order, may be null

@@ -131,6 +131,13 @@ typedef struct cil_colony_params {
   double div_rmin_ratio;  /* DIVISION.Rmin_RATIO (0: Rmin decides) */
   double mig_tau_mu, mig_tau_sigma; /* TAU_MIGRATION */
   double sigma_core[2];   /* SIGMA_CORE of the two elements (what a division resets to) */
+  /* CIL_INTRA_FENE in 2D: the bond's active noise (NOISE_ACTIVE of StochasticHeun, Input.cpp:99-111,
+   * CIL.cu:803-815; binaryCellForce, MD.cu:573-578): per cell and force evaluation a radial and an
+   * angular normal of amplitude sqrt(2 D) / sqrt(dt), drawn after the passive noise (oracle-mode
+   * draws, no Verlet skin); the bond term gains rnd_d r_ij,d with rnd = (Wr r_ij,x / r - Wt r_ij,y,
+   * Wr r_ij,y / r + Wt r_ij,x) / 2 */
+  double noise_radial;    /* NOISE.RADIAL (D_r) */
+  double noise_angular;   /* NOISE.ANGULAR (D_a) */
 } cil_colony_params;
 
 typedef struct cil_config {

@@ -269,6 +269,7 @@ struct Oracle {
   double fene_r2max = 0.0, fene_rss = 0.0;  // intra_law 1: RMAX^2, steady-state length
   double fene_r2max_div = 0.0;                // intra_law 1: RMAX_DIVISION^2 (RMAX^2 without it)
   std::vector<int> cst;                       // CellState per cell (Cell.cuh:26-30)
+  std::vector<double> awr, awt;               // the bond's active noise per cell (radial, angular)
   std::vector<double> pos, vel, frc, sig, wiener;
   std::vector<int> t0, tsw;
   Rng rng;
@@ -307,6 +308,15 @@ struct Oracle {
     double frac = span > 0 ? static_cast<double>(ts - t0[c]) / static_cast<double>(span) : 1.0;
     frac = std::min(1.0, std::max(0.0, frac));
     return p.rest0 + (p.rest1 - p.rest0) * frac;
+  }
+
+  // the bond's active noise term (MD.cu:573-579, 2D): rnd = (Wr r_x / r - Wt r_y,
+  // Wr r_y / r + Wt r_x) / 2, added as rnd_d r_ij,d
+  void active_noise(int c, const double *rij, double r, double *rnd) const {
+    if (D != 2 || awr.empty()) return;
+    const double wr = awr[c], wt = awt[c];
+    rnd[0] = 0.5 * (wr * rij[0] / r - wt * rij[1]);
+    rnd[1] = 0.5 * (wr * rij[1] / r + wt * rij[0]);
   }
 
   // binaryCellForce (MD.cu:525-598) with the linear bond: spring kappa (r - l)
@@ -348,17 +358,21 @@ struct Oracle {
         const double fdm = -p.fene_kappa / (1.0 - qd * qd);
         double act[2];
         for (int j = 0; j < 2; ++j) act[j] = -p.growth_k0[j] * fdm + p.growth_k1[j] + p.growth_k2[j] * (r2 * r2);
+        double rnd[3] = {0, 0, 0};
+        active_noise(c, rij, r, rnd);
         for (int d = 0; d < D; ++d) {
-          f0[d] = -(act[0] * rij[d] + spring * rij[d] * 1.0);
-          f1[d] = act[1] * rij[d] + spring * rij[d] * 1.0;
+          f0[d] = -(act[0] * rij[d] + spring * rij[d] * 1.0 + rnd[d] * rij[d]);
+          f1[d] = act[1] * rij[d] + spring * rij[d] * 1.0 + rnd[d] * rij[d];
         }
         return;
       }
       const double scaling = p.cil ? 1.0 : fene_rss / r;
+      double rnd[3] = {0, 0, 0};
+      active_noise(c, rij, r, rnd);
       for (int d = 0; d < D; ++d) {
         const double nd = p.cil ? rij[d] : rij[d] * scaling;
-        f0[d] = -(p.motility[0] * nd + spring * rij[d] * 2.0);
-        f1[d] = p.motility[1] * nd + spring * rij[d] * 2.0;
+        f0[d] = -(p.motility[0] * nd + spring * rij[d] * 2.0 + rnd[d] * rij[d]);
+        f1[d] = p.motility[1] * nd + spring * rij[d] * 2.0 + rnd[d] * rij[d];
       }
       return;
     }
@@ -387,11 +401,26 @@ struct Oracle {
   // updateWienerProcess, CIL.cu:793-818: amplitude sqrt(2 D) (Input.cpp:112) / sqrt(dt)
   // (CIL.cuh:211-215); drawn for every entry in storage order only when D > 0.
   void draw_noise() {
-    if (!(p.noise_D > 0.0)) return;
-    const double amp = std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt));
-    const size_t m = static_cast<size_t>(n) * (p.noise_per_cell ? 1 : 2) * D;
-    wiener.resize(std::max(wiener.size(), m));
-    for (size_t i = 0; i < m; ++i) wiener[i] = amp * rng.normal();
+    if (p.noise_D > 0.0) {
+      const double amp = std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt));
+      const size_t m = static_cast<size_t>(n) * (p.noise_per_cell ? 1 : 2) * D;
+      wiener.resize(std::max(wiener.size(), m));
+      for (size_t i = 0; i < m; ++i) wiener[i] = amp * rng.normal();
+    }
+    // the bond's active noise after the passive one (CIL.cu:803-815): radial for every cell,
+    // then angular; a component whose amplitude is zero is never drawn and stays 0
+    if (p.intra_law == 1 && D == 2) {
+      awr.assign(static_cast<size_t>(cap), 0.0);
+      awt.assign(static_cast<size_t>(cap), 0.0);
+      if (p.noise_radial > 0.0) {
+        const double amp = std::sqrt(2.0 * p.noise_radial) * (1.0 / std::sqrt(p.dt));
+        for (int i = 0; i < n; ++i) awr[i] = amp * rng.normal();
+      }
+      if (p.noise_angular > 0.0) {
+        const double amp = std::sqrt(2.0 * p.noise_angular) * (1.0 / std::sqrt(p.dt));
+        for (int i = 0; i < n; ++i) awt[i] = amp * rng.normal();
+      }
+    }
   }
   void add_noise(int c, int j) {
     if (!(p.noise_D > 0.0)) return;
@@ -665,6 +694,8 @@ struct Oracle {
       reorient(P(k, 1), P(k, 0), radius);
       t0[k] = ts;
       t0[i] = ts;
+      cst[k] = kCrawling;  // both cells crawl after a division (CIL.cu:403, 425)
+      cst[i] = kCrawling;
       tsw[k] = ts + time_span();
       for (int j = 0; j < 2; ++j)
         for (int d = 0; d < D; ++d) V(k, j)[d] = V(i, j)[d] = F(k, j)[d] = F(i, j)[d] = 0.0;

@@ -63,6 +63,7 @@ typedef struct ora_params {
   double div_r0, div_rmin, div_rmin_ratio;
   double mig_tau_mu, mig_tau_sigma;
   double sigma_core[2];
+  double noise_radial, noise_angular; /* intra_law 1, 2D: the bond's active noise (NOISE_ACTIVE) */
 } ora_params;
 
 typedef struct ora_event {

@@ -5,8 +5,8 @@ device each step):
 
 * forces of a colony with crawling, dividing and undefined cells: 1e-12 (FP64), 2e-5 (mixed);
 * 300 steps in which cells start dividing, divide and fail to divide, with apoptosis, Euler and
-  the reference's own Heun integrator: cell counts, birth and switch times and states equal,
-  positions 1e-9 (FP64).
+  the reference's own Heun integrator (also with the bond's active noise): cell counts, birth and
+  switch times and states equal, positions 1e-9 (FP64).
 """
 import numpy as np
 import pytest
@@ -37,10 +37,12 @@ def minimage(a, b, L):
     return d - np.round(d / L) * L
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_forces_with_cell_states(gpu_lib, oracle_lib, precision):
+@pytest.mark.parametrize("precision,active", [(0, False), (1, False), (0, True)])
+def test_forces_with_cell_states(gpu_lib, oracle_lib, precision, active):
     G = gpu_lib
     p = machine_params(noise_D=0.0, growth_k0=[0.3, 0.1], growth_k2=[0.05, 0.02])
+    if active:  # the bond's active noise, drawn by both sides from the reference's stream
+        p.update(noise_D=0.002, noise_radial=0.05, noise_angular=0.03)
     st = colony(p)
     eng = G.Engine([p], [len(st["sigma"])], precision=precision, rng=G.RNG_DSFMT, seed=5)
     eng.upload(0, **st)
@@ -53,10 +55,11 @@ def test_forces_with_cell_states(gpu_lib, oracle_lib, precision):
     assert err <= (1e-12 if precision == 0 else 2e-5), err
 
 
-@pytest.mark.parametrize("integrator", [0, 1])
-def test_state_machine_matches_oracle(gpu_lib, oracle_lib, integrator):
+@pytest.mark.parametrize("integrator,active", [(0, False), (1, False), (1, True)])
+def test_state_machine_matches_oracle(gpu_lib, oracle_lib, integrator, active):
+    """active: the bond's active noise of StochasticHeun (radial and angular, CIL.cu:803-815)."""
     G = gpu_lib
-    p = machine_params()
+    p = machine_params(noise_radial=0.01, noise_angular=0.02) if active else machine_params()
     st = colony(p)
     cap = 4000
     eng = G.Engine([p], [cap], precision=G.PREC_FP64, rng=G.RNG_DSFMT, seed=7, integrator=integrator)
@@ -86,3 +89,6 @@ def test_state_machine_forms_refused(gpu_lib):
     for kw in (dict(rng=G.RNG_PHILOX), dict(rng=G.RNG_DSFMT, precision=G.PREC_MIXED, skin=0.3)):
         with pytest.raises(G.CilError):
             G.Engine([p], [1000], **kw)
+    q = S.fene_params(noise_radial=0.01)  # active noise: the same forms
+    with pytest.raises(G.CilError):
+        G.Engine([q], [1000], rng=G.RNG_PHILOX)

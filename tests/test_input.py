@@ -256,6 +256,26 @@ def test_dividing_cells_with_the_reference_bond_are_read(G):
     assert "SWELLING" in str(e.value)
 
 
+def test_heun_active_noise_on_the_reference_bond(G):
+    """STOCHASTIC_HEUN turns NOISE_ACTIVE on (Input.cpp:533-535): with the reference's bond its
+    RADIAL and ANGULAR amplitudes are read (reference draws, no skin); 3D is refused as the
+    reference refuses it."""
+    d = copy.deepcopy(doc())
+    del d["GPU"]["SPRING"]
+    d["SPECIES"]["A"]["DIVISION"]["ENABLED"] = False
+    d["MD"]["INTEGRATOR"]["SELECT"] = "STOCHASTIC_HEUN"
+    d["SPECIES"]["A"]["NOISE"].update(RADIAL=0.01, ANGULAR=0.02)
+    r = load(G, d)
+    assert (r.params["noise_radial"], r.params["noise_angular"]) == (0.01, 0.02)
+    assert r.config["rng_mode"] == G.RNG_DSFMT and r.config["skin"] == 0.0
+    d["MD"]["DIM"] = 3
+    d["MD"]["BOX"] = [60, 60, 60]
+    d["MD"]["PBC"] = [True, True, True]
+    with pytest.raises(G.CilError) as e:
+        load(G, d)
+    assert "Active noise not yet implemented for 3D systems" in str(e.value)
+
+
 def sc_doc():
     d = copy.deepcopy(doc())
     del d["GPU"]["FORCE_LAW"]
