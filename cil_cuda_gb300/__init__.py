@@ -95,6 +95,8 @@ class ColonyParams(C.Structure):
         ("sigma_core", C.c_double * 2),
         ("noise_radial", C.c_double),
         ("noise_angular", C.c_double),
+        ("div_swelling", C.c_int32),
+        ("pad_swell", C.c_int32),
     ]
 
 

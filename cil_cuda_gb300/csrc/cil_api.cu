@@ -228,7 +228,10 @@ double bin_width_for(const cil_handle *h, const HostColony &c) {
   // a colony without cells stays without (nothing divides): one bin
   if (!(c.sigma_max > 0.0)) return std::max(c.p.box[0], std::max(c.p.box[1], c.p.box[2]));
   // the law's reach for the largest diameter (the soft-core well reaches xi past contact)
-  const double reach = c.p.force_law == CIL_FORCE_SC ? c.sigma_max + c.p.well_sigma : c.sigma_max;
+  // crawling/dividing cells take SIGMA_CORE at a division and may swell up to its larger value
+  double smax = c.sigma_max;
+  if (c.p.intra_law == CIL_INTRA_FENE && c.p.divide) smax = std::max(smax, std::max(c.p.sigma_core[0], c.p.sigma_core[1]));
+  const double reach = c.p.force_law == CIL_FORCE_SC ? smax + c.p.well_sigma : smax;
   const double need = c.p.rcut_scale * reach + h->cfg.skin;
   return h->cfg.bin_width > need ? h->cfg.bin_width : need;
 }
@@ -731,6 +734,14 @@ cil_status oracle_events(cil_handle *h) {
     launch_divisions_list(a, c, n0, ndiv, h->d_oracle_i, h->d_oracle_d, h->d_oracle_i + ndiv, D, h->stream);
     launch_apo_ops_with_div(a, c, ndiv, static_cast<int>(ops.size()), h->d_oracle_i + 3 * ndiv, D, h->stream);
     h->launches += (ndiv > 0 ? 1 : 0) + (nsm > 0 ? 1 : 0) + 1;
+  }
+  // updateDiameters (CIL.cu:970-991) after the events: swelling of dividing cells
+  for (int c = 0; c < h->B; ++c) {
+    const HostColony &hc = h->hc[c];
+    if (hc.p.divide && hc.p.intra_law == CIL_INTRA_FENE && hc.p.div_swelling && hc.n > 0) {
+      launch_sm_swell(event_args(h), c, hc.n, ts, h->stream);
+      h->launches += 1;
+    }
   }
   if (cap_hit >= 0) return fail(h, CIL_ERR_CAPACITY, "cell capacity exceeded in colony " + std::to_string(cap_hit));
   return CIL_OK;

@@ -1095,6 +1095,32 @@ __global__ void k_sm_ops(EventArgs a, int c, int nops, const int *ops, const dou
   }
 }
 
+// updateDiameters (CIL.cu:970-991) with SWELLING: a dividing cell's diameters below the larger
+// SIGMA_CORE grow by (max - sigma) / (tswitch - ts); canonical and binned copies.
+__global__ void k_sm_swell(EventArgs a, int c, int n, int ts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ColonyConst &C = a.col[c];
+  const int g = C.cell_base + i;
+  if (a.cst[g] != kCellDividing) return;
+  const double smax = C.sigma_core[0] > C.sigma_core[1] ? C.sigma_core[0] : C.sigma_core[1];
+  const double span = static_cast<double>(a.tsw[g] - ts);
+  for (int j = 0; j < 2; ++j) {
+    double s = a.sigma_c[2 * g + j];
+    if (s < smax) {
+      s = __dadd_rn(s, (smax - s) / span);
+      a.sigma_c[2 * g + j] = s;
+      const int sl = a.slot_of[2 * g + j];
+      if (a.sig) a.sig[sl] = s;
+      if (a.pk) a.pk[sl].w = copysignf(static_cast<float>(s), a.pk[sl].w);
+    }
+  }
+}
+
+void launch_sm_swell(const EventArgs &a, int colony, int n, int ts, cudaStream_t s) {
+  if (n > 0) k_sm_swell<<<(n + 255) / 256, 256, 0, s>>>(a, colony, n, ts);
+}
+
 __global__ void k_fill_int(int *dst, int n, int value) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = value;

@@ -882,8 +882,7 @@ void read_all(cil_input *in) {
         p.sigma_core[j] = in->sigma[j];
       }
       p.fene_rmax_division = fene.has("RMAX_DIVISION") ? fene.nums("RMAX_DIVISION", 1)[0] : 0.0;
-      if (dv.has("SWELLING") && dv.boolean("SWELLING"))
-        key_error(dv.path + ".SWELLING", "swelling of dividing cells is not modelled by the GPU step");
+      p.div_swelling = dv.has("SWELLING") && dv.boolean("SWELLING") ? 1 : 0;
       // the outcomes of the divisions are read back each step to draw the reference's stream
       cfg.rng_mode = CIL_RNG_DSFMT;
       cfg.skin = 0.0;

@@ -876,6 +876,7 @@ void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops,
                              cudaStream_t s);
 void launch_fill_int(int *dst, int n, int value, cudaStream_t s);
 void launch_sm_flags(const EventArgs &a, int colony, int n, int dim, cudaStream_t s);
+void launch_sm_swell(const EventArgs &a, int colony, int n, int ts, cudaStream_t s);
 void launch_sm_ops(const EventArgs &a, int colony, int nops, const int *ops, const double *dirs, int dim,
                    cudaStream_t s);
 void launch_upload(const ColonyConst *col, int colony, int ncells, int dim, size_t SS, const double *stage,

@@ -138,6 +138,10 @@ typedef struct cil_colony_params {
    * Wr r_ij,y / r + Wt r_ij,x) / 2 */
   double noise_radial;    /* NOISE.RADIAL (D_r) */
   double noise_angular;   /* NOISE.ANGULAR (D_a) */
+  /* crawling/dividing cells: DIVISION.SWELLING, each step a dividing cell's diameters below the
+   * larger SIGMA_CORE grow by (max - sigma) / (tswitch - ts) (updateDiameters, CIL.cu:970-991) */
+  int32_t div_swelling;
+  int32_t pad_swell;
 } cil_colony_params;
 
 typedef struct cil_config {

@@ -706,6 +706,20 @@ struct Oracle {
     return err;
   }
 
+  // updateDiameters (CIL.cu:970-991): with SWELLING a dividing cell's diameters below the larger
+  // SIGMA_CORE grow by (max - sigma) / (tswitch - ts) each step
+  void swell() {
+    if (!(p.divide && p.intra_law == 1 && p.div_swelling)) return;
+    const double smax = std::max(p.sigma_core[0], p.sigma_core[1]);
+    for (int i = 0; i < n; ++i) {
+      if (cst[i] != kDividing) continue;
+      for (int j = 0; j < 2; ++j) {
+        double &s = sig[2 * static_cast<size_t>(i) + j];
+        if (s < smax) s += (smax - s) / (tsw[i] - ts);
+      }
+    }
+  }
+
   // calculApoptosis, CIL.cu:627-649: sequential test of every slot, swap-with-last removal
   // (removeCell, Colony.cpp:365-399) and a re-test of the same slot.
   void apoptosis() {
@@ -738,6 +752,7 @@ struct Oracle {
     ++ts;
     const int err = divisions();
     apoptosis();
+    swell();
     // checkPositions (CIL.cu:945-966): every coordinate inside the box
     for (int c = 0; c < n; ++c)
       for (int j = 0; j < 2; ++j)

@@ -64,6 +64,8 @@ typedef struct ora_params {
   double mig_tau_mu, mig_tau_sigma;
   double sigma_core[2];
   double noise_radial, noise_angular; /* intra_law 1, 2D: the bond's active noise (NOISE_ACTIVE) */
+  int32_t div_swelling;               /* intra_law 1 with divide: DIVISION.SWELLING */
+  int32_t pad_swell;
 } ora_params;
 
 typedef struct ora_event {

@@ -55,11 +55,16 @@ def test_forces_with_cell_states(gpu_lib, oracle_lib, precision, active):
     assert err <= (1e-12 if precision == 0 else 2e-5), err
 
 
-@pytest.mark.parametrize("integrator,active", [(0, False), (1, False), (1, True)])
-def test_state_machine_matches_oracle(gpu_lib, oracle_lib, integrator, active):
-    """active: the bond's active noise of StochasticHeun (radial and angular, CIL.cu:803-815)."""
+@pytest.mark.parametrize("integrator,extra", [(0, None), (1, None), (1, "active"), (1, "swelling")])
+def test_state_machine_matches_oracle(gpu_lib, oracle_lib, integrator, extra):
+    """active: the bond's active noise of StochasticHeun (radial and angular, CIL.cu:803-815);
+    swelling: dividing cells' diameters grow towards the larger SIGMA_CORE (CIL.cu:970-991)."""
     G = gpu_lib
-    p = machine_params(noise_radial=0.01, noise_angular=0.02) if active else machine_params()
+    p = machine_params()
+    if extra == "active":
+        p.update(noise_radial=0.01, noise_angular=0.02)
+    elif extra == "swelling":
+        p.update(div_swelling=1, sigma_core=[1.0, 1.2])
     st = colony(p)
     cap = 4000
     eng = G.Engine([p], [cap], precision=G.PREC_FP64, rng=G.RNG_DSFMT, seed=7, integrator=integrator)

@@ -249,11 +249,10 @@ def test_dividing_cells_with_the_reference_bond_are_read(G):
     with pytest.raises(G.CilError) as e:
         load(G, d)
     assert "GPU.RNG" in str(e.value)
+    assert p["div_swelling"] == 0
     d = machine_doc()
     d["SPECIES"]["A"]["DIVISION"]["SWELLING"] = True
-    with pytest.raises(G.CilError) as e:
-        load(G, d)
-    assert "SWELLING" in str(e.value)
+    assert load(G, d).params["div_swelling"] == 1
 
 
 def test_heun_active_noise_on_the_reference_bond(G):
