@@ -131,6 +131,7 @@ struct cil_handle {
   int *d_slot_of = nullptr;
   int *d_t0 = nullptr, *d_tsw = nullptr;
   int *d_cst = nullptr;     // cell states [CC] (crawling/dividing cells)
+  bool any_cell_sm = false, any_swell = false;  // some colony has crawling/dividing cells (with swelling)
   unsigned char *d_smflag = nullptr;  // per cell: division criterion met (oracle mode, state machine)
   int *d_tiles_used = nullptr, *d_tiles_live = nullptr, *d_tiles_cell = nullptr;
   int *d_tiles_pairs = nullptr;  // skin mode: tiles over slot pairs (the cell-major force kernel)
@@ -821,8 +822,12 @@ cil_status enqueue_step(cil_handle *h, bool last, bool timed, size_t e0) {
     launch_events_due(event_args(h), h->D, h->stream);
     h->launches += 1;
   } else {
-    launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream);
-    h->launches += 3;
+    launch_events_fast(event_args(h), h->grid_cells, h->D, h->stream, h->any_cell_sm);
+    h->launches += h->any_cell_sm ? 4 : 3;
+    if (h->any_swell) {
+      launch_sm_swell_all(event_args(h), h->grid_cells, h->stream);
+      h->launches += 1;
+    }
   }
   if (timed) CUDA_TRY(h, cudaEventRecord(pool_event(h, e0 + 3), h->stream));
   CUDA_TRY(h, cudaGetLastError());
@@ -1145,7 +1150,7 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
         // the crawling/dividing cells: oracle-mode draws (their outcomes are read back each step),
         // bins rebuilt every step (no Verlet skin), positive spans and radius
         (p.intra_law == CIL_INTRA_FENE && p.divide &&
-         (cfg->rng_mode != CIL_RNG_DSFMT || cfg->skin > 0.0 || !(p.dt > 0.0) || !(p.div_r0 >= 0.0) ||
+         (cfg->skin > 0.0 || !(p.dt > 0.0) || !(p.div_r0 >= 0.0) ||
           !(p.div_rmin >= 0.0) || !(p.mig_tau_mu > 0.0) || !(p.mig_tau_sigma >= 0.0) ||
           !(p.sigma_core[0] > 0.0) || !(p.sigma_core[1] > 0.0) || !(p.fene_rmax_division >= 0.0))) ||
         // the bond's active noise: 2D, the reference's bond, oracle-mode draws, no Verlet skin
@@ -1231,6 +1236,12 @@ cil_status cil_create(const cil_config *cfg, const cil_colony_params *params, co
     C.div_rmin_ratio = p.div_rmin_ratio;
     C.div_radius = C.cell_sm ? p.div_r0 : 0.5 * p.rest0;
     C.act_noise = p.intra_law == CIL_INTRA_FENE && (p.noise_radial > 0.0 || p.noise_angular > 0.0) ? 1 : 0;
+    C.dim = p.dim;
+    C.swelling = C.cell_sm && p.div_swelling ? 1 : 0;
+    if (C.cell_sm) h->any_cell_sm = true;
+    if (C.swelling) h->any_swell = true;
+    C.mig_mu_steps_f = static_cast<float>(p.mig_tau_mu / p.dt);
+    C.mig_sd_steps_f = static_cast<float>(p.mig_tau_sigma / p.dt);
     C.noise_amp = p.noise_D > 0.0 ? std::sqrt(2.0 * p.noise_D) * (1.0 / std::sqrt(p.dt)) : 0.0;
     C.dt = p.dt;
     C.div_tau_mu = p.div_tau_mu;

@@ -258,10 +258,34 @@ __device__ void division_draws(const EventArgs &a, int i, double *dir_m, double 
   }
   float n0, n1;
   box_muller(r2.v[0], r2.v[1], n0, n1);
-  const int sd = __float2int_rn(C.tau_mu_steps_f + C.tau_sd_steps_f * n0);
-  const int sm = __float2int_rn(C.tau_mu_steps_f + C.tau_sd_steps_f * n1);
+  const float mu = C.cell_sm ? C.mig_mu_steps_f : C.tau_mu_steps_f;
+  const float sdv = C.cell_sm ? C.mig_sd_steps_f : C.tau_sd_steps_f;
+  const int sd = __float2int_rn(mu + sdv * n0);
+  const int sm = __float2int_rn(mu + sdv * n1);
   span_d = sd >= 1 ? sd : 1;  // randomTimeSpan, MD.cuh:434-436
   span_m = sm >= 1 ? sm : 1;
+}
+
+// The crawling/dividing cells: whether dividing cell g has its elements Rmin apart
+// (binaryCellDivisionCriteria, MD.cuh:426-433; BoundingBox::distance, Utils.hpp:536-544, without
+// fused arithmetic, as the restatement computes it).
+__device__ __forceinline__ bool sm_ready(const EventArgs &a, const ColonyConst &C, int g) {
+  const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+  double r2 = 0.0;
+  for (int d = 0; d < C.dim; ++d) {
+    double v = __dsub_rn(a.x[d * a.SS + s0], a.x[d * a.SS + s1]);  // r0 - r1
+    if (C.periodic[d]) v = __dsub_rn(v, __dmul_rn(static_cast<double>(nint(v / C.box[d])), C.box[d]));
+    r2 = __dadd_rn(r2, __dmul_rn(v, v));
+  }
+  return C.div_rmin_ratio != 0.0 ? r2 >= __dmul_rn(C.div_rmin_ratio, a.sigma_c[2 * g]) : r2 >= C.div_r2min;
+}
+
+// A division at this step: the cycle ends (linear growth), or a dividing cell is ready
+// (crawling/dividing cells).
+__device__ __forceinline__ bool division_due(const EventArgs &a, const ColonyConst &C, int i, int ts) {
+  const int g = C.cell_base + i;
+  if (C.cell_sm) return a.cst[g] == kCellDividing && sm_ready(a, C, g);
+  return a.tsw[g] == ts;
 }
 
 // division detection: kCellItems consecutive cells per thread
@@ -278,7 +302,7 @@ __global__ void __launch_bounds__(kTile) k_div_count(EventArgs a_) {
     if (C.divide) {
 #pragma unroll
       for (int q = 0; q < kCellItems; ++q)
-        due += (i0 + q < n && a.tsw[C.cell_base + i0 + q] == a.ts) ? 1 : 0;
+        due += (i0 + q < n && division_due(a, C, i0 + q, a.ts)) ? 1 : 0;
     }
     int tot;
     block_excl_scan_ev(due, &tot);
@@ -327,7 +351,7 @@ __global__ void __launch_bounds__(kTile) k_div_rank(EventArgs a_) {
     int cnt = 0;
 #pragma unroll
     for (int q = 0; q < kCellItems; ++q) {
-      due[q] = C.divide && i0 + q < n && a.tsw[C.cell_base + i0 + q] == ts;
+      due[q] = C.divide && i0 + q < n && division_due(a, C, i0 + q, ts);
       cnt += due[q] ? 1 : 0;
     }
     int tot;
@@ -650,7 +674,9 @@ __global__ void __launch_bounds__(kTile) k_events_exec(EventArgs a_) {
     double dm[D], dd[D];
     int span_d, span_m;
     division_draws<D>(a, i, dm, dd, span_d, span_m, C);
-    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, a.ts + span_m, nslot, r);
+    // crawling/dividing cells: migration spans, the mother's added to her own time (CIL.cu:403, 424)
+    const int tm = C.cell_sm ? a.tsw[C.cell_base + i] + span_m : a.ts + span_m;
+    divide_cell<D>(a, C, c, i, n + r, dm, dd, a.ts + span_d, tm, nslot, r);
   }
   __syncthreads();  // every division is placed, and visible to the whole block
   apo_colony(a, c, D);
@@ -1003,9 +1029,10 @@ void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s, const Colo
   k_step_end<<<1, kTile, 0, s>>>(ts_dev, any_rebuild, cnt, B, tiles_cell);
 }
 
-void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s) {
+void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s, bool cell_states) {
   k_div_count<<<grid_cells, kTile, 0, s>>>(a);
   k_div_rank<<<grid_cells, kTile, 0, s>>>(a);
+  if (cell_states) launch_sm_philox(a, grid_cells, s);
   if (dim == 2)
     k_events_exec<2><<<a.B, kTile, 0, s>>>(a);
   else
@@ -1097,11 +1124,15 @@ __global__ void k_sm_ops(EventArgs a, int c, int nops, const int *ops, const dou
 
 // updateDiameters (CIL.cu:970-991) with SWELLING: a dividing cell's diameters below the larger
 // SIGMA_CORE grow by (max - sigma) / (tswitch - ts); canonical and binned copies.
+__device__ __forceinline__ void swell_cell(const EventArgs &a, const ColonyConst &C, int g, int ts);
+
 __global__ void k_sm_swell(EventArgs a, int c, int n, int ts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const ColonyConst &C = a.col[c];
-  const int g = C.cell_base + i;
+  swell_cell(a, a.col[c], a.col[c].cell_base + i, ts);
+}
+
+__device__ __forceinline__ void swell_cell(const EventArgs &a, const ColonyConst &C, int g, int ts) {
   if (a.cst[g] != kCellDividing) return;
   const double smax = C.sigma_core[0] > C.sigma_core[1] ? C.sigma_core[0] : C.sigma_core[1];
   const double span = static_cast<double>(a.tsw[g] - ts);
@@ -1119,6 +1150,107 @@ __global__ void k_sm_swell(EventArgs a, int c, int n, int ts) {
 
 void launch_sm_swell(const EventArgs &a, int colony, int n, int ts, cudaStream_t s) {
   if (n > 0) k_sm_swell<<<(n + 255) / 256, 256, 0, s>>>(a, colony, n, ts);
+}
+
+// Philox mode, crawling/dividing cells, before the divisions are placed: a crawling (or
+// undefined) cell whose time ends starts dividing (time += a division span); a dividing cell
+// short of Rmin whose time ends fails (binaryCellDivisionFail at R0 along a random axis; crawling;
+// time += a migration span). Draws keyed by (cell, step, purpose, colony stream).
+__global__ void __launch_bounds__(kTile) k_sm_philox(EventArgs a_) {
+  EventArgs a = a_;
+  a.ts = *a_.ts_dev;
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    if (!C.cell_sm) continue;
+    const int n = a.cnt[c].ncell;
+    const int i0 = (t - a.tiles_cell[c]) * kCellTile + threadIdx.x * kCellItems;
+    for (int q = 0; q < kCellItems; ++q) {
+      const int i = i0 + q;
+      if (i >= n) break;
+      const int g = C.cell_base + i;
+      if (a.tsw[g] != a.ts) continue;
+      const bool dividing = a.cst[g] == kCellDividing;
+      if (dividing && sm_ready(a, C, g)) continue;  // divides (k_events_exec)
+      const u32x4 r = philox4x32_10(static_cast<uint32_t>(i), static_cast<uint32_t>(a.ts), kRngCellState,
+                                    C.rng_stream, a.seed_lo, a.seed_hi);
+      float n0, n1;
+      box_muller(r.v[0], r.v[1], n0, n1);
+      const float mu = dividing ? C.mig_mu_steps_f : C.tau_mu_steps_f;
+      const float sd = dividing ? C.mig_sd_steps_f : C.tau_sd_steps_f;
+      const int span = max(__float2int_rn(mu + sd * n0), 1);
+      const int s0 = a.slot_of[2 * g], s1 = a.slot_of[2 * g + 1];
+      if (dividing) {  // failed division
+        const float k24 = 5.9604644775390625e-08f;  // 2^-24
+        double dir[3] = {0.0, 0.0, 0.0};
+        if (C.dim == 2) {
+          float sn, cs;
+          sincospif(2.0f * static_cast<float>(r.v[2] >> 8) * k24, &sn, &cs);
+          dir[0] = cs;
+          dir[1] = sn;
+        } else {
+          const float z = 2.0f * static_cast<float>(r.v[2] >> 8) * k24 - 1.0f;
+          const float qz = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+          float sn, cs;
+          sincospif(2.0f * static_cast<float>(r.v[3] >> 8) * k24, &sn, &cs);
+          dir[0] = qz * cs;
+          dir[1] = qz * sn;
+          dir[2] = z;
+        }
+        double x0[3], x1[3];
+        for (int d = 0; d < C.dim; ++d) {
+          x0[d] = a.x[d * a.SS + s0];
+          x1[d] = a.x[d * a.SS + s1];
+          double v = __dsub_rn(x1[d], x0[d]);
+          if (C.periodic[d]) v = __dsub_rn(v, __dmul_rn(static_cast<double>(nint(v / C.box[d])), C.box[d]));
+          x0[d] = __dadd_rn(x0[d], __dmul_rn(v, 0.5));
+        }
+        for (int d = 0; d < C.dim; ++d) {
+          const double m = __dadd_rn(x0[d], __dmul_rn(C.div_radius, dir[d]));
+          const double sl = __dadd_rn(x0[d], __dmul_rn(-C.div_radius, dir[d]));
+          a.x[d * a.SS + s0] = C.periodic[d] ? wrap_like_fmod(m, C.box[d]) : m;
+          a.x[d * a.SS + s1] = C.periodic[d] ? wrap_like_fmod(sl, C.box[d]) : sl;
+        }
+        a.sigma_c[2 * g] = C.sigma_core[0];
+        a.sigma_c[2 * g + 1] = C.sigma_core[1];
+        if (a.sig) {
+          a.sig[s0] = C.sigma_core[0];
+          a.sig[s1] = C.sigma_core[1];
+        }
+        a.cst[g] = kCellCrawling;
+      } else {
+        a.cst[g] = kCellDividing;
+      }
+      a.tsw[g] += span;
+      if (a.vel)
+        for (int d = 0; d < C.dim; ++d) a.vel[d * a.SS + s0] = a.vel[d * a.SS + s1] = 0.0;
+    }
+  }
+}
+
+// Philox mode: swelling of every colony's dividing cells after the events (the step from the
+// device counter, so that a captured step replays correctly)
+__global__ void __launch_bounds__(kTile) k_sm_swell_all(EventArgs a_) {
+  const EventArgs &a = a_;
+  const int ts = *a.ts_dev;
+  const int total = a.tiles_cell[a.B];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int c = colony_of_tile(a.tiles_cell, a.B, t);
+    const ColonyConst &C = a.col[c];
+    if (!C.cell_sm || !C.swelling) continue;
+    const int n = a.cnt[c].ncell;
+    const int i0 = (t - a.tiles_cell[c]) * kCellTile + threadIdx.x * kCellItems;
+    for (int q = 0; q < kCellItems && i0 + q < n; ++q) swell_cell(a, C, C.cell_base + i0 + q, ts);
+  }
+}
+
+void launch_sm_philox(const EventArgs &a, int grid_cells, cudaStream_t s) {
+  k_sm_philox<<<grid_cells, kTile, 0, s>>>(a);
+}
+
+void launch_sm_swell_all(const EventArgs &a, int grid_cells, cudaStream_t s) {
+  k_sm_swell_all<<<grid_cells, kTile, 0, s>>>(a);
 }
 
 __global__ void k_fill_int(int *dst, int n, int value) {

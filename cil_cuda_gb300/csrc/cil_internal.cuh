@@ -41,6 +41,7 @@ constexpr int kErrCap = 1 << CIL_ERR_CAPACITY;
 
 // Philox purposes (third counter word)
 constexpr uint32_t kRngNoise = 1, kRngDiv = 2, kRngDiv2 = 3, kRngApo = 4, kRngApoPick = 5;
+constexpr uint32_t kRngCellState = 6;  // the crawling/dividing cells' start and failed-division draws
 
 // per-slot state in skin mode
 constexpr unsigned char kSlotNormal = 0;  // in the bins and Verlet lists of the last rebuild
@@ -191,6 +192,9 @@ struct ColonyConst {
   float fene_r2max_div_f, growth_k0_f[2], growth_k1_f[2], growth_k2_f[2], div_r2min_f;
   double div_radius, sigma_core[2];
   int act_noise;  // the bond's active noise (2D, uploaded with the passive noise)
+  int dim;
+  float mig_mu_steps_f, mig_sd_steps_f;  // migration time mean and sd in steps (Philox draws)
+  int swelling;  // crawling/dividing cells with SWELLING
 };
 
 // Cell states of the reference's two-element cells (CellState, Cell.cuh:26-30)
@@ -868,7 +872,7 @@ void launch_fresh_pairs(const SkinArgs &a, int dim, int law, cudaStream_t s);
 void launch_advance_ts(int *ts_dev, int *any_rebuild, cudaStream_t s, const ColonyCounters *cnt = nullptr, int B = 0,
                        int *tiles_cell = nullptr);
 int mlp_param_count();
-void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s);
+void launch_events_fast(const EventArgs &a, int grid_cells, int dim, cudaStream_t s, bool cell_states);
 void launch_events_due(const EventArgs &a, int dim, cudaStream_t s);
 void launch_divisions_list(const EventArgs &a, int colony, int n0, int ndiv, const int *mothers,
                            const double *dirs, const int *spans, int dim, cudaStream_t s);
@@ -877,6 +881,8 @@ void launch_apo_ops_with_div(const EventArgs &a, int colony, int ndiv, int nops,
 void launch_fill_int(int *dst, int n, int value, cudaStream_t s);
 void launch_sm_flags(const EventArgs &a, int colony, int n, int dim, cudaStream_t s);
 void launch_sm_swell(const EventArgs &a, int colony, int n, int ts, cudaStream_t s);
+void launch_sm_philox(const EventArgs &a, int grid_cells, cudaStream_t s);
+void launch_sm_swell_all(const EventArgs &a, int grid_cells, cudaStream_t s);
 void launch_sm_ops(const EventArgs &a, int colony, int nops, const int *ops, const double *dirs, int dim,
                    cudaStream_t s);
 void launch_upload(const ColonyConst *col, int colony, int ncells, int dim, size_t SS, const double *stage,

@@ -88,12 +88,44 @@ def test_state_machine_matches_oracle(gpu_lib, oracle_lib, integrator, extra):
 
 
 def test_state_machine_forms_refused(gpu_lib):
-    """Only the oracle-mode draws (their outcomes are read back) and bins rebuilt every step."""
+    """Bins rebuilt every step (no Verlet skin); the bond's active noise with the reference's draws."""
     G = gpu_lib
     p = machine_params()
-    for kw in (dict(rng=G.RNG_PHILOX), dict(rng=G.RNG_DSFMT, precision=G.PREC_MIXED, skin=0.3)):
+    for rng in (G.RNG_DSFMT, G.RNG_PHILOX):
         with pytest.raises(G.CilError):
-            G.Engine([p], [1000], **kw)
-    q = S.fene_params(noise_radial=0.01)  # active noise: the same forms
+            G.Engine([p], [1000], rng=rng, precision=G.PREC_MIXED, skin=0.3)
+    q = S.fene_params(noise_radial=0.01)
     with pytest.raises(G.CilError):
         G.Engine([q], [1000], rng=G.RNG_PHILOX)
+
+
+@pytest.mark.parametrize("swelling", [0, 1])
+def test_state_machine_philox(gpu_lib, oracle_lib, swelling):
+    """The device's own draws (Philox; starts, failures and divisions decided on the device, no
+    read-back): graph replay equals launching step by step; the colony grows as the oracle's
+    (other random numbers, so the counts agree statistically), every transition happens, and the
+    states stay crawling or dividing."""
+    G = gpu_lib
+    p = machine_params(div_swelling=swelling, sigma_core=[1.0, 1.2] if swelling else [1.0, 1.0])
+    st = colony(p)
+    outs = []
+    for graphs in (True, False):
+        eng = G.Engine([p], [4000], precision=G.PREC_FP64, rng=G.RNG_PHILOX, seed=7, graphs=graphs)
+        eng.upload(0, **st)
+        eng.step(300)
+        outs.append(eng.download(0))
+        eng.close()
+    g, g2 = outs
+    assert g["ncells"] == g2["ncells"]
+    np.testing.assert_array_equal(g["pos"], g2["pos"])
+    np.testing.assert_array_equal(g["cell_state"], g2["cell_state"])
+    o = oracle_lib.Oracle(p, 4000, 7)
+    o.set_state(**st)
+    assert o.step(300) == 0
+    n_o = o.ncells
+    assert abs(g["ncells"] - n_o) <= 0.2 * n_o, (g["ncells"], n_o)
+    assert set(np.unique(g["cell_state"]).tolist()) <= {0, 1, 2}
+    assert (g["cell_state"] == 0).sum() > 20 and (g["cell_state"] == 1).sum() > 20
+    assert (g["tswitch"] > 300).all()
+    if swelling:
+        assert np.abs(g["sigma"] - 1.0).max() > 0.0 and g["sigma"].max() <= 1.2
