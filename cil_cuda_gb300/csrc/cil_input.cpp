@@ -883,11 +883,9 @@ void read_all(cil_input *in) {
       }
       p.fene_rmax_division = fene.has("RMAX_DIVISION") ? fene.nums("RMAX_DIVISION", 1)[0] : 0.0;
       p.div_swelling = dv.has("SWELLING") && dv.boolean("SWELLING") ? 1 : 0;
-      // the outcomes of the divisions are read back each step to draw the reference's stream
-      cfg.rng_mode = CIL_RNG_DSFMT;
+      // bins rebuilt every step; the reference's own draws unless GPU.RNG asks for the device's
       cfg.skin = 0.0;
-      if (has_gpu && gpu.has("RNG") && gpu.pick("RNG", {"PHILOX", "DSFMT"}) != "DSFMT")
-        key_error("GPU.RNG", "dividing two-element cells with the reference's bond run with the reference's draws (DSFMT)");
+      if (!(has_gpu && gpu.has("RNG"))) cfg.rng_mode = CIL_RNG_DSFMT;
     }
     p.intra_law = CIL_INTRA_FENE;
     p.cil = loc.boolean("CIL") ? 1 : 0;

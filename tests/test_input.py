@@ -232,8 +232,8 @@ def machine_doc():
 def test_dividing_cells_with_the_reference_bond_are_read(G):
     """Dividing cells without GPU.SPRING: the reference's crawling/dividing cells with the DIVISION
     block's R0, Rmin, Rmin_RATIO, TAU_MIGRATION, the species' GROWTHK0/1/2 and RMAX_DIVISION
-    (Input.cpp:36-38, 153-243), drawn with the reference's stream and without a Verlet skin; the
-    initial states follow initializeCellStatus (CIL.cuh:279-290)."""
+    (Input.cpp:36-38, 153-243), without a Verlet skin, drawn with the reference's stream unless
+    GPU.RNG asks otherwise; the initial states follow initializeCellStatus (CIL.cuh:279-290)."""
     r = load(G, machine_doc())
     p, c = r.params, r.config
     assert p["intra_law"] == G.INTRA_FENE and p["divide"] == 1
@@ -245,10 +245,8 @@ def test_dividing_cells_with_the_reference_bond_are_read(G):
     st = r.initial_state()
     assert set(np.unique(st["cell_state"]).tolist()) == {0, 1}
     d = machine_doc()
-    d["GPU"]["RNG"] = "PHILOX"
-    with pytest.raises(G.CilError) as e:
-        load(G, d)
-    assert "GPU.RNG" in str(e.value)
+    d["GPU"]["RNG"] = "PHILOX"  # the device's own draws, asked for
+    assert load(G, d).config["rng_mode"] == G.RNG_PHILOX
     assert p["div_swelling"] == 0
     d = machine_doc()
     d["SPECIES"]["A"]["DIVISION"]["SWELLING"] = True
